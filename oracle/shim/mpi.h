@@ -1,0 +1,16 @@
+/* Types-only stand-in for <mpi.h>, used solely to compile the reference codec
+ * sources into the oracle library.  The codec files include the MPI header
+ * through ZCCL.h but call no MPI function on the compress / decompress /
+ * homomorphic-add path. */
+#ifndef ORACLE_SHIM_MPI_H
+#define ORACLE_SHIM_MPI_H
+typedef int MPI_Datatype;
+typedef int MPI_Comm;
+typedef int MPI_Op;
+typedef long MPI_Aint;
+typedef int MPI_Request;
+typedef int MPI_Win;
+typedef struct { int MPI_SOURCE, MPI_TAG, MPI_ERROR; } MPI_Status;
+#define MPI_WIN_NULL 0
+#define MPI_COMM_NULL 0
+#endif

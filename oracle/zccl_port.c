@@ -1,0 +1,340 @@
+/*
+ * zccl_port.c -- CPU restatement of ZCCL's fastmode1 float32 codec.
+ *
+ * TEST INFRASTRUCTURE ONLY: the oracle.  tests/ use it as the checker,
+ * bench.py times it as the CPU baseline.  The GPU product never links it.
+ *
+ * Stream layout (the reference writes it at ZCCL/src/ZCCL_float.c:529-791):
+ *   header : T little-endian uint64 chunk offsets, relative to the end of the
+ *            header (header[0] == 0)                     (ZCCL_float.c:777-790)
+ *   chunk t: segment t; the last chunk also carries segment T when
+ *            N % T != 0                                  (ZCCL_float.c:672-772)
+ *   segment: raw int32 quantized head, then blocks of L deltas, the last one
+ *            shortened to (len-1) % L elements           (ZCCL_float.c:563-670)
+ *   block  : 1 width byte b; if b > 0: ceil(n/8) sign bytes (MSB first),
+ *            n * (b/8) high bytes (little-endian per element), then the low
+ *            b%8 bits of every element as an MSB-first bit stream
+ *                                                        (ZCCL_TypeManager.c:12-91,
+ *                                                         :118-421, :824-848)
+ * Quantization truncates toward zero: q = (int)((double)x * (double)(1.0f/eb))
+ * (ZCCL_float.c:540,580).  Widths use the host libm: (int)log2f(max) + 1
+ * (ZCCL_float.c:606).  Deltas chain across the blocks of a segment
+ * (ZCCL_float.c:581-582) and wrap as int32.
+ */
+#include "zccl_port.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ---- geometry -------------------------------------------------------- */
+
+/* Bytes of one encoded block of n elements at width b. */
+static size_t block_bytes(int b, size_t n)
+{
+    if (b == 0) return 1;
+    return 1 + (n + 7) / 8 + (size_t)(b / 8) * n + ((size_t)(b % 8) * n + 7) / 8;
+}
+
+/* Largest possible encoding of a segment of len elements (every block at
+ * width 32). */
+static size_t segment_worst_bytes(size_t len, size_t L)
+{
+    size_t nfull = (len - 1) / L, ntail = (len - 1) % L;
+    size_t s = 4 + nfull * block_bytes(32, L);
+    if (ntail) s += block_bytes(32, ntail);
+    return s;
+}
+
+int port_width(uint32_t m)
+{
+    if (m == 0) return 0;
+    return (int)log2f((float)m) + 1; /* ZCCL_float.c:606, host libm */
+}
+
+static inline int32_t quantize(float x, double inv)
+{
+    /* float * double is computed in double and exact; (int) truncates. */
+    return (int32_t)(x * inv);
+}
+
+static inline uint32_t magnitude(int32_t d)
+{
+    return d < 0 ? 0u - (uint32_t)d : (uint32_t)d;
+}
+
+/* ---- block coder ----------------------------------------------------- */
+
+/* Encode n deltas into o; returns bytes written. */
+static size_t encode_block(unsigned char *o, const int32_t *d, size_t n)
+{
+    uint32_t m = 0;
+    for (size_t j = 0; j < n; j++) {
+        uint32_t v = magnitude(d[j]);
+        if (v > m) m = v;
+    }
+    if (m == 0) {
+        o[0] = 0;
+        return 1;
+    }
+    int b = port_width(m);
+    int B = b / 8, r = b % 8;
+    unsigned char *p = o;
+    *p++ = (unsigned char)b;
+
+    size_t ns = (n + 7) / 8;
+    memset(p, 0, ns);
+    for (size_t j = 0; j < n; j++)
+        if (d[j] < 0) p[j / 8] |= (unsigned char)(0x80u >> (j % 8));
+    p += ns;
+
+    for (size_t j = 0; j < n; j++) {
+        uint32_t v = magnitude(d[j]) >> r;
+        for (int k = 0; k < B; k++) *p++ = (unsigned char)(v >> (8 * k));
+    }
+    if (r) {
+        uint32_t mask = (1u << r) - 1u;
+        uint32_t acc = 0;
+        int nacc = 0;
+        for (size_t j = 0; j < n; j++) {
+            acc = (acc << r) | (magnitude(d[j]) & mask);
+            nacc += r;
+            if (nacc >= 8) {
+                nacc -= 8;
+                *p++ = (unsigned char)(acc >> nacc);
+            }
+        }
+        if (nacc) *p++ = (unsigned char)(acc << (8 - nacc));
+    }
+    return (size_t)(p - o);
+}
+
+/* Decode one block of n deltas from s into d; returns bytes consumed. */
+static size_t decode_block(const unsigned char *s, size_t n, int32_t *d)
+{
+    int b = s[0];
+    if (b == 0) {
+        memset(d, 0, n * sizeof(int32_t));
+        return 1;
+    }
+    int B = b / 8, r = b % 8;
+    const unsigned char *sg = s + 1;
+    const unsigned char *hi = sg + (n + 7) / 8;
+    const unsigned char *lo = hi + (size_t)B * n;
+    uint32_t acc = 0;
+    int nacc = 0;
+    for (size_t j = 0; j < n; j++) {
+        uint32_t v = 0;
+        for (int k = 0; k < B; k++) v |= (uint32_t)hi[j * B + k] << (8 * k);
+        v <<= r;
+        if (r) {
+            while (nacc < r) {
+                acc = (acc << 8) | *lo++;
+                nacc += 8;
+            }
+            nacc -= r;
+            v |= (acc >> nacc) & ((1u << r) - 1u);
+        }
+        int neg = (sg[j / 8] >> (7 - j % 8)) & 1;
+        d[j] = (int32_t)(neg ? 0u - v : v);
+    }
+    return block_bytes(b, n);
+}
+
+/* ---- per-segment passes ---------------------------------------------- */
+
+static size_t encode_segment(unsigned char *o, const float *x, size_t len, double inv, size_t L,
+                             int32_t *d)
+{
+    unsigned char *p = o;
+    int32_t prior = quantize(x[0], inv);
+    memcpy(p, &prior, 4);
+    p += 4;
+    for (size_t i = 1; i < len; i += L) {
+        size_t n = len - i < L ? len - i : L;
+        for (size_t j = 0; j < n; j++) {
+            int32_t q = quantize(x[i + j], inv);
+            d[j] = (int32_t)((uint32_t)q - (uint32_t)prior);
+            prior = q;
+        }
+        p += encode_block(p, d, n);
+    }
+    return (size_t)(p - o);
+}
+
+static size_t decode_segment(float *y, const unsigned char *s, size_t len, float eb, size_t L,
+                             int32_t *d)
+{
+    const unsigned char *p = s;
+    int32_t prior;
+    memcpy(&prior, p, 4);
+    p += 4;
+    y[0] = (float)prior * eb;
+    for (size_t i = 1; i < len; i += L) {
+        size_t n = len - i < L ? len - i : L;
+        p += decode_block(p, n, d);
+        for (size_t j = 0; j < n; j++) {
+            prior = (int32_t)((uint32_t)prior + (uint32_t)d[j]);
+            y[i + j] = (float)prior * eb;
+        }
+    }
+    return (size_t)(p - s);
+}
+
+/* Homomorphic add of one segment pair (ZCCLd_float.c:1072-1221): heads add
+ * as int32; a block pair with one zero-width side copies the other block;
+ * otherwise both are decoded, added and re-encoded. */
+static void homadd_segment(unsigned char **po, const unsigned char **pa, const unsigned char **pb,
+                           size_t len, size_t L, int32_t *d1, int32_t *d2)
+{
+    unsigned char *o = *po;
+    const unsigned char *a = *pa, *b = *pb;
+    int32_t h1, h2, hs;
+    memcpy(&h1, a, 4);
+    memcpy(&h2, b, 4);
+    hs = (int32_t)((uint32_t)h1 + (uint32_t)h2);
+    memcpy(o, &hs, 4);
+    a += 4;
+    b += 4;
+    o += 4;
+    for (size_t i = 1; i < len; i += L) {
+        size_t n = len - i < L ? len - i : L;
+        int w1 = a[0], w2 = b[0];
+        if (w1 == 0 && w2 == 0) {
+            *o++ = 0;
+            a++;
+            b++;
+        } else if (w1 == 0) {
+            size_t s2 = block_bytes(w2, n);
+            memcpy(o, b, s2);
+            o += s2;
+            b += s2;
+            a++;
+        } else if (w2 == 0) {
+            size_t s1 = block_bytes(w1, n);
+            memcpy(o, a, s1);
+            o += s1;
+            a += s1;
+            b++;
+        } else {
+            a += decode_block(a, n, d1);
+            b += decode_block(b, n, d2);
+            for (size_t j = 0; j < n; j++) d1[j] = (int32_t)((uint32_t)d1[j] + (uint32_t)d2[j]);
+            o += encode_block(o, d1, n);
+        }
+    }
+    *po = o;
+    *pa = a;
+    *pb = b;
+}
+
+/* ---- stream-level entry points --------------------------------------- */
+
+void port_compress(unsigned char *out, const float *in, size_t *outSize, float absErrBound,
+                   size_t nbEle, int blockSize, int T)
+{
+    const size_t L = (size_t)blockSize;
+    const size_t tbs = nbEle / (size_t)T, rem = nbEle % (size_t)T;
+    const double inv = (double)(1.0f / absErrBound); /* float division, ZCCL_float.c:540 */
+    unsigned char **bufs = (unsigned char **)malloc((size_t)T * sizeof(*bufs));
+    size_t *sizes = (size_t *)malloc((size_t)T * sizeof(size_t));
+
+#pragma omp parallel for schedule(static)
+    for (int t = 0; t < T; t++) {
+        size_t lo = (size_t)t * tbs;
+        int has_rm = (t == T - 1 && rem != 0);
+        size_t cap = segment_worst_bytes(tbs, L) + (has_rm ? segment_worst_bytes(rem, L) : 0);
+        unsigned char *buf = (unsigned char *)malloc(cap);
+        int32_t *d = (int32_t *)malloc(L * sizeof(int32_t));
+        size_t s = encode_segment(buf, in + lo, tbs, inv, L, d);
+        if (has_rm) s += encode_segment(buf + s, in + lo + tbs, rem, inv, L, d);
+        bufs[t] = buf;
+        sizes[t] = s;
+        free(d);
+    }
+
+    uint64_t off = 0;
+    for (int t = 0; t < T; t++) {
+        memcpy(out + 8 * (size_t)t, &off, 8);
+        off += sizes[t];
+    }
+    *outSize = 8 * (size_t)T + off;
+
+#pragma omp parallel for schedule(static)
+    for (int t = 0; t < T; t++) {
+        uint64_t o;
+        memcpy(&o, out + 8 * (size_t)t, 8);
+        memcpy(out + 8 * (size_t)T + o, bufs[t], sizes[t]);
+        free(bufs[t]);
+    }
+    free(bufs);
+    free(sizes);
+}
+
+void port_decompress(float *out, size_t nbEle, float absErrBound, int blockSize,
+                     const unsigned char *cmp, int T)
+{
+    const size_t L = (size_t)blockSize;
+    const size_t tbs = nbEle / (size_t)T, rem = nbEle % (size_t)T;
+    const unsigned char *data = cmp + 8 * (size_t)T;
+
+#pragma omp parallel for schedule(static)
+    for (int t = 0; t < T; t++) {
+        uint64_t o;
+        memcpy(&o, cmp + 8 * (size_t)t, 8);
+        int32_t *d = (int32_t *)malloc(L * sizeof(int32_t));
+        size_t lo = (size_t)t * tbs;
+        size_t used = decode_segment(out + lo, data + o, tbs, absErrBound, L, d);
+        if (t == T - 1 && rem != 0)
+            decode_segment(out + lo + tbs, data + o + used, rem, absErrBound, L, d);
+        free(d);
+    }
+}
+
+void port_homadd(unsigned char *out, size_t *outSize, size_t nbEle, float absErrBound,
+                 int blockSize, const unsigned char *cmp1, const unsigned char *cmp2, int T)
+{
+    (void)absErrBound;
+    const size_t L = (size_t)blockSize;
+    const size_t tbs = nbEle / (size_t)T, rem = nbEle % (size_t)T;
+    unsigned char **bufs = (unsigned char **)malloc((size_t)T * sizeof(*bufs));
+    size_t *sizes = (size_t *)malloc((size_t)T * sizeof(size_t));
+
+#pragma omp parallel for schedule(static)
+    for (int t = 0; t < T; t++) {
+        uint64_t o1, o2;
+        memcpy(&o1, cmp1 + 8 * (size_t)t, 8);
+        memcpy(&o2, cmp2 + 8 * (size_t)t, 8);
+        const unsigned char *a = cmp1 + 8 * (size_t)T + o1;
+        const unsigned char *b = cmp2 + 8 * (size_t)T + o2;
+        int has_rm = (t == T - 1 && rem != 0);
+        size_t cap = segment_worst_bytes(tbs, L) + (has_rm ? segment_worst_bytes(rem, L) : 0);
+        unsigned char *buf = (unsigned char *)malloc(cap);
+        unsigned char *o = buf;
+        int32_t *d1 = (int32_t *)malloc(L * sizeof(int32_t));
+        int32_t *d2 = (int32_t *)malloc(L * sizeof(int32_t));
+        homadd_segment(&o, &a, &b, tbs, L, d1, d2);
+        if (has_rm) homadd_segment(&o, &a, &b, rem, L, d1, d2);
+        bufs[t] = buf;
+        sizes[t] = (size_t)(o - buf);
+        free(d1);
+        free(d2);
+    }
+    /* Every input byte has been read; out may now overwrite cmp2. */
+    uint64_t off = 0;
+    for (int t = 0; t < T; t++) {
+        memcpy(out + 8 * (size_t)t, &off, 8);
+        off += sizes[t];
+    }
+    *outSize += 8 * (size_t)T + off;
+
+#pragma omp parallel for schedule(static)
+    for (int t = 0; t < T; t++) {
+        uint64_t o;
+        memcpy(&o, out + 8 * (size_t)t, 8);
+        memcpy(out + 8 * (size_t)T + o, bufs[t], sizes[t]);
+        free(bufs[t]);
+    }
+    free(bufs);
+    free(sizes);
+}

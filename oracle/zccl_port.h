@@ -1,0 +1,43 @@
+/*
+ * zccl_port.h -- CPU restatement of ZCCL's fastmode1 float32 codec.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle: tests/ use it as the
+ * checker and bench.py times it as the CPU baseline.  The GPU product never
+ * links, loads or calls it.
+ *
+ * The thread count T is explicit here (the reference takes it implicitly from
+ * the OpenMP runtime); T fixes the stream layout, see zccl_port.c.
+ */
+#ifndef ZCCL_PORT_H
+#define ZCCL_PORT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Compress nbEle floats into out (8*T-byte chunk-offset header followed by T
+ * chunks); *outSize is assigned.  Follows ZCCL/src/ZCCL_float.c:501-807. */
+void port_compress(unsigned char *out, const float *in, size_t *outSize, float absErrBound,
+                   size_t nbEle, int blockSize, int T);
+
+/* Decompress a stream written with the same T.  ZCCL/src/ZCCLd_float.c:538-754. */
+void port_decompress(float *out, size_t nbEle, float absErrBound, int blockSize,
+                     const unsigned char *cmp, int T);
+
+/* Homomorphic add of two streams (same nbEle, eb, L, T).  *outSize is
+ * INCREMENTED, like the reference (ZCCL/src/ZCCLd_float.c:1027,1655).
+ * out may alias cmp2.  ZCCL/src/ZCCLd_float.c:988-1679. */
+void port_homadd(unsigned char *out, size_t *outSize, size_t nbEle, float absErrBound,
+                 int blockSize, const unsigned char *cmp1, const unsigned char *cmp2, int T);
+
+/* Width of a block whose largest delta magnitude is m, with the host libm:
+ * 0 when m == 0, else (int)log2f((float)m) + 1 (ZCCL/src/ZCCL_float.c:606). */
+int port_width(uint32_t m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,188 @@
+"""CPU checkers for the fastmode1 codec.  TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg may
+import this module.  It wraps two shared libraries:
+
+* ``port`` -- ``oracle/libzccl_port.so``, our C restatement of the reference
+  codec (``oracle/zccl_port.c``); builds on any host.
+* ``ref``  -- ``oracle/_ref/libzccl_ref.so``, the reference's own codec
+  compiled in place from its sources by ``oracle/Makefile``; only where the
+  reference checkout exists and the binary matches this host.
+
+Both take the OpenMP thread count T explicitly because T fixes the stream
+layout (``ZCCL/src/ZCCL_float.c:532-545``).  For ``ref`` it is set through
+``omp_set_num_threads`` right before each call, which is the only way the
+reference learns it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "libzccl_port.so")
+REF_SO = os.path.join(HERE, "_ref", "libzccl_ref.so")
+
+_u8p = ctypes.POINTER(ctypes.c_ubyte)
+_f32p = ctypes.POINTER(ctypes.c_float)
+_szp = ctypes.POINTER(ctypes.c_size_t)
+
+
+def build(ref: bool = True) -> None:
+    """Compile the port (and the reference library when its sources exist)."""
+    targets = ["port"] + (["ref"] if ref else [])
+    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+
+
+def _ptr(a, typ):
+    return a.ctypes.data_as(typ)
+
+
+def worst_stream_bytes(n: int, L: int, T: int) -> int:
+    """Capacity that always holds a stream (every block at width 32)."""
+    tbs, rem = n // T, n % T
+
+    def seg(length):
+        if length == 0:
+            return 0
+        nfull, ntail = (length - 1) // L, (length - 1) % L
+        s = 4 + nfull * (1 + (L + 7) // 8 + 4 * L)
+        if ntail:
+            s += 1 + (ntail + 7) // 8 + 4 * ntail
+        return s
+
+    return 8 * T + T * seg(tbs) + seg(rem) + 64
+
+
+class _Codec:
+    def __init__(self, path: str, kind: str):
+        self.kind = kind
+        self.lib = ctypes.CDLL(path)
+        if kind == "port":
+            self._c = self.lib.port_compress
+            self._c.argtypes = [_u8p, _f32p, _szp, ctypes.c_float, ctypes.c_size_t,
+                                ctypes.c_int, ctypes.c_int]
+            self._d = self.lib.port_decompress
+            self._d.argtypes = [_f32p, ctypes.c_size_t, ctypes.c_float, ctypes.c_int, _u8p,
+                                ctypes.c_int]
+            self._h = self.lib.port_homadd
+            self._h.argtypes = [_u8p, _szp, ctypes.c_size_t, ctypes.c_float, ctypes.c_int,
+                                _u8p, _u8p, ctypes.c_int]
+            self.width = self.lib.port_width
+            self.width.argtypes = [ctypes.c_uint32]
+            self.width.restype = ctypes.c_int
+        else:
+            self._c = self.lib.ZCCL_float_openmp_threadblock_arg
+            self._c.argtypes = [_u8p, _f32p, _szp, ctypes.c_float, ctypes.c_size_t, ctypes.c_int]
+            self._d = self.lib.ZCCL_float_decompress_openmp_threadblock_arg
+            self._d.argtypes = [_f32p, ctypes.c_size_t, ctypes.c_float, ctypes.c_int, _u8p]
+            self._h = self.lib.ZCCL_float_homomophic_add_openmp_threadblock
+            self._h.argtypes = [_u8p, _szp, ctypes.c_size_t, ctypes.c_float, ctypes.c_int,
+                                _u8p, _u8p]
+            self._set_threads = self.lib.omp_set_num_threads
+            self._set_threads.argtypes = [ctypes.c_int]
+        for f in (self._c, self._d, self._h):
+            f.restype = None
+
+    def _args_T(self, T):
+        if self.kind == "port":
+            return (ctypes.c_int(T),)
+        self._set_threads(T)
+        return ()
+
+    def compress(self, x: np.ndarray, eb: float, L: int, T: int) -> bytes:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        n = x.size
+        out = np.zeros(worst_stream_bytes(n, L, T), dtype=np.uint8)
+        size = ctypes.c_size_t(0)
+        self._c(_ptr(out, _u8p), _ptr(x, _f32p), ctypes.byref(size), ctypes.c_float(eb),
+                ctypes.c_size_t(n), ctypes.c_int(L), *self._args_T(T))
+        return out[: size.value].tobytes()
+
+    def decompress(self, stream: bytes, n: int, eb: float, L: int, T: int) -> np.ndarray:
+        buf = np.frombuffer(stream, dtype=np.uint8).copy()
+        # the reference's 3/5/6/7-bit unpackers may read one byte past a field
+        buf = np.concatenate([buf, np.zeros(16, np.uint8)])
+        y = np.zeros(n, dtype=np.float32)
+        self._d(_ptr(y, _f32p), ctypes.c_size_t(n), ctypes.c_float(eb), ctypes.c_int(L),
+                _ptr(buf, _u8p), *self._args_T(T))
+        return y
+
+    def homadd(self, s1: bytes, s2: bytes, n: int, eb: float, L: int, T: int) -> bytes:
+        a = np.concatenate([np.frombuffer(s1, np.uint8), np.zeros(16, np.uint8)])
+        b = np.concatenate([np.frombuffer(s2, np.uint8), np.zeros(16, np.uint8)])
+        out = np.zeros(worst_stream_bytes(n, L, T), dtype=np.uint8)
+        size = ctypes.c_size_t(0)
+        self._h(_ptr(out, _u8p), ctypes.byref(size), ctypes.c_size_t(n), ctypes.c_float(eb),
+                ctypes.c_int(L), _ptr(a, _u8p), _ptr(b, _u8p), *self._args_T(T))
+        return out[: size.value].tobytes()
+
+    def homadd_fold(self, streams, n: int, eb: float, L: int, T: int) -> bytes:
+        """P-way sum folded pairwise the way the ring's reduce-scatter does it
+        (acc = add(received, acc), ZCCL/src/ZCCL_ring_ho.c:281-287)."""
+        acc = streams[0]
+        for s in streams[1:]:
+            acc = self.homadd(s, acc, n, eb, L, T)
+        return acc
+
+
+_cache: dict = {}
+
+
+def port() -> _Codec:
+    if "port" not in _cache:
+        if not os.path.exists(PORT_SO):
+            build(ref=False)
+        _cache["port"] = _Codec(PORT_SO, "port")
+    return _cache["port"]
+
+
+def ref_available() -> bool:
+    if not os.path.exists(REF_SO):
+        return False
+    try:
+        ref()
+        return True
+    except OSError:
+        return False
+
+
+def ref() -> _Codec:
+    if "ref" not in _cache:
+        _cache["ref"] = _Codec(REF_SO, "ref")
+    return _cache["ref"]
+
+
+def chunk_sizes(stream: bytes, T: int) -> list:
+    """Byte length of each of the T chunks of a stream, from its header."""
+    hdr = np.frombuffer(stream[: 8 * T], dtype="<u8").astype(np.int64)
+    ends = list(hdr[1:]) + [len(stream) - 8 * T]
+    return [int(e - b) for b, e in zip(hdr, ends)]
+
+
+def ref_scratch_ok(stream: bytes, n: int, T: int) -> bool:
+    """True when every chunk of ``stream`` fits the reference's per-thread
+    scratch of ceil(4n/T) bytes (ZCCL/src/ZCCL_float.c:539,548-549 and
+    ZCCL/src/ZCCLd_float.c:1031,1040-1041).  Larger chunks overflow that heap
+    buffer inside the reference, so the reference only runs on cases where
+    this holds."""
+    cap = (4 * n + T - 1) // T
+    return max(chunk_sizes(stream, T)) <= cap
+
+
+def width_thresholds(width_fn=None) -> list:
+    """thr[w] = smallest m with bit length w whose width is w+1 (0 if none),
+    found by scanning down from 2**w - 1 (the width is monotone in m)."""
+    f = width_fn or port().width
+    thr = [0] * 33
+    for w in range(1, 33):
+        lo, m = 1 << (w - 1), (1 << w) - 1
+        first = 0
+        while m >= lo and f(m) == w + 1:
+            first = m
+            m -= 1
+        thr[w] = first
+    return thr
