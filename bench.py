@@ -1,0 +1,383 @@
+#!/usr/bin/env python
+"""Throughput of the fastmode1 hot path on one GB300 (or N, as replicas).
+
+Workload: a 512^3 float32 field (512 MiB), a log-normal Gaussian random
+field with P(k) ~ k^-3 (exp(1.5 g)), error bound eb = 1e-4 * range, block
+size 32, writer thread count T = the host's core count.  One step is one
+pass of the hot path over it:
+
+    compress(field A) -> decompress(that stream) -> homomorphic add of that
+    stream and the (resident) stream of a second field B.
+
+value  = uncompressed bytes handled per second, 3 * 4N per step (GB/s), the
+         reference's own convention (one input's bytes per operation),
+         device-resident inputs, CUDA events on the launching stream.
+e2e    = the same step through the reference-facing C-ABI entry points with
+         host buffers (host->device and device->host copies inside).
+roofline: algorithmic bytes of the dominant kernel per launch over its mean
+         event-timed duration, against the measured HBM copy bandwidth.
+cpu_baseline: the oracle's C restatement of the reference codec with every
+         host core, on the same field.
+
+Launched as ``python bench.py --gpus N --steps K --warmup W``; for N > 1
+under torchrun every rank compresses its own field (weak scaling, no
+collective on the data path).  ``--impl reference`` times the CPU codec
+instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "compress/decompress/homo-add GB/s vs HBM peak; batched speedup; p50/p99 at eb=1e-4"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--side", type=int, default=512)
+    p.add_argument("--eb-rel", type=float, default=1e-4)
+    p.add_argument("--L", type=int, default=32)
+    p.add_argument("--T", type=int, default=0, help="writer thread count (default: host cores)")
+    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_field(side: int, seed: int, device):
+    """Log-normal Gaussian random field: white noise shaped to P(k) ~ k^-3 in
+    Fourier space, normalised to unit variance, then exp(1.5 g)."""
+    import torch
+    g = torch.Generator(device=device).manual_seed(seed)
+    kx = torch.fft.fftfreq(side, device=device)
+    kz = torch.fft.rfftfreq(side, device=device)
+    k2 = kx[:, None, None] ** 2 + kx[None, :, None] ** 2 + kz[None, None, :] ** 2
+    amp = torch.where(k2 > 0, k2.clamp_min(1e-12) ** (-0.75), torch.zeros_like(k2))  # |k|^-1.5
+    del k2
+    shape = (side, side, side // 2 + 1)
+    spec = torch.complex(torch.randn(shape, generator=g, device=device),
+                         torch.randn(shape, generator=g, device=device)) * amp
+    del amp
+    f = torch.fft.irfftn(spec, s=(side, side, side))
+    del spec
+    f = (f - f.mean()) / f.std()
+    return torch.exp(1.5 * f).reshape(-1).contiguous().float()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str):
+        self.gpu_id = gpu_id
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", self.gpu_id], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def seg_worst(length: int, L: int) -> int:
+    """Largest encoding of a segment (every block at width 32)."""
+    if length == 0:
+        return 0
+    nfull, ntail = (length - 1) // L, (length - 1) % L
+    s = 4 + nfull * (1 + (L + 7) // 8 + 4 * L)
+    return s + (1 + (ntail + 7) // 8 + 4 * ntail if ntail else 0)
+
+
+def host_read_bytes(stream_bytes: bytes, n: int, L: int, T: int) -> int:
+    """Bytes the drop-in copies to the device for a host stream: the chunk
+    offsets give all but the last chunk, which is read up to its largest
+    possible size but not past 4*n bytes (include/zccl_gpu.h)."""
+    last = int.from_bytes(stream_bytes[8 * (T - 1): 8 * T], "little")
+    known = 8 * T + last
+    want = known + seg_worst(n // T, L) + seg_worst(n % T, L)
+    return min(want, max(4 * n, known + 4))
+
+
+def cpu_codec_rate(x, y, eb, L, T, reps=1):
+    """GB/s of uncompressed input for compress + decompress + homomorphic add
+    with the oracle port on all host cores; returns (GB/s, seconds/pass)."""
+    from oracle import zoracle
+    port = zoracle.port()
+    n = x.size
+    sb = port.compress(y, eb, L, T)
+    best = None
+    for _ in range(reps + 1):
+        t0 = time.perf_counter()
+        sa = port.compress(x, eb, L, T)
+        port.decompress(sa, n, eb, L, T)
+        port.homadd(sa, sb, n, eb, L, T)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return 3 * 4 * n / best / 1e9, best
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference codec's CPU path on the host cores."""
+    import numpy as np
+    import torch
+    if rank != 0:
+        return
+    T = args.T or host_cores()
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    x = make_field(args.side, 0, dev).cpu().numpy()
+    y = make_field(args.side, 1, dev).cpu().numpy()
+    eb = float(np.float32(args.eb_rel * max(float(x.max() - x.min()), float(y.max() - y.min()))))
+    from oracle import zoracle
+    port = zoracle.port()
+    n = x.size
+    sb = port.compress(y, eb, args.L, T)
+    times = []
+    for s in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        sa = port.compress(x, eb, args.L, T)
+        port.decompress(sa, n, eb, args.L, T)
+        port.homadd(sa, sb, n, eb, args.L, T)
+        if s >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = 3 * 4 * n * args.steps / tot / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * tot / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": workload_config(args, n, T),
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": T, "kind": "port",
+                         "sample": "whole 512^3 field per step; oracle C restatement, OpenMP"},
+        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, n, T):
+    return {"workload": f"{args.side}^3 float32 log-normal GRF ({4 * n >> 20} MiB): compress + "
+                        f"decompress + 2-way homomorphic add, eb={args.eb_rel:g}*range",
+            "elements": n, "eb_rel": args.eb_rel, "block_size": args.L, "writer_threads_T": T,
+            "l2": "inputs 512 MiB > 129 MB L2, no flush needed"}
+
+
+def run_ours(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+
+    import zccl_gb300 as Z
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    T = args.T or host_cores()
+    L = args.L
+    x = make_field(args.side, 2 * rank, dev)
+    y = make_field(args.side, 2 * rank + 1, dev)
+    n = x.numel()
+    eb = float(np.float32(args.eb_rel * max(float(x.max() - x.min()), float(y.max() - y.min()))))
+    codec = Z.Codec(n, L, T, device=str(dev))
+    st = codec.torch_stream
+    sa, sb, ss = codec.new_stream(), codec.new_stream(), codec.new_stream()
+    xo = torch.empty(n, dtype=torch.float32, device=dev)
+    codec.compress(y, eb, out=sb)
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(st)
+        codec.compress(x, eb, out=sa)
+        if ev:
+            ev[1].record(st)
+        codec.decompress(sa, eb, out=xo)
+        if ev:
+            ev[2].record(st)
+        codec.homadd([sa, sb], out=ss)
+        if ev:
+            ev[3].record(st)
+
+    for _ in range(args.warmup):
+        step()
+    codec.check()
+    ca, cb, cs = sa.size(), sb.size(), ss.size()
+    # correctness guard on the timed workload: decompression error within eb
+    err = (xo.double() - x.double()).abs().max().item()
+    assert err <= eb * (1 + 1e-3) + 4 * np.spacing(np.float32(x.abs().max().item())), err
+
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    gpu_id = os.environ.get("CUDA_VISIBLE_DEVICES", str(local_rank)).split(",")[0] or "0"
+    with ClockSampler(gpu_id) as clk:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(st)
+        for k in range(args.steps):
+            step(evs[k])
+        t_end.record(st)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    codec.check()
+    ms = t_start.elapsed_time(t_end) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = t.item()
+    op_ms = [statistics.mean(e[i].elapsed_time(e[i + 1]) for e in evs) for i in range(3)]
+    value = world * 3 * 4 * n / (ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    alg = {"compress": 4 * n + ca, "decompress": ca + 4 * n, "homadd": ca + cb + cs}
+    per_op = {}
+    for name, t_ms in zip(("compress", "decompress", "homadd"), op_ms):
+        gbs = alg[name] / (t_ms * 1e-3) / 1e9
+        per_op[name] = {"ms": round(t_ms, 4), "uncompressed_GBps": round(4 * n / (t_ms * 1e-3) / 1e9, 1),
+                        "algorithmic_GBps": round(gbs, 1), "roofline_frac": round(gbs / peak, 4),
+                        "algorithmic_bytes": alg[name]}
+    dom = max(per_op, key=lambda k: per_op[k]["ms"])
+    roofline = {"bound": "hbm", "achieved": per_op[dom]["algorithmic_GBps"], "peak": peak,
+                "unit": "GB/s", "frac": per_op[dom]["roofline_frac"], "traffic": None,
+                "kernel": dom, "peak_source": f"{peak_kind} hbm_gbs"}
+
+    # e2e through the reference-facing entry points with host buffers
+    xh, yh = x.cpu().numpy(), y.cpu().numpy()
+    Z.set_omp_threads(T)
+    cap = max(4 * n, codec.max_stream_bytes)
+    hs_a = np.zeros(cap, np.uint8)
+    hs_b = np.zeros(cap, np.uint8)
+    hs_s = np.zeros(cap, np.uint8)
+    hy = np.zeros(n, np.float32)
+    Z.ZCCL_float_openmp_threadblock_arg(hs_b, yh, 0, eb, n, L)
+
+    def e2e_step():
+        size = Z.ZCCL_float_openmp_threadblock_arg(hs_a, xh, 0, eb, n, L)
+        Z.ZCCL_float_decompress_openmp_threadblock_arg(hy, n, eb, L, hs_a)
+        Z.ZCCL_float_homomophic_add_openmp_threadblock(hs_s, 0, n, eb, L, hs_a, hs_b)
+        return size
+
+    e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    sa_host = hs_a[:ca].tobytes()
+    rd_a = host_read_bytes(sa_host, n, L, T)
+    rd_b = host_read_bytes(hs_b[:cb].tobytes(), n, L, T)
+    e2e = {"value": round(world * 3 * 4 * n / e2e_s / 1e9, 3), "unit": "GB/s",
+           "h2d_bytes_per_step": 4 * n + 2 * rd_a + rd_b,
+           "d2h_bytes_per_step": ca + 4 * n + cs,
+           "api": "ZCCL_float_openmp_threadblock_arg / _decompress_ / _homomophic_add_ (host)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, secs = cpu_codec_rate(xh, yh, eb, L, T)
+        cpu = {"value": round(rate, 3), "unit": "GB/s", "cores": T, "kind": "port",
+               "sample": f"whole field, one pass ({secs:.2f} s) of compress+decompress+homadd, "
+                         f"oracle C restatement, OpenMP {T} threads"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic: seeded log-normal GRF, P(k)~k^-3, exp(1.5 g) (stands in for NYX 512^3)",
+            "config": workload_config(args, n, T),
+            "roofline": roofline, "per_op": per_op,
+            "compression_ratio": {"A": round(4 * n / ca, 3), "B": round(4 * n / cb, 3),
+                                  "sum": round(4 * n / cs, 3)},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        backend = "nccl" if torch.cuda.is_available() and args.impl == "ours" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local_rank)
+        torch.distributed.init_process_group(backend)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

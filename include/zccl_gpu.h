@@ -1,0 +1,158 @@
+/*
+ * zccl_gpu.h -- C ABI of the GB300 implementation of ZCCL's fastmode1
+ * compression hot path (compress, decompress, homomorphic add).
+ *
+ * Two layers:
+ *
+ * 1. Drop-in replacements.  Same names, signatures, argument meaning and
+ *    byte layout as the reference's OpenMP codec, so a caller relinks
+ *    against libzccl_gpu.so instead of libZCCL.  Pointers may be host memory
+ *    (copied through the GPU) or device memory (used in place).  Calls are
+ *    synchronous and return void like the reference; the outcome of the last
+ *    call on the calling thread is available from zccl_gpu_last_status().
+ *    The writer thread count T that fixes the stream layout is taken the way
+ *    the reference takes it: omp_get_max_threads() for the *_openmp_*
+ *    functions, 1 for the *_single_thread* ones.
+ *
+ * 2. The device API (zccl_gpu_*).  Explicit T, device pointers, a CUDA
+ *    stream, status codes, and a side index kept next to every resident
+ *    stream so decompression and homomorphic add never have to walk the
+ *    1-byte block headers.  Calls are asynchronous on the given stream.
+ */
+#ifndef ZCCL_GPU_H
+#define ZCCL_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ===================================================================
+ * 1. Drop-in replacements of the reference entry points
+ * =================================================================== */
+
+/* Replaces ZCCL_float_openmp_threadblock_arg, declared at
+ * ZCCL/include/ZCCL_float.h:31 and defined at ZCCL/src/ZCCL_float.c:501.
+ * Compresses nbEle floats into outputBytes and ASSIGNS *outSize.  As with
+ * the reference, outputBytes must hold the whole stream; every reference
+ * caller allocates 4*nbEle bytes. */
+void ZCCL_float_openmp_threadblock_arg(unsigned char *outputBytes, float *oriData, size_t *outSize,
+                                       float absErrBound, size_t nbEle, int blockSize);
+
+/* Replaces ZCCL_float_single_thread_arg (ZCCL/include/ZCCL_float.h:34,
+ * ZCCL/src/ZCCL_float.c:809): the same stream with T = 1. */
+void ZCCL_float_single_thread_arg(unsigned char *outputBytes, float *oriData, size_t *outSize,
+                                  float absErrBound, size_t nbEle, int blockSize);
+
+/* Replaces ZCCL_float_decompress_openmp_threadblock_arg
+ * (ZCCL/include/ZCCLd_float.h:21, ZCCL/src/ZCCLd_float.c:538).  The stream
+ * carries no length; with a host pointer, cmpBytes must be readable for
+ * min(4*nbEle, largest possible stream) bytes, the capacity every reference
+ * caller gives its stream buffers; with a device pointer, up to the end of
+ * its allocation. */
+void ZCCL_float_decompress_openmp_threadblock_arg(float *newData, size_t nbEle, float absErrBound,
+                                                  int blockSize, unsigned char *cmpBytes);
+
+/* Replaces ZCCL_float_decompress_single_thread_arg
+ * (ZCCL/include/ZCCLd_float.h:23, ZCCL/src/ZCCLd_float.c:247), T = 1. */
+void ZCCL_float_decompress_single_thread_arg(float *newData, size_t nbEle, float absErrBound,
+                                             int blockSize, unsigned char *cmpBytes);
+
+/* Replaces ZCCL_float_homomophic_add_openmp_threadblock (the reference's
+ * spelling), ZCCL/include/ZCCLd_float.h:29, ZCCL/src/ZCCLd_float.c:988.
+ * final_cmpBytes may alias cmpBytes2 (the ring allreduce adds in place,
+ * ZCCL/src/ZCCL_ring_ho.c:281-287).  *final_cmpSize is INCREMENTED by the
+ * result size, like the reference (ZCCLd_float.c:1027,1655); callers zero
+ * it first. */
+void ZCCL_float_homomophic_add_openmp_threadblock(unsigned char *final_cmpBytes,
+                                                  size_t *final_cmpSize, size_t nbEle,
+                                                  float absErrBound, int blockSize,
+                                                  unsigned char *cmpBytes,
+                                                  unsigned char *cmpBytes2);
+
+/* Replaces ZCCL_float_homomophic_add_single_thread
+ * (ZCCL/include/ZCCLd_float.h:33, ZCCL/src/ZCCLd_float.c:1681), T = 1. */
+void ZCCL_float_homomophic_add_single_thread(unsigned char *final_cmpBytes, size_t *final_cmpSize,
+                                             size_t nbEle, float absErrBound, int blockSize,
+                                             unsigned char *cmpBytes, unsigned char *cmpBytes2);
+
+/* ===================================================================
+ * 2. Device API
+ * =================================================================== */
+
+#define ZCCL_GPU_OK 0
+#define ZCCL_GPU_EINVAL (-1)    /* bad arguments: n < T, L outside 1..256, null pointers */
+#define ZCCL_GPU_ECUDA (-2)     /* a CUDA runtime call failed */
+#define ZCCL_GPU_ERANGE (-3)    /* input not finite, or |x / eb| >= 2^31 */
+#define ZCCL_GPU_ECORRUPT (-4)  /* stream bytes disagree with its geometry or index */
+#define ZCCL_GPU_EBOUNDS (-5)   /* stream runs past its readable bytes */
+#define ZCCL_GPU_ETIMEOUT (-6)  /* a bounded device wait gave up */
+#define ZCCL_GPU_ENOMEM (-7)    /* device or host allocation failed */
+#define ZCCL_GPU_ECAPACITY (-8) /* destination buffer too small */
+
+/* A compressed stream resident in device memory. */
+typedef struct zccl_gpu_stream {
+    unsigned char *bytes; /* device: wire bytes in the reference layout */
+    size_t capacity;      /* bytes readable (and writable) at `bytes` */
+    void *index;          /* device: side index, zccl_gpu_index_bytes() bytes */
+    int indexed;          /* index holds block widths and tile offsets */
+    int qprev_valid;      /* index holds the quantized value before each tile */
+} zccl_gpu_stream;
+
+/* Largest stream of n floats (every block at width 32). */
+size_t zccl_gpu_max_stream_bytes(size_t n, int L, int T);
+/* Bytes of the side index of one stream (about n/L + 12 per 4096 floats). */
+size_t zccl_gpu_index_bytes(size_t n, int L, int T);
+/* Bytes of device scratch one call needs (look-back state, error word). */
+size_t zccl_gpu_workspace_bytes(size_t n, int L, int T);
+
+/* Compress n device floats into out->bytes and fill out's index.
+ * Enqueued on cuda_stream; the size is read with zccl_gpu_stream_size(). */
+int zccl_gpu_compress(zccl_gpu_stream *out, const float *d_in, size_t n, float eb, int L, int T,
+                      void *d_ws, void *cuda_stream);
+
+/* Decompress into n device floats.  Builds the index first when
+ * in->indexed is 0; recovers and stores the tile starting values when
+ * in->qprev_valid is 0. */
+int zccl_gpu_decompress(float *d_out, zccl_gpu_stream *in, size_t n, float eb, int L, int T,
+                        void *d_ws, void *cuda_stream);
+
+/* Homomorphic sum of P streams (same n, L, T, eb) into out, in one pass.
+ * out->bytes must not alias any input.  Inputs without an index get one. */
+int zccl_gpu_homadd(zccl_gpu_stream *out, zccl_gpu_stream *ins, int P, size_t n, int L, int T,
+                    void *d_ws, void *cuda_stream);
+
+/* Same, also accumulating the reference's four branch counters of a
+ * two-input add (both zero, first zero, second zero, both non-zero,
+ * ZCCL/src/ZCCLd_float.c:2175-2764) into d_cases[4] (device uint64). */
+int zccl_gpu_homadd_cases(zccl_gpu_stream *out, zccl_gpu_stream *ins, int P, size_t n, int L,
+                          int T, void *d_ws, unsigned long long *d_cases, void *cuda_stream);
+
+/* Build the side index of a stream that arrived as bytes only. */
+int zccl_gpu_build_index(zccl_gpu_stream *s, size_t n, int L, int T, void *d_ws, void *cuda_stream);
+
+/* Synchronize cuda_stream and return the total stream bytes of s. */
+int zccl_gpu_stream_size(const zccl_gpu_stream *s, size_t n, int L, int T, size_t *size,
+                         void *cuda_stream);
+
+/* Synchronize cuda_stream and turn the workspace's device error bits into a
+ * status code (ZCCL_GPU_OK when none). */
+int zccl_gpu_check(void *d_ws, void *cuda_stream);
+
+/* Status of the last drop-in call made by this thread. */
+int zccl_gpu_last_status(void);
+
+/* Text for a status code. */
+const char *zccl_gpu_strerror(int status);
+
+/* The width threshold table in use: thr[w] (w = 0..32) is the smallest
+ * integer of bit length w whose (int)log2f((float)m) + 1 is w + 1 with this
+ * host's libm, or 0xFFFFFFFF.  Fills 33 entries. */
+void zccl_gpu_width_table(uint32_t thr[33]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

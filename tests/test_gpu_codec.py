@@ -1,0 +1,240 @@
+"""GPU parity: every result of the CUDA path, called through the C ABI, must be
+bit-identical to the reference codec's (golden vectors written by the
+reference itself) or to the oracle port on larger inputs.  Floats are
+compared bit for bit; the error bounds are checked as properties."""
+from __future__ import annotations
+
+import hashlib
+
+import numpy as np
+import pytest
+
+import zccl_gb300 as Z
+
+pytestmark = pytest.mark.gpu
+
+
+def sha(a) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.fixture(scope="module")
+def torch():
+    t = pytest.importorskip("torch")
+    if not t.cuda.is_available():
+        pytest.skip("no CUDA device")
+    Z.lib()
+    return t
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def test_compress_matches_reference(golden, torch):
+    for c in golden.cases:
+        codec = Z.Codec(c["n"], c["L"], c["T"])
+        s = codec.compress(dev(torch, golden.x(c)), c["eb"])
+        codec.check()
+        assert s.tobytes() == golden.stream(c, "s"), c
+
+
+def test_decompress_matches_reference(golden, torch):
+    for c in golden.cases:
+        codec = Z.Codec(c["n"], c["L"], c["T"])
+        own = codec.compress(dev(torch, golden.x(c)), c["eb"])
+        y = codec.decompress(own, c["eb"])
+        codec.check()
+        assert sha(y.cpu().numpy()) == c["dec_s"], c
+        foreign = Z.DeviceStream.from_bytes(codec, golden.stream(c, "s"))
+        y2 = codec.decompress(foreign, c["eb"])  # walks the headers, then value look-back
+        codec.check()
+        assert sha(y2.cpu().numpy()) == c["dec_s"], c
+        y3 = codec.decompress(foreign, c["eb"])  # second pass uses the recovered index
+        codec.check()
+        assert sha(y3.cpu().numpy()) == c["dec_s"], c
+
+
+def test_homadd_matches_reference(golden, torch):
+    for c in golden.cases:
+        codec = Z.Codec(c["n"], c["L"], c["T"])
+        a = codec.compress(dev(torch, golden.x(c)), c["eb"])
+        b = codec.compress(dev(torch, golden.y(c)), c["eb"])
+        h = codec.homadd([a, b])
+        codec.check()
+        assert h.tobytes() == golden.stream(c, "h"), c
+        assert sha(codec.decompress(h, c["eb"]).cpu().numpy()) == c["dec_h"], c
+        fa = Z.DeviceStream.from_bytes(codec, golden.stream(c, "s"))
+        fb = Z.DeviceStream.from_bytes(codec, golden.stream(c, "t"))
+        hf = codec.homadd([fa, fb])
+        codec.check()
+        assert hf.tobytes() == golden.stream(c, "h"), c
+        assert sha(codec.decompress(hf, c["eb"]).cpu().numpy()) == c["dec_h"], c
+
+
+def test_pway_reduction_equals_reference_fold(golden, torch):
+    r = golden.meta["reduction"]
+    codec = Z.Codec(r["n"], r["L"], r["T"])
+    streams = [codec.compress(dev(torch, golden.arr[f"p8x{k}"]), r["eb"]) for k in range(r["P"])]
+    s = codec.homadd(streams)
+    codec.check()
+    assert s.tobytes() == golden.arr["p8sum"].tobytes()
+    assert sha(codec.decompress(s, r["eb"]).cpu().numpy()) == r["dec_sum"]
+    foreign = [Z.DeviceStream.from_bytes(codec, st.tobytes()) for st in streams]
+    assert codec.homadd(foreign[::-1]).tobytes() == golden.arr["p8sum"].tobytes()
+
+
+def n_blocks(n, L, T):
+    def seg(m):
+        return -(-(m - 1) // L) if m else 0
+    return T * seg(n // T) + seg(n % T)
+
+
+def test_branch_case_counters(golden, torch):
+    """The reference's four two-input branch counters (ZCCLd_float.c:2175-2764):
+    a constant input against a noisy one only takes 'first zero' (or 'both
+    zero' where the noisy block happens to be flat)."""
+    c = next(c for c in golden.cases if c["kind"] == "const_vs_noise")
+    codec = Z.Codec(c["n"], c["L"], c["T"])
+    a = codec.compress(dev(torch, golden.x(c)), c["eb"])
+    b = codec.compress(dev(torch, golden.y(c)), c["eb"])
+    cases = torch.zeros(4, dtype=torch.int64, device="cuda")
+    codec.homadd([a, b], cases=cases)
+    codec.check()
+    both0, first0, second0, both = cases.cpu().tolist()
+    assert second0 == 0 and both == 0
+    assert both0 + first0 == n_blocks(c["n"], c["L"], c["T"])
+    assert first0 > 0
+
+
+@pytest.mark.parametrize("T", [1, 3])
+def test_dropin_host_pointers(golden, torch, T):
+    Z.set_omp_threads(T)
+    picked = [c for c in golden.cases if c["T"] == T][::9]
+    for c in picked:
+        n, L, eb = c["n"], c["L"], c["eb"]
+        x, y = golden.x(c), golden.y(c)
+        cap = 4 * n + 8 * T + 4096
+        s = np.zeros(cap, np.uint8)
+        size = Z.ZCCL_float_openmp_threadblock_arg(s, x, 0, eb, n, L)
+        assert s[:size].tobytes() == golden.stream(c, "s"), c
+        t = np.zeros(cap, np.uint8)
+        tsize = Z.ZCCL_float_openmp_threadblock_arg(t, y, 0, eb, n, L)
+        out = np.zeros(n, np.float32)
+        Z.ZCCL_float_decompress_openmp_threadblock_arg(out, n, eb, L, s)
+        assert sha(out) == c["dec_s"], c
+        # in place, as the ring does: result written over the second input
+        acc = Z.ZCCL_float_homomophic_add_openmp_threadblock(t, 5, n, eb, L, s, t)
+        assert acc - 5 == len(golden.stream(c, "h"))  # *final_cmpSize is incremented
+        assert t[: acc - 5].tobytes() == golden.stream(c, "h"), c
+        assert tsize > 0
+
+
+def test_dropin_single_thread_variants(golden, torch):
+    for c in [c for c in golden.cases if c["T"] == 1][::11]:
+        n, L, eb = c["n"], c["L"], c["eb"]
+        s = np.zeros(4 * n + 4096, np.uint8)
+        size = Z.ZCCL_float_single_thread_arg(s, golden.x(c), 0, eb, n, L)
+        assert s[:size].tobytes() == golden.stream(c, "s")
+        out = np.zeros(n, np.float32)
+        Z.ZCCL_float_decompress_single_thread_arg(out, n, eb, L, s)
+        assert sha(out) == c["dec_s"]
+        t = np.frombuffer(golden.stream(c, "t"), np.uint8).copy()
+        h = np.zeros(4 * n + 4096, np.uint8)
+        hs = Z.ZCCL_float_homomophic_add_single_thread(h, 0, n, eb, L, s, t)
+        assert h[:hs].tobytes() == golden.stream(c, "h")
+
+
+def test_dropin_device_pointers(golden, torch):
+    Z.set_omp_threads(8)
+    for c in [c for c in golden.cases if c["T"] == 8][::13]:
+        n, L, eb = c["n"], c["L"], c["eb"]
+        x = dev(torch, golden.x(c))
+        s = torch.zeros(4 * n + 8192, dtype=torch.uint8, device="cuda")
+        size = Z.ZCCL_float_openmp_threadblock_arg(s, x, 0, eb, n, L)
+        assert s[:size].cpu().numpy().tobytes() == golden.stream(c, "s")
+        out = torch.zeros(n, dtype=torch.float32, device="cuda")
+        Z.ZCCL_float_decompress_openmp_threadblock_arg(out, n, eb, L, s)
+        assert sha(out.cpu().numpy()) == c["dec_s"]
+        t = dev(torch, np.frombuffer(golden.stream(c, "t"), np.uint8).copy())
+        t2 = torch.zeros(4 * n + 8192, dtype=torch.uint8, device="cuda")
+        t2[: t.numel()] = t
+        hs = Z.ZCCL_float_homomophic_add_openmp_threadblock(t2, 0, n, eb, L, s, t2)
+        assert t2[:hs].cpu().numpy().tobytes() == golden.stream(c, "h")
+
+
+def test_generic_block_sizes_against_port(port, torch):
+    rng = np.random.default_rng(3)
+    for L in (33, 64, 100, 256):
+        for T in (1, 5):
+            n = 20000 + L
+            x = np.cumsum(rng.normal(0, 0.1, n)).astype(np.float32)
+            y = np.cumsum(rng.normal(0, 0.1, n)).astype(np.float32)
+            eb = float(np.float32(1e-4 * (x.max() - x.min())))
+            codec = Z.Codec(n, L, T)
+            a, b = codec.compress(dev(torch, x), eb), codec.compress(dev(torch, y), eb)
+            sa, sb = port.compress(x, eb, L, T), port.compress(y, eb, L, T)
+            assert a.tobytes() == sa
+            assert codec.homadd([a, b]).tobytes() == port.homadd(sa, sb, n, eb, L, T)
+            assert np.array_equal(codec.decompress(a, eb).cpu().numpy(),
+                                  port.decompress(sa, n, eb, L, T))
+            codec.check()
+
+
+def sinusoid_config1(n, seed):
+    """16M-element test signal: sin(2 pi i/4096) + 0.3 sin(2 pi i/97) + N(0, 0.01)."""
+    i = np.arange(n, dtype=np.float64)
+    rng = np.random.default_rng(seed)
+    return (np.sin(2 * np.pi * i / 4096) + 0.3 * np.sin(2 * np.pi * i / 97)
+            + rng.normal(0, 0.01, n)).astype(np.float32)
+
+
+def test_full_size_sinusoid_against_port(port, torch):
+    n, L, T = 16_777_216, 32, 16
+    x, y = sinusoid_config1(n, 0), sinusoid_config1(n, 1)
+    eb = float(np.float32(1e-4 * max(x.max() - x.min(), y.max() - y.min())))
+    codec = Z.Codec(n, L, T)
+    a, b = codec.compress(dev(torch, x), eb), codec.compress(dev(torch, y), eb)
+    h = codec.homadd([a, b])
+    da, dh = codec.decompress(a, eb).cpu().numpy(), codec.decompress(h, eb).cpu().numpy()
+    codec.check()
+    sa, sb = port.compress(x, eb, L, T), port.compress(y, eb, L, T)
+    assert a.tobytes() == sa and b.tobytes() == sb
+    assert h.tobytes() == port.homadd(sa, sb, n, eb, L, T)
+    assert np.array_equal(da, port.decompress(sa, n, eb, L, T))
+    slack = 4.0 * np.spacing(np.float32(2.0))
+    assert np.max(np.abs(da.astype(np.float64) - x)) <= eb + slack
+    assert np.max(np.abs(dh.astype(np.float64) - (x.astype(np.float64) + y))) <= 2 * eb + 2 * slack
+
+
+def test_errors_are_reported_not_faulted(torch):
+    n, L, T = 10000, 32, 2
+    codec = Z.Codec(n, L, T)
+    x = np.linspace(-1, 1, n).astype(np.float32)
+    x[1234] = np.nan
+    codec.compress(dev(torch, x), 1e-3)
+    with pytest.raises(Z.ZcclError) as e:
+        codec.check()
+    assert e.value.status == -3
+    good = codec.compress(dev(torch, np.linspace(-1, 1, n).astype(np.float32)), 1e-3)
+    codec.check()
+    raw = good.tobytes()
+    # truncated: the walk runs past the readable bytes
+    short = Z.DeviceStream.from_bytes(codec, raw[: len(raw) // 2])
+    codec.decompress(short, 1e-3)
+    with pytest.raises(Z.ZcclError) as e:
+        codec.check()
+    assert e.value.status in (-4, -5)
+    # a chunk offset that disagrees with the block walk
+    bad = bytearray(raw)
+    bad[8] ^= 0x01
+    codec.decompress(Z.DeviceStream.from_bytes(codec, bytes(bad)), 1e-3)
+    with pytest.raises(Z.ZcclError) as e:
+        codec.check()
+    assert e.value.status in (-4, -5)
+    # output capacity too small
+    tiny = codec.new_stream(capacity=64)
+    codec.compress(dev(torch, np.linspace(-1, 1, n).astype(np.float32)), 1e-3, out=tiny)
+    with pytest.raises(Z.ZcclError) as e:
+        codec.check()
+    assert e.value.status == -8

@@ -1,0 +1,277 @@
+"""GB300 implementation of ZCCL's fastmode1 compression hot path.
+
+Python bindings of the C ABI in ``include/zccl_gpu.h`` (the shared library
+``zccl_gb300/libzccl_gpu.so``).  Two layers, mirroring the C header:
+
+* the reference's entry points under their own names
+  (``ZCCL_float_openmp_threadblock_arg`` ...), taking numpy arrays (host
+  memory) or torch CUDA tensors (device memory);
+* ``Codec``: the device API with explicit writer thread count T, resident
+  compressed streams (``DeviceStream``) that carry their side index, and a
+  CUDA stream.
+
+The library is required: nothing here falls back to a CPU implementation.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libzccl_gpu.so")
+
+STATUS = {
+    0: "ok", -1: "invalid argument", -2: "CUDA runtime error",
+    -3: "input not finite or |x/eb| >= 2^31", -4: "stream inconsistent with its geometry",
+    -5: "stream runs past its readable bytes", -6: "device wait timed out",
+    -7: "out of memory", -8: "destination buffer too small",
+}
+
+EXPORTS = [
+    "ZCCL_float_openmp_threadblock_arg", "ZCCL_float_single_thread_arg",
+    "ZCCL_float_decompress_openmp_threadblock_arg", "ZCCL_float_decompress_single_thread_arg",
+    "ZCCL_float_homomophic_add_openmp_threadblock", "ZCCL_float_homomophic_add_single_thread",
+    "zccl_gpu_max_stream_bytes", "zccl_gpu_index_bytes", "zccl_gpu_workspace_bytes",
+    "zccl_gpu_compress", "zccl_gpu_decompress", "zccl_gpu_homadd", "zccl_gpu_homadd_cases",
+    "zccl_gpu_build_index", "zccl_gpu_stream_size", "zccl_gpu_check", "zccl_gpu_last_status",
+    "zccl_gpu_strerror", "zccl_gpu_width_table",
+]
+
+
+class ZcclError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        super().__init__(f"{what}: {STATUS.get(status, status)} ({status})")
+
+
+class StreamDesc(ctypes.Structure):
+    """``zccl_gpu_stream`` of include/zccl_gpu.h."""
+    _fields_ = [("bytes", ctypes.c_void_p), ("capacity", ctypes.c_size_t),
+                ("index", ctypes.c_void_p), ("indexed", ctypes.c_int),
+                ("qprev_valid", ctypes.c_int)]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load libzccl_gpu.so (build it first with ``python -m zccl_gb300.build``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing; build it with `python -m zccl_gb300.build`")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, sz, i, f = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_float
+    sp = ctypes.POINTER(StreamDesc)
+    sig = {
+        "ZCCL_float_openmp_threadblock_arg": (None, [vp, vp, vp, f, sz, i]),
+        "ZCCL_float_single_thread_arg": (None, [vp, vp, vp, f, sz, i]),
+        "ZCCL_float_decompress_openmp_threadblock_arg": (None, [vp, sz, f, i, vp]),
+        "ZCCL_float_decompress_single_thread_arg": (None, [vp, sz, f, i, vp]),
+        "ZCCL_float_homomophic_add_openmp_threadblock": (None, [vp, vp, sz, f, i, vp, vp]),
+        "ZCCL_float_homomophic_add_single_thread": (None, [vp, vp, sz, f, i, vp, vp]),
+        "zccl_gpu_max_stream_bytes": (sz, [sz, i, i]),
+        "zccl_gpu_index_bytes": (sz, [sz, i, i]),
+        "zccl_gpu_workspace_bytes": (sz, [sz, i, i]),
+        "zccl_gpu_compress": (i, [sp, vp, sz, f, i, i, vp, vp]),
+        "zccl_gpu_decompress": (i, [vp, sp, sz, f, i, i, vp, vp]),
+        "zccl_gpu_homadd": (i, [sp, sp, i, sz, i, i, vp, vp]),
+        "zccl_gpu_homadd_cases": (i, [sp, sp, i, sz, i, i, vp, vp, vp]),
+        "zccl_gpu_build_index": (i, [sp, sz, i, i, vp, vp]),
+        "zccl_gpu_stream_size": (i, [sp, sz, i, i, ctypes.POINTER(sz), vp]),
+        "zccl_gpu_check": (i, [vp, vp]),
+        "zccl_gpu_last_status": (i, []),
+        "zccl_gpu_strerror": (ctypes.c_char_p, [i]),
+        "zccl_gpu_width_table": (None, [ctypes.POINTER(ctypes.c_uint32)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def set_omp_threads(T: int) -> None:
+    """Set the OpenMP thread count the drop-in entry points read as T."""
+    fn = lib().omp_set_num_threads
+    fn.argtypes = [ctypes.c_int]
+    fn(T)
+
+
+def width_table() -> list:
+    arr = (ctypes.c_uint32 * 33)()
+    lib().zccl_gpu_width_table(arr)
+    return list(arr)
+
+
+def _check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise ZcclError(rc, what)
+
+
+def _ptr(a) -> int:
+    """Data pointer of a numpy array or a torch tensor."""
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()
+
+
+# ---------------------------------------------------------------------------
+# Reference entry points (host numpy arrays or device torch tensors)
+# ---------------------------------------------------------------------------
+
+def _size_slot(outSize):
+    return outSize if isinstance(outSize, ctypes.c_size_t) else ctypes.c_size_t(int(outSize or 0))
+
+
+def ZCCL_float_openmp_threadblock_arg(outputBytes, oriData, outSize, absErrBound, nbEle, blockSize):
+    """ZCCL/src/ZCCL_float.c:501; returns the assigned size."""
+    s = _size_slot(outSize)
+    lib().ZCCL_float_openmp_threadblock_arg(_ptr(outputBytes), _ptr(oriData), ctypes.byref(s),
+                                            absErrBound, nbEle, blockSize)
+    _check(lib().zccl_gpu_last_status(), "ZCCL_float_openmp_threadblock_arg")
+    return s.value
+
+
+def ZCCL_float_single_thread_arg(outputBytes, oriData, outSize, absErrBound, nbEle, blockSize):
+    """ZCCL/src/ZCCL_float.c:809; returns the assigned size."""
+    s = _size_slot(outSize)
+    lib().ZCCL_float_single_thread_arg(_ptr(outputBytes), _ptr(oriData), ctypes.byref(s),
+                                       absErrBound, nbEle, blockSize)
+    _check(lib().zccl_gpu_last_status(), "ZCCL_float_single_thread_arg")
+    return s.value
+
+
+def ZCCL_float_decompress_openmp_threadblock_arg(newData, nbEle, absErrBound, blockSize, cmpBytes):
+    """ZCCL/src/ZCCLd_float.c:538."""
+    lib().ZCCL_float_decompress_openmp_threadblock_arg(_ptr(newData), nbEle, absErrBound,
+                                                       blockSize, _ptr(cmpBytes))
+    _check(lib().zccl_gpu_last_status(), "ZCCL_float_decompress_openmp_threadblock_arg")
+
+
+def ZCCL_float_decompress_single_thread_arg(newData, nbEle, absErrBound, blockSize, cmpBytes):
+    """ZCCL/src/ZCCLd_float.c:247."""
+    lib().ZCCL_float_decompress_single_thread_arg(_ptr(newData), nbEle, absErrBound, blockSize,
+                                                  _ptr(cmpBytes))
+    _check(lib().zccl_gpu_last_status(), "ZCCL_float_decompress_single_thread_arg")
+
+
+def ZCCL_float_homomophic_add_openmp_threadblock(final_cmpBytes, final_cmpSize, nbEle, absErrBound,
+                                                 blockSize, cmpBytes, cmpBytes2):
+    """ZCCL/src/ZCCLd_float.c:988; returns the accumulated size (the
+    reference adds the result size to *final_cmpSize)."""
+    s = _size_slot(final_cmpSize)
+    lib().ZCCL_float_homomophic_add_openmp_threadblock(_ptr(final_cmpBytes), ctypes.byref(s),
+                                                       nbEle, absErrBound, blockSize,
+                                                       _ptr(cmpBytes), _ptr(cmpBytes2))
+    _check(lib().zccl_gpu_last_status(), "ZCCL_float_homomophic_add_openmp_threadblock")
+    return s.value
+
+
+def ZCCL_float_homomophic_add_single_thread(final_cmpBytes, final_cmpSize, nbEle, absErrBound,
+                                            blockSize, cmpBytes, cmpBytes2):
+    """ZCCL/src/ZCCLd_float.c:1681; returns the accumulated size."""
+    s = _size_slot(final_cmpSize)
+    lib().ZCCL_float_homomophic_add_single_thread(_ptr(final_cmpBytes), ctypes.byref(s), nbEle,
+                                                  absErrBound, blockSize, _ptr(cmpBytes),
+                                                  _ptr(cmpBytes2))
+    _check(lib().zccl_gpu_last_status(), "ZCCL_float_homomophic_add_single_thread")
+    return s.value
+
+
+# ---------------------------------------------------------------------------
+# Device API
+# ---------------------------------------------------------------------------
+
+class DeviceStream:
+    """A compressed stream resident in device memory with its side index."""
+
+    def __init__(self, codec: "Codec", capacity: int | None = None, data=None):
+        import torch
+        self.codec = codec
+        cap = capacity if capacity is not None else codec.max_stream_bytes
+        if data is not None:
+            self.buf = data
+            cap = data.numel()
+        else:
+            self.buf = torch.empty(max(cap, 16), dtype=torch.uint8, device=codec.device)
+        self.index = torch.empty(codec.index_bytes, dtype=torch.uint8, device=codec.device)
+        self.desc = StreamDesc(self.buf.data_ptr(), cap, self.index.data_ptr(), 0, 0)
+
+    @classmethod
+    def from_bytes(cls, codec: "Codec", data) -> "DeviceStream":
+        """Wrap wire bytes (a CUDA uint8 tensor, or bytes copied to the device)."""
+        import torch
+        if not isinstance(data, torch.Tensor):
+            data = torch.frombuffer(bytearray(data), dtype=torch.uint8).to(codec.device)
+        return cls(codec, data=data)
+
+    def size(self) -> int:
+        s = ctypes.c_size_t(0)
+        _check(lib().zccl_gpu_stream_size(ctypes.byref(self.desc), self.codec.n, self.codec.L,
+                                          self.codec.T, ctypes.byref(s), self.codec.stream_ptr),
+               "zccl_gpu_stream_size")
+        return s.value
+
+    def tobytes(self) -> bytes:
+        return self.buf[: self.size()].cpu().numpy().tobytes()
+
+
+class Codec:
+    """Device API for one geometry (n floats, block size L, writer count T)."""
+
+    def __init__(self, n: int, L: int = 32, T: int = 1, device: str = "cuda", stream=None):
+        import torch
+        self.n, self.L, self.T = int(n), int(L), int(T)
+        self.device = torch.device(device)
+        self.max_stream_bytes = lib().zccl_gpu_max_stream_bytes(self.n, self.L, self.T)
+        self.index_bytes = lib().zccl_gpu_index_bytes(self.n, self.L, self.T)
+        ws = lib().zccl_gpu_workspace_bytes(self.n, self.L, self.T)
+        if not (self.max_stream_bytes and self.index_bytes and ws):
+            raise ZcclError(-1, f"geometry n={n} L={L} T={T}")
+        self.ws = torch.zeros(ws, dtype=torch.uint8, device=self.device)
+        self.torch_stream = stream or torch.cuda.current_stream(self.device)
+        self.stream_ptr = ctypes.c_void_p(self.torch_stream.cuda_stream)
+
+    def new_stream(self, capacity: int | None = None) -> DeviceStream:
+        return DeviceStream(self, capacity)
+
+    def compress(self, x, eb: float, out: DeviceStream | None = None) -> DeviceStream:
+        out = out or self.new_stream()
+        _check(lib().zccl_gpu_compress(ctypes.byref(out.desc), x.data_ptr(), self.n, eb, self.L,
+                                       self.T, self.ws.data_ptr(), self.stream_ptr),
+               "zccl_gpu_compress")
+        return out
+
+    def decompress(self, s: DeviceStream, eb: float, out=None):
+        import torch
+        out = out if out is not None else torch.empty(self.n, dtype=torch.float32,
+                                                      device=self.device)
+        _check(lib().zccl_gpu_decompress(out.data_ptr(), ctypes.byref(s.desc), self.n, eb, self.L,
+                                         self.T, self.ws.data_ptr(), self.stream_ptr),
+               "zccl_gpu_decompress")
+        return out
+
+    def homadd(self, ins, out: DeviceStream | None = None, cases=None) -> DeviceStream:
+        out = out or self.new_stream()
+        arr = (StreamDesc * len(ins))(*[s.desc for s in ins])
+        rc = lib().zccl_gpu_homadd_cases(ctypes.byref(out.desc), arr, len(ins), self.n, self.L,
+                                         self.T, self.ws.data_ptr(),
+                                         cases.data_ptr() if cases is not None else None,
+                                         self.stream_ptr)
+        for s, d in zip(ins, arr):  # the call may have indexed the inputs
+            s.desc.indexed, s.desc.qprev_valid = d.indexed, d.qprev_valid
+        _check(rc, "zccl_gpu_homadd")
+        return out
+
+    def build_index(self, s: DeviceStream) -> None:
+        _check(lib().zccl_gpu_build_index(ctypes.byref(s.desc), self.n, self.L, self.T,
+                                          self.ws.data_ptr(), self.stream_ptr),
+               "zccl_gpu_build_index")
+
+    def check(self) -> None:
+        _check(lib().zccl_gpu_check(self.ws.data_ptr(), self.stream_ptr), "device status")

@@ -1,0 +1,618 @@
+/*
+ * zccl_capi.cu -- the C ABI declared in include/zccl_gpu.h.
+ *
+ * Device API: argument checks, index / workspace layout, kernel launches.
+ * Drop-in layer: the reference's six codec entry points on top of it, with
+ * host pointers staged through cached device buffers and device pointers
+ * used in place.
+ */
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <omp.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "../../include/zccl_gpu.h"
+#include "zkern.cuh"
+
+namespace {
+
+/* ------------------------------------------------------------------ */
+/* width thresholds from this host's libm                              */
+/* ------------------------------------------------------------------ */
+
+ZWidthTable g_wt;
+std::once_flag g_wt_once;
+
+/* The reference's width: (int)(log2f(max)) + 1 with max an unsigned int
+ * (ZCCL/src/ZCCL_float.c:606). */
+__host__ int host_width(uint32_t m)
+{
+    volatile float f = (float)m;
+    return (int)(log2f(f)) + 1;
+}
+
+void init_width_table()
+{
+    g_wt.thr[0] = 0xFFFFFFFFu;
+    for (uint32_t w = 1; w <= 32; w++) {
+        uint64_t lo = 1ull << (w - 1), m = (1ull << w) - 1;
+        uint32_t first = 0xFFFFFFFFu;
+        while (m >= lo && host_width((uint32_t)m) == (int)w + 1) {
+            first = (uint32_t)m;
+            m--;
+        }
+        g_wt.thr[w] = first;
+    }
+}
+
+const ZWidthTable &width_table()
+{
+    std::call_once(g_wt_once, init_width_table);
+    return g_wt;
+}
+
+/* ------------------------------------------------------------------ */
+/* layouts                                                             */
+/* ------------------------------------------------------------------ */
+
+size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+int make_geom(size_t n, int L, int T, ZGeom *g)
+{
+    if (L < 1 || T < 1) return ZCCL_GPU_EINVAL;
+    if (zg_init(g, (uint64_t)n, (uint32_t)L, (uint32_t)T) != 0) return ZCCL_GPU_EINVAL;
+    return ZCCL_GPU_OK;
+}
+
+/* Side index: size | tile_off[ntiles] | tile_qprev[ntiles] | widths[nblocks] */
+struct IndexLayout {
+    size_t tile_off, qprev, widths, total;
+};
+
+IndexLayout index_layout(const ZGeom &g)
+{
+    IndexLayout l;
+    l.tile_off = 16;
+    l.qprev = align16(l.tile_off + 8 * g.ntiles);
+    l.widths = align16(l.qprev + 4 * g.ntiles);
+    l.total = align16(l.widths + g.nblocks) + 16;
+    return l;
+}
+
+ZIndex bind_index(void *mem, const ZGeom &g)
+{
+    IndexLayout l = index_layout(g);
+    uint8_t *p = (uint8_t *)mem;
+    ZIndex z;
+    z.size = (uint64_t *)p;
+    z.tile_off = (uint64_t *)(p + l.tile_off);
+    z.tile_qprev = (int32_t *)(p + l.qprev);
+    z.widths = p + l.widths;
+    return z;
+}
+
+/* Workspace: err u32 | pad | ticket u32 | pad | status[ntiles] */
+size_t ws_bytes(const ZGeom &g) { return 16 + 8 * g.ntiles + 16; }
+
+ZWork bind_ws(void *ws)
+{
+    uint8_t *p = (uint8_t *)ws;
+    ZWork w;
+    w.err = (uint32_t *)p;
+    w.ticket = (uint32_t *)(p + 8);
+    w.status = (uint64_t *)(p + 16);
+    return w;
+}
+
+int status_of_bits(uint32_t bits)
+{
+    if (bits & ZERR_TIMEOUT) return ZCCL_GPU_ETIMEOUT;
+    if (bits & ZERR_CORRUPT) return ZCCL_GPU_ECORRUPT;
+    if (bits & ZERR_BOUNDS) return ZCCL_GPU_EBOUNDS;
+    if (bits & ZERR_CAPACITY) return ZCCL_GPU_ECAPACITY;
+    if (bits & ZERR_RANGE) return ZCCL_GPU_ERANGE;
+    return ZCCL_GPU_OK;
+}
+
+int cuda_status(cudaError_t e) { return e == cudaSuccess ? ZCCL_GPU_OK : ZCCL_GPU_ECUDA; }
+
+/* Enqueue the index walk of a byte-only stream (no workspace reset). */
+int walk_stream(zccl_gpu_stream *s, const ZGeom &g, const ZWork &w, cudaStream_t st)
+{
+    WalkArgs a;
+    a.in = s->bytes;
+    a.avail = s->capacity;
+    a.g = g;
+    a.idx = bind_index(s->index, g);
+    a.err = w.err;
+    int rc = cuda_status(launch_walk(a, st));
+    if (rc == ZCCL_GPU_OK) {
+        s->indexed = 1;
+        s->qprev_valid = 0;
+    }
+    return rc;
+}
+
+bool valid_stream(const zccl_gpu_stream *s) { return s && s->bytes && s->index; }
+
+} // namespace
+
+/* ==================================================================== */
+/* device API                                                           */
+/* ==================================================================== */
+
+extern "C" size_t zccl_gpu_max_stream_bytes(size_t n, int L, int T)
+{
+    ZGeom g;
+    if (make_geom(n, L, T, &g)) return 0;
+    return (size_t)zg_stream_worst(&g);
+}
+
+extern "C" size_t zccl_gpu_index_bytes(size_t n, int L, int T)
+{
+    ZGeom g;
+    if (make_geom(n, L, T, &g)) return 0;
+    return index_layout(g).total;
+}
+
+extern "C" size_t zccl_gpu_workspace_bytes(size_t n, int L, int T)
+{
+    ZGeom g;
+    if (make_geom(n, L, T, &g)) return 0;
+    return ws_bytes(g);
+}
+
+extern "C" void zccl_gpu_width_table(uint32_t thr[33])
+{
+    const ZWidthTable &wt = width_table();
+    memcpy(thr, wt.thr, sizeof(wt.thr));
+}
+
+extern "C" int zccl_gpu_compress(zccl_gpu_stream *out, const float *d_in, size_t n, float eb, int L,
+                                 int T, void *d_ws, void *cuda_stream)
+{
+    ZGeom g;
+    if (make_geom(n, L, T, &g) || !valid_stream(out) || !d_in || !d_ws) return ZCCL_GPU_EINVAL;
+    if (!(eb > 0.0f) || !isfinite(eb)) return ZCCL_GPU_EINVAL;
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    CompressArgs a;
+    a.x = d_in;
+    a.out = out->bytes;
+    a.cap = out->capacity;
+    a.g = g;
+    a.inv = 1.0f / eb; /* float division, as ZCCL/src/ZCCL_float.c:540 */
+    a.idx = bind_index(out->index, g);
+    a.w = bind_ws(d_ws);
+    a.wt = width_table();
+    a.sm = zg_smem(g.L, g.TB);
+    if (cudaMemsetAsync(d_ws, 0, ws_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    int rc = cuda_status(launch_compress(a, st));
+    if (rc == ZCCL_GPU_OK) {
+        out->indexed = 1;
+        out->qprev_valid = 1;
+    }
+    return rc;
+}
+
+extern "C" int zccl_gpu_build_index(zccl_gpu_stream *s, size_t n, int L, int T, void *d_ws,
+                                    void *cuda_stream)
+{
+    ZGeom g;
+    if (make_geom(n, L, T, &g) || !valid_stream(s) || !d_ws) return ZCCL_GPU_EINVAL;
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    if (cudaMemsetAsync(d_ws, 0, ws_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    return walk_stream(s, g, bind_ws(d_ws), st);
+}
+
+extern "C" int zccl_gpu_decompress(float *d_out, zccl_gpu_stream *in, size_t n, float eb, int L,
+                                   int T, void *d_ws, void *cuda_stream)
+{
+    ZGeom g;
+    if (make_geom(n, L, T, &g) || !valid_stream(in) || !d_out || !d_ws) return ZCCL_GPU_EINVAL;
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    if (cudaMemsetAsync(d_ws, 0, ws_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    ZWork w = bind_ws(d_ws);
+    if (!in->indexed) {
+        int rc = walk_stream(in, g, w, st);
+        if (rc) return rc;
+    }
+    DecompressArgs a;
+    a.in = in->bytes;
+    a.avail = in->capacity;
+    a.y = d_out;
+    a.g = g;
+    a.eb = eb;
+    a.idx = bind_index(in->index, g);
+    a.qprev_valid = in->qprev_valid;
+    a.w = w;
+    a.sm = zg_smem(g.L, g.TB);
+    int rc = cuda_status(launch_decompress(a, st));
+    if (rc == ZCCL_GPU_OK) in->qprev_valid = 1;
+    return rc;
+}
+
+extern "C" int zccl_gpu_homadd_cases(zccl_gpu_stream *out, zccl_gpu_stream *ins, int P, size_t n,
+                                     int L, int T, void *d_ws, unsigned long long *d_cases,
+                                     void *cuda_stream)
+{
+    ZGeom g;
+    if (make_geom(n, L, T, &g) || !valid_stream(out) || !ins || P < 1 || P > ZH_MAXP || !d_ws)
+        return ZCCL_GPU_EINVAL;
+    for (int p = 0; p < P; p++)
+        if (!valid_stream(&ins[p]) || ins[p].bytes == out->bytes) return ZCCL_GPU_EINVAL;
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    if (cudaMemsetAsync(d_ws, 0, ws_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    ZWork w = bind_ws(d_ws);
+    HomAddArgs a;
+    memset(&a, 0, sizeof(a));
+    int qv = 1;
+    for (int p = 0; p < P; p++) {
+        if (!ins[p].indexed) {
+            int rc = walk_stream(&ins[p], g, w, st);
+            if (rc) return rc;
+        }
+        ZIndex ix = bind_index(ins[p].index, g);
+        a.in[p].bytes = ins[p].bytes;
+        a.in[p].avail = ins[p].capacity;
+        a.in[p].widths = ix.widths;
+        a.in[p].tile_off = ix.tile_off;
+        a.in[p].tile_qprev = ix.tile_qprev;
+        qv &= ins[p].qprev_valid ? 1 : 0;
+    }
+    a.P = (uint32_t)P;
+    a.qprev_valid = qv;
+    a.out = out->bytes;
+    a.cap = out->capacity;
+    a.idx = bind_index(out->index, g);
+    a.cases = d_cases;
+    a.g = g;
+    a.w = w;
+    a.wt = width_table();
+    a.sm = zg_smem(g.L, g.TB);
+    int rc = cuda_status(launch_homadd(a, st));
+    if (rc == ZCCL_GPU_OK) {
+        out->indexed = 1;
+        out->qprev_valid = qv;
+    }
+    return rc;
+}
+
+extern "C" int zccl_gpu_homadd(zccl_gpu_stream *out, zccl_gpu_stream *ins, int P, size_t n, int L,
+                               int T, void *d_ws, void *cuda_stream)
+{
+    return zccl_gpu_homadd_cases(out, ins, P, n, L, T, d_ws, nullptr, cuda_stream);
+}
+
+extern "C" int zccl_gpu_stream_size(const zccl_gpu_stream *s, size_t n, int L, int T, size_t *size,
+                                    void *cuda_stream)
+{
+    ZGeom g;
+    if (make_geom(n, L, T, &g) || !valid_stream(s) || !size) return ZCCL_GPU_EINVAL;
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    uint64_t v = 0;
+    if (cudaMemcpyAsync(&v, s->index, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return ZCCL_GPU_ECUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    *size = (size_t)v;
+    return ZCCL_GPU_OK;
+}
+
+extern "C" int zccl_gpu_check(void *d_ws, void *cuda_stream)
+{
+    if (!d_ws) return ZCCL_GPU_EINVAL;
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    uint32_t bits = 0;
+    if (cudaMemcpyAsync(&bits, d_ws, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return ZCCL_GPU_ECUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    return status_of_bits(bits);
+}
+
+extern "C" const char *zccl_gpu_strerror(int status)
+{
+    switch (status) {
+    case ZCCL_GPU_OK: return "ok";
+    case ZCCL_GPU_EINVAL: return "invalid argument";
+    case ZCCL_GPU_ECUDA: return "CUDA runtime error";
+    case ZCCL_GPU_ERANGE: return "input not finite or |x/eb| >= 2^31";
+    case ZCCL_GPU_ECORRUPT: return "stream inconsistent with its geometry";
+    case ZCCL_GPU_EBOUNDS: return "stream runs past its readable bytes";
+    case ZCCL_GPU_ETIMEOUT: return "device wait timed out";
+    case ZCCL_GPU_ENOMEM: return "out of memory";
+    case ZCCL_GPU_ECAPACITY: return "destination buffer too small";
+    default: return "unknown status";
+    }
+}
+
+/* ==================================================================== */
+/* drop-in layer                                                        */
+/* ==================================================================== */
+
+namespace {
+
+thread_local int t_last_status = ZCCL_GPU_OK;
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t n = 0;
+    int ensure(size_t bytes)
+    {
+        if (bytes <= n) return ZCCL_GPU_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        size_t want = bytes + bytes / 8 + 256;
+        if (cudaMalloc(&p, want) != cudaSuccess) {
+            cudaGetLastError();
+            return ZCCL_GPU_ENOMEM;
+        }
+        n = want;
+        return ZCCL_GPU_OK;
+    }
+};
+
+/* Cached device buffers of the drop-in layer, one set per device. */
+struct DropCtx {
+    std::mutex mu;
+    cudaStream_t st = nullptr;
+    DevBuf fin, fout, s[3], ix[3], ws;
+};
+
+DropCtx *drop_ctx()
+{
+    static std::mutex gmu;
+    static DropCtx *ctxs[64] = {nullptr};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(gmu);
+    if (!ctxs[dev]) {
+        DropCtx *c = new DropCtx();
+        if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
+            delete c;
+            return nullptr;
+        }
+        ctxs[dev] = c;
+    }
+    return ctxs[dev];
+}
+
+bool is_device_ptr(const void *p)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+/* Bytes from p to the end of its device allocation.  The driver call is
+ * reached through the runtime's entry-point table so the library does not
+ * link libcuda (it loads on hosts without a GPU driver). */
+typedef CUresult (*PFN_range)(CUdeviceptr *, size_t *, CUdeviceptr);
+
+size_t device_room(const void *p)
+{
+    static PFN_range fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuMemGetAddressRange", &f, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_range)f;
+        else
+            cudaGetLastError();
+    });
+    CUdeviceptr base = 0;
+    size_t size = 0;
+    if (!fn || fn(&base, &size, (CUdeviceptr)p) != CUDA_SUCCESS) return 0;
+    return (size_t)(base + size - (CUdeviceptr)p);
+}
+
+int finish(DropCtx *c, void *ws)
+{
+    int rc = zccl_gpu_check(ws, c->st);
+    return rc;
+}
+
+void report(const char *fn, int rc)
+{
+    t_last_status = rc;
+    if (rc != ZCCL_GPU_OK) fprintf(stderr, "zccl_gpu: %s: %s\n", fn, zccl_gpu_strerror(rc));
+}
+
+/* Make a stream view of cmp: in place for device memory, else copied. */
+int stage_stream(DropCtx *c, int slot, const unsigned char *cmp, const ZGeom &g,
+                 zccl_gpu_stream *s)
+{
+    size_t ixb = index_layout(g).total;
+    if (int rc = c->ix[slot].ensure(ixb)) return rc;
+    s->index = c->ix[slot].p;
+    s->indexed = 0;
+    s->qprev_valid = 0;
+    if (is_device_ptr(cmp)) {
+        s->bytes = (unsigned char *)cmp;
+        s->capacity = device_room(cmp);
+        return s->capacity ? ZCCL_GPU_OK : ZCCL_GPU_EINVAL;
+    }
+    /* Host stream: the header gives the first T-1 chunk lengths; the last
+     * chunk is read up to its largest possible size, but not past the
+     * 4*nbEle bytes every reference caller allocates for a stream. */
+    const size_t hdr = 8ull * g.T;
+    uint64_t last;
+    memcpy(&last, cmp + 8ull * (g.T - 1), 8);
+    size_t known = hdr + (size_t)last;
+    size_t want = known + (size_t)(zg_seg_worst(g.tbs, g.L) + zg_seg_worst(g.rem, g.L));
+    size_t room = 4 * (size_t)g.n > known + 4 ? 4 * (size_t)g.n : known + 4;
+    size_t bytes = want < room ? want : room;
+    if (int rc = c->s[slot].ensure(bytes)) return rc;
+    if (cudaMemcpyAsync(c->s[slot].p, cmp, bytes, cudaMemcpyHostToDevice, c->st) != cudaSuccess)
+        return ZCCL_GPU_ECUDA;
+    s->bytes = (unsigned char *)c->s[slot].p;
+    s->capacity = bytes;
+    return ZCCL_GPU_OK;
+}
+
+int dropin_compress(unsigned char *outputBytes, const float *oriData, size_t *outSize, float eb,
+                    size_t n, int L, int T)
+{
+    ZGeom g;
+    if (!outputBytes || !oriData || !outSize || make_geom(n, L, T, &g)) return ZCCL_GPU_EINVAL;
+    DropCtx *c = drop_ctx();
+    if (!c) return ZCCL_GPU_ECUDA;
+    std::lock_guard<std::mutex> lk(c->mu);
+    const float *d_in = oriData;
+    if (!is_device_ptr(oriData)) {
+        if (int rc = c->fin.ensure(4 * n)) return rc;
+        if (cudaMemcpyAsync(c->fin.p, oriData, 4 * n, cudaMemcpyHostToDevice, c->st) != cudaSuccess)
+            return ZCCL_GPU_ECUDA;
+        d_in = (const float *)c->fin.p;
+    }
+    const size_t worst = (size_t)zg_stream_worst(&g);
+    const bool dout = is_device_ptr(outputBytes);
+    const size_t room = dout ? device_room(outputBytes) : 0;
+    zccl_gpu_stream s;
+    if (int rc = c->ix[0].ensure(index_layout(g).total)) return rc;
+    if (int rc = c->ws.ensure(ws_bytes(g))) return rc;
+    s.index = c->ix[0].p;
+    if (dout && room >= worst) {
+        s.bytes = outputBytes;
+        s.capacity = room;
+    } else {
+        if (int rc = c->s[0].ensure(worst)) return rc;
+        s.bytes = (unsigned char *)c->s[0].p;
+        s.capacity = worst;
+    }
+    if (int rc = zccl_gpu_compress(&s, d_in, n, eb, L, T, c->ws.p, c->st)) return rc;
+    if (int rc = finish(c, c->ws.p)) return rc;
+    size_t size = 0;
+    if (int rc = zccl_gpu_stream_size(&s, n, L, T, &size, c->st)) return rc;
+    if (s.bytes != outputBytes) {
+        if (dout && size > room) return ZCCL_GPU_ECAPACITY;
+        cudaMemcpyKind k = dout ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        if (cudaMemcpyAsync(outputBytes, s.bytes, size, k, c->st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+        if (cudaStreamSynchronize(c->st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    }
+    *outSize = size;
+    return ZCCL_GPU_OK;
+}
+
+int dropin_decompress(float *newData, size_t n, float eb, int L, const unsigned char *cmp, int T)
+{
+    ZGeom g;
+    if (!newData || !cmp || make_geom(n, L, T, &g)) return ZCCL_GPU_EINVAL;
+    DropCtx *c = drop_ctx();
+    if (!c) return ZCCL_GPU_ECUDA;
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (int rc = c->ws.ensure(ws_bytes(g))) return rc;
+    zccl_gpu_stream s;
+    if (int rc = stage_stream(c, 0, cmp, g, &s)) return rc;
+    const bool dout = is_device_ptr(newData);
+    float *d_out = newData;
+    if (!dout) {
+        if (int rc = c->fout.ensure(4 * n)) return rc;
+        d_out = (float *)c->fout.p;
+    }
+    if (int rc = zccl_gpu_decompress(d_out, &s, n, eb, L, T, c->ws.p, c->st)) return rc;
+    if (int rc = finish(c, c->ws.p)) return rc;
+    if (!dout) {
+        if (cudaMemcpyAsync(newData, d_out, 4 * n, cudaMemcpyDeviceToHost, c->st) != cudaSuccess)
+            return ZCCL_GPU_ECUDA;
+        if (cudaStreamSynchronize(c->st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    }
+    return ZCCL_GPU_OK;
+}
+
+int dropin_homadd(unsigned char *final_cmp, size_t *final_size, size_t n, float eb, int L,
+                  const unsigned char *cmp1, const unsigned char *cmp2, int T)
+{
+    (void)eb;
+    ZGeom g;
+    if (!final_cmp || !final_size || !cmp1 || !cmp2 || make_geom(n, L, T, &g)) return ZCCL_GPU_EINVAL;
+    DropCtx *c = drop_ctx();
+    if (!c) return ZCCL_GPU_ECUDA;
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (int rc = c->ws.ensure(ws_bytes(g))) return rc;
+    zccl_gpu_stream in[2], out;
+    if (int rc = stage_stream(c, 0, cmp1, g, &in[0])) return rc;
+    if (int rc = stage_stream(c, 1, cmp2, g, &in[1])) return rc;
+    const size_t worst = (size_t)zg_stream_worst(&g);
+    if (int rc = c->s[2].ensure(worst)) return rc;
+    if (int rc = c->ix[2].ensure(index_layout(g).total)) return rc;
+    out.bytes = (unsigned char *)c->s[2].p;
+    out.capacity = worst;
+    out.index = c->ix[2].p;
+    if (int rc = zccl_gpu_homadd(&out, in, 2, n, L, T, c->ws.p, c->st)) return rc;
+    if (int rc = finish(c, c->ws.p)) return rc;
+    size_t size = 0;
+    if (int rc = zccl_gpu_stream_size(&out, n, L, T, &size, c->st)) return rc;
+    const bool dout = is_device_ptr(final_cmp);
+    if (dout && size > device_room(final_cmp)) return ZCCL_GPU_ECAPACITY;
+    cudaMemcpyKind k = dout ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (cudaMemcpyAsync(final_cmp, out.bytes, size, k, c->st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    if (cudaStreamSynchronize(c->st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    *final_size += size;
+    return ZCCL_GPU_OK;
+}
+
+int omp_threads() { return omp_get_max_threads(); }
+
+} // namespace
+
+extern "C" int zccl_gpu_last_status(void) { return t_last_status; }
+
+extern "C" void ZCCL_float_openmp_threadblock_arg(unsigned char *outputBytes, float *oriData,
+                                                  size_t *outSize, float absErrBound, size_t nbEle,
+                                                  int blockSize)
+{
+    report(__func__, dropin_compress(outputBytes, oriData, outSize, absErrBound, nbEle, blockSize,
+                                     omp_threads()));
+}
+
+extern "C" void ZCCL_float_single_thread_arg(unsigned char *outputBytes, float *oriData,
+                                             size_t *outSize, float absErrBound, size_t nbEle,
+                                             int blockSize)
+{
+    report(__func__, dropin_compress(outputBytes, oriData, outSize, absErrBound, nbEle, blockSize, 1));
+}
+
+extern "C" void ZCCL_float_decompress_openmp_threadblock_arg(float *newData, size_t nbEle,
+                                                             float absErrBound, int blockSize,
+                                                             unsigned char *cmpBytes)
+{
+    report(__func__,
+           dropin_decompress(newData, nbEle, absErrBound, blockSize, cmpBytes, omp_threads()));
+}
+
+extern "C" void ZCCL_float_decompress_single_thread_arg(float *newData, size_t nbEle,
+                                                        float absErrBound, int blockSize,
+                                                        unsigned char *cmpBytes)
+{
+    report(__func__, dropin_decompress(newData, nbEle, absErrBound, blockSize, cmpBytes, 1));
+}
+
+extern "C" void ZCCL_float_homomophic_add_openmp_threadblock(unsigned char *final_cmpBytes,
+                                                             size_t *final_cmpSize, size_t nbEle,
+                                                             float absErrBound, int blockSize,
+                                                             unsigned char *cmpBytes,
+                                                             unsigned char *cmpBytes2)
+{
+    report(__func__, dropin_homadd(final_cmpBytes, final_cmpSize, nbEle, absErrBound, blockSize,
+                                   cmpBytes, cmpBytes2, omp_threads()));
+}
+
+extern "C" void ZCCL_float_homomophic_add_single_thread(unsigned char *final_cmpBytes,
+                                                        size_t *final_cmpSize, size_t nbEle,
+                                                        float absErrBound, int blockSize,
+                                                        unsigned char *cmpBytes,
+                                                        unsigned char *cmpBytes2)
+{
+    report(__func__, dropin_homadd(final_cmpBytes, final_cmpSize, nbEle, absErrBound, blockSize,
+                                   cmpBytes, cmpBytes2, 1));
+}
