@@ -50,8 +50,10 @@ void ZCCL_float_single_thread_arg(unsigned char *outputBytes, float *oriData, si
  * (ZCCL/include/ZCCLd_float.h:21, ZCCL/src/ZCCLd_float.c:538).  The stream
  * carries no length; with a host pointer, cmpBytes must be readable for
  * min(4*nbEle, largest possible stream) bytes, the capacity every reference
- * caller gives its stream buffers; with a device pointer, up to the end of
- * its allocation. */
+ * caller gives its stream buffers (a stream longer than 4*nbEle -- tiny
+ * arrays, or blocks near 32 bits wide -- must be readable up to its largest
+ * possible size, zccl_gpu_max_stream_bytes()); with a device pointer, up to
+ * the end of its allocation. */
 void ZCCL_float_decompress_openmp_threadblock_arg(float *newData, size_t nbEle, float absErrBound,
                                                   int blockSize, unsigned char *cmpBytes);
 

@@ -95,14 +95,44 @@ ZIndex bind_index(void *mem, const ZGeom &g)
     return z;
 }
 
-/* Workspace: err u32 | pad | ticket u32 | pad | status[ntiles] */
-size_t ws_bytes(const ZGeom &g) { return 16 + 8 * g.ntiles + 16; }
+/* Workspace: err u32 | walk_err u32 | ticket u32 | pad | status[ntiles] |
+ * header-walk scratch.  Only the first part is cleared per call. */
+struct WalkLayout {
+    uint32_t M, max_windows, max_groups;
+    size_t seg_P, seg_R, seg_end, seg_ok, win_base, grp_base, wtab, gtab, gentry, gbase, total;
+};
+
+size_t ws_clear_bytes(const ZGeom &g) { return 16 + 8 * g.ntiles; }
+
+WalkLayout walk_layout(const ZGeom &g)
+{
+    WalkLayout l;
+    l.M = zg_block_bytes(32, g.L);
+    l.max_windows = (uint32_t)(zg_stream_worst(&g) / WALK_WW + g.T + 2);
+    l.max_groups = (l.max_windows + WALK_G - 1) / WALK_G + g.T + 1;
+    size_t o = align16(ws_clear_bytes(g));
+    l.seg_P = o; o = align16(o + 8ull * g.T);
+    l.seg_R = o; o = align16(o + 8ull * g.T);
+    l.seg_end = o; o = align16(o + 8ull * g.T);
+    l.seg_ok = o; o = align16(o + 4ull * g.T);
+    l.win_base = o; o = align16(o + 4ull * (g.T + 1));
+    l.grp_base = o; o = align16(o + 4ull * (g.T + 1));
+    l.wtab = o; o = align16(o + 4ull * l.max_windows * l.M);
+    l.gtab = o; o = align16(o + 8ull * l.max_groups * l.M);
+    l.gentry = o; o = align16(o + 4ull * l.max_groups);
+    l.gbase = o; o = align16(o + 8ull * l.max_groups);
+    l.total = o + 16;
+    return l;
+}
+
+size_t ws_bytes(const ZGeom &g) { return walk_layout(g).total; }
 
 ZWork bind_ws(void *ws)
 {
     uint8_t *p = (uint8_t *)ws;
     ZWork w;
     w.err = (uint32_t *)p;
+    w.walk_err = (uint32_t *)(p + 4);
     w.ticket = (uint32_t *)(p + 8);
     w.status = (uint64_t *)(p + 16);
     return w;
@@ -111,8 +141,9 @@ ZWork bind_ws(void *ws)
 int status_of_bits(uint32_t bits)
 {
     if (bits & ZERR_TIMEOUT) return ZCCL_GPU_ETIMEOUT;
-    if (bits & ZERR_CORRUPT) return ZCCL_GPU_ECORRUPT;
+    /* running out of bytes makes later checks fail too: report it first */
     if (bits & ZERR_BOUNDS) return ZCCL_GPU_EBOUNDS;
+    if (bits & ZERR_CORRUPT) return ZCCL_GPU_ECORRUPT;
     if (bits & ZERR_CAPACITY) return ZCCL_GPU_ECAPACITY;
     if (bits & ZERR_RANGE) return ZCCL_GPU_ERANGE;
     return ZCCL_GPU_OK;
@@ -121,14 +152,30 @@ int status_of_bits(uint32_t bits)
 int cuda_status(cudaError_t e) { return e == cudaSuccess ? ZCCL_GPU_OK : ZCCL_GPU_ECUDA; }
 
 /* Enqueue the index walk of a byte-only stream (no workspace reset). */
-int walk_stream(zccl_gpu_stream *s, const ZGeom &g, const ZWork &w, cudaStream_t st)
+int walk_stream(zccl_gpu_stream *s, const ZGeom &g, void *ws, cudaStream_t st)
 {
+    const WalkLayout l = walk_layout(g);
+    uint8_t *p = (uint8_t *)ws;
     WalkArgs a;
+    memset(&a, 0, sizeof(a));
     a.in = s->bytes;
     a.avail = s->capacity;
+    a.end_bound = zg_stream_worst(&g);
     a.g = g;
     a.idx = bind_index(s->index, g);
-    a.err = w.err;
+    a.err = bind_ws(ws).walk_err;
+    a.ws.seg_P = (uint64_t *)(p + l.seg_P);
+    a.ws.seg_R = (uint64_t *)(p + l.seg_R);
+    a.ws.seg_end = (uint64_t *)(p + l.seg_end);
+    a.ws.seg_ok = (uint32_t *)(p + l.seg_ok);
+    a.ws.win_base = (uint32_t *)(p + l.win_base);
+    a.ws.grp_base = (uint32_t *)(p + l.grp_base);
+    a.ws.wtab = (uint32_t *)(p + l.wtab);
+    a.ws.gtab = (uint64_t *)(p + l.gtab);
+    a.ws.gentry = (uint32_t *)(p + l.gentry);
+    a.ws.gbase = (uint64_t *)(p + l.gbase);
+    a.max_windows = l.max_windows;
+    a.max_groups = l.max_groups;
     int rc = cuda_status(launch_walk(a, st));
     if (rc == ZCCL_GPU_OK) {
         s->indexed = 1;
@@ -189,7 +236,7 @@ extern "C" int zccl_gpu_compress(zccl_gpu_stream *out, const float *d_in, size_t
     a.w = bind_ws(d_ws);
     a.wt = width_table();
     a.sm = zg_smem(g.L, g.TB);
-    if (cudaMemsetAsync(d_ws, 0, ws_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    if (cudaMemsetAsync(d_ws, 0, ws_clear_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
     int rc = cuda_status(launch_compress(a, st));
     if (rc == ZCCL_GPU_OK) {
         out->indexed = 1;
@@ -204,8 +251,8 @@ extern "C" int zccl_gpu_build_index(zccl_gpu_stream *s, size_t n, int L, int T, 
     ZGeom g;
     if (make_geom(n, L, T, &g) || !valid_stream(s) || !d_ws) return ZCCL_GPU_EINVAL;
     cudaStream_t st = (cudaStream_t)cuda_stream;
-    if (cudaMemsetAsync(d_ws, 0, ws_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
-    return walk_stream(s, g, bind_ws(d_ws), st);
+    if (cudaMemsetAsync(d_ws, 0, ws_clear_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    return walk_stream(s, g, d_ws, st);
 }
 
 extern "C" int zccl_gpu_decompress(float *d_out, zccl_gpu_stream *in, size_t n, float eb, int L,
@@ -214,10 +261,10 @@ extern "C" int zccl_gpu_decompress(float *d_out, zccl_gpu_stream *in, size_t n, 
     ZGeom g;
     if (make_geom(n, L, T, &g) || !valid_stream(in) || !d_out || !d_ws) return ZCCL_GPU_EINVAL;
     cudaStream_t st = (cudaStream_t)cuda_stream;
-    if (cudaMemsetAsync(d_ws, 0, ws_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    if (cudaMemsetAsync(d_ws, 0, ws_clear_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
     ZWork w = bind_ws(d_ws);
     if (!in->indexed) {
-        int rc = walk_stream(in, g, w, st);
+        int rc = walk_stream(in, g, d_ws, st);
         if (rc) return rc;
     }
     DecompressArgs a;
@@ -245,14 +292,14 @@ extern "C" int zccl_gpu_homadd_cases(zccl_gpu_stream *out, zccl_gpu_stream *ins,
     for (int p = 0; p < P; p++)
         if (!valid_stream(&ins[p]) || ins[p].bytes == out->bytes) return ZCCL_GPU_EINVAL;
     cudaStream_t st = (cudaStream_t)cuda_stream;
-    if (cudaMemsetAsync(d_ws, 0, ws_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    if (cudaMemsetAsync(d_ws, 0, ws_clear_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
     ZWork w = bind_ws(d_ws);
     HomAddArgs a;
     memset(&a, 0, sizeof(a));
     int qv = 1;
     for (int p = 0; p < P; p++) {
         if (!ins[p].indexed) {
-            int rc = walk_stream(&ins[p], g, w, st);
+            int rc = walk_stream(&ins[p], g, d_ws, st);
             if (rc) return rc;
         }
         ZIndex ix = bind_index(ins[p].index, g);
@@ -305,11 +352,12 @@ extern "C" int zccl_gpu_check(void *d_ws, void *cuda_stream)
 {
     if (!d_ws) return ZCCL_GPU_EINVAL;
     cudaStream_t st = (cudaStream_t)cuda_stream;
-    uint32_t bits = 0;
-    if (cudaMemcpyAsync(&bits, d_ws, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    uint32_t bits[2] = {0, 0};
+    if (cudaMemcpyAsync(bits, d_ws, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess)
         return ZCCL_GPU_ECUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return ZCCL_GPU_ECUDA;
-    return status_of_bits(bits);
+    /* a failed walk leaves nothing for the codec kernels to report */
+    return status_of_bits(bits[1] ? bits[1] : bits[0]);
 }
 
 extern "C" const char *zccl_gpu_strerror(int status)
@@ -427,10 +475,13 @@ void report(const char *fn, int rc)
     if (rc != ZCCL_GPU_OK) fprintf(stderr, "zccl_gpu: %s: %s\n", fn, zccl_gpu_strerror(rc));
 }
 
-/* Make a stream view of cmp: in place for device memory, else copied. */
+/* Make a stream view of cmp: in place for device memory, else copied.
+ * *capped reports whether a host copy stopped short of the largest size the
+ * stream could have. */
 int stage_stream(DropCtx *c, int slot, const unsigned char *cmp, const ZGeom &g,
-                 zccl_gpu_stream *s)
+                 zccl_gpu_stream *s, bool full, bool *capped)
 {
+    *capped = false;
     size_t ixb = index_layout(g).total;
     if (int rc = c->ix[slot].ensure(ixb)) return rc;
     s->index = c->ix[slot].p;
@@ -450,7 +501,8 @@ int stage_stream(DropCtx *c, int slot, const unsigned char *cmp, const ZGeom &g,
     size_t known = hdr + (size_t)last;
     size_t want = known + (size_t)(zg_seg_worst(g.tbs, g.L) + zg_seg_worst(g.rem, g.L));
     size_t room = 4 * (size_t)g.n > known + 4 ? 4 * (size_t)g.n : known + 4;
-    size_t bytes = want < room ? want : room;
+    size_t bytes = (full || want < room) ? want : room;
+    *capped = bytes < want;
     if (int rc = c->s[slot].ensure(bytes)) return rc;
     if (cudaMemcpyAsync(c->s[slot].p, cmp, bytes, cudaMemcpyHostToDevice, c->st) != cudaSuccess)
         return ZCCL_GPU_ECUDA;
@@ -511,16 +563,25 @@ int dropin_decompress(float *newData, size_t n, float eb, int L, const unsigned 
     if (!c) return ZCCL_GPU_ECUDA;
     std::lock_guard<std::mutex> lk(c->mu);
     if (int rc = c->ws.ensure(ws_bytes(g))) return rc;
-    zccl_gpu_stream s;
-    if (int rc = stage_stream(c, 0, cmp, g, &s)) return rc;
     const bool dout = is_device_ptr(newData);
     float *d_out = newData;
     if (!dout) {
         if (int rc = c->fout.ensure(4 * n)) return rc;
         d_out = (float *)c->fout.p;
     }
-    if (int rc = zccl_gpu_decompress(d_out, &s, n, eb, L, T, c->ws.p, c->st)) return rc;
-    if (int rc = finish(c, c->ws.p)) return rc;
+    /* A host stream is first read up to 4*nbEle bytes; only a stream that
+     * really runs past that (tiny arrays, near-32-bit widths) is read again
+     * up to its largest possible size. */
+    for (int pass = 0;; pass++) {
+        zccl_gpu_stream s;
+        bool capped;
+        if (int rc = stage_stream(c, 0, cmp, g, &s, pass > 0, &capped)) return rc;
+        if (int rc = zccl_gpu_decompress(d_out, &s, n, eb, L, T, c->ws.p, c->st)) return rc;
+        int rc = finish(c, c->ws.p);
+        if (rc == ZCCL_GPU_EBOUNDS && capped && pass == 0) continue;
+        if (rc) return rc;
+        break;
+    }
     if (!dout) {
         if (cudaMemcpyAsync(newData, d_out, 4 * n, cudaMemcpyDeviceToHost, c->st) != cudaSuccess)
             return ZCCL_GPU_ECUDA;
@@ -540,16 +601,22 @@ int dropin_homadd(unsigned char *final_cmp, size_t *final_size, size_t n, float 
     std::lock_guard<std::mutex> lk(c->mu);
     if (int rc = c->ws.ensure(ws_bytes(g))) return rc;
     zccl_gpu_stream in[2], out;
-    if (int rc = stage_stream(c, 0, cmp1, g, &in[0])) return rc;
-    if (int rc = stage_stream(c, 1, cmp2, g, &in[1])) return rc;
     const size_t worst = (size_t)zg_stream_worst(&g);
     if (int rc = c->s[2].ensure(worst)) return rc;
     if (int rc = c->ix[2].ensure(index_layout(g).total)) return rc;
     out.bytes = (unsigned char *)c->s[2].p;
     out.capacity = worst;
     out.index = c->ix[2].p;
-    if (int rc = zccl_gpu_homadd(&out, in, 2, n, L, T, c->ws.p, c->st)) return rc;
-    if (int rc = finish(c, c->ws.p)) return rc;
+    for (int pass = 0;; pass++) { /* second pass: see dropin_decompress */
+        bool cap1, cap2;
+        if (int rc = stage_stream(c, 0, cmp1, g, &in[0], pass > 0, &cap1)) return rc;
+        if (int rc = stage_stream(c, 1, cmp2, g, &in[1], pass > 0, &cap2)) return rc;
+        if (int rc = zccl_gpu_homadd(&out, in, 2, n, L, T, c->ws.p, c->st)) return rc;
+        int rc = finish(c, c->ws.p);
+        if (rc == ZCCL_GPU_EBOUNDS && (cap1 || cap2) && pass == 0) continue;
+        if (rc) return rc;
+        break;
+    }
     size_t size = 0;
     if (int rc = zccl_gpu_stream_size(&out, n, L, T, &size, c->st)) return rc;
     const bool dout = is_device_ptr(final_cmp);

@@ -36,6 +36,10 @@ __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, nw = blockDim.x >> 5;
     const uint32_t L = g.L, stride = zg_row_stride(L);
     uint32_t bad = 0;
+    /* The index walk ran to completion before this launch, so every CTA sees
+     * the same word: after a failed walk no CTA touches the stream and no
+     * CTA waits on another. */
+    if (*(volatile const uint32_t *)a.w.walk_err) return;
 
     if (tid == 0) {
         bcast[0] = a.qprev_valid ? (uint64_t)blockIdx.x : (uint64_t)atomicAdd(a.w.ticket, 1u);

@@ -3,63 +3,37 @@
  * (written by the reference, or by any writer that did not keep the index).
  *
  * The wire format has no block index: inside a chunk, block k starts where
- * block k-1 ends, and only the 1-byte width header says how long a block is
- * (ZCCL/src/ZCCLd_float.c:598-614).  The chunk starts come from the T-entry
- * header.  This builder follows each chunk's headers from its start (one
- * thread per chunk), records every width, the byte offset of every tile and
- * the stream's total size, and checks the walk against the geometry: widths
- * must be <= 32, every chunk must end exactly where the next one starts, and
- * no block may pass the readable bytes.
+ * block k-1 ends, and only its 1-byte width header says how long it is
+ * (ZCCL/src/ZCCLd_float.c:598-614).  Walking the headers is a chain of
+ * dependent loads as long as the chunk, so it is split into windows of WW
+ * bytes and done in parallel, exactly:
+ *
+ *   W0  chunk starts from the T-entry header; per segment its block region
+ *       and window count; heads' tile offsets.
+ *   W1  for every window and every possible entry offset e in [0, M) (M = the
+ *       largest block) follow the headers to the window end: the exit offset
+ *       into the next window and the blocks passed.  Walks that land on a
+ *       position another walk already claimed stop there and inherit its
+ *       result, so a window costs about one walk plus M short ones, also
+ *       when every block has the same size.
+ *   W2  compose the tables: per group of G windows (parallel), then per
+ *       segment across groups, giving each group its true entry offset and
+ *       first block number.
+ *   W3  per window, from its true entry, record every block's width and the
+ *       offset of every tile, and check each chunk ends where the next starts.
+ *   W4  the extra segment of the last chunk (N % T elements) and the total
+ *       size.
+ * Widths above 32, chunk ends that disagree with the header, and blocks past
+ * the readable bytes set ZERR_CORRUPT / ZERR_BOUNDS instead of faulting.
  */
 #include "zkern.cuh"
 
 namespace {
 
-/* Walk one segment starting at byte `pos` (its head); returns the byte just
- * past its last block, or UINT64_MAX after an error. */
-__device__ uint64_t walk_segment(const WalkArgs &a, uint32_t seg, uint64_t pos)
-{
-    const ZGeom &g = a.g;
-    uint64_t len, nb, gblk, tile0;
-    if (seg < g.T) {
-        len = g.tbs;
-        nb = g.nb_reg;
-        gblk = (uint64_t)seg * g.nb_reg;
-        tile0 = (uint64_t)seg * g.nt_reg;
-    } else {
-        len = g.rem;
-        nb = g.nb_rm;
-        gblk = (uint64_t)g.T * g.nb_reg;
-        tile0 = (uint64_t)g.T * g.nt_reg;
-    }
-    if (pos + 4 > a.avail) {
-        atomicOr(a.err, ZERR_BOUNDS);
-        return UINT64_MAX;
-    }
-    a.idx.tile_off[tile0] = pos;
-    pos += 4;
-    for (uint64_t j = 0; j < nb; j++) {
-        if (j && j % g.TB == 0) a.idx.tile_off[tile0 + j / g.TB] = pos;
-        if (pos >= a.avail) {
-            atomicOr(a.err, ZERR_BOUNDS);
-            return UINT64_MAX;
-        }
-        uint32_t b = a.in[pos];
-        if (b > 32) {
-            atomicOr(a.err, ZERR_CORRUPT);
-            return UINT64_MAX;
-        }
-        a.idx.widths[gblk + j] = (uint8_t)b;
-        pos += zg_block_bytes(b, zg_block_len(len, g.L, j));
-    }
-    if (pos > a.avail) {
-        atomicOr(a.err, ZERR_BOUNDS);
-        return UINT64_MAX;
-    }
-    return pos;
-}
+constexpr uint32_t WARPS_W1 = 2;
+constexpr uint32_t NONE = 0xFFFFFFFFu;
 
-__device__ uint64_t load_u64(const uint8_t *p)
+__device__ __forceinline__ uint64_t load_u64(const uint8_t *p)
 {
     uint64_t v = 0;
 #pragma unroll
@@ -67,38 +41,409 @@ __device__ uint64_t load_u64(const uint8_t *p)
     return v;
 }
 
-__global__ void k_walk(const WalkArgs a)
+/* Size of a full block whose header byte is b; bytes that cannot be a
+ * header (b > 32) count as 1 so speculative walks stay bounded. */
+__device__ __forceinline__ uint32_t full_size(uint32_t b, uint32_t L)
+{
+    return b <= 32 ? zg_block_bytes(b, L) : 1u;
+}
+
+/* Segment of a window / group index: last s with base[s] <= i. */
+__device__ __forceinline__ uint32_t find_seg(const uint32_t *base, uint32_t T, uint32_t i)
+{
+    uint32_t lo = 0, hi = T; /* base[lo] <= i < base[hi] */
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (base[mid] <= i)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+/* ---- W0 -------------------------------------------------------------- */
+__global__ void k_walk_setup(const WalkArgs a)
 {
     const ZGeom &g = a.g;
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= g.T) return;
+    const WalkScratch &w = a.ws;
     const uint64_t hdr = 8ull * g.T;
-    if (hdr > a.avail) {
-        atomicOr(a.err, ZERR_BOUNDS);
-        return;
+    __shared__ uint32_t wsum[33];
+    uint32_t carry_w = 0, carry_g = 0;
+    for (uint32_t s0 = 0; s0 < g.T; s0 += blockDim.x) {
+        const uint32_t s = s0 + threadIdx.x;
+        uint32_t nwin = 0;
+        if (s < g.T) {
+            uint64_t P = 0, R = 0;
+            bool ok = hdr <= a.avail;
+            if (!ok) atomicOr(a.err, ZERR_BOUNDS);
+            if (ok) {
+                uint64_t rel = load_u64(a.in + 8ull * s);
+                if (s == 0 && rel != 0) atomicOr(a.err, ZERR_CORRUPT);
+                if (rel > a.avail - hdr || hdr + rel + 4 > a.avail) {
+                    atomicOr(a.err, ZERR_BOUNDS);
+                    ok = false;
+                } else {
+                    a.idx.tile_off[(uint64_t)s * g.nt_reg] = hdr + rel;
+                    P = hdr + rel + 4;
+                    if (s + 1 < g.T) {
+                        uint64_t rn = load_u64(a.in + 8ull * (s + 1));
+                        R = hdr + rn;
+                        /* chunk starts increase and a stream never exceeds end_bound,
+                         * which keeps the window count within the scratch */
+                        if (rn > a.avail - hdr || R < P || R > a.end_bound) {
+                            atomicOr(a.err, ZERR_CORRUPT);
+                            ok = false;
+                        }
+                    } else {
+                        R = a.avail < a.end_bound ? a.avail : a.end_bound;
+                        if (R < P) R = P;
+                    }
+                }
+            }
+            if (ok && g.nb_reg > 0) nwin = (uint32_t)zg_div_up(R - P, WALK_WW);
+            if (ok && g.nb_reg > 0 && nwin == 0) {
+                atomicOr(a.err, ZERR_BOUNDS);
+                ok = false;
+            }
+            w.seg_P[s] = P;
+            w.seg_R[s] = R;
+            w.seg_end[s] = (ok && g.nb_reg == 0) ? P : 0;
+            w.seg_ok[s] = ok ? 1u : 0u;
+            if (ok && g.nb_reg == 0 && s + 1 < g.T && P != R) atomicOr(a.err, ZERR_CORRUPT);
+        }
+        uint32_t tot_w, tot_g;
+        uint32_t bw = cta_excl_scan(nwin, wsum, &tot_w);
+        uint32_t bg = cta_excl_scan((nwin + WALK_G - 1) / WALK_G, wsum, &tot_g);
+        if (s < g.T) {
+            w.win_base[s] = carry_w + bw;
+            w.grp_base[s] = carry_g + bg;
+        }
+        carry_w += tot_w;
+        carry_g += tot_g;
     }
-    const uint64_t rel = load_u64(a.in + 8ull * s);
-    if (s == 0 && rel != 0) atomicOr(a.err, ZERR_CORRUPT); /* header[0] is always 0 */
-    if (rel > a.avail - hdr) {
-        atomicOr(a.err, ZERR_BOUNDS);
-        return;
+    if (threadIdx.x == 0) {
+        w.win_base[g.T] = carry_w;
+        w.grp_base[g.T] = carry_g;
     }
-    uint64_t pos = hdr + rel;
-    uint64_t end = walk_segment(a, s, pos);
-    if (end == UINT64_MAX) return;
-    if (s + 1 < g.T) {
-        if (end != hdr + load_u64(a.in + 8ull * (s + 1))) atomicOr(a.err, ZERR_CORRUPT);
-    } else {
-        if (g.rem) end = walk_segment(a, g.T, end);
-        if (end != UINT64_MAX) *a.idx.size = end;
+}
+
+/* ---- W1 -------------------------------------------------------------- */
+__global__ void __launch_bounds__(32 * WARPS_W1) k_walk_tables(const WalkArgs a)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    const ZGeom &g = a.g;
+    const WalkScratch &w = a.ws;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t M = a.M;
+    const uint32_t wg = blockIdx.x * WARPS_W1 + warp;
+    if (wg >= w.win_base[g.T]) return;
+    const uint32_t s = find_seg(w.win_base, g.T, wg);
+    const uint64_t start = w.seg_P[s] + (uint64_t)(wg - w.win_base[s]) * WALK_WW;
+
+    /* per-warp shared area: bytes[WW + M + 16] | own[WW] | ex, cnt, par, at, ordp [M] */
+    uint8_t *base = smem + warp * a.w1_warp_bytes;
+    uint8_t *bytes = base;
+    uint32_t *own = reinterpret_cast<uint32_t *>(base + ((WALK_WW + M + 16 + 15) & ~15u));
+    uint32_t *ex = own + WALK_WW;
+    uint32_t *cnt = ex + M;
+    int32_t *par = reinterpret_cast<int32_t *>(cnt + M);
+    uint32_t *at = reinterpret_cast<uint32_t *>(par + M);
+    uint32_t *ordp = at + M;
+
+    for (uint32_t i = lane; i < WALK_WW + M; i += 32) {
+        uint64_t p = start + i;
+        bytes[i] = p < a.avail ? a.in[p] : 0;
     }
+    for (uint32_t i = lane; i < WALK_WW; i += 32) own[i] = NONE;
+    __syncwarp();
+
+    for (uint32_t e0 = 0; e0 < M; e0 += 32) {
+        const uint32_t e = e0 + lane;
+        bool active = e < M;
+        uint32_t pos = e, k = 0;
+        for (uint32_t it = 0; it < WALK_WW + M + 2; it++) {
+            if (!__any_sync(0xffffffffu, active)) break;
+            if (active) {
+                if (pos >= WALK_WW) {
+                    ex[e] = pos - WALK_WW;
+                    cnt[e] = k;
+                    par[e] = -1;
+                    active = false;
+                } else {
+                    uint32_t o = own[pos];
+                    if (o != NONE) {
+                        par[e] = (int32_t)(o >> 16);
+                        at[e] = k;
+                        ordp[e] = o & 0xFFFFu;
+                        active = false;
+                    } else {
+                        own[pos] = (e << 16) | k;
+                    }
+                }
+            }
+            __syncwarp();
+            if (active) {
+                uint32_t o = own[pos];
+                if ((o >> 16) != e) { /* another walk claimed the same byte this step */
+                    par[e] = (int32_t)(o >> 16);
+                    at[e] = k;
+                    ordp[e] = o & 0xFFFFu;
+                    active = false;
+                } else {
+                    pos += full_size(bytes[pos], g.L);
+                    k++;
+                }
+            }
+            __syncwarp();
+        }
+    }
+    /* a walk that merged into walk o at o's step ordp: exit(o), at + cnt(o) - ordp.
+     * Parents claimed their byte first, so resolving repeatedly terminates. */
+    for (uint32_t round = 0; round < M + 1; round++) {
+        bool pending = false;
+        for (uint32_t e = lane; e < M; e += 32) {
+            int32_t p = par[e];
+            if (p >= 0) {
+                if (par[p] < 0) {
+                    ex[e] = ex[p];
+                    cnt[e] = at[e] + cnt[p] - ordp[e];
+                    par[e] = -1;
+                } else {
+                    pending = true;
+                }
+            }
+        }
+        __syncwarp();
+        if (!__any_sync(0xffffffffu, pending)) break;
+    }
+    uint32_t *tab = a.ws.wtab + (uint64_t)wg * M;
+    for (uint32_t e = lane; e < M; e += 32) tab[e] = (ex[e] << 16) | cnt[e];
+}
+
+/* ---- W2a: compose the window tables of each group ---------------------- */
+__global__ void k_walk_groups(const WalkArgs a)
+{
+    const ZGeom &g = a.g;
+    const WalkScratch &w = a.ws;
+    const uint32_t gg = blockIdx.x;
+    if (gg >= w.grp_base[g.T]) return;
+    const uint32_t s = find_seg(w.grp_base, g.T, gg);
+    const uint32_t nwin = w.win_base[s + 1] - w.win_base[s];
+    const uint32_t w0 = (gg - w.grp_base[s]) * WALK_G;
+    const uint32_t w1 = min(w0 + WALK_G, nwin);
+    for (uint32_t e = threadIdx.x; e < a.M; e += blockDim.x) {
+        uint32_t x = e;
+        uint64_t c = 0;
+        for (uint32_t k = w0; k < w1; k++) {
+            uint32_t t = __ldg(w.wtab + (uint64_t)(w.win_base[s] + k) * a.M + x);
+            c += t & 0xFFFFu;
+            x = t >> 16;
+        }
+        w.gtab[(uint64_t)gg * a.M + e] = (c << 32) | x;
+    }
+}
+
+/* ---- W2b: per segment, carry the entry offset across its groups -------- */
+__global__ void k_walk_segments(const WalkArgs a)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint64_t *rows = reinterpret_cast<uint64_t *>(smem);
+    __shared__ uint64_t s_base;
+    __shared__ uint32_t s_x;
+    const ZGeom &g = a.g;
+    const WalkScratch &w = a.ws;
+    const uint32_t s = blockIdx.x;
+    if (!w.seg_ok[s]) return;
+    const uint32_t g0 = w.grp_base[s], g1 = w.grp_base[s + 1];
+    uint32_t x = 0;
+    uint64_t base = 0;
+    for (uint32_t b0 = g0; b0 < g1; b0 += a.seg_batch) {
+        const uint32_t nb = min(a.seg_batch, g1 - b0);
+        if (base < g.nb_reg) /* groups past the last block need no table */
+            for (uint32_t i = threadIdx.x; i < nb * a.M; i += blockDim.x)
+                rows[i] = w.gtab[(uint64_t)b0 * a.M + i];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (uint32_t j = 0; j < nb; j++) {
+                w.gentry[b0 + j] = x;
+                w.gbase[b0 + j] = base;
+                if (base < g.nb_reg) {
+                    uint64_t t = rows[j * a.M + x];
+                    base += t >> 32;
+                    x = (uint32_t)t;
+                }
+            }
+            s_base = base;
+            s_x = x;
+        }
+        __syncthreads();
+        base = s_base;
+        x = s_x;
+    }
+}
+
+/* ---- W3: the true walk of every window ------------------------------- */
+__global__ void __launch_bounds__(128) k_walk_final(const WalkArgs a)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    const ZGeom &g = a.g;
+    const WalkScratch &w = a.ws;
+    const uint32_t gg = blockIdx.x;
+    if (gg >= w.grp_base[g.T]) return;
+    const uint32_t s = find_seg(w.grp_base, g.T, gg);
+    if (!w.seg_ok[s]) return;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const uint32_t nwin = w.win_base[s + 1] - w.win_base[s];
+    const uint32_t w0 = (gg - w.grp_base[s]) * WALK_G;
+    const uint32_t w1 = min(w0 + WALK_G, nwin);
+    uint32_t *entry = reinterpret_cast<uint32_t *>(smem);
+    uint64_t *bbase = reinterpret_cast<uint64_t *>(smem + 4 * WALK_G);
+    uint8_t *wbuf = smem + 12 * WALK_G;
+    const uint32_t wstride = (WALK_WW + a.M + 16 + 15) & ~15u;
+
+    const uint64_t nb = g.nb_reg;
+    const uint64_t nfull = (g.tbs - 1) / g.L;
+    const uint32_t ntail = (uint32_t)((g.tbs - 1) % g.L);
+    const uint64_t gblk0 = (uint64_t)s * g.nb_reg, tile0 = (uint64_t)s * g.nt_reg;
+
+    if (threadIdx.x == 0) {
+        uint32_t x = w.gentry[gg];
+        uint64_t b = w.gbase[gg];
+        for (uint32_t k = w0; k < w1; k++) {
+            entry[k - w0] = x;
+            bbase[k - w0] = b;
+            if (b >= nb) continue;
+            uint32_t t = w.wtab[(uint64_t)(w.win_base[s] + k) * a.M + x];
+            b += t & 0xFFFFu;
+            x = t >> 16;
+        }
+    }
+    __syncthreads();
+    for (uint32_t k = w0 + warp; k < w1; k += nw) {
+        const uint64_t b0 = bbase[k - w0];
+        if (b0 >= nb) continue;
+        const uint64_t start = w.seg_P[s] + (uint64_t)k * WALK_WW;
+        uint8_t *buf = wbuf + warp * wstride;
+        for (uint32_t i = lane; i < WALK_WW + a.M; i += 32) {
+            uint64_t p = start + i;
+            buf[i] = p < a.avail ? a.in[p] : 0;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            uint32_t pos = entry[k - w0];
+            uint64_t blk = b0;
+            while (pos < WALK_WW && blk < nb) {
+                const uint64_t gpos = start + pos;
+                if (gpos >= a.avail) {
+                    atomicOr(a.err, ZERR_BOUNDS);
+                    break;
+                }
+                const uint32_t b = buf[pos];
+                if (b > 32) {
+                    atomicOr(a.err, ZERR_CORRUPT);
+                    break;
+                }
+                if (blk % g.TB == 0 && blk) a.idx.tile_off[tile0 + blk / g.TB] = gpos;
+                a.idx.widths[gblk0 + blk] = (uint8_t)b;
+                const uint32_t n = blk < nfull ? g.L : ntail;
+                pos += zg_block_bytes(b, n);
+                blk++;
+                if (blk == nb) {
+                    const uint64_t end = start + pos;
+                    if (end > a.avail) atomicOr(a.err, ZERR_BOUNDS);
+                    w.seg_end[s] = end;
+                    if (s + 1 < g.T && end != w.seg_R[s]) atomicOr(a.err, ZERR_CORRUPT);
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+/* ---- W4: extra segment and total size -------------------------------- */
+__global__ void k_walk_finish(const WalkArgs a)
+{
+    const ZGeom &g = a.g;
+    const WalkScratch &w = a.ws;
+    if (threadIdx.x != 0) return;
+    for (uint32_t s = 0; s < g.T; s++) {
+        if (!w.seg_ok[s]) return; /* W0 already reported why */
+        if (w.seg_end[s] == 0) {  /* the walk never reached this segment's last block */
+            atomicOr(a.err, ZERR_CORRUPT);
+            return;
+        }
+    }
+    uint64_t pos = w.seg_end[g.T - 1];
+    if (g.rem) {
+        const uint64_t tile0 = (uint64_t)g.T * g.nt_reg, gblk0 = (uint64_t)g.T * g.nb_reg;
+        if (pos + 4 > a.avail) {
+            atomicOr(a.err, ZERR_BOUNDS);
+            return;
+        }
+        a.idx.tile_off[tile0] = pos;
+        pos += 4;
+        for (uint64_t j = 0; j < g.nb_rm; j++) {
+            if (j && j % g.TB == 0) a.idx.tile_off[tile0 + j / g.TB] = pos;
+            if (pos >= a.avail) {
+                atomicOr(a.err, ZERR_BOUNDS);
+                return;
+            }
+            uint32_t b = a.in[pos];
+            if (b > 32) {
+                atomicOr(a.err, ZERR_CORRUPT);
+                return;
+            }
+            a.idx.widths[gblk0 + j] = (uint8_t)b;
+            pos += zg_block_bytes(b, zg_block_len(g.rem, g.L, j));
+        }
+        if (pos > a.avail) {
+            atomicOr(a.err, ZERR_BOUNDS);
+            return;
+        }
+    }
+    *a.idx.size = pos;
 }
 
 } // namespace
 
-cudaError_t launch_walk(const WalkArgs &a, cudaStream_t st)
+size_t walk_w1_warp_bytes(uint32_t M)
 {
-    const unsigned threads = 64;
-    k_walk<<<(a.g.T + threads - 1) / threads, threads, 0, st>>>(a);
+    return ((WALK_WW + M + 16 + 15) & ~15u) + 4u * WALK_WW + 20u * M + 16;
+}
+
+cudaError_t launch_walk(const WalkArgs &a0, cudaStream_t st)
+{
+    WalkArgs a = a0;
+    a.M = zg_block_bytes(32, a.g.L);
+    a.w1_warp_bytes = (uint32_t)walk_w1_warp_bytes(a.M);
+    cudaError_t e;
+    k_walk_setup<<<1, 256, 0, st>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const uint32_t smem1 = WARPS_W1 * a.w1_warp_bytes;
+    if ((e = cudaFuncSetAttribute(k_walk_tables, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  smem1)) != cudaSuccess)
+        return e;
+    k_walk_tables<<<(a.max_windows + WARPS_W1 - 1) / WARPS_W1, 32 * WARPS_W1, smem1, st>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_walk_groups<<<a.max_groups, 128, 0, st>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    a.seg_batch = (160u * 1024u) / (8u * a.M);
+    if (a.seg_batch > WALK_G) a.seg_batch = WALK_G;
+    if (a.seg_batch < 1) a.seg_batch = 1;
+    const uint32_t smem2 = a.seg_batch * a.M * 8u;
+    if ((e = cudaFuncSetAttribute(k_walk_segments, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  smem2)) != cudaSuccess)
+        return e;
+    k_walk_segments<<<a.g.T, 256, smem2, st>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const uint32_t wstride = (WALK_WW + a.M + 16 + 15) & ~15u;
+    const uint32_t smem3 = 12 * WALK_G + 4 * wstride;
+    if ((e = cudaFuncSetAttribute(k_walk_final, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  smem3)) != cudaSuccess)
+        return e;
+    k_walk_final<<<a.max_groups, 128, smem3, st>>>(a);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_walk_finish<<<1, 32, 0, st>>>(a);
     return cudaGetLastError();
 }

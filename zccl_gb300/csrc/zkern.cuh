@@ -13,12 +13,13 @@
 
 #define ZH_MAXP 32 /* most inputs one homomorphic-add launch accepts */
 
-/* Per-call scratch in device memory, zeroed before every launch:
- * err | ticket | pad | status[ntiles]. */
+/* Per-call scratch in device memory, zeroed before every call:
+ * err | walk_err | ticket | pad | status[ntiles]. */
 struct ZWork {
-    uint32_t *err;    /* ZERR_* bits */
-    uint32_t *ticket; /* next tile to hand out */
-    uint64_t *status; /* decoupled look-back state, one word per tile */
+    uint32_t *err;      /* ZERR_* bits of the codec kernels */
+    uint32_t *walk_err; /* ZERR_* bits of the index walk that ran before, if any */
+    uint32_t *ticket;   /* next tile to hand out */
+    uint64_t *status;   /* decoupled look-back state, one word per tile */
 };
 
 /* Side index of a resident stream: enough to find every block without
@@ -77,13 +78,39 @@ struct HomAddArgs {
     ZSmem sm;
 };
 
+#define WALK_WW 4096u /* bytes per window of the parallel header walk */
+#define WALK_G 32u     /* windows per group */
+
+/* Device scratch of the header walk (part of the workspace). */
+struct WalkScratch {
+    uint64_t *seg_P;    /* [T]   first block byte of each regular segment */
+    uint64_t *seg_R;    /* [T]   end of its byte region (next chunk start, or a bound) */
+    uint64_t *seg_end;  /* [T]   byte after its last block, found by the walk */
+    uint32_t *seg_ok;   /* [T]   header entries usable */
+    uint32_t *win_base; /* [T+1] first window of each segment (prefix sum) */
+    uint32_t *grp_base; /* [T+1] first window group of each segment */
+    uint32_t *wtab;     /* [max_windows * M] exit offset << 16 | blocks, per entry offset */
+    uint64_t *gtab;     /* [max_groups * M]  blocks << 32 | exit offset, per group */
+    uint32_t *gentry;   /* [max_groups] true entry offset of each group */
+    uint64_t *gbase;    /* [max_groups] first block (in its segment) of each group */
+};
+
 struct WalkArgs {
     const uint8_t *in;
-    uint64_t avail;
+    uint64_t avail;     /* readable bytes at `in` */
+    uint64_t end_bound; /* no stream of this geometry is longer */
     ZGeom g;
     ZIndex idx;
     uint32_t *err;
+    WalkScratch ws;
+    uint32_t max_windows, max_groups;
+    uint32_t M;             /* largest full block in bytes (filled by launch_walk) */
+    uint32_t w1_warp_bytes; /* filled by launch_walk */
+    uint32_t seg_batch;     /* group tables staged per step of W2b (filled by launch_walk) */
 };
+
+/* Shared bytes per warp of the window-table kernel. */
+size_t walk_w1_warp_bytes(uint32_t M);
 
 /* Launchers; each returns the cudaError_t of the launch. */
 cudaError_t launch_compress(const CompressArgs &a, cudaStream_t st);
