@@ -235,7 +235,7 @@ extern "C" int zccl_gpu_compress(zccl_gpu_stream *out, const float *d_in, size_t
     a.idx = bind_index(out->index, g);
     a.w = bind_ws(d_ws);
     a.wt = width_table();
-    a.sm = zg_smem(g.L, g.TB);
+    a.sm = zg_smem(0, g.L, g.TB);
     if (cudaMemsetAsync(d_ws, 0, ws_clear_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
     int rc = cuda_status(launch_compress(a, st));
     if (rc == ZCCL_GPU_OK) {
@@ -276,7 +276,7 @@ extern "C" int zccl_gpu_decompress(float *d_out, zccl_gpu_stream *in, size_t n, 
     a.idx = bind_index(in->index, g);
     a.qprev_valid = in->qprev_valid;
     a.w = w;
-    a.sm = zg_smem(g.L, g.TB);
+    a.sm = zg_smem(1, g.L, g.TB);
     int rc = cuda_status(launch_decompress(a, st));
     if (rc == ZCCL_GPU_OK) in->qprev_valid = 1;
     return rc;
@@ -319,7 +319,7 @@ extern "C" int zccl_gpu_homadd_cases(zccl_gpu_stream *out, zccl_gpu_stream *ins,
     a.g = g;
     a.w = w;
     a.wt = width_table();
-    a.sm = zg_smem(g.L, g.TB);
+    a.sm = zg_smem(2, g.L, g.TB);
     int rc = cuda_status(launch_homadd(a, st));
     if (rc == ZCCL_GPU_OK) {
         out->indexed = 1;

@@ -150,27 +150,36 @@ ZG_HD uint64_t zg_stream_worst(const ZGeom *g)
     return 8ull * g->T + (uint64_t)g->T * zg_seg_worst(g->tbs, g->L) + zg_seg_worst(g->rem, g->L);
 }
 
-/* Shared-memory layout of the codec kernels (bytes):
- *   [0, 256)            mbarrier, scan scratch, broadcast slots
- *   [256, stage)        per-block rows, TB x row_stride 4-byte words
- *   [stage, total)      staging for TMA copies (raw input floats, tile
- *                       bytes in or out), 16-byte aligned, with slack */
+/* Shared-memory layout of the codec kernels (bytes), all regions 16-byte
+ * aligned:
+ *   [0, 256)   mbarriers, scan scratch, broadcast slots
+ *   rows       per-block rows, TB x row_stride 4-byte words (floats or ints)
+ *   in0, in1   double-buffered TMA input (raw floats or tile bytes)
+ *   out        packed output tile (compressor, homomorphic add) */
 typedef struct ZSmem {
-    uint32_t rows;  /* offset of the row area */
-    uint32_t stage; /* offset of the staging area */
-    uint32_t total; /* bytes of dynamic shared memory */
+    uint32_t rows, in0, in1, out, total;
 } ZSmem;
 
-ZG_HD ZSmem zg_smem(uint32_t L, uint32_t TB)
+ZG_HD uint32_t zg_a16(uint32_t v) { return (v + 15u) & ~15u; }
+
+/* Largest tile in bytes: head + TB blocks at width 32. */
+ZG_HD uint32_t zg_tile_worst(uint32_t L, uint32_t TB) { return TB * zg_block_bytes(32, L) + 4u; }
+
+/* kind: 0 compressor, 1 decompressor, 2 homomorphic add */
+ZG_HD ZSmem zg_smem(uint32_t kind, uint32_t L, uint32_t TB)
 {
     ZSmem m;
-    uint32_t rows_bytes = TB * zg_row_stride(L) * 4u;
-    uint32_t xin = (TB * L + 1u) * 4u + 16u;
-    uint32_t tile = TB * zg_block_bytes(32, L) + 4u + 16u;
-    uint32_t st = xin > tile ? xin : tile;
+    const uint32_t rows_bytes = TB * zg_row_stride(L) * 4u;
+    const uint32_t raw_in = (TB * L + 1u) * 4u + 32u;     /* floats, 16-byte superset */
+    const uint32_t tile_in = zg_tile_worst(L, TB) + 48u;  /* bytes, superset + reader slack */
+    const uint32_t tile_out = zg_tile_worst(L, TB) + 48u; /* realigning store reads 32 past */
+    const uint32_t in = kind == 0 ? raw_in : tile_in;
+    const int need_rows = kind != 2 || L > 32;
     m.rows = 256u;
-    m.stage = (m.rows + rows_bytes + 15u) & ~15u;
-    m.total = m.stage + ((st + 15u) & ~15u) + 64u;
+    m.in0 = zg_a16(m.rows + (need_rows ? rows_bytes : 0u));
+    m.in1 = zg_a16(m.in0 + in);
+    m.out = zg_a16(m.in1 + in);
+    m.total = zg_a16(m.out + (kind == 1 ? 0u : tile_out));
     return m;
 }
 

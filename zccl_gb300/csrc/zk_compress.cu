@@ -2,37 +2,56 @@
  * zk_compress.cu -- fused single-pass compressor.
  *
  * Replaces ZCCL_float_openmp_threadblock_arg (ZCCL/src/ZCCL_float.c:501-807)
- * and produces the same bytes.  One CTA per tile of TB blocks, one thread per
- * block:
- *   1. TMA bulk copy of the tile's floats (plus the element before it) into
- *      shared memory, then a warp-cooperative transpose into padded rows so
- *      each thread walks its own block without bank conflicts;
+ * and produces the same bytes.  Persistent CTAs take tiles of TB blocks in
+ * ticket order; one thread owns one block.  Per tile:
+ *   1. its floats (and the element before them) arrived by a TMA bulk copy
+ *      issued while the previous tile was being coded (double buffering);
+ *      a warp-cooperative transpose puts every block in its own padded row,
+ *      so the per-thread walk below has no bank conflicts;
  *   2. every thread quantizes its block (truncation, ZCCL_float.c:580),
  *      forms the running deltas (ZCCL_float.c:581-582; the element before the
- *      block supplies the first one), its sign mask, maximum magnitude, width
+ *      block supplies the first one), sign mask, largest magnitude, width
  *      (ZCCL_float.c:606) and encoded size;
- *   3. block-wide exclusive scan of the sizes, then a decoupled look-back
- *      across tiles places the tile in the output in the same pass (the
- *      reference's per-thread scan and second memcpy pass,
- *      ZCCL_float.c:774-791, disappear);
- *   4. every thread packs its block into a shared staging copy of the output
- *      that keeps the global 16-byte phase, and one TMA bulk store writes it.
- * The tile also records the side index: block widths, the tile's byte
- * offset and the quantized value before it.
+ *   3. a block-wide scan gives each block its offset in the tile; the tile's
+ *      size is published for the decoupled look-back at once, the blocks are
+ *      packed into shared memory, and only then is the tile's place in the
+ *      stream resolved (the reference's per-thread scan and second memcpy
+ *      pass, ZCCL_float.c:774-791, disappear);
+ *   4. the packed tile goes out with 16-byte vector stores realigned to its
+ *      byte offset, and the tile records the side index: block widths, its
+ *      byte offset, and the quantized value before it.
  */
 #include "zkern.cuh"
 
 namespace {
 
+/* Thread 0: claim the next tile and start its input copy. */
+__device__ __forceinline__ uint64_t claim_and_load(const CompressArgs &a, uint8_t *buf,
+                                                   uint64_t *bar)
+{
+    uint64_t t = atomicAdd(a.w.ticket, 1u);
+    if (t < a.g.ntiles) {
+        ZTile z;
+        zg_tile(&a.g, t, &z);
+        const uint32_t nel = (uint32_t)(z.e_end - z.e_first + 1);
+        tma_load_superset(buf, reinterpret_cast<const uint8_t *>(a.x + (z.e_first - 1)), nel * 4u,
+                          bar);
+    }
+    return t;
+}
+
 template <bool FAST>
 __global__ void __launch_bounds__(128) k_compress(const CompressArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem); /* [2] */
     uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 16);
-    uint64_t *bcast = reinterpret_cast<uint64_t *>(smem + 160);
+    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160); /* [0..1] tiles, [2] prefix */
+    uint32_t *s_amax = reinterpret_cast<uint32_t *>(smem + 192);
     float *rows = reinterpret_cast<float *>(smem + a.sm.rows);
-    uint8_t *stage = smem + a.sm.stage;
+    uint8_t *inb[2] = {smem + a.sm.in0, smem + a.sm.in1};
+    uint8_t *outs = smem + a.sm.out;
+    uint32_t *outw = reinterpret_cast<uint32_t *>(outs);
 
     const ZGeom &g = a.g;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, nw = blockDim.x >> 5;
@@ -40,148 +59,165 @@ __global__ void __launch_bounds__(128) k_compress(const CompressArgs a)
     uint32_t bad = 0;
 
     if (tid == 0) {
-        bcast[0] = atomicAdd(a.w.ticket, 1u);
-        mbar_init(bar, 1);
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        bc[0] = claim_and_load(a, inb[0], &bar[0]);
+        *s_amax = 0;
     }
     __syncthreads();
-    const uint64_t tile = bcast[0];
-    ZTile z;
-    zg_tile(&g, tile, &z);
 
-    /* 1. stage x[e_first - 1, e_end) and transpose into rows */
-    const uint32_t nel = (uint32_t)(z.e_end - z.e_first + 1);
-    const uint32_t ph =
-        stage_in(stage, reinterpret_cast<const uint8_t *>(a.x + (z.e_first - 1)), nel * 4u, bar);
-    stage_in_wait(bar, 0, a.w.err);
-    const float *xin = reinterpret_cast<const float *>(stage + ph);
-    for (uint32_t k = warp; k < z.nblk; k += nw) {
-        uint32_t n = zg_block_len(z.seg_len, L, z.blk0 + k);
-        for (uint32_t j = lane; j < n; j += 32) rows[k * stride + j] = xin[1 + k * L + j];
-    }
-    const float xprev0 = xin[0]; /* head for tile 0 of a segment, else last element of the previous tile */
-    __syncthreads();
+    for (uint32_t it = 0;; it++) {
+        const uint32_t cb = it & 1u;
+        const uint64_t tile = bc[cb];
+        if (tile >= g.ntiles) break;
+        if (tid == 0) bc[cb ^ 1u] = claim_and_load(a, inb[cb ^ 1u], &bar[cb ^ 1u]);
+        ZTile z;
+        zg_tile(&g, tile, &z);
 
-    /* 2. per-block quantize / delta / width */
-    uint32_t b = 0, size = 0, n = 0, smask = 0, mx = 0;
-    uint32_t m[FAST ? 32 : 1];
-    float xp = 0.0f;
-    if (tid < z.nblk) {
-        n = zg_block_len(z.seg_len, L, z.blk0 + tid);
-        const float *row = rows + tid * stride;
-        xp = tid == 0 ? xprev0 : rows[(tid - 1) * stride + L - 1];
-        int32_t qp = quantize(xp, a.inv, bad);
-        if (FAST) {
-#pragma unroll
-            for (uint32_t j = 0; j < 32; j++) {
-                uint32_t mg = 0;
-                if (j < n) {
-                    int32_t q = quantize(row[j], a.inv, bad);
-                    int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
-                    qp = q;
-                    uint32_t neg = d < 0 ? 1u : 0u;
-                    mg = neg ? 0u - (uint32_t)d : (uint32_t)d;
-                    smask |= neg << (31 - j);
-                    mx = mx > mg ? mx : mg;
-                }
-                m[j] = mg;
-            }
-        } else {
-            for (uint32_t j = 0; j < n; j++) {
-                int32_t q = quantize(row[j], a.inv, bad);
-                int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
-                qp = q;
-                uint32_t mg = d < 0 ? 0u - (uint32_t)d : (uint32_t)d;
-                mx = mx > mg ? mx : mg;
+        /* 1. wait for this tile's floats, transpose blocks into rows and
+         *    find the largest magnitude (decides the quantization path) */
+        mbar_wait(&bar[cb], (it >> 1) & 1u, a.w.err);
+        const float *xin = reinterpret_cast<const float *>(
+            inb[cb] + ((uintptr_t)(a.x + (z.e_first - 1)) & 15u));
+        const float xprev0 = xin[0]; /* the head, or the last element of the previous tile */
+        uint32_t amax = abs_bits(xprev0);
+        for (uint32_t k = warp; k < z.nblk; k += nw) {
+            uint32_t n = zg_block_len(z.seg_len, L, z.blk0 + k);
+            for (uint32_t j = lane; j < n; j += 32) {
+                float v = xin[1 + k * L + j];
+                amax = max(amax, abs_bits(v));
+                rows[k * stride + j] = v;
             }
         }
-        b = width_of(mx, a.wt);
-        size = zg_block_bytes(b, n);
-    }
+        amax = __reduce_max_sync(0xffffffffu, amax);
+        if (lane == 0) atomicMax(s_amax, amax);
+        __syncthreads();
+        const bool fastq = tile_fast_ok(*s_amax, a.inv);
 
-    /* 3. place the tile: block scan + look-back */
-    const uint32_t headb = z.has_head ? 4u : 0u;
-    uint32_t total;
-    const uint32_t off = cta_excl_scan(size, wsum, &total);
-    total += headb;
-    if (warp == 0) {
-        uint64_t prefix = lookback(a.w.status, tile, total, tile == 0, 0, a.w.err);
-        if (lane == 0) bcast[1] = prefix;
-    }
-    __syncthreads();
-    const uint64_t base = 8ull * g.T + bcast[1];
-    const bool fits = base + total <= a.cap; /* uniform over the CTA */
-    if (!fits) bad |= ZERR_CAPACITY;
-
-    if (tid < z.nblk) a.idx.widths[z.gblk0 + tid] = (uint8_t)b;
-    const int32_t qprev0 = quantize(xprev0, a.inv, bad);
-    if (tid == 0) {
-        a.idx.tile_off[tile] = base;
-        a.idx.tile_qprev[tile] = qprev0;
-        if (fits && z.has_head && z.seg < g.T) {
-            uint64_t h = base - 8ull * g.T;
+        /* 2. quantize, delta, width */
+        uint32_t b = 0, size = 0, n = 0, smask = 0, mx = 0;
+        uint32_t m[FAST ? 32 : 1];
+        float xp = 0.0f;
+        if (tid < z.nblk) {
+            n = zg_block_len(z.seg_len, L, z.blk0 + tid);
+            const float *row = rows + tid * stride;
+            xp = tid == 0 ? xprev0 : rows[(tid - 1) * stride + L - 1];
+            int32_t qp = fastq ? quantize_fast(xp, a.inv) : quantize(xp, a.inv, bad);
+            if (FAST) {
 #pragma unroll
-            for (int k = 0; k < 8; k++) a.out[8ull * z.seg + k] = (uint8_t)(h >> (8 * k));
-        }
-        if (tile == g.ntiles - 1) *a.idx.size = base + total;
-    }
-
-    /* 4. pack into staging (16-byte phase of the destination) and store */
-    uint8_t *gout = a.out + base;
-    const uint32_t sph = (uint32_t)((uintptr_t)gout & 15u);
-    uint32_t *sw = reinterpret_cast<uint32_t *>(stage);
-    if (z.has_head && tid == 0) {
-#pragma unroll
-        for (int k = 0; k < 4; k++) stage[sph + k] = (uint8_t)((uint32_t)qprev0 >> (8 * k));
-    }
-    if (tid < z.nblk) {
-        const uint32_t o = sph + headb + off;
-        const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
-        if (FAST) {
-            BitWriter bw;
-            bw.init(sw, o, size);
-            bw.put(b, 8);
-            if (b) {
-                bw.put(smask >> (32 - 8 * ns), 8 * ns);
-                if (B) {
-#pragma unroll
-                    for (uint32_t j = 0; j < 32; j++)
-                        if (j < n) bw.put(bswap32(m[j] >> r) >> (32 - 8 * B), 8 * B);
+                for (uint32_t j = 0; j < 32; j++) {
+                    uint32_t mg = 0;
+                    if (j < n) {
+                        int32_t q = fastq ? quantize_fast(row[j], a.inv) : quantize(row[j], a.inv, bad);
+                        int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
+                        qp = q;
+                        mg = (uint32_t)abs(d); /* |INT_MIN| wraps to 2^31, as in the reference */
+                        smask |= ((uint32_t)d >> 31) << (31 - j);
+                        mx = max(mx, mg);
+                    }
+                    m[j] = mg;
                 }
-                if (r) {
-                    const uint32_t mask = (1u << r) - 1u;
-#pragma unroll
-                    for (uint32_t j = 0; j < 32; j++)
-                        if (j < n) bw.put(m[j] & mask, r);
-                }
-            }
-            bw.finish();
-        } else {
-            stage[o] = (uint8_t)b;
-            if (b) {
-                BitWriter ws, wh, wl;
-                ws.init(sw, o + 1, ns);
-                wh.init(sw, o + 1 + ns, B * n);
-                wl.init(sw, o + 1 + ns + B * n, size - 1 - ns - B * n);
-                const float *row = rows + tid * stride;
-                int32_t qp = quantize(xp, a.inv, bad);
-                const uint32_t mask = r ? (1u << r) - 1u : 0u;
+            } else {
                 for (uint32_t j = 0; j < n; j++) {
                     int32_t q = quantize(row[j], a.inv, bad);
                     int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
                     qp = q;
-                    uint32_t neg = d < 0 ? 1u : 0u;
-                    uint32_t mg = neg ? 0u - (uint32_t)d : (uint32_t)d;
-                    ws.put(neg, 1);
-                    if (B) wh.put(bswap32(mg >> r) >> (32 - 8 * B), 8 * B);
-                    if (r) wl.put(mg & mask, r);
+                    mx = max(mx, (uint32_t)abs(d));
                 }
-                ws.finish();
-                if (B) wh.finish();
-                if (r) wl.finish();
+            }
+            b = width_of(mx, a.wt);
+            size = zg_block_bytes(b, n);
+        }
+
+        /* 3. offsets in the tile, publish the tile size, pack, then place */
+        const uint32_t headb = z.has_head ? 4u : 0u;
+        uint32_t total;
+        const uint32_t off = cta_excl_scan(size, wsum, &total);
+        total += headb;
+        if (warp == 0) lb_publish(a.w.status, tile, total, tile == 0, 0);
+
+        const int32_t qprev0 = fastq ? quantize_fast(xprev0, a.inv) : quantize(xprev0, a.inv, bad);
+        smem_zero(outs, total + 8);
+        __syncthreads();
+        if (z.has_head && tid == 0) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) outs[k] = (uint8_t)((uint32_t)qprev0 >> (8 * k));
+        }
+        if (tid < z.nblk) {
+            const uint32_t o = headb + off;
+            const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
+            if (FAST) {
+                Packer pk;
+                pk.init(outw, o);
+                pk.put(b, 8);
+                pk.flush();
+                if (b) {
+                    pk.put(smask >> (32 - 8 * ns), 8 * ns);
+                    pk.flush();
+                    if (B) put_high_bytes(pk, m, n, B, r);
+                    if (r) put_low_bits(pk, m, n, r, B > 0);
+                }
+                pk.finish();
+            } else {
+                Packer ph;
+                ph.init(outw, o);
+                ph.put(b, 8);
+                ph.finish();
+                if (b) {
+                    Packer ws, wh, wl;
+                    ws.init(outw, o + 1);
+                    wh.init(outw, o + 1 + ns);
+                    wl.init(outw, o + 1 + ns + B * n);
+                    const float *row = rows + tid * stride;
+                    int32_t qp = fastq ? quantize_fast(xp, a.inv) : quantize(xp, a.inv, bad);
+                    const uint32_t mask = r ? (1u << r) - 1u : 0u;
+                    for (uint32_t j = 0; j < n; j++) {
+                        int32_t q = fastq ? quantize_fast(row[j], a.inv) : quantize(row[j], a.inv, bad);
+                        int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
+                        qp = q;
+                        uint32_t mg = (uint32_t)abs(d);
+                        ws.put((uint32_t)d >> 31, 1);
+                        ws.flush();
+                        if (B) {
+                            wh.put(bswap32(mg >> r) >> (32 - 8 * B), 8 * B);
+                            wh.flush();
+                        }
+                        if (r) {
+                            wl.put(mg & mask, r);
+                            wl.flush();
+                        }
+                    }
+                    ws.finish();
+                    if (B) wh.finish();
+                    if (r) wl.finish();
+                }
             }
         }
+        if (warp == 0) {
+            uint64_t prefix = lb_resolve(a.w.status, tile, total, tile == 0, 0, a.w.err);
+            if (lane == 0) bc[2] = prefix;
+        }
+        __syncthreads();
+
+        /* 4. write the tile and its index entries */
+        const uint64_t base = 8ull * g.T + bc[2];
+        const bool fits = base + total <= a.cap; /* uniform over the CTA */
+        if (!fits) bad |= ZERR_CAPACITY;
+        if (tid < z.nblk) a.idx.widths[z.gblk0 + tid] = (uint8_t)b;
+        if (tid == 0) {
+            a.idx.tile_off[tile] = base;
+            a.idx.tile_qprev[tile] = qprev0;
+            if (fits && z.has_head && z.seg < g.T) {
+                uint64_t h = base - 8ull * g.T;
+#pragma unroll
+                for (int k = 0; k < 8; k++) a.out[8ull * z.seg + k] = (uint8_t)(h >> (8 * k));
+            }
+            if (tile == g.ntiles - 1) *a.idx.size = base + total;
+        }
+        if (fits) store_realign(a.out + base, outs, total);
+        if (tid == 0) *s_amax = 0;
+        __syncthreads(); /* rows, outs, bc[2] and the maximum are reused by the next tile */
     }
-    if (fits) stage_out(gout, stage, total);
     if (bad) atomicOr(a.w.err, bad);
 }
 
@@ -193,10 +229,10 @@ cudaError_t launch_compress(const CompressArgs &a, cudaStream_t st)
     const void *fn = fast ? (const void *)k_compress<true> : (const void *)k_compress<false>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
     if (e != cudaSuccess) return e;
-    dim3 grid((unsigned)a.g.ntiles), block(a.g.TB);
+    unsigned grid = persistent_grid(fn, a.g.TB, a.sm.total, a.g.ntiles);
     if (fast)
-        k_compress<true><<<grid, block, a.sm.total, st>>>(a);
+        k_compress<true><<<grid, a.g.TB, a.sm.total, st>>>(a);
     else
-        k_compress<false><<<grid, block, a.sm.total, st>>>(a);
+        k_compress<false><<<grid, a.g.TB, a.sm.total, st>>>(a);
     return cudaGetLastError();
 }

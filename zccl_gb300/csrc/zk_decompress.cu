@@ -2,19 +2,20 @@
  * zk_decompress.cu -- decompressor.
  *
  * Replaces ZCCL_float_decompress_openmp_threadblock_arg
- * (ZCCL/src/ZCCLd_float.c:538-754) and produces the same floats.  One CTA
- * per tile, one thread per block, mirroring the compressor:
- *   1. block sizes come from the width index, a block-wide scan gives every
- *      block's byte offset inside the tile, and the tile's bytes arrive in
- *      shared memory with one TMA bulk copy;
+ * (ZCCL/src/ZCCLd_float.c:538-754) and produces the same floats.  Persistent
+ * CTAs take tiles in ticket order, one thread per block, mirroring the
+ * compressor:
+ *   1. for the NEXT tile: block sizes from the width index, a block-wide
+ *      scan for every block's offset, and one TMA bulk copy of its bytes,
+ *      so the copy runs while the current tile is decoded (double buffer);
  *   2. every thread unpacks its block (sign bits, high bytes, low-bit
  *      stream, ZCCL/src/ZCCL_TypeManager.c:423-950) into int32 deltas;
  *   3. a block-wide scan of the per-block delta sums, started from the
  *      quantized value before the tile, restores the running values
- *      (ZCCLd_float.c:617-628); the starting value comes from the index when
- *      the stream was produced on the device, otherwise from a decoupled
- *      look-back over tile delta sums that restarts at every segment head,
- *      and is then written back into the index;
+ *      (ZCCLd_float.c:617-628); that starting value comes from the index
+ *      when the stream was produced on the device, otherwise from a
+ *      decoupled look-back over tile delta sums that restarts at every
+ *      segment head, and is then written back into the index;
  *   4. x = (float)q * eb (ZCCLd_float.c:624) into padded rows, written out
  *      row by row with coalesced stores.
  */
@@ -22,15 +23,59 @@
 
 namespace {
 
+/* Per-thread view of its block in a staged tile. */
+struct BlockSlot {
+    uint32_t b, n, off;
+};
+
+/* All threads: sizes of tile t's blocks from the index, their offsets, and
+ * (thread 0) the TMA copy of the tile's bytes into buf.  Returns the slot of
+ * this thread's block; the tile's byte offset lands in *s_base. */
+__device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, uint64_t t, uint8_t *buf,
+                                                uint64_t *bar, uint32_t *wsum, uint64_t *s_base,
+                                                uint32_t &bad)
+{
+    BlockSlot sl = {0, 0, 0};
+    ZTile z;
+    zg_tile(&a.g, t, &z);
+    uint32_t size = 0;
+    if (threadIdx.x < z.nblk) {
+        sl.n = zg_block_len(z.seg_len, a.g.L, z.blk0 + threadIdx.x);
+        sl.b = a.idx.widths[z.gblk0 + threadIdx.x];
+        if (sl.b > 32) {
+            bad |= ZERR_CORRUPT;
+            sl.b = 0;
+        }
+        size = zg_block_bytes(sl.b, sl.n);
+    }
+    uint32_t total;
+    sl.off = cta_excl_scan(size, wsum, &total);
+    total += z.has_head ? 4u : 0u;
+    if (threadIdx.x == 0) {
+        uint64_t base = a.idx.tile_off[t];
+        uint32_t nload = total;
+        /* overflow-safe: base comes from the index and is not trusted */
+        if (base > a.avail || total > a.avail - base) {
+            bad |= ZERR_BOUNDS;
+            nload = base < a.avail ? (uint32_t)min((uint64_t)total, a.avail - base) : 0u;
+            if (base > a.avail) base = 0;
+        }
+        *s_base = base;
+        tma_load_superset(buf, a.in + base, nload, bar);
+    }
+    return sl;
+}
+
 template <bool FAST>
 __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem); /* [2] */
     uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 16);
-    uint64_t *bcast = reinterpret_cast<uint64_t *>(smem + 160);
+    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160);     /* [0,1] tiles, [2] q0 */
+    uint64_t *s_base = reinterpret_cast<uint64_t *>(smem + 192); /* [2] */
     float *rows = reinterpret_cast<float *>(smem + a.sm.rows);
-    uint8_t *stage = smem + a.sm.stage;
+    uint8_t *inb[2] = {smem + a.sm.in0, smem + a.sm.in1};
 
     const ZGeom &g = a.g;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, nw = blockDim.x >> 5;
@@ -42,141 +87,139 @@ __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
     if (*(volatile const uint32_t *)a.w.walk_err) return;
 
     if (tid == 0) {
-        bcast[0] = a.qprev_valid ? (uint64_t)blockIdx.x : (uint64_t)atomicAdd(a.w.ticket, 1u);
-        mbar_init(bar, 1);
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        bc[0] = atomicAdd(a.w.ticket, 1u);
     }
     __syncthreads();
-    const uint64_t tile = bcast[0];
-    ZTile z;
-    zg_tile(&g, tile, &z);
+    BlockSlot cur = {0, 0, 0};
+    if (bc[0] < g.ntiles) cur = stage_tile(a, bc[0], inb[0], &bar[0], wsum, &s_base[0], bad);
 
-    /* 1. block sizes and the tile's bytes */
-    uint32_t b = 0, n = 0, size = 0;
-    if (tid < z.nblk) {
-        n = zg_block_len(z.seg_len, L, z.blk0 + tid);
-        b = a.idx.widths[z.gblk0 + tid];
-        if (b > 32) {
-            bad |= ZERR_CORRUPT;
-            b = 0;
+    for (uint32_t it = 0;; it++) {
+        const uint32_t cb = it & 1u;
+        __syncthreads();
+        const uint64_t tile = bc[cb];
+        if (tile >= g.ntiles) break;
+        ZTile z;
+        zg_tile(&g, tile, &z);
+
+        /* 1. claim the next tile and start its copy */
+        if (tid == 0) bc[cb ^ 1u] = atomicAdd(a.w.ticket, 1u);
+        __syncthreads();
+        BlockSlot nxt = {0, 0, 0};
+        if (bc[cb ^ 1u] < g.ntiles)
+            nxt = stage_tile(a, bc[cb ^ 1u], inb[cb ^ 1u], &bar[cb ^ 1u], wsum, &s_base[cb ^ 1u],
+                             bad);
+
+        /* 2. unpack this tile's deltas */
+        mbar_wait(&bar[cb], (it >> 1) & 1u, a.w.err);
+        const uint32_t ph = (uint32_t)((uintptr_t)(a.in + s_base[cb]) & 15u);
+        const uint8_t *tb = inb[cb] + ph;
+        const uint32_t *sw = reinterpret_cast<const uint32_t *>(inb[cb]);
+        int32_t head = 0;
+        if (z.has_head) {
+            uint32_t h = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) h |= (uint32_t)tb[k] << (8 * k);
+            head = (int32_t)h;
         }
-        size = zg_block_bytes(b, n);
-    }
-    const uint32_t headb = z.has_head ? 4u : 0u;
-    uint32_t total;
-    const uint32_t off = cta_excl_scan(size, wsum, &total);
-    total += headb;
-    const uint64_t base = a.idx.tile_off[tile];
-    uint32_t nload = total;
-    /* overflow-safe: base comes from the index and is not trusted */
-    if (base > a.avail || total > a.avail - base) {
-        bad |= ZERR_BOUNDS;
-        nload = base < a.avail ? (uint32_t)min((uint64_t)total, a.avail - base) : 0u;
-    }
-    const uint32_t ph = stage_in(stage, a.in + base, nload, bar);
-    stage_in_wait(bar, 0, a.w.err);
-    const uint32_t *sw = reinterpret_cast<const uint32_t *>(stage);
-
-    int32_t head = 0;
-    if (z.has_head) {
-        uint32_t h = 0;
+        const uint32_t headb = z.has_head ? 4u : 0u;
+        const uint32_t o = ph + headb + cur.off; /* this block, in buffer coordinates */
+        const uint32_t b = cur.b, n = cur.n;
+        uint32_t d[FAST ? 32 : 1];
+        uint32_t bsum = 0;
+        if (tid < z.nblk) {
+            if (inb[cb][o] != b) bad |= ZERR_CORRUPT;
+            if (FAST) {
 #pragma unroll
-        for (int k = 0; k < 4; k++) h |= (uint32_t)stage[ph + k] << (8 * k);
-        head = (int32_t)h;
-    }
-
-    /* 2. unpack deltas */
-    const uint32_t o = ph + headb + off;
-    uint32_t d[FAST ? 32 : 1];
-    uint32_t bsum = 0;
-    if (tid < z.nblk) {
-        if (stage[o] != b) bad |= ZERR_CORRUPT;
-        if (FAST) {
-#pragma unroll
-            for (uint32_t j = 0; j < 32; j++) d[j] = 0;
-            if (b) {
-                const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
-                BitReader br;
-                br.init(sw, o + 1);
-                const uint32_t sg = br.get(8 * ns) << (32 - 8 * ns);
-                if (B) {
-#pragma unroll
-                    for (uint32_t j = 0; j < 32; j++)
-                        if (j < n) d[j] = bswap32(br.get(8 * B) << (32 - 8 * B)) << r;
-                }
-                if (r) {
-#pragma unroll
-                    for (uint32_t j = 0; j < 32; j++)
-                        if (j < n) d[j] |= br.get(r);
-                }
-#pragma unroll
-                for (uint32_t j = 0; j < 32; j++) {
-                    if ((sg >> (31 - j)) & 1u) d[j] = 0u - d[j];
-                    bsum += d[j];
-                }
-            }
-        } else if (b) {
-            const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
-            BitReader rs, rh, rl;
-            rs.init(sw, o + 1);
-            rh.init(sw, o + 1 + ns);
-            rl.init(sw, o + 1 + ns + B * n);
-            for (uint32_t j = 0; j < n; j++) {
-                uint32_t v = B ? bswap32(rh.get(8 * B) << (32 - 8 * B)) << r : 0u;
-                if (r) v |= rl.get(r);
-                if (rs.get(1)) v = 0u - v;
-                bsum += v;
-            }
-        }
-    }
-
-    /* 3. starting value of every block */
-    uint32_t tsum;
-    const uint32_t pre = cta_excl_scan(bsum, wsum, &tsum);
-    if (a.qprev_valid) {
-        if (tid == 0) bcast[1] = (uint32_t)(z.has_head ? head : a.idx.tile_qprev[tile]);
-    } else if (warp == 0) {
-        uint64_t q0 = lookback(a.w.status, tile, tsum, z.has_head != 0, (uint32_t)head, a.w.err);
-        if (lane == 0) {
-            bcast[1] = (uint32_t)q0;
-            a.idx.tile_qprev[tile] = (int32_t)(uint32_t)q0;
-        }
-    }
-    __syncthreads();
-    const uint32_t q0 = (uint32_t)bcast[1];
-
-    /* 4. values into rows, then out */
-    if (tid < z.nblk) {
-        uint32_t q = q0 + pre;
-        float *row = rows + tid * stride;
-        if (FAST) {
-#pragma unroll
-            for (uint32_t j = 0; j < 32; j++) {
-                q += d[j];
-                if (j < n) row[j] = __fmul_rn(__int2float_rn((int32_t)q), a.eb);
-            }
-        } else {
-            const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
-            BitReader rs, rh, rl;
-            rs.init(sw, o + 1);
-            rh.init(sw, o + 1 + ns);
-            rl.init(sw, o + 1 + ns + B * n);
-            for (uint32_t j = 0; j < n; j++) {
+                for (uint32_t j = 0; j < 32; j++) d[j] = 0;
                 if (b) {
+                    const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
+                    Reader rd;
+                    rd.init(sw, o + 1);
+                    const uint32_t sg = rd.get(8 * ns) << (32 - 8 * ns);
+                    if (B) get_high_bytes(rd, d, n, B, r);
+                    if (r) get_low_bits(rd, d, n, r);
+#pragma unroll
+                    for (uint32_t j = 0; j < 32; j++) {
+                        if ((sg >> (31 - j)) & 1u) d[j] = 0u - d[j];
+                        bsum += d[j];
+                    }
+                }
+            } else if (b) {
+                const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
+                Reader rs, rh, rl;
+                rs.init(sw, o + 1);
+                rh.init(sw, o + 1 + ns);
+                rl.init(sw, o + 1 + ns + B * n);
+                for (uint32_t j = 0; j < n; j++) {
+                    rh.refill();
+                    rl.refill();
+                    rs.refill();
                     uint32_t v = B ? bswap32(rh.get(8 * B) << (32 - 8 * B)) << r : 0u;
                     if (r) v |= rl.get(r);
                     if (rs.get(1)) v = 0u - v;
-                    q += v;
+                    bsum += v;
                 }
-                row[j] = __fmul_rn(__int2float_rn((int32_t)q), a.eb);
             }
         }
-    }
-    if (z.has_head && tid == 0) a.y[z.seg_start] = __fmul_rn(__int2float_rn(head), a.eb);
-    __syncthreads();
-    for (uint32_t k = warp; k < z.nblk; k += nw) {
-        uint32_t nk = zg_block_len(z.seg_len, L, z.blk0 + k);
-        float *dst = a.y + z.e_first + (uint64_t)k * L;
-        for (uint32_t j = lane; j < nk; j += 32) dst[j] = rows[k * stride + j];
+
+        /* 3. starting value of every block */
+        uint32_t tsum;
+        const uint32_t pre = cta_excl_scan(bsum, wsum, &tsum);
+        if (a.qprev_valid) {
+            if (tid == 0) bc[2] = (uint32_t)(z.has_head ? head : a.idx.tile_qprev[tile]);
+        } else if (warp == 0) {
+            lb_publish(a.w.status, tile, tsum, z.has_head != 0, (uint32_t)head);
+            uint64_t q0 = lb_resolve(a.w.status, tile, tsum, z.has_head != 0, (uint32_t)head, a.w.err);
+            if (lane == 0) {
+                bc[2] = (uint32_t)q0;
+                a.idx.tile_qprev[tile] = (int32_t)(uint32_t)q0;
+            }
+        }
+        __syncthreads();
+        const uint32_t q0 = (uint32_t)bc[2];
+
+        /* 4. values into rows, then out */
+        if (tid < z.nblk) {
+            uint32_t q = q0 + pre;
+            float *row = rows + tid * stride;
+            if (FAST) {
+#pragma unroll
+                for (uint32_t j = 0; j < 32; j++) {
+                    q += d[j];
+                    if (j < n) row[j] = __fmul_rn(__int2float_rn((int32_t)q), a.eb);
+                }
+            } else {
+                const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
+                Reader rs, rh, rl;
+                if (b) {
+                    rs.init(sw, o + 1);
+                    rh.init(sw, o + 1 + ns);
+                    rl.init(sw, o + 1 + ns + B * n);
+                }
+                for (uint32_t j = 0; j < n; j++) {
+                    if (b) {
+                        rh.refill();
+                        rl.refill();
+                        rs.refill();
+                        uint32_t v = B ? bswap32(rh.get(8 * B) << (32 - 8 * B)) << r : 0u;
+                        if (r) v |= rl.get(r);
+                        if (rs.get(1)) v = 0u - v;
+                        q += v;
+                    }
+                    row[j] = __fmul_rn(__int2float_rn((int32_t)q), a.eb);
+                }
+            }
+        }
+        if (z.has_head && tid == 0) a.y[z.seg_start] = __fmul_rn(__int2float_rn(head), a.eb);
+        __syncthreads();
+        for (uint32_t k = warp; k < z.nblk; k += nw) {
+            uint32_t nk = zg_block_len(z.seg_len, L, z.blk0 + k);
+            float *dst = a.y + z.e_first + (uint64_t)k * L;
+            for (uint32_t j = lane; j < nk; j += 32) dst[j] = rows[k * stride + j];
+        }
+        cur = nxt;
     }
     if (bad) atomicOr(a.w.err, bad);
 }
@@ -189,10 +232,10 @@ cudaError_t launch_decompress(const DecompressArgs &a, cudaStream_t st)
     const void *fn = fast ? (const void *)k_decompress<true> : (const void *)k_decompress<false>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
     if (e != cudaSuccess) return e;
-    dim3 grid((unsigned)a.g.ntiles), block(a.g.TB);
+    unsigned grid = persistent_grid(fn, a.g.TB, a.sm.total, a.g.ntiles);
     if (fast)
-        k_decompress<true><<<grid, block, a.sm.total, st>>>(a);
+        k_decompress<true><<<grid, a.g.TB, a.sm.total, st>>>(a);
     else
-        k_decompress<false><<<grid, block, a.sm.total, st>>>(a);
+        k_decompress<false><<<grid, a.g.TB, a.sm.total, st>>>(a);
     return cudaGetLastError();
 }

@@ -9,123 +9,166 @@
  * canonical).  Integer addition is associative modulo 2^32, so one pass over
  * P inputs equals the ring's pairwise fold in any order, bit for bit.
  *
- * One CTA per tile, one thread per block.  For each input in turn: block
- * sizes from its width index, one TMA bulk copy of its tile bytes, and each
- * thread adds the block's deltas into registers; zero-width input blocks
- * are skipped without touching their bytes.  The sum is then re-encoded
- * exactly like the compressor (width, scan, look-back, packed staging, TMA
- * bulk store) and the output's side index is written; the output's
- * quantized value before each tile is the sum of the inputs' values.
+ * Persistent CTAs take tiles in ticket order, one thread per block.  The
+ * (tile, input) pairs form one stream of TMA copies through two buffers:
+ * while one input's tile bytes are unpacked and added into per-thread
+ * registers, the next input's (or the next tile's first input's) sizes are
+ * scanned from its width index and its bytes are already in flight.
+ * Zero-width input blocks are skipped without touching their bytes.  After
+ * the last input the sum is re-encoded like the compressor does (width,
+ * scan, early look-back publish, OR-packing, realigned vector stores) and
+ * the output's side index is written; its starting value per tile is the
+ * sum of the inputs' values.
  */
 #include "zkern.cuh"
 
 namespace {
 
-template <bool FAST>
-__global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
+struct BlockSlot {
+    uint32_t b, n, off;
+};
+
+/* All threads: sizes of input p's blocks in tile t, their offsets, and
+ * (thread 0) the TMA copy of those bytes into buf. */
+__device__ __forceinline__ BlockSlot stage_input(const HomAddArgs &a, uint64_t t, uint32_t p,
+                                                 uint8_t *buf, uint64_t *bar, uint32_t *wsum,
+                                                 uint64_t *s_base, uint32_t &bad)
 {
-    extern __shared__ __align__(16) uint8_t smem[];
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
-    uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 16);
-    uint64_t *bcast = reinterpret_cast<uint64_t *>(smem + 160);
-    uint32_t *acc_rows = reinterpret_cast<uint32_t *>(smem + a.sm.rows);
-    uint8_t *stage = smem + a.sm.stage;
-    uint32_t *sw = reinterpret_cast<uint32_t *>(stage);
-
-    const ZGeom &g = a.g;
-    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t L = g.L, stride = zg_row_stride(L);
-    uint32_t bad = 0;
-    /* The index walk ran to completion before this launch, so every CTA sees
-     * the same word: after a failed walk no CTA touches the stream and no
-     * CTA waits on another. */
-    if (*(volatile const uint32_t *)a.w.walk_err) return;
-
-    if (tid == 0) {
-        bcast[0] = atomicAdd(a.w.ticket, 1u);
-        mbar_init(bar, 1);
-    }
-    __syncthreads();
-    const uint64_t tile = bcast[0];
+    const HomInput &in = a.in[p];
+    BlockSlot sl = {0, 0, 0};
     ZTile z;
-    zg_tile(&g, tile, &z);
-    const bool own = tid < z.nblk;
-    const uint32_t n = own ? zg_block_len(z.seg_len, L, z.blk0 + tid) : 0u;
-    const uint32_t headb = z.has_head ? 4u : 0u;
-
-    uint32_t acc[FAST ? 32 : 1];
-    if (FAST) {
-#pragma unroll
-        for (uint32_t j = 0; j < 32; j++) acc[j] = 0;
-    } else if (own) {
-        for (uint32_t j = 0; j < n; j++) acc_rows[tid * stride + j] = 0;
-    }
-    uint32_t hsum = 0, qsum = 0, nzmask = 0;
-
-    for (uint32_t p = 0; p < a.P; p++) {
-        const HomInput in = a.in[p];
-        uint32_t b = 0, size = 0;
-        if (own) {
-            b = in.widths[z.gblk0 + tid];
-            if (b > 32) {
-                bad |= ZERR_CORRUPT;
-                b = 0;
-            }
-            size = zg_block_bytes(b, n);
-            if (b) nzmask |= 1u << (p & 31);
+    zg_tile(&a.g, t, &z);
+    uint32_t size = 0;
+    if (threadIdx.x < z.nblk) {
+        sl.n = zg_block_len(z.seg_len, a.g.L, z.blk0 + threadIdx.x);
+        sl.b = in.widths[z.gblk0 + threadIdx.x];
+        if (sl.b > 32) {
+            bad |= ZERR_CORRUPT;
+            sl.b = 0;
         }
-        uint32_t total;
-        const uint32_t off = cta_excl_scan(size, wsum, &total);
-        total += headb;
-        const uint64_t base = in.tile_off[tile];
+        size = zg_block_bytes(sl.b, sl.n);
+    }
+    uint32_t total;
+    sl.off = cta_excl_scan(size, wsum, &total);
+    total += z.has_head ? 4u : 0u;
+    if (threadIdx.x == 0) {
+        uint64_t base = in.tile_off[t];
         uint32_t nload = total;
         /* overflow-safe: base comes from the index and is not trusted */
         if (base > in.avail || total > in.avail - base) {
             bad |= ZERR_BOUNDS;
             nload = base < in.avail ? (uint32_t)min((uint64_t)total, in.avail - base) : 0u;
+            if (base > in.avail) base = 0;
         }
-        const uint32_t ph = stage_in(stage, in.bytes + base, nload, bar);
-        stage_in_wait(bar, p & 1u, a.w.err);
+        *s_base = base;
+        tma_load_superset(buf, in.bytes + base, nload, bar);
+    }
+    return sl;
+}
+
+template <bool FAST>
+__global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem); /* [2] */
+    uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 16);
+    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160);     /* [0] next tile, [1] prefix */
+    uint64_t *s_base = reinterpret_cast<uint64_t *>(smem + 192); /* [2] */
+    uint32_t *acc_rows = reinterpret_cast<uint32_t *>(smem + a.sm.rows);
+    uint8_t *inb[2] = {smem + a.sm.in0, smem + a.sm.in1};
+    uint8_t *outs = smem + a.sm.out;
+    uint32_t *outw = reinterpret_cast<uint32_t *>(outs);
+
+    const ZGeom &g = a.g;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t L = g.L, stride = zg_row_stride(L), P = a.P;
+    uint32_t bad = 0;
+    /* see k_decompress: a failed index walk stops every CTA alike */
+    if (*(volatile const uint32_t *)a.w.walk_err) return;
+
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        bc[0] = atomicAdd(a.w.ticket, 1u);
+    }
+    __syncthreads();
+    uint64_t tile = bc[0];
+    if (tile >= g.ntiles) return;
+    BlockSlot cur = stage_input(a, tile, 0, inb[0], &bar[0], wsum, &s_base[0], bad);
+
+    uint32_t acc[FAST ? 32 : 1];
+    uint32_t hsum = 0, qsum = 0, nzmask = 0;
+    uint32_t ld = 0; /* index of the current copy in the two-buffer stream */
+    uint32_t p = 0;  /* input of the current copy */
+
+    for (;;) {
+        const uint32_t cb = ld & 1u;
+        ZTile z;
+        zg_tile(&g, tile, &z);
+        const bool own = tid < z.nblk;
+        if (p == 0) {
+            if (FAST) {
+#pragma unroll
+                for (uint32_t j = 0; j < 32; j++) acc[j] = 0;
+            } else if (own) {
+                for (uint32_t j = 0; j < cur.n; j++) acc_rows[tid * stride + j] = 0;
+            }
+            hsum = qsum = nzmask = 0;
+        }
+
+        /* start the next copy: the next input of this tile, or input 0 of the next tile */
+        uint64_t ntile = tile;
+        uint32_t np = p + 1;
+        if (np == P) {
+            if (tid == 0) bc[0] = atomicAdd(a.w.ticket, 1u);
+            __syncthreads();
+            ntile = bc[0];
+            np = 0;
+        }
+        BlockSlot nxt = {0, 0, 0};
+        if (ntile < g.ntiles)
+            nxt = stage_input(a, ntile, np, inb[cb ^ 1u], &bar[cb ^ 1u], wsum, &s_base[cb ^ 1u], bad);
+
+        /* add this input's deltas */
+        mbar_wait(&bar[cb], (ld >> 1) & 1u, a.w.err);
+        const uint32_t ph = (uint32_t)((uintptr_t)(a.in[p].bytes + s_base[cb]) & 15u);
+        const uint8_t *tb = inb[cb] + ph;
+        const uint32_t *sw = reinterpret_cast<const uint32_t *>(inb[cb]);
+        const uint32_t headb = z.has_head ? 4u : 0u;
         if (z.has_head) {
             uint32_t h = 0;
 #pragma unroll
-            for (int k = 0; k < 4; k++) h |= (uint32_t)stage[ph + k] << (8 * k);
+            for (int k = 0; k < 4; k++) h |= (uint32_t)tb[k] << (8 * k);
             hsum += h;
         }
-        if (a.qprev_valid) qsum += (uint32_t)in.tile_qprev[tile];
+        if (a.qprev_valid) qsum += (uint32_t)a.in[p].tile_qprev[tile];
         if (own) {
-            const uint32_t o = ph + headb + off;
-            if (stage[o] != b) bad |= ZERR_CORRUPT;
+            const uint32_t b = cur.b, n = cur.n, o = ph + headb + cur.off;
+            if (inb[cb][o] != b) bad |= ZERR_CORRUPT;
             if (b) {
+                nzmask |= 1u << (p & 31);
                 const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
                 if (FAST) {
-                    /* -(hi << r | lo) == -(hi << r) - lo: each part is added
-                     * with the element's sign as soon as it is read */
-                    BitReader br;
-                    br.init(sw, o + 1);
-                    const uint32_t sg = br.get(8 * ns) << (32 - 8 * ns);
-                    if (B) {
+                    uint32_t v[32];
 #pragma unroll
-                        for (uint32_t j = 0; j < 32; j++)
-                            if (j < n) {
-                                uint32_t t = bswap32(br.get(8 * B) << (32 - 8 * B)) << r;
-                                acc[j] += ((sg >> (31 - j)) & 1u) ? 0u - t : t;
-                            }
-                    }
-                    if (r) {
+                    for (uint32_t j = 0; j < 32; j++) v[j] = 0;
+                    Reader rd;
+                    rd.init(sw, o + 1);
+                    const uint32_t sg = rd.get(8 * ns) << (32 - 8 * ns);
+                    if (B) get_high_bytes(rd, v, n, B, r);
+                    if (r) get_low_bits(rd, v, n, r);
 #pragma unroll
-                        for (uint32_t j = 0; j < 32; j++)
-                            if (j < n) {
-                                uint32_t t = br.get(r);
-                                acc[j] += ((sg >> (31 - j)) & 1u) ? 0u - t : t;
-                            }
-                    }
+                    for (uint32_t j = 0; j < 32; j++)
+                        acc[j] += ((sg >> (31 - j)) & 1u) ? 0u - v[j] : v[j];
                 } else {
-                    BitReader rs, rh, rl;
+                    Reader rs, rh, rl;
                     rs.init(sw, o + 1);
                     rh.init(sw, o + 1 + ns);
                     rl.init(sw, o + 1 + ns + B * n);
                     for (uint32_t j = 0; j < n; j++) {
+                        rh.refill();
+                        rl.refill();
+                        rs.refill();
                         uint32_t v = B ? bswap32(rh.get(8 * B) << (32 - 8 * B)) << r : 0u;
                         if (r) v |= rl.get(r);
                         if (rs.get(1)) v = 0u - v;
@@ -134,121 +177,125 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
                 }
             }
         }
-        __syncthreads(); /* staging is reused by the next input */
-    }
 
-    /* branch-case counters of the two-input add (ZCCLd_float.c:2175-2764) */
-    if (a.cases && a.P == 2) {
-        uint32_t c0 = __syncthreads_count(own && nzmask == 0u);
-        uint32_t c1 = __syncthreads_count(own && nzmask == 2u);
-        uint32_t c2 = __syncthreads_count(own && nzmask == 1u);
-        uint32_t c3 = __syncthreads_count(own && nzmask == 3u);
-        if (tid == 0) {
-            atomicAdd(a.cases + 0, (unsigned long long)c0);
-            atomicAdd(a.cases + 1, (unsigned long long)c1);
-            atomicAdd(a.cases + 2, (unsigned long long)c2);
-            atomicAdd(a.cases + 3, (unsigned long long)c3);
-        }
-    }
-
-    /* re-encode the sum */
-    uint32_t b = 0, size = 0, smask = 0, mx = 0;
-    if (own) {
-        if (FAST) {
-#pragma unroll
-            for (uint32_t j = 0; j < 32; j++) {
-                int32_t d = (int32_t)acc[j];
-                uint32_t neg = d < 0 ? 1u : 0u;
-                uint32_t mg = neg ? 0u - acc[j] : acc[j];
-                smask |= neg << (31 - j);
-                mx = mx > mg ? mx : mg;
-                acc[j] = mg;
-            }
-        } else {
-            for (uint32_t j = 0; j < n; j++) {
-                uint32_t v = acc_rows[tid * stride + j];
-                uint32_t mg = (int32_t)v < 0 ? 0u - v : v;
-                mx = mx > mg ? mx : mg;
-            }
-        }
-        b = width_of(mx, a.wt);
-        size = zg_block_bytes(b, n);
-    }
-    uint32_t total;
-    const uint32_t off = cta_excl_scan(size, wsum, &total);
-    total += headb;
-    if (warp == 0) {
-        uint64_t prefix = lookback(a.w.status, tile, total, tile == 0, 0, a.w.err);
-        if (lane == 0) bcast[1] = prefix;
-    }
-    __syncthreads();
-    const uint64_t base = 8ull * g.T + bcast[1];
-    const bool fits = base + total <= a.cap; /* uniform over the CTA */
-    if (!fits) bad |= ZERR_CAPACITY;
-
-    if (own) a.idx.widths[z.gblk0 + tid] = (uint8_t)b;
-    if (tid == 0) {
-        a.idx.tile_off[tile] = base;
-        if (a.qprev_valid) a.idx.tile_qprev[tile] = (int32_t)qsum;
-        if (fits && z.has_head && z.seg < g.T) {
-            uint64_t h = base - 8ull * g.T;
-#pragma unroll
-            for (int k = 0; k < 8; k++) a.out[8ull * z.seg + k] = (uint8_t)(h >> (8 * k));
-        }
-        if (tile == g.ntiles - 1) *a.idx.size = base + total;
-    }
-
-    uint8_t *gout = a.out + base;
-    const uint32_t sph = (uint32_t)((uintptr_t)gout & 15u);
-    if (z.has_head && tid == 0) {
-#pragma unroll
-        for (int k = 0; k < 4; k++) stage[sph + k] = (uint8_t)(hsum >> (8 * k));
-    }
-    if (own) {
-        const uint32_t o = sph + headb + off;
-        const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
-        if (FAST) {
-            BitWriter bw;
-            bw.init(sw, o, size);
-            bw.put(b, 8);
-            if (b) {
-                bw.put(smask >> (32 - 8 * ns), 8 * ns);
-                if (B) {
-#pragma unroll
-                    for (uint32_t j = 0; j < 32; j++)
-                        if (j < n) bw.put(bswap32(acc[j] >> r) >> (32 - 8 * B), 8 * B);
-                }
-                if (r) {
-                    const uint32_t mask = (1u << r) - 1u;
-#pragma unroll
-                    for (uint32_t j = 0; j < 32; j++)
-                        if (j < n) bw.put(acc[j] & mask, r);
+        if (p + 1 == P) {
+            /* branch-case counters of the two-input add (ZCCLd_float.c:2175-2764) */
+            if (a.cases && P == 2) {
+                uint32_t c0 = __syncthreads_count(own && nzmask == 0u);
+                uint32_t c1 = __syncthreads_count(own && nzmask == 2u);
+                uint32_t c2 = __syncthreads_count(own && nzmask == 1u);
+                uint32_t c3 = __syncthreads_count(own && nzmask == 3u);
+                if (tid == 0) {
+                    atomicAdd(a.cases + 0, (unsigned long long)c0);
+                    atomicAdd(a.cases + 1, (unsigned long long)c1);
+                    atomicAdd(a.cases + 2, (unsigned long long)c2);
+                    atomicAdd(a.cases + 3, (unsigned long long)c3);
                 }
             }
-            bw.finish();
-        } else {
-            stage[o] = (uint8_t)b;
-            if (b) {
-                BitWriter ws, wh, wl;
-                ws.init(sw, o + 1, ns);
-                wh.init(sw, o + 1 + ns, B * n);
-                wl.init(sw, o + 1 + ns + B * n, size - 1 - ns - B * n);
-                const uint32_t mask = r ? (1u << r) - 1u : 0u;
-                for (uint32_t j = 0; j < n; j++) {
-                    uint32_t v = acc_rows[tid * stride + j];
-                    uint32_t neg = (int32_t)v < 0 ? 1u : 0u;
-                    uint32_t mg = neg ? 0u - v : v;
-                    ws.put(neg, 1);
-                    if (B) wh.put(bswap32(mg >> r) >> (32 - 8 * B), 8 * B);
-                    if (r) wl.put(mg & mask, r);
+            /* re-encode the sum */
+            const uint32_t n = cur.n;
+            uint32_t b = 0, size = 0, smask = 0, mx = 0;
+            if (own) {
+                if (FAST) {
+#pragma unroll
+                    for (uint32_t j = 0; j < 32; j++) {
+                        uint32_t neg = acc[j] >> 31;
+                        uint32_t mg = (uint32_t)abs((int32_t)acc[j]);
+                        smask |= neg << (31 - j);
+                        mx = max(mx, mg);
+                        acc[j] = mg;
+                    }
+                } else {
+                    for (uint32_t j = 0; j < n; j++)
+                        mx = max(mx, (uint32_t)abs((int32_t)acc_rows[tid * stride + j]));
                 }
-                ws.finish();
-                if (B) wh.finish();
-                if (r) wl.finish();
+                b = width_of(mx, a.wt);
+                size = zg_block_bytes(b, n);
             }
+            uint32_t total;
+            const uint32_t off = cta_excl_scan(size, wsum, &total);
+            total += headb;
+            if (warp == 0) lb_publish(a.w.status, tile, total, tile == 0, 0);
+            smem_zero(outs, total + 8);
+            __syncthreads();
+            if (z.has_head && tid == 0) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) outs[k] = (uint8_t)(hsum >> (8 * k));
+            }
+            if (own) {
+                const uint32_t o = headb + off;
+                const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
+                if (FAST) {
+                    Packer pk;
+                    pk.init(outw, o);
+                    pk.put(b, 8);
+                    pk.flush();
+                    if (b) {
+                        pk.put(smask >> (32 - 8 * ns), 8 * ns);
+                        pk.flush();
+                        if (B) put_high_bytes(pk, acc, n, B, r);
+                        if (r) put_low_bits(pk, acc, n, r, B > 0);
+                    }
+                    pk.finish();
+                } else {
+                    Packer ph;
+                    ph.init(outw, o);
+                    ph.put(b, 8);
+                    ph.finish();
+                    if (b) {
+                        Packer ws, wh, wl;
+                        ws.init(outw, o + 1);
+                        wh.init(outw, o + 1 + ns);
+                        wl.init(outw, o + 1 + ns + B * n);
+                        const uint32_t mask = r ? (1u << r) - 1u : 0u;
+                        for (uint32_t j = 0; j < n; j++) {
+                            uint32_t v = acc_rows[tid * stride + j];
+                            uint32_t mg = (uint32_t)abs((int32_t)v);
+                            ws.put(v >> 31, 1);
+                            ws.flush();
+                            if (B) {
+                                wh.put(bswap32(mg >> r) >> (32 - 8 * B), 8 * B);
+                                wh.flush();
+                            }
+                            if (r) {
+                                wl.put(mg & mask, r);
+                                wl.flush();
+                            }
+                        }
+                        ws.finish();
+                        if (B) wh.finish();
+                        if (r) wl.finish();
+                    }
+                }
+            }
+            if (warp == 0) {
+                uint64_t prefix = lb_resolve(a.w.status, tile, total, tile == 0, 0, a.w.err);
+                if (lane == 0) bc[1] = prefix;
+            }
+            __syncthreads();
+            const uint64_t base = 8ull * g.T + bc[1];
+            const bool fits = base + total <= a.cap; /* uniform over the CTA */
+            if (!fits) bad |= ZERR_CAPACITY;
+            if (own) a.idx.widths[z.gblk0 + tid] = (uint8_t)b;
+            if (tid == 0) {
+                a.idx.tile_off[tile] = base;
+                if (a.qprev_valid) a.idx.tile_qprev[tile] = (int32_t)qsum;
+                if (fits && z.has_head && z.seg < g.T) {
+                    uint64_t h = base - 8ull * g.T;
+#pragma unroll
+                    for (int k = 0; k < 8; k++) a.out[8ull * z.seg + k] = (uint8_t)(h >> (8 * k));
+                }
+                if (tile == g.ntiles - 1) *a.idx.size = base + total;
+            }
+            if (fits) store_realign(a.out + base, outs, total);
         }
+        __syncthreads(); /* buffers, outs and the broadcast slots are reused */
+        if (ntile >= g.ntiles) break;
+        tile = ntile;
+        p = np;
+        cur = nxt;
+        ld++;
     }
-    if (fits) stage_out(gout, stage, total);
     if (bad) atomicOr(a.w.err, bad);
 }
 
@@ -260,10 +307,10 @@ cudaError_t launch_homadd(const HomAddArgs &a, cudaStream_t st)
     const void *fn = fast ? (const void *)k_homadd<true> : (const void *)k_homadd<false>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
     if (e != cudaSuccess) return e;
-    dim3 grid((unsigned)a.g.ntiles), block(a.g.TB);
+    unsigned grid = persistent_grid(fn, a.g.TB, a.sm.total, a.g.ntiles);
     if (fast)
-        k_homadd<true><<<grid, block, a.sm.total, st>>>(a);
+        k_homadd<true><<<grid, a.g.TB, a.sm.total, st>>>(a);
     else
-        k_homadd<false><<<grid, block, a.sm.total, st>>>(a);
+        k_homadd<false><<<grid, a.g.TB, a.sm.total, st>>>(a);
     return cudaGetLastError();
 }

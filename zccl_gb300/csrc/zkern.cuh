@@ -112,6 +112,20 @@ struct WalkArgs {
 /* Shared bytes per warp of the window-table kernel. */
 size_t walk_w1_warp_bytes(uint32_t M);
 
+/* Grid of a persistent kernel: every CTA that fits on the device at once,
+ * but no more CTAs than tiles. */
+static inline unsigned persistent_grid(const void *fn, int threads, size_t smem, uint64_t ntiles)
+{
+    int dev = 0, nsm = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, smem);
+    if (nsm < 1) nsm = 1;
+    if (occ < 1) occ = 1;
+    uint64_t g = (uint64_t)nsm * (uint64_t)occ;
+    return (unsigned)(g < ntiles ? g : ntiles);
+}
+
 /* Launchers; each returns the cudaError_t of the launch. */
 cudaError_t launch_compress(const CompressArgs &a, cudaStream_t st);
 cudaError_t launch_decompress(const DecompressArgs &a, cudaStream_t st);
