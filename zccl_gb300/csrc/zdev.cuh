@@ -1,12 +1,15 @@
 /*
  * zdev.cuh -- device building blocks shared by the codec kernels.
  *
- *   quantize()      bit-exact stand-in for (int)((double)x * (double)inv)
- *   width_of()      bit-exact stand-in for (int)log2f((float)m) + 1
- *   BitWriter/Reader MSB-first byte streams in shared memory
- *   stage_in/out()  TMA bulk copies between global memory and shared memory
- *   lookback()      single-pass decoupled look-back scan over tiles
- *   cta_scan*()     block-wide exclusive scans
+ *   quantize*()          bit-exact stand-ins for (int)((double)x * (double)inv)
+ *   width_of()           bit-exact stand-in for (int)log2f((float)m) + 1
+ *   encode_full/decode_full   one 32-element block, registers <-> packed bytes
+ *   encode_any/decode_any     any block, one element at a time
+ *   Packer / Reader      MSB-first bit streams in shared memory
+ *   tma_load_superset()  TMA bulk copy global -> shared
+ *   store_realign()      shared -> global at any byte alignment
+ *   cta_excl_scan()      block-wide exclusive scan
+ *   lb_publish/resolve   single-pass decoupled look-back across tiles
  */
 #ifndef ZCCL_GB300_ZDEV_CUH
 #define ZCCL_GB300_ZDEV_CUH
@@ -14,8 +17,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "zgeom.h"
 #include "zccl_err.h"
+#include "zgeom.h"
+
+/* ---------------------------------------------------------------------
+ * Exact arithmetic
+ * ------------------------------------------------------------------- */
 
 /* Width thresholds, filled on the host from the host's libm: thr[w] is the
  * smallest m of bit length w whose (int)log2f((float)m) equals w (so its
@@ -65,57 +72,75 @@ __device__ __forceinline__ int32_t quantize_fast(float x, float inv)
     return __float2int_rz(__fmul_rz(x, inv));
 }
 
+/* max over |x| as raw float bits: NaN ranks above +inf, so a NaN also fails
+ * the fast-quantization test. */
+__device__ __forceinline__ uint32_t abs_bits(float x) { return __float_as_uint(x) & 0x7FFFFFFFu; }
+
+/* Fast quantization is exact for the whole tile when the rounded-toward-
+ * zero product of its largest magnitude stays below 2^24. */
+__device__ __forceinline__ bool tile_fast_ok(uint32_t amax_bits, float inv)
+{
+    float am = __uint_as_float(amax_bits);
+    return am == am && fabsf(__fmul_rz(am, inv)) < 16777216.0f;
+}
+
 __device__ __forceinline__ uint32_t bswap32(uint32_t v) { return __byte_perm(v, 0, 0x0123); }
 
 /* ---------------------------------------------------------------------
- * Bit streams in shared memory.  A stream is a sequence of bytes; bits go
+ * Bit streams in shared memory.  A block is a sequence of bytes; bits go
  * MSB first within a byte, which is how the reference packs sign bits and
  * the low r bits of every magnitude (ZCCL/src/ZCCL_TypeManager.c:118-421,
- * :824-848).  Whole bytes written through put(v, 8k) keep their order.
+ * :824-848).  Whole bytes put as 8k-bit values keep their order.
  * ------------------------------------------------------------------- */
 
-/* Packs MSB-first bits into a ZEROED shared buffer starting at byte offset
- * o.  Finished 32-bit words are OR-ed in, so blocks that share a boundary
- * word (or several tiny blocks sharing one word) need no coordination and
- * the leading bits of a block's first word stay untouched.  The 64-bit
- * accumulator holds `nacc` pending bits right-aligned; flush() must run
- * before it passes 64 bits (puts of up to 32 bits with nacc < 32 are safe). */
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+/* OR a finished word into shared memory (the packing buffer starts zeroed,
+ * so neighbouring blocks that share a boundary word need no coordination). */
+__device__ __forceinline__ void sh_or(uint32_t saddr, uint32_t v)
+{
+    asm volatile("red.shared.or.b32 [%0], %1;" ::"r"(saddr), "r"(v) : "memory");
+}
+
+/* Packs MSB-first bits into a zeroed shared buffer from byte offset o.  The
+ * 64-bit accumulator holds nacc pending bits right-aligned; callers keep
+ * nacc < 32 before a put of up to 32 bits by calling flush(). */
 struct Packer {
-    uint32_t *w;
-    uint32_t wi, nacc;
+    uint32_t wa, nacc; /* shared address of the current word; pending bits */
     uint64_t acc;
 
-    __device__ __forceinline__ void init(uint32_t *words, uint32_t o)
+    __device__ __forceinline__ void init(uint32_t sbase, uint32_t o)
     {
-        w = words;
-        wi = o >> 2;
+        wa = sbase + (o & ~3u);
         nacc = (o & 3u) * 8u;
         acc = 0;
     }
-    /* append the low n bits of v (1 <= n <= 32, v < 2^n) */
-    __device__ __forceinline__ void put(uint32_t v, uint32_t n)
+    __device__ __forceinline__ void put(uint32_t v, uint32_t n) /* v < 2^n, n <= 32 */
     {
-        acc = (n < 32u ? acc << n : acc << 32) | v;
+        acc = (acc << n) | v;
         nacc += n;
     }
     __device__ __forceinline__ void flush()
     {
         if (nacc >= 32u) {
             nacc -= 32u;
-            atomicOr(&w[wi++], bswap32((uint32_t)(acc >> nacc)));
+            sh_or(wa, bswap32((uint32_t)(acc >> nacc)));
+            wa += 4;
         }
     }
     __device__ __forceinline__ void finish()
     {
         flush();
-        if (nacc) atomicOr(&w[wi], bswap32((uint32_t)(acc << (32u - nacc))));
+        if (nacc) sh_or(wa, bswap32((uint32_t)acc << (32u - nacc)));
     }
 };
 
-/* Reads MSB-first bits from byte offset o of a shared buffer.  refill()
- * guarantees at least 32 valid bits; gets totalling up to 32 bits may follow
- * one refill.  Loads whole aligned words, so it may read up to 8 bytes past
- * the last bit it returns (buffers carry slack). */
+/* Reads MSB-first bits from byte offset o of a shared word array.  After
+ * refill() at least 33 bits are buffered.  Loads whole aligned words, so it
+ * may read up to 8 bytes past the last bit it returns (buffers carry slack). */
 struct Reader {
     const uint32_t *w;
     uint32_t wi, nacc;
@@ -139,130 +164,177 @@ struct Reader {
             nacc += 32u;
         }
     }
-    /* next n bits, 1 <= n <= 32 */
-    __device__ __forceinline__ uint32_t get(uint32_t n)
+    __device__ __forceinline__ uint32_t get(uint32_t n) /* 1 <= n <= 32 */
     {
         uint32_t v = (uint32_t)(acc >> 32) >> (32u - n);
-        acc = n < 32u ? acc << n : acc << 32;
+        acc <<= n;
         nacc -= n;
         return v;
     }
 };
 
-/* The r-bit fields of a block, MSB first: the 32 elements of a full block
- * are r words exactly.  Four r-bit values are merged with multiply-adds into
- * one 4r-bit group (4r <= 28) before they enter the packer. */
-__device__ __forceinline__ void put_low_bits(Packer &pk, const uint32_t *m, uint32_t n, uint32_t r,
-                                             bool masked)
+/* One full block of 32 elements: magnitudes m[] (m[j] >> b == 0), the sign
+ * mask (element j at bit 31 - j) and the width b, packed at byte o of the
+ * zeroed shared buffer at sbase.  Straight-line code: the header and the 32
+ * sign bits, then the B = b/8 high bytes of each element (little-endian per
+ * element, four elements per word when B == 1), then the r = b%8 low bits of
+ * each element (four r-bit fields merged per put).  A zero-width block is a
+ * single 0x00 byte, already in the buffer. */
+__device__ __forceinline__ void encode_full(uint32_t sbase, uint32_t o, uint32_t b, uint32_t smask,
+                                            const uint32_t (&m)[32])
 {
-    const uint32_t mask = (1u << r) - 1u, p = 1u << r;
+    if (b == 0) return;
+    const uint32_t B = b >> 3, r = b & 7u;
+    Packer pk;
+    pk.init(sbase, o);
+    pk.put(b, 8);
+    pk.flush();
+    pk.put(smask, 32);
+    pk.flush();
+    if (B == 1) {
 #pragma unroll
-    for (uint32_t j = 0; j < 32; j += 4) {
-        if (j < n) {
+        for (int j = 0; j < 32; j += 4) {
+            uint32_t h = (((m[j] >> r) * 256u + (m[j + 1] >> r)) * 256u + (m[j + 2] >> r)) * 256u +
+                         (m[j + 3] >> r);
+            pk.put(h, 32);
+            pk.flush();
+        }
+    } else if (B > 1) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            pk.put(bswap32(m[j] >> r) >> (32u - 8u * B), 8u * B);
+            pk.flush();
+        }
+    }
+    if (r) {
+        const uint32_t p = 1u << r, mask = p - 1u;
+#pragma unroll
+        for (int j = 0; j < 32; j += 4) {
             uint32_t v0 = m[j], v1 = m[j + 1], v2 = m[j + 2], v3 = m[j + 3];
-            if (masked) {
+            if (B) {
                 v0 &= mask;
                 v1 &= mask;
                 v2 &= mask;
                 v3 &= mask;
             }
-            if (j + 4 <= n) {
-                pk.put(((v0 * p + v1) * p + v2) * p + v3, 4 * r);
-            } else { /* the ragged group of a short block */
-                pk.put(v0, r);
-                if (j + 1 < n) pk.put(v1, r);
-                if (j + 2 < n) pk.put(v2, r);
-            }
+            pk.put(((v0 * p + v1) * p + v2) * p + v3, 4u * r);
             pk.flush();
         }
     }
+    pk.finish();
 }
 
-/* Inverse of put_low_bits: ORs the r-bit fields into m[]. */
-__device__ __forceinline__ void get_low_bits(Reader &rd, uint32_t *m, uint32_t n, uint32_t r)
+/* Inverse of encode_full for a block of width b at byte o of the shared
+ * words w: d[j] = the int32 delta of element j (as uint32).  Returns the
+ * wrapped sum of the deltas. */
+__device__ __forceinline__ uint32_t decode_full(const uint32_t *w, uint32_t o, uint32_t b,
+                                                uint32_t (&d)[32])
 {
-    const uint32_t mask = (1u << r) - 1u;
 #pragma unroll
-    for (uint32_t j = 0; j < 32; j += 4) {
-        if (j < n) {
+    for (int j = 0; j < 32; j++) d[j] = 0;
+    if (b == 0) return 0;
+    const uint32_t B = b >> 3, r = b & 7u;
+    Reader rd;
+    rd.init(w, o + 1);
+    const uint32_t sg = rd.get(32);
+    if (B == 1) {
+#pragma unroll
+        for (int j = 0; j < 32; j += 4) {
             rd.refill();
-            if (j + 4 <= n) {
-                uint32_t q = rd.get(4 * r);
-                m[j] |= q >> (3 * r);
-                m[j + 1] |= (q >> (2 * r)) & mask;
-                m[j + 2] |= (q >> r) & mask;
-                m[j + 3] |= q & mask;
-            } else {
-                m[j] |= rd.get(r);
-                if (j + 1 < n) m[j + 1] |= rd.get(r);
-                if (j + 2 < n) m[j + 2] |= rd.get(r);
-            }
+            const uint32_t q = rd.get(32);
+            d[j] = (q >> 24) << r;
+            d[j + 1] = ((q >> 16) & 0xFFu) << r;
+            d[j + 2] = ((q >> 8) & 0xFFu) << r;
+            d[j + 3] = (q & 0xFFu) << r;
+        }
+    } else if (B > 1) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            rd.refill();
+            d[j] = bswap32(rd.get(8u * B) << (32u - 8u * B)) << r;
         }
     }
-}
-
-/* The B = b/8 high bytes of every element, little-endian per element
- * (ZCCL/src/ZCCL_TypeManager.c:34-47).  With B == 1 four elements fill one
- * word, merged with multiply-adds. */
-__device__ __forceinline__ void put_high_bytes(Packer &pk, const uint32_t *m, uint32_t n, uint32_t B,
-                                               uint32_t r)
-{
-    if (B == 1) {
+    if (r) {
+        const uint32_t mask = (1u << r) - 1u;
 #pragma unroll
-        for (uint32_t j = 0; j < 32; j += 4) {
-            if (j < n) {
-                uint32_t h0 = m[j] >> r, h1 = m[j + 1] >> r, h2 = m[j + 2] >> r, h3 = m[j + 3] >> r;
-                if (j + 4 <= n) {
-                    pk.put(((h0 * 256u + h1) * 256u + h2) * 256u + h3, 32);
-                } else {
-                    pk.put(h0, 8);
-                    if (j + 1 < n) pk.put(h1, 8);
-                    if (j + 2 < n) pk.put(h2, 8);
-                }
-                pk.flush();
-            }
-        }
-    } else {
-#pragma unroll
-        for (uint32_t j = 0; j < 32; j++) {
-            if (j < n) {
-                pk.put(bswap32(m[j] >> r) >> (32 - 8 * B), 8 * B);
-                pk.flush();
-            }
+        for (int j = 0; j < 32; j += 4) {
+            rd.refill();
+            const uint32_t q = rd.get(4u * r);
+            d[j] |= q >> (3u * r);
+            d[j + 1] |= (q >> (2u * r)) & mask;
+            d[j + 2] |= (q >> r) & mask;
+            d[j + 3] |= q & mask;
         }
     }
+    uint32_t sum = 0;
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+        const uint32_t s = (uint32_t)((int32_t)(sg << j) >> 31); /* all ones when negative */
+        d[j] = (d[j] ^ s) - s;
+        sum += d[j];
+    }
+    return sum;
 }
 
-/* Inverse of put_high_bytes: m[j] = high part << r. */
-__device__ __forceinline__ void get_high_bytes(Reader &rd, uint32_t *m, uint32_t n, uint32_t B,
-                                               uint32_t r)
+/* Any block (n elements, any width), one element at a time: separate
+ * streams for the header, the sign bits, the high bytes and the low bits.
+ * Used for short tail blocks, block sizes above 32 and tiles that need the
+ * exact slow quantization path.  elem(j, neg, mag) gives element j. */
+template <class Elem>
+__device__ __forceinline__ void encode_any(uint32_t sbase, uint32_t o, uint32_t b, uint32_t n,
+                                           Elem elem)
 {
-    if (B == 1) {
-#pragma unroll
-        for (uint32_t j = 0; j < 32; j += 4) {
-            if (j < n) {
-                rd.refill();
-                if (j + 4 <= n) {
-                    uint32_t q = rd.get(32);
-                    m[j] = (q >> 24) << r;
-                    m[j + 1] = ((q >> 16) & 0xFFu) << r;
-                    m[j + 2] = ((q >> 8) & 0xFFu) << r;
-                    m[j + 3] = (q & 0xFFu) << r;
-                } else {
-                    m[j] = rd.get(8) << r;
-                    if (j + 1 < n) m[j + 1] = rd.get(8) << r;
-                    if (j + 2 < n) m[j + 2] = rd.get(8) << r;
-                }
-            }
+    if (b == 0) return;
+    const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
+    const uint32_t mask = r ? (1u << r) - 1u : 0u;
+    Packer ph, ps, pb, pl;
+    ph.init(sbase, o);
+    ph.put(b, 8);
+    ph.finish();
+    ps.init(sbase, o + 1);
+    pb.init(sbase, o + 1 + ns);
+    pl.init(sbase, o + 1 + ns + B * n);
+    for (uint32_t j = 0; j < n; j++) {
+        uint32_t neg, mg;
+        elem(j, neg, mg);
+        ps.put(neg, 1);
+        ps.flush();
+        if (B) {
+            pb.put(bswap32(mg >> r) >> (32u - 8u * B), 8u * B);
+            pb.flush();
         }
-    } else {
-#pragma unroll
-        for (uint32_t j = 0; j < 32; j++) {
-            if (j < n) {
-                rd.refill();
-                m[j] = bswap32(rd.get(8 * B) << (32 - 8 * B)) << r;
-            }
+        if (r) {
+            pl.put(mg & mask, r);
+            pl.flush();
         }
+    }
+    ps.finish();
+    if (B) pb.finish();
+    if (r) pl.finish();
+}
+
+/* Element-at-a-time decoder for any block; sink(j, delta). */
+template <class Sink>
+__device__ __forceinline__ void decode_any(const uint32_t *w, uint32_t o, uint32_t b, uint32_t n,
+                                           Sink sink)
+{
+    if (b == 0) {
+        for (uint32_t j = 0; j < n; j++) sink(j, 0u);
+        return;
+    }
+    const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
+    Reader rs, rh, rl;
+    rs.init(w, o + 1);
+    rh.init(w, o + 1 + ns);
+    rl.init(w, o + 1 + ns + B * n);
+    for (uint32_t j = 0; j < n; j++) {
+        rs.refill();
+        rh.refill();
+        rl.refill();
+        uint32_t v = B ? bswap32(rh.get(8u * B) << (32u - 8u * B)) << r : 0u;
+        if (r) v |= rl.get(r);
+        if (rs.get(1)) v = 0u - v;
+        sink(j, v);
     }
 }
 
@@ -274,30 +346,9 @@ __device__ __forceinline__ void smem_zero(uint8_t *s, uint32_t nbytes)
     for (uint32_t i = threadIdx.x; i < (nbytes + 15u) >> 4; i += blockDim.x) s4[i] = z;
 }
 
-/* max over |x| as raw float bits: NaN ranks above +inf, so a NaN also fails
- * the fast-quantization test. */
-__device__ __forceinline__ uint32_t abs_bits(float x) { return __float_as_uint(x) & 0x7FFFFFFFu; }
-
-/* Fast quantization is exact for the whole tile when the rounded-toward-
- * zero product of its largest magnitude stays below 2^24 (see quantize()). */
-__device__ __forceinline__ bool tile_fast_ok(uint32_t amax_bits, float inv)
-{
-    float am = __uint_as_float(amax_bits);
-    return am == am && fabsf(__fmul_rz(am, inv)) < 16777216.0f;
-}
-
 /* ---------------------------------------------------------------------
- * TMA (cp.async.bulk) staging between global and shared memory.
- * The shared copy of a global byte range keeps the range's 16-byte phase:
- * global byte g lands at smem[phase + (g - start)], phase = start & 15, so
- * the 16-byte-aligned middle of the range moves with one bulk copy and the
- * ragged ends (< 16 bytes each) with plain byte accesses.
+ * TMA (cp.async.bulk) global -> shared, completion on an mbarrier
  * ------------------------------------------------------------------- */
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p)
-{
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
 
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
 {
@@ -332,6 +383,11 @@ __device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t parity, uint32
     atomicOr(err, ZERR_TIMEOUT);
 }
 
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 __device__ __forceinline__ void bulk_g2s(void *sdst, const void *gsrc, uint32_t bytes, uint64_t *bar)
 {
     asm volatile(
@@ -341,110 +397,26 @@ __device__ __forceinline__ void bulk_g2s(void *sdst, const void *gsrc, uint32_t 
         : "memory");
 }
 
-__device__ __forceinline__ void bulk_s2g(void *gdst, const void *ssrc, uint32_t bytes)
-{
-    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst),
-                 "r"(smem_u32(ssrc)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ void bulk_commit_and_wait()
-{
-    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
-}
-
-__device__ __forceinline__ void fence_proxy_async_smem()
-{
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-/* Stage global bytes [g, g + nbytes) into the 16-byte-aligned buffer s.
- * Called by every thread of the CTA; thread 0 issues the bulk copy and the
- * barrier arrival, threads 0..31 copy the ragged ends.  Returns the phase
- * (g & 15); the copy is complete after stage_in_wait(). */
-__device__ __forceinline__ uint32_t stage_in(uint8_t *s, const uint8_t *g, uint32_t nbytes,
-                                             uint64_t *bar)
-{
-    uintptr_t ga = (uintptr_t)g, ge = ga + nbytes;
-    uint32_t phase = (uint32_t)(ga & 15u);
-    uintptr_t a0 = (ga + 15u) & ~(uintptr_t)15u, a1 = ge & ~(uintptr_t)15u;
-    uint32_t tid = threadIdx.x;
-    if (a1 > a0) {
-        if (tid == 0) {
-            fence_proxy_async_smem(); /* earlier generic accesses of s before the async write */
-            mbar_expect_tx(bar, (uint32_t)(a1 - a0));
-            bulk_g2s(s + phase + (a0 - ga), (const void *)a0, (uint32_t)(a1 - a0), bar);
-        }
-        if (tid < 32) {
-            if (ga + tid < a0) s[phase + tid] = g[tid];
-            uintptr_t t = a1 + tid;
-            if (t < ge) s[phase + (t - ga)] = *(const uint8_t *)t;
-        }
-    } else {
-        if (tid == 0) mbar_expect_tx(bar, 0);
-        for (uint32_t i = tid; i < nbytes; i += blockDim.x) s[phase + i] = g[i];
-    }
-    return phase;
-}
-
-__device__ __forceinline__ void stage_in_wait(uint64_t *bar, uint32_t parity, uint32_t *err)
-{
-    mbar_wait(bar, parity, err);
-    __syncthreads();
-}
-
-/* Write shared bytes s[phase .. phase + nbytes) to global [g, g + nbytes),
- * where phase == (g & 15).  Every thread calls it after its last write to s;
- * returns once the bulk copy has completed. */
-__device__ __forceinline__ void stage_out(uint8_t *g, const uint8_t *s, uint32_t nbytes)
-{
-    fence_proxy_async_smem();
-    __syncthreads();
-    uintptr_t ga = (uintptr_t)g, ge = ga + nbytes;
-    uint32_t phase = (uint32_t)(ga & 15u);
-    uintptr_t a0 = (ga + 15u) & ~(uintptr_t)15u, a1 = ge & ~(uintptr_t)15u;
-    uint32_t tid = threadIdx.x;
-    if (a1 > a0) {
-        if (tid < 32) {
-            if (ga + tid < a0) g[tid] = s[phase + tid];
-            uintptr_t t = a1 + tid;
-            if (t < ge) *(uint8_t *)t = s[phase + (t - ga)];
-        }
-        if (tid == 0) {
-            bulk_s2g((void *)a0, s + phase + (a0 - ga), (uint32_t)(a1 - a0));
-            bulk_commit_and_wait();
-        }
-    } else {
-        for (uint32_t i = tid; i < nbytes; i += blockDim.x) g[i] = s[phase + i];
-    }
-}
-
-/* Issue (thread 0 only) a TMA bulk copy of the 16-byte-aligned superset
- * [floor16(g), ceil16(g + nbytes)) into the 16-byte-aligned buffer s and
- * arm the barrier; returns g & 15, the offset of g inside s.  The superset
- * only adds bytes of 16-byte chunks that already contain bytes of the range,
- * so it never touches a page the range does not.  Every thread may call it
- * to learn the phase; only thread 0 issues. */
-__device__ __forceinline__ uint32_t tma_load_superset(uint8_t *s, const uint8_t *g, uint32_t nbytes,
-                                                      uint64_t *bar)
+/* Thread 0 only: TMA bulk copy of the 16-byte-aligned superset
+ * [floor16(g), ceil16(g + nbytes)) into the 16-byte-aligned buffer s, arming
+ * the barrier with its byte count.  The superset only adds bytes of 16-byte
+ * chunks that already contain bytes of the range, so it never touches a page
+ * the range does not.  The range starts at s + (g & 15). */
+__device__ __forceinline__ void tma_load_superset(uint8_t *s, const uint8_t *g, uint32_t nbytes,
+                                                  uint64_t *bar)
 {
     uintptr_t a0 = (uintptr_t)g & ~(uintptr_t)15u;
     uintptr_t a1 = ((uintptr_t)g + nbytes + 15u) & ~(uintptr_t)15u;
-    if (threadIdx.x == 0) {
-        fence_proxy_async_smem();
-        mbar_expect_tx(bar, (uint32_t)(a1 - a0));
-        if (a1 > a0) bulk_g2s(s, (const void *)a0, (uint32_t)(a1 - a0), bar);
-    }
-    return (uint32_t)((uintptr_t)g & 15u);
+    fence_proxy_async_smem(); /* earlier generic accesses of s before the async write */
+    mbar_expect_tx(bar, (uint32_t)(a1 - a0));
+    if (a1 > a0) bulk_g2s(s, (const void *)a0, (uint32_t)(a1 - a0), bar);
 }
 
 /* Write shared bytes s[0, nbytes) to global [g, g + nbytes) for any
  * alignment of g.  16-byte-aligned global chunks get one vector store each,
- * assembled from two aligned shared loads and a funnel shift; the ragged
+ * assembled from two aligned shared loads and funnel shifts; the ragged
  * ends (shared with neighbouring tiles) are stored byte by byte.  s must be
- * 16-byte aligned with 32 readable bytes of slack.  Called by all threads;
- * ends with the data written (no trailing barrier). */
+ * 16-byte aligned with 32 readable bytes of slack.  Called by all threads. */
 __device__ __forceinline__ void store_realign(uint8_t *g, const uint8_t *s, uint32_t nbytes)
 {
     const uintptr_t g0 = (uintptr_t)g, g1 = g0 + nbytes;
@@ -455,31 +427,29 @@ __device__ __forceinline__ void store_realign(uint8_t *g, const uint8_t *s, uint
         return;
     }
     const uint32_t d = (uint32_t)(a0 - g0); /* shared offset of the first aligned chunk */
-    if (tid < d) g[tid] = s[tid];
     const uint32_t tail = (uint32_t)(g1 - a1);
-    if (tid >= 32 && tid - 32 < tail) {
-        uint32_t i = (uint32_t)(a1 - g0) + (tid - 32);
-        g[i] = s[i];
+    for (uint32_t i = tid; i < d + tail; i += blockDim.x) { /* ragged ends, any block size */
+        const uint32_t k = i < d ? i : (uint32_t)(a1 - g0) + (i - d);
+        g[k] = s[k];
     }
     const uint32_t nch = (uint32_t)((a1 - a0) >> 4), q = d >> 2, sh = (d & 3u) * 8u;
     const uint4 *s4 = reinterpret_cast<const uint4 *>(s);
     uint4 *g4 = reinterpret_cast<uint4 *>(a0);
     for (uint32_t c = tid; c < nch; c += blockDim.x) {
         uint4 lo = s4[c], hi = s4[c + 1];
-        uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-        uint32_t o[5];
+        uint32_t o0, o1, o2, o3, o4;
         /* q is the same for every thread of the tile: a uniform branch */
         switch (q) {
-        case 0: o[0] = w[0]; o[1] = w[1]; o[2] = w[2]; o[3] = w[3]; o[4] = w[4]; break;
-        case 1: o[0] = w[1]; o[1] = w[2]; o[2] = w[3]; o[3] = w[4]; o[4] = w[5]; break;
-        case 2: o[0] = w[2]; o[1] = w[3]; o[2] = w[4]; o[3] = w[5]; o[4] = w[6]; break;
-        default: o[0] = w[3]; o[1] = w[4]; o[2] = w[5]; o[3] = w[6]; o[4] = w[7]; break;
+        case 0: o0 = lo.x; o1 = lo.y; o2 = lo.z; o3 = lo.w; o4 = hi.x; break;
+        case 1: o0 = lo.y; o1 = lo.z; o2 = lo.w; o3 = hi.x; o4 = hi.y; break;
+        case 2: o0 = lo.z; o1 = lo.w; o2 = hi.x; o3 = hi.y; o4 = hi.z; break;
+        default: o0 = lo.w; o1 = hi.x; o2 = hi.y; o3 = hi.z; o4 = hi.w; break;
         }
         uint4 v;
-        v.x = __funnelshift_r(o[0], o[1], sh);
-        v.y = __funnelshift_r(o[1], o[2], sh);
-        v.z = __funnelshift_r(o[2], o[3], sh);
-        v.w = __funnelshift_r(o[3], o[4], sh);
+        v.x = __funnelshift_r(o0, o1, sh);
+        v.y = __funnelshift_r(o1, o2, sh);
+        v.z = __funnelshift_r(o2, o3, sh);
+        v.w = __funnelshift_r(o3, o4, sh);
         g4[c] = v;
     }
 }
@@ -523,8 +493,9 @@ __device__ __forceinline__ uint32_t cta_excl_scan(uint32_t v, uint32_t *wsum, ui
 /* ---------------------------------------------------------------------
  * Decoupled look-back (Merrill & Garland 2016).  status[t] packs a 2-bit
  * flag (1 = aggregate of tile t only, 2 = inclusive prefix through t) over
- * a 62-bit value.  Tiles are taken in ticket order, so every tile a CTA
- * waits on belongs to a CTA that is already running.
+ * a 62-bit value; values add modulo 2^62.  Tiles are taken in ticket order,
+ * so every tile a CTA waits on belongs to a CTA that is already running and
+ * never waits on a later tile.
  * ------------------------------------------------------------------- */
 #define LB_FLAG_A (1ull << 62)
 #define LB_FLAG_P (2ull << 62)
@@ -549,8 +520,9 @@ __device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v)
     return v;
 }
 
-/* Lane 0 of the publishing warp: make this tile's aggregate (or, for a
- * first tile, its inclusive value start + agg) visible to successors. */
+/* Any lane of the publishing warp may call it; lane 0 stores: this tile's
+ * aggregate, or, for a first tile (no predecessor in its scan), its
+ * inclusive value start + agg. */
 __device__ __forceinline__ void lb_publish(uint64_t *status, uint64_t tile, uint64_t agg, bool first,
                                            uint64_t start)
 {
@@ -560,88 +532,65 @@ __device__ __forceinline__ void lb_publish(uint64_t *status, uint64_t tile, uint
 }
 
 /* Called by all lanes of one warp after lb_publish: returns the exclusive
- * prefix of the tile and publishes its inclusive value.  Same semantics as
- * lookback(). */
+ * prefix of the tile (the sum of every tile back to and including the
+ * nearest one that published an inclusive value, or `start` for a first
+ * tile) and publishes the tile's inclusive value.  Each round inspects 256
+ * predecessors (lane l reads tiles pos - l - 32k, k < 8, all loads in flight
+ * together): with a persistent grid several hundred tiles are in flight at
+ * once, and the nearest inclusive value is typically that far back.  A
+ * predecessor that never publishes makes the wait give up after a bounded
+ * number of polls: ZERR_TIMEOUT is set, the missing value counts as 0 and
+ * the inclusive value is still published, so successors never hang. */
 static __device__ __noinline__ uint64_t lb_resolve(uint64_t *status, uint64_t tile, uint64_t agg,
                                                    bool first, uint64_t start, uint32_t *err)
 {
-    uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lane = threadIdx.x & 31u;
     if (first) return start;
     uint64_t prefix = 0;
     int64_t pos = (int64_t)tile - 1;
     uint32_t spins = 0;
     for (;;) {
-        int64_t idx = pos - (int64_t)lane;
-        uint64_t v = idx >= 0 ? ld_acquire(status + idx) : LB_FLAG_P;
-        uint32_t flag = (uint32_t)(v >> 62);
-        uint32_t pm = __ballot_sync(0xffffffffu, flag == 2u);
-        uint32_t xm = __ballot_sync(0xffffffffu, flag == 0u);
-        uint32_t fp = pm ? (uint32_t)(__ffs(pm) - 1) : 32u;
-        uint32_t need = fp >= 31u ? 0xffffffffu : ((2u << fp) - 1u);
-        if (xm & need) {
+        uint64_t v[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            int64_t idx = pos - (int64_t)(lane + 32u * k);
+            v[k] = idx >= 0 ? ld_acquire(status + idx) : LB_FLAG_P; /* before tile 0: value 0 */
+        }
+        /* nearest inclusive value: smallest distance lane + 32k flagged P */
+        uint32_t kp = 8, fp = 31, pending = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t flag = (uint32_t)(v[k] >> 62);
+            const uint32_t pm = __ballot_sync(0xffffffffu, flag == 2u);
+            const uint32_t xm = __ballot_sync(0xffffffffu, flag == 0u);
+            if (kp == 8) {
+                if (pm) {
+                    kp = k;
+                    fp = (uint32_t)(__ffs(pm) - 1);
+                    pending |= xm & ((1u << fp) - 1u);
+                } else {
+                    pending |= xm;
+                }
+            }
+        }
+        if (pending) {
             if (++spins < (1u << 22)) {
                 __nanosleep(32);
                 continue;
             }
+            /* give up: missing values count as 0 */
             if (lane == 0) atomicOr(err, ZERR_TIMEOUT);
-            if (flag == 0u) {
-                v = 0;
-                flag = 1u;
-            }
         }
-        uint64_t c = (lane <= fp && flag != 0u) ? (v & LB_VAL) : 0ull;
-        prefix += warp_sum_u64(c);
-        if (fp < 32u) break;
-        pos -= 32;
-        spins = 0;
-    }
-    if (lane == 0) st_release(status + tile, LB_FLAG_P | ((prefix + agg) & LB_VAL));
-    return prefix & LB_VAL;
-}
-
-/* Called by all lanes of one warp.  Publishes this tile's aggregate `agg`
- * (or, when `first`, the inclusive value start + agg) and returns the
- * exclusive prefix: the sum of every tile back to and including the nearest
- * tile that published an inclusive value (or `start` when first).  Values
- * add modulo 2^62.  A predecessor that never publishes makes the wait give
- * up after a bounded number of polls: ZERR_TIMEOUT is set, the missing value
- * counts as 0 and the inclusive value is still published, so successors
- * never hang. */
-static __device__ __noinline__ uint64_t lookback(uint64_t *status, uint64_t tile, uint64_t agg, bool first,
-                                          uint64_t start, uint32_t *err)
-{
-    uint32_t lane = threadIdx.x & 31u;
-    if (first) {
-        if (lane == 0) st_release(status + tile, LB_FLAG_P | ((start + agg) & LB_VAL));
-        return start;
-    }
-    if (lane == 0) st_release(status + tile, LB_FLAG_A | (agg & LB_VAL));
-    uint64_t prefix = 0;
-    int64_t pos = (int64_t)tile - 1;
-    uint32_t spins = 0;
-    for (;;) {
-        int64_t idx = pos - (int64_t)lane;
-        uint64_t v = idx >= 0 ? ld_acquire(status + idx) : LB_FLAG_P;
-        uint32_t flag = (uint32_t)(v >> 62);
-        uint32_t pm = __ballot_sync(0xffffffffu, flag == 2u);
-        uint32_t xm = __ballot_sync(0xffffffffu, flag == 0u);
-        uint32_t fp = pm ? (uint32_t)(__ffs(pm) - 1) : 32u;
-        uint32_t need = fp >= 31u ? 0xffffffffu : ((2u << fp) - 1u);
-        if (xm & need) {
-            if (++spins < (1u << 22)) {
-                __nanosleep(64);
-                continue;
-            }
-            if (lane == 0) atomicOr(err, ZERR_TIMEOUT);
-            if (flag == 0u) {
-                v = 0;
-                flag = 1u;
-            }
+        uint64_t c = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const bool ready = (v[k] >> 62) != 0;
+            if ((uint32_t)k < kp || ((uint32_t)k == kp && lane <= fp))
+                c += ready ? (v[k] & LB_VAL) : 0ull;
         }
-        uint64_t c = (lane <= fp && flag != 0u) ? (v & LB_VAL) : 0ull;
         prefix += warp_sum_u64(c);
-        if (fp < 32u) break;
-        pos -= 32;
+        if (kp < 8) break;
+        pos -= 256;
         spins = 0;
     }
     if (lane == 0) st_release(status + tile, LB_FLAG_P | ((prefix + agg) & LB_VAL));

@@ -7,7 +7,9 @@
  *   1. its floats (and the element before them) arrived by a TMA bulk copy
  *      issued while the previous tile was being coded (double buffering);
  *      a warp-cooperative transpose puts every block in its own padded row,
- *      so the per-thread walk below has no bank conflicts;
+ *      so the per-thread walk below has no bank conflicts, and finds the
+ *      tile's largest magnitude, which decides whether the one-multiply
+ *      quantization is exact for the whole tile;
  *   2. every thread quantizes its block (truncation, ZCCL_float.c:580),
  *      forms the running deltas (ZCCL_float.c:581-582; the element before the
  *      block supplies the first one), sign mask, largest magnitude, width
@@ -20,6 +22,9 @@
  *   4. the packed tile goes out with 16-byte vector stores realigned to its
  *      byte offset, and the tile records the side index: block widths, its
  *      byte offset, and the quantized value before it.
+ * Full 32-element blocks with exact fast quantization take straight-line
+ * code; short tail blocks, blocks above 32 elements and tiles that need the
+ * slow exact quantization take an element-at-a-time path.
  */
 #include "zkern.cuh"
 
@@ -49,9 +54,8 @@ __global__ void __launch_bounds__(128) k_compress(const CompressArgs a)
     uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160); /* [0..1] tiles, [2] prefix */
     uint32_t *s_amax = reinterpret_cast<uint32_t *>(smem + 192);
     float *rows = reinterpret_cast<float *>(smem + a.sm.rows);
-    uint8_t *inb[2] = {smem + a.sm.in0, smem + a.sm.in1};
     uint8_t *outs = smem + a.sm.out;
-    uint32_t *outw = reinterpret_cast<uint32_t *>(outs);
+    const uint32_t outs_sa = smem_u32(outs);
 
     const ZGeom &g = a.g;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, nw = blockDim.x >> 5;
@@ -61,7 +65,7 @@ __global__ void __launch_bounds__(128) k_compress(const CompressArgs a)
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
-        bc[0] = claim_and_load(a, inb[0], &bar[0]);
+        bc[0] = claim_and_load(a, smem + a.sm.in0, &bar[0]);
         *s_amax = 0;
     }
     __syncthreads();
@@ -70,21 +74,22 @@ __global__ void __launch_bounds__(128) k_compress(const CompressArgs a)
         const uint32_t cb = it & 1u;
         const uint64_t tile = bc[cb];
         if (tile >= g.ntiles) break;
-        if (tid == 0) bc[cb ^ 1u] = claim_and_load(a, inb[cb ^ 1u], &bar[cb ^ 1u]);
+        if (tid == 0)
+            bc[cb ^ 1u] = claim_and_load(a, smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u]);
         ZTile z;
         zg_tile(&g, tile, &z);
 
-        /* 1. wait for this tile's floats, transpose blocks into rows and
-         *    find the largest magnitude (decides the quantization path) */
+        /* 1. wait for this tile's floats, transpose blocks into rows, find
+         *    the largest magnitude */
         mbar_wait(&bar[cb], (it >> 1) & 1u, a.w.err);
         const float *xin = reinterpret_cast<const float *>(
-            inb[cb] + ((uintptr_t)(a.x + (z.e_first - 1)) & 15u));
+            smem + (cb ? a.sm.in1 : a.sm.in0) + ((uintptr_t)(a.x + (z.e_first - 1)) & 15u));
         const float xprev0 = xin[0]; /* the head, or the last element of the previous tile */
         uint32_t amax = abs_bits(xprev0);
         for (uint32_t k = warp; k < z.nblk; k += nw) {
-            uint32_t n = zg_block_len(z.seg_len, L, z.blk0 + k);
+            const uint32_t n = zg_block_len(z.seg_len, L, z.blk0 + k);
             for (uint32_t j = lane; j < n; j += 32) {
-                float v = xin[1 + k * L + j];
+                const float v = xin[1 + k * L + j];
                 amax = max(amax, abs_bits(v));
                 rows[k * stride + j] = v;
             }
@@ -95,35 +100,34 @@ __global__ void __launch_bounds__(128) k_compress(const CompressArgs a)
         const bool fastq = tile_fast_ok(*s_amax, a.inv);
 
         /* 2. quantize, delta, width */
-        uint32_t b = 0, size = 0, n = 0, smask = 0, mx = 0;
-        uint32_t m[FAST ? 32 : 1];
-        float xp = 0.0f;
-        if (tid < z.nblk) {
-            n = zg_block_len(z.seg_len, L, z.blk0 + tid);
-            const float *row = rows + tid * stride;
-            xp = tid == 0 ? xprev0 : rows[(tid - 1) * stride + L - 1];
-            int32_t qp = fastq ? quantize_fast(xp, a.inv) : quantize(xp, a.inv, bad);
-            if (FAST) {
+        const bool own = tid < z.nblk;
+        const uint32_t n = own ? zg_block_len(z.seg_len, L, z.blk0 + tid) : 0u;
+        const bool full = FAST && fastq && n == 32; /* straight-line path */
+        const float *row = rows + tid * stride;
+        const float xp = !own ? 0.0f : (tid == 0 ? xprev0 : rows[(tid - 1) * stride + L - 1]);
+        uint32_t b = 0, size = 0, smask = 0;
+        uint32_t m[32];
+        if (full) {
+            int32_t qp = quantize_fast(xp, a.inv);
+            uint32_t mx = 0;
 #pragma unroll
-                for (uint32_t j = 0; j < 32; j++) {
-                    uint32_t mg = 0;
-                    if (j < n) {
-                        int32_t q = fastq ? quantize_fast(row[j], a.inv) : quantize(row[j], a.inv, bad);
-                        int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
-                        qp = q;
-                        mg = (uint32_t)abs(d); /* |INT_MIN| wraps to 2^31, as in the reference */
-                        smask |= ((uint32_t)d >> 31) << (31 - j);
-                        mx = max(mx, mg);
-                    }
-                    m[j] = mg;
-                }
-            } else {
-                for (uint32_t j = 0; j < n; j++) {
-                    int32_t q = quantize(row[j], a.inv, bad);
-                    int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
-                    qp = q;
-                    mx = max(mx, (uint32_t)abs(d));
-                }
+            for (int j = 0; j < 32; j++) {
+                const int32_t q = quantize_fast(row[j], a.inv);
+                const int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
+                qp = q;
+                smask = (smask << 1) | ((uint32_t)d >> 31);
+                m[j] = (uint32_t)abs(d); /* |INT_MIN| wraps to 2^31, as in the reference */
+                mx = max(mx, m[j]);
+            }
+            b = width_of(mx, a.wt);
+            size = zg_block_bytes(b, 32);
+        } else if (own) {
+            int32_t qp = fastq ? quantize_fast(xp, a.inv) : quantize(xp, a.inv, bad);
+            uint32_t mx = 0;
+            for (uint32_t j = 0; j < n; j++) {
+                const int32_t q = fastq ? quantize_fast(row[j], a.inv) : quantize(row[j], a.inv, bad);
+                mx = max(mx, (uint32_t)abs((int32_t)((uint32_t)q - (uint32_t)qp)));
+                qp = q;
             }
             b = width_of(mx, a.wt);
             size = zg_block_bytes(b, n);
@@ -135,66 +139,25 @@ __global__ void __launch_bounds__(128) k_compress(const CompressArgs a)
         const uint32_t off = cta_excl_scan(size, wsum, &total);
         total += headb;
         if (warp == 0) lb_publish(a.w.status, tile, total, tile == 0, 0);
-
         const int32_t qprev0 = fastq ? quantize_fast(xprev0, a.inv) : quantize(xprev0, a.inv, bad);
         smem_zero(outs, total + 8);
         __syncthreads();
-        if (z.has_head && tid == 0) {
-#pragma unroll
-            for (int k = 0; k < 4; k++) outs[k] = (uint8_t)((uint32_t)qprev0 >> (8 * k));
-        }
-        if (tid < z.nblk) {
-            const uint32_t o = headb + off;
-            const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
-            if (FAST) {
-                Packer pk;
-                pk.init(outw, o);
-                pk.put(b, 8);
-                pk.flush();
-                if (b) {
-                    pk.put(smask >> (32 - 8 * ns), 8 * ns);
-                    pk.flush();
-                    if (B) put_high_bytes(pk, m, n, B, r);
-                    if (r) put_low_bits(pk, m, n, r, B > 0);
-                }
-                pk.finish();
-            } else {
-                Packer ph;
-                ph.init(outw, o);
-                ph.put(b, 8);
-                ph.finish();
-                if (b) {
-                    Packer ws, wh, wl;
-                    ws.init(outw, o + 1);
-                    wh.init(outw, o + 1 + ns);
-                    wl.init(outw, o + 1 + ns + B * n);
-                    const float *row = rows + tid * stride;
-                    int32_t qp = fastq ? quantize_fast(xp, a.inv) : quantize(xp, a.inv, bad);
-                    const uint32_t mask = r ? (1u << r) - 1u : 0u;
-                    for (uint32_t j = 0; j < n; j++) {
-                        int32_t q = fastq ? quantize_fast(row[j], a.inv) : quantize(row[j], a.inv, bad);
-                        int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
-                        qp = q;
-                        uint32_t mg = (uint32_t)abs(d);
-                        ws.put((uint32_t)d >> 31, 1);
-                        ws.flush();
-                        if (B) {
-                            wh.put(bswap32(mg >> r) >> (32 - 8 * B), 8 * B);
-                            wh.flush();
-                        }
-                        if (r) {
-                            wl.put(mg & mask, r);
-                            wl.flush();
-                        }
-                    }
-                    ws.finish();
-                    if (B) wh.finish();
-                    if (r) wl.finish();
-                }
-            }
+        if (z.has_head && tid == 0) *reinterpret_cast<int32_t *>(outs) = qprev0;
+        const uint32_t o = headb + off;
+        if (full) {
+            encode_full(outs_sa, o, b, smask, m);
+        } else if (own) {
+            int32_t qp = fastq ? quantize_fast(xp, a.inv) : quantize(xp, a.inv, bad);
+            encode_any(outs_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
+                const int32_t q = fastq ? quantize_fast(row[j], a.inv) : quantize(row[j], a.inv, bad);
+                const int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
+                qp = q;
+                neg = (uint32_t)d >> 31;
+                mg = (uint32_t)abs(d);
+            });
         }
         if (warp == 0) {
-            uint64_t prefix = lb_resolve(a.w.status, tile, total, tile == 0, 0, a.w.err);
+            const uint64_t prefix = lb_resolve(a.w.status, tile, total, tile == 0, 0, a.w.err);
             if (lane == 0) bc[2] = prefix;
         }
         __syncthreads();
@@ -203,19 +166,19 @@ __global__ void __launch_bounds__(128) k_compress(const CompressArgs a)
         const uint64_t base = 8ull * g.T + bc[2];
         const bool fits = base + total <= a.cap; /* uniform over the CTA */
         if (!fits) bad |= ZERR_CAPACITY;
-        if (tid < z.nblk) a.idx.widths[z.gblk0 + tid] = (uint8_t)b;
+        if (own) a.idx.widths[z.gblk0 + tid] = (uint8_t)b;
         if (tid == 0) {
             a.idx.tile_off[tile] = base;
             a.idx.tile_qprev[tile] = qprev0;
             if (fits && z.has_head && z.seg < g.T) {
-                uint64_t h = base - 8ull * g.T;
+                const uint64_t h = base - 8ull * g.T;
 #pragma unroll
                 for (int k = 0; k < 8; k++) a.out[8ull * z.seg + k] = (uint8_t)(h >> (8 * k));
             }
             if (tile == g.ntiles - 1) *a.idx.size = base + total;
+            *s_amax = 0;
         }
         if (fits) store_realign(a.out + base, outs, total);
-        if (tid == 0) *s_amax = 0;
         __syncthreads(); /* rows, outs, bc[2] and the maximum are reused by the next tile */
     }
     if (bad) atomicOr(a.w.err, bad);

@@ -75,7 +75,6 @@ __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
     uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160);     /* [0,1] tiles, [2] q0 */
     uint64_t *s_base = reinterpret_cast<uint64_t *>(smem + 192); /* [2] */
     float *rows = reinterpret_cast<float *>(smem + a.sm.rows);
-    uint8_t *inb[2] = {smem + a.sm.in0, smem + a.sm.in1};
 
     const ZGeom &g = a.g;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, nw = blockDim.x >> 5;
@@ -93,7 +92,7 @@ __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
     }
     __syncthreads();
     BlockSlot cur = {0, 0, 0};
-    if (bc[0] < g.ntiles) cur = stage_tile(a, bc[0], inb[0], &bar[0], wsum, &s_base[0], bad);
+    if (bc[0] < g.ntiles) cur = stage_tile(a, bc[0], smem + a.sm.in0, &bar[0], wsum, &s_base[0], bad);
 
     for (uint32_t it = 0;; it++) {
         const uint32_t cb = it & 1u;
@@ -108,60 +107,33 @@ __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
         __syncthreads();
         BlockSlot nxt = {0, 0, 0};
         if (bc[cb ^ 1u] < g.ntiles)
-            nxt = stage_tile(a, bc[cb ^ 1u], inb[cb ^ 1u], &bar[cb ^ 1u], wsum, &s_base[cb ^ 1u],
-                             bad);
+            nxt = stage_tile(a, bc[cb ^ 1u], smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u], wsum,
+                             &s_base[cb ^ 1u], bad);
 
         /* 2. unpack this tile's deltas */
         mbar_wait(&bar[cb], (it >> 1) & 1u, a.w.err);
+        const uint8_t *buf = smem + (cb ? a.sm.in1 : a.sm.in0);
+        const uint32_t *sw = reinterpret_cast<const uint32_t *>(buf);
         const uint32_t ph = (uint32_t)((uintptr_t)(a.in + s_base[cb]) & 15u);
-        const uint8_t *tb = inb[cb] + ph;
-        const uint32_t *sw = reinterpret_cast<const uint32_t *>(inb[cb]);
         int32_t head = 0;
         if (z.has_head) {
             uint32_t h = 0;
 #pragma unroll
-            for (int k = 0; k < 4; k++) h |= (uint32_t)tb[k] << (8 * k);
+            for (int k = 0; k < 4; k++) h |= (uint32_t)buf[ph + k] << (8 * k);
             head = (int32_t)h;
         }
         const uint32_t headb = z.has_head ? 4u : 0u;
         const uint32_t o = ph + headb + cur.off; /* this block, in buffer coordinates */
         const uint32_t b = cur.b, n = cur.n;
-        uint32_t d[FAST ? 32 : 1];
+        const bool own = tid < z.nblk;
+        const bool full = FAST && own && n == 32;
+        uint32_t d[32];
         uint32_t bsum = 0;
-        if (tid < z.nblk) {
-            if (inb[cb][o] != b) bad |= ZERR_CORRUPT;
-            if (FAST) {
-#pragma unroll
-                for (uint32_t j = 0; j < 32; j++) d[j] = 0;
-                if (b) {
-                    const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
-                    Reader rd;
-                    rd.init(sw, o + 1);
-                    const uint32_t sg = rd.get(8 * ns) << (32 - 8 * ns);
-                    if (B) get_high_bytes(rd, d, n, B, r);
-                    if (r) get_low_bits(rd, d, n, r);
-#pragma unroll
-                    for (uint32_t j = 0; j < 32; j++) {
-                        if ((sg >> (31 - j)) & 1u) d[j] = 0u - d[j];
-                        bsum += d[j];
-                    }
-                }
-            } else if (b) {
-                const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
-                Reader rs, rh, rl;
-                rs.init(sw, o + 1);
-                rh.init(sw, o + 1 + ns);
-                rl.init(sw, o + 1 + ns + B * n);
-                for (uint32_t j = 0; j < n; j++) {
-                    rh.refill();
-                    rl.refill();
-                    rs.refill();
-                    uint32_t v = B ? bswap32(rh.get(8 * B) << (32 - 8 * B)) << r : 0u;
-                    if (r) v |= rl.get(r);
-                    if (rs.get(1)) v = 0u - v;
-                    bsum += v;
-                }
-            }
+        if (own && buf[o] != b) bad |= ZERR_CORRUPT;
+        if (full) {
+            bsum = decode_full(sw, o, b, d);
+        } else if (own) { /* short or long block: sum now, decode again for the values */
+            decode_any(sw, o, b, n, [&](uint32_t, uint32_t v) { bsum += v; });
         }
 
         /* 3. starting value of every block */
@@ -171,7 +143,8 @@ __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
             if (tid == 0) bc[2] = (uint32_t)(z.has_head ? head : a.idx.tile_qprev[tile]);
         } else if (warp == 0) {
             lb_publish(a.w.status, tile, tsum, z.has_head != 0, (uint32_t)head);
-            uint64_t q0 = lb_resolve(a.w.status, tile, tsum, z.has_head != 0, (uint32_t)head, a.w.err);
+            const uint64_t q0 =
+                lb_resolve(a.w.status, tile, tsum, z.has_head != 0, (uint32_t)head, a.w.err);
             if (lane == 0) {
                 bc[2] = (uint32_t)q0;
                 a.idx.tile_qprev[tile] = (int32_t)(uint32_t)q0;
@@ -181,41 +154,25 @@ __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
         const uint32_t q0 = (uint32_t)bc[2];
 
         /* 4. values into rows, then out */
-        if (tid < z.nblk) {
+        float *row = rows + tid * stride;
+        if (full) {
             uint32_t q = q0 + pre;
-            float *row = rows + tid * stride;
-            if (FAST) {
 #pragma unroll
-                for (uint32_t j = 0; j < 32; j++) {
-                    q += d[j];
-                    if (j < n) row[j] = __fmul_rn(__int2float_rn((int32_t)q), a.eb);
-                }
-            } else {
-                const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
-                Reader rs, rh, rl;
-                if (b) {
-                    rs.init(sw, o + 1);
-                    rh.init(sw, o + 1 + ns);
-                    rl.init(sw, o + 1 + ns + B * n);
-                }
-                for (uint32_t j = 0; j < n; j++) {
-                    if (b) {
-                        rh.refill();
-                        rl.refill();
-                        rs.refill();
-                        uint32_t v = B ? bswap32(rh.get(8 * B) << (32 - 8 * B)) << r : 0u;
-                        if (r) v |= rl.get(r);
-                        if (rs.get(1)) v = 0u - v;
-                        q += v;
-                    }
-                    row[j] = __fmul_rn(__int2float_rn((int32_t)q), a.eb);
-                }
+            for (int j = 0; j < 32; j++) {
+                q += d[j];
+                row[j] = __fmul_rn(__int2float_rn((int32_t)q), a.eb);
             }
+        } else if (own) {
+            uint32_t q = q0 + pre;
+            decode_any(sw, o, b, n, [&](uint32_t j, uint32_t v) {
+                q += v;
+                row[j] = __fmul_rn(__int2float_rn((int32_t)q), a.eb);
+            });
         }
         if (z.has_head && tid == 0) a.y[z.seg_start] = __fmul_rn(__int2float_rn(head), a.eb);
         __syncthreads();
         for (uint32_t k = warp; k < z.nblk; k += nw) {
-            uint32_t nk = zg_block_len(z.seg_len, L, z.blk0 + k);
+            const uint32_t nk = zg_block_len(z.seg_len, L, z.blk0 + k);
             float *dst = a.y + z.e_first + (uint64_t)k * L;
             for (uint32_t j = lane; j < nk; j += 32) dst[j] = rows[k * stride + j];
         }

@@ -16,9 +16,9 @@
  * scanned from its width index and its bytes are already in flight.
  * Zero-width input blocks are skipped without touching their bytes.  After
  * the last input the sum is re-encoded like the compressor does (width,
- * scan, early look-back publish, OR-packing, realigned vector stores) and
- * the output's side index is written; its starting value per tile is the
- * sum of the inputs' values.
+ * scan, early look-back publish, packing, realigned vector stores) and the
+ * output's side index is written; its starting value per tile is the sum of
+ * the inputs' values.
  */
 #include "zkern.cuh"
 
@@ -27,6 +27,15 @@ namespace {
 struct BlockSlot {
     uint32_t b, n, off;
 };
+
+/* acc[j] for a runtime j (short tail blocks only). */
+__device__ __forceinline__ uint32_t &pick(uint32_t (&acc)[32], uint32_t j)
+{
+#pragma unroll
+    for (int k = 0; k < 31; k++)
+        if ((uint32_t)k == j) return acc[k];
+    return acc[31];
+}
 
 /* All threads: sizes of input p's blocks in tile t, their offsets, and
  * (thread 0) the TMA copy of those bytes into buf. */
@@ -75,9 +84,8 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
     uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160);     /* [0] next tile, [1] prefix */
     uint64_t *s_base = reinterpret_cast<uint64_t *>(smem + 192); /* [2] */
     uint32_t *acc_rows = reinterpret_cast<uint32_t *>(smem + a.sm.rows);
-    uint8_t *inb[2] = {smem + a.sm.in0, smem + a.sm.in1};
     uint8_t *outs = smem + a.sm.out;
-    uint32_t *outw = reinterpret_cast<uint32_t *>(outs);
+    const uint32_t outs_sa = smem_u32(outs);
 
     const ZGeom &g = a.g;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -94,9 +102,9 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
     __syncthreads();
     uint64_t tile = bc[0];
     if (tile >= g.ntiles) return;
-    BlockSlot cur = stage_input(a, tile, 0, inb[0], &bar[0], wsum, &s_base[0], bad);
+    BlockSlot cur = stage_input(a, tile, 0, smem + a.sm.in0, &bar[0], wsum, &s_base[0], bad);
 
-    uint32_t acc[FAST ? 32 : 1];
+    uint32_t acc[32];
     uint32_t hsum = 0, qsum = 0, nzmask = 0;
     uint32_t ld = 0; /* index of the current copy in the two-buffer stream */
     uint32_t p = 0;  /* input of the current copy */
@@ -106,12 +114,14 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
         ZTile z;
         zg_tile(&g, tile, &z);
         const bool own = tid < z.nblk;
+        const uint32_t n = cur.n;
+        const bool full = FAST && own && n == 32;
         if (p == 0) {
             if (FAST) {
 #pragma unroll
-                for (uint32_t j = 0; j < 32; j++) acc[j] = 0;
+                for (int j = 0; j < 32; j++) acc[j] = 0;
             } else if (own) {
-                for (uint32_t j = 0; j < cur.n; j++) acc_rows[tid * stride + j] = 0;
+                for (uint32_t j = 0; j < n; j++) acc_rows[tid * stride + j] = 0;
             }
             hsum = qsum = nzmask = 0;
         }
@@ -127,53 +137,37 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
         }
         BlockSlot nxt = {0, 0, 0};
         if (ntile < g.ntiles)
-            nxt = stage_input(a, ntile, np, inb[cb ^ 1u], &bar[cb ^ 1u], wsum, &s_base[cb ^ 1u], bad);
+            nxt = stage_input(a, ntile, np, smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u], wsum,
+                              &s_base[cb ^ 1u], bad);
 
         /* add this input's deltas */
         mbar_wait(&bar[cb], (ld >> 1) & 1u, a.w.err);
+        const uint8_t *buf = smem + (cb ? a.sm.in1 : a.sm.in0);
+        const uint32_t *sw = reinterpret_cast<const uint32_t *>(buf);
         const uint32_t ph = (uint32_t)((uintptr_t)(a.in[p].bytes + s_base[cb]) & 15u);
-        const uint8_t *tb = inb[cb] + ph;
-        const uint32_t *sw = reinterpret_cast<const uint32_t *>(inb[cb]);
         const uint32_t headb = z.has_head ? 4u : 0u;
         if (z.has_head) {
             uint32_t h = 0;
 #pragma unroll
-            for (int k = 0; k < 4; k++) h |= (uint32_t)tb[k] << (8 * k);
+            for (int k = 0; k < 4; k++) h |= (uint32_t)buf[ph + k] << (8 * k);
             hsum += h;
         }
         if (a.qprev_valid) qsum += (uint32_t)a.in[p].tile_qprev[tile];
         if (own) {
-            const uint32_t b = cur.b, n = cur.n, o = ph + headb + cur.off;
-            if (inb[cb][o] != b) bad |= ZERR_CORRUPT;
+            const uint32_t b = cur.b, o = ph + headb + cur.off;
+            if (buf[o] != b) bad |= ZERR_CORRUPT;
             if (b) {
                 nzmask |= 1u << (p & 31);
-                const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
-                if (FAST) {
+                if (full) {
                     uint32_t v[32];
+                    decode_full(sw, o, b, v);
 #pragma unroll
-                    for (uint32_t j = 0; j < 32; j++) v[j] = 0;
-                    Reader rd;
-                    rd.init(sw, o + 1);
-                    const uint32_t sg = rd.get(8 * ns) << (32 - 8 * ns);
-                    if (B) get_high_bytes(rd, v, n, B, r);
-                    if (r) get_low_bits(rd, v, n, r);
-#pragma unroll
-                    for (uint32_t j = 0; j < 32; j++)
-                        acc[j] += ((sg >> (31 - j)) & 1u) ? 0u - v[j] : v[j];
+                    for (int j = 0; j < 32; j++) acc[j] += v[j];
+                } else if (FAST) {
+                    decode_any(sw, o, b, n, [&](uint32_t j, uint32_t v) { pick(acc, j) += v; });
                 } else {
-                    Reader rs, rh, rl;
-                    rs.init(sw, o + 1);
-                    rh.init(sw, o + 1 + ns);
-                    rl.init(sw, o + 1 + ns + B * n);
-                    for (uint32_t j = 0; j < n; j++) {
-                        rh.refill();
-                        rl.refill();
-                        rs.refill();
-                        uint32_t v = B ? bswap32(rh.get(8 * B) << (32 - 8 * B)) << r : 0u;
-                        if (r) v |= rl.get(r);
-                        if (rs.get(1)) v = 0u - v;
-                        acc_rows[tid * stride + j] += v;
-                    }
+                    decode_any(sw, o, b, n,
+                               [&](uint32_t j, uint32_t v) { acc_rows[tid * stride + j] += v; });
                 }
             }
         }
@@ -181,10 +175,10 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
         if (p + 1 == P) {
             /* branch-case counters of the two-input add (ZCCLd_float.c:2175-2764) */
             if (a.cases && P == 2) {
-                uint32_t c0 = __syncthreads_count(own && nzmask == 0u);
-                uint32_t c1 = __syncthreads_count(own && nzmask == 2u);
-                uint32_t c2 = __syncthreads_count(own && nzmask == 1u);
-                uint32_t c3 = __syncthreads_count(own && nzmask == 3u);
+                const uint32_t c0 = __syncthreads_count(own && nzmask == 0u);
+                const uint32_t c1 = __syncthreads_count(own && nzmask == 2u);
+                const uint32_t c2 = __syncthreads_count(own && nzmask == 1u);
+                const uint32_t c3 = __syncthreads_count(own && nzmask == 3u);
                 if (tid == 0) {
                     atomicAdd(a.cases + 0, (unsigned long long)c0);
                     atomicAdd(a.cases + 1, (unsigned long long)c1);
@@ -193,21 +187,22 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
                 }
             }
             /* re-encode the sum */
-            const uint32_t n = cur.n;
-            uint32_t b = 0, size = 0, smask = 0, mx = 0;
-            if (own) {
-                if (FAST) {
+            uint32_t b = 0, size = 0, smask = 0;
+            if (full) {
+                uint32_t mx = 0;
 #pragma unroll
-                    for (uint32_t j = 0; j < 32; j++) {
-                        uint32_t neg = acc[j] >> 31;
-                        uint32_t mg = (uint32_t)abs((int32_t)acc[j]);
-                        smask |= neg << (31 - j);
-                        mx = max(mx, mg);
-                        acc[j] = mg;
-                    }
-                } else {
-                    for (uint32_t j = 0; j < n; j++)
-                        mx = max(mx, (uint32_t)abs((int32_t)acc_rows[tid * stride + j]));
+                for (int j = 0; j < 32; j++) {
+                    smask = (smask << 1) | (acc[j] >> 31);
+                    acc[j] = (uint32_t)abs((int32_t)acc[j]);
+                    mx = max(mx, acc[j]);
+                }
+                b = width_of(mx, a.wt);
+                size = zg_block_bytes(b, 32);
+            } else if (own) {
+                uint32_t mx = 0;
+                for (uint32_t j = 0; j < n; j++) {
+                    const uint32_t v = FAST ? pick(acc, j) : acc_rows[tid * stride + j];
+                    mx = max(mx, (uint32_t)abs((int32_t)v));
                 }
                 b = width_of(mx, a.wt);
                 size = zg_block_bytes(b, n);
@@ -218,58 +213,19 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
             if (warp == 0) lb_publish(a.w.status, tile, total, tile == 0, 0);
             smem_zero(outs, total + 8);
             __syncthreads();
-            if (z.has_head && tid == 0) {
-#pragma unroll
-                for (int k = 0; k < 4; k++) outs[k] = (uint8_t)(hsum >> (8 * k));
-            }
-            if (own) {
-                const uint32_t o = headb + off;
-                const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
-                if (FAST) {
-                    Packer pk;
-                    pk.init(outw, o);
-                    pk.put(b, 8);
-                    pk.flush();
-                    if (b) {
-                        pk.put(smask >> (32 - 8 * ns), 8 * ns);
-                        pk.flush();
-                        if (B) put_high_bytes(pk, acc, n, B, r);
-                        if (r) put_low_bits(pk, acc, n, r, B > 0);
-                    }
-                    pk.finish();
-                } else {
-                    Packer ph;
-                    ph.init(outw, o);
-                    ph.put(b, 8);
-                    ph.finish();
-                    if (b) {
-                        Packer ws, wh, wl;
-                        ws.init(outw, o + 1);
-                        wh.init(outw, o + 1 + ns);
-                        wl.init(outw, o + 1 + ns + B * n);
-                        const uint32_t mask = r ? (1u << r) - 1u : 0u;
-                        for (uint32_t j = 0; j < n; j++) {
-                            uint32_t v = acc_rows[tid * stride + j];
-                            uint32_t mg = (uint32_t)abs((int32_t)v);
-                            ws.put(v >> 31, 1);
-                            ws.flush();
-                            if (B) {
-                                wh.put(bswap32(mg >> r) >> (32 - 8 * B), 8 * B);
-                                wh.flush();
-                            }
-                            if (r) {
-                                wl.put(mg & mask, r);
-                                wl.flush();
-                            }
-                        }
-                        ws.finish();
-                        if (B) wh.finish();
-                        if (r) wl.finish();
-                    }
-                }
+            if (z.has_head && tid == 0) *reinterpret_cast<uint32_t *>(outs) = hsum;
+            const uint32_t o = headb + off;
+            if (full) {
+                encode_full(outs_sa, o, b, smask, acc);
+            } else if (own) {
+                encode_any(outs_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
+                    const uint32_t v = FAST ? pick(acc, j) : acc_rows[tid * stride + j];
+                    neg = v >> 31;
+                    mg = (uint32_t)abs((int32_t)v);
+                });
             }
             if (warp == 0) {
-                uint64_t prefix = lb_resolve(a.w.status, tile, total, tile == 0, 0, a.w.err);
+                const uint64_t prefix = lb_resolve(a.w.status, tile, total, tile == 0, 0, a.w.err);
                 if (lane == 0) bc[1] = prefix;
             }
             __syncthreads();
@@ -281,7 +237,7 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
                 a.idx.tile_off[tile] = base;
                 if (a.qprev_valid) a.idx.tile_qprev[tile] = (int32_t)qsum;
                 if (fits && z.has_head && z.seg < g.T) {
-                    uint64_t h = base - 8ull * g.T;
+                    const uint64_t h = base - 8ull * g.T;
 #pragma unroll
                     for (int k = 0; k < 8; k++) a.out[8ull * z.seg + k] = (uint8_t)(h >> (8 * k));
                 }
