@@ -96,6 +96,7 @@ ZG_HD int zg_init(ZGeom *g, uint64_t n, uint32_t L, uint32_t T)
     g->nt_rm = g->rem ? (g->nb_rm ? zg_div_up(g->nb_rm, g->TB) : 1) : 0;
     g->nblocks = (uint64_t)T * g->nb_reg + g->nb_rm;
     g->ntiles = (uint64_t)T * g->nt_reg + g->nt_rm;
+    if (g->ntiles >> 32) return -1; /* tile indices are 32-bit on the device */
     return 0;
 }
 
@@ -103,7 +104,7 @@ ZG_HD void zg_tile(const ZGeom *g, uint64_t t, ZTile *z)
 {
     uint64_t k, nb;
     if (t < (uint64_t)g->T * g->nt_reg) {
-        uint64_t s = t / g->nt_reg;
+        uint64_t s = (uint32_t)t / (uint32_t)g->nt_reg; /* tiles and tiles per segment < 2^32 */
         k = t - s * g->nt_reg;
         z->seg = (uint32_t)s;
         z->seg_start = s * g->tbs;
@@ -165,7 +166,10 @@ ZG_HD uint32_t zg_a16(uint32_t v) { return (v + 15u) & ~15u; }
 /* Largest tile in bytes: head + TB blocks at width 32. */
 ZG_HD uint32_t zg_tile_worst(uint32_t L, uint32_t TB) { return TB * zg_block_bytes(32, L) + 4u; }
 
-/* kind: 0 compressor, 1 decompressor, 2 homomorphic add */
+/* kind: 0 compressor, 1 decompressor, 2 homomorphic add.
+ * The compressor stages one tile at a time: its packed output reuses the
+ * input buffer once the floats are in rows (in1 == in0 == out).  The
+ * decompressor and the homomorphic add double-buffer their input. */
 ZG_HD ZSmem zg_smem(uint32_t kind, uint32_t L, uint32_t TB)
 {
     ZSmem m;
@@ -173,12 +177,17 @@ ZG_HD ZSmem zg_smem(uint32_t kind, uint32_t L, uint32_t TB)
     const uint32_t raw_in = (TB * L + 1u) * 4u + 32u;     /* floats, 16-byte superset */
     const uint32_t tile_in = zg_tile_worst(L, TB) + 48u;  /* bytes, superset + reader slack */
     const uint32_t tile_out = zg_tile_worst(L, TB) + 48u; /* realigning store reads 32 past */
-    const uint32_t in = kind == 0 ? raw_in : tile_in;
     const int need_rows = kind != 2 || L > 32;
     m.rows = 256u;
     m.in0 = zg_a16(m.rows + (need_rows ? rows_bytes : 0u));
-    m.in1 = zg_a16(m.in0 + in);
-    m.out = zg_a16(m.in1 + in);
+    if (kind == 0) {
+        m.in1 = m.in0;
+        m.out = m.in0;
+        m.total = zg_a16(m.in0 + (raw_in > tile_out ? raw_in : tile_out));
+        return m;
+    }
+    m.in1 = zg_a16(m.in0 + tile_in);
+    m.out = zg_a16(m.in1 + tile_in);
     m.total = zg_a16(m.out + (kind == 1 ? 0u : tile_out));
     return m;
 }

@@ -30,68 +30,73 @@
 
 namespace {
 
-/* Thread 0: claim the next tile and start its input copy. */
-__device__ __forceinline__ uint64_t claim_and_load(const CompressArgs &a, uint8_t *buf,
-                                                   uint64_t *bar)
-{
-    uint64_t t = atomicAdd(a.w.ticket, 1u);
-    if (t < a.g.ntiles) {
-        ZTile z;
-        zg_tile(&a.g, t, &z);
-        const uint32_t nel = (uint32_t)(z.e_end - z.e_first + 1);
-        tma_load_superset(buf, reinterpret_cast<const uint8_t *>(a.x + (z.e_first - 1)), nel * 4u,
-                          bar);
-    }
-    return t;
-}
-
 template <bool FAST>
 __global__ void __launch_bounds__(128) k_compress(const CompressArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem); /* [2] */
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
     uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 16);
-    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160); /* [0..1] tiles, [2] prefix */
+    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160); /* [0] tile, [2] prefix */
     uint32_t *s_amax = reinterpret_cast<uint32_t *>(smem + 192);
     float *rows = reinterpret_cast<float *>(smem + a.sm.rows);
-    uint8_t *outs = smem + a.sm.out;
-    const uint32_t outs_sa = smem_u32(outs);
+    uint8_t *buf = smem + a.sm.in0; /* the tile's floats, then its packed bytes */
+    const uint32_t buf_sa = smem_u32(buf);
 
     const ZGeom &g = a.g;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, nw = blockDim.x >> 5;
     const uint32_t L = g.L, stride = zg_row_stride(L);
     uint32_t bad = 0;
 
-    if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        bc[0] = claim_and_load(a, smem + a.sm.in0, &bar[0]);
-        *s_amax = 0;
-    }
-    __syncthreads();
+    if (tid == 0) mbar_init(bar, 1);
 
     for (uint32_t it = 0;; it++) {
-        const uint32_t cb = it & 1u;
-        const uint64_t tile = bc[cb];
+        /* A tile is claimed only when this CTA is ready to work on it: a
+         * claimed tile publishes its size soon after, so later tiles never
+         * wait on a tile that sits idle behind another one. */
+        if (tid == 0) {
+            const uint64_t t = atomicAdd(a.w.ticket, 1u);
+            bc[0] = t;
+            *s_amax = 0;
+            if (t < g.ntiles) {
+                ZTile zt;
+                zg_tile(&g, t, &zt);
+                const uint32_t nel = (uint32_t)(zt.e_end - zt.e_first + 1);
+                tma_load_superset(buf, reinterpret_cast<const uint8_t *>(a.x + (zt.e_first - 1)),
+                                  nel * 4u, bar);
+            }
+        }
+        __syncthreads();
+        const uint64_t tile = bc[0];
         if (tile >= g.ntiles) break;
-        if (tid == 0)
-            bc[cb ^ 1u] = claim_and_load(a, smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u]);
         ZTile z;
         zg_tile(&g, tile, &z);
 
         /* 1. wait for this tile's floats, transpose blocks into rows, find
          *    the largest magnitude */
-        mbar_wait(&bar[cb], (it >> 1) & 1u, a.w.err);
-        const float *xin = reinterpret_cast<const float *>(
-            smem + (cb ? a.sm.in1 : a.sm.in0) + ((uintptr_t)(a.x + (z.e_first - 1)) & 15u));
+        mbar_wait(bar, it & 1u, a.w.err);
+        const float *xin =
+            reinterpret_cast<const float *>(buf + ((uintptr_t)(a.x + (z.e_first - 1)) & 15u));
         const float xprev0 = xin[0]; /* the head, or the last element of the previous tile */
         uint32_t amax = abs_bits(xprev0);
-        for (uint32_t k = warp; k < z.nblk; k += nw) {
-            const uint32_t n = zg_block_len(z.seg_len, L, z.blk0 + k);
-            for (uint32_t j = lane; j < n; j += 32) {
-                const float v = xin[1 + k * L + j];
+        if (FAST && L == 32 && z.nblk == g.TB && z.e_end - z.e_first == 32ull * g.TB) {
+            /* a full tile: every row is 32 floats; unrolled so that many
+             * shared loads are in flight per warp */
+            const uint32_t nrow = g.TB / nw; /* rows per warp */
+#pragma unroll 8
+            for (uint32_t r = 0; r < nrow; r++) {
+                const uint32_t k = warp + r * nw;
+                const float v = xin[1 + k * 32 + lane];
                 amax = max(amax, abs_bits(v));
-                rows[k * stride + j] = v;
+                rows[k * stride + lane] = v;
+            }
+        } else {
+            for (uint32_t k = warp; k < z.nblk; k += nw) {
+                const uint32_t n = zg_block_len(z.seg_len, L, z.blk0 + k);
+                for (uint32_t j = lane; j < n; j += 32) {
+                    const float v = xin[1 + k * L + j];
+                    amax = max(amax, abs_bits(v));
+                    rows[k * stride + j] = v;
+                }
             }
         }
         amax = __reduce_max_sync(0xffffffffu, amax);
@@ -140,15 +145,15 @@ __global__ void __launch_bounds__(128) k_compress(const CompressArgs a)
         total += headb;
         if (warp == 0) lb_publish(a.w.status, tile, total, tile == 0, 0);
         const int32_t qprev0 = fastq ? quantize_fast(xprev0, a.inv) : quantize(xprev0, a.inv, bad);
-        smem_zero(outs, total + 8);
+        smem_zero(buf, total + 8); /* the floats are all in rows now */
         __syncthreads();
-        if (z.has_head && tid == 0) *reinterpret_cast<int32_t *>(outs) = qprev0;
+        if (z.has_head && tid == 0) *reinterpret_cast<int32_t *>(buf) = qprev0;
         const uint32_t o = headb + off;
         if (full) {
-            encode_full(outs_sa, o, b, smask, m);
+            encode_full(buf_sa, o, b, smask, m);
         } else if (own) {
             int32_t qp = fastq ? quantize_fast(xp, a.inv) : quantize(xp, a.inv, bad);
-            encode_any(outs_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
+            encode_any(buf_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
                 const int32_t q = fastq ? quantize_fast(row[j], a.inv) : quantize(row[j], a.inv, bad);
                 const int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
                 qp = q;
@@ -176,10 +181,9 @@ __global__ void __launch_bounds__(128) k_compress(const CompressArgs a)
                 for (int k = 0; k < 8; k++) a.out[8ull * z.seg + k] = (uint8_t)(h >> (8 * k));
             }
             if (tile == g.ntiles - 1) *a.idx.size = base + total;
-            *s_amax = 0;
         }
-        if (fits) store_realign(a.out + base, outs, total);
-        __syncthreads(); /* rows, outs, bc[2] and the maximum are reused by the next tile */
+        if (fits) store_realign(a.out + base, buf, total);
+        __syncthreads(); /* rows, buf and the broadcast slots are reused by the next tile */
     }
     if (bad) atomicOr(a.w.err, bad);
 }

@@ -33,7 +33,7 @@ struct BlockSlot {
  * this thread's block; the tile's byte offset lands in *s_base. */
 __device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, uint64_t t, uint8_t *buf,
                                                 uint64_t *bar, uint32_t *wsum, uint64_t *s_base,
-                                                uint32_t &bad)
+                                                uint32_t *s_q0, uint32_t &bad)
 {
     BlockSlot sl = {0, 0, 0};
     ZTile z;
@@ -61,6 +61,7 @@ __device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, uint64_
             if (base > a.avail) base = 0;
         }
         *s_base = base;
+        if (a.qprev_valid) *s_q0 = (uint32_t)a.idx.tile_qprev[t]; /* fetched early, used later */
         tma_load_superset(buf, a.in + base, nload, bar);
     }
     return sl;
@@ -74,6 +75,7 @@ __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
     uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 16);
     uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160);     /* [0,1] tiles, [2] q0 */
     uint64_t *s_base = reinterpret_cast<uint64_t *>(smem + 192); /* [2] */
+    uint32_t *s_q0 = reinterpret_cast<uint32_t *>(smem + 208);   /* [2] */
     float *rows = reinterpret_cast<float *>(smem + a.sm.rows);
 
     const ZGeom &g = a.g;
@@ -92,7 +94,8 @@ __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
     }
     __syncthreads();
     BlockSlot cur = {0, 0, 0};
-    if (bc[0] < g.ntiles) cur = stage_tile(a, bc[0], smem + a.sm.in0, &bar[0], wsum, &s_base[0], bad);
+    if (bc[0] < g.ntiles)
+        cur = stage_tile(a, bc[0], smem + a.sm.in0, &bar[0], wsum, &s_base[0], &s_q0[0], bad);
 
     for (uint32_t it = 0;; it++) {
         const uint32_t cb = it & 1u;
@@ -108,7 +111,7 @@ __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
         BlockSlot nxt = {0, 0, 0};
         if (bc[cb ^ 1u] < g.ntiles)
             nxt = stage_tile(a, bc[cb ^ 1u], smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u], wsum,
-                             &s_base[cb ^ 1u], bad);
+                             &s_base[cb ^ 1u], &s_q0[cb ^ 1u], bad);
 
         /* 2. unpack this tile's deltas */
         mbar_wait(&bar[cb], (it >> 1) & 1u, a.w.err);
@@ -140,7 +143,7 @@ __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
         uint32_t tsum;
         const uint32_t pre = cta_excl_scan(bsum, wsum, &tsum);
         if (a.qprev_valid) {
-            if (tid == 0) bc[2] = (uint32_t)(z.has_head ? head : a.idx.tile_qprev[tile]);
+            if (tid == 0) bc[2] = z.has_head ? (uint32_t)head : s_q0[cb];
         } else if (warp == 0) {
             lb_publish(a.w.status, tile, tsum, z.has_head != 0, (uint32_t)head);
             const uint64_t q0 =

@@ -9,11 +9,11 @@
  * canonical).  Integer addition is associative modulo 2^32, so one pass over
  * P inputs equals the ring's pairwise fold in any order, bit for bit.
  *
- * Persistent CTAs take tiles in ticket order, one thread per block.  The
- * (tile, input) pairs form one stream of TMA copies through two buffers:
- * while one input's tile bytes are unpacked and added into per-thread
- * registers, the next input's (or the next tile's first input's) sizes are
- * scanned from its width index and its bytes are already in flight.
+ * Persistent CTAs take tiles in ticket order, one thread per block.  A
+ * tile's P inputs form a stream of TMA copies through two buffers: while one
+ * input's tile bytes are unpacked and added into per-thread registers, the
+ * next input's sizes are scanned from its width index and its bytes are
+ * already in flight.
  * Zero-width input blocks are skipped without touching their bytes.  After
  * the last input the sum is re-encoded like the compressor does (width,
  * scan, early look-back publish, packing, realigned vector stores) and the
@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
     extern __shared__ __align__(16) uint8_t smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem); /* [2] */
     uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 16);
-    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160);     /* [0] next tile, [1] prefix */
+    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160);     /* [0] tile, [1] prefix */
     uint64_t *s_base = reinterpret_cast<uint64_t *>(smem + 192); /* [2] */
     uint32_t *acc_rows = reinterpret_cast<uint32_t *>(smem + a.sm.rows);
     uint8_t *outs = smem + a.sm.out;
@@ -93,164 +93,151 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
     uint32_t bad = 0;
     /* see k_decompress: a failed index walk stops every CTA alike */
     if (*(volatile const uint32_t *)a.w.walk_err) return;
-
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
-        bc[0] = atomicAdd(a.w.ticket, 1u);
     }
-    __syncthreads();
-    uint64_t tile = bc[0];
-    if (tile >= g.ntiles) return;
-    BlockSlot cur = stage_input(a, tile, 0, smem + a.sm.in0, &bar[0], wsum, &s_base[0], bad);
-
     uint32_t acc[32];
-    uint32_t hsum = 0, qsum = 0, nzmask = 0;
     uint32_t ld = 0; /* index of the current copy in the two-buffer stream */
-    uint32_t p = 0;  /* input of the current copy */
 
     for (;;) {
-        const uint32_t cb = ld & 1u;
+        /* Claim a tile only when this CTA is ready to work on it, so that a
+         * claimed tile publishes its size soon after and later tiles never
+         * wait on a tile that sits idle behind another one. */
+        if (tid == 0) bc[0] = atomicAdd(a.w.ticket, 1u);
+        __syncthreads();
+        const uint64_t tile = bc[0];
+        if (tile >= g.ntiles) break;
         ZTile z;
         zg_tile(&g, tile, &z);
         const bool own = tid < z.nblk;
+        BlockSlot cur =
+            stage_input(a, tile, 0, smem + (ld & 1u ? a.sm.in1 : a.sm.in0), &bar[ld & 1u], wsum,
+                        &s_base[ld & 1u], bad);
         const uint32_t n = cur.n;
         const bool full = FAST && own && n == 32;
-        if (p == 0) {
-            if (FAST) {
+        if (FAST) {
 #pragma unroll
-                for (int j = 0; j < 32; j++) acc[j] = 0;
-            } else if (own) {
-                for (uint32_t j = 0; j < n; j++) acc_rows[tid * stride + j] = 0;
-            }
-            hsum = qsum = nzmask = 0;
+            for (int j = 0; j < 32; j++) acc[j] = 0;
+        } else if (own) {
+            for (uint32_t j = 0; j < n; j++) acc_rows[tid * stride + j] = 0;
         }
-
-        /* start the next copy: the next input of this tile, or input 0 of the next tile */
-        uint64_t ntile = tile;
-        uint32_t np = p + 1;
-        if (np == P) {
-            if (tid == 0) bc[0] = atomicAdd(a.w.ticket, 1u);
-            __syncthreads();
-            ntile = bc[0];
-            np = 0;
-        }
-        BlockSlot nxt = {0, 0, 0};
-        if (ntile < g.ntiles)
-            nxt = stage_input(a, ntile, np, smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u], wsum,
-                              &s_base[cb ^ 1u], bad);
-
-        /* add this input's deltas */
-        mbar_wait(&bar[cb], (ld >> 1) & 1u, a.w.err);
-        const uint8_t *buf = smem + (cb ? a.sm.in1 : a.sm.in0);
-        const uint32_t *sw = reinterpret_cast<const uint32_t *>(buf);
-        const uint32_t ph = (uint32_t)((uintptr_t)(a.in[p].bytes + s_base[cb]) & 15u);
+        uint32_t hsum = 0, qsum = 0, nzmask = 0;
         const uint32_t headb = z.has_head ? 4u : 0u;
-        if (z.has_head) {
-            uint32_t h = 0;
+
+        for (uint32_t p = 0; p < P; p++, ld++) {
+            const uint32_t cb = ld & 1u;
+            /* the next input's copy runs while this one is added */
+            BlockSlot nxt = {0, 0, 0};
+            if (p + 1 < P)
+                nxt = stage_input(a, tile, p + 1, smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u],
+                                  wsum, &s_base[cb ^ 1u], bad);
+            if (a.qprev_valid && tid == 0) qsum += (uint32_t)a.in[p].tile_qprev[tile];
+            mbar_wait(&bar[cb], (ld >> 1) & 1u, a.w.err);
+            const uint8_t *buf = smem + (cb ? a.sm.in1 : a.sm.in0);
+            const uint32_t *sw = reinterpret_cast<const uint32_t *>(buf);
+            const uint32_t ph = (uint32_t)((uintptr_t)(a.in[p].bytes + s_base[cb]) & 15u);
+            if (z.has_head && tid == 0) {
+                uint32_t h = 0;
 #pragma unroll
-            for (int k = 0; k < 4; k++) h |= (uint32_t)buf[ph + k] << (8 * k);
-            hsum += h;
-        }
-        if (a.qprev_valid) qsum += (uint32_t)a.in[p].tile_qprev[tile];
-        if (own) {
-            const uint32_t b = cur.b, o = ph + headb + cur.off;
-            if (buf[o] != b) bad |= ZERR_CORRUPT;
-            if (b) {
-                nzmask |= 1u << (p & 31);
-                if (full) {
-                    uint32_t v[32];
-                    decode_full(sw, o, b, v);
+                for (int k = 0; k < 4; k++) h |= (uint32_t)buf[ph + k] << (8 * k);
+                hsum += h;
+            }
+            if (own) {
+                const uint32_t b = cur.b, o = ph + headb + cur.off;
+                if (buf[o] != b) bad |= ZERR_CORRUPT;
+                if (b) {
+                    nzmask |= 1u << (p & 31);
+                    if (full) {
+                        uint32_t v[32];
+                        decode_full(sw, o, b, v);
 #pragma unroll
-                    for (int j = 0; j < 32; j++) acc[j] += v[j];
-                } else if (FAST) {
-                    decode_any(sw, o, b, n, [&](uint32_t j, uint32_t v) { pick(acc, j) += v; });
-                } else {
-                    decode_any(sw, o, b, n,
-                               [&](uint32_t j, uint32_t v) { acc_rows[tid * stride + j] += v; });
+                        for (int j = 0; j < 32; j++) acc[j] += v[j];
+                    } else if (FAST) {
+                        decode_any(sw, o, b, n, [&](uint32_t j, uint32_t v) { pick(acc, j) += v; });
+                    } else {
+                        decode_any(sw, o, b, n,
+                                   [&](uint32_t j, uint32_t v) { acc_rows[tid * stride + j] += v; });
+                    }
                 }
             }
+            cur = nxt;
+            /* the buffer just read is refilled by the copy staged next round,
+             * after that round's scan has synchronised every thread */
         }
 
-        if (p + 1 == P) {
-            /* branch-case counters of the two-input add (ZCCLd_float.c:2175-2764) */
-            if (a.cases && P == 2) {
-                const uint32_t c0 = __syncthreads_count(own && nzmask == 0u);
-                const uint32_t c1 = __syncthreads_count(own && nzmask == 2u);
-                const uint32_t c2 = __syncthreads_count(own && nzmask == 1u);
-                const uint32_t c3 = __syncthreads_count(own && nzmask == 3u);
-                if (tid == 0) {
-                    atomicAdd(a.cases + 0, (unsigned long long)c0);
-                    atomicAdd(a.cases + 1, (unsigned long long)c1);
-                    atomicAdd(a.cases + 2, (unsigned long long)c2);
-                    atomicAdd(a.cases + 3, (unsigned long long)c3);
-                }
-            }
-            /* re-encode the sum */
-            uint32_t b = 0, size = 0, smask = 0;
-            if (full) {
-                uint32_t mx = 0;
-#pragma unroll
-                for (int j = 0; j < 32; j++) {
-                    smask = (smask << 1) | (acc[j] >> 31);
-                    acc[j] = (uint32_t)abs((int32_t)acc[j]);
-                    mx = max(mx, acc[j]);
-                }
-                b = width_of(mx, a.wt);
-                size = zg_block_bytes(b, 32);
-            } else if (own) {
-                uint32_t mx = 0;
-                for (uint32_t j = 0; j < n; j++) {
-                    const uint32_t v = FAST ? pick(acc, j) : acc_rows[tid * stride + j];
-                    mx = max(mx, (uint32_t)abs((int32_t)v));
-                }
-                b = width_of(mx, a.wt);
-                size = zg_block_bytes(b, n);
-            }
-            uint32_t total;
-            const uint32_t off = cta_excl_scan(size, wsum, &total);
-            total += headb;
-            if (warp == 0) lb_publish(a.w.status, tile, total, tile == 0, 0);
-            smem_zero(outs, total + 8);
-            __syncthreads();
-            if (z.has_head && tid == 0) *reinterpret_cast<uint32_t *>(outs) = hsum;
-            const uint32_t o = headb + off;
-            if (full) {
-                encode_full(outs_sa, o, b, smask, acc);
-            } else if (own) {
-                encode_any(outs_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
-                    const uint32_t v = FAST ? pick(acc, j) : acc_rows[tid * stride + j];
-                    neg = v >> 31;
-                    mg = (uint32_t)abs((int32_t)v);
-                });
-            }
-            if (warp == 0) {
-                const uint64_t prefix = lb_resolve(a.w.status, tile, total, tile == 0, 0, a.w.err);
-                if (lane == 0) bc[1] = prefix;
-            }
-            __syncthreads();
-            const uint64_t base = 8ull * g.T + bc[1];
-            const bool fits = base + total <= a.cap; /* uniform over the CTA */
-            if (!fits) bad |= ZERR_CAPACITY;
-            if (own) a.idx.widths[z.gblk0 + tid] = (uint8_t)b;
+        /* branch-case counters of the two-input add (ZCCLd_float.c:2175-2764) */
+        if (a.cases && P == 2) {
+            const uint32_t c0 = __syncthreads_count(own && nzmask == 0u);
+            const uint32_t c1 = __syncthreads_count(own && nzmask == 2u);
+            const uint32_t c2 = __syncthreads_count(own && nzmask == 1u);
+            const uint32_t c3 = __syncthreads_count(own && nzmask == 3u);
             if (tid == 0) {
-                a.idx.tile_off[tile] = base;
-                if (a.qprev_valid) a.idx.tile_qprev[tile] = (int32_t)qsum;
-                if (fits && z.has_head && z.seg < g.T) {
-                    const uint64_t h = base - 8ull * g.T;
-#pragma unroll
-                    for (int k = 0; k < 8; k++) a.out[8ull * z.seg + k] = (uint8_t)(h >> (8 * k));
-                }
-                if (tile == g.ntiles - 1) *a.idx.size = base + total;
+                atomicAdd(a.cases + 0, (unsigned long long)c0);
+                atomicAdd(a.cases + 1, (unsigned long long)c1);
+                atomicAdd(a.cases + 2, (unsigned long long)c2);
+                atomicAdd(a.cases + 3, (unsigned long long)c3);
             }
-            if (fits) store_realign(a.out + base, outs, total);
         }
+        /* re-encode the sum */
+        uint32_t b = 0, size = 0, smask = 0;
+        if (full) {
+            uint32_t mx = 0;
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+                smask = (smask << 1) | (acc[j] >> 31);
+                acc[j] = (uint32_t)abs((int32_t)acc[j]);
+                mx = max(mx, acc[j]);
+            }
+            b = width_of(mx, a.wt);
+            size = zg_block_bytes(b, 32);
+        } else if (own) {
+            uint32_t mx = 0;
+            for (uint32_t j = 0; j < n; j++) {
+                const uint32_t v = FAST ? pick(acc, j) : acc_rows[tid * stride + j];
+                mx = max(mx, (uint32_t)abs((int32_t)v));
+            }
+            b = width_of(mx, a.wt);
+            size = zg_block_bytes(b, n);
+        }
+        uint32_t total;
+        const uint32_t off = cta_excl_scan(size, wsum, &total);
+        total += headb;
+        if (warp == 0) lb_publish(a.w.status, tile, total, tile == 0, 0);
+        smem_zero(outs, total + 8);
+        __syncthreads();
+        if (z.has_head && tid == 0) *reinterpret_cast<uint32_t *>(outs) = hsum;
+        const uint32_t o = headb + off;
+        if (full) {
+            encode_full(outs_sa, o, b, smask, acc);
+        } else if (own) {
+            encode_any(outs_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
+                const uint32_t v = FAST ? pick(acc, j) : acc_rows[tid * stride + j];
+                neg = v >> 31;
+                mg = (uint32_t)abs((int32_t)v);
+            });
+        }
+        if (warp == 0) {
+            const uint64_t prefix = lb_resolve(a.w.status, tile, total, tile == 0, 0, a.w.err);
+            if (lane == 0) bc[1] = prefix;
+        }
+        __syncthreads();
+        const uint64_t base = 8ull * g.T + bc[1];
+        const bool fits = base + total <= a.cap; /* uniform over the CTA */
+        if (!fits) bad |= ZERR_CAPACITY;
+        if (own) a.idx.widths[z.gblk0 + tid] = (uint8_t)b;
+        if (tid == 0) {
+            a.idx.tile_off[tile] = base;
+            if (a.qprev_valid) a.idx.tile_qprev[tile] = (int32_t)qsum;
+            if (fits && z.has_head && z.seg < g.T) {
+                const uint64_t h = base - 8ull * g.T;
+#pragma unroll
+                for (int k = 0; k < 8; k++) a.out[8ull * z.seg + k] = (uint8_t)(h >> (8 * k));
+            }
+            if (tile == g.ntiles - 1) *a.idx.size = base + total;
+        }
+        if (fits) store_realign(a.out + base, outs, total);
         __syncthreads(); /* buffers, outs and the broadcast slots are reused */
-        if (ntile >= g.ntiles) break;
-        tile = ntile;
-        p = np;
-        cur = nxt;
-        ld++;
     }
     if (bad) atomicOr(a.w.err, bad);
 }
