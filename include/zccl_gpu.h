@@ -93,6 +93,7 @@ void ZCCL_float_homomophic_add_single_thread(unsigned char *final_cmpBytes, size
 #define ZCCL_GPU_ETIMEOUT (-6)  /* a bounded device wait gave up */
 #define ZCCL_GPU_ENOMEM (-7)    /* device or host allocation failed */
 #define ZCCL_GPU_ECAPACITY (-8) /* destination buffer too small */
+#define ZCCL_GPU_ESCRATCH (-9)  /* input needs more than the fixed scratch array holds */
 
 /* A compressed stream resident in device memory. */
 typedef struct zccl_gpu_stream {
@@ -131,6 +132,35 @@ int zccl_gpu_homadd(zccl_gpu_stream *out, zccl_gpu_stream *ins, int P, size_t n,
  * ZCCL/src/ZCCLd_float.c:2175-2764) into d_cases[4] (device uint64). */
 int zccl_gpu_homadd_cases(zccl_gpu_stream *out, zccl_gpu_stream *ins, int P, size_t n, int L,
                           int T, void *d_ws, unsigned long long *d_cases, void *cuda_stream);
+
+/* Bytes of the fixed device scratch array zccl_gpu_compress_noalloc uses. */
+#define ZCCL_GPU_NOALLOC_SCRATCH_BYTES (1u << 20)
+
+/* zccl_gpu_compress without a workspace argument and without allocating any
+ * memory; it has no counterpart in the reference.  It is for callers that
+ * cannot allocate device memory while they compress: a collective's step
+ * loop, where cudaMalloc or cudaFree can synchronize the whole device and
+ * stall kernels that other ranks are waiting on, or a process whose device
+ * memory is already held by a caching pool, where a fresh allocation fails.
+ *
+ * The scratch is a 1 MiB array (ZCCL_GPU_NOALLOC_SCRATCH_BYTES) inside this
+ * library's device code, one per device.  A call needs 16 + 8 * tiles bytes
+ * of it, a tile being up to 128 blocks of one segment (4096 floats at
+ * L = 32), so n may reach about 5.3e8 floats at L = 32 and T = 1; fewer with
+ * smaller L or many segments.  Larger inputs return ZCCL_GPU_ESCRATCH and
+ * launch nothing.  Those bytes must be zero when the kernel starts; the
+ * call clears them itself on cuda_stream.
+ *
+ * The first call with a device current looks up the array's address on that
+ * device, a one-time setup; make it before any stream capture begins.  All
+ * calls on a device share the one array: two calls whose work overlaps in
+ * time (different streams or host threads) race on it, so order them, for
+ * example by issuing them on one stream.  The output, status and size are
+ * those of zccl_gpu_compress.  When d_scratch is not NULL it receives the
+ * array's address, which zccl_gpu_check() takes to read this call's device
+ * status (before the next call on the device reuses the array). */
+int zccl_gpu_compress_noalloc(zccl_gpu_stream *out, const float *d_in, size_t n, float eb, int L,
+                              int T, void *cuda_stream, void **d_scratch);
 
 /* Build the side index of a stream that arrived as bytes only. */
 int zccl_gpu_build_index(zccl_gpu_stream *s, size_t n, int L, int T, void *d_ws, void *cuda_stream);

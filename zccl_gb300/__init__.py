@@ -27,6 +27,7 @@ STATUS = {
     -3: "input not finite or |x/eb| >= 2^31", -4: "stream inconsistent with its geometry",
     -5: "stream runs past its readable bytes", -6: "device wait timed out",
     -7: "out of memory", -8: "destination buffer too small",
+    -9: "input needs more than the fixed scratch array",
 }
 
 EXPORTS = [
@@ -36,7 +37,7 @@ EXPORTS = [
     "zccl_gpu_max_stream_bytes", "zccl_gpu_index_bytes", "zccl_gpu_workspace_bytes",
     "zccl_gpu_compress", "zccl_gpu_decompress", "zccl_gpu_homadd", "zccl_gpu_homadd_cases",
     "zccl_gpu_build_index", "zccl_gpu_stream_size", "zccl_gpu_check", "zccl_gpu_last_status",
-    "zccl_gpu_strerror", "zccl_gpu_width_table",
+    "zccl_gpu_strerror", "zccl_gpu_width_table", "zccl_gpu_compress_noalloc",
 ]
 
 
@@ -86,6 +87,7 @@ def lib() -> ctypes.CDLL:
         "zccl_gpu_last_status": (i, []),
         "zccl_gpu_strerror": (ctypes.c_char_p, [i]),
         "zccl_gpu_width_table": (None, [ctypes.POINTER(ctypes.c_uint32)]),
+        "zccl_gpu_compress_noalloc": (i, [sp, vp, sz, f, i, i, vp, ctypes.POINTER(vp)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -372,6 +372,7 @@ extern "C" const char *zccl_gpu_strerror(int status)
     case ZCCL_GPU_ETIMEOUT: return "device wait timed out";
     case ZCCL_GPU_ENOMEM: return "out of memory";
     case ZCCL_GPU_ECAPACITY: return "destination buffer too small";
+    case ZCCL_GPU_ESCRATCH: return "input needs more than the fixed scratch array";
     default: return "unknown status";
     }
 }
