@@ -10,6 +10,7 @@
  *   store_realign()      shared -> global at any byte alignment
  *   cta_excl_scan()      block-wide exclusive scan
  *   lb_publish/resolve   single-pass decoupled look-back across tiles
+ *   lb_resolve_cta       the same look-back with every warp of the CTA
  */
 #ifndef ZCCL_GB300_ZDEV_CUH
 #define ZCCL_GB300_ZDEV_CUH
@@ -338,6 +339,23 @@ __device__ __forceinline__ void decode_any(const uint32_t *w, uint32_t o, uint32
     }
 }
 
+/* v[j] and v[j] += x for a runtime j, as selects and predicated adds so
+ * that the register array stays in registers (short tail blocks only). */
+__device__ __forceinline__ uint32_t pick(const uint32_t (&v)[32], uint32_t j)
+{
+    uint32_t r = v[0];
+#pragma unroll
+    for (int k = 1; k < 32; k++) r = (uint32_t)k == j ? v[k] : r;
+    return r;
+}
+
+__device__ __forceinline__ void add_at(uint32_t (&v)[32], uint32_t j, uint32_t x)
+{
+#pragma unroll
+    for (int k = 0; k < 32; k++)
+        if ((uint32_t)k == j) v[k] += x;
+}
+
 /* Zero shared bytes [0, nbytes) (rounded up to 16) of a 16-byte-aligned buffer. */
 __device__ __forceinline__ void smem_zero(uint8_t *s, uint32_t nbytes)
 {
@@ -501,15 +519,20 @@ __device__ __forceinline__ uint32_t cta_excl_scan(uint32_t v, uint32_t *wsum, ui
 #define LB_FLAG_P (2ull << 62)
 #define LB_VAL (LB_FLAG_A - 1ull)
 
-__device__ __forceinline__ void st_release(uint64_t *p, uint64_t v)
+/* A status word carries its flag and its value together, and a reader
+ * uses nothing else that the writer produced, so relaxed device-scope
+ * accesses suffice: no acquire (which would keep a lane's eight loads from
+ * overlapping) and no release (which would hold the store until the
+ * thread's earlier output stores complete). */
+__device__ __forceinline__ void st_flag(uint64_t *p, uint64_t v)
 {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-__device__ __forceinline__ uint64_t ld_acquire(const uint64_t *p)
+__device__ __forceinline__ uint64_t ld_flag(const uint64_t *p)
 {
     uint64_t v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
 
@@ -527,7 +550,7 @@ __device__ __forceinline__ void lb_publish(uint64_t *status, uint64_t tile, uint
                                            uint64_t start)
 {
     if ((threadIdx.x & 31u) == 0)
-        st_release(status + tile, first ? (LB_FLAG_P | ((start + agg) & LB_VAL))
+        st_flag(status + tile, first ? (LB_FLAG_P | ((start + agg) & LB_VAL))
                                         : (LB_FLAG_A | (agg & LB_VAL)));
 }
 
@@ -554,7 +577,7 @@ static __device__ __noinline__ uint64_t lb_resolve(uint64_t *status, uint64_t ti
 #pragma unroll
         for (int k = 0; k < 8; k++) {
             int64_t idx = pos - (int64_t)(lane + 32u * k);
-            v[k] = idx >= 0 ? ld_acquire(status + idx) : LB_FLAG_P; /* before tile 0: value 0 */
+            v[k] = idx >= 0 ? ld_flag(status + idx) : LB_FLAG_P; /* before tile 0: value 0 */
         }
         /* nearest inclusive value: smallest distance lane + 32k flagged P */
         uint32_t kp = 8, fp = 31, pending = 0;
@@ -593,7 +616,87 @@ static __device__ __noinline__ uint64_t lb_resolve(uint64_t *status, uint64_t ti
         pos -= 256;
         spins = 0;
     }
-    if (lane == 0) st_release(status + tile, LB_FLAG_P | ((prefix + agg) & LB_VAL));
+    if (lane == 0) st_flag(status + tile, LB_FLAG_P | ((prefix + agg) & LB_VAL));
+    return prefix & LB_VAL;
+}
+
+/* lb_resolve for all threads of the CTA at once: warp w inspects the 256
+ * predecessors from distance 256w + 1 on, so one round covers 256 per warp
+ * (1024 with four warps), and the warps' findings are combined nearest
+ * first through rec (two words per warp of shared scratch).  Every thread
+ * returns the same prefix; thread 0 publishes the inclusive value.  The
+ * same bounded wait as lb_resolve. */
+static __device__ __forceinline__ uint64_t lb_resolve_cta(uint64_t *status, uint64_t tile, uint64_t agg,
+                                                       bool first, uint64_t start, uint32_t *err,
+                                                       uint64_t *rec)
+{
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (first) return start;
+    uint64_t prefix = 0;
+    int64_t pos = (int64_t)tile - 1 - 256 * (int64_t)warp;
+    uint32_t spins = 0;
+    for (;;) {
+        uint64_t v[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            int64_t idx = pos - (int64_t)(lane + 32u * k);
+            v[k] = idx >= 0 ? ld_flag(status + idx) : LB_FLAG_P; /* before tile 0: value 0 */
+        }
+        uint32_t kp = 8, fp = 31, pending = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t flag = (uint32_t)(v[k] >> 62);
+            const uint32_t pm = __ballot_sync(0xffffffffu, flag == 2u);
+            const uint32_t xm = __ballot_sync(0xffffffffu, flag == 0u);
+            if (kp == 8) {
+                if (pm) {
+                    kp = k;
+                    fp = (uint32_t)(__ffs(pm) - 1);
+                    pending |= xm & ((1u << fp) - 1u);
+                } else {
+                    pending |= xm;
+                }
+            }
+        }
+        uint64_t c = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const bool ready = (v[k] >> 62) != 0;
+            if ((uint32_t)k < kp || ((uint32_t)k == kp && lane <= fp))
+                c += ready ? (v[k] & LB_VAL) : 0ull;
+        }
+        c = warp_sum_u64(c);
+        if (lane == 0) {
+            rec[2 * warp] = c;
+            rec[2 * warp + 1] = (kp < 8 ? 1u : 0u) | (pending ? 2u : 0u);
+        }
+        __syncthreads();
+        uint64_t sum = 0;
+        bool found = false, pend = false;
+        for (uint32_t w = 0; w < nw; w++) {
+            const uint64_t st = rec[2 * w + 1];
+            sum += rec[2 * w];
+            pend |= (st & 2u) != 0;
+            if (st & 1u) {
+                found = true;
+                break;
+            }
+        }
+        __syncthreads(); /* rec is rewritten by the next round */
+        if (pend) {
+            if (++spins < (1u << 22)) {
+                __nanosleep(32);
+                continue;
+            }
+            /* give up: missing values count as 0 */
+            if (threadIdx.x == 0) atomicOr(err, ZERR_TIMEOUT);
+        }
+        prefix += sum;
+        if (found) break;
+        pos -= 256 * (int64_t)nw;
+        spins = 0;
+    }
+    if (threadIdx.x == 0) st_flag(status + tile, LB_FLAG_P | ((prefix + agg) & LB_VAL));
     return prefix & LB_VAL;
 }
 

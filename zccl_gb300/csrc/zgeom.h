@@ -154,6 +154,7 @@ ZG_HD uint64_t zg_stream_worst(const ZGeom *g)
 /* Shared-memory layout of the codec kernels (bytes), all regions 16-byte
  * aligned:
  *   [0, 256)   mbarriers, scan scratch, broadcast slots
+ *   [256, 512) look-back records
  *   rows       per-block rows, TB x row_stride 4-byte words (floats or ints)
  *   in0, in1   double-buffered TMA input (raw floats or tile bytes)
  *   out        packed output tile (compressor, homomorphic add) */
@@ -167,9 +168,12 @@ ZG_HD uint32_t zg_a16(uint32_t v) { return (v + 15u) & ~15u; }
 ZG_HD uint32_t zg_tile_worst(uint32_t L, uint32_t TB) { return TB * zg_block_bytes(32, L) + 4u; }
 
 /* kind: 0 compressor, 1 decompressor, 2 homomorphic add.
- * The compressor stages one tile at a time: its packed output reuses the
- * input buffer once the floats are in rows (in1 == in0 == out).  The
- * decompressor and the homomorphic add double-buffer their input. */
+ * The compressor stages one tile of floats at a time (in1 == in0) and keeps
+ * a packed tile in out until the next tile has been quantized.  With
+ * L <= 32 every warp holds its rows' floats in registers while they move
+ * from the input into the rows, so the rows share the input's space
+ * (rows == in0); longer blocks get separate regions.  The decompressor and
+ * the homomorphic add double-buffer their input. */
 ZG_HD ZSmem zg_smem(uint32_t kind, uint32_t L, uint32_t TB)
 {
     ZSmem m;
@@ -178,14 +182,22 @@ ZG_HD ZSmem zg_smem(uint32_t kind, uint32_t L, uint32_t TB)
     const uint32_t tile_in = zg_tile_worst(L, TB) + 48u;  /* bytes, superset + reader slack */
     const uint32_t tile_out = zg_tile_worst(L, TB) + 48u; /* realigning store reads 32 past */
     const int need_rows = kind != 2 || L > 32;
-    m.rows = 256u;
-    m.in0 = zg_a16(m.rows + (need_rows ? rows_bytes : 0u));
+    m.rows = 512u;
     if (kind == 0) {
-        m.in1 = m.in0;
-        m.out = m.in0;
-        m.total = zg_a16(m.in0 + (raw_in > tile_out ? raw_in : tile_out));
+        if (L <= 32) {
+            m.in0 = m.rows;
+            m.in1 = m.in0;
+            m.out = zg_a16(m.rows + (rows_bytes > raw_in ? rows_bytes : raw_in));
+            m.total = zg_a16(m.out + tile_out);
+        } else {
+            m.in0 = zg_a16(m.rows + rows_bytes);
+            m.in1 = m.in0;
+            m.out = zg_a16(m.in0 + raw_in);
+            m.total = zg_a16(m.out + tile_out);
+        }
         return m;
     }
+    m.in0 = zg_a16(m.rows + (need_rows ? rows_bytes : 0u));
     m.in1 = zg_a16(m.in0 + tile_in);
     m.out = zg_a16(m.in1 + tile_in);
     m.total = zg_a16(m.out + (kind == 1 ? 0u : tile_out));

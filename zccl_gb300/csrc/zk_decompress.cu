@@ -3,8 +3,11 @@
  *
  * Replaces ZCCL_float_decompress_openmp_threadblock_arg
  * (ZCCL/src/ZCCLd_float.c:538-754) and produces the same floats.  Persistent
- * CTAs take tiles in ticket order, one thread per block, mirroring the
- * compressor:
+ * CTAs, one thread per block, mirroring the compressor.  When the index
+ * holds every tile's starting value the tiles are independent: CTA c takes
+ * tiles c, c + grid, ... and loads the index entries of the tile after
+ * next while it works; otherwise tiles go in ticket order for the look-back.
+ * Per tile:
  *   1. for the NEXT tile: block sizes from the width index, a block-wide
  *      scan for every block's offset, and one TMA bulk copy of its bytes,
  *      so the copy runs while the current tile is decoded (double buffer);
@@ -28,12 +31,36 @@ struct BlockSlot {
     uint32_t b, n, off;
 };
 
-/* All threads: sizes of tile t's blocks from the index, their offsets, and
- * (thread 0) the TMA copy of the tile's bytes into buf.  Returns the slot of
- * this thread's block; the tile's byte offset lands in *s_base. */
-__device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, uint64_t t, uint8_t *buf,
-                                                uint64_t *bar, uint32_t *wsum, uint64_t *s_base,
-                                                uint32_t *s_q0, uint32_t &bad)
+/* The index entries one tile needs: this thread's block width, and on
+ * thread 0 the tile's byte offset and the quantized value before it.  Loaded
+ * a tile ahead of their use, so the loads' latency is hidden. */
+struct TileIdx {
+    uint32_t b;
+    uint64_t base;
+    uint32_t q0;
+};
+
+__device__ __forceinline__ TileIdx load_idx(const DecompressArgs &a, uint64_t t)
+{
+    TileIdx r = {0, 0, 0};
+    if (t >= a.g.ntiles) return r;
+    ZTile z;
+    zg_tile(&a.g, t, &z);
+    if (threadIdx.x < z.nblk) r.b = a.idx.widths[z.gblk0 + threadIdx.x];
+    if (threadIdx.x == 0) {
+        r.base = a.idx.tile_off[t];
+        if (a.qprev_valid) r.q0 = (uint32_t)a.idx.tile_qprev[t];
+    }
+    return r;
+}
+
+/* All threads: sizes of tile t's blocks, their offsets, and (thread 0) the
+ * TMA copy of the tile's bytes into buf.  Returns the slot of this thread's
+ * block; the tile's byte offset lands in *s_base, its starting value in
+ * *s_q0. */
+__device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, uint64_t t, const TileIdx &ix,
+                                                uint8_t *buf, uint64_t *bar, uint32_t *wsum,
+                                                uint64_t *s_base, uint32_t *s_q0, uint32_t &bad)
 {
     BlockSlot sl = {0, 0, 0};
     ZTile z;
@@ -41,7 +68,7 @@ __device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, uint64_
     uint32_t size = 0;
     if (threadIdx.x < z.nblk) {
         sl.n = zg_block_len(z.seg_len, a.g.L, z.blk0 + threadIdx.x);
-        sl.b = a.idx.widths[z.gblk0 + threadIdx.x];
+        sl.b = ix.b;
         if (sl.b > 32) {
             bad |= ZERR_CORRUPT;
             sl.b = 0;
@@ -52,7 +79,7 @@ __device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, uint64_
     sl.off = cta_excl_scan(size, wsum, &total);
     total += z.has_head ? 4u : 0u;
     if (threadIdx.x == 0) {
-        uint64_t base = a.idx.tile_off[t];
+        uint64_t base = ix.base;
         uint32_t nload = total;
         /* overflow-safe: base comes from the index and is not trusted */
         if (base > a.avail || total > a.avail - base) {
@@ -61,21 +88,27 @@ __device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, uint64_
             if (base > a.avail) base = 0;
         }
         *s_base = base;
-        if (a.qprev_valid) *s_q0 = (uint32_t)a.idx.tile_qprev[t]; /* fetched early, used later */
+        *s_q0 = ix.q0;
         tma_load_superset(buf, a.in + base, nload, bar);
     }
     return sl;
 }
 
-template <bool FAST>
+/* ORDERED: tiles in ticket order, needed when the starting values come from
+ * the look-back (a CTA only ever waits on tiles claimed before its own).
+ * Otherwise every tile is independent and CTA c takes tiles c, c + grid,
+ * c + 2 grid, ..., with the index entries of the tile after next already
+ * loading. */
+template <bool FAST, bool ORDERED>
 __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem); /* [2] */
     uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 16);
-    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160);     /* [0,1] tiles, [2] q0 */
+    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160);     /* [0] claimed tile, [2] q0 */
     uint64_t *s_base = reinterpret_cast<uint64_t *>(smem + 192); /* [2] */
     uint32_t *s_q0 = reinterpret_cast<uint32_t *>(smem + 208);   /* [2] */
+    uint64_t *rec = reinterpret_cast<uint64_t *>(smem + 256);
     float *rows = reinterpret_cast<float *>(smem + a.sm.rows);
 
     const ZGeom &g = a.g;
@@ -90,28 +123,35 @@ __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
-        bc[0] = atomicAdd(a.w.ticket, 1u);
+        if (ORDERED) bc[0] = atomicAdd(a.w.ticket, 1u);
     }
     __syncthreads();
+    uint64_t tile = ORDERED ? bc[0] : blockIdx.x;
+    uint64_t tnext = tile + gridDim.x; /* the static order's next tile */
+    TileIdx ix = load_idx(a, tile);
     BlockSlot cur = {0, 0, 0};
-    if (bc[0] < g.ntiles)
-        cur = stage_tile(a, bc[0], smem + a.sm.in0, &bar[0], wsum, &s_base[0], &s_q0[0], bad);
+    if (tile < g.ntiles) cur = stage_tile(a, tile, ix, smem + a.sm.in0, &bar[0], wsum, &s_base[0], &s_q0[0], bad);
+    if (!ORDERED) ix = load_idx(a, tnext);
 
     for (uint32_t it = 0;; it++) {
         const uint32_t cb = it & 1u;
-        __syncthreads();
-        const uint64_t tile = bc[cb];
+        __syncthreads(); /* the previous tile's buffer, rows and slots are free */
         if (tile >= g.ntiles) break;
         ZTile z;
         zg_tile(&g, tile, &z);
 
-        /* 1. claim the next tile and start its copy */
-        if (tid == 0) bc[cb ^ 1u] = atomicAdd(a.w.ticket, 1u);
-        __syncthreads();
+        /* 1. the next tile: its sizes, offsets and TMA copy */
+        if (ORDERED) {
+            if (tid == 0) bc[0] = atomicAdd(a.w.ticket, 1u);
+            __syncthreads();
+            tnext = bc[0];
+            ix = load_idx(a, tnext);
+        }
         BlockSlot nxt = {0, 0, 0};
-        if (bc[cb ^ 1u] < g.ntiles)
-            nxt = stage_tile(a, bc[cb ^ 1u], smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u], wsum,
+        if (tnext < g.ntiles)
+            nxt = stage_tile(a, tnext, ix, smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u], wsum,
                              &s_base[cb ^ 1u], &s_q0[cb ^ 1u], bad);
+        if (!ORDERED) ix = load_idx(a, tnext + gridDim.x);
 
         /* 2. unpack this tile's deltas */
         mbar_wait(&bar[cb], (it >> 1) & 1u, a.w.err);
@@ -144,11 +184,11 @@ __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
         const uint32_t pre = cta_excl_scan(bsum, wsum, &tsum);
         if (a.qprev_valid) {
             if (tid == 0) bc[2] = z.has_head ? (uint32_t)head : s_q0[cb];
-        } else if (warp == 0) {
-            lb_publish(a.w.status, tile, tsum, z.has_head != 0, (uint32_t)head);
+        } else {
+            if (warp == 0) lb_publish(a.w.status, tile, tsum, z.has_head != 0, (uint32_t)head);
             const uint64_t q0 =
-                lb_resolve(a.w.status, tile, tsum, z.has_head != 0, (uint32_t)head, a.w.err);
-            if (lane == 0) {
+                lb_resolve_cta(a.w.status, tile, tsum, z.has_head != 0, (uint32_t)head, a.w.err, rec);
+            if (tid == 0) {
                 bc[2] = (uint32_t)q0;
                 a.idx.tile_qprev[tile] = (int32_t)(uint32_t)q0;
             }
@@ -174,12 +214,26 @@ __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
         }
         if (z.has_head && tid == 0) a.y[z.seg_start] = __fmul_rn(__int2float_rn(head), a.eb);
         __syncthreads();
-        for (uint32_t k = warp; k < z.nblk; k += nw) {
-            const uint32_t nk = zg_block_len(z.seg_len, L, z.blk0 + k);
-            float *dst = a.y + z.e_first + (uint64_t)k * L;
-            for (uint32_t j = lane; j < nk; j += 32) dst[j] = rows[k * stride + j];
+        if (FAST && L == 32 && z.nblk == g.TB && z.e_end - z.e_first == 32ull * g.TB) {
+            /* a full tile: 32-float rows, unrolled so that many stores are
+             * in flight per warp */
+            float *dst = a.y + z.e_first + lane;
+            const uint32_t nrow = g.TB / nw; /* rows per warp */
+#pragma unroll 8
+            for (uint32_t r = 0; r < nrow; r++) {
+                const uint32_t k = warp + r * nw;
+                dst[k * 32u] = rows[k * stride + lane];
+            }
+        } else {
+            for (uint32_t k = warp; k < z.nblk; k += nw) {
+                const uint32_t nk = zg_block_len(z.seg_len, L, z.blk0 + k);
+                float *dst = a.y + z.e_first + (uint64_t)k * L;
+                for (uint32_t j = lane; j < nk; j += 32) dst[j] = rows[k * stride + j];
+            }
         }
         cur = nxt;
+        tile = tnext;
+        if (!ORDERED) tnext += gridDim.x;
     }
     if (bad) atomicOr(a.w.err, bad);
 }
@@ -188,14 +242,14 @@ __global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
 
 cudaError_t launch_decompress(const DecompressArgs &a, cudaStream_t st)
 {
-    const bool fast = a.g.L <= 32;
-    const void *fn = fast ? (const void *)k_decompress<true> : (const void *)k_decompress<false>;
+    const bool fast = a.g.L <= 32, ordered = !a.qprev_valid;
+    const void *fn = fast ? (ordered ? (const void *)k_decompress<true, true>
+                                     : (const void *)k_decompress<true, false>)
+                          : (ordered ? (const void *)k_decompress<false, true>
+                                     : (const void *)k_decompress<false, false>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
     if (e != cudaSuccess) return e;
     unsigned grid = persistent_grid(fn, a.g.TB, a.sm.total, a.g.ntiles);
-    if (fast)
-        k_decompress<true><<<grid, a.g.TB, a.sm.total, st>>>(a);
-    else
-        k_decompress<false><<<grid, a.g.TB, a.sm.total, st>>>(a);
-    return cudaGetLastError();
+    void *args[] = {const_cast<DecompressArgs *>(&a)};
+    return cudaLaunchKernel(fn, dim3(grid), dim3(a.g.TB), args, a.sm.total, st);
 }

@@ -13,12 +13,13 @@
  * tile's P inputs form a stream of TMA copies through two buffers: while one
  * input's tile bytes are unpacked and added into per-thread registers, the
  * next input's sizes are scanned from its width index and its bytes are
- * already in flight.
- * Zero-width input blocks are skipped without touching their bytes.  After
- * the last input the sum is re-encoded like the compressor does (width,
- * scan, early look-back publish, packing, realigned vector stores) and the
- * output's side index is written; its starting value per tile is the sum of
- * the inputs' values.
+ * already in flight.  Zero-width input blocks are skipped without touching
+ * their bytes.  After the last input the sum is re-encoded like the
+ * compressor does (width, scan, early look-back publish); like the
+ * compressor, the CTA then places the sum it packed one round before (one
+ * tile after that sum published its size), claims its next tile and starts
+ * that tile's first copy, and packs the new sum while the copy runs.  The
+ * starting value per tile is the sum of the inputs' values.
  */
 #include "zkern.cuh"
 
@@ -27,15 +28,6 @@ namespace {
 struct BlockSlot {
     uint32_t b, n, off;
 };
-
-/* acc[j] for a runtime j (short tail blocks only). */
-__device__ __forceinline__ uint32_t &pick(uint32_t (&acc)[32], uint32_t j)
-{
-#pragma unroll
-    for (int k = 0; k < 31; k++)
-        if ((uint32_t)k == j) return acc[k];
-    return acc[31];
-}
 
 /* All threads: sizes of input p's blocks in tile t, their offsets, and
  * (thread 0) the TMA copy of those bytes into buf. */
@@ -81,14 +73,15 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
     extern __shared__ __align__(16) uint8_t smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem); /* [2] */
     uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 16);
-    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160);     /* [0] tile, [1] prefix */
+    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160);     /* [0] tile */
     uint64_t *s_base = reinterpret_cast<uint64_t *>(smem + 192); /* [2] */
+    uint64_t *rec = reinterpret_cast<uint64_t *>(smem + 256);
     uint32_t *acc_rows = reinterpret_cast<uint32_t *>(smem + a.sm.rows);
     uint8_t *outs = smem + a.sm.out;
     const uint32_t outs_sa = smem_u32(outs);
 
     const ZGeom &g = a.g;
-    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
     const uint32_t L = g.L, stride = zg_row_stride(L), P = a.P;
     uint32_t bad = 0;
     /* see k_decompress: a failed index walk stops every CTA alike */
@@ -99,21 +92,23 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
     }
     uint32_t acc[32];
     uint32_t ld = 0; /* index of the current copy in the two-buffer stream */
+    ZPending pd = {ZP_NONE, 0, 0, 0};
+
+    /* Tiles are claimed one at a time when the CTA is ready for them, and
+     * the CTA never waits while it holds a claimed tile whose size is not
+     * yet published, so later tiles never wait on a tile sitting idle. */
+    if (tid == 0) bc[0] = atomicAdd(a.w.ticket, 1u);
+    __syncthreads();
+    uint64_t tile = bc[0];
+    BlockSlot cur = {0, 0, 0};
+    if (tile < g.ntiles)
+        cur = stage_input(a, tile, 0, smem + a.sm.in0, &bar[0], wsum, &s_base[0], bad);
 
     for (;;) {
-        /* Claim a tile only when this CTA is ready to work on it, so that a
-         * claimed tile publishes its size soon after and later tiles never
-         * wait on a tile that sits idle behind another one. */
-        if (tid == 0) bc[0] = atomicAdd(a.w.ticket, 1u);
-        __syncthreads();
-        const uint64_t tile = bc[0];
         if (tile >= g.ntiles) break;
         ZTile z;
         zg_tile(&g, tile, &z);
         const bool own = tid < z.nblk;
-        BlockSlot cur =
-            stage_input(a, tile, 0, smem + (ld & 1u ? a.sm.in1 : a.sm.in0), &bar[ld & 1u], wsum,
-                        &s_base[ld & 1u], bad);
         const uint32_t n = cur.n;
         const bool full = FAST && own && n == 32;
         if (FAST) {
@@ -154,7 +149,7 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
 #pragma unroll
                         for (int j = 0; j < 32; j++) acc[j] += v[j];
                     } else if (FAST) {
-                        decode_any(sw, o, b, n, [&](uint32_t j, uint32_t v) { pick(acc, j) += v; });
+                        decode_any(sw, o, b, n, [&](uint32_t j, uint32_t v) { add_at(acc, j, v); });
                     } else {
                         decode_any(sw, o, b, n,
                                    [&](uint32_t j, uint32_t v) { acc_rows[tid * stride + j] += v; });
@@ -179,7 +174,7 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
                 atomicAdd(a.cases + 3, (unsigned long long)c3);
             }
         }
-        /* re-encode the sum */
+        /* width of the sum, offsets in the tile, early size publication */
         uint32_t b = 0, size = 0, smask = 0;
         if (full) {
             uint32_t mx = 0;
@@ -204,6 +199,19 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
         const uint32_t off = cta_excl_scan(size, wsum, &total);
         total += headb;
         if (warp == 0) lb_publish(a.w.status, tile, total, tile == 0, 0);
+
+        /* place the sum packed one round ago (its size went out a whole tile
+         * earlier), then claim the next tile and start its first input's
+         * copy, and pack this sum while it arrives */
+        if (pd.tile != ZP_NONE)
+            place_tile(g, pd, outs, a.out, a.cap, a.idx, a.qprev_valid != 0, a.w.status, a.w.err, rec,
+                       bad);
+        if (tid == 0) bc[0] = atomicAdd(a.w.ticket, 1u);
+        __syncthreads();
+        const uint64_t next = bc[0];
+        if (next < g.ntiles)
+            cur = stage_input(a, next, 0, smem + (ld & 1u ? a.sm.in1 : a.sm.in0), &bar[ld & 1u], wsum,
+                              &s_base[ld & 1u], bad);
         smem_zero(outs, total + 8);
         __syncthreads();
         if (z.has_head && tid == 0) *reinterpret_cast<uint32_t *>(outs) = hsum;
@@ -217,28 +225,16 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
                 mg = (uint32_t)abs((int32_t)v);
             });
         }
-        if (warp == 0) {
-            const uint64_t prefix = lb_resolve(a.w.status, tile, total, tile == 0, 0, a.w.err);
-            if (lane == 0) bc[1] = prefix;
-        }
-        __syncthreads();
-        const uint64_t base = 8ull * g.T + bc[1];
-        const bool fits = base + total <= a.cap; /* uniform over the CTA */
-        if (!fits) bad |= ZERR_CAPACITY;
-        if (own) a.idx.widths[z.gblk0 + tid] = (uint8_t)b;
-        if (tid == 0) {
-            a.idx.tile_off[tile] = base;
-            if (a.qprev_valid) a.idx.tile_qprev[tile] = (int32_t)qsum;
-            if (fits && z.has_head && z.seg < g.T) {
-                const uint64_t h = base - 8ull * g.T;
-#pragma unroll
-                for (int k = 0; k < 8; k++) a.out[8ull * z.seg + k] = (uint8_t)(h >> (8 * k));
-            }
-            if (tile == g.ntiles - 1) *a.idx.size = base + total;
-        }
-        if (fits) store_realign(a.out + base, outs, total);
-        __syncthreads(); /* buffers, outs and the broadcast slots are reused */
+        pd.tile = tile;
+        pd.total = total;
+        pd.b = b;
+        pd.q = qsum;
+        tile = next;
+        __syncthreads(); /* the packed sum is complete; acc_rows are free */
     }
+    /* the last packed sum */
+    if (pd.tile != ZP_NONE)
+        place_tile(g, pd, outs, a.out, a.cap, a.idx, a.qprev_valid != 0, a.w.status, a.w.err, rec, bad);
     if (bad) atomicOr(a.w.err, bad);
 }
 

@@ -114,6 +114,44 @@ size_t walk_w1_warp_bytes(uint32_t M);
 
 /* Grid of a persistent kernel: every CTA that fits on the device at once,
  * but no more CTAs than tiles. */
+/* A packed tile in shared memory waiting for its place in the stream. */
+struct ZPending {
+    uint64_t tile;  /* ZP_NONE when there is none (uniform over the CTA) */
+    uint32_t total; /* its bytes */
+    uint32_t b;     /* this thread's block width */
+    uint32_t q;     /* thread 0: quantized value before the tile, for the index */
+};
+#define ZP_NONE (~0ull)
+
+/* All threads of the CTA: find the pending tile's byte offset with the
+ * CTA-wide look-back, write its side-index entries (and its segment's chunk
+ * offset when it opens a segment), and store its bytes from s_out.  The
+ * caller synchronises before s_out is reused. */
+__device__ __forceinline__ void place_tile(const ZGeom &g, const ZPending &pd, const uint8_t *s_out,
+                                           uint8_t *out, uint64_t cap, const ZIndex &idx, bool write_q,
+                                           uint64_t *status, uint32_t *err, uint64_t *rec,
+                                           uint32_t &bad)
+{
+    const uint64_t prefix = lb_resolve_cta(status, pd.tile, pd.total, pd.tile == 0, 0, err, rec);
+    const uint64_t base = 8ull * g.T + prefix;
+    const bool fits = base + pd.total <= cap; /* uniform over the CTA */
+    if (!fits) bad |= ZERR_CAPACITY;
+    ZTile z;
+    zg_tile(&g, pd.tile, &z);
+    if (threadIdx.x < z.nblk) idx.widths[z.gblk0 + threadIdx.x] = (uint8_t)pd.b;
+    if (threadIdx.x == 0) {
+        idx.tile_off[pd.tile] = base;
+        if (write_q) idx.tile_qprev[pd.tile] = (int32_t)pd.q;
+        if (fits && z.has_head && z.seg < g.T) {
+            const uint64_t h = base - 8ull * g.T;
+#pragma unroll
+            for (int k = 0; k < 8; k++) out[8ull * z.seg + k] = (uint8_t)(h >> (8 * k));
+        }
+        if (pd.tile == g.ntiles - 1) *idx.size = base + pd.total;
+    }
+    if (fits) store_realign(out + base, s_out, pd.total);
+}
+
 static inline unsigned persistent_grid(const void *fn, int threads, size_t smem, uint64_t ntiles)
 {
     int dev = 0, nsm = 0, occ = 0;
