@@ -357,11 +357,23 @@ __device__ __forceinline__ void add_at(uint32_t (&v)[32], uint32_t j, uint32_t x
 }
 
 /* Zero shared bytes [0, nbytes) (rounded up to 16) of a 16-byte-aligned buffer. */
-__device__ __forceinline__ void smem_zero(uint8_t *s, uint32_t nbytes)
+__device__ __forceinline__ void smem_zero(uint8_t *s, uint32_t nbytes, uint32_t t, uint32_t nt)
 {
     uint4 *s4 = reinterpret_cast<uint4 *>(s);
     const uint4 z = make_uint4(0, 0, 0, 0);
-    for (uint32_t i = threadIdx.x; i < (nbytes + 15u) >> 4; i += blockDim.x) s4[i] = z;
+    for (uint32_t i = t; i < (nbytes + 15u) >> 4; i += nt) s4[i] = z;
+}
+
+__device__ __forceinline__ void smem_zero(uint8_t *s, uint32_t nbytes)
+{
+    smem_zero(s, nbytes, threadIdx.x, blockDim.x);
+}
+
+/* Barrier `id` (1..15) over the first n threads of the CTA (a multiple of
+ * 32), for kernels whose warps split into groups; id 0 is __syncthreads. */
+__device__ __forceinline__ void named_sync(uint32_t id, uint32_t n)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
 /* ---------------------------------------------------------------------
@@ -380,6 +392,13 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
                  "r"(bytes)
                  : "memory");
+}
+
+/* One arrival on a barrier (release at CTA scope: the caller's earlier
+ * shared-memory writes are visible to whoever sees the phase complete). */
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 /* Wait for phase `parity` of the barrier to complete.  Gives up after a
@@ -435,25 +454,25 @@ __device__ __forceinline__ void tma_load_superset(uint8_t *s, const uint8_t *g, 
  * assembled from two aligned shared loads and funnel shifts; the ragged
  * ends (shared with neighbouring tiles) are stored byte by byte.  s must be
  * 16-byte aligned with 32 readable bytes of slack.  Called by all threads. */
-__device__ __forceinline__ void store_realign(uint8_t *g, const uint8_t *s, uint32_t nbytes)
+__device__ __forceinline__ void store_realign(uint8_t *g, const uint8_t *s, uint32_t nbytes, uint32_t tid,
+                                              uint32_t nt)
 {
     const uintptr_t g0 = (uintptr_t)g, g1 = g0 + nbytes;
     const uintptr_t a0 = (g0 + 15u) & ~(uintptr_t)15u, a1 = g1 & ~(uintptr_t)15u;
-    const uint32_t tid = threadIdx.x;
     if (a1 <= a0) {
-        for (uint32_t i = tid; i < nbytes; i += blockDim.x) g[i] = s[i];
+        for (uint32_t i = tid; i < nbytes; i += nt) g[i] = s[i];
         return;
     }
     const uint32_t d = (uint32_t)(a0 - g0); /* shared offset of the first aligned chunk */
     const uint32_t tail = (uint32_t)(g1 - a1);
-    for (uint32_t i = tid; i < d + tail; i += blockDim.x) { /* ragged ends, any block size */
+    for (uint32_t i = tid; i < d + tail; i += nt) { /* ragged ends, any thread count */
         const uint32_t k = i < d ? i : (uint32_t)(a1 - g0) + (i - d);
         g[k] = s[k];
     }
     const uint32_t nch = (uint32_t)((a1 - a0) >> 4), q = d >> 2, sh = (d & 3u) * 8u;
     const uint4 *s4 = reinterpret_cast<const uint4 *>(s);
     uint4 *g4 = reinterpret_cast<uint4 *>(a0);
-    for (uint32_t c = tid; c < nch; c += blockDim.x) {
+    for (uint32_t c = tid; c < nch; c += nt) {
         uint4 lo = s4[c], hi = s4[c + 1];
         uint32_t o0, o1, o2, o3, o4;
         /* q is the same for every thread of the tile: a uniform branch */
@@ -472,6 +491,11 @@ __device__ __forceinline__ void store_realign(uint8_t *g, const uint8_t *s, uint
     }
 }
 
+__device__ __forceinline__ void store_realign(uint8_t *g, const uint8_t *s, uint32_t nbytes)
+{
+    store_realign(g, s, nbytes, threadIdx.x, blockDim.x);
+}
+
 /* ---------------------------------------------------------------------
  * Block-wide exclusive scans (blockDim.x <= 1024, multiple of 32).
  * `wsum` is shared scratch of 33 words.
@@ -487,25 +511,33 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v)
     return v;
 }
 
-/* Exclusive scan of v over the CTA (wrapping uint32 add, so it also serves
- * int32 sums); *total receives the sum of all v. */
-__device__ __forceinline__ uint32_t cta_excl_scan(uint32_t v, uint32_t *wsum, uint32_t *total)
+/* Exclusive scan of v over the first n threads of the CTA, synchronised
+ * on barrier `id` (wrapping uint32 add, so it also serves int32 sums);
+ * *total receives the sum of all v. */
+__device__ __forceinline__ uint32_t grp_excl_scan(uint32_t v, uint32_t *wsum, uint32_t *total, uint32_t n,
+                                                  uint32_t id)
 {
-    uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = n >> 5;
     uint32_t inc = warp_incl_scan(v);
     if (lane == 31) wsum[warp] = inc;
-    __syncthreads();
+    named_sync(id, n);
     if (warp == 0) {
         uint32_t t = lane < nw ? wsum[lane] : 0u;
         uint32_t ti = warp_incl_scan(t);
         if (lane < nw) wsum[lane] = ti - t;
         if (lane == 31) wsum[32] = ti;
     }
-    __syncthreads();
+    named_sync(id, n);
     uint32_t r = wsum[warp] + inc - v;
     *total = wsum[32];
-    __syncthreads();
+    named_sync(id, n);
     return r;
+}
+
+/* The same over the whole CTA. */
+__device__ __forceinline__ uint32_t cta_excl_scan(uint32_t v, uint32_t *wsum, uint32_t *total)
+{
+    return grp_excl_scan(v, wsum, total, blockDim.x, 0);
 }
 
 /* ---------------------------------------------------------------------

@@ -3,29 +3,26 @@
  *
  * Replaces ZCCL_float_openmp_threadblock_arg (ZCCL/src/ZCCL_float.c:501-807)
  * and produces the same bytes.  Persistent CTAs take tiles of TB blocks in
- * ticket order; one thread owns one block.  Per tile:
- *   1. its floats (and the element before them) arrive by one TMA bulk
+ * ticket order.  Each CTA runs TB compute threads, one per block, and one
+ * placer warp.  Per tile, the compute warps
+ *   1. receive its floats (and the element before them) by one TMA bulk
  *      copy; a warp-cooperative transpose puts every block in its own padded
  *      row, so the per-thread walk below has no bank conflicts, and finds
  *      the tile's largest magnitude, which decides whether the one-multiply
  *      quantization is exact for the whole tile;
- *   2. every thread quantizes its block (truncation, ZCCL_float.c:580),
- *      forms the running deltas (ZCCL_float.c:581-582; the element before the
- *      block supplies the first one), sign mask, largest magnitude, width
+ *   2. quantize every block (truncation, ZCCL_float.c:580) and form the
+ *      running deltas (ZCCL_float.c:581-582; the element before the block
+ *      supplies the first one), sign mask, largest magnitude, width
  *      (ZCCL_float.c:606) and encoded size;
- *   3. a block-wide scan gives each block its offset in the tile, and the
- *      tile's size is published for the decoupled look-back at once;
- *   4. the CTA places the tile it packed one round before: a CTA-wide
- *      look-back gives its byte offset, its bytes go out with 16-byte vector
- *      stores realigned to that offset, and the side index (block widths,
- *      byte offset, quantized value before the tile) is written.  Placing a
- *      tile one round late gives its predecessors a whole tile's time to
- *      publish their sizes, so the look-back rarely waits, and the CTA never
- *      waits while it holds a claimed tile whose size is not yet published
- *      (the reference's per-thread scan and second memcpy pass,
- *      ZCCL_float.c:774-791, disappear);
- *   5. the next tile is claimed and its copy started, and this tile's
- *      blocks are packed into shared memory meanwhile.
+ *   3. scan the block sizes for their offsets in the tile and publish the
+ *      tile's size for the decoupled look-back at once;
+ *   4. claim the next tile (starting its copy) and pack this one into
+ *      shared memory, then hand it to the placer.
+ * The placer finds the packed tile's byte offset with the look-back, writes
+ * its bytes with 16-byte vector stores realigned to that offset and records
+ * the offset, all while the compute warps work on the next tile, so the
+ * look-back's latency never stalls them (the reference's per-thread scan and
+ * second memcpy pass, ZCCL_float.c:774-791, disappear).
  * Full 32-element blocks with exact fast quantization take straight-line
  * code; other blocks of up to 32 elements are handled element by element
  * into the same registers, and blocks above 32 elements are re-read from
@@ -53,70 +50,127 @@ __device__ __forceinline__ void claim_tile(const CompressArgs &a, uint8_t *in, u
     }
 }
 
-/* Six CTAs per SM fit the shared memory (about 35 KB each); asking for
- * them caps the registers at 80, and the few values spilled around the
- * placement cost less than a seventh of the SM's warps. */
+/* Block size TB + 32: warps 0 .. TB/32 - 1 compute (one thread per block of
+ * the tile), the last warp places packed tiles in the stream. */
 template <bool FAST>
-__global__ void __launch_bounds__(128, 6) k_compress(const CompressArgs a)
+__global__ void __launch_bounds__(160, 5) k_compress(const CompressArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
-    uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 16);
-    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160); /* [0] claimed tile */
-    uint32_t *s_amax = reinterpret_cast<uint32_t *>(smem + 192);
-    uint64_t *rec = reinterpret_cast<uint64_t *>(smem + 256);
+    uint64_t *bar_tma = reinterpret_cast<uint64_t *>(smem);          /* the tile's floats arrived */
+    uint64_t *bar_packed = reinterpret_cast<uint64_t *>(smem + 8);   /* a packed tile is in out */
+    uint64_t *bar_free = reinterpret_cast<uint64_t *>(smem + 16);    /* out may be overwritten */
+    uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 32);        /* [33] */
+    uint64_t *s_tile = reinterpret_cast<uint64_t *>(smem + 168);     /* the claimed tile */
+    uint32_t *s_amax = reinterpret_cast<uint32_t *>(smem + 176);
+    uint64_t *s_pend = reinterpret_cast<uint64_t *>(smem + 184);     /* the tile in out */
+    uint32_t *s_ptotal = reinterpret_cast<uint32_t *>(smem + 192);   /* its bytes */
     float *rows = reinterpret_cast<float *>(smem + a.sm.rows); /* FAST: the same space as in */
     uint8_t *in = smem + a.sm.in0;
     uint8_t *outb = smem + a.sm.out;
     const uint32_t out_sa = smem_u32(outb);
 
     const ZGeom &g = a.g;
-    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, nw = blockDim.x >> 5;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t NC = g.TB, nw = NC >> 5; /* compute threads, compute warps */
     const uint32_t L = g.L, stride = zg_row_stride(L);
     uint32_t bad = 0;
-    ZPending pd = {ZP_NONE, 0, 0, 0};
 
-    if (tid == 0) mbar_init(bar, 1);
-    claim_tile(a, in, bar, &bc[0], s_amax);
+    if (tid == 0) {
+        mbar_init(bar_tma, 1);
+        mbar_init(bar_packed, 1);
+        mbar_init(bar_free, 1);
+    }
     __syncthreads();
-    uint64_t tile = bc[0];
+
+    if (tid >= NC) {
+        /* The placer: for every packed tile, the decoupled look-back gives
+         * its byte offset; its bytes go out with 16-byte vector stores
+         * realigned to that offset, with its offset in the side index and,
+         * for a segment's first tile, the chunk offset in the header.  It
+         * runs while the compute warps work on the next tile, so the
+         * look-back's latency stays off their path. */
+        if (lane == 0) mbar_arrive(bar_free); /* out starts empty */
+        for (uint64_t k = 0; k <= g.ntiles; k++) {
+            mbar_wait(bar_packed, (uint32_t)k & 1u, a.w.err);
+            const uint64_t t = *s_pend;
+            const uint32_t total = *s_ptotal;
+            if (t >= g.ntiles) break;
+            const uint64_t base = 8ull * g.T + lb_resolve(a.w.status, t, total, t == 0, 0, a.w.err);
+            const bool fits = base + total <= a.cap;
+            if (!fits) bad |= ZERR_CAPACITY;
+            if (lane == 0) {
+                ZTile z;
+                zg_tile(&g, t, &z);
+                a.idx.tile_off[t] = base;
+                if (fits && z.has_head && z.seg < g.T) {
+                    const uint64_t h = base - 8ull * g.T;
+#pragma unroll
+                    for (int k8 = 0; k8 < 8; k8++) a.out[8ull * z.seg + k8] = (uint8_t)(h >> (8 * k8));
+                }
+                if (t == g.ntiles - 1) *a.idx.size = base + total;
+            }
+            if (fits) store_realign(a.out + base, outb, total, lane, 32);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(bar_free);
+        }
+        if (bad) atomicOr(a.w.err, bad);
+        return;
+    }
+
+    /* the compute warps */
+    if (tid == 0) claim_tile(a, in, bar_tma, s_tile, s_amax);
+    named_sync(1, NC);
+    uint64_t tile = *s_tile;
 
     for (uint32_t it = 0;; it++) {
-        if (tile >= g.ntiles) break;
+        if (tile >= g.ntiles) {
+            /* tell the placer there is nothing more, once it has taken the last tile */
+            mbar_wait(bar_free, it & 1u, a.w.err);
+            if (tid == 0) {
+                *s_pend = ZP_NONE;
+                mbar_arrive(bar_packed);
+            }
+            break;
+        }
         ZTile z;
         zg_tile(&g, tile, &z);
 
         /* 1. wait for the floats, move every block into its own padded row
          *    (so the per-thread walk below has no bank conflicts), and find
          *    the tile's largest magnitude */
-        mbar_wait(bar, it & 1u, a.w.err);
+        mbar_wait(bar_tma, it & 1u, a.w.err);
         const float *xin =
             reinterpret_cast<const float *>(in + ((uintptr_t)(a.x + (z.e_first - 1)) & 15u));
         const float xprev0 = xin[0]; /* the head, or the last element of the previous tile */
         uint32_t amax = abs_bits(xprev0);
         if (FAST) {
-            /* warp w owns rows w, w + nw, ... (32 of them: TB = 128 when
-             * L <= 32); all floats are read before any row overwrites them */
-            float v[32];
+            /* TB = 128 rows (L <= 32) in four chunks of 32, warp w owning
+             * rows w, w + nw, ... of each.  The rows overlay the floats: row
+             * k (stride above L) covers floats of rows k and later only, and
+             * never a float of a lower chunk.  So chunks go highest first,
+             * each read into registers before any of its rows is written. */
             const bool full = L == 32 && z.nblk == g.TB && z.e_end - z.e_first == 32ull * g.TB;
-            if (full) {
+            for (int c = 3; c >= 0; c--) {
+                float v[8];
+                if (full) {
 #pragma unroll
-                for (int r = 0; r < 32; r++) v[r] = xin[1 + (warp + r * nw) * 32 + lane];
-            } else {
+                    for (int r = 0; r < 8; r++) v[r] = xin[1 + (warp + (uint32_t)(8 * c + r) * nw) * 32 + lane];
+                } else {
 #pragma unroll
-                for (int r = 0; r < 32; r++) {
-                    const uint32_t k = warp + r * nw;
-                    v[r] = 0.0f;
-                    if (k < z.nblk && lane < zg_block_len(z.seg_len, L, z.blk0 + k))
-                        v[r] = xin[1 + k * L + lane];
+                    for (int r = 0; r < 8; r++) {
+                        const uint32_t k = warp + (uint32_t)(8 * c + r) * nw;
+                        v[r] = 0.0f;
+                        if (k < z.nblk && lane < zg_block_len(z.seg_len, L, z.blk0 + k))
+                            v[r] = xin[1 + k * L + lane];
+                    }
                 }
-            }
 #pragma unroll
-            for (int r = 0; r < 32; r++) amax = max(amax, abs_bits(v[r]));
-            __syncthreads();
-            if (lane < L) { /* a row holds L floats */
+                for (int r = 0; r < 8; r++) amax = max(amax, abs_bits(v[r]));
+                named_sync(1, NC);
+                if (lane < L) { /* a row holds L floats */
 #pragma unroll
-                for (int r = 0; r < 32; r++) rows[(warp + r * nw) * stride + lane] = v[r];
+                    for (int r = 0; r < 8; r++) rows[(warp + (uint32_t)(8 * c + r) * nw) * stride + lane] = v[r];
+                }
             }
         } else {
             for (uint32_t k = warp; k < z.nblk; k += nw) {
@@ -130,7 +184,7 @@ __global__ void __launch_bounds__(128, 6) k_compress(const CompressArgs a)
         }
         amax = __reduce_max_sync(0xffffffffu, amax);
         if (lane == 0) atomicMax(s_amax, amax);
-        __syncthreads();
+        named_sync(1, NC);
         const bool fastq = tile_fast_ok(*s_amax, a.inv);
 
         /* 2. quantize, delta, width */
@@ -183,30 +237,27 @@ __global__ void __launch_bounds__(128, 6) k_compress(const CompressArgs a)
             size = zg_block_bytes(b, n);
         }
 
-        /* 3. offsets in the tile and early publication of its size; the
+        /* 3. offsets in the tile and early publication of its size (the
          *    scan's barriers also end every read of the rows above when
-         *    L <= 32 */
+         *    L <= 32); the index entries that do not depend on the tile's
+         *    place */
         const uint32_t headb = z.has_head ? 4u : 0u;
         uint32_t total;
-        const uint32_t off = cta_excl_scan(size, wsum, &total);
+        const uint32_t off = grp_excl_scan(size, wsum, &total, NC, 1);
         total += headb;
         if (warp == 0) lb_publish(a.w.status, tile, total, tile == 0, 0);
         const int32_t qprev0 = fastq ? quantize_fast(xprev0, a.inv) : quantize(xprev0, a.inv, bad);
+        if (own) a.idx.widths[z.gblk0 + tid] = (uint8_t)b;
+        if (tid == 0) a.idx.tile_qprev[tile] = qprev0;
 
-        /* 4. place the tile packed one round ago: its size went out a whole
-         *    tile's time ago, so its predecessors have had time to publish
-         *    theirs.  This CTA holds no claimed tile without a published
-         *    size while it waits here. */
-        if (pd.tile != ZP_NONE)
-            place_tile(g, pd, outb, a.out, a.cap, a.idx, true, a.w.status, a.w.err, rec, bad);
-        __syncthreads(); /* out is free again */
-
-        /* 5. claim the next tile, whose floats arrive while this one is
-         *    packed (with L <= 32 the rows are no longer needed: the
-         *    magnitudes are in registers) */
-        if (FAST) claim_tile(a, in, bar, &bc[0], s_amax);
-        smem_zero(outb, total + 8);
-        __syncthreads();
+        /* 4. once the placer has written out the previous tile, claim the
+         *    next tile (its floats arrive while this one is packed) and pack
+         *    this one.  Waiting before claiming means these warps never wait
+         *    while holding a claimed tile whose size is not yet published. */
+        mbar_wait(bar_free, it & 1u, a.w.err);
+        if (FAST && tid == 0) claim_tile(a, in, bar_tma, s_tile, s_amax);
+        smem_zero(outb, total + 8, tid, NC);
+        named_sync(1, NC);
         if (z.has_head && tid == 0) *reinterpret_cast<int32_t *>(outb) = qprev0;
         const uint32_t o = headb + off;
         if (FAST) {
@@ -229,19 +280,17 @@ __global__ void __launch_bounds__(128, 6) k_compress(const CompressArgs a)
                     mg = (uint32_t)abs(d);
                 });
             }
-            __syncthreads(); /* the rows have been read for the last time */
-            claim_tile(a, in, bar, &bc[0], s_amax);
+            named_sync(1, NC); /* the rows have been read for the last time */
+            if (tid == 0) claim_tile(a, in, bar_tma, s_tile, s_amax);
         }
-        pd.tile = tile;
-        pd.total = total;
-        pd.b = b;
-        pd.q = (uint32_t)qprev0;
-        __syncthreads(); /* the claimed index is visible; the packed tile is complete */
-        tile = bc[0];
+        named_sync(1, NC); /* the packed tile is complete; the claimed index is visible */
+        if (tid == 0) {
+            *s_pend = tile;
+            *s_ptotal = total;
+            mbar_arrive(bar_packed);
+        }
+        tile = *s_tile;
     }
-    /* the last packed tile */
-    if (pd.tile != ZP_NONE)
-        place_tile(g, pd, outb, a.out, a.cap, a.idx, true, a.w.status, a.w.err, rec, bad);
     if (bad) atomicOr(a.w.err, bad);
 }
 
@@ -253,10 +302,11 @@ cudaError_t launch_compress(const CompressArgs &a, cudaStream_t st)
     const void *fn = fast ? (const void *)k_compress<true> : (const void *)k_compress<false>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
     if (e != cudaSuccess) return e;
-    unsigned grid = persistent_grid(fn, a.g.TB, a.sm.total, a.g.ntiles);
+    const unsigned threads = a.g.TB + 32; /* compute warps and the placer warp */
+    unsigned grid = persistent_grid(fn, threads, a.sm.total, a.g.ntiles);
     if (fast)
-        k_compress<true><<<grid, a.g.TB, a.sm.total, st>>>(a);
+        k_compress<true><<<grid, threads, a.sm.total, st>>>(a);
     else
-        k_compress<false><<<grid, a.g.TB, a.sm.total, st>>>(a);
+        k_compress<false><<<grid, threads, a.sm.total, st>>>(a);
     return cudaGetLastError();
 }
