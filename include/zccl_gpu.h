@@ -106,7 +106,7 @@ typedef struct zccl_gpu_stream {
 
 /* Largest stream of n floats (every block at width 32). */
 size_t zccl_gpu_max_stream_bytes(size_t n, int L, int T);
-/* Bytes of the side index of one stream (about n/L + 12 per 4096 floats). */
+/* Bytes of the side index of one stream (about n/L + 12 per 8192 floats). */
 size_t zccl_gpu_index_bytes(size_t n, int L, int T);
 /* Bytes of device scratch one call needs (look-back state, error word). */
 size_t zccl_gpu_workspace_bytes(size_t n, int L, int T);
@@ -145,9 +145,9 @@ int zccl_gpu_homadd_cases(zccl_gpu_stream *out, zccl_gpu_stream *ins, int P, siz
  *
  * The scratch is a 1 MiB array (ZCCL_GPU_NOALLOC_SCRATCH_BYTES) inside this
  * library's device code, one per device.  A call needs 16 + 8 * tiles bytes
- * of it, a tile being up to 128 blocks of one segment (4096 floats at
- * L = 32), so n may reach about 5.3e8 floats at L = 32 and T = 1; fewer with
- * smaller L or many segments.  Larger inputs return ZCCL_GPU_ESCRATCH and
+ * of it, a tile being up to 256 blocks of one segment (8192 floats at
+ * L = 32), so n may reach about 1.07e9 floats at L = 32 and T = 1; fewer
+ * with smaller L or many segments.  Larger inputs return ZCCL_GPU_ESCRATCH and
  * launch nothing.  Those bytes must be zero when the kernel starts; the
  * call clears them itself on cuda_stream.
  *

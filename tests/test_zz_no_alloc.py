@@ -14,7 +14,7 @@ import zccl_gb300 as Z
 
 ESCRATCH = -9
 SCRATCH_BYTES = 1 << 20
-TILE_FLOATS = 128 * 32  # blocks per tile x block size at L = 32
+TILE_FLOATS = 256 * 32  # blocks per tile x block size at L = 32
 
 
 def _status(rc):

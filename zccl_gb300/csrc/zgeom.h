@@ -61,7 +61,7 @@ ZG_HD uint64_t zg_div_up(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
 
 ZG_HD uint32_t zg_tile_blocks(uint32_t L)
 {
-    if (L <= 32) return 128;
+    if (L <= 32) return 256;
     uint32_t k = 4096u / (32u * L);
     return 32u * (k ? k : 1u);
 }
@@ -167,6 +167,13 @@ ZG_HD uint32_t zg_a16(uint32_t v) { return (v + 15u) & ~15u; }
 /* Largest tile in bytes: head + TB blocks at width 32. */
 ZG_HD uint32_t zg_tile_worst(uint32_t L, uint32_t TB) { return TB * zg_block_bytes(32, L) + 4u; }
 
+/* Bytes a packed tile of `total` bytes takes in the output ring (its bytes,
+ * the packer's zeroed tail, 16-byte granularity), and the ring's size: the
+ * largest tile fits; readers may look 32 bytes past a tile, so the region
+ * behind the ring has that slack. */
+ZG_HD uint32_t zg_ring_need(uint32_t total) { return (total + 8u + 15u) & ~15u; }
+ZG_HD uint32_t zg_ring_bytes(uint32_t L, uint32_t TB) { return zg_ring_need(zg_tile_worst(L, TB)); }
+
 /* kind: 0 compressor, 1 decompressor, 2 homomorphic add.
  * The compressor stages one tile of floats at a time (in1 == in0) and keeps
  * a packed tile in out until the next tile has been quantized.  With
@@ -180,7 +187,7 @@ ZG_HD ZSmem zg_smem(uint32_t kind, uint32_t L, uint32_t TB)
     const uint32_t rows_bytes = TB * zg_row_stride(L) * 4u;
     const uint32_t raw_in = (TB * L + 1u) * 4u + 32u;     /* floats, 16-byte superset */
     const uint32_t tile_in = zg_tile_worst(L, TB) + 48u;  /* bytes, superset + reader slack */
-    const uint32_t tile_out = zg_tile_worst(L, TB) + 48u; /* realigning store reads 32 past */
+    const uint32_t tile_out = zg_ring_bytes(L, TB) + 48u; /* the ring; readers look 32 past */
     const int need_rows = kind != 2 || L > 32;
     m.rows = 512u;
     if (kind == 0) {

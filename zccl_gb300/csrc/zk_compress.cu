@@ -18,9 +18,10 @@
  *      tile's size for the decoupled look-back at once;
  *   4. claim the next tile (starting its copy) and pack this one into
  *      shared memory, then hand it to the placer.
- * The placer finds the packed tile's byte offset with the look-back, writes
+ * The packed tiles wait in a shared-memory ring that holds two typical
+ * tiles.  The placer finds each one's byte offset with the look-back, writes
  * its bytes with 16-byte vector stores realigned to that offset and records
- * the offset, all while the compute warps work on the next tile, so the
+ * the offset, all while the compute warps work on the next tiles, so the
  * look-back's latency never stalls them (the reference's per-thread scan and
  * second memcpy pass, ZCCL_float.c:774-791, disappear).
  * Full 32-element blocks with exact fast quantization take straight-line
@@ -53,21 +54,18 @@ __device__ __forceinline__ void claim_tile(const CompressArgs &a, uint8_t *in, u
 /* Block size TB + 32: warps 0 .. TB/32 - 1 compute (one thread per block of
  * the tile), the last warp places packed tiles in the stream. */
 template <bool FAST>
-__global__ void __launch_bounds__(160, 5) k_compress(const CompressArgs a)
+__global__ void __launch_bounds__(288, 3) k_compress(const CompressArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
-    uint64_t *bar_tma = reinterpret_cast<uint64_t *>(smem);          /* the tile's floats arrived */
-    uint64_t *bar_packed = reinterpret_cast<uint64_t *>(smem + 8);   /* a packed tile is in out */
-    uint64_t *bar_free = reinterpret_cast<uint64_t *>(smem + 16);    /* out may be overwritten */
-    uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 32);        /* [33] */
-    uint64_t *s_tile = reinterpret_cast<uint64_t *>(smem + 168);     /* the claimed tile */
+    uint64_t *bar_tma = reinterpret_cast<uint64_t *>(smem);      /* the tile's floats arrived */
+    uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 32);    /* [33] */
+    uint64_t *s_tile = reinterpret_cast<uint64_t *>(smem + 168); /* the claimed tile */
     uint32_t *s_amax = reinterpret_cast<uint32_t *>(smem + 176);
-    uint64_t *s_pend = reinterpret_cast<uint64_t *>(smem + 184);     /* the tile in out */
-    uint32_t *s_ptotal = reinterpret_cast<uint32_t *>(smem + 192);   /* its bytes */
+    uint32_t *s_pos = reinterpret_cast<uint32_t *>(smem + 184);  /* ring position of this tile */
+    ZRing *ring = reinterpret_cast<ZRing *>(smem + 256);
     float *rows = reinterpret_cast<float *>(smem + a.sm.rows); /* FAST: the same space as in */
     uint8_t *in = smem + a.sm.in0;
-    uint8_t *outb = smem + a.sm.out;
-    const uint32_t out_sa = smem_u32(outb);
+    uint8_t *outb = smem + a.sm.out; /* the ring of packed tiles */
 
     const ZGeom &g = a.g;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -77,58 +75,30 @@ __global__ void __launch_bounds__(160, 5) k_compress(const CompressArgs a)
 
     if (tid == 0) {
         mbar_init(bar_tma, 1);
-        mbar_init(bar_packed, 1);
-        mbar_init(bar_free, 1);
+        ring->packed = 0;
+        ring->placed = 0;
     }
     __syncthreads();
 
-    if (tid >= NC) {
-        /* The placer: for every packed tile, the decoupled look-back gives
-         * its byte offset; its bytes go out with 16-byte vector stores
-         * realigned to that offset, with its offset in the side index and,
-         * for a segment's first tile, the chunk offset in the header.  It
-         * runs while the compute warps work on the next tile, so the
-         * look-back's latency stays off their path. */
-        if (lane == 0) mbar_arrive(bar_free); /* out starts empty */
-        for (uint64_t k = 0; k <= g.ntiles; k++) {
-            mbar_wait(bar_packed, (uint32_t)k & 1u, a.w.err);
-            const uint64_t t = *s_pend;
-            const uint32_t total = *s_ptotal;
-            if (t >= g.ntiles) break;
-            const uint64_t base = 8ull * g.T + lb_resolve(a.w.status, t, total, t == 0, 0, a.w.err);
-            const bool fits = base + total <= a.cap;
-            if (!fits) bad |= ZERR_CAPACITY;
-            if (lane == 0) {
-                ZTile z;
-                zg_tile(&g, t, &z);
-                a.idx.tile_off[t] = base;
-                if (fits && z.has_head && z.seg < g.T) {
-                    const uint64_t h = base - 8ull * g.T;
-#pragma unroll
-                    for (int k8 = 0; k8 < 8; k8++) a.out[8ull * z.seg + k8] = (uint8_t)(h >> (8 * k8));
-                }
-                if (t == g.ntiles - 1) *a.idx.size = base + total;
-            }
-            if (fits) store_realign(a.out + base, outb, total, lane, 32);
-            __syncwarp();
-            if (lane == 0) mbar_arrive(bar_free);
-        }
+    if (tid >= NC) { /* the placer warp */
+        placer_loop(g, ring, outb, a.out, a.cap, a.idx, a.w.status, a.w.err, bad);
         if (bad) atomicOr(a.w.err, bad);
         return;
     }
 
     /* the compute warps */
+    const uint32_t R = zg_ring_bytes(L, NC);
+    uint32_t pos_prev = 0, end_prev = 0; /* thread 0: the previous tile's place in the ring */
     if (tid == 0) claim_tile(a, in, bar_tma, s_tile, s_amax);
     named_sync(1, NC);
     uint64_t tile = *s_tile;
 
     for (uint32_t it = 0;; it++) {
         if (tile >= g.ntiles) {
-            /* tell the placer there is nothing more, once it has taken the last tile */
-            mbar_wait(bar_free, it & 1u, a.w.err);
+            /* tell the placer there is nothing more (once it has read the slot) */
             if (tid == 0) {
-                *s_pend = ZP_NONE;
-                mbar_arrive(bar_packed);
+                ring_wait(&ring->placed, it >= 1 ? it - 1 : 0u, a.w.err);
+                ring_publish(ring, it, ZP_NONE, 0, 0);
             }
             break;
         }
@@ -144,7 +114,7 @@ __global__ void __launch_bounds__(160, 5) k_compress(const CompressArgs a)
         const float xprev0 = xin[0]; /* the head, or the last element of the previous tile */
         uint32_t amax = abs_bits(xprev0);
         if (FAST) {
-            /* TB = 128 rows (L <= 32) in four chunks of 32, warp w owning
+            /* TB rows (32 per compute warp) in four chunks, warp w owning
              * rows w, w + nw, ... of each.  The rows overlay the floats: row
              * k (stride above L) covers floats of rows k and later only, and
              * never a float of a lower chunk.  So chunks go highest first,
@@ -250,21 +220,28 @@ __global__ void __launch_bounds__(160, 5) k_compress(const CompressArgs a)
         if (own) a.idx.widths[z.gblk0 + tid] = (uint8_t)b;
         if (tid == 0) a.idx.tile_qprev[tile] = qprev0;
 
-        /* 4. once the placer has written out the previous tile, claim the
-         *    next tile (its floats arrive while this one is packed) and pack
-         *    this one.  Waiting before claiming means these warps never wait
+        /* 4. take room for the packed tile in the ring (waiting, if need
+         *    be, for the placer to write out an earlier one), claim the next
+         *    tile (its floats arrive while this one is packed) and pack this
+         *    one.  Claiming after any such wait means these warps never wait
          *    while holding a claimed tile whose size is not yet published. */
-        mbar_wait(bar_free, it & 1u, a.w.err);
-        if (FAST && tid == 0) claim_tile(a, in, bar_tma, s_tile, s_amax);
-        smem_zero(outb, total + 8, tid, NC);
+        if (tid == 0) {
+            *s_pos = ring_reserve(ring, it, zg_ring_need(total), R, pos_prev, end_prev, a.w.err);
+            if (FAST) claim_tile(a, in, bar_tma, s_tile, s_amax);
+        }
         named_sync(1, NC);
-        if (z.has_head && tid == 0) *reinterpret_cast<int32_t *>(outb) = qprev0;
+        const uint32_t pos = *s_pos;
+        uint8_t *pk = outb + pos;
+        const uint32_t pk_sa = smem_u32(pk);
+        smem_zero(pk, total + 8, tid, NC);
+        named_sync(1, NC);
+        if (z.has_head && tid == 0) *reinterpret_cast<int32_t *>(pk) = qprev0;
         const uint32_t o = headb + off;
         if (FAST) {
             if (n == 32) {
-                encode_full(out_sa, o, b, smask, m);
+                encode_full(pk_sa, o, b, smask, m);
             } else if (own) {
-                encode_any(out_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
+                encode_any(pk_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
                     neg = (smask >> (31u - j)) & 1u;
                     mg = pick(m, j);
                 });
@@ -272,7 +249,7 @@ __global__ void __launch_bounds__(160, 5) k_compress(const CompressArgs a)
         } else {
             if (own) {
                 int32_t qp = fastq ? quantize_fast(xp, a.inv) : quantize(xp, a.inv, bad);
-                encode_any(out_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
+                encode_any(pk_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
                     const int32_t q = fastq ? quantize_fast(row[j], a.inv) : quantize(row[j], a.inv, bad);
                     const int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
                     qp = q;
@@ -284,11 +261,7 @@ __global__ void __launch_bounds__(160, 5) k_compress(const CompressArgs a)
             if (tid == 0) claim_tile(a, in, bar_tma, s_tile, s_amax);
         }
         named_sync(1, NC); /* the packed tile is complete; the claimed index is visible */
-        if (tid == 0) {
-            *s_pend = tile;
-            *s_ptotal = total;
-            mbar_arrive(bar_packed);
-        }
+        if (tid == 0) ring_publish(ring, it, tile, total, pos);
         tile = *s_tile;
     }
     if (bad) atomicOr(a.w.err, bad);

@@ -100,7 +100,7 @@ __device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, uint64_
  * c + 2 grid, ..., with the index entries of the tile after next already
  * loading. */
 template <bool FAST, bool ORDERED>
-__global__ void __launch_bounds__(128) k_decompress(const DecompressArgs a)
+__global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem); /* [2] */

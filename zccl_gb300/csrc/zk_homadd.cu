@@ -9,17 +9,16 @@
  * canonical).  Integer addition is associative modulo 2^32, so one pass over
  * P inputs equals the ring's pairwise fold in any order, bit for bit.
  *
- * Persistent CTAs take tiles in ticket order, one thread per block.  A
- * tile's P inputs form a stream of TMA copies through two buffers: while one
- * input's tile bytes are unpacked and added into per-thread registers, the
- * next input's sizes are scanned from its width index and its bytes are
- * already in flight.  Zero-width input blocks are skipped without touching
- * their bytes.  After the last input the sum is re-encoded like the
- * compressor does (width, scan, early look-back publish); like the
- * compressor, the CTA then places the sum it packed one round before (one
- * tile after that sum published its size), claims its next tile and starts
- * that tile's first copy, and packs the new sum while the copy runs.  The
- * starting value per tile is the sum of the inputs' values.
+ * Persistent CTAs take tiles in ticket order, one compute thread per block
+ * plus one placer warp.  A tile's P inputs form a stream of TMA copies
+ * through two buffers: while one input's tile bytes are unpacked and added
+ * into per-thread registers, the next input's sizes are scanned from its
+ * width index and its bytes are already in flight.  Zero-width input blocks
+ * are skipped without touching their bytes.  After the last input the sum
+ * is re-encoded like the compressor does (width, scan, early look-back
+ * publish, packing), and the placer warp finds its place in the stream with
+ * the look-back and writes it out while the compute warps add the next
+ * tile.  The starting value per tile is the sum of the inputs' values.
  */
 #include "zkern.cuh"
 
@@ -29,8 +28,8 @@ struct BlockSlot {
     uint32_t b, n, off;
 };
 
-/* All threads: sizes of input p's blocks in tile t, their offsets, and
- * (thread 0) the TMA copy of those bytes into buf. */
+/* The compute threads: sizes of input p's blocks in tile t, their offsets,
+ * and (thread 0) the TMA copy of those bytes into buf. */
 __device__ __forceinline__ BlockSlot stage_input(const HomAddArgs &a, uint64_t t, uint32_t p,
                                                  uint8_t *buf, uint64_t *bar, uint32_t *wsum,
                                                  uint64_t *s_base, uint32_t &bad)
@@ -50,7 +49,7 @@ __device__ __forceinline__ BlockSlot stage_input(const HomAddArgs &a, uint64_t t
         size = zg_block_bytes(sl.b, sl.n);
     }
     uint32_t total;
-    sl.off = cta_excl_scan(size, wsum, &total);
+    sl.off = grp_excl_scan(size, wsum, &total, a.g.TB, 1);
     total += z.has_head ? 4u : 0u;
     if (threadIdx.x == 0) {
         uint64_t base = in.tile_off[t];
@@ -67,21 +66,24 @@ __device__ __forceinline__ BlockSlot stage_input(const HomAddArgs &a, uint64_t t
     return sl;
 }
 
+/* Block size TB + 32: warps 0 .. TB/32 - 1 add (one thread per block of the
+ * tile), the last warp places packed sums in the stream. */
 template <bool FAST>
-__global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
+__global__ void __launch_bounds__(288, 2) k_homadd(const HomAddArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem); /* [2] */
-    uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 16);
-    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160);     /* [0] tile */
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);          /* [2] input copies */
+    uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 32);    /* [33] */
+    uint64_t *s_tile = reinterpret_cast<uint64_t *>(smem + 168); /* the claimed tile */
+    uint32_t *s_pos = reinterpret_cast<uint32_t *>(smem + 176);  /* ring position of this sum */
     uint64_t *s_base = reinterpret_cast<uint64_t *>(smem + 192); /* [2] */
-    uint64_t *rec = reinterpret_cast<uint64_t *>(smem + 256);
+    ZRing *ring = reinterpret_cast<ZRing *>(smem + 256);
     uint32_t *acc_rows = reinterpret_cast<uint32_t *>(smem + a.sm.rows);
-    uint8_t *outs = smem + a.sm.out;
-    const uint32_t outs_sa = smem_u32(outs);
+    uint8_t *outs = smem + a.sm.out; /* the ring of packed sums */
 
     const ZGeom &g = a.g;
-    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t NC = g.TB; /* compute threads */
     const uint32_t L = g.L, stride = zg_row_stride(L), P = a.P;
     uint32_t bad = 0;
     /* see k_decompress: a failed index walk stops every CTA alike */
@@ -89,23 +91,40 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
+        ring->packed = 0;
+        ring->placed = 0;
     }
+    __syncthreads();
+
+    if (tid >= NC) { /* the placer warp */
+        placer_loop(g, ring, outs, a.out, a.cap, a.idx, a.w.status, a.w.err, bad);
+        if (bad) atomicOr(a.w.err, bad);
+        return;
+    }
+
+    /* the compute warps.  Tiles are claimed one at a time when these warps
+     * are ready for them, and they never wait while holding a claimed tile
+     * whose size is not yet published. */
     uint32_t acc[32];
     uint32_t ld = 0; /* index of the current copy in the two-buffer stream */
-    ZPending pd = {ZP_NONE, 0, 0, 0};
-
-    /* Tiles are claimed one at a time when the CTA is ready for them, and
-     * the CTA never waits while it holds a claimed tile whose size is not
-     * yet published, so later tiles never wait on a tile sitting idle. */
-    if (tid == 0) bc[0] = atomicAdd(a.w.ticket, 1u);
-    __syncthreads();
-    uint64_t tile = bc[0];
+    const uint32_t R = zg_ring_bytes(L, NC);
+    uint32_t pos_prev = 0, end_prev = 0; /* thread 0: the previous sum's place in the ring */
+    if (tid == 0) *s_tile = atomicAdd(a.w.ticket, 1u);
+    named_sync(1, NC);
+    uint64_t tile = *s_tile;
     BlockSlot cur = {0, 0, 0};
     if (tile < g.ntiles)
         cur = stage_input(a, tile, 0, smem + a.sm.in0, &bar[0], wsum, &s_base[0], bad);
 
-    for (;;) {
-        if (tile >= g.ntiles) break;
+    for (uint32_t it = 0;; it++) {
+        if (tile >= g.ntiles) {
+            /* tell the placer there is nothing more (once it has read the slot) */
+            if (tid == 0) {
+                ring_wait(&ring->placed, it >= 1 ? it - 1 : 0u, a.w.err);
+                ring_publish(ring, it, ZP_NONE, 0, 0);
+            }
+            break;
+        }
         ZTile z;
         zg_tile(&g, tile, &z);
         const bool own = tid < z.nblk;
@@ -158,16 +177,16 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
             }
             cur = nxt;
             /* the buffer just read is refilled by the copy staged next round,
-             * after that round's scan has synchronised every thread */
+             * after that round's scan has synchronised every compute thread */
         }
 
         /* branch-case counters of the two-input add (ZCCLd_float.c:2175-2764) */
         if (a.cases && P == 2) {
-            const uint32_t c0 = __syncthreads_count(own && nzmask == 0u);
-            const uint32_t c1 = __syncthreads_count(own && nzmask == 2u);
-            const uint32_t c2 = __syncthreads_count(own && nzmask == 1u);
-            const uint32_t c3 = __syncthreads_count(own && nzmask == 3u);
-            if (tid == 0) {
+            const uint32_t c0 = __popc(__ballot_sync(0xffffffffu, own && nzmask == 0u));
+            const uint32_t c1 = __popc(__ballot_sync(0xffffffffu, own && nzmask == 2u));
+            const uint32_t c2 = __popc(__ballot_sync(0xffffffffu, own && nzmask == 1u));
+            const uint32_t c3 = __popc(__ballot_sync(0xffffffffu, own && nzmask == 3u));
+            if (lane == 0) {
                 atomicAdd(a.cases + 0, (unsigned long long)c0);
                 atomicAdd(a.cases + 1, (unsigned long long)c1);
                 atomicAdd(a.cases + 2, (unsigned long long)c2);
@@ -196,45 +215,44 @@ __global__ void __launch_bounds__(128) k_homadd(const HomAddArgs a)
             size = zg_block_bytes(b, n);
         }
         uint32_t total;
-        const uint32_t off = cta_excl_scan(size, wsum, &total);
+        const uint32_t off = grp_excl_scan(size, wsum, &total, NC, 1);
         total += headb;
         if (warp == 0) lb_publish(a.w.status, tile, total, tile == 0, 0);
+        if (own) a.idx.widths[z.gblk0 + tid] = (uint8_t)b;
+        if (tid == 0 && a.qprev_valid) a.idx.tile_qprev[tile] = (int32_t)qsum;
 
-        /* place the sum packed one round ago (its size went out a whole tile
-         * earlier), then claim the next tile and start its first input's
-         * copy, and pack this sum while it arrives */
-        if (pd.tile != ZP_NONE)
-            place_tile(g, pd, outs, a.out, a.cap, a.idx, a.qprev_valid != 0, a.w.status, a.w.err, rec,
-                       bad);
-        if (tid == 0) bc[0] = atomicAdd(a.w.ticket, 1u);
-        __syncthreads();
-        const uint64_t next = bc[0];
+        /* take room for the packed sum in the ring (waiting, if need be, for
+         * the placer to write out an earlier one), claim the next tile and
+         * start its first input's copy, and pack this sum while it arrives */
+        if (tid == 0) {
+            *s_pos = ring_reserve(ring, it, zg_ring_need(total), R, pos_prev, end_prev, a.w.err);
+            *s_tile = atomicAdd(a.w.ticket, 1u);
+        }
+        named_sync(1, NC);
+        const uint64_t next = *s_tile;
+        const uint32_t pos = *s_pos;
         if (next < g.ntiles)
             cur = stage_input(a, next, 0, smem + (ld & 1u ? a.sm.in1 : a.sm.in0), &bar[ld & 1u], wsum,
                               &s_base[ld & 1u], bad);
-        smem_zero(outs, total + 8);
-        __syncthreads();
-        if (z.has_head && tid == 0) *reinterpret_cast<uint32_t *>(outs) = hsum;
+        uint8_t *pk = outs + pos;
+        const uint32_t pk_sa = smem_u32(pk);
+        smem_zero(pk, total + 8, tid, NC);
+        named_sync(1, NC);
+        if (z.has_head && tid == 0) *reinterpret_cast<uint32_t *>(pk) = hsum;
         const uint32_t o = headb + off;
         if (full) {
-            encode_full(outs_sa, o, b, smask, acc);
+            encode_full(pk_sa, o, b, smask, acc);
         } else if (own) {
-            encode_any(outs_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
+            encode_any(pk_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
                 const uint32_t v = FAST ? pick(acc, j) : acc_rows[tid * stride + j];
                 neg = v >> 31;
                 mg = (uint32_t)abs((int32_t)v);
             });
         }
-        pd.tile = tile;
-        pd.total = total;
-        pd.b = b;
-        pd.q = qsum;
+        named_sync(1, NC); /* the packed sum is complete; acc_rows are free */
+        if (tid == 0) ring_publish(ring, it, tile, total, pos);
         tile = next;
-        __syncthreads(); /* the packed sum is complete; acc_rows are free */
     }
-    /* the last packed sum */
-    if (pd.tile != ZP_NONE)
-        place_tile(g, pd, outs, a.out, a.cap, a.idx, a.qprev_valid != 0, a.w.status, a.w.err, rec, bad);
     if (bad) atomicOr(a.w.err, bad);
 }
 
@@ -246,10 +264,11 @@ cudaError_t launch_homadd(const HomAddArgs &a, cudaStream_t st)
     const void *fn = fast ? (const void *)k_homadd<true> : (const void *)k_homadd<false>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
     if (e != cudaSuccess) return e;
-    unsigned grid = persistent_grid(fn, a.g.TB, a.sm.total, a.g.ntiles);
+    const unsigned threads = a.g.TB + 32; /* compute warps and the placer warp */
+    unsigned grid = persistent_grid(fn, threads, a.sm.total, a.g.ntiles);
     if (fast)
-        k_homadd<true><<<grid, a.g.TB, a.sm.total, st>>>(a);
+        k_homadd<true><<<grid, threads, a.sm.total, st>>>(a);
     else
-        k_homadd<false><<<grid, a.g.TB, a.sm.total, st>>>(a);
+        k_homadd<false><<<grid, threads, a.sm.total, st>>>(a);
     return cudaGetLastError();
 }

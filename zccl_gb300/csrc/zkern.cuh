@@ -152,6 +152,110 @@ __device__ __forceinline__ void place_tile(const ZGeom &g, const ZPending &pd, c
     if (fits) store_realign(out + base, s_out, pd.total);
 }
 
+/* ------------------------------------------------------------------
+ * Hand-off of packed tiles from the compute warps to the placer warp.
+ *
+ * The packed tiles wait in a ring of R bytes of shared memory (R holds
+ * the largest tile; two typical tiles fit at once), so the compute warps
+ * can pack tile k + 1 while the placer still writes out tile k.  Two
+ * counters order the hand-off: `packed` (tiles packed, written by compute
+ * thread 0) and `placed` (tiles written out, written by placer lane 0).
+ * Tile k's size, ring position and index sit in slot k % 2.  All waits are
+ * bounded: on time-out ZERR_TIMEOUT is set and the caller goes on.
+ * ------------------------------------------------------------------ */
+struct ZRing {
+    uint32_t packed, placed;
+    uint32_t pos[2], total[2];
+    uint64_t tile[2];
+};
+
+__device__ __forceinline__ void ring_set(uint32_t *p, uint32_t v)
+{
+    asm volatile("st.release.cta.shared.u32 [%0], %1;" ::"r"(smem_u32(p)), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ uint32_t ring_get(const uint32_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.acquire.cta.shared.u32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+    return v;
+}
+
+/* One thread: wait until *p >= v. */
+__device__ __forceinline__ void ring_wait(const uint32_t *p, uint32_t v, uint32_t *err)
+{
+    for (uint32_t i = 0; i < (1u << 24); i++) {
+        if ((int32_t)(ring_get(p) - v) >= 0) return;
+        __nanosleep(64);
+    }
+    atomicOr(err, ZERR_TIMEOUT);
+}
+
+/* Compute thread 0, before packing tile k (0-based) of `need` bytes: its
+ * ring position, after waiting until the placer has released the space.
+ * end_prev / pos_prev describe tile k - 1 (updated here). */
+__device__ __forceinline__ uint32_t ring_reserve(ZRing *ring, uint32_t k, uint32_t need, uint32_t R,
+                                                 uint32_t &pos_prev, uint32_t &end_prev, uint32_t *err)
+{
+    const uint32_t pos = end_prev + need <= R ? end_prev : 0u;
+    /* tile k - 2 is always out of the way (its slot is reused); tile k - 1
+     * too when this tile wraps onto it */
+    uint32_t req = k >= 1 ? k - 1 : 0u;
+    if (k >= 1 && pos < end_prev && pos + need > pos_prev) req = k;
+    ring_wait(&ring->placed, req, err);
+    pos_prev = pos;
+    end_prev = pos + need;
+    return pos;
+}
+
+/* Compute thread 0, after every compute thread has finished packing tile k
+ * (pass ZP_NONE as `tile` once there are no more tiles). */
+__device__ __forceinline__ void ring_publish(ZRing *ring, uint32_t k, uint64_t tile, uint32_t total,
+                                             uint32_t pos)
+{
+    ring->tile[k & 1u] = tile;
+    ring->total[k & 1u] = total;
+    ring->pos[k & 1u] = pos;
+    ring_set(&ring->packed, k + 1);
+}
+
+/* The placer warp: for every packed tile, in order, the decoupled look-back
+ * gives its byte offset in the stream; its bytes go out with 16-byte vector
+ * stores realigned to that offset, with its offset in the side index, the
+ * stream size after the last tile and, for a segment's first tile, the
+ * chunk offset in the header. */
+__device__ __forceinline__ void placer_loop(const ZGeom &g, ZRing *ring, const uint8_t *ringb, uint8_t *out,
+                                            uint64_t cap, const ZIndex &idx, uint64_t *status,
+                                            uint32_t *err, uint32_t &bad)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint64_t k = 0; k <= g.ntiles; k++) {
+        if (lane == 0) ring_wait(&ring->packed, (uint32_t)k + 1, err);
+        __syncwarp();
+        const uint32_t slot = (uint32_t)k & 1u;
+        const uint64_t t = ring->tile[slot];
+        const uint32_t total = ring->total[slot], pos = ring->pos[slot];
+        if (t >= g.ntiles) break;
+        const uint64_t base = 8ull * g.T + lb_resolve(status, t, total, t == 0, 0, err);
+        const bool fits = base + total <= cap;
+        if (!fits) bad |= ZERR_CAPACITY;
+        if (lane == 0) {
+            ZTile z;
+            zg_tile(&g, t, &z);
+            idx.tile_off[t] = base;
+            if (fits && z.has_head && z.seg < g.T) {
+                const uint64_t h = base - 8ull * g.T;
+#pragma unroll
+                for (int k8 = 0; k8 < 8; k8++) out[8ull * z.seg + k8] = (uint8_t)(h >> (8 * k8));
+            }
+            if (t == g.ntiles - 1) *idx.size = base + total;
+        }
+        if (fits) store_realign(out + base, ringb + pos, total, lane, 32);
+        __syncwarp();
+        if (lane == 0) ring_set(&ring->placed, (uint32_t)k + 1);
+    }
+}
+
 static inline unsigned persistent_grid(const void *fn, int threads, size_t smem, uint64_t ntiles)
 {
     int dev = 0, nsm = 0, occ = 0;
