@@ -11,16 +11,17 @@
  *   W0  chunk starts from the T-entry header; per segment its block region
  *       and window count; heads' tile offsets.
  *   W1  for every window and every possible entry offset e in [0, M) (M = the
- *       largest block) follow the headers to the window end: the exit offset
- *       into the next window and the blocks passed.  Walks that land on a
- *       position another walk already claimed stop there and inherit its
- *       result, so a window costs about one walk plus M short ones, also
- *       when every block has the same size.
+ *       largest block): the exit offset into the next window and the blocks
+ *       passed.  The path from entry 0 is stitched from 32 speculative
+ *       sub-window walks run in parallel (see below), and every other entry
+ *       is walked only until it meets that path, so a window costs a few
+ *       dozen dependent steps instead of a full walk.
  *   W2  compose the tables: per group of G windows (parallel), then per
  *       segment across groups, giving each group its true entry offset and
  *       first block number.
- *   W3  per window, from its true entry, record every block's width and the
- *       offset of every tile, and check each chunk ends where the next starts.
+ *   W3  per window, the path from its true entry, stitched the same way,
+ *       gives every block's width and every tile's offset, written by all
+ *       lanes at once; each chunk must end where the next starts.
  *   W4  the extra segment of the last chunk (N % T elements) and the total
  *       size.
  * Widths above 32, chunk ends that disagree with the header, and blocks past
@@ -30,8 +31,7 @@
 
 namespace {
 
-constexpr uint32_t WARPS_W1 = 2;
-constexpr uint32_t NONE = 0xFFFFFFFFu;
+constexpr uint32_t WARPS_W1 = 8;
 
 __device__ __forceinline__ uint64_t load_u64(const uint8_t *p)
 {
@@ -128,6 +128,115 @@ __global__ void k_walk_setup(const WalkArgs a)
     }
 }
 
+/* ---- shared by W1 and W3: the path of the headers through one window ---
+ *
+ * A window of WW = 32 x 128 bytes sits in shared memory.  Lane j walks the
+ * headers speculatively from byte 128 j until it leaves its sub-window and
+ * records the positions it visited (a 128-bit map).  A walk from a true
+ * block start is the true path, and two walks that meet at a position go
+ * on together, so the true path from a known entry is stitched across the
+ * sub-windows: where it enters sub-window j at a position lane j visited,
+ * it is lane j's walk from there on; otherwise it is walked until it meets
+ * lane j's walk or leaves the sub-window (a few blocks).  Bytes that cannot
+ * be headers (above 32) count as 1-byte blocks, so walks stay bounded. */
+constexpr uint32_t SUB = WALK_WW / 32; /* bytes per sub-window */
+static_assert(SUB == 128, "a sub-window map is four 32-bit words");
+
+struct WinPath {
+    uint32_t spec[32][4]; /* lane j's visited positions in sub-window j */
+    uint32_t sx[32];      /* where lane j's walk left its sub-window */
+    uint32_t tm[32][4];   /* the true path's positions, per sub-window */
+    uint32_t pref[33];    /* true-path positions before sub-window j; [32] = all */
+    uint32_t exit;        /* where the true path leaves the window */
+};
+
+__device__ __forceinline__ bool map_bit(const uint32_t *m, uint32_t i)
+{
+    return (m[i >> 5] >> (i & 31u)) & 1u;
+}
+
+/* All lanes: the speculative sub-window walks. */
+__device__ __forceinline__ void spec_walks(const uint8_t *bytes, uint32_t L, WinPath *wp)
+{
+    const uint32_t lane = threadIdx.x & 31u, lo = lane * SUB;
+    uint32_t m0 = 0, m1 = 0, m2 = 0, m3 = 0, pos = lo;
+    while (pos < lo + SUB) {
+        const uint32_t i = pos - lo, bit = 1u << (i & 31u), w = i >> 5;
+        m0 |= w == 0 ? bit : 0u;
+        m1 |= w == 1 ? bit : 0u;
+        m2 |= w == 2 ? bit : 0u;
+        m3 |= w == 3 ? bit : 0u;
+        pos += full_size(bytes[pos], L);
+    }
+    wp->spec[lane][0] = m0;
+    wp->spec[lane][1] = m1;
+    wp->spec[lane][2] = m2;
+    wp->spec[lane][3] = m3;
+    wp->sx[lane] = pos;
+}
+
+/* One lane: the true path from window position `entry`, per sub-window,
+ * with the prefix counts; returns where it leaves the window. */
+__device__ __forceinline__ uint32_t stitch(const uint8_t *bytes, uint32_t L, uint32_t entry, WinPath *wp)
+{
+    uint32_t p = entry, cnt = 0;
+    for (uint32_t j = 0; j < 32; j++) {
+        const uint32_t lo = j * SUB, hi = lo + SUB;
+        uint32_t t[4] = {0, 0, 0, 0};
+        wp->pref[j] = cnt;
+        if (p < hi) {
+            uint32_t q = p;
+            for (;;) {
+                const uint32_t i = q - lo;
+                if (map_bit(wp->spec[j], i)) { /* joins lane j's walk: the rest of it */
+#pragma unroll
+                    for (uint32_t w = 0; w < 4; w++) {
+                        const uint32_t sw = wp->spec[j][w];
+                        t[w] |= w < (i >> 5) ? 0u : w > (i >> 5) ? sw : sw & ~((1u << (i & 31u)) - 1u);
+                    }
+                    q = wp->sx[j];
+                    break;
+                }
+#pragma unroll
+                for (uint32_t w = 0; w < 4; w++) t[w] |= w == (i >> 5) ? 1u << (i & 31u) : 0u;
+                q += full_size(bytes[q], L);
+                if (q >= hi) break;
+            }
+            p = q;
+        }
+#pragma unroll
+        for (uint32_t w = 0; w < 4; w++) {
+            wp->tm[j][w] = t[w];
+            cnt += __popc(t[w]);
+        }
+    }
+    wp->pref[32] = cnt;
+    wp->exit = p;
+    return p;
+}
+
+/* True-path positions before window position q (q < WW). */
+__device__ __forceinline__ uint32_t path_rank(const WinPath *wp, uint32_t q)
+{
+    const uint32_t j = q / SUB, i = q % SUB;
+    uint32_t r = wp->pref[j];
+#pragma unroll
+    for (uint32_t w = 0; w < 4; w++) {
+        const uint32_t m = wp->tm[j][w];
+        r += w < (i >> 5) ? __popc(m) : w == (i >> 5) ? __popc(m & ((1u << (i & 31u)) - 1u)) : 0u;
+    }
+    return r;
+}
+
+__device__ __forceinline__ void load_window(const WalkArgs &a, uint64_t start, uint8_t *bytes)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t i = lane; i < WALK_WW + a.M; i += 32) {
+        const uint64_t p = start + i;
+        bytes[i] = p < a.avail ? a.in[p] : 0;
+    }
+}
+
 /* ---- W1 -------------------------------------------------------------- */
 __global__ void __launch_bounds__(32 * WARPS_W1) k_walk_tables(const WalkArgs a)
 {
@@ -141,84 +250,29 @@ __global__ void __launch_bounds__(32 * WARPS_W1) k_walk_tables(const WalkArgs a)
     const uint32_t s = find_seg(w.win_base, g.T, wg);
     const uint64_t start = w.seg_P[s] + (uint64_t)(wg - w.win_base[s]) * WALK_WW;
 
-    /* per-warp shared area: bytes[WW + M + 16] | own[WW] | ex, cnt, par, at, ordp [M] */
-    uint8_t *base = smem + warp * a.w1_warp_bytes;
-    uint8_t *bytes = base;
-    uint32_t *own = reinterpret_cast<uint32_t *>(base + ((WALK_WW + M + 16 + 15) & ~15u));
-    uint32_t *ex = own + WALK_WW;
-    uint32_t *cnt = ex + M;
-    int32_t *par = reinterpret_cast<int32_t *>(cnt + M);
-    uint32_t *at = reinterpret_cast<uint32_t *>(par + M);
-    uint32_t *ordp = at + M;
-
-    for (uint32_t i = lane; i < WALK_WW + M; i += 32) {
-        uint64_t p = start + i;
-        bytes[i] = p < a.avail ? a.in[p] : 0;
-    }
-    for (uint32_t i = lane; i < WALK_WW; i += 32) own[i] = NONE;
+    /* per-warp shared area: bytes[WW + M + 16] | WinPath */
+    uint8_t *bytes = smem + warp * a.w1_warp_bytes;
+    WinPath *wp = reinterpret_cast<WinPath *>(bytes + ((WALK_WW + M + 16 + 15) & ~15u));
+    load_window(a, start, bytes);
     __syncwarp();
-
-    for (uint32_t e0 = 0; e0 < M; e0 += 32) {
-        const uint32_t e = e0 + lane;
-        bool active = e < M;
-        uint32_t pos = e, k = 0;
-        for (uint32_t it = 0; it < WALK_WW + M + 2; it++) {
-            if (!__any_sync(0xffffffffu, active)) break;
-            if (active) {
-                if (pos >= WALK_WW) {
-                    ex[e] = pos - WALK_WW;
-                    cnt[e] = k;
-                    par[e] = -1;
-                    active = false;
-                } else {
-                    uint32_t o = own[pos];
-                    if (o != NONE) {
-                        par[e] = (int32_t)(o >> 16);
-                        at[e] = k;
-                        ordp[e] = o & 0xFFFFu;
-                        active = false;
-                    } else {
-                        own[pos] = (e << 16) | k;
-                    }
-                }
-            }
-            __syncwarp();
-            if (active) {
-                uint32_t o = own[pos];
-                if ((o >> 16) != e) { /* another walk claimed the same byte this step */
-                    par[e] = (int32_t)(o >> 16);
-                    at[e] = k;
-                    ordp[e] = o & 0xFFFFu;
-                    active = false;
-                } else {
-                    pos += full_size(bytes[pos], g.L);
-                    k++;
-                }
-            }
-            __syncwarp();
-        }
-    }
-    /* a walk that merged into walk o at o's step ordp: exit(o), at + cnt(o) - ordp.
-     * Parents claimed their byte first, so resolving repeatedly terminates. */
-    for (uint32_t round = 0; round < M + 1; round++) {
-        bool pending = false;
-        for (uint32_t e = lane; e < M; e += 32) {
-            int32_t p = par[e];
-            if (p >= 0) {
-                if (par[p] < 0) {
-                    ex[e] = ex[p];
-                    cnt[e] = at[e] + cnt[p] - ordp[e];
-                    par[e] = -1;
-                } else {
-                    pending = true;
-                }
-            }
-        }
-        __syncwarp();
-        if (!__any_sync(0xffffffffu, pending)) break;
-    }
+    spec_walks(bytes, g.L, wp);
+    __syncwarp();
+    if (lane == 0) stitch(bytes, g.L, 0, wp);
+    __syncwarp();
+    /* entry e: walk until the path from entry 0 is met (then its exit and
+     * the blocks left on it) or the window ends */
+    const uint32_t x0 = wp->exit - WALK_WW, c0 = wp->pref[32];
     uint32_t *tab = a.ws.wtab + (uint64_t)wg * M;
-    for (uint32_t e = lane; e < M; e += 32) tab[e] = (ex[e] << 16) | cnt[e];
+    for (uint32_t e = lane; e < M; e += 32) {
+        uint32_t q = e, k = 0;
+        while (q < WALK_WW && !map_bit(wp->tm[q / SUB], q % SUB)) {
+            q += full_size(bytes[q], g.L);
+            k++;
+        }
+        const uint32_t ex = q < WALK_WW ? x0 : q - WALK_WW;
+        const uint32_t cnt = q < WALK_WW ? k + c0 - path_rank(wp, q) : k;
+        tab[e] = (ex << 16) | cnt;
+    }
 }
 
 /* ---- W2a: compose the window tables of each group ---------------------- */
@@ -300,7 +354,7 @@ __global__ void __launch_bounds__(128) k_walk_final(const WalkArgs a)
     uint32_t *entry = reinterpret_cast<uint32_t *>(smem);
     uint64_t *bbase = reinterpret_cast<uint64_t *>(smem + 4 * WALK_G);
     uint8_t *wbuf = smem + 12 * WALK_G;
-    const uint32_t wstride = (WALK_WW + a.M + 16 + 15) & ~15u;
+    const uint32_t wstride = a.w1_warp_bytes;
 
     const uint64_t nb = g.nb_reg;
     const uint64_t nfull = (g.tbs - 1) / g.L;
@@ -325,32 +379,39 @@ __global__ void __launch_bounds__(128) k_walk_final(const WalkArgs a)
         if (b0 >= nb) continue;
         const uint64_t start = w.seg_P[s] + (uint64_t)k * WALK_WW;
         uint8_t *buf = wbuf + warp * wstride;
-        for (uint32_t i = lane; i < WALK_WW + a.M; i += 32) {
-            uint64_t p = start + i;
-            buf[i] = p < a.avail ? a.in[p] : 0;
-        }
+        WinPath *wp = reinterpret_cast<WinPath *>(buf + ((WALK_WW + a.M + 16 + 15) & ~15u));
+        load_window(a, start, buf);
         __syncwarp();
-        if (lane == 0) {
-            uint32_t pos = entry[k - w0];
-            uint64_t blk = b0;
-            while (pos < WALK_WW && blk < nb) {
+        spec_walks(buf, g.L, wp);
+        __syncwarp();
+        if (lane == 0) stitch(buf, g.L, entry[k - w0], wp);
+        __syncwarp();
+        /* lane j records the true-path blocks of its sub-window */
+        uint64_t blk = b0 + wp->pref[lane];
+#pragma unroll
+        for (uint32_t wd = 0; wd < 4; wd++) {
+            uint32_t m = wp->tm[lane][wd];
+            while (m && blk < nb) {
+                const uint32_t pos = lane * SUB + wd * 32 + (uint32_t)(__ffs(m) - 1);
+                m &= m - 1;
                 const uint64_t gpos = start + pos;
                 if (gpos >= a.avail) {
                     atomicOr(a.err, ZERR_BOUNDS);
+                    m = 0;
                     break;
                 }
                 const uint32_t b = buf[pos];
                 if (b > 32) {
                     atomicOr(a.err, ZERR_CORRUPT);
+                    m = 0;
                     break;
                 }
                 if (blk % g.TB == 0 && blk) a.idx.tile_off[tile0 + blk / g.TB] = gpos;
                 a.idx.widths[gblk0 + blk] = (uint8_t)b;
                 const uint32_t n = blk < nfull ? g.L : ntail;
-                pos += zg_block_bytes(b, n);
                 blk++;
                 if (blk == nb) {
-                    const uint64_t end = start + pos;
+                    const uint64_t end = gpos + zg_block_bytes(b, n);
                     if (end > a.avail) atomicOr(a.err, ZERR_BOUNDS);
                     w.seg_end[s] = end;
                     if (s + 1 < g.T && end != w.seg_R[s]) atomicOr(a.err, ZERR_CORRUPT);
@@ -409,7 +470,7 @@ __global__ void k_walk_finish(const WalkArgs a)
 
 size_t walk_w1_warp_bytes(uint32_t M)
 {
-    return ((WALK_WW + M + 16 + 15) & ~15u) + 4u * WALK_WW + 20u * M + 16;
+    return ((WALK_WW + M + 16 + 15) & ~15u) + sizeof(WinPath);
 }
 
 cudaError_t launch_walk(const WalkArgs &a0, cudaStream_t st)
@@ -437,7 +498,7 @@ cudaError_t launch_walk(const WalkArgs &a0, cudaStream_t st)
         return e;
     k_walk_segments<<<a.g.T, 256, smem2, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    const uint32_t wstride = (WALK_WW + a.M + 16 + 15) & ~15u;
+    const uint32_t wstride = (uint32_t)walk_w1_warp_bytes(a.M);
     const uint32_t smem3 = 12 * WALK_G + 4 * wstride;
     if ((e = cudaFuncSetAttribute(k_walk_final, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   smem3)) != cudaSuccess)
