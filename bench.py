@@ -53,6 +53,10 @@ def parse():
     p.add_argument("--T", type=int, default=0, help="writer thread count (default: host cores)")
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the P-way reduction, batched and serving measurements")
+    p.add_argument("--red-n", type=int, default=1 << 24, help="floats per rank chunk (reduction)")
+    p.add_argument("--red-p", type=int, default=8, help="ranks (reduction)")
     return p.parse_args()
 
 
@@ -224,6 +228,103 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def make_rank_chunks(n: int, P: int, seed: int, device):
+    """P ranks' chunks: a shared smooth base (a sum of 8 random-phase
+    sinusoids) plus each rank's N(0, 0.05) perturbation from seed r."""
+    import math
+    import torch
+    g = torch.Generator(device=device).manual_seed(seed)
+    i = torch.arange(n, device=device, dtype=torch.float64)
+    period = 500.0 + 49500.0 * torch.rand(8, generator=g, device=device, dtype=torch.float64)
+    phase = 2 * math.pi * torch.rand(8, generator=g, device=device, dtype=torch.float64)
+    base = torch.zeros(n, device=device, dtype=torch.float64)
+    for k in range(8):
+        base += torch.sin(2 * math.pi * i / period[k] + phase[k])
+    del i
+    xs = []
+    for r in range(P):
+        gr = torch.Generator(device=device).manual_seed(r)
+        xs.append((base + 0.05 * torch.randn(n, generator=gr, device=device, dtype=torch.float64)).float())
+    return xs
+
+
+def timed(fn, reps, stream):
+    """Mean device ms of fn over reps runs (after one warm-up), CUDA events
+    on the launching stream."""
+    import torch
+    fn()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def reduction_bench(args, L, T, dev):
+    """P ranks' chunks of red_n floats (P = 8 x 16M by default), eb =
+    1e-4 * range: the P-way homomorphic add against the pairwise fold and
+    decompress-add-recompress, their errors against the exact sum, and the
+    ring allreduce run for the P ranks on this device, both variants."""
+    import numpy as np
+    import torch
+    import zccl_gb300 as Z
+    from zccl_gb300.ring import RingAllreduce, reduce_doc, reduce_homomorphic, reduce_pairwise
+    n, P = args.red_n, args.red_p
+    xs = make_rank_chunks(n, P, 3, dev)
+    lo = min(float(x.min()) for x in xs)
+    hi = max(float(x.max()) for x in xs)
+    eb = float(np.float32(1e-4 * (hi - lo)))
+    codec = Z.Codec(n, L, T, device=str(dev))
+    st = codec.torch_stream
+    streams = [codec.new_stream() for _ in range(P)]
+    out = codec.new_stream()
+    ms_compress = timed(lambda: [codec.compress(x, eb, out=s) for x, s in zip(xs, streams)], 3, st)
+    ms_pway = timed(lambda: reduce_homomorphic(codec, streams, out=out), 5, st)
+    ms_pair = timed(lambda: reduce_pairwise(codec, streams), 3, st)
+    docs = codec.new_stream()
+    ms_doc = timed(lambda: reduce_doc(codec, streams, eb, out=docs), 3, st)
+    codec.check()
+    same = reduce_homomorphic(codec, streams, out=out).tobytes() == reduce_pairwise(codec, streams).tobytes()
+    exact = torch.zeros(n, dtype=torch.float64, device=dev)
+    for x in xs:
+        exact += x.double()
+    y_ho = codec.decompress(out, eb)
+    doc_stream, _ = reduce_doc(codec, streams, eb, out=docs)
+    y_doc = codec.decompress(doc_stream, eb)
+    err_ho = float((y_ho.double() - exact).abs().max()) / eb
+    err_doc = float((y_doc.double() - exact).abs().max()) / eb
+    cin = sum(s.size() for s in streams)
+    cout = out.size()
+    ring = RingAllreduce(n, P, L, T, device=str(dev))
+    ms_ring_ho = timed(lambda: ring.homomorphic(xs, eb), 2, st)
+    ms_ring_doc = timed(lambda: ring.doc(xs, eb), 2, st)
+    y_rho = ring.homomorphic(xs, eb)
+    y_rdoc = ring.doc(xs, eb)
+    res = {
+        "workload": f"P={P} ranks x {n} float32 (smooth base of 8 random-phase sinusoids + rank N(0,0.05)), "
+                    f"eb=1e-4*range, L={L}, T={T}",
+        "pway_homadd_ms": round(ms_pway, 4),
+        "pway_homadd_GBps_alg": round((cin + cout) / (ms_pway * 1e-3) / 1e9, 1),
+        "pway_homadd_GBps_uncompressed": round(4 * n * P / (ms_pway * 1e-3) / 1e9, 1),
+        "pairwise_fold_ms": round(ms_pair, 4),
+        "doc_ms": round(ms_doc, 4),
+        "compress_all_ms": round(ms_compress, 4),
+        "pway_equals_pairwise_bytes": same,
+        "max_err_over_eb": {"homomorphic": round(err_ho, 3), "doc": round(err_doc, 3), "bound": P},
+        "ring_allreduce_emulated_ms": {"homomorphic": round(ms_ring_ho, 3), "doc": round(ms_ring_doc, 3),
+                                       "note": f"all {P} ranks' codec work on one GPU"},
+        "ring_max_err_over_eb": {
+            "homomorphic": round(float((y_rho.double() - exact).abs().max()) / eb, 3),
+            "doc": round(float((y_rdoc.double() - exact).abs().max()) / eb, 3)},
+    }
+    del xs, exact
+    torch.cuda.empty_cache()
+    return res
+
+
 def workload_config(args, n, T):
     return {"workload": f"{args.side}^3 float32 log-normal GRF ({4 * n >> 20} MiB): compress + "
                         f"decompress + 2-way homomorphic add, eb={args.eb_rel:g}*range",
@@ -343,6 +444,11 @@ def run_ours(args, rank, world, local_rank):
                "sample": f"whole field, one pass ({secs:.2f} s) of compress+decompress+homadd, "
                          f"oracle C restatement, OpenMP {T} threads"}
 
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        del hs_a, hs_b, hs_s, hy
+        extras["reduction"] = reduction_bench(args, L, T, dev)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world,
@@ -356,6 +462,7 @@ def run_ours(args, rank, world, local_rank):
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * args.steps,
             "clocks": clk.summary(),
         }
+        line.update(extras)
         print(json.dumps(line), flush=True)
 
 

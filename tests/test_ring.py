@@ -1,0 +1,124 @@
+"""The compressed ring allreduce run for P ranks on one device
+(zccl_gb300/ring.py) against the same ring run by the oracle on the CPU:
+reduced compressed chunks bit for bit, the allreduced floats bit for bit,
+every rank's copy alike, and the error bounds of the homomorphic sum
+(P * eb) next to decompress-add-recompress.  The chunking rule runs on
+the CPU."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from zccl_gb300.ring import ring_counts
+
+
+def test_ring_counts_follow_the_reference():
+    # ceil(count / P) per chunk, the last one shorter (ZCCL_ring_ho.c:219-233)
+    assert ring_counts(80011, 8) == ([10002] * 7 + [9997], [10002 * i for i in range(8)])
+    assert ring_counts(64, 8) == ([8] * 8, [8 * i for i in range(8)])
+    cnts, displs = ring_counts(10, 4)
+    assert cnts == [3, 3, 3, 1] and displs == [0, 3, 6, 9]
+    cnts, _ = ring_counts(5, 4)  # 2 + 2 + 1 + nothing
+    assert cnts == [2, 2, 1, 0]
+
+
+def rank_data(count, P, seed=0):
+    """P ranks' arrays: a shared smooth base (8 random-phase sinusoids) plus
+    a rank's own N(0, 0.05) from seed r."""
+    rng = np.random.default_rng(seed)
+    i = np.arange(count, dtype=np.float64)
+    base = sum(np.sin(2 * np.pi * i / rng.uniform(500, 50000) + rng.uniform(0, 2 * np.pi))
+               for _ in range(8))
+    return [(base + np.random.default_rng(r).normal(0, 0.05, count)).astype(np.float32) for r in range(P)]
+
+
+def oracle_ring_ho(port, xs, eb, L, T, P):
+    cnts, displs = ring_counts(xs[0].size, P)
+    chunk = lambda x, c: np.ascontiguousarray(x[displs[c]: displs[c] + cnts[c]])
+    S = [[port.compress(chunk(xs[r], c), eb, L, T) for c in range(P)] for r in range(P)]
+    for i in range(P - 1):
+        for r in range(P):
+            src, c = (r - 1) % P, (r - 2 - i) % P
+            S[r][c] = port.homadd(S[src][c], S[r][c], cnts[c], eb, L, T)
+    reduced = [S[c][c] for c in range(P)]
+    y = np.concatenate([port.decompress(reduced[c], cnts[c], eb, L, T) for c in range(P)])
+    return reduced, y
+
+
+def oracle_ring_doc(port, xs, eb, L, T, P):
+    cnts, displs = ring_counts(xs[0].size, P)
+    acc = [x.copy() for x in xs]
+    sl = lambda c: slice(displs[c], displs[c] + cnts[c])
+    for i in range(P - 1):
+        msgs = [port.compress(np.ascontiguousarray(acc[r][sl((r - 1 - i) % P)]), eb, L, T) for r in range(P)]
+        for r in range(P):
+            src, c = (r - 1) % P, (r - 2 - i) % P
+            acc[r][sl(c)] += port.decompress(msgs[src], cnts[c], eb, L, T)
+    reduced = [port.compress(np.ascontiguousarray(acc[c][sl(c)]), eb, L, T) for c in range(P)]
+    y = np.concatenate([port.decompress(reduced[c], cnts[c], eb, L, T) for c in range(P)])
+    return reduced, y
+
+
+@pytest.fixture(scope="module")
+def torch():
+    t = pytest.importorskip("torch")
+    if not t.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return t
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("count,P,T", [(80011, 8, 3), (24000, 4, 1)])
+def test_homomorphic_ring_matches_oracle(torch, port, count, P, T):
+    from zccl_gb300.ring import RingAllreduce
+    L = 32
+    xs = rank_data(count, P)
+    eb = float(np.float32(1e-4 * (max(x.max() for x in xs) - min(x.min() for x in xs))))
+    ring = RingAllreduce(count, P, L, T)
+    ys = ring.homomorphic([torch.from_numpy(x).cuda() for x in xs], eb, per_rank_outputs=True)
+    reduced, y_ref = oracle_ring_ho(port, xs, eb, L, T, P)
+    for c in range(P):
+        assert ring.reduced[c].tobytes() == reduced[c], c
+    for y in ys:  # every rank ends with the same floats
+        assert np.array_equal(y.cpu().numpy().view(np.uint32), y_ref.view(np.uint32))
+    exact = np.sum([x.astype(np.float64) for x in xs], axis=0)
+    err = np.abs(y_ref.astype(np.float64) - exact).max()
+    assert err <= P * eb + 8 * np.spacing(np.float32(np.abs(exact).max())), (err, eb)
+
+
+@pytest.mark.gpu
+def test_doc_ring_matches_oracle(torch, port):
+    from zccl_gb300.ring import RingAllreduce
+    count, P, T, L = 80011, 8, 3, 32
+    xs = rank_data(count, P, seed=1)
+    eb = float(np.float32(1e-4 * (max(x.max() for x in xs) - min(x.min() for x in xs))))
+    ring = RingAllreduce(count, P, L, T)
+    ys = ring.doc([torch.from_numpy(x).cuda() for x in xs], eb, per_rank_outputs=True)
+    reduced, y_ref = oracle_ring_doc(port, xs, eb, L, T, P)
+    for c in range(P):
+        assert ring.reduced[c].tobytes() == reduced[c], c
+    for y in ys:
+        assert np.array_equal(y.cpu().numpy().view(np.uint32), y_ref.view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_one_shot_reductions_match_oracle(torch, port):
+    import zccl_gb300 as Z
+    from zccl_gb300.ring import reduce_doc, reduce_homomorphic, reduce_pairwise
+    n, P, T, L = 100003, 8, 4, 32
+    xs = rank_data(n, P, seed=2)
+    eb = float(np.float32(1e-4 * (max(x.max() for x in xs) - min(x.min() for x in xs))))
+    codec = Z.Codec(n, L, T)
+    streams = [codec.compress(torch.from_numpy(x).cuda(), eb) for x in xs]
+    host = [port.compress(x, eb, L, T) for x in xs]
+    for s, h in zip(streams, host):
+        assert s.tobytes() == h
+    fold = port.homadd_fold(host, n, eb, L, T)
+    assert reduce_homomorphic(codec, streams).tobytes() == fold
+    assert reduce_pairwise(codec, streams).tobytes() == fold
+    doc, _ = reduce_doc(codec, streams, eb)
+    total = np.zeros(n, np.float32)
+    for h in host:
+        total += port.decompress(h, n, eb, L, T)
+    assert doc.tobytes() == port.compress(total, eb, L, T)
+    codec.check()
