@@ -173,6 +173,64 @@ int zccl_gpu_stream_size(const zccl_gpu_stream *s, size_t n, int L, int T, size_
  * status code (ZCCL_GPU_OK when none). */
 int zccl_gpu_check(void *d_ws, void *cuda_stream);
 
+/* -------------------------------------------------------------------
+ * Batches: thousands of streams in one persistent launch.  No counterpart
+ * in the reference, whose callers compress one buffer per call.
+ *
+ * A batch is planned once (tables built on the host and copied into the
+ * caller's device memory, synchronously) and then run any number of times
+ * with one memset and one kernel launch on the given stream -- no host
+ * copies, so a run can be recorded into a CUDA graph.  All jobs of a batch
+ * share L; n, T and (for compression) eb are per job.  Every stream keeps
+ * the reference's byte layout and gets its side index as with the calls
+ * above.  Sums take P indexed input streams of one geometry (for example
+ * the outputs of a compression batch that ran before).
+ * ------------------------------------------------------------------- */
+#define ZCCL_GPU_BATCH_COMPRESS 0
+#define ZCCL_GPU_BATCH_HOMADD 1
+
+typedef struct zccl_gpu_batch_job {
+    const float *d_in;    /* compression: n device floats */
+    zccl_gpu_stream *ins; /* sum: P indexed input streams */
+    int P;                /* sum: number of inputs (1..32) */
+    size_t n;             /* floats of the buffer */
+    float eb;             /* compression: absolute error bound */
+    int T;                /* writer thread count of the stream layout */
+    zccl_gpu_stream *out; /* output stream (capacity >= zccl_gpu_max_stream_bytes) */
+} zccl_gpu_batch_job;
+
+typedef struct zccl_gpu_batch {
+    int kind;         /* ZCCL_GPU_BATCH_COMPRESS or ZCCL_GPU_BATCH_HOMADD */
+    int L;            /* block size of every job */
+    unsigned grid;    /* CTAs per launch, 0 = as many as fit; set by zccl_gpu_batch_tune() */
+    size_t njobs;     /* jobs in the batch */
+    size_t ntiles;    /* tiles of all jobs */
+    void *d_mem;      /* the caller's device memory, zccl_gpu_batch_bytes() bytes */
+    size_t clear_bytes; /* leading bytes of d_mem zeroed before every run */
+    size_t jobs_off, map_off, tile0_off; /* tables inside d_mem */
+    unsigned tb;      /* blocks per tile */
+    unsigned smem[6]; /* shared-memory layout of the launch */
+    int qprev_valid;  /* sums: every input carries its tile starting values */
+} zccl_gpu_batch;
+
+/* Device bytes a batch of these jobs needs (0 if a job is invalid). */
+size_t zccl_gpu_batch_bytes(int kind, const zccl_gpu_batch_job *jobs, size_t njobs, int L);
+
+/* Plan a batch into d_mem (bytes from zccl_gpu_batch_bytes); synchronous.
+ * The output streams are marked indexed. */
+int zccl_gpu_batch_plan(zccl_gpu_batch *b, int kind, const zccl_gpu_batch_job *jobs, size_t njobs,
+                        int L, void *d_mem, size_t bytes, void *cuda_stream);
+
+/* Run a planned batch on cuda_stream (asynchronous). */
+int zccl_gpu_batch_run(const zccl_gpu_batch *b, void *cuda_stream);
+
+/* The autotuner: time a few launch shapes of this batch on cuda_stream
+ * (running it several times) and keep the fastest in b->grid. */
+int zccl_gpu_batch_tune(zccl_gpu_batch *b, void *cuda_stream);
+
+/* Synchronize cuda_stream and return the batch's device status. */
+int zccl_gpu_batch_check(const zccl_gpu_batch *b, void *cuda_stream);
+
 /* Status of the last drop-in call made by this thread. */
 int zccl_gpu_last_status(void);
 

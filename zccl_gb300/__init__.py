@@ -38,6 +38,8 @@ EXPORTS = [
     "zccl_gpu_compress", "zccl_gpu_decompress", "zccl_gpu_homadd", "zccl_gpu_homadd_cases",
     "zccl_gpu_build_index", "zccl_gpu_stream_size", "zccl_gpu_check", "zccl_gpu_last_status",
     "zccl_gpu_strerror", "zccl_gpu_width_table", "zccl_gpu_compress_noalloc",
+    "zccl_gpu_batch_bytes", "zccl_gpu_batch_plan", "zccl_gpu_batch_run", "zccl_gpu_batch_tune",
+    "zccl_gpu_batch_check",
 ]
 
 
@@ -52,6 +54,22 @@ class StreamDesc(ctypes.Structure):
     _fields_ = [("bytes", ctypes.c_void_p), ("capacity", ctypes.c_size_t),
                 ("index", ctypes.c_void_p), ("indexed", ctypes.c_int),
                 ("qprev_valid", ctypes.c_int)]
+
+
+class BatchJobDesc(ctypes.Structure):
+    """``zccl_gpu_batch_job`` of include/zccl_gpu.h."""
+    _fields_ = [("d_in", ctypes.c_void_p), ("ins", ctypes.POINTER(StreamDesc)), ("P", ctypes.c_int),
+                ("n", ctypes.c_size_t), ("eb", ctypes.c_float), ("T", ctypes.c_int),
+                ("out", ctypes.POINTER(StreamDesc))]
+
+
+class BatchDesc(ctypes.Structure):
+    """``zccl_gpu_batch`` of include/zccl_gpu.h."""
+    _fields_ = [("kind", ctypes.c_int), ("L", ctypes.c_int), ("grid", ctypes.c_uint),
+                ("njobs", ctypes.c_size_t), ("ntiles", ctypes.c_size_t), ("d_mem", ctypes.c_void_p),
+                ("clear_bytes", ctypes.c_size_t), ("jobs_off", ctypes.c_size_t),
+                ("map_off", ctypes.c_size_t), ("tile0_off", ctypes.c_size_t), ("tb", ctypes.c_uint),
+                ("smem", ctypes.c_uint * 6), ("qprev_valid", ctypes.c_int)]
 
 
 _lib = None
@@ -88,6 +106,12 @@ def lib() -> ctypes.CDLL:
         "zccl_gpu_strerror": (ctypes.c_char_p, [i]),
         "zccl_gpu_width_table": (None, [ctypes.POINTER(ctypes.c_uint32)]),
         "zccl_gpu_compress_noalloc": (i, [sp, vp, sz, f, i, i, vp, ctypes.POINTER(vp)]),
+        "zccl_gpu_batch_bytes": (sz, [i, ctypes.POINTER(BatchJobDesc), sz, i]),
+        "zccl_gpu_batch_plan": (i, [ctypes.POINTER(BatchDesc), i, ctypes.POINTER(BatchJobDesc), sz, i, vp,
+                                    sz, vp]),
+        "zccl_gpu_batch_run": (i, [ctypes.POINTER(BatchDesc), vp]),
+        "zccl_gpu_batch_tune": (i, [ctypes.POINTER(BatchDesc), vp]),
+        "zccl_gpu_batch_check": (i, [ctypes.POINTER(BatchDesc), vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -201,7 +225,7 @@ class DeviceStream:
             cap = data.numel()
         else:
             self.buf = torch.empty(max(cap, 16), dtype=torch.uint8, device=codec.device)
-        self.index = torch.empty(codec.index_bytes, dtype=torch.uint8, device=codec.device)
+        self.index = torch.zeros(codec.index_bytes, dtype=torch.uint8, device=codec.device)
         self.desc = StreamDesc(self.buf.data_ptr(), cap, self.index.data_ptr(), 0, 0)
 
     @classmethod
@@ -277,3 +301,61 @@ class Codec:
 
     def check(self) -> None:
         _check(lib().zccl_gpu_check(self.ws.data_ptr(), self.stream_ptr), "device status")
+
+
+BATCH_COMPRESS, BATCH_HOMADD = 0, 1
+
+
+class Batch:
+    """Many streams in one persistent launch (the zccl_gpu_batch_* calls).
+
+    kind BATCH_COMPRESS: jobs are (x, eb, T, out) with x a CUDA float
+    tensor and out a DeviceStream; kind BATCH_HOMADD: jobs are (ins, T, out)
+    with ins a list of indexed DeviceStreams of one geometry.  Planned once;
+    run() is one memset and one launch on `stream` (a torch stream, default
+    the current one), which can be recorded into a CUDA graph."""
+
+    def __init__(self, kind: int, jobs, L: int = 32, device: str = "cuda", stream=None):
+        import torch
+        self.kind, self.L = kind, int(L)
+        self.torch_stream = stream or torch.cuda.current_stream(torch.device(device))
+        n = len(jobs)
+        arr = (BatchJobDesc * n)()
+        self._keep = []  # ctypes arrays the descriptors point into
+        self.outs = []
+        for k, job in enumerate(jobs):
+            d = arr[k]
+            if kind == BATCH_COMPRESS:
+                x, eb, T, out = job
+                d.d_in, d.n, d.eb, d.T = x.data_ptr(), x.numel(), float(eb), int(T)
+            else:
+                ins, T, out = job
+                ia = (StreamDesc * len(ins))(*[s.desc for s in ins])
+                self._keep.append(ia)
+                d.ins, d.P, d.n, d.T = ia, len(ins), out.codec.n, int(T)
+            d.out = ctypes.pointer(out.desc)
+            self.outs.append(out)
+        self._jobs = arr
+        nbytes = lib().zccl_gpu_batch_bytes(kind, arr, n, self.L)
+        if not nbytes:
+            raise ZcclError(-1, "zccl_gpu_batch_bytes")
+        self.mem = torch.empty(nbytes, dtype=torch.uint8, device=device)
+        self.desc = BatchDesc()
+        _check(lib().zccl_gpu_batch_plan(ctypes.byref(self.desc), kind, arr, n, self.L, self.mem.data_ptr(),
+                                         nbytes, ctypes.c_void_p(self.torch_stream.cuda_stream)),
+               "zccl_gpu_batch_plan")
+
+    def _st(self, stream):
+        import torch
+        s = stream or torch.cuda.current_stream()
+        return ctypes.c_void_p(s.cuda_stream)
+
+    def run(self, stream=None) -> None:
+        _check(lib().zccl_gpu_batch_run(ctypes.byref(self.desc), self._st(stream)), "zccl_gpu_batch_run")
+
+    def tune(self, stream=None) -> int:
+        _check(lib().zccl_gpu_batch_tune(ctypes.byref(self.desc), self._st(stream)), "zccl_gpu_batch_tune")
+        return self.desc.grid
+
+    def check(self, stream=None) -> None:
+        _check(lib().zccl_gpu_batch_check(ctypes.byref(self.desc), self._st(stream)), "batch status")

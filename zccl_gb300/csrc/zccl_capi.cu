@@ -14,6 +14,7 @@
 #include <string.h>
 
 #include <mutex>
+#include <vector>
 
 #include "../../include/zccl_gpu.h"
 #include "zkern.cuh"
@@ -186,6 +187,19 @@ int walk_stream(zccl_gpu_stream *s, const ZGeom &g, void *ws, cudaStream_t st)
 
 bool valid_stream(const zccl_gpu_stream *s) { return s && s->bytes && s->index; }
 
+/* Shared-memory layouts, with room for the kernels' copies of their jobs:
+ * two compute slots (the tile in progress and the one just claimed) and the
+ * placer's. */
+ZSmem compress_smem(const ZGeom &g)
+{
+    return zg_smem(0, g.L, g.TB, (uint32_t)(2 * sizeof(CompressJob) + sizeof(ZPlace)));
+}
+
+ZSmem homadd_smem(const ZGeom &g)
+{
+    return zg_smem(2, g.L, g.TB, (uint32_t)(2 * sizeof(HomAddJob) + sizeof(ZPlace)));
+}
+
 } // namespace
 
 /* ==================================================================== */
@@ -227,15 +241,17 @@ extern "C" int zccl_gpu_compress(zccl_gpu_stream *out, const float *d_in, size_t
     if (!(eb > 0.0f) || !isfinite(eb)) return ZCCL_GPU_EINVAL;
     cudaStream_t st = (cudaStream_t)cuda_stream;
     CompressArgs a;
-    a.x = d_in;
-    a.out = out->bytes;
-    a.cap = out->capacity;
-    a.g = g;
-    a.inv = 1.0f / eb; /* float division, as ZCCL/src/ZCCL_float.c:540 */
-    a.idx = bind_index(out->index, g);
+    memset(&a, 0, sizeof(a));
+    a.job.g = g;
+    a.job.x = d_in;
+    a.job.out = out->bytes;
+    a.job.cap = out->capacity;
+    a.job.inv = 1.0f / eb; /* float division, as ZCCL/src/ZCCL_float.c:540 */
+    a.job.idx = bind_index(out->index, g);
     a.w = bind_ws(d_ws);
+    a.job.status = a.w.status;
     a.wt = width_table();
-    a.sm = zg_smem(0, g.L, g.TB);
+    a.sm = compress_smem(g);
     if (cudaMemsetAsync(d_ws, 0, ws_clear_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
     int rc = cuda_status(launch_compress(a, st));
     if (rc == ZCCL_GPU_OK) {
@@ -276,7 +292,7 @@ extern "C" int zccl_gpu_decompress(float *d_out, zccl_gpu_stream *in, size_t n, 
     a.idx = bind_index(in->index, g);
     a.qprev_valid = in->qprev_valid;
     a.w = w;
-    a.sm = zg_smem(1, g.L, g.TB);
+    a.sm = zg_smem(1, g.L, g.TB, 0);
     int rc = cuda_status(launch_decompress(a, st));
     if (rc == ZCCL_GPU_OK) in->qprev_valid = 1;
     return rc;
@@ -303,23 +319,24 @@ extern "C" int zccl_gpu_homadd_cases(zccl_gpu_stream *out, zccl_gpu_stream *ins,
             if (rc) return rc;
         }
         ZIndex ix = bind_index(ins[p].index, g);
-        a.in[p].bytes = ins[p].bytes;
-        a.in[p].avail = ins[p].capacity;
-        a.in[p].widths = ix.widths;
-        a.in[p].tile_off = ix.tile_off;
-        a.in[p].tile_qprev = ix.tile_qprev;
+        a.job.in[p].bytes = ins[p].bytes;
+        a.job.in[p].avail = ins[p].capacity;
+        a.job.in[p].widths = ix.widths;
+        a.job.in[p].tile_off = ix.tile_off;
+        a.job.in[p].tile_qprev = ix.tile_qprev;
         qv &= ins[p].qprev_valid ? 1 : 0;
     }
-    a.P = (uint32_t)P;
-    a.qprev_valid = qv;
-    a.out = out->bytes;
-    a.cap = out->capacity;
-    a.idx = bind_index(out->index, g);
+    a.job.P = (uint32_t)P;
+    a.job.qprev_valid = qv;
+    a.job.out = out->bytes;
+    a.job.cap = out->capacity;
+    a.job.idx = bind_index(out->index, g);
+    a.job.g = g;
+    a.job.status = w.status;
     a.cases = d_cases;
-    a.g = g;
     a.w = w;
     a.wt = width_table();
-    a.sm = zg_smem(2, g.L, g.TB);
+    a.sm = homadd_smem(g);
     int rc = cuda_status(launch_homadd(a, st));
     if (rc == ZCCL_GPU_OK) {
         out->indexed = 1;
@@ -375,6 +392,234 @@ extern "C" const char *zccl_gpu_strerror(int status)
     case ZCCL_GPU_ESCRATCH: return "input needs more than the fixed scratch array";
     default: return "unknown status";
     }
+}
+
+/* ==================================================================== */
+/* batches                                                              */
+/* ==================================================================== */
+
+namespace {
+
+/* d_mem: err | walk_err | ticket | pad | status[ntiles] | jobs | tile_job[ntiles] | job_tile0[njobs] */
+struct BatchLayout {
+    size_t clear, jobs, map, tile0, total;
+};
+
+BatchLayout batch_layout(int kind, size_t njobs, size_t ntiles)
+{
+    BatchLayout l;
+    l.clear = 16 + 8 * ntiles;
+    l.jobs = align16(l.clear);
+    l.map = align16(l.jobs + njobs * (kind == ZCCL_GPU_BATCH_COMPRESS ? sizeof(CompressJob) : sizeof(HomAddJob)));
+    l.tile0 = align16(l.map + 2 * ntiles);
+    l.total = l.tile0 + 8 * njobs;
+    return l;
+}
+
+/* Geometry of every job, checked; returns the total tile count or 0. */
+size_t batch_geoms(int kind, const zccl_gpu_batch_job *jobs, size_t njobs, int L, std::vector<ZGeom> &gs)
+{
+    if ((kind != ZCCL_GPU_BATCH_COMPRESS && kind != ZCCL_GPU_BATCH_HOMADD) || !jobs || njobs < 1 ||
+        njobs > 65535)
+        return 0;
+    gs.resize(njobs);
+    size_t ntiles = 0;
+    for (size_t j = 0; j < njobs; j++) {
+        const zccl_gpu_batch_job &J = jobs[j];
+        if (make_geom(J.n, L, J.T, &gs[j]) || !valid_stream(J.out)) return 0;
+        if (kind == ZCCL_GPU_BATCH_COMPRESS) {
+            if (!J.d_in || !(J.eb > 0.0f) || !isfinite(J.eb)) return 0;
+        } else {
+            if (!J.ins || J.P < 1 || J.P > ZH_MAXP) return 0;
+            for (int p = 0; p < J.P; p++)
+                if (!valid_stream(&J.ins[p]) || !J.ins[p].indexed || J.ins[p].bytes == J.out->bytes) return 0;
+        }
+        ntiles += gs[j].ntiles;
+    }
+    return ntiles;
+}
+
+} // namespace
+
+extern "C" size_t zccl_gpu_batch_bytes(int kind, const zccl_gpu_batch_job *jobs, size_t njobs, int L)
+{
+    std::vector<ZGeom> gs;
+    const size_t ntiles = batch_geoms(kind, jobs, njobs, L, gs);
+    return ntiles ? batch_layout(kind, njobs, ntiles).total : 0;
+}
+
+extern "C" int zccl_gpu_batch_plan(zccl_gpu_batch *b, int kind, const zccl_gpu_batch_job *jobs,
+                                   size_t njobs, int L, void *d_mem, size_t bytes, void *cuda_stream)
+{
+    std::vector<ZGeom> gs;
+    const size_t ntiles = b && d_mem ? batch_geoms(kind, jobs, njobs, L, gs) : 0;
+    if (!ntiles || ntiles > 0xFFFFFFFFull) return ZCCL_GPU_EINVAL;
+    const BatchLayout lay = batch_layout(kind, njobs, ntiles);
+    if (bytes < lay.total) return ZCCL_GPU_ECAPACITY;
+    uint8_t *base = static_cast<uint8_t *>(d_mem);
+    uint64_t *status = reinterpret_cast<uint64_t *>(base + 16);
+    std::vector<uint16_t> map(ntiles);
+    std::vector<uint64_t> tile0(njobs);
+    std::vector<CompressJob> cj(kind == ZCCL_GPU_BATCH_COMPRESS ? njobs : 0);
+    std::vector<HomAddJob> hj(kind == ZCCL_GPU_BATCH_HOMADD ? njobs : 0);
+    int qv = 1;
+    size_t t0 = 0;
+    for (size_t j = 0; j < njobs; j++) {
+        const zccl_gpu_batch_job &J = jobs[j];
+        const ZGeom &g = gs[j];
+        tile0[j] = t0;
+        for (uint64_t t = 0; t < g.ntiles; t++) map[t0 + t] = (uint16_t)j;
+        if (kind == ZCCL_GPU_BATCH_COMPRESS) {
+            CompressJob &c = cj[j];
+            memset(&c, 0, sizeof(c));
+            c.g = g;
+            c.x = J.d_in;
+            c.out = J.out->bytes;
+            c.cap = J.out->capacity;
+            c.idx = bind_index(J.out->index, g);
+            c.status = status + t0;
+            c.inv = 1.0f / J.eb; /* float division, as ZCCL/src/ZCCL_float.c:540 */
+        } else {
+            HomAddJob &h = hj[j];
+            memset(&h, 0, sizeof(h));
+            h.g = g;
+            int jq = 1;
+            for (int p = 0; p < J.P; p++) {
+                const ZIndex ix = bind_index(J.ins[p].index, g);
+                h.in[p].bytes = J.ins[p].bytes;
+                h.in[p].avail = J.ins[p].capacity;
+                h.in[p].widths = ix.widths;
+                h.in[p].tile_off = ix.tile_off;
+                h.in[p].tile_qprev = ix.tile_qprev;
+                jq &= J.ins[p].qprev_valid ? 1 : 0;
+            }
+            h.P = (uint32_t)J.P;
+            h.qprev_valid = jq;
+            h.out = J.out->bytes;
+            h.cap = J.out->capacity;
+            h.idx = bind_index(J.out->index, g);
+            h.status = status + t0;
+            qv &= jq;
+        }
+        t0 += g.ntiles;
+    }
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    const void *jsrc = kind == ZCCL_GPU_BATCH_COMPRESS ? (const void *)cj.data() : (const void *)hj.data();
+    const size_t jbytes = njobs * (kind == ZCCL_GPU_BATCH_COMPRESS ? sizeof(CompressJob) : sizeof(HomAddJob));
+    if (cudaMemcpyAsync(base + lay.jobs, jsrc, jbytes, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(base + lay.map, map.data(), 2 * ntiles, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(base + lay.tile0, tile0.data(), 8 * njobs, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return ZCCL_GPU_ECUDA;
+    memset(b, 0, sizeof(*b));
+    b->kind = kind;
+    b->L = L;
+    b->njobs = njobs;
+    b->ntiles = ntiles;
+    b->d_mem = d_mem;
+    b->clear_bytes = lay.clear;
+    b->jobs_off = lay.jobs;
+    b->map_off = lay.map;
+    b->tile0_off = lay.tile0;
+    b->tb = gs[0].TB;
+    const ZSmem sm = kind == ZCCL_GPU_BATCH_COMPRESS ? compress_smem(gs[0]) : homadd_smem(gs[0]);
+    static_assert(sizeof(sm) == sizeof(b->smem), "layout fields");
+    memcpy(b->smem, &sm, sizeof(sm));
+    b->qprev_valid = kind == ZCCL_GPU_BATCH_COMPRESS ? 1 : qv;
+    for (size_t j = 0; j < njobs; j++) {
+        jobs[j].out->indexed = 1;
+        jobs[j].out->qprev_valid = b->qprev_valid;
+    }
+    return ZCCL_GPU_OK;
+}
+
+extern "C" int zccl_gpu_batch_run(const zccl_gpu_batch *b, void *cuda_stream)
+{
+    if (!b || !b->d_mem || !b->ntiles) return ZCCL_GPU_EINVAL;
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    uint8_t *base = static_cast<uint8_t *>(b->d_mem);
+    if (cudaMemsetAsync(base, 0, b->clear_bytes, st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    ZBatch bt;
+    bt.jobs = base + b->jobs_off;
+    bt.tile_job = reinterpret_cast<const uint16_t *>(base + b->map_off);
+    bt.job_tile0 = reinterpret_cast<const uint64_t *>(base + b->tile0_off);
+    bt.njobs = (uint32_t)b->njobs;
+    bt.ntiles = b->ntiles;
+    ZSmem sm;
+    memcpy(&sm, b->smem, sizeof(sm));
+    if (b->kind == ZCCL_GPU_BATCH_COMPRESS) {
+        CompressArgs a;
+        memset(&a, 0, sizeof(a));
+        a.job.g.L = (uint32_t)b->L; /* the batch's shared L and tile size */
+        a.job.g.TB = b->tb;
+        a.batch = bt;
+        a.w = bind_ws(base);
+        a.wt = width_table();
+        a.sm = sm;
+        a.grid = b->grid;
+        return cuda_status(launch_compress(a, st));
+    }
+    HomAddArgs a;
+    memset(&a, 0, sizeof(a));
+    a.job.g.L = (uint32_t)b->L;
+    a.job.g.TB = b->tb;
+    a.batch = bt;
+    a.w = bind_ws(base);
+    a.wt = width_table();
+    a.sm = sm;
+    a.grid = b->grid;
+    return cuda_status(launch_homadd(a, st));
+}
+
+extern "C" int zccl_gpu_batch_check(const zccl_gpu_batch *b, void *cuda_stream)
+{
+    return b ? zccl_gpu_check(b->d_mem, cuda_stream) : ZCCL_GPU_EINVAL;
+}
+
+extern "C" int zccl_gpu_batch_tune(zccl_gpu_batch *b, void *cuda_stream)
+{
+    if (!b || !b->d_mem) return ZCCL_GPU_EINVAL;
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return ZCCL_GPU_ECUDA;
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return ZCCL_GPU_ECUDA;
+    }
+    /* CTAs per SM from one to what fits (0), each timed over three runs after one warm-up */
+    const unsigned per_sm[] = {1, 2, 3, 4, 6, 0};
+    unsigned best = 0;
+    float best_ms = 1e30f;
+    int rc = ZCCL_GPU_OK;
+    for (unsigned k : per_sm) {
+        b->grid = k * (unsigned)nsm;
+        rc = zccl_gpu_batch_run(b, st);
+        for (int r = 0; r < 3 && rc == ZCCL_GPU_OK; r++) {
+            if (r == 0) cudaEventRecord(e0, st);
+            rc = zccl_gpu_batch_run(b, st);
+        }
+        if (rc) break;
+        cudaEventRecord(e1, st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+            rc = ZCCL_GPU_ECUDA;
+            break;
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = b->grid;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->grid = best;
+    if (rc == ZCCL_GPU_OK) rc = zccl_gpu_check(b->d_mem, st);
+    return rc;
 }
 
 /* ==================================================================== */

@@ -157,9 +157,10 @@ ZG_HD uint64_t zg_stream_worst(const ZGeom *g)
  *   [256, 512) look-back records
  *   rows       per-block rows, TB x row_stride 4-byte words (floats or ints)
  *   in0, in1   double-buffered TMA input (raw floats or tile bytes)
- *   out        packed output tile (compressor, homomorphic add) */
+ *   out        packed output tile (compressor, homomorphic add)
+ *   jobs       copies of the jobs in progress (job_bytes) */
 typedef struct ZSmem {
-    uint32_t rows, in0, in1, out, total;
+    uint32_t rows, in0, in1, out, jobs, total;
 } ZSmem;
 
 ZG_HD uint32_t zg_a16(uint32_t v) { return (v + 15u) & ~15u; }
@@ -181,7 +182,17 @@ ZG_HD uint32_t zg_ring_bytes(uint32_t L, uint32_t TB) { return zg_ring_need(zg_t
  * from the input into the rows, so the rows share the input's space
  * (rows == in0); longer blocks get separate regions.  The decompressor and
  * the homomorphic add double-buffer their input. */
-ZG_HD ZSmem zg_smem(uint32_t kind, uint32_t L, uint32_t TB)
+ZG_HD ZSmem zg_smem_base(uint32_t kind, uint32_t L, uint32_t TB);
+
+ZG_HD ZSmem zg_smem(uint32_t kind, uint32_t L, uint32_t TB, uint32_t job_bytes)
+{
+    ZSmem m = zg_smem_base(kind, L, TB);
+    m.jobs = m.total;
+    m.total = zg_a16(m.jobs + job_bytes);
+    return m;
+}
+
+ZG_HD ZSmem zg_smem_base(uint32_t kind, uint32_t L, uint32_t TB)
 {
     ZSmem m;
     const uint32_t rows_bytes = TB * zg_row_stride(L) * 4u;

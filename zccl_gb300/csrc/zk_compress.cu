@@ -33,44 +33,56 @@
 
 namespace {
 
-/* Thread 0: claim the next tile in ticket order and start the TMA copy of
- * its floats (and the element before them) into `in`.  The claimed index
- * lands in *slot; the caller synchronises before reading it. */
+/* Thread 0: claim the next tile in ticket order, copy its job into `slot`
+ * and start the TMA copy of its floats (and the element before them) into
+ * `in`.  The tile within its job lands in *s_tile (ZP_NONE when all are
+ * taken), the job in *s_job; the caller synchronises before reading them. */
 __device__ __forceinline__ void claim_tile(const CompressArgs &a, uint8_t *in, uint64_t *bar,
-                                           uint64_t *slot, uint32_t *s_amax)
+                                           uint64_t *s_tile, uint32_t *s_job, uint32_t *s_amax,
+                                           CompressJob *slot)
 {
     if (threadIdx.x != 0) return;
     const uint64_t t = atomicAdd(a.w.ticket, 1u);
-    *slot = t;
     *s_amax = 0;
-    if (t < a.g.ntiles) {
-        ZTile zt;
-        zg_tile(&a.g, t, &zt);
-        const uint32_t nel = (uint32_t)(zt.e_end - zt.e_first + 1);
-        tma_load_superset(in, reinterpret_cast<const uint8_t *>(a.x + (zt.e_first - 1)), nel * 4u, bar);
+    const uint64_t total = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
+    if (t >= total) {
+        *s_tile = ZP_NONE;
+        return;
     }
+    uint64_t local;
+    const uint32_t j = batch_job(a.batch, t, &local);
+    copy16(slot, a.batch.jobs ? static_cast<const CompressJob *>(a.batch.jobs) + j : &a.job,
+           sizeof(CompressJob));
+    *s_tile = local;
+    *s_job = j;
+    ZTile zt;
+    zg_tile(&slot->g, local, &zt);
+    const uint32_t nel = (uint32_t)(zt.e_end - zt.e_first + 1);
+    tma_load_superset(in, reinterpret_cast<const uint8_t *>(slot->x + (zt.e_first - 1)), nel * 4u, bar);
 }
 
 /* Block size TB + 32: warps 0 .. TB/32 - 1 compute (one thread per block of
  * the tile), the last warp places packed tiles in the stream. */
 template <bool FAST>
-__global__ void __launch_bounds__(288, 3) k_compress(const CompressArgs a)
+__global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ CompressArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     uint64_t *bar_tma = reinterpret_cast<uint64_t *>(smem);      /* the tile's floats arrived */
     uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 32);    /* [33] */
-    uint64_t *s_tile = reinterpret_cast<uint64_t *>(smem + 168); /* the claimed tile */
+    uint64_t *s_tile = reinterpret_cast<uint64_t *>(smem + 168); /* the claimed tile (within its job) */
     uint32_t *s_amax = reinterpret_cast<uint32_t *>(smem + 176);
     uint32_t *s_pos = reinterpret_cast<uint32_t *>(smem + 184);  /* ring position of this tile */
+    uint32_t *s_job = reinterpret_cast<uint32_t *>(smem + 188);  /* the claimed tile's job */
     ZRing *ring = reinterpret_cast<ZRing *>(smem + 256);
+    CompressJob *cj = reinterpret_cast<CompressJob *>(smem + a.sm.jobs); /* [2], by round */
+    ZPlace *pj = reinterpret_cast<ZPlace *>(smem + a.sm.jobs + 2 * sizeof(CompressJob));
     float *rows = reinterpret_cast<float *>(smem + a.sm.rows); /* FAST: the same space as in */
     uint8_t *in = smem + a.sm.in0;
     uint8_t *outb = smem + a.sm.out; /* the ring of packed tiles */
 
-    const ZGeom &g = a.g;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t NC = g.TB, nw = NC >> 5; /* compute threads, compute warps */
-    const uint32_t L = g.L, stride = zg_row_stride(L);
+    const uint32_t NC = blockDim.x - 32, nw = NC >> 5; /* compute threads (TB), compute warps */
+    const uint32_t L = a.job.g.L, stride = zg_row_stride(L); /* one L for the whole batch */
     uint32_t bad = 0;
 
     if (tid == 0) {
@@ -81,7 +93,23 @@ __global__ void __launch_bounds__(288, 3) k_compress(const CompressArgs a)
     __syncthreads();
 
     if (tid >= NC) { /* the placer warp */
-        placer_loop(g, ring, outb, a.out, a.cap, a.idx, a.w.status, a.w.err, bad);
+        const uint64_t max_tiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
+        placer_loop(ring, outb, pj, a.w.err, max_tiles, bad, [&](uint32_t j, ZPlace *p) {
+            if (a.batch.jobs) {
+                const CompressJob &J = static_cast<const CompressJob *>(a.batch.jobs)[j];
+                p->g = J.g;
+                p->out = J.out;
+                p->cap = J.cap;
+                p->idx = J.idx;
+                p->status = J.status;
+            } else {
+                p->g = a.job.g;
+                p->out = a.job.out;
+                p->cap = a.job.cap;
+                p->idx = a.job.idx;
+                p->status = a.job.status;
+            }
+        });
         if (bad) atomicOr(a.w.err, bad);
         return;
     }
@@ -89,19 +117,22 @@ __global__ void __launch_bounds__(288, 3) k_compress(const CompressArgs a)
     /* the compute warps */
     const uint32_t R = zg_ring_bytes(L, NC);
     uint32_t pos_prev = 0, end_prev = 0; /* thread 0: the previous tile's place in the ring */
-    if (tid == 0) claim_tile(a, in, bar_tma, s_tile, s_amax);
+    claim_tile(a, in, bar_tma, s_tile, s_job, s_amax, &cj[0]);
     named_sync(1, NC);
     uint64_t tile = *s_tile;
+    uint32_t job = *s_job;
 
     for (uint32_t it = 0;; it++) {
-        if (tile >= g.ntiles) {
+        if (tile == ZP_NONE) {
             /* tell the placer there is nothing more (once it has read the slot) */
             if (tid == 0) {
                 ring_wait(&ring->placed, it >= 1 ? it - 1 : 0u, a.w.err);
-                ring_publish(ring, it, ZP_NONE, 0, 0);
+                ring_publish(ring, it, ZP_NONE, 0, 0, 0);
             }
             break;
         }
+        const CompressJob &J = cj[it & 1u];
+        const ZGeom &g = J.g;
         ZTile z;
         zg_tile(&g, tile, &z);
 
@@ -110,7 +141,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const CompressArgs a)
          *    the tile's largest magnitude */
         mbar_wait(bar_tma, it & 1u, a.w.err);
         const float *xin =
-            reinterpret_cast<const float *>(in + ((uintptr_t)(a.x + (z.e_first - 1)) & 15u));
+            reinterpret_cast<const float *>(in + ((uintptr_t)(J.x + (z.e_first - 1)) & 15u));
         const float xprev0 = xin[0]; /* the head, or the last element of the previous tile */
         uint32_t amax = abs_bits(xprev0);
         if (FAST) {
@@ -155,7 +186,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const CompressArgs a)
         amax = __reduce_max_sync(0xffffffffu, amax);
         if (lane == 0) atomicMax(s_amax, amax);
         named_sync(1, NC);
-        const bool fastq = tile_fast_ok(*s_amax, a.inv);
+        const bool fastq = tile_fast_ok(*s_amax, J.inv);
 
         /* 2. quantize, delta, width */
         const bool own = tid < z.nblk;
@@ -165,11 +196,11 @@ __global__ void __launch_bounds__(288, 3) k_compress(const CompressArgs a)
         uint32_t b = 0, size = 0, smask = 0;
         uint32_t m[32];
         if (FAST && fastq && n == 32) { /* the straight-line path */
-            int32_t qp = quantize_fast(xp, a.inv);
+            int32_t qp = quantize_fast(xp, J.inv);
             uint32_t mx = 0;
 #pragma unroll
             for (int j = 0; j < 32; j++) {
-                const int32_t q = quantize_fast(row[j], a.inv);
+                const int32_t q = quantize_fast(row[j], J.inv);
                 const int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
                 qp = q;
                 smask = (smask << 1) | ((uint32_t)d >> 31);
@@ -179,13 +210,13 @@ __global__ void __launch_bounds__(288, 3) k_compress(const CompressArgs a)
             b = width_of(mx, a.wt);
             size = zg_block_bytes(b, 32);
         } else if (FAST && own) { /* a short block or the exact slow quantization */
-            int32_t qp = fastq ? quantize_fast(xp, a.inv) : quantize(xp, a.inv, bad);
+            int32_t qp = fastq ? quantize_fast(xp, J.inv) : quantize(xp, J.inv, bad);
             uint32_t mx = 0;
 #pragma unroll
             for (int j = 0; j < 32; j++) {
                 m[j] = 0;
                 if ((uint32_t)j < n) {
-                    const int32_t q = fastq ? quantize_fast(row[j], a.inv) : quantize(row[j], a.inv, bad);
+                    const int32_t q = fastq ? quantize_fast(row[j], J.inv) : quantize(row[j], J.inv, bad);
                     const int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
                     qp = q;
                     smask |= ((uint32_t)d >> 31) << (31 - j);
@@ -196,10 +227,10 @@ __global__ void __launch_bounds__(288, 3) k_compress(const CompressArgs a)
             b = width_of(mx, a.wt);
             size = zg_block_bytes(b, n);
         } else if (own) { /* blocks above 32 elements: the rows are read again when packing */
-            int32_t qp = fastq ? quantize_fast(xp, a.inv) : quantize(xp, a.inv, bad);
+            int32_t qp = fastq ? quantize_fast(xp, J.inv) : quantize(xp, J.inv, bad);
             uint32_t mx = 0;
             for (uint32_t j = 0; j < n; j++) {
-                const int32_t q = fastq ? quantize_fast(row[j], a.inv) : quantize(row[j], a.inv, bad);
+                const int32_t q = fastq ? quantize_fast(row[j], J.inv) : quantize(row[j], J.inv, bad);
                 mx = max(mx, (uint32_t)abs((int32_t)((uint32_t)q - (uint32_t)qp)));
                 qp = q;
             }
@@ -215,10 +246,10 @@ __global__ void __launch_bounds__(288, 3) k_compress(const CompressArgs a)
         uint32_t total;
         const uint32_t off = grp_excl_scan(size, wsum, &total, NC, 1);
         total += headb;
-        if (warp == 0) lb_publish(a.w.status, tile, total, tile == 0, 0);
-        const int32_t qprev0 = fastq ? quantize_fast(xprev0, a.inv) : quantize(xprev0, a.inv, bad);
-        if (own) a.idx.widths[z.gblk0 + tid] = (uint8_t)b;
-        if (tid == 0) a.idx.tile_qprev[tile] = qprev0;
+        if (warp == 0) lb_publish(J.status, tile, total, tile == 0, 0);
+        const int32_t qprev0 = fastq ? quantize_fast(xprev0, J.inv) : quantize(xprev0, J.inv, bad);
+        if (own) J.idx.widths[z.gblk0 + tid] = (uint8_t)b;
+        if (tid == 0) J.idx.tile_qprev[tile] = qprev0;
 
         /* 4. take room for the packed tile in the ring (waiting, if need
          *    be, for the placer to write out an earlier one), claim the next
@@ -227,7 +258,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const CompressArgs a)
          *    while holding a claimed tile whose size is not yet published. */
         if (tid == 0) {
             *s_pos = ring_reserve(ring, it, zg_ring_need(total), R, pos_prev, end_prev, a.w.err);
-            if (FAST) claim_tile(a, in, bar_tma, s_tile, s_amax);
+            if (FAST) claim_tile(a, in, bar_tma, s_tile, s_job, s_amax, &cj[(it + 1) & 1u]);
         }
         named_sync(1, NC);
         const uint32_t pos = *s_pos;
@@ -248,9 +279,9 @@ __global__ void __launch_bounds__(288, 3) k_compress(const CompressArgs a)
             }
         } else {
             if (own) {
-                int32_t qp = fastq ? quantize_fast(xp, a.inv) : quantize(xp, a.inv, bad);
+                int32_t qp = fastq ? quantize_fast(xp, J.inv) : quantize(xp, J.inv, bad);
                 encode_any(pk_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
-                    const int32_t q = fastq ? quantize_fast(row[j], a.inv) : quantize(row[j], a.inv, bad);
+                    const int32_t q = fastq ? quantize_fast(row[j], J.inv) : quantize(row[j], J.inv, bad);
                     const int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
                     qp = q;
                     neg = (uint32_t)d >> 31;
@@ -258,11 +289,12 @@ __global__ void __launch_bounds__(288, 3) k_compress(const CompressArgs a)
                 });
             }
             named_sync(1, NC); /* the rows have been read for the last time */
-            if (tid == 0) claim_tile(a, in, bar_tma, s_tile, s_amax);
+            if (tid == 0) claim_tile(a, in, bar_tma, s_tile, s_job, s_amax, &cj[(it + 1) & 1u]);
         }
         named_sync(1, NC); /* the packed tile is complete; the claimed index is visible */
-        if (tid == 0) ring_publish(ring, it, tile, total, pos);
+        if (tid == 0) ring_publish(ring, it, tile, job, total, pos);
         tile = *s_tile;
+        job = *s_job;
     }
     if (bad) atomicOr(a.w.err, bad);
 }
@@ -271,12 +303,14 @@ __global__ void __launch_bounds__(288, 3) k_compress(const CompressArgs a)
 
 cudaError_t launch_compress(const CompressArgs &a, cudaStream_t st)
 {
-    const bool fast = a.g.L <= 32;
+    const bool fast = a.job.g.L <= 32;
     const void *fn = fast ? (const void *)k_compress<true> : (const void *)k_compress<false>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
     if (e != cudaSuccess) return e;
-    const unsigned threads = a.g.TB + 32; /* compute warps and the placer warp */
-    unsigned grid = persistent_grid(fn, threads, a.sm.total, a.g.ntiles);
+    const unsigned threads = a.job.g.TB + 32; /* compute warps and the placer warp */
+    const uint64_t tiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
+    unsigned grid = persistent_grid(fn, threads, a.sm.total, tiles);
+    if (a.grid && a.grid < grid) grid = a.grid;
     if (fast)
         k_compress<true><<<grid, threads, a.sm.total, st>>>(a);
     else

@@ -30,17 +30,17 @@ struct BlockSlot {
 
 /* The compute threads: sizes of input p's blocks in tile t, their offsets,
  * and (thread 0) the TMA copy of those bytes into buf. */
-__device__ __forceinline__ BlockSlot stage_input(const HomAddArgs &a, uint64_t t, uint32_t p,
+__device__ __forceinline__ BlockSlot stage_input(const HomAddJob &J, uint64_t t, uint32_t p,
                                                  uint8_t *buf, uint64_t *bar, uint32_t *wsum,
                                                  uint64_t *s_base, uint32_t &bad)
 {
-    const HomInput &in = a.in[p];
+    const HomInput &in = J.in[p];
     BlockSlot sl = {0, 0, 0};
     ZTile z;
-    zg_tile(&a.g, t, &z);
+    zg_tile(&J.g, t, &z);
     uint32_t size = 0;
     if (threadIdx.x < z.nblk) {
-        sl.n = zg_block_len(z.seg_len, a.g.L, z.blk0 + threadIdx.x);
+        sl.n = zg_block_len(z.seg_len, J.g.L, z.blk0 + threadIdx.x);
         sl.b = in.widths[z.gblk0 + threadIdx.x];
         if (sl.b > 32) {
             bad |= ZERR_CORRUPT;
@@ -49,7 +49,7 @@ __device__ __forceinline__ BlockSlot stage_input(const HomAddArgs &a, uint64_t t
         size = zg_block_bytes(sl.b, sl.n);
     }
     uint32_t total;
-    sl.off = grp_excl_scan(size, wsum, &total, a.g.TB, 1);
+    sl.off = grp_excl_scan(size, wsum, &total, J.g.TB, 1);
     total += z.has_head ? 4u : 0u;
     if (threadIdx.x == 0) {
         uint64_t base = in.tile_off[t];
@@ -66,25 +66,56 @@ __device__ __forceinline__ BlockSlot stage_input(const HomAddArgs &a, uint64_t t
     return sl;
 }
 
+/* One thread: a job into shared memory, with only the inputs it uses. */
+__device__ __forceinline__ void copy_job(HomAddJob *dst, const HomAddJob *src)
+{
+    const uint32_t P = src->P < ZH_MAXP ? src->P : ZH_MAXP;
+    copy16(dst, src, (uint32_t)offsetof(HomAddJob, in));
+    copy16(&dst->in[0], &src->in[0], (uint32_t)((P * sizeof(HomInput) + 15u) & ~15u));
+    copy16(&dst->P, &src->P, (uint32_t)(sizeof(HomAddJob) - offsetof(HomAddJob, P)));
+}
+
+/* Thread 0: claim the next tile and copy its job into `slot`; the tile
+ * within its job lands in *s_tile (ZP_NONE when all are taken), the job in
+ * *s_job.  The caller synchronises before reading them. */
+__device__ __forceinline__ void claim_sum(const HomAddArgs &a, uint64_t *s_tile, uint32_t *s_job,
+                                          HomAddJob *slot)
+{
+    if (threadIdx.x != 0) return;
+    const uint64_t t = atomicAdd(a.w.ticket, 1u);
+    const uint64_t total = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
+    if (t >= total) {
+        *s_tile = ZP_NONE;
+        return;
+    }
+    uint64_t local;
+    const uint32_t j = batch_job(a.batch, t, &local);
+    copy_job(slot, a.batch.jobs ? static_cast<const HomAddJob *>(a.batch.jobs) + j : &a.job);
+    *s_tile = local;
+    *s_job = j;
+}
+
 /* Block size TB + 32: warps 0 .. TB/32 - 1 add (one thread per block of the
  * tile), the last warp places packed sums in the stream. */
 template <bool FAST>
-__global__ void __launch_bounds__(288, 2) k_homadd(const HomAddArgs a)
+__global__ void __launch_bounds__(288, 2) k_homadd(const __grid_constant__ HomAddArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);          /* [2] input copies */
     uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 32);    /* [33] */
-    uint64_t *s_tile = reinterpret_cast<uint64_t *>(smem + 168); /* the claimed tile */
+    uint64_t *s_tile = reinterpret_cast<uint64_t *>(smem + 168); /* the claimed tile (within its job) */
     uint32_t *s_pos = reinterpret_cast<uint32_t *>(smem + 176);  /* ring position of this sum */
+    uint32_t *s_job = reinterpret_cast<uint32_t *>(smem + 180);  /* the claimed tile's job */
     uint64_t *s_base = reinterpret_cast<uint64_t *>(smem + 192); /* [2] */
     ZRing *ring = reinterpret_cast<ZRing *>(smem + 256);
+    HomAddJob *hj = reinterpret_cast<HomAddJob *>(smem + a.sm.jobs); /* [2], by round */
+    ZPlace *pj = reinterpret_cast<ZPlace *>(smem + a.sm.jobs + 2 * sizeof(HomAddJob));
     uint32_t *acc_rows = reinterpret_cast<uint32_t *>(smem + a.sm.rows);
     uint8_t *outs = smem + a.sm.out; /* the ring of packed sums */
 
-    const ZGeom &g = a.g;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t NC = g.TB; /* compute threads */
-    const uint32_t L = g.L, stride = zg_row_stride(L), P = a.P;
+    const uint32_t NC = blockDim.x - 32; /* compute threads (TB) */
+    const uint32_t L = a.job.g.L, stride = zg_row_stride(L); /* one L for the whole batch */
     uint32_t bad = 0;
     /* see k_decompress: a failed index walk stops every CTA alike */
     if (*(volatile const uint32_t *)a.w.walk_err) return;
@@ -97,7 +128,23 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const HomAddArgs a)
     __syncthreads();
 
     if (tid >= NC) { /* the placer warp */
-        placer_loop(g, ring, outs, a.out, a.cap, a.idx, a.w.status, a.w.err, bad);
+        const uint64_t max_tiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
+        placer_loop(ring, outs, pj, a.w.err, max_tiles, bad, [&](uint32_t j, ZPlace *p) {
+            if (a.batch.jobs) {
+                const HomAddJob &J = static_cast<const HomAddJob *>(a.batch.jobs)[j];
+                p->g = J.g;
+                p->out = J.out;
+                p->cap = J.cap;
+                p->idx = J.idx;
+                p->status = J.status;
+            } else {
+                p->g = a.job.g;
+                p->out = a.job.out;
+                p->cap = a.job.cap;
+                p->idx = a.job.idx;
+                p->status = a.job.status;
+            }
+        });
         if (bad) atomicOr(a.w.err, bad);
         return;
     }
@@ -109,22 +156,25 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const HomAddArgs a)
     uint32_t ld = 0; /* index of the current copy in the two-buffer stream */
     const uint32_t R = zg_ring_bytes(L, NC);
     uint32_t pos_prev = 0, end_prev = 0; /* thread 0: the previous sum's place in the ring */
-    if (tid == 0) *s_tile = atomicAdd(a.w.ticket, 1u);
+    claim_sum(a, s_tile, s_job, &hj[0]);
     named_sync(1, NC);
     uint64_t tile = *s_tile;
+    uint32_t job = *s_job;
     BlockSlot cur = {0, 0, 0};
-    if (tile < g.ntiles)
-        cur = stage_input(a, tile, 0, smem + a.sm.in0, &bar[0], wsum, &s_base[0], bad);
+    if (tile != ZP_NONE) cur = stage_input(hj[0], tile, 0, smem + a.sm.in0, &bar[0], wsum, &s_base[0], bad);
 
     for (uint32_t it = 0;; it++) {
-        if (tile >= g.ntiles) {
+        if (tile == ZP_NONE) {
             /* tell the placer there is nothing more (once it has read the slot) */
             if (tid == 0) {
                 ring_wait(&ring->placed, it >= 1 ? it - 1 : 0u, a.w.err);
-                ring_publish(ring, it, ZP_NONE, 0, 0);
+                ring_publish(ring, it, ZP_NONE, 0, 0, 0);
             }
             break;
         }
+        const HomAddJob &J = hj[it & 1u];
+        const ZGeom &g = J.g;
+        const uint32_t P = J.P;
         ZTile z;
         zg_tile(&g, tile, &z);
         const bool own = tid < z.nblk;
@@ -144,13 +194,13 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const HomAddArgs a)
             /* the next input's copy runs while this one is added */
             BlockSlot nxt = {0, 0, 0};
             if (p + 1 < P)
-                nxt = stage_input(a, tile, p + 1, smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u],
+                nxt = stage_input(J, tile, p + 1, smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u],
                                   wsum, &s_base[cb ^ 1u], bad);
-            if (a.qprev_valid && tid == 0) qsum += (uint32_t)a.in[p].tile_qprev[tile];
+            if (J.qprev_valid && tid == 0) qsum += (uint32_t)J.in[p].tile_qprev[tile];
             mbar_wait(&bar[cb], (ld >> 1) & 1u, a.w.err);
             const uint8_t *buf = smem + (cb ? a.sm.in1 : a.sm.in0);
             const uint32_t *sw = reinterpret_cast<const uint32_t *>(buf);
-            const uint32_t ph = (uint32_t)((uintptr_t)(a.in[p].bytes + s_base[cb]) & 15u);
+            const uint32_t ph = (uint32_t)((uintptr_t)(J.in[p].bytes + s_base[cb]) & 15u);
             if (z.has_head && tid == 0) {
                 uint32_t h = 0;
 #pragma unroll
@@ -217,23 +267,22 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const HomAddArgs a)
         uint32_t total;
         const uint32_t off = grp_excl_scan(size, wsum, &total, NC, 1);
         total += headb;
-        if (warp == 0) lb_publish(a.w.status, tile, total, tile == 0, 0);
-        if (own) a.idx.widths[z.gblk0 + tid] = (uint8_t)b;
-        if (tid == 0 && a.qprev_valid) a.idx.tile_qprev[tile] = (int32_t)qsum;
+        if (warp == 0) lb_publish(J.status, tile, total, tile == 0, 0);
+        if (own) J.idx.widths[z.gblk0 + tid] = (uint8_t)b;
+        if (tid == 0 && J.qprev_valid) J.idx.tile_qprev[tile] = (int32_t)qsum;
 
         /* take room for the packed sum in the ring (waiting, if need be, for
          * the placer to write out an earlier one), claim the next tile and
          * start its first input's copy, and pack this sum while it arrives */
-        if (tid == 0) {
-            *s_pos = ring_reserve(ring, it, zg_ring_need(total), R, pos_prev, end_prev, a.w.err);
-            *s_tile = atomicAdd(a.w.ticket, 1u);
-        }
+        if (tid == 0) *s_pos = ring_reserve(ring, it, zg_ring_need(total), R, pos_prev, end_prev, a.w.err);
+        claim_sum(a, s_tile, s_job, &hj[(it + 1) & 1u]);
         named_sync(1, NC);
         const uint64_t next = *s_tile;
+        const uint32_t next_job = *s_job;
         const uint32_t pos = *s_pos;
-        if (next < g.ntiles)
-            cur = stage_input(a, next, 0, smem + (ld & 1u ? a.sm.in1 : a.sm.in0), &bar[ld & 1u], wsum,
-                              &s_base[ld & 1u], bad);
+        if (next != ZP_NONE)
+            cur = stage_input(hj[(it + 1) & 1u], next, 0, smem + (ld & 1u ? a.sm.in1 : a.sm.in0), &bar[ld & 1u],
+                              wsum, &s_base[ld & 1u], bad);
         uint8_t *pk = outs + pos;
         const uint32_t pk_sa = smem_u32(pk);
         smem_zero(pk, total + 8, tid, NC);
@@ -250,8 +299,9 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const HomAddArgs a)
             });
         }
         named_sync(1, NC); /* the packed sum is complete; acc_rows are free */
-        if (tid == 0) ring_publish(ring, it, tile, total, pos);
+        if (tid == 0) ring_publish(ring, it, tile, job, total, pos);
         tile = next;
+        job = next_job;
     }
     if (bad) atomicOr(a.w.err, bad);
 }
@@ -260,12 +310,14 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const HomAddArgs a)
 
 cudaError_t launch_homadd(const HomAddArgs &a, cudaStream_t st)
 {
-    const bool fast = a.g.L <= 32;
+    const bool fast = a.job.g.L <= 32;
     const void *fn = fast ? (const void *)k_homadd<true> : (const void *)k_homadd<false>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
     if (e != cudaSuccess) return e;
-    const unsigned threads = a.g.TB + 32; /* compute warps and the placer warp */
-    unsigned grid = persistent_grid(fn, threads, a.sm.total, a.g.ntiles);
+    const unsigned threads = a.job.g.TB + 32; /* compute warps and the placer warp */
+    const uint64_t tiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
+    unsigned grid = persistent_grid(fn, threads, a.sm.total, tiles);
+    if (a.grid && a.grid < grid) grid = a.grid;
     if (fast)
         k_homadd<true><<<grid, threads, a.sm.total, st>>>(a);
     else

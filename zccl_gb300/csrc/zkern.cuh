@@ -32,16 +32,35 @@ struct ZIndex {
     uint64_t *size;      /* [1]       total stream bytes */
 };
 
-struct CompressArgs {
+/* One buffer to compress: the kernels take a single job from their
+ * arguments, or a batch of jobs from device memory, whose tiles then form
+ * one ticket sequence (tile_job gives every batch tile its job, job_tile0
+ * every job its first batch tile). */
+struct alignas(16) CompressJob {
+    ZGeom g;
     const float *x;
     uint8_t *out;
     uint64_t cap; /* writable bytes at `out` */
-    ZGeom g;
-    float inv; /* 1.0f / eb, computed on the host in float */
     ZIndex idx;
-    ZWork w;
+    uint64_t *status; /* this buffer's look-back words, one per tile */
+    float inv;        /* 1.0f / eb, computed on the host in float */
+};
+
+struct ZBatch {
+    const void *jobs;          /* CompressJob[] or HomAddJob[]; null: the single job */
+    const uint16_t *tile_job;  /* [ntiles] */
+    const uint64_t *job_tile0; /* [njobs] */
+    uint32_t njobs;
+    uint64_t ntiles; /* tiles of all jobs */
+};
+
+struct CompressArgs {
+    CompressJob job; /* the single job (batch.jobs == null) */
+    ZBatch batch;
+    ZWork w; /* err and ticket; status is per job */
     ZWidthTable wt;
     ZSmem sm;
+    uint32_t grid; /* CTAs to launch, 0 = as many as fit */
 };
 
 struct DecompressArgs {
@@ -64,18 +83,26 @@ struct HomInput {
     const int32_t *tile_qprev;
 };
 
-struct HomAddArgs {
+/* One homomorphic sum of P streams. */
+struct alignas(16) HomAddJob {
+    ZGeom g;
     HomInput in[ZH_MAXP];
     uint32_t P;
-    int qprev_valid;       /* every input's tile_qprev is valid */
+    int qprev_valid;  /* every input's tile_qprev is valid */
     uint8_t *out;
-    uint64_t cap;          /* writable bytes at `out` */
-    ZIndex idx;            /* index of the output stream */
+    uint64_t cap;     /* writable bytes at `out` */
+    ZIndex idx;       /* index of the output stream */
+    uint64_t *status; /* look-back words of the output, one per tile */
+};
+
+struct HomAddArgs {
+    HomAddJob job; /* the single job (batch.jobs == null) */
+    ZBatch batch;
     unsigned long long *cases; /* optional [4]: both zero, first zero, second zero, both non-zero (P == 2) */
-    ZGeom g;
     ZWork w;
     ZWidthTable wt;
     ZSmem sm;
+    uint32_t grid; /* CTAs to launch, 0 = as many as fit */
 };
 
 #define WALK_WW 4096u /* bytes per window of the parallel header walk */
@@ -166,7 +193,8 @@ __device__ __forceinline__ void place_tile(const ZGeom &g, const ZPending &pd, c
 struct ZRing {
     uint32_t packed, placed;
     uint32_t pos[2], total[2];
-    uint64_t tile[2];
+    uint64_t tile[2]; /* the tile within its job */
+    uint32_t job[2];  /* its job in the batch (0 for a single job) */
 };
 
 __device__ __forceinline__ void ring_set(uint32_t *p, uint32_t v)
@@ -210,50 +238,91 @@ __device__ __forceinline__ uint32_t ring_reserve(ZRing *ring, uint32_t k, uint32
 
 /* Compute thread 0, after every compute thread has finished packing tile k
  * (pass ZP_NONE as `tile` once there are no more tiles). */
-__device__ __forceinline__ void ring_publish(ZRing *ring, uint32_t k, uint64_t tile, uint32_t total,
-                                             uint32_t pos)
+__device__ __forceinline__ void ring_publish(ZRing *ring, uint32_t k, uint64_t tile, uint32_t job,
+                                             uint32_t total, uint32_t pos)
 {
     ring->tile[k & 1u] = tile;
+    ring->job[k & 1u] = job;
     ring->total[k & 1u] = total;
     ring->pos[k & 1u] = pos;
     ring_set(&ring->packed, k + 1);
 }
 
+/* What the placer needs of a job. */
+struct ZPlace {
+    ZGeom g;
+    uint8_t *out;
+    uint64_t cap;
+    ZIndex idx;
+    uint64_t *status;
+};
+
 /* The placer warp: for every packed tile, in order, the decoupled look-back
- * gives its byte offset in the stream; its bytes go out with 16-byte vector
+ * gives its byte offset in its stream; its bytes go out with 16-byte vector
  * stores realigned to that offset, with its offset in the side index, the
- * stream size after the last tile and, for a segment's first tile, the
- * chunk offset in the header. */
-__device__ __forceinline__ void placer_loop(const ZGeom &g, ZRing *ring, const uint8_t *ringb, uint8_t *out,
-                                            uint64_t cap, const ZIndex &idx, uint64_t *status,
-                                            uint32_t *err, uint32_t &bad)
+ * stream size after the stream's last tile and, for a segment's first tile,
+ * the chunk offset in the header.  fetch(job, ZPlace *) (lane 0) copies a
+ * job's placement data into shared memory. */
+template <class Fetch>
+__device__ __forceinline__ void placer_loop(ZRing *ring, const uint8_t *ringb, ZPlace *pj, uint32_t *err,
+                                            uint64_t max_tiles, uint32_t &bad, Fetch fetch)
 {
     const uint32_t lane = threadIdx.x & 31u;
-    for (uint64_t k = 0; k <= g.ntiles; k++) {
+    uint32_t cur_job = 0xFFFFFFFFu;
+    for (uint64_t k = 0; k <= max_tiles; k++) {
         if (lane == 0) ring_wait(&ring->packed, (uint32_t)k + 1, err);
         __syncwarp();
         const uint32_t slot = (uint32_t)k & 1u;
         const uint64_t t = ring->tile[slot];
+        const uint32_t job = ring->job[slot];
         const uint32_t total = ring->total[slot], pos = ring->pos[slot];
-        if (t >= g.ntiles) break;
-        const uint64_t base = 8ull * g.T + lb_resolve(status, t, total, t == 0, 0, err);
-        const bool fits = base + total <= cap;
+        if (t == ZP_NONE) break;
+        if (job != cur_job) {
+            if (lane == 0) fetch(job, pj);
+            __syncwarp();
+            cur_job = job;
+        }
+        const ZGeom &g = pj->g;
+        const uint64_t base = 8ull * g.T + lb_resolve(pj->status, t, total, t == 0, 0, err);
+        const bool fits = base + total <= pj->cap;
         if (!fits) bad |= ZERR_CAPACITY;
         if (lane == 0) {
             ZTile z;
             zg_tile(&g, t, &z);
-            idx.tile_off[t] = base;
+            pj->idx.tile_off[t] = base;
             if (fits && z.has_head && z.seg < g.T) {
                 const uint64_t h = base - 8ull * g.T;
 #pragma unroll
-                for (int k8 = 0; k8 < 8; k8++) out[8ull * z.seg + k8] = (uint8_t)(h >> (8 * k8));
+                for (int k8 = 0; k8 < 8; k8++) pj->out[8ull * z.seg + k8] = (uint8_t)(h >> (8 * k8));
             }
-            if (t == g.ntiles - 1) *idx.size = base + total;
+            if (t == g.ntiles - 1) *pj->idx.size = base + total;
         }
-        if (fits) store_realign(out + base, ringb + pos, total, lane, 32);
+        if (fits) store_realign(pj->out + base, ringb + pos, total, lane, 32);
         __syncwarp();
         if (lane == 0) ring_set(&ring->placed, (uint32_t)k + 1);
     }
+}
+
+/* One thread: copy n bytes (a multiple of 16, both 16-byte aligned) one
+ * vector at a time, so a job copy holds few registers. */
+__device__ __forceinline__ void copy16(void *dst, const void *src, uint32_t n)
+{
+    uint4 *d = static_cast<uint4 *>(dst);
+    const uint4 *s = static_cast<const uint4 *>(src);
+#pragma unroll 1
+    for (uint32_t i = 0; i < n / 16u; i++) d[i] = s[i];
+}
+
+/* Thread 0: the job and local tile of batch ticket t. */
+__device__ __forceinline__ uint32_t batch_job(const ZBatch &b, uint64_t t, uint64_t *local)
+{
+    if (!b.jobs) {
+        *local = t;
+        return 0;
+    }
+    const uint32_t j = b.tile_job[t];
+    *local = t - b.job_tile0[j];
+    return j;
 }
 
 static inline unsigned persistent_grid(const void *fn, int threads, size_t smem, uint64_t ntiles)
