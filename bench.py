@@ -57,6 +57,7 @@ def parse():
                    help="skip the P-way reduction, batched and serving measurements")
     p.add_argument("--red-n", type=int, default=1 << 24, help="floats per rank chunk (reduction)")
     p.add_argument("--red-p", type=int, default=8, help="ranks (reduction)")
+    p.add_argument("--batch-pairs", type=int, default=2048, help="buffer pairs (batched)")
     return p.parse_args()
 
 
@@ -325,6 +326,137 @@ def reduction_bench(args, L, T, dev):
     return res
 
 
+def batched_bench(args, L, dev):
+    """4096 gradient-bucket-like buffers (2048 pairs of equal size, log-
+    uniform 4 KB - 16 MB, Laplace(0, 1e-3), 5 % constant, eb per pair from
+    {1e-3, 1e-4, 1e-5} * range, T = 1): compress all, then add each pair
+    homomorphically.  Batched: one persistent launch for all compressions
+    and one for all sums (launch shape from the autotuner), replayed from a
+    CUDA graph.  Against: one C-ABI call (memset + launch) per buffer, run
+    eagerly and also replayed from a CUDA graph."""
+    import ctypes
+    import types
+    import numpy as np
+    import torch
+    import zccl_gb300 as Z
+    lib = Z.lib()
+    npairs = args.batch_pairs
+    rng = np.random.default_rng(7)
+    sizes = np.exp(rng.uniform(np.log(1024), np.log(4 << 20), npairs)).astype(np.int64)
+    const = rng.random(npairs) < 0.05
+    eb_rel = rng.choice([1e-3, 1e-4, 1e-5], npairs)
+    T = 1
+    total = int(2 * sizes.sum())
+    data = torch.empty(total, dtype=torch.float32, device=dev)
+    g = torch.Generator(device=dev).manual_seed(7)
+    u = (torch.rand(total, generator=g, device=dev, dtype=torch.float32) - 0.5).clamp_(-0.4999999, 0.4999999)
+    data.copy_(-1e-3 * torch.sign(u) * torch.log1p(-2 * u.abs()))  # Laplace(0, 1e-3)
+    del u
+    off, xs = 0, []
+    for k in range(npairs):
+        n = int(sizes[k])
+        pair = [data[off: off + n], data[off + n: off + 2 * n]]
+        off += 2 * n
+        if const[k]:
+            pair[0].fill_(0.5)
+            pair[1].fill_(0.25)
+        xs.append(pair)
+    lo = [min(float(p[0].min()), float(p[1].min())) for p in xs]
+    hi = [max(float(p[0].max()), float(p[1].max())) for p in xs]
+    ebs = [float(np.float32(eb_rel[k] * max(hi[k] - lo[k], 1e-3))) for k in range(npairs)]
+    caps = [lib.zccl_gpu_max_stream_bytes(int(n), L, T) for n in sizes]
+    idxb = [lib.zccl_gpu_index_bytes(int(n), L, T) for n in sizes]
+    a16 = lambda v: (v + 255) // 256 * 256
+    sbytes = torch.empty(sum(3 * a16(c) for c in caps), dtype=torch.uint8, device=dev)
+    ibytes = torch.zeros(sum(3 * a16(i) for i in idxb), dtype=torch.uint8, device=dev)
+
+    def streams():
+        so = io = 0
+        out = []
+        for k in range(npairs):
+            trio = []
+            for _ in range(3):
+                d = Z.StreamDesc(sbytes.data_ptr() + so, caps[k], ibytes.data_ptr() + io, 0, 0)
+                trio.append(types.SimpleNamespace(desc=d, codec=types.SimpleNamespace(n=int(sizes[k]))))
+                so += a16(caps[k])
+                io += a16(idxb[k])
+            out.append(trio)
+        return out
+
+    st = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(st.cuda_stream)
+    S = streams()
+    bc = Z.Batch(Z.BATCH_COMPRESS, [(xs[k][r], ebs[k], T, S[k][r]) for k in range(npairs) for r in range(2)], L)
+    bh = Z.Batch(Z.BATCH_HOMADD, [([S[k][0], S[k][1]], T, S[k][2]) for k in range(npairs)], L)
+    grid_c, grid_h = bc.tune(), bh.tune()
+
+    def batched():
+        bc.run()
+        bh.run()
+
+    batched()
+    bc.check()
+    bh.check()
+    sum_b = [(S[k][2].desc.index, S[k][2].desc.bytes) for k in range(0, npairs, 97)]
+    digest_b = [bytes(sbytes[d - sbytes.data_ptr(): d - sbytes.data_ptr() + 64].cpu().numpy())
+                for _, d in sum_b]
+
+    ws = torch.zeros(max(lib.zccl_gpu_workspace_bytes(int(n), L, T) for n in sizes), dtype=torch.uint8,
+                     device=dev)
+    pairs_desc = [(Z.StreamDesc * 2)(S[k][0].desc, S[k][1].desc) for k in range(npairs)]
+
+    def per_buffer():
+        for k in range(npairs):
+            n = int(sizes[k])
+            for r in range(2):
+                lib.zccl_gpu_compress(ctypes.byref(S[k][r].desc), xs[k][r].data_ptr(), n, ebs[k], L, T,
+                                      ws.data_ptr(), sp)
+            pairs_desc[k][0], pairs_desc[k][1] = S[k][0].desc, S[k][1].desc
+            lib.zccl_gpu_homadd(ctypes.byref(S[k][2].desc), pairs_desc[k], 2, n, L, T, ws.data_ptr(), sp)
+
+    per_buffer()
+    lib.zccl_gpu_check(ws.data_ptr(), sp)
+    digest_p = [bytes(sbytes[d - sbytes.data_ptr(): d - sbytes.data_ptr() + 64].cpu().numpy())
+                for _, d in sum_b]
+    same = digest_p == digest_b
+    ms_eager = timed(per_buffer, 2, st)
+    gp = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(st)
+    with torch.cuda.graph(gp, stream=side, capture_error_mode="relaxed"):
+        sp_saved = sp
+        sp = ctypes.c_void_p(side.cuda_stream)
+        per_buffer()
+        sp = sp_saved
+    ms_graph_per = timed(gp.replay, 3, st)
+    gb = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(gb, stream=side, capture_error_mode="relaxed"):
+        bc.run(side)
+        bh.run(side)
+    ms_batch = timed(gb.replay, 5, st)
+    bc.check()
+    bh.check()
+    unc = 4 * total
+    res = {
+        "workload": f"{2 * npairs} buffers ({npairs} pairs of equal size), log-uniform 4 KB-16 MB float32, "
+                    f"Laplace(0,1e-3), 5% constant, eb in {{1e-3,1e-4,1e-5}}*range, L={L}, T={T}: compress "
+                    f"all + pairwise homomorphic add",
+        "uncompressed_bytes": unc,
+        "batched_graph_ms": round(ms_batch, 3),
+        "per_buffer_eager_ms": round(ms_eager, 3),
+        "per_buffer_graph_ms": round(ms_graph_per, 3),
+        "speedup_vs_per_buffer_eager": round(ms_eager / ms_batch, 2),
+        "speedup_vs_per_buffer_graph": round(ms_graph_per / ms_batch, 2),
+        "batched_GBps_uncompressed": round(unc / (ms_batch * 1e-3) / 1e9, 1),
+        "launches": {"batched": 2, "per_buffer": 3 * npairs},
+        "autotuned_grid": {"compress": grid_c, "homadd": grid_h},
+        "outputs_equal_sampled": same,
+    }
+    del data, xs, sbytes, ibytes, ws, gp, gb
+    torch.cuda.empty_cache()
+    return res
+
+
 def workload_config(args, n, T):
     return {"workload": f"{args.side}^3 float32 log-normal GRF ({4 * n >> 20} MiB): compress + "
                         f"decompress + 2-way homomorphic add, eb={args.eb_rel:g}*range",
@@ -448,6 +580,7 @@ def run_ours(args, rank, world, local_rank):
     if rank == 0 and not args.no_extras:
         del hs_a, hs_b, hs_s, hy
         extras["reduction"] = reduction_bench(args, L, T, dev)
+        extras["batched"] = batched_bench(args, L, dev)
 
     if rank == 0:
         line = {
