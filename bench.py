@@ -58,6 +58,9 @@ def parse():
     p.add_argument("--red-n", type=int, default=1 << 24, help="floats per rank chunk (reduction)")
     p.add_argument("--red-p", type=int, default=8, help="ranks (reduction)")
     p.add_argument("--batch-pairs", type=int, default=2048, help="buffer pairs (batched)")
+    p.add_argument("--serve-side", type=int, default=400, help="side of the serving field")
+    p.add_argument("--serve-slots", type=int, default=4)
+    p.add_argument("--serve-secs", type=float, default=0.4, help="arrival window per load point")
     return p.parse_args()
 
 
@@ -457,6 +460,88 @@ def batched_bench(args, L, dev):
     return res
 
 
+def serving_bench(args, L, dev):
+    """Poisson arrivals: 50 % compress, 30 % decompress, 20 % homomorphic
+    add of 2-8 resident streams; sizes log-uniform 64 KB - 256 MB of float32
+    cut from a log-normal GRF (as the 512^3 field, at 400^3); eb = 1e-4 *
+    range; 120 GB admission budget.  The peak is the throughput of a closed
+    burst; offered load sweeps 10 % - 120 % of it, reporting achieved
+    throughput and p50 / p99 latency per point."""
+    import numpy as np
+    import torch
+    from zccl_gb300.serve import COMPRESS, DECOMPRESS, HOMADD, Request, Server, percentile
+    field = make_field(args.serve_side, 5, dev)
+    nf = field.numel()
+    eb = float(np.float32(1e-4 * float(field.max() - field.min())))
+    rng = np.random.default_rng(11)
+    lo_n, hi_n = (64 << 10) // 4, min((256 << 20) // 4, nf)
+    draw_n = lambda: int(np.exp(rng.uniform(np.log(lo_n), np.log(hi_n))))
+    srv = Server(120 << 30, slots=args.serve_slots, L=L)
+    groups = []
+    for gi in range(8):
+        n = draw_n()
+        keys = []
+        for r in range(8):
+            off = int(rng.integers(0, nf - n + 1))
+            srv.put((gi, r), field[off: off + n], eb, 1)
+            keys.append((gi, r))
+        groups.append((n, keys))
+    rid = [0]
+
+    def make(t):
+        u = rng.random()
+        rid[0] += 1
+        if u < 0.5:
+            n = draw_n()
+            off = int(rng.integers(0, nf - n + 1))
+            return Request(t, rid[0], COMPRESS, x=field[off: off + n], eb=eb, T=1), 4 * n
+        n, keys = groups[int(rng.integers(0, len(groups)))]
+        if u < 0.8:
+            return Request(t, rid[0], DECOMPRESS, ins=[keys[int(rng.integers(0, 8))]]), 4 * n
+        P = int(rng.integers(2, 9))
+        return Request(t, rid[0], HOMADD, ins=[keys[int(k)] for k in rng.choice(8, P, replace=False)]), 4 * n * P
+
+    def serve(reqs):
+        srv.log = []
+        base = srv.now()
+        for q, _ in reqs:
+            q.arrival += base
+            srv.submit(q)
+        log = srv.run()
+        nbytes = sum(b for _, b in reqs)
+        span = max(q.done for q in log) - min(q.arrival for q in log)
+        lat = [1e3 * (q.done - q.arrival) for q in log]
+        return nbytes / span / 1e9, percentile(lat, 50), percentile(lat, 99), len(log)
+
+    serve([make(0.0) for _ in range(60)])  # warm-up: allocator, first launches
+    peak, b50, b99, _ = serve([make(0.0) for _ in range(400)])
+    mean_b = float(np.mean([make(0.0)[1] for _ in range(4000)]))
+    points = []
+    for load in (0.1, 0.25, 0.5, 0.75, 0.9, 1.0, 1.2):
+        lam = load * peak * 1e9 / mean_b  # requests per second
+        t, reqs = 0.0, []
+        while t < args.serve_secs and len(reqs) < 600:
+            t += float(rng.exponential(1.0 / lam))
+            reqs.append(make(t))
+        thr, p50, p99, cnt = serve(reqs)
+        points.append({"offered_frac": load, "offered_GBps": round(load * peak, 1), "achieved_GBps": round(thr, 1),
+                       "p50_ms": round(p50, 3), "p99_ms": round(p99, 3), "requests": cnt})
+    sustained = [p for p in points if p["achieved_GBps"] >= 0.9 * p["offered_GBps"]]
+    res = {
+        "workload": "Poisson arrivals, 50% compress / 30% decompress / 20% homomorphic add of 2-8 resident "
+                    f"streams, log-uniform 64 KB-256 MB float32 from a {args.serve_side}^3 log-normal GRF, "
+                    f"eb=1e-4*range, 120 GB budget, {args.serve_slots} slots, continuous batching",
+        "peak_GBps_closed_burst": round(peak, 1),
+        "burst_p50_ms": round(b50, 3), "burst_p99_ms": round(b99, 3),
+        "sweep": points,
+        "max_sustained": sustained[-1] if sustained else None,
+        "bytes_counted": "uncompressed input floats: 4n (compress, decompress), 4n*P (add)",
+    }
+    del field, srv
+    torch.cuda.empty_cache()
+    return res
+
+
 def workload_config(args, n, T):
     return {"workload": f"{args.side}^3 float32 log-normal GRF ({4 * n >> 20} MiB): compress + "
                         f"decompress + 2-way homomorphic add, eb={args.eb_rel:g}*range",
@@ -581,6 +666,7 @@ def run_ours(args, rank, world, local_rank):
         del hs_a, hs_b, hs_s, hy
         extras["reduction"] = reduction_bench(args, L, T, dev)
         extras["batched"] = batched_bench(args, L, dev)
+        extras["serving"] = serving_bench(args, L, dev)
 
     if rank == 0:
         line = {

@@ -1,0 +1,125 @@
+"""The request loop (zccl_gb300/serve.py): requests served concurrently and
+batched as they arrive give the same streams and floats as the same
+requests served alone, one at a time, with the plain calls; the budget
+holds requests back; latency percentiles."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from zccl_gb300.serve import percentile
+
+
+def test_percentile():
+    assert percentile([], 50) is None
+    assert percentile([3.0], 99) == 3.0
+    v = list(range(1, 101))
+    assert percentile(v, 50) in (50, 51) and percentile(v, 99) == 99
+
+
+@pytest.fixture(scope="module")
+def torch():
+    t = pytest.importorskip("torch")
+    if not t.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return t
+
+
+def build(torch, budget, slots, batching, seed=0):
+    from zccl_gb300.serve import COMPRESS, DECOMPRESS, HOMADD, Request, Server
+    rng = np.random.default_rng(seed)
+    base = torch.from_numpy(np.cumsum(rng.normal(0, 1, 1 << 20)).astype(np.float32)).cuda()
+    eb = float(np.float32(1e-4 * float(base.max() - base.min())))
+    srv = Server(budget, slots=slots, batching=batching, keep_results=True)
+    groups = []
+    for gi, n in enumerate([777, 20000, 100003]):
+        T = 1 if gi == 0 else 3
+        keys = []
+        for r in range(5):
+            off = int(rng.integers(0, base.numel() - n))
+            srv.put((gi, r), base[off: off + n].clone(), eb, T)
+            keys.append((gi, r))
+        groups.append(keys)
+    reqs = []
+    for i in range(60):
+        u = rng.random()
+        t = float(rng.uniform(0, 0.004))
+        if u < 0.5:
+            n = int(np.exp(rng.uniform(np.log(50), np.log(300000))))
+            off = int(rng.integers(0, base.numel() - n))
+            reqs.append(Request(t, i, COMPRESS, x=base[off: off + n].clone(), eb=eb, T=int(rng.choice([1, 2]))))
+        elif u < 0.8:
+            g = groups[int(rng.integers(0, 3))]
+            reqs.append(Request(t, i, DECOMPRESS, ins=[g[int(rng.integers(0, 5))]]))
+        else:
+            g = groups[int(rng.integers(0, 3))]
+            P = int(rng.integers(2, 6))
+            reqs.append(Request(t, i, HOMADD, ins=[g[int(k)] for k in rng.choice(len(g), P, replace=False)]))
+    return srv, reqs
+
+
+def alone(torch, srv, q):
+    """The request served by itself with the plain calls."""
+    import zccl_gb300 as Z
+    from zccl_gb300.serve import COMPRESS, DECOMPRESS
+    if q.kind == COMPRESS:
+        c = Z.Codec(q.x.numel(), 32, q.T)
+        s = c.compress(q.x, q.eb)
+        c.check()
+        return s.tobytes()
+    rs = [srv.store[k] for k in q.ins]
+    c = Z.Codec(rs[0].n, 32, rs[0].T)
+    ins = []
+    for r in rs:
+        d = Z.DeviceStream(c, data=r.buf)
+        d.index = r.index
+        d.desc = Z.StreamDesc(r.buf.data_ptr(), r.buf.numel(), r.index.data_ptr(), r.desc.indexed,
+                              r.desc.qprev_valid)
+        ins.append(d)
+    if q.kind == DECOMPRESS:
+        y = c.decompress(ins[0], rs[0].eb)
+        c.check()
+        return y.cpu().numpy().view(np.uint32).tobytes()
+    s = c.homadd(ins)
+    c.check()
+    return s.tobytes()
+
+
+def served(q):
+    from zccl_gb300 import lib
+    from zccl_gb300.serve import DECOMPRESS
+    if q.kind == DECOMPRESS:
+        return q.result.cpu().numpy().view(np.uint32).tobytes()
+    r = q.result
+    size = ctypes.c_size_t(0)
+    assert lib().zccl_gpu_stream_size(ctypes.byref(r.desc), r.n, 32, r.T, ctypes.byref(size), None) == 0
+    return r.buf[: size.value].cpu().numpy().tobytes()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("batching,slots", [(True, 3), (False, 2)])
+def test_results_same_alone_and_in_the_mix(torch, batching, slots):
+    srv, reqs = build(torch, budget=1 << 30, slots=slots, batching=batching)
+    for q in reqs:
+        srv.submit(q)
+    log = srv.run()
+    assert len(log) == len(reqs) and srv.in_use == 0
+    for q in reqs:
+        assert q.done is not None and q.done >= q.arrival
+        assert served(q) == alone(torch, srv, q), (q.kind, q.rid)
+    lat = [q.done - q.arrival for q in reqs]
+    assert percentile(lat, 50) <= percentile(lat, 99)
+
+
+@pytest.mark.gpu
+def test_budget_holds_requests_back(torch):
+    # a budget for a few requests at a time: still every request completes, in full
+    srv, reqs = build(torch, budget=4 << 20, slots=3, batching=True, seed=1)
+    for q in reqs:
+        srv.submit(q)
+    log = srv.run()
+    assert len(log) == len(reqs) and srv.in_use == 0
+    for q in reqs:
+        assert served(q) == alone(torch, srv, q), (q.kind, q.rid)
