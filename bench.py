@@ -203,6 +203,17 @@ def cpu_codec_rate(x, y, eb, L, T, reps=1):
     return 3 * 4 * n / best / 1e9, best
 
 
+def max_over_ranks(v: float, world: int, device) -> float:
+    """The largest of every rank's v (the whole job is as slow as its
+    slowest rank); v itself on one rank."""
+    if world <= 1:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args, rank, world):
     """--impl reference: the reference codec's CPU path on the host cores."""
     import numpy as np
@@ -616,10 +627,7 @@ def run_ours(args, rank, world, local_rank):
         torch.distributed.barrier()
     codec.check()
     ms = t_start.elapsed_time(t_end) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = t.item()
+    ms = max_over_ranks(ms, world, dev)
     op_ms = [statistics.mean(e[i].elapsed_time(e[i + 1]) for e in evs) for i in range(3)]
     value = world * 3 * 4 * n / (ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
