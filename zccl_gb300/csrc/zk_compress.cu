@@ -33,16 +33,16 @@
 
 namespace {
 
-/* Thread 0: claim the next tile in ticket order, copy its job into `slot`
- * and start the TMA copy of its floats (and the element before them) into
- * `in`.  The tile within its job lands in *s_tile (ZP_NONE when all are
+/* Thread 0: ticket t (taken a little earlier, so that the atomic's latency
+ * overlaps other work) becomes the claimed tile: its job is copied into
+ * `slot` and the TMA copy of its floats (and the element before them) into
+ * `in` starts.  The tile within its job lands in *s_tile (ZP_NONE when all are
  * taken), the job in *s_job; the caller synchronises before reading them. */
-__device__ __forceinline__ void claim_tile(const CompressArgs &a, uint8_t *in, uint64_t *bar,
+__device__ __forceinline__ void claim_tile(const CompressArgs &a, uint64_t t, uint8_t *in, uint64_t *bar,
                                            uint64_t *s_tile, uint32_t *s_job, uint32_t *s_amax,
                                            CompressJob *slot)
 {
     if (threadIdx.x != 0) return;
-    const uint64_t t = atomicAdd(a.w.ticket, 1u);
     *s_amax = 0;
     const uint64_t total = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
     if (t >= total) {
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
     /* the compute warps */
     const uint32_t R = zg_ring_bytes(L, NC);
     uint32_t pos_prev = 0, end_prev = 0; /* thread 0: the previous tile's place in the ring */
-    claim_tile(a, in, bar_tma, s_tile, s_job, s_amax, &cj[0]);
+    if (tid == 0) claim_tile(a, atomicAdd(a.w.ticket, 1u), in, bar_tma, s_tile, s_job, s_amax, &cj[0]);
     named_sync(1, NC);
     uint64_t tile = *s_tile;
     uint32_t job = *s_job;
@@ -247,6 +247,8 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
         const uint32_t off = grp_excl_scan(size, wsum, &total, NC, 1);
         total += headb;
         if (warp == 0) lb_publish(J.status, tile, total, tile == 0, 0);
+        uint32_t ticket = 0; /* the next tile's, taken now and used after the ring reservation */
+        if (tid == 0) ticket = atomicAdd(a.w.ticket, 1u);
         const int32_t qprev0 = fastq ? quantize_fast(xprev0, J.inv) : quantize(xprev0, J.inv, bad);
         if (own) J.idx.widths[z.gblk0 + tid] = (uint8_t)b;
         if (tid == 0) J.idx.tile_qprev[tile] = qprev0;
@@ -258,7 +260,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
          *    while holding a claimed tile whose size is not yet published. */
         if (tid == 0) {
             *s_pos = ring_reserve(ring, it, zg_ring_need(total), R, pos_prev, end_prev, a.w.err);
-            if (FAST) claim_tile(a, in, bar_tma, s_tile, s_job, s_amax, &cj[(it + 1) & 1u]);
+            if (FAST) claim_tile(a, ticket, in, bar_tma, s_tile, s_job, s_amax, &cj[(it + 1) & 1u]);
         }
         named_sync(1, NC);
         const uint32_t pos = *s_pos;
@@ -289,7 +291,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
                 });
             }
             named_sync(1, NC); /* the rows have been read for the last time */
-            if (tid == 0) claim_tile(a, in, bar_tma, s_tile, s_job, s_amax, &cj[(it + 1) & 1u]);
+            if (tid == 0) claim_tile(a, ticket, in, bar_tma, s_tile, s_job, s_amax, &cj[(it + 1) & 1u]);
         }
         named_sync(1, NC); /* the packed tile is complete; the claimed index is visible */
         if (tid == 0) ring_publish(ring, it, tile, job, total, pos);

@@ -48,11 +48,13 @@ __device__ __forceinline__ BlockSlot stage_input(const HomAddJob &J, uint64_t t,
         }
         size = zg_block_bytes(sl.b, sl.n);
     }
+    uint64_t base0 = 0;
+    if (threadIdx.x == 0) base0 = in.tile_off[t]; /* on its way during the scan */
     uint32_t total;
     sl.off = grp_excl_scan(size, wsum, &total, J.g.TB, 1);
     total += z.has_head ? 4u : 0u;
     if (threadIdx.x == 0) {
-        uint64_t base = in.tile_off[t];
+        uint64_t base = base0;
         uint32_t nload = total;
         /* overflow-safe: base comes from the index and is not trusted */
         if (base > in.avail || total > in.avail - base) {
@@ -75,14 +77,14 @@ __device__ __forceinline__ void copy_job(HomAddJob *dst, const HomAddJob *src)
     copy16(&dst->P, &src->P, (uint32_t)(sizeof(HomAddJob) - offsetof(HomAddJob, P)));
 }
 
-/* Thread 0: claim the next tile and copy its job into `slot`; the tile
- * within its job lands in *s_tile (ZP_NONE when all are taken), the job in
- * *s_job.  The caller synchronises before reading them. */
-__device__ __forceinline__ void claim_sum(const HomAddArgs &a, uint64_t *s_tile, uint32_t *s_job,
-                                          HomAddJob *slot)
+/* Thread 0: ticket t (taken a little earlier, so that the atomic's latency
+ * overlaps other work) becomes the claimed tile: its job is copied into
+ * `slot`, the tile within its job lands in *s_tile (ZP_NONE when all are
+ * taken), the job in *s_job.  The caller synchronises before reading them. */
+__device__ __forceinline__ void take_ticket(const HomAddArgs &a, uint64_t t, uint64_t *s_tile, uint32_t *s_job,
+                                            HomAddJob *slot)
 {
     if (threadIdx.x != 0) return;
-    const uint64_t t = atomicAdd(a.w.ticket, 1u);
     const uint64_t total = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
     if (t >= total) {
         *s_tile = ZP_NONE;
@@ -156,7 +158,7 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const __grid_constant__ HomAd
     uint32_t ld = 0; /* index of the current copy in the two-buffer stream */
     const uint32_t R = zg_ring_bytes(L, NC);
     uint32_t pos_prev = 0, end_prev = 0; /* thread 0: the previous sum's place in the ring */
-    claim_sum(a, s_tile, s_job, &hj[0]);
+    if (tid == 0) take_ticket(a, atomicAdd(a.w.ticket, 1u), s_tile, s_job, &hj[0]);
     named_sync(1, NC);
     uint64_t tile = *s_tile;
     uint32_t job = *s_job;
@@ -230,6 +232,10 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const __grid_constant__ HomAd
              * after that round's scan has synchronised every compute thread */
         }
 
+        /* the next tile's ticket, taken now and used after the size scan */
+        uint32_t ticket = 0;
+        if (tid == 0) ticket = atomicAdd(a.w.ticket, 1u);
+
         /* branch-case counters of the two-input add (ZCCLd_float.c:2175-2764) */
         if (a.cases && P == 2) {
             const uint32_t c0 = __popc(__ballot_sync(0xffffffffu, own && nzmask == 0u));
@@ -275,7 +281,7 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const __grid_constant__ HomAd
          * the placer to write out an earlier one), claim the next tile and
          * start its first input's copy, and pack this sum while it arrives */
         if (tid == 0) *s_pos = ring_reserve(ring, it, zg_ring_need(total), R, pos_prev, end_prev, a.w.err);
-        claim_sum(a, s_tile, s_job, &hj[(it + 1) & 1u]);
+        take_ticket(a, ticket, s_tile, s_job, &hj[(it + 1) & 1u]);
         named_sync(1, NC);
         const uint64_t next = *s_tile;
         const uint32_t next_job = *s_job;
