@@ -534,6 +534,39 @@ __device__ __forceinline__ uint32_t grp_excl_scan(uint32_t v, uint32_t *wsum, ui
     return r;
 }
 
+/* Two exclusive scans at once on the same barriers: v0 with scratch ws0,
+ * v1 with ws1 (33 words each). */
+__device__ __forceinline__ void grp_excl_scan2(uint32_t v0, uint32_t v1, uint32_t *ws0, uint32_t *ws1,
+                                               uint32_t &r0, uint32_t &r1, uint32_t &t0, uint32_t &t1,
+                                               uint32_t n, uint32_t id)
+{
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = n >> 5;
+    const uint32_t i0 = warp_incl_scan(v0), i1 = warp_incl_scan(v1);
+    if (lane == 31) {
+        ws0[warp] = i0;
+        ws1[warp] = i1;
+    }
+    named_sync(id, n);
+    if (warp == 0) {
+        const uint32_t a = lane < nw ? ws0[lane] : 0u, b = lane < nw ? ws1[lane] : 0u;
+        const uint32_t ai = warp_incl_scan(a), bi = warp_incl_scan(b);
+        if (lane < nw) {
+            ws0[lane] = ai - a;
+            ws1[lane] = bi - b;
+        }
+        if (lane == 31) {
+            ws0[32] = ai;
+            ws1[32] = bi;
+        }
+    }
+    named_sync(id, n);
+    r0 = ws0[warp] + i0 - v0;
+    r1 = ws1[warp] + i1 - v1;
+    t0 = ws0[32];
+    t1 = ws1[32];
+    named_sync(id, n);
+}
+
 /* The same over the whole CTA. */
 __device__ __forceinline__ uint32_t cta_excl_scan(uint32_t v, uint32_t *wsum, uint32_t *total)
 {

@@ -28,6 +28,22 @@ struct BlockSlot {
     uint32_t b, n, off;
 };
 
+/* Thread 0: the TMA copy of `total` bytes of an input tile at byte `base`
+ * (from the index, so checked against the readable bytes) into buf. */
+__device__ __forceinline__ void issue_input(const HomInput &in, uint64_t base, uint32_t total, uint8_t *buf,
+                                            uint64_t *bar, uint64_t *s_base, uint32_t &bad)
+{
+    uint32_t nload = total;
+    /* overflow-safe: base comes from the index and is not trusted */
+    if (base > in.avail || total > in.avail - base) {
+        bad |= ZERR_BOUNDS;
+        nload = base < in.avail ? (uint32_t)min((uint64_t)total, in.avail - base) : 0u;
+        if (base > in.avail) base = 0;
+    }
+    *s_base = base;
+    tma_load_superset(buf, in.bytes + base, nload, bar);
+}
+
 /* The compute threads: sizes of input p's blocks in tile t, their offsets,
  * and (thread 0) the TMA copy of those bytes into buf. */
 __device__ __forceinline__ BlockSlot stage_input(const HomAddJob &J, uint64_t t, uint32_t p,
@@ -52,19 +68,7 @@ __device__ __forceinline__ BlockSlot stage_input(const HomAddJob &J, uint64_t t,
     if (threadIdx.x == 0) base0 = in.tile_off[t]; /* on its way during the scan */
     uint32_t total;
     sl.off = grp_excl_scan(size, wsum, &total, J.g.TB, 1);
-    total += z.has_head ? 4u : 0u;
-    if (threadIdx.x == 0) {
-        uint64_t base = base0;
-        uint32_t nload = total;
-        /* overflow-safe: base comes from the index and is not trusted */
-        if (base > in.avail || total > in.avail - base) {
-            bad |= ZERR_BOUNDS;
-            nload = base < in.avail ? (uint32_t)min((uint64_t)total, in.avail - base) : 0u;
-            if (base > in.avail) base = 0;
-        }
-        *s_base = base;
-        tma_load_superset(buf, in.bytes + base, nload, bar);
-    }
+    if (threadIdx.x == 0) issue_input(in, base0, total + (z.has_head ? 4u : 0u), buf, bar, s_base, bad);
     return sl;
 }
 
@@ -154,6 +158,8 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const __grid_constant__ HomAd
     /* the compute warps.  Tiles are claimed one at a time when these warps
      * are ready for them, and they never wait while holding a claimed tile
      * whose size is not yet published. */
+    uint32_t *ws1 = reinterpret_cast<uint32_t *>(smem + 320); /* [33] second scan scratch */
+    uint8_t *const buf0 = smem + a.sm.in0, *const buf1 = smem + a.sm.in1;
     uint32_t acc[32];
     uint32_t ld = 0; /* index of the current copy in the two-buffer stream */
     const uint32_t R = zg_ring_bytes(L, NC);
@@ -191,8 +197,10 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const __grid_constant__ HomAd
         uint32_t hsum = 0, qsum = 0, nzmask = 0;
         const uint32_t headb = z.has_head ? 4u : 0u;
 
+        uint32_t ticket = 0; /* the next tile's, taken before the last input and used after it */
         for (uint32_t p = 0; p < P; p++, ld++) {
             const uint32_t cb = ld & 1u;
+            if (p + 1 == P && tid == 0) ticket = atomicAdd(a.w.ticket, 1u);
             /* the next input's copy runs while this one is added */
             BlockSlot nxt = {0, 0, 0};
             if (p + 1 < P)
@@ -232,9 +240,24 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const __grid_constant__ HomAd
              * after that round's scan has synchronised every compute thread */
         }
 
-        /* the next tile's ticket, taken now and used after the size scan */
-        uint32_t ticket = 0;
-        if (tid == 0) ticket = atomicAdd(a.w.ticket, 1u);
+        /* the claimed next tile: its first input's widths and offset load
+         * while this sum's widths are found */
+        HomAddJob &Jn = hj[(it + 1) & 1u];
+        take_ticket(a, ticket, s_tile, s_job, &Jn);
+        named_sync(1, NC);
+        const uint64_t next = *s_tile;
+        const uint32_t next_job = *s_job;
+        ZTile zn;
+        uint32_t wn = 0, nn = 0;
+        uint64_t basen = 0;
+        if (next != ZP_NONE) {
+            zg_tile(&Jn.g, next, &zn);
+            if (tid < zn.nblk) {
+                nn = zg_block_len(zn.seg_len, Jn.g.L, zn.blk0 + tid);
+                wn = Jn.in[0].widths[zn.gblk0 + tid];
+            }
+            if (tid == 0) basen = Jn.in[0].tile_off[next];
+        }
 
         /* branch-case counters of the two-input add (ZCCLd_float.c:2175-2764) */
         if (a.cases && P == 2) {
@@ -270,25 +293,34 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const __grid_constant__ HomAd
             b = width_of(mx, a.wt);
             size = zg_block_bytes(b, n);
         }
-        uint32_t total;
-        const uint32_t off = grp_excl_scan(size, wsum, &total, NC, 1);
+        /* one scan for this sum's block offsets and the next tile's first input's */
+        uint32_t sizen = 0;
+        if (wn > 32) {
+            bad |= ZERR_CORRUPT;
+            wn = 0;
+        }
+        if (next != ZP_NONE && tid < zn.nblk) sizen = zg_block_bytes(wn, nn);
+        uint32_t total, off, offn, totaln;
+        grp_excl_scan2(size, sizen, wsum, ws1, off, offn, total, totaln, NC, 1);
         total += headb;
+        if (next != ZP_NONE) { /* every input of this tile is decoded: the buffer is free */
+            if (tid == 0)
+                issue_input(Jn.in[0], basen, totaln + (zn.has_head ? 4u : 0u), ld & 1u ? buf1 : buf0,
+                            &bar[ld & 1u], &s_base[ld & 1u], bad);
+            cur.b = wn;
+            cur.n = nn;
+            cur.off = offn;
+        }
         if (warp == 0) lb_publish(J.status, tile, total, tile == 0, 0);
         if (own) J.idx.widths[z.gblk0 + tid] = (uint8_t)b;
         if (tid == 0 && J.qprev_valid) J.idx.tile_qprev[tile] = (int32_t)qsum;
 
         /* take room for the packed sum in the ring (waiting, if need be, for
-         * the placer to write out an earlier one), claim the next tile and
-         * start its first input's copy, and pack this sum while it arrives */
+         * the placer to write out an earlier one) and pack this sum while
+         * the next tile's first input arrives */
         if (tid == 0) *s_pos = ring_reserve(ring, it, zg_ring_need(total), R, pos_prev, end_prev, a.w.err);
-        take_ticket(a, ticket, s_tile, s_job, &hj[(it + 1) & 1u]);
         named_sync(1, NC);
-        const uint64_t next = *s_tile;
-        const uint32_t next_job = *s_job;
         const uint32_t pos = *s_pos;
-        if (next != ZP_NONE)
-            cur = stage_input(hj[(it + 1) & 1u], next, 0, smem + (ld & 1u ? a.sm.in1 : a.sm.in0), &bar[ld & 1u],
-                              wsum, &s_base[ld & 1u], bad);
         uint8_t *pk = outs + pos;
         const uint32_t pk_sa = smem_u32(pk);
         smem_zero(pk, total + 8, tid, NC);
