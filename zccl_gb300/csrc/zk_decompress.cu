@@ -54,6 +54,25 @@ __device__ __forceinline__ TileIdx load_idx(const DecompressArgs &a, uint64_t t)
     return r;
 }
 
+/* Thread 0: the TMA copy of a tile's `total` bytes at the index's byte
+ * offset (checked against the readable bytes) into buf; its offset and
+ * starting value into *s_base and *s_q0. */
+__device__ __forceinline__ void issue_tile(const DecompressArgs &a, const TileIdx &ix, uint32_t total, uint8_t *buf,
+                                           uint64_t *bar, uint64_t *s_base, uint32_t *s_q0, uint32_t &bad)
+{
+    uint64_t base = ix.base;
+    uint32_t nload = total;
+    /* overflow-safe: base comes from the index and is not trusted */
+    if (base > a.avail || total > a.avail - base) {
+        bad |= ZERR_BOUNDS;
+        nload = base < a.avail ? (uint32_t)min((uint64_t)total, a.avail - base) : 0u;
+        if (base > a.avail) base = 0;
+    }
+    *s_base = base;
+    *s_q0 = ix.q0;
+    tma_load_superset(buf, a.in + base, nload, bar);
+}
+
 /* All threads: sizes of tile t's blocks, their offsets, and (thread 0) the
  * TMA copy of the tile's bytes into buf.  Returns the slot of this thread's
  * block; the tile's byte offset lands in *s_base, its starting value in
@@ -77,20 +96,7 @@ __device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, uint64_
     }
     uint32_t total;
     sl.off = cta_excl_scan(size, wsum, &total);
-    total += z.has_head ? 4u : 0u;
-    if (threadIdx.x == 0) {
-        uint64_t base = ix.base;
-        uint32_t nload = total;
-        /* overflow-safe: base comes from the index and is not trusted */
-        if (base > a.avail || total > a.avail - base) {
-            bad |= ZERR_BOUNDS;
-            nload = base < a.avail ? (uint32_t)min((uint64_t)total, a.avail - base) : 0u;
-            if (base > a.avail) base = 0;
-        }
-        *s_base = base;
-        *s_q0 = ix.q0;
-        tma_load_superset(buf, a.in + base, nload, bar);
-    }
+    if (threadIdx.x == 0) issue_tile(a, ix, total + (z.has_head ? 4u : 0u), buf, bar, s_base, s_q0, bad);
     return sl;
 }
 
@@ -109,6 +115,7 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a)
     uint64_t *s_base = reinterpret_cast<uint64_t *>(smem + 192); /* [2] */
     uint32_t *s_q0 = reinterpret_cast<uint32_t *>(smem + 208);   /* [2] */
     uint64_t *rec = reinterpret_cast<uint64_t *>(smem + 256);
+    uint32_t *ws1 = reinterpret_cast<uint32_t *>(smem + 320); /* [33] second scan scratch */
     float *rows = reinterpret_cast<float *>(smem + a.sm.rows);
 
     const ZGeom &g = a.g;
@@ -148,10 +155,9 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a)
             ix = load_idx(a, tnext);
         }
         BlockSlot nxt = {0, 0, 0};
-        if (tnext < g.ntiles)
+        if (ORDERED && tnext < g.ntiles)
             nxt = stage_tile(a, tnext, ix, smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u], wsum,
                              &s_base[cb ^ 1u], &s_q0[cb ^ 1u], bad);
-        if (!ORDERED) ix = load_idx(a, tnext + gridDim.x);
 
         /* 2. unpack this tile's deltas */
         mbar_wait(&bar[cb], (it >> 1) & 1u, a.w.err);
@@ -179,9 +185,34 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a)
             decode_any(sw, o, b, n, [&](uint32_t, uint32_t v) { bsum += v; });
         }
 
-        /* 3. starting value of every block */
-        uint32_t tsum;
-        const uint32_t pre = cta_excl_scan(bsum, wsum, &tsum);
+        /* 3. starting value of every block.  In index order the next tile's
+         *    block offsets come from the same scan (its widths arrived a tile
+         *    ago), and its copy starts right after, into the other buffer. */
+        uint32_t tsum, pre;
+        if (ORDERED) {
+            pre = cta_excl_scan(bsum, wsum, &tsum);
+        } else {
+            ZTile zn;
+            uint32_t sizen = 0;
+            if (tnext < g.ntiles) {
+                zg_tile(&g, tnext, &zn);
+                if (tid < zn.nblk) {
+                    nxt.n = zg_block_len(zn.seg_len, L, zn.blk0 + tid);
+                    nxt.b = ix.b;
+                    if (nxt.b > 32) {
+                        bad |= ZERR_CORRUPT;
+                        nxt.b = 0;
+                    }
+                    sizen = zg_block_bytes(nxt.b, nxt.n);
+                }
+            }
+            uint32_t totn;
+            grp_excl_scan2(bsum, sizen, wsum, ws1, pre, nxt.off, tsum, totn, blockDim.x, 0);
+            if (tnext < g.ntiles && tid == 0)
+                issue_tile(a, ix, totn + (zn.has_head ? 4u : 0u), smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u],
+                           &s_base[cb ^ 1u], &s_q0[cb ^ 1u], bad);
+            ix = load_idx(a, tnext + gridDim.x);
+        }
         if (a.qprev_valid) {
             if (tid == 0) bc[2] = z.has_head ? (uint32_t)head : s_q0[cb];
         } else {
