@@ -434,6 +434,33 @@ __device__ __forceinline__ void bulk_g2s(void *sdst, const void *gsrc, uint32_t 
         : "memory");
 }
 
+/* Shared stores by address (a swizzled layout computes its own). */
+__device__ __forceinline__ void st_shared_v4(uint32_t sa, float x, float y, float z, float w)
+{
+    asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(sa), "f"(x), "f"(y), "f"(z), "f"(w)
+                 : "memory");
+}
+__device__ __forceinline__ void st_shared_f32(uint32_t sa, float x)
+{
+    asm volatile("st.shared.f32 [%0], %1;" ::"r"(sa), "f"(x) : "memory");
+}
+
+/* TMA tensor store of the box at (c0, c1) of a 2-D map from shared memory,
+ * in the issuing thread's bulk group.  The writers of the shared box run
+ * fence_proxy_async_smem() and a barrier before it. */
+__device__ __forceinline__ void tma_store_2d(const void *map, uint32_t sa, int32_t c0, int32_t c1)
+{
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+                     (uint64_t)(uintptr_t)map),
+                 "r"(sa), "r"(c0), "r"(c1)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+/* The issuing thread's bulk stores have read their shared source (the
+ * buffer may be written again) / have completed. */
+__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 /* Thread 0 only: TMA bulk copy of the 16-byte-aligned superset
  * [floor16(g), ceil16(g + nbytes)) into the 16-byte-aligned buffer s, arming
  * the barrier with its byte count.  The superset only adds bytes of 16-byte

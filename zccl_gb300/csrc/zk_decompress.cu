@@ -22,6 +22,12 @@
  *   4. x = (float)q * eb (ZCCLd_float.c:624) into padded rows, written out
  *      row by row with coalesced stores.
  */
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cstring>
+#include <mutex>
+
 #include "zkern.cuh"
 
 namespace {
@@ -106,7 +112,7 @@ __device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, uint64_
  * c + 2 grid, ..., with the index entries of the tile after next already
  * loading. */
 template <bool FAST, bool ORDERED>
-__global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a)
+__global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, const __grid_constant__ CUtensorMap ymap)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem); /* [2] */
@@ -122,6 +128,15 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a)
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, nw = blockDim.x >> 5;
     const uint32_t L = g.L, stride = zg_row_stride(L);
     uint32_t bad = 0;
+    /* Full tiles of L = 32 whose first element minus one starts a 128-byte
+     * row of y leave by one TMA tensor store: 256 rows of 32 floats, the
+     * element before the tile first, in a 1024-byte-aligned box with the
+     * 128-byte swizzle (16-byte chunk k of row r at chunk k ^ (r & 7)), so
+     * that each thread's vector stores of its row meet no bank conflict. */
+    const uint32_t rows_sa = smem_u32(rows);
+    const uint32_t box_sa = (rows_sa + 1023u) & ~1023u;
+    const bool rows_ok = FAST && a.rows_map && L == 32 && g.TB == 256 && blockDim.x == 256 &&
+                         box_sa + 32768u <= rows_sa + g.TB * stride * 4u;
     /* The index walk ran to completion before this launch, so every CTA sees
      * the same word: after a failed walk no CTA touches the stream and no
      * CTA waits on another. */
@@ -224,12 +239,41 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a)
                 a.idx.tile_qprev[tile] = (int32_t)(uint32_t)q0;
             }
         }
+        if (tid == 0) bulk_wait_read0(); /* the previous box has left the rows */
         __syncthreads();
         const uint32_t q0 = (uint32_t)bc[2];
+        const bool box = rows_ok && z.nblk == 256 && z.e_end - z.e_first == 8192 && ((z.e_first - 1) & 31) == 0;
 
         /* 4. values into rows, then out */
         float *row = rows + tid * stride;
-        if (full) {
+        if (box) { /* every block is full: element e_first + 32 tid + j is box float 1 + 32 tid + j */
+            uint32_t q = q0 + pre;
+            float v[32];
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+                q += d[j];
+                v[j] = __fmul_rn(__int2float_rn((int32_t)q), a.eb);
+            }
+            /* the float before this block: the previous thread's last, or for
+             * thread 0 the value before the tile (the head or the previous
+             * tile's last element, stored there too with the same bits) */
+            float prev = __shfl_up_sync(0xffffffffu, v[31], 1);
+            if (tid == 0) prev = __fmul_rn(__int2float_rn((int32_t)q0), a.eb);
+            const uint32_t rb = box_sa + tid * 128u, x4 = (tid & 7u) << 4;
+            if (lane != 0 || tid == 0) {
+                st_shared_v4(rb | x4, prev, v[0], v[1], v[2]);
+            } else { /* chunk 0's first float is the previous warp's to write */
+                st_shared_f32((rb | x4) + 4u, v[0]);
+                st_shared_f32((rb | x4) + 8u, v[1]);
+                st_shared_f32((rb | x4) + 12u, v[2]);
+            }
+#pragma unroll
+            for (uint32_t k = 1; k < 8; k++)
+                st_shared_v4(rb | ((k << 4) ^ x4), v[4 * k - 1], v[4 * k], v[4 * k + 1], v[4 * k + 2]);
+            if (lane == 31 && tid != 255) st_shared_f32(rb + 128u, v[31]); /* row tid + 1, chunk 0 at 0 */
+            if (tid == 255) a.y[z.e_end - 1] = v[31];                      /* past the box */
+            fence_proxy_async_smem();
+        } else if (full) {
             uint32_t q = q0 + pre;
 #pragma unroll
             for (int j = 0; j < 32; j++) {
@@ -245,7 +289,9 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a)
         }
         if (z.has_head && tid == 0) a.y[z.seg_start] = __fmul_rn(__int2float_rn(head), a.eb);
         __syncthreads();
-        if (FAST && L == 32 && z.nblk == g.TB && z.e_end - z.e_first == 32ull * g.TB) {
+        if (box) {
+            if (tid == 0) tma_store_2d(&ymap, box_sa, 0, (int32_t)((z.e_first - 1) >> 5));
+        } else if (FAST && L == 32 && z.nblk == g.TB && z.e_end - z.e_first == 32ull * g.TB) {
             /* a full tile: 32-float rows, unrolled so that many stores are
              * in flight per warp */
             float *dst = a.y + z.e_first + lane;
@@ -266,7 +312,44 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a)
         tile = tnext;
         if (!ORDERED) tnext += gridDim.x;
     }
+    if (tid == 0) bulk_wait0();
     if (bad) atomicOr(a.w.err, bad);
+}
+
+/* cuTensorMapEncodeTiled from the driver, looked up once. */
+PFN_cuTensorMapEncodeTiled_v12000 encode_tiled()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+/* y[0, n) as rows of 32 floats, boxes of 256 rows, 128-byte swizzle.
+ * False (and the kernel stores rows itself) when y is not 16-byte aligned,
+ * holds fewer than one box, or the encoder is unavailable. */
+bool rows_map(CUtensorMap *map, float *y, uint64_t n)
+{
+    const uint64_t nrows = n / 32u;
+    if (((uintptr_t)y & 15u) || nrows < 256u || nrows > 0x7fffffffull) return false;
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_tiled();
+    if (!enc) return false;
+    const cuuint64_t dim[2] = {32u, nrows};
+    const cuuint64_t stride[1] = {128u};
+    const cuuint32_t box[2] = {32u, 256u};
+    const cuuint32_t estride[2] = {1u, 1u};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, y, dim, stride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 } // namespace
@@ -281,6 +364,10 @@ cudaError_t launch_decompress(const DecompressArgs &a, cudaStream_t st)
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
     if (e != cudaSuccess) return e;
     unsigned grid = persistent_grid(fn, a.g.TB, a.sm.total, a.g.ntiles);
-    void *args[] = {const_cast<DecompressArgs *>(&a)};
+    DecompressArgs b = a;
+    alignas(64) CUtensorMap map;
+    memset(&map, 0, sizeof map);
+    b.rows_map = fast && rows_map(&map, a.y, a.g.n);
+    void *args[] = {&b, &map};
     return cudaLaunchKernel(fn, dim3(grid), dim3(a.g.TB), args, a.sm.total, st);
 }

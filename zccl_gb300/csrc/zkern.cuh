@@ -73,6 +73,7 @@ struct DecompressArgs {
     int qprev_valid; /* tile_qprev valid; else recovered by look-back and written */
     ZWork w;
     ZSmem sm;
+    int rows_map;    /* set by the launcher: its tensor map views y as rows of 32 floats */
 };
 
 struct HomInput {
