@@ -181,6 +181,36 @@ def test_generic_block_sizes_against_port(port, torch):
             codec.check()
 
 
+def test_box_tiles_and_exact_quantization_against_port(port, torch):
+    """Full tiles whose element before them starts a 32-float row of a
+    16-byte-aligned buffer move as TMA boxes; the others (segments starting
+    off a row, a buffer 4 bytes off alignment) do not.  Both must give the
+    oracle's bytes and floats, also when products reach 2^24 and the exact
+    quantization takes over: everywhere (a large offset) or block by block
+    (spikes, one on the last element of a tile and one right after it)."""
+    rng = np.random.default_rng(11)
+    L = 32
+    for T, n in ((1, 5 * 8192 + 77), (4, 4 * 24576 + 3), (3, 2 * 3 * 8192 + 23)):
+        base = np.cumsum(rng.normal(0, 0.01, n)).astype(np.float32)
+        eb = float(np.float32(1e-4 * (base.max() - base.min())))
+        spiky = base.copy()
+        spiky[[8192, 8193, 5000, n - 2]] = np.float32(2.0e7 * eb)
+        for x in (base, (base + np.float32(2.0e7 * eb)).astype(np.float32), spiky):
+            codec = Z.Codec(n, L, T)
+            sx = port.compress(x, eb, L, T)
+            a = codec.compress(dev(torch, x), eb)
+            assert a.tobytes() == sx, (T, n)
+            off = torch.zeros(n + 1, dtype=torch.float32, device="cuda")
+            off[1:] = dev(torch, x)
+            assert codec.compress(off[1:], eb).tobytes() == sx, (T, n)
+            ref = port.decompress(sx, n, eb, L, T)
+            assert np.array_equal(codec.decompress(a, eb).cpu().numpy(), ref)
+            y = torch.zeros(n + 1, dtype=torch.float32, device="cuda")
+            codec.decompress(a, eb, out=y[1:])
+            assert np.array_equal(y[1:].cpu().numpy(), ref)
+            codec.check()
+
+
 def sinusoid_config1(n, seed):
     """16M-element test signal: sin(2 pi i/4096) + 0.3 sin(2 pi i/97) + N(0, 0.01)."""
     i = np.arange(n, dtype=np.float64)

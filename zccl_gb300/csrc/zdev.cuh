@@ -445,6 +445,31 @@ __device__ __forceinline__ void st_shared_f32(uint32_t sa, float x)
     asm volatile("st.shared.f32 [%0], %1;" ::"r"(sa), "f"(x) : "memory");
 }
 
+__device__ __forceinline__ float4 ld_shared_v4(uint32_t sa)
+{
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(sa)
+                 : "memory");
+    return v;
+}
+__device__ __forceinline__ float ld_shared_f32(uint32_t sa)
+{
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(sa) : "memory");
+    return v;
+}
+
+/* TMA tensor load of the box at (c0, c1) of a 2-D map into shared memory,
+ * completing on the mbarrier (whose byte count the caller arms). */
+__device__ __forceinline__ void tma_load_2d(uint32_t sa, const void *map, int32_t c0, int32_t c1, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(sa),
+        "l"((uint64_t)(uintptr_t)map), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+        : "memory");
+}
+
 /* TMA tensor store of the box at (c0, c1) of a 2-D map from shared memory,
  * in the issuing thread's bulk group.  The writers of the shared box run
  * fence_proxy_async_smem() and a barrier before it. */

@@ -29,18 +29,33 @@
  * into the same registers, and blocks above 32 elements are re-read from
  * their rows while packing.
  */
+#include <cstring>
+
 #include "zkern.cuh"
 
 namespace {
 
+/* A full tile of L = 32 whose element before it starts a 128-byte row of
+ * the single job's input arrives by one TMA tensor load of 256 rows of 32
+ * floats (the element before the tile first, 128-byte swizzle: 16-byte
+ * chunk k of row r at chunk k ^ (r & 7)) and a 16-byte copy that starts at
+ * its last element; every thread then reads its block straight from its
+ * row with vector loads that meet no bank conflict. */
+__device__ __forceinline__ bool box_tile(const CompressArgs &a, const ZGeom &g, const ZTile &z)
+{
+    return a.rows_map && !a.batch.jobs && g.L == 32 && g.TB == 256 && z.nblk == 256 &&
+           z.e_end - z.e_first == 8192 && ((z.e_first - 1) & 31) == 0;
+}
+
 /* Thread 0: ticket t (taken a little earlier, so that the atomic's latency
  * overlaps other work) becomes the claimed tile: its job is copied into
  * `slot` and the TMA copy of its floats (and the element before them) into
- * `in` starts.  The tile within its job lands in *s_tile (ZP_NONE when all are
- * taken), the job in *s_job; the caller synchronises before reading them. */
+ * `in` (or, for a box tile, into `box`) starts.  The tile within its job
+ * lands in *s_tile (ZP_NONE when all are taken), the job in *s_job; the
+ * caller synchronises before reading them. */
 __device__ __forceinline__ void claim_tile(const CompressArgs &a, uint64_t t, uint8_t *in, uint64_t *bar,
                                            uint64_t *s_tile, uint32_t *s_job, uint32_t *s_amax,
-                                           CompressJob *slot)
+                                           CompressJob *slot, uint8_t *box, const CUtensorMap *xmap)
 {
     if (threadIdx.x != 0) return;
     *s_amax = 0;
@@ -57,6 +72,13 @@ __device__ __forceinline__ void claim_tile(const CompressArgs &a, uint64_t t, ui
     *s_job = j;
     ZTile zt;
     zg_tile(&slot->g, local, &zt);
+    if (box && box_tile(a, slot->g, zt)) {
+        fence_proxy_async_smem(); /* earlier generic accesses of the box before the async writes */
+        mbar_expect_tx(bar, 32768u + 16u);
+        tma_load_2d(smem_u32(box), xmap, 0, (int32_t)((zt.e_first - 1) >> 5), bar);
+        bulk_g2s(box + 32768, slot->x + (zt.e_end - 1), 16u, bar); /* 16-byte aligned, like the row */
+        return;
+    }
     const uint32_t nel = (uint32_t)(zt.e_end - zt.e_first + 1);
     tma_load_superset(in, reinterpret_cast<const uint8_t *>(slot->x + (zt.e_first - 1)), nel * 4u, bar);
 }
@@ -64,7 +86,8 @@ __device__ __forceinline__ void claim_tile(const CompressArgs &a, uint64_t t, ui
 /* Block size TB + 32: warps 0 .. TB/32 - 1 compute (one thread per block of
  * the tile), the last warp places packed tiles in the stream. */
 template <bool FAST>
-__global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ CompressArgs a)
+__global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ CompressArgs a,
+                                                     const __grid_constant__ CUtensorMap xmap)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     uint64_t *bar_tma = reinterpret_cast<uint64_t *>(smem);      /* the tile's floats arrived */
@@ -84,6 +107,12 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
     const uint32_t NC = blockDim.x - 32, nw = NC >> 5; /* compute threads (TB), compute warps */
     const uint32_t L = a.job.g.L, stride = zg_row_stride(L); /* one L for the whole batch */
     uint32_t bad = 0;
+    /* the box of a box tile: 32 KB + 16 bytes at the first 1024-byte
+     * boundary of the input region, if it fits there */
+    const uint32_t box_sa = (smem_u32(in) + 1023u) & ~1023u;
+    uint8_t *box = FAST && a.rows_map && box_sa + 32768u + 16u <= smem_u32(smem) + a.sm.out
+                       ? in + (box_sa - smem_u32(in))
+                       : nullptr;
 
     if (tid == 0) {
         mbar_init(bar_tma, 1);
@@ -117,7 +146,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
     /* the compute warps */
     const uint32_t R = zg_ring_bytes(L, NC);
     uint32_t pos_prev = 0, end_prev = 0; /* thread 0: the previous tile's place in the ring */
-    if (tid == 0) claim_tile(a, atomicAdd(a.w.ticket, 1u), in, bar_tma, s_tile, s_job, s_amax, &cj[0]);
+    if (tid == 0) claim_tile(a, atomicAdd(a.w.ticket, 1u), in, bar_tma, s_tile, s_job, s_amax, &cj[0], box, &xmap);
     named_sync(1, NC);
     uint64_t tile = *s_tile;
     uint32_t job = *s_job;
@@ -136,15 +165,19 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
         ZTile z;
         zg_tile(&g, tile, &z);
 
-        /* 1. wait for the floats, move every block into its own padded row
-         *    (so the per-thread walk below has no bank conflicts), and find
-         *    the tile's largest magnitude */
+        /* 1. wait for the floats; unless they came as a box, move every
+         *    block into its own padded row (so the per-thread walk below has
+         *    no bank conflicts).  Blocks above 32 elements also find the
+         *    tile's largest magnitude, which decides whether the
+         *    one-multiply quantization is exact for the whole tile. */
         mbar_wait(bar_tma, it & 1u, a.w.err);
+        const bool bx = FAST && box && box_tile(a, g, z);
         const float *xin =
             reinterpret_cast<const float *>(in + ((uintptr_t)(J.x + (z.e_first - 1)) & 15u));
-        const float xprev0 = xin[0]; /* the head, or the last element of the previous tile */
-        uint32_t amax = abs_bits(xprev0);
-        if (FAST) {
+        /* the head, or the last element of the previous tile */
+        const float xprev0 = bx ? ld_shared_f32(box_sa) : xin[0];
+        bool fastq = true;
+        if (FAST && !bx) {
             /* TB rows (32 per compute warp) in four chunks, warp w owning
              * rows w, w + nw, ... of each.  The rows overlay the floats: row
              * k (stride above L) covers floats of rows k and later only, and
@@ -165,15 +198,15 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
                             v[r] = xin[1 + k * L + lane];
                     }
                 }
-#pragma unroll
-                for (int r = 0; r < 8; r++) amax = max(amax, abs_bits(v[r]));
                 named_sync(1, NC);
                 if (lane < L) { /* a row holds L floats */
 #pragma unroll
                     for (int r = 0; r < 8; r++) rows[(warp + (uint32_t)(8 * c + r) * nw) * stride + lane] = v[r];
                 }
             }
-        } else {
+            named_sync(1, NC);
+        } else if (!FAST) {
+            uint32_t amax = abs_bits(xprev0);
             for (uint32_t k = warp; k < z.nblk; k += nw) {
                 const uint32_t n = zg_block_len(z.seg_len, L, z.blk0 + k);
                 for (uint32_t j = lane; j < n; j += 32) {
@@ -182,41 +215,88 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
                     rows[k * stride + j] = v;
                 }
             }
+            amax = __reduce_max_sync(0xffffffffu, amax);
+            if (lane == 0) atomicMax(s_amax, amax);
+            named_sync(1, NC);
+            fastq = tile_fast_ok(*s_amax, J.inv);
         }
-        amax = __reduce_max_sync(0xffffffffu, amax);
-        if (lane == 0) atomicMax(s_amax, amax);
-        named_sync(1, NC);
-        const bool fastq = tile_fast_ok(*s_amax, J.inv);
 
-        /* 2. quantize, delta, width */
+        /* 2. quantize, delta, width.  A full block of up to 32 elements
+         *    takes the one-multiply quantization and checks on the way that
+         *    every product stayed below 2^24 in magnitude (then it is exact,
+         *    and a NaN fails the check); otherwise the block is done again
+         *    with the exact quantization. */
         const bool own = tid < z.nblk;
         const uint32_t n = own ? zg_block_len(z.seg_len, L, z.blk0 + tid) : 0u;
         const float *row = rows + tid * stride;
-        const float xp = !own ? 0.0f : (tid == 0 ? xprev0 : rows[(tid - 1) * stride + L - 1]);
+        const uint32_t rb = box_sa + tid * 128u, x4 = (tid & 7u) << 4; /* a box tile: this row */
         uint32_t b = 0, size = 0, smask = 0;
         uint32_t m[32];
-        if (FAST && fastq && n == 32) { /* the straight-line path */
-            int32_t qp = quantize_fast(xp, J.inv);
+        bool done = false;
+        if (FAST && own && n == 32) { /* the straight-line path */
+            bool ok = true;
             uint32_t mx = 0;
-#pragma unroll
-            for (int j = 0; j < 32; j++) {
-                const int32_t q = quantize_fast(row[j], J.inv);
+            int32_t qp = 0;
+            auto step = [&](float x, int j) {
+                const float pz = __fmul_rz(x, J.inv);
+                ok = ok && fabsf(pz) < 16777216.0f;
+                const int32_t q = __float2int_rz(pz);
                 const int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
                 qp = q;
                 smask = (smask << 1) | ((uint32_t)d >> 31);
                 m[j] = (uint32_t)abs(d); /* |INT_MIN| wraps to 2^31, as in the reference */
                 mx = max(mx, m[j]);
+            };
+            auto first = [&](float x) {
+                const float pz = __fmul_rz(x, J.inv);
+                ok = fabsf(pz) < 16777216.0f;
+                qp = __float2int_rz(pz);
+            };
+            if (bx) { /* chunk 0 is the element before the block and its first three */
+                float4 c = ld_shared_v4(rb | x4);
+                /* the last float is the next row's first; row 256 is the 16 bytes after the box */
+                float last = __shfl_down_sync(0xffffffffu, c.x, 1);
+                if (lane == 31) last = ld_shared_f32(rb + 128u);
+                first(c.x);
+                step(c.y, 0);
+                step(c.z, 1);
+                step(c.w, 2);
+#pragma unroll
+                for (uint32_t k = 1; k < 8; k++) {
+                    c = ld_shared_v4(rb | ((k << 4) ^ x4));
+                    step(c.x, 4 * k - 1);
+                    step(c.y, 4 * k);
+                    step(c.z, 4 * k + 1);
+                    step(c.w, 4 * k + 2);
+                }
+                step(last, 31);
+            } else {
+                first(tid == 0 ? xprev0 : rows[(tid - 1) * stride + L - 1]);
+#pragma unroll
+                for (int j = 0; j < 32; j++) step(row[j], j);
             }
-            b = width_of(mx, a.wt);
-            size = zg_block_bytes(b, 32);
-        } else if (FAST && own) { /* a short block or the exact slow quantization */
-            int32_t qp = fastq ? quantize_fast(xp, J.inv) : quantize(xp, J.inv, bad);
+            if (ok) {
+                b = width_of(mx, a.wt);
+                size = zg_block_bytes(b, 32);
+                done = true;
+            }
+        }
+        if (FAST && own && !done) { /* a short block or the exact quantization */
+            /* element j of a box row sits at box float 32 tid + 1 + j */
+            auto elem = [&](uint32_t j) -> float {
+                if (!bx) return row[j];
+                const uint32_t q = 32u * tid + 1u + j, r = q >> 5;
+                return ld_shared_f32(box_sa + r * 128u + ((((q >> 2) & 7u) ^ (r & 7u)) << 4) + (q & 3u) * 4u);
+            };
+            const float xp = bx ? ld_shared_f32(rb | x4) : (tid == 0 ? xprev0 : rows[(tid - 1) * stride + L - 1]);
+            int32_t qp = quantize(xp, J.inv, bad);
             uint32_t mx = 0;
+            smask = 0;
 #pragma unroll
             for (int j = 0; j < 32; j++) {
                 m[j] = 0;
                 if ((uint32_t)j < n) {
-                    const int32_t q = fastq ? quantize_fast(row[j], J.inv) : quantize(row[j], J.inv, bad);
+                    const int32_t q = quantize(elem(j), J.inv, bad);
                     const int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
                     qp = q;
                     smask |= ((uint32_t)d >> 31) << (31 - j);
@@ -226,7 +306,8 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
             }
             b = width_of(mx, a.wt);
             size = zg_block_bytes(b, n);
-        } else if (own) { /* blocks above 32 elements: the rows are read again when packing */
+        } else if (!FAST && own) { /* blocks above 32 elements: the rows are read again when packing */
+            const float xp = tid == 0 ? xprev0 : rows[(tid - 1) * stride + L - 1];
             int32_t qp = fastq ? quantize_fast(xp, J.inv) : quantize(xp, J.inv, bad);
             uint32_t mx = 0;
             for (uint32_t j = 0; j < n; j++) {
@@ -249,7 +330,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
         if (warp == 0) lb_publish(J.status, tile, total, tile == 0, 0);
         uint32_t ticket = 0; /* the next tile's, taken now and used after the ring reservation */
         if (tid == 0) ticket = atomicAdd(a.w.ticket, 1u);
-        const int32_t qprev0 = fastq ? quantize_fast(xprev0, J.inv) : quantize(xprev0, J.inv, bad);
+        const int32_t qprev0 = quantize(xprev0, J.inv, bad);
         if (own) J.idx.widths[z.gblk0 + tid] = (uint8_t)b;
         if (tid == 0) J.idx.tile_qprev[tile] = qprev0;
 
@@ -260,7 +341,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
          *    while holding a claimed tile whose size is not yet published. */
         if (tid == 0) {
             *s_pos = ring_reserve(ring, it, zg_ring_need(total), R, pos_prev, end_prev, a.w.err);
-            if (FAST) claim_tile(a, ticket, in, bar_tma, s_tile, s_job, s_amax, &cj[(it + 1) & 1u]);
+            if (FAST) claim_tile(a, ticket, in, bar_tma, s_tile, s_job, s_amax, &cj[(it + 1) & 1u], box, &xmap);
         }
         named_sync(1, NC);
         const uint32_t pos = *s_pos;
@@ -281,6 +362,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
             }
         } else {
             if (own) {
+                const float xp = tid == 0 ? xprev0 : rows[(tid - 1) * stride + L - 1];
                 int32_t qp = fastq ? quantize_fast(xp, J.inv) : quantize(xp, J.inv, bad);
                 encode_any(pk_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
                     const int32_t q = fastq ? quantize_fast(row[j], J.inv) : quantize(row[j], J.inv, bad);
@@ -291,7 +373,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
                 });
             }
             named_sync(1, NC); /* the rows have been read for the last time */
-            if (tid == 0) claim_tile(a, ticket, in, bar_tma, s_tile, s_job, s_amax, &cj[(it + 1) & 1u]);
+            if (tid == 0) claim_tile(a, ticket, in, bar_tma, s_tile, s_job, s_amax, &cj[(it + 1) & 1u], box, &xmap);
         }
         named_sync(1, NC); /* the packed tile is complete; the claimed index is visible */
         if (tid == 0) ring_publish(ring, it, tile, job, total, pos);
@@ -313,9 +395,13 @@ cudaError_t launch_compress(const CompressArgs &a, cudaStream_t st)
     const uint64_t tiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
     unsigned grid = persistent_grid(fn, threads, a.sm.total, tiles);
     if (a.grid && a.grid < grid) grid = a.grid;
+    CompressArgs b = a;
+    alignas(64) CUtensorMap map;
+    memset(&map, 0, sizeof map);
+    b.rows_map = fast && !a.batch.jobs && zk_rows_map(&map, a.job.x, a.job.g.n);
     if (fast)
-        k_compress<true><<<grid, threads, a.sm.total, st>>>(a);
+        k_compress<true><<<grid, threads, a.sm.total, st>>>(b, map);
     else
-        k_compress<false><<<grid, threads, a.sm.total, st>>>(a);
+        k_compress<false><<<grid, threads, a.sm.total, st>>>(b, map);
     return cudaGetLastError();
 }

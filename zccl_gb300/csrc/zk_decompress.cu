@@ -22,7 +22,6 @@
  *   4. x = (float)q * eb (ZCCLd_float.c:624) into padded rows, written out
  *      row by row with coalesced stores.
  */
-#include <cuda.h>
 #include <cudaTypedefs.h>
 
 #include <cstring>
@@ -334,25 +333,22 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_tiled()
     return fn;
 }
 
-/* y[0, n) as rows of 32 floats, boxes of 256 rows, 128-byte swizzle.
- * False (and the kernel stores rows itself) when y is not 16-byte aligned,
- * holds fewer than one box, or the encoder is unavailable. */
-bool rows_map(CUtensorMap *map, float *y, uint64_t n)
+} // namespace
+
+bool zk_rows_map(CUtensorMap *map, const void *p, uint64_t n)
 {
     const uint64_t nrows = n / 32u;
-    if (((uintptr_t)y & 15u) || nrows < 256u || nrows > 0x7fffffffull) return false;
+    if (((uintptr_t)p & 15u) || nrows < 256u || nrows > 0x7fffffffull) return false;
     PFN_cuTensorMapEncodeTiled_v12000 enc = encode_tiled();
     if (!enc) return false;
     const cuuint64_t dim[2] = {32u, nrows};
     const cuuint64_t stride[1] = {128u};
     const cuuint32_t box[2] = {32u, 256u};
     const cuuint32_t estride[2] = {1u, 1u};
-    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, y, dim, stride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(p), dim, stride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
                CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
-
-} // namespace
 
 cudaError_t launch_decompress(const DecompressArgs &a, cudaStream_t st)
 {
@@ -367,7 +363,7 @@ cudaError_t launch_decompress(const DecompressArgs &a, cudaStream_t st)
     DecompressArgs b = a;
     alignas(64) CUtensorMap map;
     memset(&map, 0, sizeof map);
-    b.rows_map = fast && rows_map(&map, a.y, a.g.n);
+    b.rows_map = fast && zk_rows_map(&map, a.y, a.g.n);
     void *args[] = {&b, &map};
     return cudaLaunchKernel(fn, dim3(grid), dim3(a.g.TB), args, a.sm.total, st);
 }

@@ -5,6 +5,7 @@
 #ifndef ZCCL_GB300_ZKERN_CUH
 #define ZCCL_GB300_ZKERN_CUH
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -61,6 +62,7 @@ struct CompressArgs {
     ZWidthTable wt;
     ZSmem sm;
     uint32_t grid; /* CTAs to launch, 0 = as many as fit */
+    int rows_map;  /* set by the launcher: its tensor map views job.x as rows of 32 floats */
 };
 
 struct DecompressArgs {
@@ -341,6 +343,12 @@ static inline unsigned persistent_grid(const void *fn, int threads, size_t smem,
 /* Launchers; each returns the cudaError_t of the launch. */
 cudaError_t launch_compress(const CompressArgs &a, cudaStream_t st);
 cudaError_t launch_decompress(const DecompressArgs &a, cudaStream_t st);
+
+/* Host: a 2-D TMA map of the floats p[0, n) as rows of 32, boxes of 256
+ * rows, 128-byte swizzle (16-byte chunk k of row r lands at chunk k ^ (r & 7)
+ * of a 1024-byte-aligned box).  False when p is not 16-byte aligned, holds
+ * fewer than one box, or the driver's encoder is unavailable. */
+bool zk_rows_map(CUtensorMap *map, const void *p, uint64_t n);
 cudaError_t launch_homadd(const HomAddArgs &a, cudaStream_t st);
 cudaError_t launch_walk(const WalkArgs &a, cudaStream_t st);
 
