@@ -211,6 +211,30 @@ def test_box_tiles_and_exact_quantization_against_port(port, torch):
             codec.check()
 
 
+def test_every_block_width_against_port(port, torch):
+    """Blocks of every width 0..31 side by side (block k's values spread
+    over 2^(k mod 32) quantization steps), through compress, decompress
+    and the homomorphic add, in full tiles and in a ragged tail."""
+    rng = np.random.default_rng(5)
+    L, eb = 32, 1.0e-3
+    for T, n in ((1, 3 * 8192 + 1000), (3, 3 * 8192 + 7)):
+        k = np.arange(n) // L
+        amp = np.ldexp(1.0, (k % 32).astype(np.int64) - 1)
+        x = (eb * np.round(rng.uniform(-1, 1, n) * amp)).astype(np.float32)
+        x[(k % 32) == 0] = np.float32(eb * 7)  # constant blocks: width 0
+        y = (eb * np.round(rng.uniform(-1, 1, n) * amp[::-1])).astype(np.float32)
+        codec = Z.Codec(n, L, T)
+        sx, sy = port.compress(x, eb, L, T), port.compress(y, eb, L, T)
+        a, b = codec.compress(dev(torch, x), eb), codec.compress(dev(torch, y), eb)
+        assert a.tobytes() == sx and b.tobytes() == sy, (T, n)
+        assert np.array_equal(codec.decompress(a, eb).cpu().numpy(), port.decompress(sx, n, eb, L, T))
+        h = codec.homadd([a, b])
+        sh = port.homadd(sx, sy, n, eb, L, T)
+        assert h.tobytes() == sh
+        assert np.array_equal(codec.decompress(h, eb).cpu().numpy(), port.decompress(sh, n, eb, L, T))
+        codec.check()
+
+
 def sinusoid_config1(n, seed):
     """16M-element test signal: sin(2 pi i/4096) + 0.3 sin(2 pi i/97) + N(0, 0.01)."""
     i = np.arange(n, dtype=np.float64)

@@ -225,54 +225,101 @@ __device__ __forceinline__ void encode_full(uint32_t sbase, uint32_t o, uint32_t
     pk.finish();
 }
 
+/* Bytes a .. a + 7 of the shared words w as a 64-bit big-endian value
+ * (hi: bytes a .. a + 3).  Reads the three words that hold them. */
+__device__ __forceinline__ void be64_at(const uint32_t *w, uint32_t a, uint32_t &hi, uint32_t &lo)
+{
+    const uint32_t k = a >> 2, sh = (a & 3u) * 8u;
+    const uint32_t w0 = bswap32(w[k]), w1 = bswap32(w[k + 1]), w2 = bswap32(w[k + 2]);
+    hi = __funnelshift_l(w1, w0, sh);
+    lo = __funnelshift_l(w2, w1, sh);
+}
+
+/* prmt.b32 with a selector whose nibbles may ask for the sign of a byte
+ * replicated (nibble bit 3), which __byte_perm does not offer. */
+__device__ __forceinline__ uint32_t prmt_sign(uint32_t a, uint32_t sel)
+{
+    uint32_t r;
+    asm("prmt.b32 %0, %1, 0, %2;" : "=r"(r) : "r"(a), "r"(sel));
+    return r;
+}
+
 /* Inverse of encode_full for a block of width b at byte o of the shared
  * words w: d[j] = the int32 delta of element j (as uint32).  Returns the
- * wrapped sum of the deltas. */
+ * wrapped sum of the deltas.  Branch-free in the width's low part, so the
+ * threads of a warp stay together whatever their blocks' widths:
+ *   - the high bytes (B = b / 8 == 1, the common case) come from nine
+ *     aligned words realigned by funnel shifts, one byte per element;
+ *   - the r = b % 8 low bits of eight consecutive elements fill r whole
+ *     bytes (byte g r on for group g), read as one big-endian window whose
+ *     two 4r-bit halves give four fields each;
+ *   - element j's sign (bit 31 - j of the sign word) becomes a mask by
+ *     replicating the sign of byte j / 8 of the sign word shifted by j % 8.
+ * Reads up to 12 bytes past the block (buffers carry slack). */
 __device__ __forceinline__ uint32_t decode_full(const uint32_t *w, uint32_t o, uint32_t b,
                                                 uint32_t (&d)[32])
 {
+    if (b == 0) {
 #pragma unroll
-    for (int j = 0; j < 32; j++) d[j] = 0;
-    if (b == 0) return 0;
+        for (int j = 0; j < 32; j++) d[j] = 0;
+        return 0;
+    }
     const uint32_t B = b >> 3, r = b & 7u;
-    Reader rd;
-    rd.init(w, o + 1);
-    const uint32_t sg = rd.get(32);
+    uint32_t sg, unused;
+    be64_at(w, o + 1, sg, unused);
+    const uint32_t hb = o + 5, lb = hb + 32u * B;
     if (B == 1) {
+        const uint32_t k0 = hb >> 2, sh = (hb & 3u) * 8u;
+        uint32_t prev = w[k0];
 #pragma unroll
-        for (int j = 0; j < 32; j += 4) {
-            rd.refill();
-            const uint32_t q = rd.get(32);
-            d[j] = (q >> 24) << r;
-            d[j + 1] = ((q >> 16) & 0xFFu) << r;
-            d[j + 2] = ((q >> 8) & 0xFFu) << r;
-            d[j + 3] = (q & 0xFFu) << r;
+        for (int k = 0; k < 8; k++) {
+            const uint32_t next = w[k0 + k + 1];
+            const uint32_t A = __funnelshift_r(prev, next, sh); /* bytes hb + 4k .. hb + 4k + 3 */
+            prev = next;
+#pragma unroll
+            for (int i = 0; i < 4; i++) d[4 * k + i] = __byte_perm(A, 0, 0x4440 | i) << r;
         }
     } else if (B > 1) {
+        Reader rd;
+        rd.init(w, hb);
 #pragma unroll
         for (int j = 0; j < 32; j++) {
             rd.refill();
             d[j] = bswap32(rd.get(8u * B) << (32u - 8u * B)) << r;
         }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 32; j++) d[j] = 0;
     }
     if (r) {
         const uint32_t mask = (1u << r) - 1u;
+        const uint32_t s1 = 32u - r, s2 = s1 - r, s3 = s2 - r, s4 = s3 - r; /* >= 4 */
 #pragma unroll
-        for (int j = 0; j < 32; j += 4) {
-            rd.refill();
-            const uint32_t q = rd.get(4u * r);
-            d[j] |= q >> (3u * r);
-            d[j + 1] |= (q >> (2u * r)) & mask;
-            d[j + 2] |= (q >> r) & mask;
-            d[j + 3] |= q & mask;
+        for (int g = 0; g < 4; g++) {
+            uint32_t hi, lo;
+            be64_at(w, lb + (uint32_t)g * r, hi, lo);
+            const uint32_t h2 = __funnelshift_l(lo, hi, 4u * r); /* fields 4 .. 7 on top */
+            d[8 * g + 0] |= (hi >> s1) & mask;
+            d[8 * g + 1] |= (hi >> s2) & mask;
+            d[8 * g + 2] |= (hi >> s3) & mask;
+            d[8 * g + 3] |= (hi >> s4) & mask;
+            d[8 * g + 4] |= (h2 >> s1) & mask;
+            d[8 * g + 5] |= (h2 >> s2) & mask;
+            d[8 * g + 6] |= (h2 >> s3) & mask;
+            d[8 * g + 7] |= (h2 >> s4) & mask;
         }
     }
     uint32_t sum = 0;
 #pragma unroll
-    for (int j = 0; j < 32; j++) {
-        const uint32_t s = (uint32_t)((int32_t)(sg << j) >> 31); /* all ones when negative */
-        d[j] = (d[j] ^ s) - s;
-        sum += d[j];
+    for (int k = 0; k < 8; k++) {
+        const uint32_t t = sg << k; /* element 8m + k's sign is the top bit of byte 3 - m */
+#pragma unroll
+        for (int m = 0; m < 4; m++) {
+            const uint32_t s = prmt_sign(t, 0x1111u * (8u | (3u - (uint32_t)m))); /* all ones when negative */
+            const int j = 8 * m + k;
+            d[j] = (d[j] ^ s) - s;
+            sum += d[j];
+        }
     }
     return sum;
 }
