@@ -197,7 +197,7 @@ ZSmem compress_smem(const ZGeom &g)
 
 ZSmem homadd_smem(const ZGeom &g)
 {
-    return zg_smem(2, g.L, g.TB, (uint32_t)(2 * sizeof(HomAddJob) + sizeof(ZPlace)));
+    return zg_smem(2, g.L, g.TB, homadd_job_bytes(g.TB));
 }
 
 } // namespace

@@ -448,6 +448,12 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+/* `n` arrivals at once (release at CTA scope). */
+__device__ __forceinline__ void mbar_arrive_n(uint64_t *bar, uint32_t n)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(n) : "memory");
+}
+
 /* Wait for phase `parity` of the barrier to complete.  Gives up after a
  * bounded number of polls and reports ZERR_TIMEOUT instead of hanging. */
 __device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t parity, uint32_t *err)
@@ -631,6 +637,21 @@ __device__ __forceinline__ uint32_t grp_excl_scan(uint32_t v, uint32_t *wsum, ui
     *total = wsum[32];
     named_sync(id, n);
     return r;
+}
+
+/* The same with one barrier: every warp reads all warp sums.  Callers
+ * alternate between two scratch arrays on consecutive calls, so that a
+ * warp's next write cannot overtake a slower warp's read. */
+__device__ __forceinline__ uint32_t grp_excl_scan1(uint32_t v, uint32_t *ws, uint32_t *total, uint32_t n,
+                                                   uint32_t id)
+{
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = n >> 5;
+    const uint32_t inc = warp_incl_scan(v);
+    if (lane == 31) ws[warp] = inc;
+    named_sync(id, n);
+    const uint32_t t = lane < nw ? ws[lane] : 0u;
+    *total = __reduce_add_sync(0xffffffffu, t);
+    return __reduce_add_sync(0xffffffffu, lane < warp ? t : 0u) + inc - v;
 }
 
 /* Two exclusive scans at once on the same barriers: v0 with scratch ws0,

@@ -123,7 +123,12 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
 
     if (tid >= NC) { /* the placer warp */
         const uint64_t max_tiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
-        placer_loop(ring, outb, pj, a.w.err, max_tiles, bad, [&](uint32_t j, ZPlace *p) {
+        placer_loop(
+            ring, outb, pj, a.w.err, max_tiles, bad, false,
+            [&](uint64_t k) {
+                if (lane == 0) ring_wait(&ring->packed, (uint32_t)k + 1, a.w.err);
+            },
+            [&](uint32_t j, ZPlace *p) {
             if (a.batch.jobs) {
                 const CompressJob &J = static_cast<const CompressJob *>(a.batch.jobs)[j];
                 p->g = J.g;

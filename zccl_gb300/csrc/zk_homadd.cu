@@ -9,185 +9,199 @@
  * canonical).  Integer addition is associative modulo 2^32, so one pass over
  * P inputs equals the ring's pairwise fold in any order, bit for bit.
  *
- * Persistent CTAs take tiles in ticket order, one compute thread per block
- * plus one placer warp.  A tile's P inputs form a stream of TMA copies
- * through two buffers: while one input's tile bytes are unpacked and added
- * into per-thread registers, the next input's sizes are scanned from its
- * width index and its bytes are already in flight.  Zero-width input blocks
- * are skipped without touching their bytes.  After the last input the sum
- * is re-encoded like the compressor does (width, scan, early look-back
- * publish, packing), and the placer warp finds its place in the stream with
- * the look-back and writes it out while the compute warps add the next
- * tile.  The starting value per tile is the sum of the inputs' values.
+ * Persistent CTAs take tiles in ticket order with three kinds of warps.  A
+ * loader warp turns every input of every claimed tile into one TMA copy
+ * into one of two buffers, with a table of each block's offset and width
+ * found from the input's width index.  The adding warps, one thread per
+ * block, unpack their block of each input as it arrives and add it into
+ * registers (zero-width blocks are skipped without touching their bytes),
+ * handing each buffer back through an mbarrier.  After the last input the
+ * sum is re-encoded like the compressor does (width, scan, early look-back
+ * publish, packing into a shared-memory ring), and the placer warp finds its
+ * place in the stream with the look-back and writes it out while the adding
+ * warps go on.  The starting value per tile is the sum of the inputs'
+ * values.
  */
 #include "zkern.cuh"
 
 namespace {
 
-struct BlockSlot {
-    uint32_t b, n, off;
-};
-
-/* Thread 0: the TMA copy of `total` bytes of an input tile at byte `base`
- * (from the index, so checked against the readable bytes) into buf. */
-__device__ __forceinline__ void issue_input(const HomInput &in, uint64_t base, uint32_t total, uint8_t *buf,
-                                            uint64_t *bar, uint64_t *s_base, uint32_t &bad)
+/* The job of batch ticket j (or the single job), read in place. */
+__device__ __forceinline__ const HomAddJob &job_of(const HomAddArgs &a, uint32_t j)
 {
-    uint32_t nload = total;
-    /* overflow-safe: base comes from the index and is not trusted */
-    if (base > in.avail || total > in.avail - base) {
-        bad |= ZERR_BOUNDS;
-        nload = base < in.avail ? (uint32_t)min((uint64_t)total, in.avail - base) : 0u;
-        if (base > in.avail) base = 0;
-    }
-    *s_base = base;
-    tma_load_superset(buf, in.bytes + base, nload, bar);
+    return a.batch.jobs ? static_cast<const HomAddJob *>(a.batch.jobs)[j] : a.job;
 }
 
-/* The compute threads: sizes of input p's blocks in tile t, their offsets,
- * and (thread 0) the TMA copy of those bytes into buf. */
-__device__ __forceinline__ BlockSlot stage_input(const HomAddJob &J, uint64_t t, uint32_t p,
-                                                 uint8_t *buf, uint64_t *bar, uint32_t *wsum,
-                                                 uint64_t *s_base, uint32_t &bad)
-{
-    const HomInput &in = J.in[p];
-    BlockSlot sl = {0, 0, 0};
-    ZTile z;
-    zg_tile(&J.g, t, &z);
-    uint32_t size = 0;
-    if (threadIdx.x < z.nblk) {
-        sl.n = zg_block_len(z.seg_len, J.g.L, z.blk0 + threadIdx.x);
-        sl.b = in.widths[z.gblk0 + threadIdx.x];
-        if (sl.b > 32) {
-            bad |= ZERR_CORRUPT;
-            sl.b = 0;
-        }
-        size = zg_block_bytes(sl.b, sl.n);
-    }
-    uint64_t base0 = 0;
-    if (threadIdx.x == 0) base0 = in.tile_off[t]; /* on its way during the scan */
-    uint32_t total;
-    sl.off = grp_excl_scan(size, wsum, &total, J.g.TB, 1);
-    if (threadIdx.x == 0) issue_input(in, base0, total + (z.has_head ? 4u : 0u), buf, bar, s_base, bad);
-    return sl;
-}
-
-/* One thread: a job into shared memory, with only the inputs it uses. */
-__device__ __forceinline__ void copy_job(HomAddJob *dst, const HomAddJob *src)
-{
-    const uint32_t P = src->P < ZH_MAXP ? src->P : ZH_MAXP;
-    copy16(dst, src, (uint32_t)offsetof(HomAddJob, in));
-    copy16(&dst->in[0], &src->in[0], (uint32_t)((P * sizeof(HomInput) + 15u) & ~15u));
-    copy16(&dst->P, &src->P, (uint32_t)(sizeof(HomAddJob) - offsetof(HomAddJob, P)));
-}
-
-/* Thread 0: ticket t (taken a little earlier, so that the atomic's latency
- * overlaps other work) becomes the claimed tile: its job is copied into
- * `slot`, the tile within its job lands in *s_tile (ZP_NONE when all are
- * taken), the job in *s_job.  The caller synchronises before reading them. */
-__device__ __forceinline__ void take_ticket(const HomAddArgs &a, uint64_t t, uint64_t *s_tile, uint32_t *s_job,
-                                            HomAddJob *slot)
-{
-    if (threadIdx.x != 0) return;
-    const uint64_t total = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
-    if (t >= total) {
-        *s_tile = ZP_NONE;
-        return;
-    }
-    uint64_t local;
-    const uint32_t j = batch_job(a.batch, t, &local);
-    copy_job(slot, a.batch.jobs ? static_cast<const HomAddJob *>(a.batch.jobs) + j : &a.job);
-    *s_tile = local;
-    *s_job = j;
-}
-
-/* Block size TB + 32: warps 0 .. TB/32 - 1 add (one thread per block of the
- * tile), the last warp places packed sums in the stream. */
+/* The loader warp.  It claims tiles in ticket order and, for every input of
+ * every claimed tile, waits for a free buffer, finds each block's width and
+ * offset from the input's width index (eight blocks per lane and a warp
+ * scan), writes them into the buffer's block table (offset << 8 | width),
+ * and starts one TMA copy of the tile's bytes; the copy's mbarrier tells the
+ * adding warps.  After the last tile it hands over a stage marked ZP_NONE.
+ * Tiles are claimed at most two inputs ahead of the adding warps, which
+ * never wait on another CTA before they publish their tile's size, so the
+ * look-back always progresses. */
 template <bool FAST>
-__global__ void __launch_bounds__(288, 2) k_homadd(const __grid_constant__ HomAddArgs a)
+__device__ __forceinline__ void loader_loop(const HomAddArgs &a, uint8_t *buf0, uint8_t *buf1, HStage *stage,
+                                            uint32_t *btab0, uint32_t *btab1, uint64_t *full, uint64_t *empty,
+                                            uint32_t &bad)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t ntiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
+    uint32_t seq = 0; /* copies handed over so far */
+    for (;;) {
+        uint64_t t = 0, tk = 0;
+        uint32_t j = 0;
+        if (lane == 0) {
+            tk = atomicAdd(a.w.ticket, 1u);
+            if (tk < ntiles) j = batch_job(a.batch, tk, &t);
+        }
+        tk = __shfl_sync(0xffffffffu, tk, 0);
+        if (tk >= ntiles) {
+            const uint32_t s = seq & 1u;
+            if (seq >= 2) mbar_wait(&empty[s], ((seq >> 1) + 1u) & 1u, a.w.err);
+            if (lane == 0) {
+                stage[s].tile = ZP_NONE;
+                mbar_arrive(&full[s]);
+            }
+            return;
+        }
+        t = __shfl_sync(0xffffffffu, t, 0);
+        j = __shfl_sync(0xffffffffu, j, 0);
+        const HomAddJob &J = job_of(a, j);
+        ZTile z;
+        zg_tile(&J.g, t, &z);
+        const uint32_t P = J.P;
+        for (uint32_t p = 0; p < P; p++, seq++) {
+            const HomInput &in = J.in[p];
+            uint64_t base = 0;
+            if (lane == 0) base = in.tile_off[t];
+            uint32_t bw[8], off[8], sum = 0;
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const uint32_t i = 8u * lane + (uint32_t)k;
+                uint32_t b = 0, size = 0;
+                if (i < z.nblk) {
+                    b = in.widths[z.gblk0 + i];
+                    if (b > 32) {
+                        bad |= ZERR_CORRUPT;
+                        b = 0;
+                    }
+                    size = zg_block_bytes(b, zg_block_len(z.seg_len, J.g.L, z.blk0 + i));
+                }
+                bw[k] = b;
+                off[k] = sum;
+                sum += size;
+            }
+            const uint32_t incl = warp_incl_scan(sum);
+            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31) + (z.has_head ? 4u : 0u);
+            const uint32_t s = seq & 1u;
+            if (seq >= 2) mbar_wait(&empty[s], ((seq >> 1) + 1u) & 1u, a.w.err); /* copy seq - 2 consumed */
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const uint32_t i = 8u * lane + (uint32_t)k;
+                if (i < z.nblk) (s ? btab1 : btab0)[i] = (incl - sum + off[k]) << 8 | bw[k];
+            }
+            __syncwarp();
+            if (lane == 0) {
+                uint32_t nload = total;
+                /* overflow-safe: base comes from the index and is not trusted */
+                if (base > in.avail || total > in.avail - base) {
+                    bad |= ZERR_BOUNDS;
+                    nload = base < in.avail ? (uint32_t)min((uint64_t)total, in.avail - base) : 0u;
+                    if (base > in.avail) base = 0;
+                }
+                stage[s].tile = t;
+                stage[s].job = j;
+                stage[s].p = p;
+                stage[s].ph = (uint32_t)((uintptr_t)(in.bytes + base) & 15u);
+                tma_load_superset(s ? buf1 : buf0, in.bytes + base, nload, &full[s]);
+            }
+        }
+    }
+}
+
+/* Block size TB + 64: warps 0 .. TB/32 - 1 add (one thread per block of the
+ * tile), warp TB/32 places packed sums in the stream, warp TB/32 + 1 loads
+ * the inputs.  The adding warps meet at one barrier per tile (the scan of
+ * the sum's block sizes); inputs arrive and buffers are returned through
+ * mbarriers, and packed sums go to the placer through a per-slot mbarrier
+ * that every adding warp arrives on. */
+template <bool FAST>
+__global__ void __launch_bounds__(320, 2) k_homadd(const __grid_constant__ HomAddArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem);          /* [2] input copies */
-    uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 32);    /* [33] */
-    uint64_t *s_tile = reinterpret_cast<uint64_t *>(smem + 168); /* the claimed tile (within its job) */
-    uint32_t *s_pos = reinterpret_cast<uint32_t *>(smem + 176);  /* ring position of this sum */
-    uint32_t *s_job = reinterpret_cast<uint32_t *>(smem + 180);  /* the claimed tile's job */
-    uint64_t *s_base = reinterpret_cast<uint64_t *>(smem + 192); /* [2] */
-    ZRing *ring = reinterpret_cast<ZRing *>(smem + 256);
-    HomAddJob *hj = reinterpret_cast<HomAddJob *>(smem + a.sm.jobs); /* [2], by round */
-    ZPlace *pj = reinterpret_cast<ZPlace *>(smem + a.sm.jobs + 2 * sizeof(HomAddJob));
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem);        /* [2] input copy arrived */
+    uint64_t *empty = reinterpret_cast<uint64_t *>(smem + 16);  /* [2] input buffer consumed */
+    uint32_t *wsum0 = reinterpret_cast<uint32_t *>(smem + 48);  /* [33] scan scratch, even tiles */
+    uint32_t *wsum1 = reinterpret_cast<uint32_t *>(smem + 184); /* [33] odd tiles */
+    ZRing4 *ring = reinterpret_cast<ZRing4 *>(smem + 320);
+    ZPlace *pj = reinterpret_cast<ZPlace *>(smem + a.sm.jobs);
+    HStage *stage = reinterpret_cast<HStage *>(smem + a.sm.jobs + zg_a16(sizeof(ZPlace))); /* [2] */
+    uint32_t *const btab0 = reinterpret_cast<uint32_t *>(stage + 2), *const btab1 = btab0 + a.job.g.TB;
     uint32_t *acc_rows = reinterpret_cast<uint32_t *>(smem + a.sm.rows);
     uint8_t *outs = smem + a.sm.out; /* the ring of packed sums */
+    uint8_t *const buf0 = smem + a.sm.in0, *const buf1 = smem + a.sm.in1;
 
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t NC = blockDim.x - 32; /* compute threads (TB) */
+    const uint32_t NC = blockDim.x - 64, nwc = NC >> 5; /* adding threads (TB), adding warps */
     const uint32_t L = a.job.g.L, stride = zg_row_stride(L); /* one L for the whole batch */
+    const uint32_t R = zg_ring_bytes(L, NC);
     uint32_t bad = 0;
     /* see k_decompress: a failed index walk stops every CTA alike */
     if (*(volatile const uint32_t *)a.w.walk_err) return;
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        ring->packed = 0;
-        ring->placed = 0;
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        mbar_init(&empty[0], nwc);
+        mbar_init(&empty[1], nwc);
+        ring4_init(ring, nwc);
     }
+    /* the ring starts zeroed, and the placer zeroes what it has written out */
+    for (uint32_t i = tid; i < (R + 48u) / 16u; i += blockDim.x) reinterpret_cast<uint4 *>(outs)[i] = make_uint4(0, 0, 0, 0);
     __syncthreads();
 
-    if (tid >= NC) { /* the placer warp */
+    if (warp == nwc) { /* the placer warp */
         const uint64_t max_tiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
-        placer_loop(ring, outs, pj, a.w.err, max_tiles, bad, [&](uint32_t j, ZPlace *p) {
-            if (a.batch.jobs) {
-                const HomAddJob &J = static_cast<const HomAddJob *>(a.batch.jobs)[j];
+        placer_loop4(ring, outs, pj, a.w.err, max_tiles, bad, [&](uint32_t j, ZPlace *p) {
+                const HomAddJob &J = job_of(a, j);
                 p->g = J.g;
                 p->out = J.out;
                 p->cap = J.cap;
                 p->idx = J.idx;
                 p->status = J.status;
-            } else {
-                p->g = a.job.g;
-                p->out = a.job.out;
-                p->cap = a.job.cap;
-                p->idx = a.job.idx;
-                p->status = a.job.status;
-            }
-        });
+            });
+        if (bad) atomicOr(a.w.err, bad);
+        return;
+    }
+    if (warp == nwc + 1) { /* the loader warp */
+        loader_loop<FAST>(a, buf0, buf1, stage, btab0, btab1, full, empty, bad);
         if (bad) atomicOr(a.w.err, bad);
         return;
     }
 
-    /* the compute warps.  Tiles are claimed one at a time when these warps
-     * are ready for them, and they never wait while holding a claimed tile
-     * whose size is not yet published. */
-    uint32_t *ws1 = reinterpret_cast<uint32_t *>(smem + 320); /* [33] second scan scratch */
-    uint8_t *const buf0 = smem + a.sm.in0, *const buf1 = smem + a.sm.in1;
+    /* the adding warps */
     uint32_t acc[32];
-    uint32_t ld = 0; /* index of the current copy in the two-buffer stream */
-    const uint32_t R = zg_ring_bytes(L, NC);
-    uint32_t pos_prev = 0, end_prev = 0; /* thread 0: the previous sum's place in the ring */
-    if (tid == 0) take_ticket(a, atomicAdd(a.w.ticket, 1u), s_tile, s_job, &hj[0]);
-    named_sync(1, NC);
-    uint64_t tile = *s_tile;
-    uint32_t job = *s_job;
-    BlockSlot cur = {0, 0, 0};
-    if (tile != ZP_NONE) cur = stage_input(hj[0], tile, 0, smem + a.sm.in0, &bar[0], wsum, &s_base[0], bad);
-
-    for (uint32_t it = 0;; it++) {
+    uint32_t seq = 0;                    /* input copies consumed */
+    uint32_t H = 0, hp = 0; /* ring bytes taken and the ring's next position (the same in every thread) */
+    const uint64_t max_tiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
+    for (uint32_t it = 0; it <= max_tiles; it++) { /* bounded even if a wait gave up */
+        uint32_t s = seq & 1u;
+        mbar_wait(&full[s], (seq >> 1) & 1u, a.w.err);
+        const uint64_t tile = stage[s].tile;
         if (tile == ZP_NONE) {
-            /* tell the placer there is nothing more (once it has read the slot) */
-            if (tid == 0) {
-                ring_wait(&ring->placed, it >= 1 ? it - 1 : 0u, a.w.err);
-                ring_publish(ring, it, ZP_NONE, 0, 0, 0);
-            }
+            if (tid == 0) ring4_sized(ring, it, ZP_NONE, 0, 0, a.w.err); /* nothing more */
             break;
         }
-        const HomAddJob &J = hj[it & 1u];
+        const uint32_t job = stage[s].job;
+        const HomAddJob &J = job_of(a, job);
         const ZGeom &g = J.g;
         const uint32_t P = J.P;
         ZTile z;
         zg_tile(&g, tile, &z);
         const bool own = tid < z.nblk;
-        const uint32_t n = cur.n;
-        const bool full = FAST && own && n == 32;
+        const uint32_t n = own ? zg_block_len(z.seg_len, L, z.blk0 + tid) : 0u;
+        const bool full32 = FAST && own && n == 32;
         if (FAST) {
 #pragma unroll
             for (int j = 0; j < 32; j++) acc[j] = 0;
@@ -197,20 +211,13 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const __grid_constant__ HomAd
         uint32_t hsum = 0, qsum = 0, nzmask = 0;
         const uint32_t headb = z.has_head ? 4u : 0u;
 
-        uint32_t ticket = 0; /* the next tile's, taken before the last input and used after it */
-        for (uint32_t p = 0; p < P; p++, ld++) {
-            const uint32_t cb = ld & 1u;
-            if (p + 1 == P && tid == 0) ticket = atomicAdd(a.w.ticket, 1u);
-            /* the next input's copy runs while this one is added */
-            BlockSlot nxt = {0, 0, 0};
-            if (p + 1 < P)
-                nxt = stage_input(J, tile, p + 1, smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u],
-                                  wsum, &s_base[cb ^ 1u], bad);
+        for (uint32_t p = 0; p < P; p++, seq++) {
+            s = seq & 1u;
+            if (p) mbar_wait(&full[s], (seq >> 1) & 1u, a.w.err);
             if (J.qprev_valid && tid == 0) qsum += (uint32_t)J.in[p].tile_qprev[tile];
-            mbar_wait(&bar[cb], (ld >> 1) & 1u, a.w.err);
-            const uint8_t *buf = smem + (cb ? a.sm.in1 : a.sm.in0);
+            const uint8_t *buf = s ? buf1 : buf0;
             const uint32_t *sw = reinterpret_cast<const uint32_t *>(buf);
-            const uint32_t ph = (uint32_t)((uintptr_t)(J.in[p].bytes + s_base[cb]) & 15u);
+            const uint32_t ph = stage[s].ph;
             if (z.has_head && tid == 0) {
                 uint32_t h = 0;
 #pragma unroll
@@ -218,11 +225,11 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const __grid_constant__ HomAd
                 hsum += h;
             }
             if (own) {
-                const uint32_t b = cur.b, o = ph + headb + cur.off;
+                const uint32_t e = (s ? btab1 : btab0)[tid], b = e & 0xFFu, o = ph + headb + (e >> 8);
                 if (buf[o] != b) bad |= ZERR_CORRUPT;
                 if (b) {
                     nzmask |= 1u << (p & 31);
-                    if (full) {
+                    if (full32) {
                         uint32_t v[32];
                         decode_full(sw, o, b, v);
 #pragma unroll
@@ -235,28 +242,8 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const __grid_constant__ HomAd
                     }
                 }
             }
-            cur = nxt;
-            /* the buffer just read is refilled by the copy staged next round,
-             * after that round's scan has synchronised every compute thread */
-        }
-
-        /* the claimed next tile: its first input's widths and offset load
-         * while this sum's widths are found */
-        HomAddJob &Jn = hj[(it + 1) & 1u];
-        take_ticket(a, ticket, s_tile, s_job, &Jn);
-        named_sync(1, NC);
-        const uint64_t next = *s_tile;
-        const uint32_t next_job = *s_job;
-        ZTile zn;
-        uint32_t wn = 0, nn = 0;
-        uint64_t basen = 0;
-        if (next != ZP_NONE) {
-            zg_tile(&Jn.g, next, &zn);
-            if (tid < zn.nblk) {
-                nn = zg_block_len(zn.seg_len, Jn.g.L, zn.blk0 + tid);
-                wn = Jn.in[0].widths[zn.gblk0 + tid];
-            }
-            if (tid == 0) basen = Jn.in[0].tile_off[next];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[s]); /* this warp is done with the buffer */
         }
 
         /* branch-case counters of the two-input add (ZCCLd_float.c:2175-2764) */
@@ -274,7 +261,7 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const __grid_constant__ HomAd
         }
         /* width of the sum, offsets in the tile, early size publication */
         uint32_t b = 0, size = 0, smask = 0;
-        if (full) {
+        if (full32) {
             uint32_t mx = 0;
 #pragma unroll
             for (int j = 0; j < 32; j++) {
@@ -293,41 +280,24 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const __grid_constant__ HomAd
             b = width_of(mx, a.wt);
             size = zg_block_bytes(b, n);
         }
-        /* one scan for this sum's block offsets and the next tile's first input's */
-        uint32_t sizen = 0;
-        if (wn > 32) {
-            bad |= ZERR_CORRUPT;
-            wn = 0;
-        }
-        if (next != ZP_NONE && tid < zn.nblk) sizen = zg_block_bytes(wn, nn);
-        uint32_t total, off, offn, totaln;
-        grp_excl_scan2(size, sizen, wsum, ws1, off, offn, total, totaln, NC, 1);
+        uint32_t total;
+        const uint32_t off = grp_excl_scan1(size, (it & 1u) ? wsum1 : wsum0, &total, NC, 1);
         total += headb;
-        if (next != ZP_NONE) { /* every input of this tile is decoded: the buffer is free */
-            if (tid == 0)
-                issue_input(Jn.in[0], basen, totaln + (zn.has_head ? 4u : 0u), ld & 1u ? buf1 : buf0,
-                            &bar[ld & 1u], &s_base[ld & 1u], bad);
-            cur.b = wn;
-            cur.n = nn;
-            cur.off = offn;
-        }
         if (warp == 0) lb_publish(J.status, tile, total, tile == 0, 0);
+        if (tid == 0) ring4_sized(ring, it, tile, job, total, a.w.err); /* the placer's look-back starts */
         if (own) J.idx.widths[z.gblk0 + tid] = (uint8_t)b;
         if (tid == 0 && J.qprev_valid) J.idx.tile_qprev[tile] = (int32_t)qsum;
 
-        /* take room for the packed sum in the ring (waiting, if need be, for
-         * the placer to write out an earlier one) and pack this sum while
-         * the next tile's first input arrives */
-        if (tid == 0) *s_pos = ring_reserve(ring, it, zg_ring_need(total), R, pos_prev, end_prev, a.w.err);
-        named_sync(1, NC);
-        const uint32_t pos = *s_pos;
+        /* room for the packed sum in the ring: every thread finds the same
+         * place and waits, if need be, for the placer to have written out
+         * (and zeroed) what was there */
+        uint32_t mend;
+        const uint32_t pos = ring4_space(ring, zg_ring_need(total), R, H, hp, mend, a.w.err);
         uint8_t *pk = outs + pos;
         const uint32_t pk_sa = smem_u32(pk);
-        smem_zero(pk, total + 8, tid, NC);
-        named_sync(1, NC);
         if (z.has_head && tid == 0) *reinterpret_cast<uint32_t *>(pk) = hsum;
         const uint32_t o = headb + off;
-        if (full) {
+        if (full32) {
             encode_full(pk_sa, o, b, smask, acc);
         } else if (own) {
             encode_any(pk_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
@@ -336,10 +306,9 @@ __global__ void __launch_bounds__(288, 2) k_homadd(const __grid_constant__ HomAd
                 mg = (uint32_t)abs((int32_t)v);
             });
         }
-        named_sync(1, NC); /* the packed sum is complete; acc_rows are free */
-        if (tid == 0) ring_publish(ring, it, tile, job, total, pos);
-        tile = next;
-        job = next_job;
+        if (tid == 0) ring4_where(ring, it, pos, mend);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&ring->packed[it % ZR_SLOTS]); /* this warp's blocks are packed */
     }
     if (bad) atomicOr(a.w.err, bad);
 }
@@ -352,7 +321,7 @@ cudaError_t launch_homadd(const HomAddArgs &a, cudaStream_t st)
     const void *fn = fast ? (const void *)k_homadd<true> : (const void *)k_homadd<false>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
     if (e != cudaSuccess) return e;
-    const unsigned threads = a.job.g.TB + 32; /* compute warps and the placer warp */
+    const unsigned threads = a.job.g.TB + 64; /* adding warps, the placer warp, the loader warp */
     const uint64_t tiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
     unsigned grid = persistent_grid(fn, threads, a.sm.total, tiles);
     if (a.grid && a.grid < grid) grid = a.grid;

@@ -98,6 +98,17 @@ struct alignas(16) HomAddJob {
     uint64_t *status; /* look-back words of the output, one per tile */
 };
 
+/* One staged input tile of the homomorphic add: which tile and input it
+ * is, and where its bytes start within the buffer (the TMA copy keeps the
+ * source's 16-byte phase). */
+struct HStage {
+    uint64_t tile; /* within its job; ZP_NONE: no more tiles */
+    uint32_t job;
+    uint32_t p;    /* the input */
+    uint32_t ph;   /* the tile's first byte in the buffer */
+    uint32_t pad[3];
+};
+
 struct HomAddArgs {
     HomAddJob job; /* the single job (batch.jobs == null) */
     ZBatch batch;
@@ -251,6 +262,79 @@ __device__ __forceinline__ void ring_publish(ZRing *ring, uint32_t k, uint64_t t
     ring_set(&ring->packed, k + 1);
 }
 
+/* ------------------------------------------------------------------
+ * The same hand-off with early sizes and four slots.  A tile's identity and
+ * size go to the placer (mbarrier `sized`, one arrival by thread 0) right
+ * after the scan has found them, so the placer's look-back runs while the
+ * tile is still being packed; `packed` (one arrival per packing warp) then
+ * hands over its bytes.  Ring space is counted in running bytes: a tile
+ * takes the next `need` bytes (skipping to the ring's start when it would
+ * not fit before the end) and may be written once the placer's running
+ * count of released bytes, `tail`, shows that the space is free.  Up to
+ * four packed tiles wait at once.
+ * ------------------------------------------------------------------ */
+#define ZR_SLOTS 4u
+
+struct ZRing4 {
+    uint32_t placed; /* tiles written out (placer lane 0, release) */
+    uint32_t tail;   /* running count of released ring bytes (release) */
+    uint32_t total[ZR_SLOTS], pos[ZR_SLOTS], mend[ZR_SLOTS], job[ZR_SLOTS];
+    uint64_t tile[ZR_SLOTS];
+    uint64_t sized[ZR_SLOTS], packed[ZR_SLOTS]; /* mbarriers */
+};
+
+/* Thread 0, before the CTA's first barrier. */
+__device__ __forceinline__ void ring4_init(ZRing4 *r, uint32_t packers)
+{
+    r->placed = 0;
+    r->tail = 0;
+    for (uint32_t i = 0; i < ZR_SLOTS; i++) {
+        mbar_init(&r->sized[i], 1);
+        mbar_init(&r->packed[i], packers);
+    }
+}
+
+/* Thread 0: tile k's identity and size for the placer, once the placer is
+ * done with tile k - ZR_SLOTS, the previous user of the slot.  ZP_NONE as
+ * `tile` ends the placer. */
+__device__ __forceinline__ void ring4_sized(ZRing4 *r, uint32_t k, uint64_t tile, uint32_t job, uint32_t total,
+                                            uint32_t *err)
+{
+    if (k >= ZR_SLOTS) ring_wait(&r->placed, k - ZR_SLOTS + 1, err);
+    const uint32_t s = k % ZR_SLOTS;
+    r->tile[s] = tile;
+    r->job[s] = job;
+    r->total[s] = total;
+    mbar_arrive(&r->sized[s]);
+}
+
+/* Every packing thread (the same result in each): the ring position of the
+ * next tile of `need` bytes, after waiting until its bytes are free.  H is
+ * the running count of ring bytes taken (compared with wrap-around) and hp
+ * the ring position after the last tile; *mend receives the tile's running
+ * end. */
+__device__ __forceinline__ uint32_t ring4_space(ZRing4 *r, uint32_t need, uint32_t R, uint32_t &H, uint32_t &hp,
+                                                uint32_t &mend, uint32_t *err)
+{
+    uint32_t M = H, pos = hp;
+    if (pos + need > R) { /* skip the ring's end */
+        M += R - pos;
+        pos = 0;
+    }
+    H = M + need;
+    hp = pos + need;
+    mend = H;
+    ring_wait(&r->tail, M + need - R, err);
+    return pos;
+}
+
+/* Thread 0, before its warp's `packed` arrival: where tile k lies. */
+__device__ __forceinline__ void ring4_where(ZRing4 *r, uint32_t k, uint32_t pos, uint32_t mend)
+{
+    r->pos[k % ZR_SLOTS] = pos;
+    r->mend[k % ZR_SLOTS] = mend;
+}
+
 /* What the placer needs of a job. */
 struct ZPlace {
     ZGeom g;
@@ -260,20 +344,31 @@ struct ZPlace {
     uint64_t *status;
 };
 
+/* Shared bytes of the homomorphic add's job region: the placer's job, two
+ * stage records and two block tables (offset << 8 | width per block). */
+static inline uint32_t homadd_job_bytes(uint32_t TB)
+{
+    return zg_a16((uint32_t)sizeof(ZPlace)) + 2u * (uint32_t)sizeof(HStage) + 2u * TB * 4u;
+}
+
+
 /* The placer warp: for every packed tile, in order, the decoupled look-back
  * gives its byte offset in its stream; its bytes go out with 16-byte vector
  * stores realigned to that offset, with its offset in the side index, the
  * stream size after the stream's last tile and, for a segment's first tile,
- * the chunk offset in the header.  fetch(job, ZPlace *) (lane 0) copies a
- * job's placement data into shared memory. */
-template <class Fetch>
-__device__ __forceinline__ void placer_loop(ZRing *ring, const uint8_t *ringb, ZPlace *pj, uint32_t *err,
-                                            uint64_t max_tiles, uint32_t &bad, Fetch fetch)
+ * the chunk offset in the header.  wait_packed(k) (all lanes) returns once
+ * tile k is packed; fetch(job, ZPlace *) (lane 0) copies a job's placement
+ * data into shared memory.  With `zero`, the ring bytes of a tile are set
+ * back to zero once written out, so the packers find zeroed space. */
+template <class Wait, class Fetch>
+__device__ __forceinline__ void placer_loop(ZRing *ring, uint8_t *ringb, ZPlace *pj, uint32_t *err,
+                                            uint64_t max_tiles, uint32_t &bad, bool zero, Wait wait_packed,
+                                            Fetch fetch)
 {
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t cur_job = 0xFFFFFFFFu;
     for (uint64_t k = 0; k <= max_tiles; k++) {
-        if (lane == 0) ring_wait(&ring->packed, (uint32_t)k + 1, err);
+        wait_packed(k);
         __syncwarp();
         const uint32_t slot = (uint32_t)k & 1u;
         const uint64_t t = ring->tile[slot];
@@ -301,8 +396,62 @@ __device__ __forceinline__ void placer_loop(ZRing *ring, const uint8_t *ringb, Z
             if (t == g.ntiles - 1) *pj->idx.size = base + total;
         }
         if (fits) store_realign(pj->out + base, ringb + pos, total, lane, 32);
+        if (zero) {
+            __syncwarp(); /* every lane has read the tile */
+            uint4 *zr = reinterpret_cast<uint4 *>(ringb + pos);
+            for (uint32_t i = lane; i < zg_ring_need(total) / 16u; i += 32) zr[i] = make_uint4(0, 0, 0, 0);
+        }
         __syncwarp();
         if (lane == 0) ring_set(&ring->placed, (uint32_t)k + 1);
+    }
+}
+
+/* The placer warp on a ZRing4: for tile k, the look-back starts as soon
+ * as its size is known; the side-index entries follow, and once the tile is
+ * packed its bytes go out and its ring bytes are zeroed and released. */
+template <class Fetch>
+__device__ __forceinline__ void placer_loop4(ZRing4 *r, uint8_t *ringb, ZPlace *pj, uint32_t *err,
+                                             uint64_t max_tiles, uint32_t &bad, Fetch fetch)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t cur_job = 0xFFFFFFFFu;
+    for (uint64_t k = 0; k <= max_tiles; k++) {
+        const uint32_t s = (uint32_t)(k % ZR_SLOTS), par = (uint32_t)(k / ZR_SLOTS) & 1u;
+        mbar_wait(&r->sized[s], par, err);
+        const uint64_t t = r->tile[s];
+        const uint32_t job = r->job[s], total = r->total[s];
+        if (t == ZP_NONE) break;
+        if (job != cur_job) {
+            if (lane == 0) fetch(job, pj);
+            __syncwarp();
+            cur_job = job;
+        }
+        const ZGeom &g = pj->g;
+        const uint64_t base = 8ull * g.T + lb_resolve(pj->status, t, total, t == 0, 0, err);
+        const bool fits = base + total <= pj->cap;
+        if (!fits) bad |= ZERR_CAPACITY;
+        if (lane == 0) {
+            ZTile z;
+            zg_tile(&g, t, &z);
+            pj->idx.tile_off[t] = base;
+            if (fits && z.has_head && z.seg < g.T) {
+                const uint64_t h = base - 8ull * g.T;
+#pragma unroll
+                for (int k8 = 0; k8 < 8; k8++) pj->out[8ull * z.seg + k8] = (uint8_t)(h >> (8 * k8));
+            }
+            if (t == g.ntiles - 1) *pj->idx.size = base + total;
+        }
+        mbar_wait(&r->packed[s], par, err);
+        const uint32_t pos = r->pos[s], mend = r->mend[s];
+        if (fits) store_realign(pj->out + base, ringb + pos, total, lane, 32);
+        __syncwarp(); /* every lane has read the tile */
+        uint4 *zr = reinterpret_cast<uint4 *>(ringb + pos);
+        for (uint32_t i = lane; i < zg_ring_need(total) / 16u; i += 32) zr[i] = make_uint4(0, 0, 0, 0);
+        __syncwarp();
+        if (lane == 0) {
+            ring_set(&r->tail, mend);
+            ring_set(&r->placed, (uint32_t)k + 1);
+        }
     }
 }
 
