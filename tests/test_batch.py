@@ -105,3 +105,30 @@ def test_batch_matches_single_calls_and_graph_replay(torch):
     bc.check()
     bh.check()
     check_all()
+
+
+@pytest.mark.gpu
+def test_batch_one_cta_uneven_sums_wrap_the_ring(torch):
+    """One CTA takes every tile in ticket order, so packed sums of very
+    different sizes follow each other through its output ring: a small sum
+    (widths 8) and then one of widths 23, too large for the rest of the ring
+    and larger than the part the small one used, which has to start at the
+    ring's beginning once everything before it is out."""
+    rng = np.random.default_rng(9)
+    n, T, eb = 8193, 1, 1.0  # one full tile per buffer; integer values are exact
+    codec = Z.Codec(n, 32, T)
+    jobs, singles = [], []
+    for w in (6, 21, 6, 21, 21, 6):
+        xs = [torch.from_numpy(rng.integers(-(1 << (w - 1)), 1 << (w - 1), n).astype(np.float32)).cuda()
+              for _ in range(2)]
+        ins = [codec.compress(x, eb) for x in xs]
+        singles.append(codec.homadd(ins))
+        jobs.append((ins, T, codec.new_stream()))
+    codec.check()
+    bh = Z.Batch(Z.BATCH_HOMADD, jobs)
+    bh.desc.grid = 1
+    bh.run()
+    bh.check()
+    for (ins, _, out), s in zip(jobs, singles):
+        assert out.tobytes() == s.tobytes()
+        assert torch.equal(out.index, s.index)

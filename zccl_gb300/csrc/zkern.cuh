@@ -316,6 +316,7 @@ __device__ __forceinline__ void ring4_sized(ZRing4 *r, uint32_t k, uint64_t tile
 __device__ __forceinline__ uint32_t ring4_space(ZRing4 *r, uint32_t need, uint32_t R, uint32_t &H, uint32_t &hp,
                                                 uint32_t &mend, uint32_t *err)
 {
+    const uint32_t H0 = H;
     uint32_t M = H, pos = hp;
     if (pos + need > R) { /* skip the ring's end */
         M += R - pos;
@@ -324,7 +325,12 @@ __device__ __forceinline__ uint32_t ring4_space(ZRing4 *r, uint32_t need, uint32
     H = M + need;
     hp = pos + need;
     mend = H;
-    ring_wait(&r->tail, M + need - R, err);
+    /* the bytes' previous contents end at running byte M + need - R, but
+     * nothing past H0 was ever written: after a skip the requirement is at
+     * most that every earlier tile is out */
+    uint32_t req = M + need - R;
+    if ((int32_t)(req - H0) > 0) req = H0;
+    ring_wait(&r->tail, req, err);
     return pos;
 }
 
