@@ -454,12 +454,15 @@ __device__ __forceinline__ void mbar_arrive_n(uint64_t *bar, uint32_t n)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(n) : "memory");
 }
 
-/* Wait for phase `parity` of the barrier to complete.  Gives up after a
- * bounded number of polls and reports ZERR_TIMEOUT instead of hanging. */
+/* Wait for phase `parity` of the barrier to complete.  Gives up after about
+ * 2^32 SM clock cycles (two seconds or more) and reports ZERR_TIMEOUT
+ * instead of hanging; a wait that spans other stages of a pipeline (which
+ * may themselves wait on other CTAs) stays well inside that limit. */
 __device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t parity, uint32_t *err)
 {
     uint32_t addr = smem_u32(bar);
-    for (uint32_t it = 0; it < (1u << 21); it++) {
+    const long long t0 = clock64();
+    for (uint32_t it = 0; it < (1u << 30); it++) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n"
@@ -469,6 +472,7 @@ __device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t parity, uint32
             : "r"(addr), "r"(parity)
             : "memory");
         if (done) return;
+        if (clock64() - t0 > (1ll << 32)) break;
     }
     atomicOr(err, ZERR_TIMEOUT);
 }
