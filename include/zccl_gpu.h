@@ -169,6 +169,14 @@ int zccl_gpu_build_index(zccl_gpu_stream *s, size_t n, int L, int T, void *d_ws,
 int zccl_gpu_stream_size(const zccl_gpu_stream *s, size_t n, int L, int T, size_t *size,
                          void *cuda_stream);
 
+/* Segment framing of the segmented ring allgatherv
+ * (MPIR_Allgatherv_intra_ring_RI2_mt_oa_record_seg, ZCCL/src/ZCCL_ring.c:1599-1774):
+ * a compressed segment travels as its size (size_t, little-endian) followed by
+ * its stream bytes (ZCCL_ring.c:1672-1673).  Enqueues on cuda_stream a device
+ * copy of s's total size, once s has been produced on that stream, into the
+ * 8 bytes at d_frame; no synchronization. */
+int zccl_gpu_frame_size(const zccl_gpu_stream *s, void *d_frame, void *cuda_stream);
+
 /* Synchronize cuda_stream and turn the workspace's device error bits into a
  * status code (ZCCL_GPU_OK when none). */
 int zccl_gpu_check(void *d_ws, void *cuda_stream);

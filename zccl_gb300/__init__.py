@@ -36,7 +36,7 @@ EXPORTS = [
     "ZCCL_float_homomophic_add_openmp_threadblock", "ZCCL_float_homomophic_add_single_thread",
     "zccl_gpu_max_stream_bytes", "zccl_gpu_index_bytes", "zccl_gpu_workspace_bytes",
     "zccl_gpu_compress", "zccl_gpu_decompress", "zccl_gpu_homadd", "zccl_gpu_homadd_cases",
-    "zccl_gpu_build_index", "zccl_gpu_stream_size", "zccl_gpu_check", "zccl_gpu_last_status",
+    "zccl_gpu_build_index", "zccl_gpu_stream_size", "zccl_gpu_frame_size", "zccl_gpu_check", "zccl_gpu_last_status",
     "zccl_gpu_strerror", "zccl_gpu_width_table", "zccl_gpu_compress_noalloc",
     "zccl_gpu_batch_bytes", "zccl_gpu_batch_plan", "zccl_gpu_batch_run", "zccl_gpu_batch_tune",
     "zccl_gpu_batch_check",
@@ -101,6 +101,7 @@ def lib() -> ctypes.CDLL:
         "zccl_gpu_homadd_cases": (i, [sp, sp, i, sz, i, i, vp, vp, vp]),
         "zccl_gpu_build_index": (i, [sp, sz, i, i, vp, vp]),
         "zccl_gpu_stream_size": (i, [sp, sz, i, i, ctypes.POINTER(sz), vp]),
+        "zccl_gpu_frame_size": (i, [sp, vp, vp]),
         "zccl_gpu_check": (i, [vp, vp]),
         "zccl_gpu_last_status": (i, []),
         "zccl_gpu_strerror": (ctypes.c_char_p, [i]),

@@ -365,6 +365,15 @@ extern "C" int zccl_gpu_stream_size(const zccl_gpu_stream *s, size_t n, int L, i
     return ZCCL_GPU_OK;
 }
 
+extern "C" int zccl_gpu_frame_size(const zccl_gpu_stream *s, void *d_frame, void *cuda_stream)
+{
+    if (!valid_stream(s) || !d_frame) return ZCCL_GPU_EINVAL;
+    /* the index starts with the stream's total size, a little-endian uint64 */
+    return cudaMemcpyAsync(d_frame, s->index, 8, cudaMemcpyDeviceToDevice, (cudaStream_t)cuda_stream) == cudaSuccess
+               ? ZCCL_GPU_OK
+               : ZCCL_GPU_ECUDA;
+}
+
 extern "C" int zccl_gpu_check(void *d_ws, void *cuda_stream)
 {
     if (!d_ws) return ZCCL_GPU_EINVAL;
