@@ -3,10 +3,13 @@
  *
  * Replaces ZCCL_float_decompress_openmp_threadblock_arg
  * (ZCCL/src/ZCCLd_float.c:538-754) and produces the same floats.  Persistent
- * CTAs, one thread per block, mirroring the compressor.  When the index
- * holds every tile's starting value the tiles are independent: CTA c takes
- * tiles c, c + grid, ... and loads the index entries of the tile after
- * next while it works; otherwise tiles go in ticket order for the look-back.
+ * CTAs, one thread per block, mirroring the compressor.  With the index
+ * holding every tile's starting value the tiles are independent: CTA c
+ * takes tiles c, c + grid, ... and loads the index entries of the tile
+ * after next while it works.  A stream that arrived as bytes gets those
+ * values first: the same kernel in its SUMS form writes every tile's delta
+ * sum into the index, and k_qprev_scan turns them, segment by segment, into
+ * starting values from the segment's raw head.
  * Per tile:
  *   1. for the NEXT tile: block sizes from the width index, a block-wide
  *      scan for every block's offset, and one TMA bulk copy of its bytes,
@@ -14,11 +17,8 @@
  *   2. every thread unpacks its block (sign bits, high bytes, low-bit
  *      stream, ZCCL/src/ZCCL_TypeManager.c:423-950) into int32 deltas;
  *   3. a block-wide scan of the per-block delta sums, started from the
- *      quantized value before the tile, restores the running values
- *      (ZCCLd_float.c:617-628); that starting value comes from the index
- *      when the stream was produced on the device, otherwise from a
- *      decoupled look-back over tile delta sums that restarts at every
- *      segment head, and is then written back into the index;
+ *      quantized value before the tile (from the index), restores the
+ *      running values (ZCCLd_float.c:617-628);
  *   4. x = (float)q * eb (ZCCLd_float.c:624) into padded rows, written out
  *      row by row with coalesced stores.
  */
@@ -105,21 +105,18 @@ __device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, uint64_
     return sl;
 }
 
-/* ORDERED: tiles in ticket order, needed when the starting values come from
- * the look-back (a CTA only ever waits on tiles claimed before its own).
- * Otherwise every tile is independent and CTA c takes tiles c, c + grid,
- * c + 2 grid, ..., with the index entries of the tile after next already
- * loading. */
-template <bool FAST, bool ORDERED>
+/* CTA c takes tiles c, c + grid, c + 2 grid, ..., with the index entries of
+ * the tile after next already loading.  SUMS: only each tile's wrapped sum of
+ * deltas, into the index's tile_qprev (k_qprev_scan completes it). */
+template <bool FAST, bool SUMS>
 __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, const __grid_constant__ CUtensorMap ymap)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem); /* [2] */
     uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 16);
-    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160);     /* [0] claimed tile, [2] q0 */
+    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160);     /* [2] the tile's starting value */
     uint64_t *s_base = reinterpret_cast<uint64_t *>(smem + 192); /* [2] */
     uint32_t *s_q0 = reinterpret_cast<uint32_t *>(smem + 208);   /* [2] */
-    uint64_t *rec = reinterpret_cast<uint64_t *>(smem + 256);
     uint32_t *ws1 = reinterpret_cast<uint32_t *>(smem + 320); /* [33] second scan scratch */
     float *rows = reinterpret_cast<float *>(smem + a.sm.rows);
 
@@ -144,15 +141,14 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
-        if (ORDERED) bc[0] = atomicAdd(a.w.ticket, 1u);
     }
     __syncthreads();
-    uint64_t tile = ORDERED ? bc[0] : blockIdx.x;
+    uint64_t tile = blockIdx.x;
     uint64_t tnext = tile + gridDim.x; /* the static order's next tile */
     TileIdx ix = load_idx(a, tile);
     BlockSlot cur = {0, 0, 0};
     if (tile < g.ntiles) cur = stage_tile(a, tile, ix, smem + a.sm.in0, &bar[0], wsum, &s_base[0], &s_q0[0], bad);
-    if (!ORDERED) ix = load_idx(a, tnext);
+    ix = load_idx(a, tnext);
 
     for (uint32_t it = 0;; it++) {
         const uint32_t cb = it & 1u;
@@ -161,17 +157,7 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
         ZTile z;
         zg_tile(&g, tile, &z);
 
-        /* 1. the next tile: its sizes, offsets and TMA copy */
-        if (ORDERED) {
-            if (tid == 0) bc[0] = atomicAdd(a.w.ticket, 1u);
-            __syncthreads();
-            tnext = bc[0];
-            ix = load_idx(a, tnext);
-        }
-        BlockSlot nxt = {0, 0, 0};
-        if (ORDERED && tnext < g.ntiles)
-            nxt = stage_tile(a, tnext, ix, smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u], wsum,
-                             &s_base[cb ^ 1u], &s_q0[cb ^ 1u], bad);
+        BlockSlot nxt = {0, 0, 0}; /* the next tile's block, found in step 3 */
 
         /* 2. unpack this tile's deltas */
         mbar_wait(&bar[cb], (it >> 1) & 1u, a.w.err);
@@ -203,9 +189,7 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
          *    block offsets come from the same scan (its widths arrived a tile
          *    ago), and its copy starts right after, into the other buffer. */
         uint32_t tsum, pre;
-        if (ORDERED) {
-            pre = cta_excl_scan(bsum, wsum, &tsum);
-        } else {
+        {
             ZTile zn;
             uint32_t sizen = 0;
             if (tnext < g.ntiles) {
@@ -227,17 +211,14 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
                            &s_base[cb ^ 1u], &s_q0[cb ^ 1u], bad);
             ix = load_idx(a, tnext + gridDim.x);
         }
-        if (a.qprev_valid) {
-            if (tid == 0) bc[2] = z.has_head ? (uint32_t)head : s_q0[cb];
-        } else {
-            if (warp == 0) lb_publish(a.w.status, tile, tsum, z.has_head != 0, (uint32_t)head);
-            const uint64_t q0 =
-                lb_resolve_cta(a.w.status, tile, tsum, z.has_head != 0, (uint32_t)head, a.w.err, rec);
-            if (tid == 0) {
-                bc[2] = (uint32_t)q0;
-                a.idx.tile_qprev[tile] = (int32_t)(uint32_t)q0;
-            }
+        if (SUMS) { /* the tile's delta sum; the values wait for the scan */
+            if (tid == 0) a.idx.tile_qprev[tile] = (int32_t)tsum;
+            cur = nxt;
+            tile = tnext;
+            tnext += gridDim.x;
+            continue;
         }
+        if (tid == 0) bc[2] = z.has_head ? (uint32_t)head : s_q0[cb];
         if (tid == 0) bulk_wait_read0(); /* the previous box has left the rows */
         __syncthreads();
         const uint32_t q0 = (uint32_t)bc[2];
@@ -309,10 +290,40 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
         }
         cur = nxt;
         tile = tnext;
-        if (!ORDERED) tnext += gridDim.x;
+        tnext += gridDim.x;
     }
     if (tid == 0) bulk_wait0();
     if (bad) atomicOr(a.w.err, bad);
+}
+
+/* One warp per segment: its tiles' delta sums (from k_decompress<_, true>)
+ * become the quantized value before each tile, starting from the
+ * segment's raw int32 head (the four bytes at its first tile's offset) and
+ * wrapping like the reference's int32 running value (ZCCLd_float.c:582-628). */
+__global__ void k_qprev_scan(const DecompressArgs a)
+{
+    const ZGeom &g = a.g;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t seg = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const uint64_t nseg = (uint64_t)g.T + (g.rem ? 1u : 0u);
+    if (seg >= nseg || *(volatile const uint32_t *)a.w.walk_err) return;
+    const uint64_t t0 = seg < g.T ? seg * g.nt_reg : (uint64_t)g.T * g.nt_reg;
+    const uint64_t nt = seg < g.T ? g.nt_reg : g.nt_rm;
+    const uint64_t off = a.idx.tile_off[t0];
+    uint32_t run = 0;
+    if (off <= a.avail && a.avail - off >= 4) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) run |= (uint32_t)a.in[off + k] << (8 * k);
+    } else if (lane == 0) {
+        atomicOr(a.w.err, ZERR_BOUNDS);
+    }
+    for (uint64_t k0 = 0; k0 < nt; k0 += 32) {
+        const uint64_t k = k0 + lane;
+        const uint32_t v = k < nt ? (uint32_t)a.idx.tile_qprev[t0 + k] : 0u;
+        const uint32_t inc = warp_incl_scan(v);
+        if (k < nt) a.idx.tile_qprev[t0 + k] = (int32_t)(run + inc - v);
+        run += __shfl_sync(0xffffffffu, inc, 31);
+    }
 }
 
 /* cuTensorMapEncodeTiled from the driver, looked up once. */
@@ -352,15 +363,30 @@ bool zk_rows_map(CUtensorMap *map, const void *p, uint64_t n)
 
 cudaError_t launch_decompress(const DecompressArgs &a, cudaStream_t st)
 {
-    const bool fast = a.g.L <= 32, ordered = !a.qprev_valid;
-    const void *fn = fast ? (ordered ? (const void *)k_decompress<true, true>
-                                     : (const void *)k_decompress<true, false>)
-                          : (ordered ? (const void *)k_decompress<false, true>
-                                     : (const void *)k_decompress<false, false>);
+    const bool fast = a.g.L <= 32;
+    /* a stream without starting values: tile sums, then the scan per segment */
+    if (!a.qprev_valid) {
+        const void *fs = fast ? (const void *)k_decompress<true, true> : (const void *)k_decompress<false, true>;
+        cudaError_t e = cudaFuncSetAttribute(fs, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
+        if (e != cudaSuccess) return e;
+        alignas(64) CUtensorMap none;
+        memset(&none, 0, sizeof none);
+        DecompressArgs b = a;
+        b.rows_map = 0;
+        void *args[] = {&b, &none};
+        e = cudaLaunchKernel(fs, dim3(persistent_grid(fs, a.g.TB, a.sm.total, a.g.ntiles)), dim3(a.g.TB), args,
+                             a.sm.total, st);
+        if (e != cudaSuccess) return e;
+        const unsigned nseg = a.g.T + (a.g.rem ? 1u : 0u);
+        k_qprev_scan<<<(nseg + 3) / 4, 128, 0, st>>>(a);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    const void *fn = fast ? (const void *)k_decompress<true, false> : (const void *)k_decompress<false, false>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
     if (e != cudaSuccess) return e;
     unsigned grid = persistent_grid(fn, a.g.TB, a.sm.total, a.g.ntiles);
     DecompressArgs b = a;
+    b.qprev_valid = 1;
     alignas(64) CUtensorMap map;
     memset(&map, 0, sizeof map);
     b.rows_map = fast && zk_rows_map(&map, a.y, a.g.n);

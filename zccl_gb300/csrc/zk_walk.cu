@@ -96,7 +96,12 @@ __global__ void k_walk_setup(const WalkArgs a)
                             ok = false;
                         }
                     } else {
+                        /* the last chunk: no later start bounds it, but its
+                         * blocks take at most a segment's worst size (a
+                         * remainder segment follows them and is walked apart) */
                         R = a.avail < a.end_bound ? a.avail : a.end_bound;
+                        const uint64_t worst = P - 4 + zg_seg_worst(g.tbs, g.L);
+                        if (R > worst) R = worst;
                         if (R < P) R = P;
                     }
                 }
