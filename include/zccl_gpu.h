@@ -169,6 +169,39 @@ int zccl_gpu_build_index(zccl_gpu_stream *s, size_t n, int L, int T, void *d_ws,
 int zccl_gpu_stream_size(const zccl_gpu_stream *s, size_t n, int L, int T, size_t *size,
                          void *cuda_stream);
 
+/* ---- SZp 3-D codec, serial stream form --------------------------------
+ * Drop-ins for the reference's serial 3-D Lorenzo codec: a dim1 x dim2 x
+ * dim3 float volume (dim3 fastest) in blocks of blockSideLength^3 (1..32)
+ * with absolute error bound errorBound; the stream is one rate byte per
+ * block followed by the blocks' sign and fixed-length bits.  Host or device
+ * pointers, synchronous, status in zccl_gpu_last_status().
+ *   SZp_compress3D_fast   ZCCL/include/ZCCL_float.h:83-86  (ZCCL/src/ZCCL_float.c:1706)
+ *   SZp_compress3D        ZCCL/include/ZCCL_float.h:88-91  (ZCCL/src/ZCCL_float.c:1791), same stream
+ *   SZp_decompress3D      ZCCL/include/ZCCLd_float.h:40-43 (ZCCL/src/ZCCLd_float.c:2801)
+ *   SZp_decompress3D_fast ZCCL/include/ZCCLd_float.h:35-38 (declared there, defined nowhere in the
+ *                         reference; here the inverse of SZp_compress3D_fast, i.e. SZp_decompress3D) */
+void SZp_compress3D_fast(const float *oriData, unsigned char *cmpData, size_t dim1, size_t dim2, size_t dim3,
+                         int blockSideLength, double errorBound, size_t *cmpSize);
+void SZp_compress3D(const float *oriData, unsigned char *cmpData, size_t dim1, size_t dim2, size_t dim3,
+                    int blockSideLength, double errorBound, size_t *cmpSize);
+void SZp_decompress3D(float *decData, unsigned char *cmpData, size_t dim1, size_t dim2, size_t dim3,
+                      int blockSideLength, double errorBound);
+void SZp_decompress3D_fast(float *decData, unsigned char *cmpData, size_t dim1, size_t dim2, size_t dim3,
+                           int blockSideLength, double errorBound);
+
+/* Device API of the same codec: the largest stream, device scratch (the
+ * first 16 bytes hold the status words zccl_gpu_check() reads), and the two
+ * passes enqueued on cuda_stream.  compress writes the stream size to the
+ * device size_t at d_size when it is not null; capacity too small for the
+ * rate table gives ZCCL_GPU_ECAPACITY, too small for the payload a device
+ * status of the same code. */
+size_t zccl_gpu_szp3d_max_bytes(size_t d1, size_t d2, size_t d3, int bs);
+size_t zccl_gpu_szp3d_workspace_bytes(size_t d1, size_t d2, size_t d3, int bs);
+int zccl_gpu_szp3d_compress(unsigned char *d_out, size_t capacity, const float *d_in, size_t d1, size_t d2,
+                            size_t d3, int bs, double eb, void *d_ws, size_t *d_size, void *cuda_stream);
+int zccl_gpu_szp3d_decompress(float *d_out, const unsigned char *d_in, size_t avail, size_t d1, size_t d2,
+                              size_t d3, int bs, double eb, void *d_ws, void *cuda_stream);
+
 /* Segment framing of the segmented ring allgatherv
  * (MPIR_Allgatherv_intra_ring_RI2_mt_oa_record_seg, ZCCL/src/ZCCL_ring.c:1599-1774):
  * a compressed segment travels as its size (size_t, little-endian) followed by

@@ -338,3 +338,170 @@ void port_homadd(unsigned char *out, size_t *outSize, size_t nbEle, float absErr
     free(bufs);
     free(sizes);
 }
+
+/* ======================================================================
+ * SZp 3-D codec, serial form (SZp_compress3D_fast / SZp_compress3D,
+ * ZCCL/src/ZCCL_float.c:1706-1860; SZp_decompress3D, ZCCL/src/ZCCLd_float.c:2801-2871).
+ *
+ *   q(i,j,k) = (int)floor((double)x * (0.5 / eb) + 0.5)            (ZCCL_float.h:57-61)
+ *   e = the 3-D mixed difference of q, zero outside the volume     (ZCCL_float.h:63-73)
+ *   stream = one rate byte per block (blocks of bs^3 in x, y, z order, edge
+ *            blocks cut short), then per block of non-zero rate: its sign
+ *            bits and fixed-length magnitude bits, the fastmode1 packers'
+ *            layout (signs MSB-first, B = rate/8 high bytes little-endian,
+ *            r = rate%8 low bits MSB-first); rate = bit length of the
+ *            block's largest |e| (no log2f)
+ *   x' = (float)((double)q * (2 eb)), q the 3-D prefix sum of e   (ZCCLd_float.c:2807,2855-2857)
+ * Integer arithmetic wraps modulo 2^32 like the reference's int.
+ * ====================================================================== */
+
+static size_t pack_payload(unsigned char *o, const int32_t *e, size_t n, int b)
+{
+    int B = b / 8, r = b % 8;
+    unsigned char *p = o;
+    size_t ns = (n + 7) / 8;
+    memset(p, 0, ns);
+    for (size_t j = 0; j < n; j++)
+        if (e[j] < 0) p[j / 8] |= (unsigned char)(0x80u >> (j % 8));
+    p += ns;
+    for (size_t j = 0; j < n; j++) {
+        uint32_t v = magnitude(e[j]) >> r;
+        for (int k = 0; k < B; k++) *p++ = (unsigned char)(v >> (8 * k));
+    }
+    if (r) {
+        uint32_t mask = (1u << r) - 1u, acc = 0;
+        int nacc = 0;
+        for (size_t j = 0; j < n; j++) {
+            acc = (acc << r) | (magnitude(e[j]) & mask);
+            nacc += r;
+            if (nacc >= 8) {
+                nacc -= 8;
+                *p++ = (unsigned char)(acc >> nacc);
+            }
+        }
+        if (nacc) *p++ = (unsigned char)(acc << (8 - nacc));
+    }
+    return (size_t)(p - o);
+}
+
+static size_t unpack_payload(const unsigned char *s, size_t n, int b, int32_t *e)
+{
+    int B = b / 8, r = b % 8;
+    const unsigned char *sg = s, *hi = s + (n + 7) / 8, *lo = hi + (size_t)B * n;
+    uint32_t acc = 0;
+    int nacc = 0;
+    for (size_t j = 0; j < n; j++) {
+        uint32_t v = 0;
+        for (int k = 0; k < B; k++) v |= (uint32_t)hi[j * B + k] << (8 * k);
+        v <<= r;
+        if (r) {
+            while (nacc < r) {
+                acc = (acc << 8) | *lo++;
+                nacc += 8;
+            }
+            nacc -= r;
+            v |= (acc >> nacc) & ((1u << r) - 1u);
+        }
+        int neg = (sg[j / 8] >> (7 - j % 8)) & 1;
+        e[j] = (int32_t)(neg ? 0u - v : v);
+    }
+    return (n + 7) / 8 + (size_t)B * n + ((size_t)r * n + 7) / 8;
+}
+
+static int bit_length(uint32_t m)
+{
+    int b = 0;
+    while (m) {
+        b++;
+        m >>= 1;
+    }
+    return b;
+}
+
+/* q over the volume with a zero plane before each axis: index (i+1, j+1, k+1). */
+#define ZP3(i, j, k) ((((size_t)(i)) * (d2 + 1) + (size_t)(j)) * (d3 + 1) + (size_t)(k))
+
+void port_szp3d_compress(const float *x, unsigned char *out, size_t d1, size_t d2, size_t d3, int bs,
+                         double eb, size_t *cmpSize)
+{
+    const double inv = 0.5 / eb;
+    uint32_t *q = (uint32_t *)calloc((d1 + 1) * (d2 + 1) * (d3 + 1), sizeof(uint32_t));
+    for (size_t i = 0; i < d1; i++)
+        for (size_t j = 0; j < d2; j++)
+            for (size_t k = 0; k < d3; k++) {
+                double v = floor((double)x[(i * d2 + j) * d3 + k] * inv + 0.5);
+                q[ZP3(i + 1, j + 1, k + 1)] = (uint32_t)(int32_t)v;
+            }
+    const size_t nb1 = (d1 - 1) / bs + 1, nb2 = (d2 - 1) / bs + 1, nb3 = (d3 - 1) / bs + 1;
+    int32_t *e = (int32_t *)malloc((size_t)bs * bs * bs * sizeof(int32_t));
+    unsigned char *p = out + nb1 * nb2 * nb3;
+    size_t blk = 0;
+    for (size_t bx = 0; bx < nb1; bx++)
+        for (size_t by = 0; by < nb2; by++)
+            for (size_t bz = 0; bz < nb3; bz++) {
+                size_t n = 0;
+                uint32_t m = 0;
+                for (size_t i = bx * bs; i < d1 && i < (bx + 1) * bs; i++)
+                    for (size_t j = by * bs; j < d2 && j < (by + 1) * bs; j++)
+                        for (size_t k = bz * bs; k < d3 && k < (bz + 1) * bs; k++) {
+                            uint32_t v = q[ZP3(i + 1, j + 1, k + 1)] - q[ZP3(i + 1, j + 1, k)] -
+                                         q[ZP3(i + 1, j, k + 1)] + q[ZP3(i + 1, j, k)] -
+                                         q[ZP3(i, j + 1, k + 1)] + q[ZP3(i, j + 1, k)] +
+                                         q[ZP3(i, j, k + 1)] - q[ZP3(i, j, k)];
+                            e[n++] = (int32_t)v;
+                            uint32_t a = magnitude((int32_t)v);
+                            if (a > m) m = a;
+                        }
+                int b = bit_length(m);
+                out[blk++] = (unsigned char)b;
+                if (b) p += pack_payload(p, e, n, b);
+            }
+    *cmpSize = (size_t)(p - out);
+    free(e);
+    free(q);
+}
+
+void port_szp3d_decompress(float *y, const unsigned char *cmp, size_t d1, size_t d2, size_t d3, int bs,
+                           double eb)
+{
+    const double twice = eb * 2;
+    uint32_t *q = (uint32_t *)calloc((d1 + 1) * (d2 + 1) * (d3 + 1), sizeof(uint32_t));
+    const size_t nb1 = (d1 - 1) / bs + 1, nb2 = (d2 - 1) / bs + 1, nb3 = (d3 - 1) / bs + 1;
+    int32_t *e = (int32_t *)malloc((size_t)bs * bs * bs * sizeof(int32_t));
+    const unsigned char *p = cmp + nb1 * nb2 * nb3;
+    size_t blk = 0;
+    for (size_t bx = 0; bx < nb1; bx++)
+        for (size_t by = 0; by < nb2; by++)
+            for (size_t bz = 0; bz < nb3; bz++) {
+                const size_t sx = (bx + 1) * bs < d1 ? bs : d1 - bx * bs;
+                const size_t sy = (by + 1) * bs < d2 ? bs : d2 - by * bs;
+                const size_t sz = (bz + 1) * bs < d3 ? bs : d3 - bz * bs;
+                const size_t n = sx * sy * sz;
+                int b = cmp[blk++];
+                if (b)
+                    p += unpack_payload(p, n, b, e);
+                else
+                    memset(e, 0, n * sizeof(int32_t));
+                size_t t = 0;
+                for (size_t i = bx * bs; i < bx * bs + sx; i++)
+                    for (size_t j = by * bs; j < by * bs + sy; j++)
+                        for (size_t k = bz * bs; k < bz * bs + sz; k++)
+                            q[ZP3(i + 1, j + 1, k + 1)] = (uint32_t)e[t++];
+            }
+    /* the 3-D prefix sum, one axis at a time */
+    for (size_t i = 1; i <= d1; i++)
+        for (size_t j = 1; j <= d2; j++)
+            for (size_t k = 1; k <= d3; k++) q[ZP3(i, j, k)] += q[ZP3(i, j, k - 1)];
+    for (size_t i = 1; i <= d1; i++)
+        for (size_t j = 1; j <= d2; j++)
+            for (size_t k = 1; k <= d3; k++) q[ZP3(i, j, k)] += q[ZP3(i, j - 1, k)];
+    for (size_t i = 1; i <= d1; i++)
+        for (size_t j = 1; j <= d2; j++)
+            for (size_t k = 1; k <= d3; k++) {
+                q[ZP3(i, j, k)] += q[ZP3(i - 1, j, k)];
+                y[((i - 1) * d2 + (j - 1)) * d3 + (k - 1)] = (float)((double)(int32_t)q[ZP3(i, j, k)] * twice);
+            }
+    free(e);
+    free(q);
+}
+#undef ZP3

@@ -37,6 +37,17 @@ void port_homadd(unsigned char *out, size_t *outSize, size_t nbEle, float absErr
  * 0 when m == 0, else (int)log2f((float)m) + 1 (ZCCL/src/ZCCL_float.c:606). */
 int port_width(uint32_t m);
 
+/* SZp 3-D codec, serial form: compress a dim1 x dim2 x dim3 volume (dim3
+ * fastest) in blocks of bs^3 with absolute error bound eb; *cmpSize is
+ * assigned.  ZCCL/src/ZCCL_float.c:1706-1860 (SZp_compress3D_fast and
+ * SZp_compress3D write the same stream). */
+void port_szp3d_compress(const float *x, unsigned char *out, size_t d1, size_t d2, size_t d3, int bs,
+                         double eb, size_t *cmpSize);
+
+/* Its inverse, ZCCL/src/ZCCLd_float.c:2801-2871 (SZp_decompress3D). */
+void port_szp3d_decompress(float *y, const unsigned char *cmp, size_t d1, size_t d2, size_t d3, int bs,
+                           double eb);
+
 #ifdef __cplusplus
 }
 #endif

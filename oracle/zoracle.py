@@ -86,6 +86,19 @@ class _Codec:
             self._set_threads.argtypes = [ctypes.c_int]
         for f in (self._c, self._d, self._h):
             f.restype = None
+        # the serial SZp 3-D codec (ZCCL/src/ZCCL_float.c:1706-1860, ZCCLd_float.c:2801-2871)
+        c3 = [_f32p, _u8p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int,
+              ctypes.c_double, _szp]
+        d3 = [_f32p, _u8p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int, ctypes.c_double]
+        names = ({"fast": "port_szp3d_compress", "plain": "port_szp3d_compress"}, "port_szp3d_decompress") \
+            if kind == "port" else ({"fast": "SZp_compress3D_fast", "plain": "SZp_compress3D"}, "SZp_decompress3D")
+        self._c3 = {}
+        for k, nm in names[0].items():
+            f = getattr(self.lib, nm)
+            f.argtypes, f.restype = c3, None
+            self._c3[k] = f
+        self._d3 = getattr(self.lib, names[1])
+        self._d3.argtypes, self._d3.restype = d3, None
 
     def _args_T(self, T):
         if self.kind == "port":
@@ -119,6 +132,26 @@ class _Codec:
         self._h(_ptr(out, _u8p), ctypes.byref(size), ctypes.c_size_t(n), ctypes.c_float(eb),
                 ctypes.c_int(L), _ptr(a, _u8p), _ptr(b, _u8p), *self._args_T(T))
         return out[: size.value].tobytes()
+
+    def szp3d_compress(self, x: np.ndarray, dims, bs: int, eb: float, form: str = "fast") -> bytes:
+        x = np.ascontiguousarray(x, dtype=np.float32).ravel()
+        n = int(np.prod(dims))
+        nb = 1
+        for d in dims:
+            nb *= (d - 1) // bs + 1
+        out = np.zeros(nb + nb * (bs ** 3) * 5 + 64, dtype=np.uint8)  # rates + worst payloads
+        size = ctypes.c_size_t(0)
+        assert x.size == n
+        self._c3[form](_ptr(x, _f32p), _ptr(out, _u8p), *[ctypes.c_size_t(d) for d in dims],
+                       ctypes.c_int(bs), ctypes.c_double(eb), ctypes.byref(size))
+        return out[: size.value].tobytes()
+
+    def szp3d_decompress(self, stream: bytes, dims, bs: int, eb: float) -> np.ndarray:
+        buf = np.concatenate([np.frombuffer(stream, dtype=np.uint8), np.zeros(64, np.uint8)])
+        y = np.zeros(int(np.prod(dims)), dtype=np.float32)
+        self._d3(_ptr(y, _f32p), _ptr(buf, _u8p), *[ctypes.c_size_t(d) for d in dims], ctypes.c_int(bs),
+                 ctypes.c_double(eb))
+        return y
 
     def homadd_fold(self, streams, n: int, eb: float, L: int, T: int) -> bytes:
         """P-way sum folded pairwise the way the ring's reduce-scatter does it

@@ -1,0 +1,104 @@
+"""The SZp 3-D codec (serial stream form): the oracle port against the
+reference's golden streams on the CPU, and the CUDA path, through the C ABI
+and the drop-in entry points, against both on the GPU.  Streams bit for
+bit, decompressed floats by digest or bit for bit, |x' - x| <= eb."""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def load_golden():
+    with open(os.path.join(GOLD, "szp3d.json")) as f:
+        meta = json.load(f)
+    arr = np.load(os.path.join(GOLD, "szp3d.npz"))
+    return meta["cases"], arr
+
+
+def sha(a) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def test_port_matches_reference_golden(port):
+    cases, arr = load_golden()
+    assert len(cases) == 56
+    for c in cases:
+        x, s = arr[f"x{c['i']}"], arr[f"s{c['i']}"].tobytes()
+        dims, bs, eb = tuple(c["dims"]), c["bs"], c["eb"]
+        assert port.szp3d_compress(x, dims, bs, eb) == s, c
+        y = port.szp3d_decompress(s, dims, bs, eb)
+        assert sha(y) == c["dec"], c
+        assert np.abs(y.astype(np.float64) - x).max() <= eb * (1 + 1e-6) + 1e-6 * np.abs(x).max()
+
+
+@pytest.fixture(scope="module")
+def torch():
+    t = pytest.importorskip("torch")
+    if not t.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return t
+
+
+@pytest.mark.gpu
+def test_gpu_matches_reference_golden(torch):
+    from zccl_gb300.szp3d import Szp3D
+    cases, arr = load_golden()
+    for c in cases:
+        x, s = arr[f"x{c['i']}"], arr[f"s{c['i']}"].tobytes()
+        dims, bs, eb = tuple(c["dims"]), c["bs"], c["eb"]
+        codec = Szp3D(dims, bs)
+        buf, size = codec.compress(torch.from_numpy(x).cuda(), eb)
+        n = codec.size(size)
+        codec.check()
+        assert buf[:n].cpu().numpy().tobytes() == s, c
+        y = codec.decompress(buf, eb, avail=n)
+        codec.check()
+        assert sha(y.cpu().numpy()) == c["dec"], c
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dims,bs", [((64, 80, 96), 4), ((37, 129, 70), 8), ((200, 3, 150), 2), ((40, 40, 40), 16)])
+def test_gpu_volumes_against_port(torch, port, dims, bs):
+    from zccl_gb300.szp3d import Szp3D
+    rng = np.random.default_rng(sum(dims))
+    i, j, k = np.meshgrid(*[np.arange(d, dtype=np.float64) for d in dims], indexing="ij")
+    x = (np.exp(np.sin(i / 9.0) + np.cos(j / 13.0) * np.sin(k / 7.0)) + rng.normal(0, 0.05, dims)).astype(np.float32).ravel()
+    eb = float(1e-4 * (x.max() - x.min()))
+    s = port.szp3d_compress(x, dims, bs, eb)
+    codec = Szp3D(dims, bs)
+    buf, size = codec.compress(torch.from_numpy(x).cuda(), eb)
+    n = codec.size(size)
+    assert buf[:n].cpu().numpy().tobytes() == s
+    y = codec.decompress(buf, eb, avail=n).cpu().numpy()
+    codec.check()
+    assert np.array_equal(y.view(np.uint32), port.szp3d_decompress(s, dims, bs, eb).view(np.uint32))
+    assert np.abs(y.astype(np.float64) - x).max() <= eb * (1 + 1e-6) + 1e-6 * np.abs(x).max()
+
+
+@pytest.mark.gpu
+def test_dropin_host_and_device_pointers(torch):
+    import zccl_gb300.szp3d as Z3
+    cases, arr = load_golden()
+    for c in cases[::5]:
+        x, s = arr[f"x{c['i']}"], arr[f"s{c['i']}"].tobytes()
+        dims, bs, eb = tuple(c["dims"]), c["bs"], c["eb"]
+        out = np.zeros(len(s) + 64 * 1024, np.uint8)
+        n = Z3.SZp_compress3D_fast(x, out, *dims, bs, eb)
+        assert out[:n].tobytes() == s
+        assert Z3.SZp_compress3D(x, out, *dims, bs, eb) == n
+        y = np.zeros(x.size, np.float32)
+        Z3.SZp_decompress3D(y, np.frombuffer(s, np.uint8).copy(), *dims, bs, eb)
+        assert sha(y) == c["dec"]
+        dx = torch.from_numpy(x).cuda()
+        dout = torch.zeros(len(s) + 64 * 1024, dtype=torch.uint8, device="cuda")
+        assert Z3.SZp_compress3D_fast(dx, dout, *dims, bs, eb) == n
+        assert dout[:n].cpu().numpy().tobytes() == s
+        dy = torch.zeros(x.size, dtype=torch.float32, device="cuda")
+        Z3.SZp_decompress3D(dy, dout, *dims, bs, eb)
+        assert sha(dy.cpu().numpy()) == c["dec"]

@@ -40,6 +40,9 @@ EXPORTS = [
     "zccl_gpu_strerror", "zccl_gpu_width_table", "zccl_gpu_compress_noalloc",
     "zccl_gpu_batch_bytes", "zccl_gpu_batch_plan", "zccl_gpu_batch_run", "zccl_gpu_batch_tune",
     "zccl_gpu_batch_check",
+    "SZp_compress3D_fast", "SZp_compress3D", "SZp_decompress3D", "SZp_decompress3D_fast",
+    "zccl_gpu_szp3d_max_bytes", "zccl_gpu_szp3d_workspace_bytes", "zccl_gpu_szp3d_compress",
+    "zccl_gpu_szp3d_decompress",
 ]
 
 
@@ -102,6 +105,14 @@ def lib() -> ctypes.CDLL:
         "zccl_gpu_build_index": (i, [sp, sz, i, i, vp, vp]),
         "zccl_gpu_stream_size": (i, [sp, sz, i, i, ctypes.POINTER(sz), vp]),
         "zccl_gpu_frame_size": (i, [sp, vp, vp]),
+        "SZp_compress3D_fast": (None, [vp, vp, sz, sz, sz, i, ctypes.c_double, ctypes.POINTER(sz)]),
+        "SZp_compress3D": (None, [vp, vp, sz, sz, sz, i, ctypes.c_double, ctypes.POINTER(sz)]),
+        "SZp_decompress3D": (None, [vp, vp, sz, sz, sz, i, ctypes.c_double]),
+        "SZp_decompress3D_fast": (None, [vp, vp, sz, sz, sz, i, ctypes.c_double]),
+        "zccl_gpu_szp3d_max_bytes": (sz, [sz, sz, sz, i]),
+        "zccl_gpu_szp3d_workspace_bytes": (sz, [sz, sz, sz, i]),
+        "zccl_gpu_szp3d_compress": (i, [vp, sz, vp, sz, sz, sz, i, ctypes.c_double, vp, vp, vp]),
+        "zccl_gpu_szp3d_decompress": (i, [vp, vp, sz, sz, sz, sz, i, ctypes.c_double, vp, vp]),
         "zccl_gpu_check": (i, [vp, vp]),
         "zccl_gpu_last_status": (i, []),
         "zccl_gpu_strerror": (ctypes.c_char_p, [i]),

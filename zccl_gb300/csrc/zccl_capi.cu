@@ -13,6 +13,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
+#include <cmath>
 #include <mutex>
 #include <vector>
 
@@ -885,6 +887,104 @@ int dropin_homadd(unsigned char *final_cmp, size_t *final_size, size_t n, float 
 
 int omp_threads() { return omp_get_max_threads(); }
 
+/* ---- SZp 3-D drop-ins ---------------------------------------------- */
+
+bool sz3_args_ok(size_t d1, size_t d2, size_t d3, int bs, double eb)
+{
+    return d1 && d2 && d3 && bs >= 1 && bs <= 32 && eb > 0 && std::isfinite(eb);
+}
+
+/* Stream bytes from its rate table (host memory). */
+size_t sz3_host_stream_bytes(const unsigned char *cmp, size_t d1, size_t d2, size_t d3, int bs)
+{
+    const size_t nb1 = (d1 - 1) / bs + 1, nb2 = (d2 - 1) / bs + 1, nb3 = (d3 - 1) / bs + 1;
+    size_t total = nb1 * nb2 * nb3, b = 0;
+    for (size_t x = 0; x < nb1; x++)
+        for (size_t y = 0; y < nb2; y++)
+            for (size_t z = 0; z < nb3; z++, b++) {
+                const size_t n = std::min<size_t>(bs, d1 - x * bs) * std::min<size_t>(bs, d2 - y * bs) *
+                                 std::min<size_t>(bs, d3 - z * bs);
+                const size_t r = cmp[b] > 32 ? 0 : cmp[b];
+                if (r) total += (n + 7) / 8 + (r / 8) * n + ((r % 8) * n + 7) / 8;
+            }
+    return total;
+}
+
+int dropin_szp3d_compress(const float *x, unsigned char *cmp, size_t d1, size_t d2, size_t d3, int bs,
+                          double eb, size_t *cmpSize)
+{
+    if (!x || !cmp || !cmpSize || !sz3_args_ok(d1, d2, d3, bs, eb)) return ZCCL_GPU_EINVAL;
+    DropCtx *c = drop_ctx();
+    if (!c) return ZCCL_GPU_ECUDA;
+    std::lock_guard<std::mutex> lk(c->mu);
+    const size_t n = d1 * d2 * d3, cap = sz3_max_stream_bytes(d1, d2, d3, (uint32_t)bs);
+    if (int rc = c->ws.ensure(sz3_workspace_bytes(d1, d2, d3, (uint32_t)bs, true) + 16)) return rc;
+    const bool din = is_device_ptr(x), dout = is_device_ptr(cmp);
+    const float *d_x = x;
+    if (!din) {
+        if (int rc = c->fin.ensure(4 * n)) return rc;
+        if (cudaMemcpyAsync(c->fin.p, x, 4 * n, cudaMemcpyHostToDevice, c->st) != cudaSuccess)
+            return ZCCL_GPU_ECUDA;
+        d_x = (const float *)c->fin.p;
+    }
+    unsigned char *d_out = cmp;
+    size_t room = dout ? device_room(cmp) : cap; /* callers allocate the stream; device: its allocation */
+    if (!dout) {
+        if (int rc = c->s[0].ensure(cap)) return rc;
+        d_out = (unsigned char *)c->s[0].p;
+    }
+    uint64_t *d_size = (uint64_t *)((uint8_t *)c->ws.p + sz3_workspace_bytes(d1, d2, d3, (uint32_t)bs, true));
+    if (cudaError_t e = sz3_compress(d_out, room, d_x, d1, d2, d3, (uint32_t)bs, eb, c->ws.p, d_size, c->st))
+        return e == cudaErrorInvalidValue ? ZCCL_GPU_ECAPACITY : ZCCL_GPU_ECUDA;
+    uint64_t size = 0;
+    if (cudaMemcpyAsync(&size, d_size, 8, cudaMemcpyDeviceToHost, c->st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    if (int rc = finish(c, c->ws.p)) return rc;
+    if (!dout) {
+        if (cudaMemcpyAsync(cmp, d_out, size, cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
+            cudaStreamSynchronize(c->st) != cudaSuccess)
+            return ZCCL_GPU_ECUDA;
+    }
+    *cmpSize = (size_t)size;
+    return ZCCL_GPU_OK;
+}
+
+int dropin_szp3d_decompress(float *y, const unsigned char *cmp, size_t d1, size_t d2, size_t d3, int bs, double eb)
+{
+    if (!y || !cmp || !sz3_args_ok(d1, d2, d3, bs, eb)) return ZCCL_GPU_EINVAL;
+    DropCtx *c = drop_ctx();
+    if (!c) return ZCCL_GPU_ECUDA;
+    std::lock_guard<std::mutex> lk(c->mu);
+    const size_t n = d1 * d2 * d3;
+    if (int rc = c->ws.ensure(sz3_workspace_bytes(d1, d2, d3, (uint32_t)bs, false))) return rc;
+    const bool din = is_device_ptr(cmp), dout = is_device_ptr(y);
+    const unsigned char *d_in = cmp;
+    size_t avail;
+    if (din) {
+        avail = device_room(cmp);
+        if (!avail) return ZCCL_GPU_EINVAL;
+    } else {
+        avail = sz3_host_stream_bytes(cmp, d1, d2, d3, bs);
+        if (int rc = c->s[0].ensure(avail)) return rc;
+        if (cudaMemcpyAsync(c->s[0].p, cmp, avail, cudaMemcpyHostToDevice, c->st) != cudaSuccess)
+            return ZCCL_GPU_ECUDA;
+        d_in = (const unsigned char *)c->s[0].p;
+    }
+    float *d_y = y;
+    if (!dout) {
+        if (int rc = c->fout.ensure(4 * n)) return rc;
+        d_y = (float *)c->fout.p;
+    }
+    if (sz3_decompress(d_y, d_in, avail, d1, d2, d3, (uint32_t)bs, eb, c->ws.p, c->st) != cudaSuccess)
+        return ZCCL_GPU_ECUDA;
+    if (int rc = finish(c, c->ws.p)) return rc;
+    if (!dout) {
+        if (cudaMemcpyAsync(y, d_y, 4 * n, cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
+            cudaStreamSynchronize(c->st) != cudaSuccess)
+            return ZCCL_GPU_ECUDA;
+    }
+    return ZCCL_GPU_OK;
+}
+
 } // namespace
 
 extern "C" int zccl_gpu_last_status(void) { return t_last_status; }
@@ -937,4 +1037,60 @@ extern "C" void ZCCL_float_homomophic_add_single_thread(unsigned char *final_cmp
 {
     report(__func__, dropin_homadd(final_cmpBytes, final_cmpSize, nbEle, absErrBound, blockSize,
                                    cmpBytes, cmpBytes2, 1));
+}
+
+/* ---- SZp 3-D codec ---------------------------------------------------- */
+
+extern "C" size_t zccl_gpu_szp3d_max_bytes(size_t d1, size_t d2, size_t d3, int bs)
+{
+    return sz3_args_ok(d1, d2, d3, bs, 1.0) ? sz3_max_stream_bytes(d1, d2, d3, (uint32_t)bs) : 0;
+}
+
+extern "C" size_t zccl_gpu_szp3d_workspace_bytes(size_t d1, size_t d2, size_t d3, int bs)
+{
+    return sz3_args_ok(d1, d2, d3, bs, 1.0) ? sz3_workspace_bytes(d1, d2, d3, (uint32_t)bs, true) : 0;
+}
+
+extern "C" int zccl_gpu_szp3d_compress(unsigned char *d_out, size_t capacity, const float *d_in, size_t d1,
+                                       size_t d2, size_t d3, int bs, double eb, void *d_ws, size_t *d_size,
+                                       void *cuda_stream)
+{
+    if (!d_out || !d_in || !d_ws || !sz3_args_ok(d1, d2, d3, bs, eb)) return ZCCL_GPU_EINVAL;
+    const cudaError_t e = sz3_compress(d_out, capacity, d_in, d1, d2, d3, (uint32_t)bs, eb, d_ws,
+                                       reinterpret_cast<uint64_t *>(d_size), (cudaStream_t)cuda_stream);
+    return e == cudaSuccess ? ZCCL_GPU_OK : e == cudaErrorInvalidValue ? ZCCL_GPU_ECAPACITY : ZCCL_GPU_ECUDA;
+}
+
+extern "C" int zccl_gpu_szp3d_decompress(float *d_out, const unsigned char *d_in, size_t avail, size_t d1,
+                                         size_t d2, size_t d3, int bs, double eb, void *d_ws, void *cuda_stream)
+{
+    if (!d_out || !d_in || !d_ws || !sz3_args_ok(d1, d2, d3, bs, eb)) return ZCCL_GPU_EINVAL;
+    return cuda_status(sz3_decompress(d_out, d_in, avail, d1, d2, d3, (uint32_t)bs, eb, d_ws,
+                                      (cudaStream_t)cuda_stream));
+}
+
+extern "C" void SZp_compress3D_fast(const float *oriData, unsigned char *cmpData, size_t dim1, size_t dim2,
+                                    size_t dim3, int blockSideLength, double errorBound, size_t *cmpSize)
+{
+    report(__func__, dropin_szp3d_compress(oriData, cmpData, dim1, dim2, dim3, blockSideLength, errorBound,
+                                           cmpSize));
+}
+
+extern "C" void SZp_compress3D(const float *oriData, unsigned char *cmpData, size_t dim1, size_t dim2,
+                               size_t dim3, int blockSideLength, double errorBound, size_t *cmpSize)
+{
+    report(__func__, dropin_szp3d_compress(oriData, cmpData, dim1, dim2, dim3, blockSideLength, errorBound,
+                                           cmpSize));
+}
+
+extern "C" void SZp_decompress3D(float *decData, unsigned char *cmpData, size_t dim1, size_t dim2, size_t dim3,
+                                 int blockSideLength, double errorBound)
+{
+    report(__func__, dropin_szp3d_decompress(decData, cmpData, dim1, dim2, dim3, blockSideLength, errorBound));
+}
+
+extern "C" void SZp_decompress3D_fast(float *decData, unsigned char *cmpData, size_t dim1, size_t dim2,
+                                      size_t dim3, int blockSideLength, double errorBound)
+{
+    report(__func__, dropin_szp3d_decompress(decData, cmpData, dim1, dim2, dim3, blockSideLength, errorBound));
 }

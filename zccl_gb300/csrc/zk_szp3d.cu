@@ -1,0 +1,489 @@
+/*
+ * zk_szp3d.cu -- the SZp 3-D Lorenzo codec, serial stream form.
+ *
+ * Replaces SZp_compress3D_fast / SZp_compress3D (ZCCL/src/ZCCL_float.c:1706-1860)
+ * and SZp_decompress3D (ZCCL/src/ZCCLd_float.c:2801-2871) and produces the
+ * same bytes and floats.  The reference walks the volume block by block and
+ * carries its Lorenzo state from block to block; the quantity it encodes is
+ * the 3-D mixed difference of the quantized values with zeros outside the
+ * volume (ZCCL_float.h:63-73), which every element can form on its own, and
+ * its inverse is the 3-D prefix sum.  So here every step is data parallel:
+ *
+ * compress   K0  q = (int)floor((double)x * (0.5 / eb) + 0.5) for every
+ *                element (ZCCL_float.h:57-61), in FP64 so that the rounding
+ *                is the reference's, into an int32 volume;
+ *            K1  one CTA per block: the differences of its elements, their
+ *                largest magnitude, the rate (its bit length) into the
+ *                rate table at the stream's start, the payload size;
+ *            K2  an exclusive scan of the payload sizes (three kernels);
+ *            K3  one CTA per block: the differences again, packed at the
+ *                block's offset: sign bits, then B = rate/8 high bytes per
+ *                element, then the r = rate%8 low bits (the fastmode1
+ *                packers' layout, ZCCL/src/ZCCL_TypeManager.c:12-91,824-848),
+ *                every byte by one thread;
+ * decompress K1  payload sizes from the rate table, K2 the same scan,
+ *            K3  one CTA per block: its differences into the output
+ *                buffer, viewed as int32;
+ *            K4-K6 inclusive prefix sums along z (a warp per row), y and x
+ *                (a thread per column), the last one writing
+ *                (float)((double)q * (2 eb)) in place (ZCCLd_float.c:2855-2857).
+ * Integer sums wrap modulo 2^32 like the reference's int.
+ */
+#include "zkern.cuh"
+
+namespace {
+
+constexpr uint32_t SZ_THREADS = 256;
+constexpr uint32_t SZ_CHUNK = 2048; /* sizes per CTA in the scan */
+
+struct Sz3Dims {
+    uint64_t d1, d2, d3;
+    uint32_t bs;
+    uint64_t nb1, nb2, nb3, nblocks;
+};
+
+__host__ __device__ inline Sz3Dims sz3_dims(uint64_t d1, uint64_t d2, uint64_t d3, uint32_t bs)
+{
+    Sz3Dims g;
+    g.d1 = d1;
+    g.d2 = d2;
+    g.d3 = d3;
+    g.bs = bs;
+    g.nb1 = (d1 - 1) / bs + 1;
+    g.nb2 = (d2 - 1) / bs + 1;
+    g.nb3 = (d3 - 1) / bs + 1;
+    g.nblocks = g.nb1 * g.nb2 * g.nb3;
+    return g;
+}
+
+/* Block b's first element and extent on each axis. */
+struct Sz3Block {
+    uint64_t x0, y0, z0;
+    uint32_t sx, sy, sz, n;
+};
+
+__device__ __forceinline__ Sz3Block sz3_block(const Sz3Dims &g, uint64_t b)
+{
+    Sz3Block k;
+    const uint64_t bz = b % g.nb3, by = (b / g.nb3) % g.nb2, bx = b / (g.nb3 * g.nb2);
+    k.x0 = bx * g.bs;
+    k.y0 = by * g.bs;
+    k.z0 = bz * g.bs;
+    k.sx = (uint32_t)min((uint64_t)g.bs, g.d1 - k.x0);
+    k.sy = (uint32_t)min((uint64_t)g.bs, g.d2 - k.y0);
+    k.sz = (uint32_t)min((uint64_t)g.bs, g.d3 - k.z0);
+    k.n = k.sx * k.sy * k.sz;
+    return k;
+}
+
+/* Payload bytes of a block of n elements at rate b (0 for rate 0). */
+__host__ __device__ inline uint32_t sz3_payload(uint32_t b, uint32_t n)
+{
+    if (!b) return 0;
+    return (n + 7) / 8 + (b >> 3) * n + ((b & 7u) * n + 7) / 8;
+}
+
+/* ---- K0: quantization -------------------------------------------------- */
+__global__ void k_sz3_quant(const float *__restrict__ x, int32_t *__restrict__ q, uint64_t n, double inv,
+                            uint32_t *err)
+{
+    uint32_t bad = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const double v = floor(__dadd_rn(__dmul_rn((double)x[i], inv), 0.5));
+        if (!(v >= -2147483648.0 && v < 2147483648.0)) { /* not finite, or outside int: undefined in the reference */
+            bad = 1;
+            q[i] = 0;
+        } else {
+            q[i] = (int32_t)v;
+        }
+    }
+    if (bad) atomicOr(err, ZERR_RANGE);
+}
+
+/* The mixed difference at (i, j, k), zeros outside the volume. */
+__device__ __forceinline__ uint32_t sz3_diff(const int32_t *q, const Sz3Dims &g, uint64_t i, uint64_t j, uint64_t k)
+{
+    const uint64_t s0 = g.d2 * g.d3, s1 = g.d3, p = i * s0 + j * s1 + k;
+    auto at = [&](bool ok, uint64_t o) -> uint32_t { return ok ? (uint32_t)q[o] : 0u; };
+    const bool bi = i > 0, bj = j > 0, bk = k > 0;
+    return at(true, p) - at(bk, p - 1) - at(bj, p - s1) + at(bj && bk, p - s1 - 1) - at(bi, p - s0) +
+           at(bi && bk, p - s0 - 1) + at(bi && bj, p - s0 - s1) - at(bi && bj && bk, p - s0 - s1 - 1);
+}
+
+/* Element t of a block (i slowest, k fastest), as in the reference. */
+__device__ __forceinline__ void sz3_elem(const Sz3Block &k, uint32_t t, uint64_t &i, uint64_t &j, uint64_t &z)
+{
+    const uint32_t kz = t % k.sz, jy = (t / k.sz) % k.sy, ix = t / (k.sz * k.sy);
+    i = k.x0 + ix;
+    j = k.y0 + jy;
+    z = k.z0 + kz;
+}
+
+__device__ __forceinline__ uint32_t mag(uint32_t v) { return (int32_t)v < 0 ? 0u - v : v; }
+
+/* ---- K1: rates and payload sizes (one CTA per block) -------------------- */
+__global__ void __launch_bounds__(SZ_THREADS) k_sz3_rates(const int32_t *q, Sz3Dims g, uint8_t *out, uint32_t *sizes)
+{
+    __shared__ uint32_t wmax[SZ_THREADS / 32];
+    for (uint64_t b = blockIdx.x; b < g.nblocks; b += gridDim.x) {
+        const Sz3Block k = sz3_block(g, b);
+        uint32_t m = 0;
+        for (uint32_t t = threadIdx.x; t < k.n; t += blockDim.x) {
+            uint64_t i, j, z;
+            sz3_elem(k, t, i, j, z);
+            m = max(m, mag(sz3_diff(q, g, i, j, z)));
+        }
+        m = __reduce_max_sync(0xffffffffu, m);
+        if ((threadIdx.x & 31u) == 0) wmax[threadIdx.x >> 5] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (uint32_t w = 1; w < blockDim.x / 32; w++) m = max(m, wmax[w]);
+            const uint32_t rate = 32u - __clz(max(m, wmax[0]));
+            out[b] = (uint8_t)rate;
+            sizes[b] = sz3_payload(rate, k.n);
+        }
+        __syncthreads();
+    }
+}
+
+/* ---- decompress K1: payload sizes from the rate table ------------------- */
+__global__ void k_sz3_sizes(const uint8_t *in, uint64_t avail, Sz3Dims g, uint32_t *sizes, uint32_t *err)
+{
+    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < g.nblocks; b += (uint64_t)gridDim.x * blockDim.x) {
+        if (b >= avail) {
+            atomicOr(err, ZERR_BOUNDS);
+            sizes[b] = 0;
+            continue;
+        }
+        const uint32_t rate = in[b];
+        if (rate > 32) atomicOr(err, ZERR_CORRUPT);
+        const Sz3Block k = sz3_block(g, b);
+        sizes[b] = rate > 32 ? 0 : sz3_payload(rate, k.n);
+    }
+}
+
+/* ---- K2: exclusive scan of the sizes into 64-bit offsets ---------------- */
+__global__ void __launch_bounds__(1024) k_sz3_chunk_sums(const uint32_t *sizes, uint64_t nb, uint64_t *sums)
+{
+    __shared__ uint64_t ws[32];
+    const uint64_t c = blockIdx.x, lo = c * SZ_CHUNK;
+    uint64_t s = 0;
+    for (uint64_t i = lo + threadIdx.x; i < nb && i < lo + SZ_CHUNK; i += blockDim.x) s += sizes[i];
+    for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31u) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint64_t t = 0;
+        for (uint32_t w = 0; w < blockDim.x / 32; w++) t += ws[w];
+        sums[c] = t;
+    }
+}
+
+/* One CTA: exclusive scan of the chunk sums in place; *total = all bytes. */
+__global__ void __launch_bounds__(1024) k_sz3_scan_sums(uint64_t *sums, uint64_t nchunks, uint64_t head, uint64_t *total)
+{
+    __shared__ uint64_t ws[33];
+    uint64_t carry = 0;
+    for (uint64_t c0 = 0; c0 < nchunks; c0 += blockDim.x) {
+        const uint64_t c = c0 + threadIdx.x;
+        const uint64_t v = c < nchunks ? sums[c] : 0;
+        uint64_t inc = v;
+        const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t u = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= (uint32_t)o) inc += u;
+        }
+        if (lane == 31) ws[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+            const uint64_t t = lane < blockDim.x / 32 ? ws[lane] : 0;
+            uint64_t ti = t;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint64_t u = __shfl_up_sync(0xffffffffu, ti, o);
+                if (lane >= (uint32_t)o) ti += u;
+            }
+            ws[lane] = ti - t;
+            if (lane == 31) ws[32] = ti;
+        }
+        __syncthreads();
+        if (c < nchunks) sums[c] = carry + ws[warp] + inc - v;
+        carry += ws[32];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = head + carry;
+}
+
+__global__ void __launch_bounds__(1024) k_sz3_offsets(const uint32_t *sizes, uint64_t nb, const uint64_t *sums,
+                                                      uint64_t *offs)
+{
+    __shared__ uint64_t ws[33];
+    const uint64_t c = blockIdx.x, lo = c * SZ_CHUNK;
+    const uint32_t per = SZ_CHUNK / blockDim.x; /* consecutive sizes per thread */
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint64_t v[SZ_CHUNK / 1024 > 0 ? SZ_CHUNK / 1024 : 1];
+    uint64_t s = 0;
+    for (uint32_t r = 0; r < per; r++) {
+        const uint64_t i = lo + (uint64_t)threadIdx.x * per + r;
+        v[r] = i < nb ? sizes[i] : 0;
+        s += v[r];
+    }
+    uint64_t inc = s;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= (uint32_t)o) inc += u;
+    }
+    if (lane == 31) ws[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const uint64_t t = lane < blockDim.x / 32 ? ws[lane] : 0;
+        uint64_t ti = t;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t u = __shfl_up_sync(0xffffffffu, ti, o);
+            if (lane >= (uint32_t)o) ti += u;
+        }
+        ws[lane] = ti - t;
+    }
+    __syncthreads();
+    uint64_t run = sums[c] + ws[warp] + inc - s;
+    for (uint32_t r = 0; r < per; r++) {
+        const uint64_t i = lo + (uint64_t)threadIdx.x * per + r;
+        if (i < nb) offs[i] = run;
+        run += v[r];
+    }
+}
+
+/* ---- compress K3: pack every block at its offset ------------------------ */
+__global__ void __launch_bounds__(SZ_THREADS) k_sz3_pack(const int32_t *q, Sz3Dims g, uint8_t *out, uint64_t cap,
+                                                         const uint64_t *offs, uint32_t *err)
+{
+    extern __shared__ uint32_t e[]; /* bs^3 differences */
+    for (uint64_t b = blockIdx.x; b < g.nblocks; b += gridDim.x) {
+        const uint32_t rate = out[b];
+        if (!rate) continue; /* uniform over the CTA */
+        const Sz3Block k = sz3_block(g, b);
+        const uint32_t n = k.n, B = rate >> 3, r = rate & 7u, ns = (n + 7) / 8;
+        const uint64_t base = g.nblocks + offs[b];
+        if (base + sz3_payload(rate, n) > cap) { /* uniform: the stream does not fit */
+            if (threadIdx.x == 0) atomicOr(err, ZERR_CAPACITY);
+            continue;
+        }
+        for (uint32_t t = threadIdx.x; t < n; t += blockDim.x) {
+            uint64_t i, j, z;
+            sz3_elem(k, t, i, j, z);
+            e[t] = sz3_diff(q, g, i, j, z);
+        }
+        __syncthreads();
+        uint8_t *o = out + base;
+        /* signs: bit 7 - t % 8 of byte t / 8 */
+        for (uint32_t c = threadIdx.x; c < ns; c += blockDim.x) {
+            uint32_t v = 0;
+            for (uint32_t u = 0; u < 8 && 8 * c + u < n; u++) v |= ((e[8 * c + u] >> 31) & 1u) << (7 - u);
+            o[c] = (uint8_t)v;
+        }
+        /* high bytes: element t's B bytes, little-endian */
+        uint8_t *h = o + ns;
+        for (uint32_t c = threadIdx.x; c < B * n; c += blockDim.x) {
+            const uint32_t t = c / B, byte = c % B;
+            h[c] = (uint8_t)((mag(e[t]) >> r) >> (8 * byte));
+        }
+        /* low bits: eight elements fill r bytes, MSB first */
+        if (r) {
+            uint8_t *l = h + B * n;
+            const uint32_t mask = (1u << r) - 1u, ng = (n + 7) / 8, tail = (r * n + 7) / 8;
+            for (uint32_t gi = threadIdx.x; gi < ng; gi += blockDim.x) {
+                uint64_t acc = 0;
+                for (uint32_t u = 0; u < 8; u++) {
+                    const uint32_t t = 8 * gi + u;
+                    acc = (acc << r) | (t < n ? (mag(e[t]) & mask) : 0u);
+                }
+                /* 8 r bits: byte gi * r + m is bits [8 m, 8 m + 8) from the top */
+                for (uint32_t m = 0; m < r; m++) {
+                    const uint32_t at = gi * r + m;
+                    if (at < tail) l[at] = (uint8_t)(acc >> (8 * (r - 1 - m)));
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+/* ---- decompress K3: every block's differences into the volume ---------- */
+__global__ void __launch_bounds__(SZ_THREADS) k_sz3_unpack(const uint8_t *in, uint64_t avail, Sz3Dims g,
+                                                           const uint64_t *offs, uint32_t *vol, uint32_t *err)
+{
+    const uint64_t s0 = g.d2 * g.d3, s1 = g.d3;
+    for (uint64_t b = blockIdx.x; b < g.nblocks; b += gridDim.x) {
+        const Sz3Block k = sz3_block(g, b);
+        uint32_t rate = b < avail ? in[b] : 0u;
+        const uint64_t base = g.nblocks + offs[b];
+        const uint32_t n = k.n;
+        if (rate > 32 || base + sz3_payload(rate, n) > avail) { /* uniform over the CTA */
+            if (threadIdx.x == 0) atomicOr(err, rate > 32 ? ZERR_CORRUPT : ZERR_BOUNDS);
+            rate = 0;
+        }
+        const uint32_t B = rate >> 3, r = rate & 7u, ns = (n + 7) / 8;
+        const uint8_t *sg = in + base, *h = sg + ns, *l = h + B * n;
+        for (uint32_t t = threadIdx.x; t < n; t += blockDim.x) {
+            uint32_t v = 0;
+            if (rate) {
+                for (uint32_t byte = 0; byte < B; byte++) v |= (uint32_t)h[t * B + byte] << (8 * byte);
+                v <<= r;
+                if (r) { /* bits [t r, t r + r) of the low section, MSB first */
+                    const uint64_t bit = (uint64_t)t * r;
+                    const uint64_t by = bit >> 3;
+                    const uint32_t w = ((uint32_t)l[by] << 8) | (by + 1 < (r * (uint64_t)n + 7) / 8 ? l[by + 1] : 0u);
+                    v |= (w >> (16 - (uint32_t)(bit & 7u) - r)) & ((1u << r) - 1u);
+                }
+                if ((sg[t >> 3] >> (7 - (t & 7u))) & 1u) v = 0u - v;
+            }
+            uint64_t i, j, z;
+            sz3_elem(k, t, i, j, z);
+            vol[i * s0 + j * s1 + z] = v;
+        }
+    }
+}
+
+/* ---- decompress K4-K6: the 3-D prefix sum ------------------------------ */
+__global__ void k_sz3_scan_z(uint32_t *vol, uint64_t rows, uint64_t d3)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t row = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (row >= rows) return;
+    uint32_t *p = vol + row * d3;
+    uint32_t run = 0;
+    for (uint64_t k0 = 0; k0 < d3; k0 += 32) {
+        const uint64_t k = k0 + lane;
+        const uint32_t v = k < d3 ? p[k] : 0u;
+        const uint32_t inc = warp_incl_scan(v);
+        if (k < d3) p[k] = run + inc;
+        run += __shfl_sync(0xffffffffu, inc, 31);
+    }
+}
+
+/* y: a thread per (i, k), j sequential */
+__global__ void k_sz3_scan_y(uint32_t *vol, uint64_t d1, uint64_t d2, uint64_t d3)
+{
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d1 * d3) return;
+    const uint64_t i = t / d3, k = t % d3;
+    uint32_t *p = vol + i * d2 * d3 + k;
+    uint32_t run = 0;
+#pragma unroll 8
+    for (uint64_t j = 0; j < d2; j++) {
+        run += p[j * d3];
+        p[j * d3] = run;
+    }
+}
+
+/* x: a thread per (j, k), i sequential; writes the floats in place */
+__global__ void k_sz3_scan_x(uint32_t *vol, uint64_t d1, uint64_t plane, double twice)
+{
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= plane) return;
+    uint32_t run = 0;
+#pragma unroll 8
+    for (uint64_t i = 0; i < d1; i++) {
+        run += vol[i * plane + t];
+        reinterpret_cast<float *>(vol)[i * plane + t] = (float)__dmul_rn((double)(int32_t)run, twice);
+    }
+}
+
+unsigned grid_for(uint64_t items, unsigned per_cta)
+{
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    uint64_t g = (items + per_cta - 1) / per_cta, cap = (uint64_t)(nsm > 0 ? nsm : 1) * 16;
+    return (unsigned)(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+/* Scratch layout: err[4] | sizes[nb] | offs[nb] | sums[nchunks] | total | q volume (compress). */
+struct Sz3Ws {
+    uint32_t *err, *sizes;
+    uint64_t *offs, *sums, *total;
+    int32_t *q;
+};
+
+Sz3Ws sz3_bind(void *ws, const Sz3Dims &g)
+{
+    uint8_t *p = static_cast<uint8_t *>(ws);
+    const uint64_t nch = (g.nblocks + SZ_CHUNK - 1) / SZ_CHUNK;
+    Sz3Ws w;
+    w.err = reinterpret_cast<uint32_t *>(p);
+    size_t o = 16;
+    w.sizes = reinterpret_cast<uint32_t *>(p + o);
+    o = (o + 4 * g.nblocks + 15) & ~(size_t)15;
+    w.offs = reinterpret_cast<uint64_t *>(p + o);
+    o += 8 * g.nblocks;
+    w.sums = reinterpret_cast<uint64_t *>(p + o);
+    o += 8 * nch;
+    w.total = reinterpret_cast<uint64_t *>(p + o);
+    o = (o + 8 + 255) & ~(size_t)255;
+    w.q = reinterpret_cast<int32_t *>(p + o);
+    return w;
+}
+
+cudaError_t sz3_scan(const Sz3Dims &g, const Sz3Ws &w, cudaStream_t st)
+{
+    const uint64_t nch = (g.nblocks + SZ_CHUNK - 1) / SZ_CHUNK;
+    k_sz3_chunk_sums<<<(unsigned)nch, 1024, 0, st>>>(w.sizes, g.nblocks, w.sums);
+    k_sz3_scan_sums<<<1, 1024, 0, st>>>(w.sums, nch, g.nblocks, w.total);
+    k_sz3_offsets<<<(unsigned)nch, 1024, 0, st>>>(w.sizes, g.nblocks, w.sums, w.offs);
+    return cudaGetLastError();
+}
+
+} // namespace
+
+size_t sz3_workspace_bytes(uint64_t d1, uint64_t d2, uint64_t d3, uint32_t bs, bool compress)
+{
+    const Sz3Dims g = sz3_dims(d1, d2, d3, bs);
+    Sz3Ws w = sz3_bind(nullptr, g);
+    const size_t head = (size_t)reinterpret_cast<uintptr_t>(w.q);
+    return head + (compress ? 4 * (size_t)(d1 * d2 * d3) : 0) + 256;
+}
+
+size_t sz3_max_stream_bytes(uint64_t d1, uint64_t d2, uint64_t d3, uint32_t bs)
+{
+    const Sz3Dims g = sz3_dims(d1, d2, d3, bs);
+    return (size_t)(g.nblocks + (size_t)sz3_payload(32, bs * bs * bs) * g.nblocks);
+}
+
+cudaError_t sz3_compress(uint8_t *out, uint64_t cap, const float *x, uint64_t d1, uint64_t d2, uint64_t d3,
+                         uint32_t bs, double eb, void *ws, uint64_t *d_size, cudaStream_t st)
+{
+    const Sz3Dims g = sz3_dims(d1, d2, d3, bs);
+    const Sz3Ws w = sz3_bind(ws, g);
+    cudaError_t e = cudaMemsetAsync(w.err, 0, 16, st);
+    if (e != cudaSuccess) return e;
+    const uint64_t n = d1 * d2 * d3;
+    k_sz3_quant<<<grid_for(n, 1024), 256, 0, st>>>(x, w.q, n, 0.5 / eb, w.err);
+    /* the rate table is part of the stream: cap must hold it */
+    if (cap < g.nblocks) return cudaErrorInvalidValue;
+    k_sz3_rates<<<grid_for(g.nblocks, 1), SZ_THREADS, 0, st>>>(w.q, g, out, w.sizes);
+    if ((e = sz3_scan(g, w, st)) != cudaSuccess) return e;
+    const size_t smem = 4ull * bs * bs * bs;
+    if (smem > 48 * 1024 &&
+        (e = cudaFuncSetAttribute(k_sz3_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+        return e;
+    k_sz3_pack<<<grid_for(g.nblocks, 1), SZ_THREADS, smem, st>>>(w.q, g, out, cap, w.offs, w.err);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return d_size ? cudaMemcpyAsync(d_size, w.total, 8, cudaMemcpyDeviceToDevice, st) : cudaSuccess;
+}
+
+cudaError_t sz3_decompress(float *y, const uint8_t *in, uint64_t avail, uint64_t d1, uint64_t d2, uint64_t d3,
+                           uint32_t bs, double eb, void *ws, cudaStream_t st)
+{
+    const Sz3Dims g = sz3_dims(d1, d2, d3, bs);
+    const Sz3Ws w = sz3_bind(ws, g);
+    cudaError_t e = cudaMemsetAsync(w.err, 0, 16, st);
+    if (e != cudaSuccess) return e;
+    k_sz3_sizes<<<grid_for(g.nblocks, 256), 256, 0, st>>>(in, avail, g, w.sizes, w.err);
+    if ((e = sz3_scan(g, w, st)) != cudaSuccess) return e;
+    uint32_t *vol = reinterpret_cast<uint32_t *>(y);
+    k_sz3_unpack<<<grid_for(g.nblocks, 1), SZ_THREADS, 0, st>>>(in, avail, g, w.offs, vol, w.err);
+    const uint64_t rows = d1 * d2;
+    k_sz3_scan_z<<<(unsigned)((rows * 32 + 255) / 256), 256, 0, st>>>(vol, rows, d3);
+    k_sz3_scan_y<<<(unsigned)((d1 * d3 + 255) / 256), 256, 0, st>>>(vol, d1, d2, d3);
+    k_sz3_scan_x<<<(unsigned)((d2 * d3 + 255) / 256), 256, 0, st>>>(vol, d1, d2 * d3, eb * 2);
+    return cudaGetLastError();
+}

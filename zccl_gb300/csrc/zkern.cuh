@@ -499,6 +499,16 @@ static inline unsigned persistent_grid(const void *fn, int threads, size_t smem,
 cudaError_t launch_compress(const CompressArgs &a, cudaStream_t st);
 cudaError_t launch_decompress(const DecompressArgs &a, cudaStream_t st);
 
+/* The SZp 3-D codec (zk_szp3d.cu): scratch bytes (err words, block sizes and
+ * offsets, and for compress the quantized volume), the largest stream, and
+ * the two passes, enqueued on st.  *d_size (device) receives the stream size. */
+size_t sz3_workspace_bytes(uint64_t d1, uint64_t d2, uint64_t d3, uint32_t bs, bool compress);
+size_t sz3_max_stream_bytes(uint64_t d1, uint64_t d2, uint64_t d3, uint32_t bs);
+cudaError_t sz3_compress(uint8_t *out, uint64_t cap, const float *x, uint64_t d1, uint64_t d2, uint64_t d3,
+                         uint32_t bs, double eb, void *ws, uint64_t *d_size, cudaStream_t st);
+cudaError_t sz3_decompress(float *y, const uint8_t *in, uint64_t avail, uint64_t d1, uint64_t d2, uint64_t d3,
+                           uint32_t bs, double eb, void *ws, cudaStream_t st);
+
 /* Host: a 2-D TMA map of the floats p[0, n) as rows of 32, boxes of 256
  * rows, 128-byte swizzle (16-byte chunk k of row r lands at chunk k ^ (r & 7)
  * of a 1024-byte-aligned box).  False when p is not 16-byte aligned, holds
