@@ -366,6 +366,55 @@ def reduction_bench(args, L, T, dev):
     return res
 
 
+def szp3d_bench(args, dev):
+    """The SZp 3-D codec on the side^3 field (eb = 1e-4 * range, block sides
+    4 and 8): device-timed compress and decompress, compression ratio, max
+    error over eb; the serial reference restatement (one host core, the
+    reference's form is serial) on a 128^3 corner of the field."""
+    import time
+    import numpy as np
+    import torch
+    from oracle import zoracle
+    from zccl_gb300.szp3d import Szp3D
+    side = args.side
+    x = make_field(side, 0, dev)
+    eb = float(1e-4 * float(x.max() - x.min()))
+    dims = (side, side, side)
+    res = {"workload": f"{side}^3 log-normal GRF, eb=1e-4*range (float64 {eb:.6g})"}
+    for bs in (4, 8):
+        codec = Szp3D(dims, bs, device=str(dev))
+        st = codec.torch_stream
+        buf, size = codec.compress(x, eb)
+        n = codec.size(size)
+        y = torch.empty_like(x)
+        ms_c = timed(lambda: codec.compress(x, eb, out=buf), 5, st)
+        ms_d = timed(lambda: codec.decompress(buf, eb, out=y, avail=n), 5, st)
+        codec.check()
+        err = float((y.double() - x.double()).abs().max()) / eb
+        alg = 4 * x.numel() + n
+        res[f"bs{bs}"] = {"compress_ms": round(ms_c, 3), "decompress_ms": round(ms_d, 3),
+                          "compress_GBps_uncompressed": round(4 * x.numel() / (ms_c * 1e-3) / 1e9, 1),
+                          "decompress_GBps_uncompressed": round(4 * x.numel() / (ms_d * 1e-3) / 1e9, 1),
+                          "algorithmic_GBps": {"compress": round(alg / (ms_c * 1e-3) / 1e9, 1),
+                                               "decompress": round(alg / (ms_d * 1e-3) / 1e9, 1)},
+                          "ratio": round(4 * x.numel() / n, 3), "max_err_over_eb": round(err, 4)}
+    if not args.no_cpu:
+        c = 128
+        sub = x.view(side, side, side)[:c, :c, :c].contiguous().cpu().numpy().ravel()
+        port = zoracle.port()
+        t0 = time.perf_counter()
+        s = port.szp3d_compress(sub, (c, c, c), 4, eb)
+        t1 = time.perf_counter()
+        port.szp3d_decompress(s, (c, c, c), 4, eb)
+        t2 = time.perf_counter()
+        res["cpu_baseline"] = {"kind": "port", "cores": 1, "sample": f"{c}^3 corner, block side 4",
+                               "compress_GBps": round(4 * sub.size / (t1 - t0) / 1e9, 3),
+                               "decompress_GBps": round(4 * sub.size / (t2 - t1) / 1e9, 3)}
+    del x
+    torch.cuda.empty_cache()
+    return res
+
+
 def batched_bench(args, L, dev):
     """4096 gradient-bucket-like buffers (2048 pairs of equal size, log-
     uniform 4 KB - 16 MB, Laplace(0, 1e-3), 5 % constant, eb per pair from
@@ -700,6 +749,7 @@ def run_ours(args, rank, world, local_rank):
     if rank == 0 and not args.no_extras:
         del hs_a, hs_b, hs_s, hy
         extras["reduction"] = reduction_bench(args, L, T, dev)
+        extras["szp3d"] = szp3d_bench(args, dev)
         extras["batched"] = batched_bench(args, L, dev)
         extras["serving"] = serving_bench(args, L, dev)
 
