@@ -169,6 +169,27 @@ int zccl_gpu_build_index(zccl_gpu_stream *s, size_t n, int L, int T, void *d_ws,
 int zccl_gpu_stream_size(const zccl_gpu_stream *s, size_t n, int L, int T, size_t *size,
                          void *cuda_stream);
 
+/* ---- the fixed-rate appendix codec --------------------------------------
+ * ZCCL/src/ZCCL_appendix.c:65-590: fastmode1's stream with every block's
+ * magnitudes stored as b/8 + 1 (at most 4) whole little-endian bytes and no
+ * low-bit stream.  Same arguments, pointers and threading as the fastmode1
+ * drop-ins above (declared with the same signatures at
+ * ZCCL/include/ZCCL_appendix.h:12-24).  The reference's compressor gives the remainder segment's tail
+ * block the regular segments' tail count (ZCCL_appendix.c:318-330), which
+ * its own decompressor does not read back when the two counts differ; here
+ * that block has its own count, the layout the decompressor reads. */
+void ZCCL_float_openmp_threadblock_arg_2(unsigned char *outputBytes, float *oriData, size_t *outSize,
+                                         float absErrBound, size_t nbEle, int blockSize);
+void ZCCL_float_decompress_openmp_threadblock_arg_2(float *newData, size_t nbEle, float absErrBound,
+                                                    int blockSize, unsigned char *cmpBytes);
+/* Device API for streams in that layout (arguments as zccl_gpu_compress /
+ * zccl_gpu_decompress; the descriptor does not record the layout, so a
+ * stream is always read with the call of its writer's layout). */
+int zccl_gpu_compress_fixed(zccl_gpu_stream *out, const float *d_in, size_t n, float eb, int L, int T,
+                            void *d_ws, void *cuda_stream);
+int zccl_gpu_decompress_fixed(float *d_out, zccl_gpu_stream *in, size_t n, float eb, int L, int T,
+                              void *d_ws, void *cuda_stream);
+
 /* ---- SZp 3-D codec, serial stream form --------------------------------
  * Drop-ins for the reference's serial 3-D Lorenzo codec: a dim1 x dim2 x
  * dim3 float volume (dim3 fastest) in blocks of blockSideLength^3 (1..32)

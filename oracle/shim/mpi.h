@@ -1,7 +1,8 @@
 /* Types-only stand-in for <mpi.h>, used solely to compile the reference codec
  * sources into the oracle library.  The codec files include the MPI header
  * through ZCCL.h but call no MPI function on the compress / decompress /
- * homomorphic-add path. */
+ * homomorphic-add path; the MPI functions that the appendix file's allgather
+ * variants call are link-time stubs (ref_stubs.c). */
 #ifndef ORACLE_SHIM_MPI_H
 #define ORACLE_SHIM_MPI_H
 typedef int MPI_Datatype;
@@ -13,4 +14,9 @@ typedef int MPI_Win;
 typedef struct { int MPI_SOURCE, MPI_TAG, MPI_ERROR; } MPI_Status;
 #define MPI_WIN_NULL 0
 #define MPI_COMM_NULL 0
+/* constants the appendix codec file (ZCCL/src/ZCCL_appendix.c) names in its
+ * allgather functions, which the oracle never calls */
+#define MPI_SUCCESS 0
+#define MPI_INT 1
+#define MPI_BYTE 2
 #endif

@@ -29,12 +29,31 @@
 
 /* ---- geometry -------------------------------------------------------- */
 
+/* The magnitude layout of a block of width b: B whole bytes per element,
+ * then r bits per element.  fmt 0 is fastmode1 (B = b/8, r = b%8); fmt 1 is
+ * the fixed-rate appendix codec, which keeps whole bytes only:
+ * B = b/8 + 1 (at most 4), r = 0 (ZCCL/src/ZCCL_appendix.c:18-39). */
+static void split(int fmt, int b, int *B, int *r)
+{
+    if (fmt) {
+        *B = b / 8 + 1 > 4 ? 4 : b / 8 + 1;
+        *r = 0;
+    } else {
+        *B = b / 8;
+        *r = b % 8;
+    }
+}
+
 /* Bytes of one encoded block of n elements at width b. */
-static size_t block_bytes(int b, size_t n)
+static size_t block_bytes_f(int b, size_t n, int fmt)
 {
     if (b == 0) return 1;
-    return 1 + (n + 7) / 8 + (size_t)(b / 8) * n + ((size_t)(b % 8) * n + 7) / 8;
+    int B, r;
+    split(fmt, b, &B, &r);
+    return 1 + (n + 7) / 8 + (size_t)B * n + ((size_t)r * n + 7) / 8;
 }
+
+static size_t block_bytes(int b, size_t n) { return block_bytes_f(b, n, 0); }
 
 /* Largest possible encoding of a segment of len elements (every block at
  * width 32). */
@@ -66,7 +85,7 @@ static inline uint32_t magnitude(int32_t d)
 /* ---- block coder ----------------------------------------------------- */
 
 /* Encode n deltas into o; returns bytes written. */
-static size_t encode_block(unsigned char *o, const int32_t *d, size_t n)
+static size_t encode_block_f(unsigned char *o, const int32_t *d, size_t n, int fmt)
 {
     uint32_t m = 0;
     for (size_t j = 0; j < n; j++) {
@@ -78,7 +97,8 @@ static size_t encode_block(unsigned char *o, const int32_t *d, size_t n)
         return 1;
     }
     int b = port_width(m);
-    int B = b / 8, r = b % 8;
+    int B, r;
+    split(fmt, b, &B, &r);
     unsigned char *p = o;
     *p++ = (unsigned char)b;
 
@@ -110,14 +130,15 @@ static size_t encode_block(unsigned char *o, const int32_t *d, size_t n)
 }
 
 /* Decode one block of n deltas from s into d; returns bytes consumed. */
-static size_t decode_block(const unsigned char *s, size_t n, int32_t *d)
+static size_t decode_block_f(const unsigned char *s, size_t n, int32_t *d, int fmt)
 {
     int b = s[0];
     if (b == 0) {
         memset(d, 0, n * sizeof(int32_t));
         return 1;
     }
-    int B = b / 8, r = b % 8;
+    int B, r;
+    split(fmt, b, &B, &r);
     const unsigned char *sg = s + 1;
     const unsigned char *hi = sg + (n + 7) / 8;
     const unsigned char *lo = hi + (size_t)B * n;
@@ -138,13 +159,16 @@ static size_t decode_block(const unsigned char *s, size_t n, int32_t *d)
         int neg = (sg[j / 8] >> (7 - j % 8)) & 1;
         d[j] = (int32_t)(neg ? 0u - v : v);
     }
-    return block_bytes(b, n);
+    return block_bytes_f(b, n, fmt);
 }
+
+static size_t encode_block(unsigned char *o, const int32_t *d, size_t n) { return encode_block_f(o, d, n, 0); }
+static size_t decode_block(const unsigned char *s, size_t n, int32_t *d) { return decode_block_f(s, n, d, 0); }
 
 /* ---- per-segment passes ---------------------------------------------- */
 
 static size_t encode_segment(unsigned char *o, const float *x, size_t len, double inv, size_t L,
-                             int32_t *d)
+                             int32_t *d, int fmt)
 {
     unsigned char *p = o;
     int32_t prior = quantize(x[0], inv);
@@ -157,13 +181,13 @@ static size_t encode_segment(unsigned char *o, const float *x, size_t len, doubl
             d[j] = (int32_t)((uint32_t)q - (uint32_t)prior);
             prior = q;
         }
-        p += encode_block(p, d, n);
+        p += encode_block_f(p, d, n, fmt);
     }
     return (size_t)(p - o);
 }
 
 static size_t decode_segment(float *y, const unsigned char *s, size_t len, float eb, size_t L,
-                             int32_t *d)
+                             int32_t *d, int fmt)
 {
     const unsigned char *p = s;
     int32_t prior;
@@ -172,7 +196,7 @@ static size_t decode_segment(float *y, const unsigned char *s, size_t len, float
     y[0] = (float)prior * eb;
     for (size_t i = 1; i < len; i += L) {
         size_t n = len - i < L ? len - i : L;
-        p += decode_block(p, n, d);
+        p += decode_block_f(p, n, d, fmt);
         for (size_t j = 0; j < n; j++) {
             prior = (int32_t)((uint32_t)prior + (uint32_t)d[j]);
             y[i + j] = (float)prior * eb;
@@ -230,8 +254,8 @@ static void homadd_segment(unsigned char **po, const unsigned char **pa, const u
 
 /* ---- stream-level entry points --------------------------------------- */
 
-void port_compress(unsigned char *out, const float *in, size_t *outSize, float absErrBound,
-                   size_t nbEle, int blockSize, int T)
+void port_compress_f(unsigned char *out, const float *in, size_t *outSize, float absErrBound,
+                     size_t nbEle, int blockSize, int T, int fmt)
 {
     const size_t L = (size_t)blockSize;
     const size_t tbs = nbEle / (size_t)T, rem = nbEle % (size_t)T;
@@ -246,8 +270,8 @@ void port_compress(unsigned char *out, const float *in, size_t *outSize, float a
         size_t cap = segment_worst_bytes(tbs, L) + (has_rm ? segment_worst_bytes(rem, L) : 0);
         unsigned char *buf = (unsigned char *)malloc(cap);
         int32_t *d = (int32_t *)malloc(L * sizeof(int32_t));
-        size_t s = encode_segment(buf, in + lo, tbs, inv, L, d);
-        if (has_rm) s += encode_segment(buf + s, in + lo + tbs, rem, inv, L, d);
+        size_t s = encode_segment(buf, in + lo, tbs, inv, L, d, fmt);
+        if (has_rm) s += encode_segment(buf + s, in + lo + tbs, rem, inv, L, d, fmt);
         bufs[t] = buf;
         sizes[t] = s;
         free(d);
@@ -271,8 +295,8 @@ void port_compress(unsigned char *out, const float *in, size_t *outSize, float a
     free(sizes);
 }
 
-void port_decompress(float *out, size_t nbEle, float absErrBound, int blockSize,
-                     const unsigned char *cmp, int T)
+void port_decompress_f(float *out, size_t nbEle, float absErrBound, int blockSize,
+                       const unsigned char *cmp, int T, int fmt)
 {
     const size_t L = (size_t)blockSize;
     const size_t tbs = nbEle / (size_t)T, rem = nbEle % (size_t)T;
@@ -284,11 +308,23 @@ void port_decompress(float *out, size_t nbEle, float absErrBound, int blockSize,
         memcpy(&o, cmp + 8 * (size_t)t, 8);
         int32_t *d = (int32_t *)malloc(L * sizeof(int32_t));
         size_t lo = (size_t)t * tbs;
-        size_t used = decode_segment(out + lo, data + o, tbs, absErrBound, L, d);
+        size_t used = decode_segment(out + lo, data + o, tbs, absErrBound, L, d, fmt);
         if (t == T - 1 && rem != 0)
-            decode_segment(out + lo + tbs, data + o + used, rem, absErrBound, L, d);
+            decode_segment(out + lo + tbs, data + o + used, rem, absErrBound, L, d, fmt);
         free(d);
     }
+}
+
+void port_compress(unsigned char *out, const float *in, size_t *outSize, float absErrBound,
+                   size_t nbEle, int blockSize, int T)
+{
+    port_compress_f(out, in, outSize, absErrBound, nbEle, blockSize, T, 0);
+}
+
+void port_decompress(float *out, size_t nbEle, float absErrBound, int blockSize,
+                     const unsigned char *cmp, int T)
+{
+    port_decompress_f(out, nbEle, absErrBound, blockSize, cmp, T, 0);
 }
 
 void port_homadd(unsigned char *out, size_t *outSize, size_t nbEle, float absErrBound,

@@ -27,6 +27,16 @@ void port_compress(unsigned char *out, const float *in, size_t *outSize, float a
 void port_decompress(float *out, size_t nbEle, float absErrBound, int blockSize,
                      const unsigned char *cmp, int T);
 
+/* The same two with the block magnitude layout `fmt`: 0 is fastmode1, 1
+ * the fixed-rate appendix codec (ZCCL_float_openmp_threadblock_arg_2 and
+ * ZCCL_float_decompress_openmp_threadblock_arg_2, ZCCL/src/ZCCL_appendix.c:65-590),
+ * whose blocks keep b/8 + 1 (at most 4) whole little-endian bytes per
+ * magnitude and no low-bit stream; everything else is fastmode1's. */
+void port_compress_f(unsigned char *out, const float *in, size_t *outSize, float absErrBound,
+                     size_t nbEle, int blockSize, int T, int fmt);
+void port_decompress_f(float *out, size_t nbEle, float absErrBound, int blockSize,
+                       const unsigned char *cmp, int T, int fmt);
+
 /* Homomorphic add of two streams (same nbEle, eb, L, T).  *outSize is
  * INCREMENTED, like the reference (ZCCL/src/ZCCLd_float.c:1027,1655).
  * out may alias cmp2.  ZCCL/src/ZCCLd_float.c:988-1679. */

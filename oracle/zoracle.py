@@ -86,6 +86,20 @@ class _Codec:
             self._set_threads.argtypes = [ctypes.c_int]
         for f in (self._c, self._d, self._h):
             f.restype = None
+        # the fixed-rate appendix codec (ZCCL/src/ZCCL_appendix.c:65-590)
+        if kind == "port":
+            self._cf = self.lib.port_compress_f
+            self._cf.argtypes = [_u8p, _f32p, _szp, ctypes.c_float, ctypes.c_size_t, ctypes.c_int,
+                                 ctypes.c_int, ctypes.c_int]
+            self._df = self.lib.port_decompress_f
+            self._df.argtypes = [_f32p, ctypes.c_size_t, ctypes.c_float, ctypes.c_int, _u8p, ctypes.c_int,
+                                 ctypes.c_int]
+        else:
+            self._cf = self.lib.ZCCL_float_openmp_threadblock_arg_2
+            self._cf.argtypes = [_u8p, _f32p, _szp, ctypes.c_float, ctypes.c_size_t, ctypes.c_int]
+            self._df = self.lib.ZCCL_float_decompress_openmp_threadblock_arg_2
+            self._df.argtypes = [_f32p, ctypes.c_size_t, ctypes.c_float, ctypes.c_int, _u8p]
+        self._cf.restype = self._df.restype = None
         # the serial SZp 3-D codec (ZCCL/src/ZCCL_float.c:1706-1860, ZCCLd_float.c:2801-2871)
         c3 = [_f32p, _u8p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int,
               ctypes.c_double, _szp]
@@ -132,6 +146,26 @@ class _Codec:
         self._h(_ptr(out, _u8p), ctypes.byref(size), ctypes.c_size_t(n), ctypes.c_float(eb),
                 ctypes.c_int(L), _ptr(a, _u8p), _ptr(b, _u8p), *self._args_T(T))
         return out[: size.value].tobytes()
+
+    def _fmt(self):
+        return (ctypes.c_int(1),) if self.kind == "port" else ()
+
+    def compress_fixed(self, x: np.ndarray, eb: float, L: int, T: int) -> bytes:
+        """The fixed-rate appendix codec (ZCCL_float_openmp_threadblock_arg_2)."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        n = x.size
+        out = np.zeros(worst_stream_bytes(n, L, T), dtype=np.uint8)
+        size = ctypes.c_size_t(0)
+        self._cf(_ptr(out, _u8p), _ptr(x, _f32p), ctypes.byref(size), ctypes.c_float(eb),
+                 ctypes.c_size_t(n), ctypes.c_int(L), *self._args_T(T), *self._fmt())
+        return out[: size.value].tobytes()
+
+    def decompress_fixed(self, stream: bytes, n: int, eb: float, L: int, T: int) -> np.ndarray:
+        buf = np.concatenate([np.frombuffer(stream, dtype=np.uint8), np.zeros(16, np.uint8)])
+        y = np.zeros(n, dtype=np.float32)
+        self._df(_ptr(y, _f32p), ctypes.c_size_t(n), ctypes.c_float(eb), ctypes.c_int(L), _ptr(buf, _u8p),
+                 *self._args_T(T), *self._fmt())
+        return y
 
     def szp3d_compress(self, x: np.ndarray, dims, bs: int, eb: float, form: str = "fast") -> bytes:
         x = np.ascontiguousarray(x, dtype=np.float32).ravel()

@@ -41,6 +41,8 @@ EXPORTS = [
     "zccl_gpu_batch_bytes", "zccl_gpu_batch_plan", "zccl_gpu_batch_run", "zccl_gpu_batch_tune",
     "zccl_gpu_batch_check",
     "SZp_compress3D_fast", "SZp_compress3D", "SZp_decompress3D", "SZp_decompress3D_fast",
+    "ZCCL_float_openmp_threadblock_arg_2", "ZCCL_float_decompress_openmp_threadblock_arg_2",
+    "zccl_gpu_compress_fixed", "zccl_gpu_decompress_fixed",
     "zccl_gpu_szp3d_max_bytes", "zccl_gpu_szp3d_workspace_bytes", "zccl_gpu_szp3d_compress",
     "zccl_gpu_szp3d_decompress",
 ]
@@ -100,6 +102,10 @@ def lib() -> ctypes.CDLL:
         "zccl_gpu_workspace_bytes": (sz, [sz, i, i]),
         "zccl_gpu_compress": (i, [sp, vp, sz, f, i, i, vp, vp]),
         "zccl_gpu_decompress": (i, [vp, sp, sz, f, i, i, vp, vp]),
+        "zccl_gpu_compress_fixed": (i, [sp, vp, sz, f, i, i, vp, vp]),
+        "zccl_gpu_decompress_fixed": (i, [vp, sp, sz, f, i, i, vp, vp]),
+        "ZCCL_float_openmp_threadblock_arg_2": (None, [vp, vp, vp, f, sz, i]),
+        "ZCCL_float_decompress_openmp_threadblock_arg_2": (None, [vp, sz, f, i, vp]),
         "zccl_gpu_homadd": (i, [sp, sp, i, sz, i, i, vp, vp]),
         "zccl_gpu_homadd_cases": (i, [sp, sp, i, sz, i, i, vp, vp, vp]),
         "zccl_gpu_build_index": (i, [sp, sz, i, i, vp, vp]),
@@ -198,6 +204,22 @@ def ZCCL_float_decompress_single_thread_arg(newData, nbEle, absErrBound, blockSi
     _check(lib().zccl_gpu_last_status(), "ZCCL_float_decompress_single_thread_arg")
 
 
+def ZCCL_float_openmp_threadblock_arg_2(outputBytes, oriData, outSize, absErrBound, nbEle, blockSize):
+    """The fixed-rate appendix codec, ZCCL/src/ZCCL_appendix.c:65; returns the assigned size."""
+    s = _size_slot(outSize)
+    lib().ZCCL_float_openmp_threadblock_arg_2(_ptr(outputBytes), _ptr(oriData), ctypes.byref(s),
+                                              absErrBound, nbEle, blockSize)
+    _check(lib().zccl_gpu_last_status(), "ZCCL_float_openmp_threadblock_arg_2")
+    return s.value
+
+
+def ZCCL_float_decompress_openmp_threadblock_arg_2(newData, nbEle, absErrBound, blockSize, cmpBytes):
+    """ZCCL/src/ZCCL_appendix.c:373."""
+    lib().ZCCL_float_decompress_openmp_threadblock_arg_2(_ptr(newData), nbEle, absErrBound, blockSize,
+                                                         _ptr(cmpBytes))
+    _check(lib().zccl_gpu_last_status(), "ZCCL_float_decompress_openmp_threadblock_arg_2")
+
+
 def ZCCL_float_homomophic_add_openmp_threadblock(final_cmpBytes, final_cmpSize, nbEle, absErrBound,
                                                  blockSize, cmpBytes, cmpBytes2):
     """ZCCL/src/ZCCLd_float.c:988; returns the accumulated size (the
@@ -262,9 +284,14 @@ class DeviceStream:
 class Codec:
     """Device API for one geometry (n floats, block size L, writer count T)."""
 
-    def __init__(self, n: int, L: int = 32, T: int = 1, device: str = "cuda", stream=None):
+    def __init__(self, n: int, L: int = 32, T: int = 1, device: str = "cuda", stream=None,
+                 fixed: bool = False):
+        """fixed: the fixed-rate appendix codec's block layout
+        (ZCCL/src/ZCCL_appendix.c:65-590) instead of fastmode1's; such
+        streams compress and decompress only (no homomorphic add)."""
         import torch
         self.n, self.L, self.T = int(n), int(L), int(T)
+        self.fixed = bool(fixed)
         self.device = torch.device(device)
         self.max_stream_bytes = lib().zccl_gpu_max_stream_bytes(self.n, self.L, self.T)
         self.index_bytes = lib().zccl_gpu_index_bytes(self.n, self.L, self.T)
@@ -280,21 +307,23 @@ class Codec:
 
     def compress(self, x, eb: float, out: DeviceStream | None = None) -> DeviceStream:
         out = out or self.new_stream()
-        _check(lib().zccl_gpu_compress(ctypes.byref(out.desc), x.data_ptr(), self.n, eb, self.L,
-                                       self.T, self.ws.data_ptr(), self.stream_ptr),
-               "zccl_gpu_compress")
+        fn = lib().zccl_gpu_compress_fixed if self.fixed else lib().zccl_gpu_compress
+        _check(fn(ctypes.byref(out.desc), x.data_ptr(), self.n, eb, self.L, self.T, self.ws.data_ptr(),
+                  self.stream_ptr), "zccl_gpu_compress")
         return out
 
     def decompress(self, s: DeviceStream, eb: float, out=None):
         import torch
         out = out if out is not None else torch.empty(self.n, dtype=torch.float32,
                                                       device=self.device)
-        _check(lib().zccl_gpu_decompress(out.data_ptr(), ctypes.byref(s.desc), self.n, eb, self.L,
-                                         self.T, self.ws.data_ptr(), self.stream_ptr),
-               "zccl_gpu_decompress")
+        fn = lib().zccl_gpu_decompress_fixed if self.fixed else lib().zccl_gpu_decompress
+        _check(fn(out.data_ptr(), ctypes.byref(s.desc), self.n, eb, self.L, self.T, self.ws.data_ptr(),
+                  self.stream_ptr), "zccl_gpu_decompress")
         return out
 
     def homadd(self, ins, out: DeviceStream | None = None, cases=None) -> DeviceStream:
+        if self.fixed:
+            raise ZcclError(-1, "the fixed-rate layout has no homomorphic add")
         out = out or self.new_stream()
         arr = (StreamDesc * len(ins))(*[s.desc for s in ins])
         rc = lib().zccl_gpu_homadd_cases(ctypes.byref(out.desc), arr, len(ins), self.n, self.L,

@@ -235,11 +235,13 @@ extern "C" void zccl_gpu_width_table(uint32_t thr[33])
     memcpy(thr, wt.thr, sizeof(wt.thr));
 }
 
-extern "C" int zccl_gpu_compress(zccl_gpu_stream *out, const float *d_in, size_t n, float eb, int L,
-                                 int T, void *d_ws, void *cuda_stream)
+/* Compress in block layout fmt (ZG_FASTMODE1 or ZG_FIXED_BYTES). */
+static int compress_fmt(zccl_gpu_stream *out, const float *d_in, size_t n, float eb, int L, int T, void *d_ws,
+                        void *cuda_stream, uint32_t fmt)
 {
     ZGeom g;
     if (make_geom(n, L, T, &g) || !valid_stream(out) || !d_in || !d_ws) return ZCCL_GPU_EINVAL;
+    g.fmt = fmt;
     if (!(eb > 0.0f) || !isfinite(eb)) return ZCCL_GPU_EINVAL;
     cudaStream_t st = (cudaStream_t)cuda_stream;
     CompressArgs a;
@@ -263,6 +265,18 @@ extern "C" int zccl_gpu_compress(zccl_gpu_stream *out, const float *d_in, size_t
     return rc;
 }
 
+extern "C" int zccl_gpu_compress(zccl_gpu_stream *out, const float *d_in, size_t n, float eb, int L,
+                                 int T, void *d_ws, void *cuda_stream)
+{
+    return compress_fmt(out, d_in, n, eb, L, T, d_ws, cuda_stream, ZG_FASTMODE1);
+}
+
+extern "C" int zccl_gpu_compress_fixed(zccl_gpu_stream *out, const float *d_in, size_t n, float eb, int L,
+                                       int T, void *d_ws, void *cuda_stream)
+{
+    return compress_fmt(out, d_in, n, eb, L, T, d_ws, cuda_stream, ZG_FIXED_BYTES);
+}
+
 extern "C" int zccl_gpu_build_index(zccl_gpu_stream *s, size_t n, int L, int T, void *d_ws,
                                     void *cuda_stream)
 {
@@ -273,11 +287,13 @@ extern "C" int zccl_gpu_build_index(zccl_gpu_stream *s, size_t n, int L, int T, 
     return walk_stream(s, g, d_ws, st);
 }
 
-extern "C" int zccl_gpu_decompress(float *d_out, zccl_gpu_stream *in, size_t n, float eb, int L,
-                                   int T, void *d_ws, void *cuda_stream)
+/* Decompress a stream in block layout fmt. */
+static int decompress_fmt(float *d_out, zccl_gpu_stream *in, size_t n, float eb, int L, int T, void *d_ws,
+                          void *cuda_stream, uint32_t fmt)
 {
     ZGeom g;
     if (make_geom(n, L, T, &g) || !valid_stream(in) || !d_out || !d_ws) return ZCCL_GPU_EINVAL;
+    g.fmt = fmt;
     cudaStream_t st = (cudaStream_t)cuda_stream;
     if (cudaMemsetAsync(d_ws, 0, ws_clear_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
     ZWork w = bind_ws(d_ws);
@@ -298,6 +314,18 @@ extern "C" int zccl_gpu_decompress(float *d_out, zccl_gpu_stream *in, size_t n, 
     int rc = cuda_status(launch_decompress(a, st));
     if (rc == ZCCL_GPU_OK) in->qprev_valid = 1;
     return rc;
+}
+
+extern "C" int zccl_gpu_decompress(float *d_out, zccl_gpu_stream *in, size_t n, float eb, int L,
+                                   int T, void *d_ws, void *cuda_stream)
+{
+    return decompress_fmt(d_out, in, n, eb, L, T, d_ws, cuda_stream, ZG_FASTMODE1);
+}
+
+extern "C" int zccl_gpu_decompress_fixed(float *d_out, zccl_gpu_stream *in, size_t n, float eb, int L,
+                                         int T, void *d_ws, void *cuda_stream)
+{
+    return decompress_fmt(d_out, in, n, eb, L, T, d_ws, cuda_stream, ZG_FIXED_BYTES);
 }
 
 extern "C" int zccl_gpu_homadd_cases(zccl_gpu_stream *out, zccl_gpu_stream *ins, int P, size_t n,
@@ -769,7 +797,7 @@ int stage_stream(DropCtx *c, int slot, const unsigned char *cmp, const ZGeom &g,
 }
 
 int dropin_compress(unsigned char *outputBytes, const float *oriData, size_t *outSize, float eb,
-                    size_t n, int L, int T)
+                    size_t n, int L, int T, uint32_t fmt = ZG_FASTMODE1)
 {
     ZGeom g;
     if (!outputBytes || !oriData || !outSize || make_geom(n, L, T, &g)) return ZCCL_GPU_EINVAL;
@@ -798,7 +826,7 @@ int dropin_compress(unsigned char *outputBytes, const float *oriData, size_t *ou
         s.bytes = (unsigned char *)c->s[0].p;
         s.capacity = worst;
     }
-    if (int rc = zccl_gpu_compress(&s, d_in, n, eb, L, T, c->ws.p, c->st)) return rc;
+    if (int rc = compress_fmt(&s, d_in, n, eb, L, T, c->ws.p, c->st, fmt)) return rc;
     if (int rc = finish(c, c->ws.p)) return rc;
     size_t size = 0;
     if (int rc = zccl_gpu_stream_size(&s, n, L, T, &size, c->st)) return rc;
@@ -812,7 +840,8 @@ int dropin_compress(unsigned char *outputBytes, const float *oriData, size_t *ou
     return ZCCL_GPU_OK;
 }
 
-int dropin_decompress(float *newData, size_t n, float eb, int L, const unsigned char *cmp, int T)
+int dropin_decompress(float *newData, size_t n, float eb, int L, const unsigned char *cmp, int T,
+                      uint32_t fmt = ZG_FASTMODE1)
 {
     ZGeom g;
     if (!newData || !cmp || make_geom(n, L, T, &g)) return ZCCL_GPU_EINVAL;
@@ -833,7 +862,7 @@ int dropin_decompress(float *newData, size_t n, float eb, int L, const unsigned 
         zccl_gpu_stream s;
         bool capped;
         if (int rc = stage_stream(c, 0, cmp, g, &s, pass > 0, &capped)) return rc;
-        if (int rc = zccl_gpu_decompress(d_out, &s, n, eb, L, T, c->ws.p, c->st)) return rc;
+        if (int rc = decompress_fmt(d_out, &s, n, eb, L, T, c->ws.p, c->st, fmt)) return rc;
         int rc = finish(c, c->ws.p);
         if (rc == ZCCL_GPU_EBOUNDS && capped && pass == 0) continue;
         if (rc) return rc;
@@ -1093,4 +1122,20 @@ extern "C" void SZp_decompress3D_fast(float *decData, unsigned char *cmpData, si
                                       size_t dim3, int blockSideLength, double errorBound)
 {
     report(__func__, dropin_szp3d_decompress(decData, cmpData, dim1, dim2, dim3, blockSideLength, errorBound));
+}
+
+/* ---- the fixed-rate appendix codec ------------------------------------ */
+
+extern "C" void ZCCL_float_openmp_threadblock_arg_2(unsigned char *outputBytes, float *oriData, size_t *outSize,
+                                                    float absErrBound, size_t nbEle, int blockSize)
+{
+    report(__func__, dropin_compress(outputBytes, oriData, outSize, absErrBound, nbEle, blockSize, omp_threads(),
+                                     ZG_FIXED_BYTES));
+}
+
+extern "C" void ZCCL_float_decompress_openmp_threadblock_arg_2(float *newData, size_t nbEle, float absErrBound,
+                                                               int blockSize, unsigned char *cmpBytes)
+{
+    report(__func__,
+           dropin_decompress(newData, nbEle, absErrBound, blockSize, cmpBytes, omp_threads(), ZG_FIXED_BYTES));
 }

@@ -182,10 +182,11 @@ struct Reader {
  * each element (four r-bit fields merged per put).  A zero-width block is a
  * single 0x00 byte, already in the buffer. */
 __device__ __forceinline__ void encode_full(uint32_t sbase, uint32_t o, uint32_t b, uint32_t smask,
-                                            const uint32_t (&m)[32])
+                                            const uint32_t (&m)[32], uint32_t fmt = ZG_FASTMODE1)
 {
     if (b == 0) return;
-    const uint32_t B = b >> 3, r = b & 7u;
+    uint32_t B, r;
+    zg_split(fmt, b, &B, &r);
     Packer pk;
     pk.init(sbase, o);
     pk.put(b, 8);
@@ -257,14 +258,15 @@ __device__ __forceinline__ uint32_t prmt_sign(uint32_t a, uint32_t sel)
  *     replicating the sign of byte j / 8 of the sign word shifted by j % 8.
  * Reads up to 12 bytes past the block (buffers carry slack). */
 __device__ __forceinline__ uint32_t decode_full(const uint32_t *w, uint32_t o, uint32_t b,
-                                                uint32_t (&d)[32])
+                                                uint32_t (&d)[32], uint32_t fmt = ZG_FASTMODE1)
 {
     if (b == 0) {
 #pragma unroll
         for (int j = 0; j < 32; j++) d[j] = 0;
         return 0;
     }
-    const uint32_t B = b >> 3, r = b & 7u;
+    uint32_t B, r;
+    zg_split(fmt, b, &B, &r);
     uint32_t sg, unused;
     be64_at(w, o + 1, sg, unused);
     const uint32_t hb = o + 5, lb = hb + 32u * B;
@@ -330,10 +332,12 @@ __device__ __forceinline__ uint32_t decode_full(const uint32_t *w, uint32_t o, u
  * exact slow quantization path.  elem(j, neg, mag) gives element j. */
 template <class Elem>
 __device__ __forceinline__ void encode_any(uint32_t sbase, uint32_t o, uint32_t b, uint32_t n,
-                                           Elem elem)
+                                           Elem elem, uint32_t fmt = ZG_FASTMODE1)
 {
     if (b == 0) return;
-    const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
+    uint32_t B, r;
+    zg_split(fmt, b, &B, &r);
+    const uint32_t ns = (n + 7) >> 3;
     const uint32_t mask = r ? (1u << r) - 1u : 0u;
     Packer ph, ps, pb, pl;
     ph.init(sbase, o);
@@ -364,13 +368,15 @@ __device__ __forceinline__ void encode_any(uint32_t sbase, uint32_t o, uint32_t 
 /* Element-at-a-time decoder for any block; sink(j, delta). */
 template <class Sink>
 __device__ __forceinline__ void decode_any(const uint32_t *w, uint32_t o, uint32_t b, uint32_t n,
-                                           Sink sink)
+                                           Sink sink, uint32_t fmt = ZG_FASTMODE1)
 {
     if (b == 0) {
         for (uint32_t j = 0; j < n; j++) sink(j, 0u);
         return;
     }
-    const uint32_t B = b >> 3, r = b & 7u, ns = (n + 7) >> 3;
+    uint32_t B, r;
+    zg_split(fmt, b, &B, &r);
+    const uint32_t ns = (n + 7) >> 3;
     Reader rs, rh, rl;
     rs.init(w, o + 1);
     rh.init(w, o + 1 + ns);

@@ -42,7 +42,17 @@ typedef struct ZGeom {
     uint64_t nt_rm;   /* tiles of the extra segment (0 when rem == 0) */
     uint64_t nblocks; /* all blocks */
     uint64_t ntiles;  /* all tiles */
+    uint32_t fmt;     /* block magnitude layout: ZG_FASTMODE1 or ZG_FIXED_BYTES */
+    uint32_t pad_;
 } ZGeom;
+
+/* Block magnitude layouts.  fastmode1: B = b/8 whole bytes per magnitude
+ * (little-endian), then its r = b%8 low bits as an MSB-first stream
+ * (ZCCL/src/ZCCL_TypeManager.c:12-91).  The fixed-rate appendix codec keeps
+ * whole bytes only, B = b/8 + 1 of them (at most 4), r = 0
+ * (ZCCL/src/ZCCL_appendix.c:18-39).  Everything else is shared. */
+#define ZG_FASTMODE1 0u
+#define ZG_FIXED_BYTES 1u
 
 /* Per-tile view computed from a tile index. */
 typedef struct ZTile {
@@ -74,6 +84,27 @@ ZG_HD uint32_t zg_block_bytes(uint32_t b, uint32_t n)
     return 1 + (n + 7) / 8 + (b >> 3) * n + ((b & 7) * n + 7) / 8;
 }
 
+/* Whole bytes B and low bits r per magnitude of a width-b block in layout fmt. */
+ZG_HD void zg_split(uint32_t fmt, uint32_t b, uint32_t *B, uint32_t *r)
+{
+    if (fmt == ZG_FIXED_BYTES) {
+        *B = (b >> 3) + 1 < 4 ? (b >> 3) + 1 : 4;
+        *r = 0;
+    } else {
+        *B = b >> 3;
+        *r = b & 7;
+    }
+}
+
+/* zg_block_bytes in layout fmt; both layouts take the same bytes at width 32. */
+ZG_HD uint32_t zg_block_bytes_f(uint32_t fmt, uint32_t b, uint32_t n)
+{
+    if (b == 0) return 1;
+    uint32_t B, r;
+    zg_split(fmt, b, &B, &r);
+    return 1 + (n + 7) / 8 + B * n + (r * n + 7) / 8;
+}
+
 /* Row stride (in 4-byte words) of the padded per-block shared-memory layout:
  * odd, so thread t reading word j of row t hits bank (t*stride + j) % 32,
  * distinct across a warp. */
@@ -87,6 +118,8 @@ ZG_HD int zg_init(ZGeom *g, uint64_t n, uint32_t L, uint32_t T)
     g->n = n;
     g->T = T;
     g->L = L;
+    g->fmt = ZG_FASTMODE1;
+    g->pad_ = 0;
     g->tbs = n / T;
     g->rem = (uint32_t)(n % T);
     g->TB = zg_tile_blocks(L);

@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
             }
             if (ok) {
                 b = width_of(mx, a.wt);
-                size = zg_block_bytes(b, 32);
+                size = zg_block_bytes_f(g.fmt, b, 32);
                 done = true;
             }
         }
@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
                 }
             }
             b = width_of(mx, a.wt);
-            size = zg_block_bytes(b, n);
+            size = zg_block_bytes_f(g.fmt, b, n);
         } else if (!FAST && own) { /* blocks above 32 elements: the rows are read again when packing */
             const float xp = tid == 0 ? xprev0 : rows[(tid - 1) * stride + L - 1];
             int32_t qp = fastq ? quantize_fast(xp, J.inv) : quantize(xp, J.inv, bad);
@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
                 qp = q;
             }
             b = width_of(mx, a.wt);
-            size = zg_block_bytes(b, n);
+            size = zg_block_bytes_f(g.fmt, b, n);
         }
 
         /* 3. offsets in the tile and early publication of its size (the
@@ -358,24 +358,30 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
         const uint32_t o = headb + off;
         if (FAST) {
             if (n == 32) {
-                encode_full(pk_sa, o, b, smask, m);
+                encode_full(pk_sa, o, b, smask, m, g.fmt);
             } else if (own) {
-                encode_any(pk_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
-                    neg = (smask >> (31u - j)) & 1u;
-                    mg = pick(m, j);
-                });
+                encode_any(
+                    pk_sa, o, b, n,
+                    [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
+                        neg = (smask >> (31u - j)) & 1u;
+                        mg = pick(m, j);
+                    },
+                    g.fmt);
             }
         } else {
             if (own) {
                 const float xp = tid == 0 ? xprev0 : rows[(tid - 1) * stride + L - 1];
                 int32_t qp = fastq ? quantize_fast(xp, J.inv) : quantize(xp, J.inv, bad);
-                encode_any(pk_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
-                    const int32_t q = fastq ? quantize_fast(row[j], J.inv) : quantize(row[j], J.inv, bad);
-                    const int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
-                    qp = q;
-                    neg = (uint32_t)d >> 31;
-                    mg = (uint32_t)abs(d);
-                });
+                encode_any(
+                    pk_sa, o, b, n,
+                    [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
+                        const int32_t q = fastq ? quantize_fast(row[j], J.inv) : quantize(row[j], J.inv, bad);
+                        const int32_t d = (int32_t)((uint32_t)q - (uint32_t)qp);
+                        qp = q;
+                        neg = (uint32_t)d >> 31;
+                        mg = (uint32_t)abs(d);
+                    },
+                    g.fmt);
             }
             named_sync(1, NC); /* the rows have been read for the last time */
             if (tid == 0) claim_tile(a, ticket, in, bar_tma, s_tile, s_job, s_amax, &cj[(it + 1) & 1u], box, &xmap);

@@ -97,7 +97,7 @@ __device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, uint64_
             bad |= ZERR_CORRUPT;
             sl.b = 0;
         }
-        size = zg_block_bytes(sl.b, sl.n);
+        size = zg_block_bytes_f(a.g.fmt, sl.b, sl.n);
     }
     uint32_t total;
     sl.off = cta_excl_scan(size, wsum, &total);
@@ -180,9 +180,9 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
         uint32_t bsum = 0;
         if (own && buf[o] != b) bad |= ZERR_CORRUPT;
         if (full) {
-            bsum = decode_full(sw, o, b, d);
+            bsum = decode_full(sw, o, b, d, g.fmt);
         } else if (own) { /* short or long block: sum now, decode again for the values */
-            decode_any(sw, o, b, n, [&](uint32_t, uint32_t v) { bsum += v; });
+            decode_any(sw, o, b, n, [&](uint32_t, uint32_t v) { bsum += v; }, g.fmt);
         }
 
         /* 3. starting value of every block.  In index order the next tile's
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
                         bad |= ZERR_CORRUPT;
                         nxt.b = 0;
                     }
-                    sizen = zg_block_bytes(nxt.b, nxt.n);
+                    sizen = zg_block_bytes_f(g.fmt, nxt.b, nxt.n);
                 }
             }
             uint32_t totn;
@@ -262,10 +262,13 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
             }
         } else if (own) {
             uint32_t q = q0 + pre;
-            decode_any(sw, o, b, n, [&](uint32_t j, uint32_t v) {
-                q += v;
-                row[j] = __fmul_rn(__int2float_rn((int32_t)q), a.eb);
-            });
+            decode_any(
+                sw, o, b, n,
+                [&](uint32_t j, uint32_t v) {
+                    q += v;
+                    row[j] = __fmul_rn(__int2float_rn((int32_t)q), a.eb);
+                },
+                g.fmt);
         }
         if (z.has_head && tid == 0) a.y[z.seg_start] = __fmul_rn(__int2float_rn(head), a.eb);
         __syncthreads();

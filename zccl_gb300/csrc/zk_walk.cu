@@ -43,9 +43,9 @@ __device__ __forceinline__ uint64_t load_u64(const uint8_t *p)
 
 /* Size of a full block whose header byte is b; bytes that cannot be a
  * header (b > 32) count as 1 so speculative walks stay bounded. */
-__device__ __forceinline__ uint32_t full_size(uint32_t b, uint32_t L)
+__device__ __forceinline__ uint32_t full_size(uint32_t b, uint32_t L, uint32_t fmt)
 {
-    return b <= 32 ? zg_block_bytes(b, L) : 1u;
+    return b <= 32 ? zg_block_bytes_f(fmt, b, L) : 1u;
 }
 
 /* Segment of a window / group index: last s with base[s] <= i. */
@@ -161,7 +161,7 @@ __device__ __forceinline__ bool map_bit(const uint32_t *m, uint32_t i)
 }
 
 /* All lanes: the speculative sub-window walks. */
-__device__ __forceinline__ void spec_walks(const uint8_t *bytes, uint32_t L, WinPath *wp)
+__device__ __forceinline__ void spec_walks(const uint8_t *bytes, uint32_t L, uint32_t fmt, WinPath *wp)
 {
     const uint32_t lane = threadIdx.x & 31u, lo = lane * SUB;
     uint32_t m0 = 0, m1 = 0, m2 = 0, m3 = 0, pos = lo;
@@ -171,7 +171,7 @@ __device__ __forceinline__ void spec_walks(const uint8_t *bytes, uint32_t L, Win
         m1 |= w == 1 ? bit : 0u;
         m2 |= w == 2 ? bit : 0u;
         m3 |= w == 3 ? bit : 0u;
-        pos += full_size(bytes[pos], L);
+        pos += full_size(bytes[pos], L, fmt);
     }
     wp->spec[lane][0] = m0;
     wp->spec[lane][1] = m1;
@@ -182,7 +182,7 @@ __device__ __forceinline__ void spec_walks(const uint8_t *bytes, uint32_t L, Win
 
 /* One lane: the true path from window position `entry`, per sub-window,
  * with the prefix counts; returns where it leaves the window. */
-__device__ __forceinline__ uint32_t stitch(const uint8_t *bytes, uint32_t L, uint32_t entry, WinPath *wp)
+__device__ __forceinline__ uint32_t stitch(const uint8_t *bytes, uint32_t L, uint32_t fmt, uint32_t entry, WinPath *wp)
 {
     uint32_t p = entry, cnt = 0;
     for (uint32_t j = 0; j < 32; j++) {
@@ -204,7 +204,7 @@ __device__ __forceinline__ uint32_t stitch(const uint8_t *bytes, uint32_t L, uin
                 }
 #pragma unroll
                 for (uint32_t w = 0; w < 4; w++) t[w] |= w == (i >> 5) ? 1u << (i & 31u) : 0u;
-                q += full_size(bytes[q], L);
+                q += full_size(bytes[q], L, fmt);
                 if (q >= hi) break;
             }
             p = q;
@@ -260,9 +260,9 @@ __global__ void __launch_bounds__(32 * WARPS_W1) k_walk_tables(const WalkArgs a)
     WinPath *wp = reinterpret_cast<WinPath *>(bytes + ((WALK_WW + M + 16 + 15) & ~15u));
     load_window(a, start, bytes);
     __syncwarp();
-    spec_walks(bytes, g.L, wp);
+    spec_walks(bytes, g.L, g.fmt, wp);
     __syncwarp();
-    if (lane == 0) stitch(bytes, g.L, 0, wp);
+    if (lane == 0) stitch(bytes, g.L, g.fmt, 0, wp);
     __syncwarp();
     /* entry e: walk until the path from entry 0 is met (then its exit and
      * the blocks left on it) or the window ends */
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(32 * WARPS_W1) k_walk_tables(const WalkArgs a)
     for (uint32_t e = lane; e < M; e += 32) {
         uint32_t q = e, k = 0;
         while (q < WALK_WW && !map_bit(wp->tm[q / SUB], q % SUB)) {
-            q += full_size(bytes[q], g.L);
+            q += full_size(bytes[q], g.L, g.fmt);
             k++;
         }
         const uint32_t ex = q < WALK_WW ? x0 : q - WALK_WW;
@@ -387,9 +387,9 @@ __global__ void __launch_bounds__(128) k_walk_final(const WalkArgs a)
         WinPath *wp = reinterpret_cast<WinPath *>(buf + ((WALK_WW + a.M + 16 + 15) & ~15u));
         load_window(a, start, buf);
         __syncwarp();
-        spec_walks(buf, g.L, wp);
+        spec_walks(buf, g.L, g.fmt, wp);
         __syncwarp();
-        if (lane == 0) stitch(buf, g.L, entry[k - w0], wp);
+        if (lane == 0) stitch(buf, g.L, g.fmt, entry[k - w0], wp);
         __syncwarp();
         /* lane j records the true-path blocks of its sub-window */
         uint64_t blk = b0 + wp->pref[lane];
@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(128) k_walk_final(const WalkArgs a)
                 const uint32_t n = blk < nfull ? g.L : ntail;
                 blk++;
                 if (blk == nb) {
-                    const uint64_t end = gpos + zg_block_bytes(b, n);
+                    const uint64_t end = gpos + zg_block_bytes_f(g.fmt, b, n);
                     if (end > a.avail) atomicOr(a.err, ZERR_BOUNDS);
                     w.seg_end[s] = end;
                     if (s + 1 < g.T && end != w.seg_R[s]) atomicOr(a.err, ZERR_CORRUPT);
@@ -461,7 +461,7 @@ __global__ void k_walk_finish(const WalkArgs a)
                 return;
             }
             a.idx.widths[gblk0 + j] = (uint8_t)b;
-            pos += zg_block_bytes(b, zg_block_len(g.rem, g.L, j));
+            pos += zg_block_bytes_f(g.fmt, b, zg_block_len(g.rem, g.L, j));
         }
         if (pos > a.avail) {
             atomicOr(a.err, ZERR_BOUNDS);
