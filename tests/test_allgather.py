@@ -28,13 +28,15 @@ def test_segments_shorter_than_the_writer_count_are_refused():
         SegmentedAllgatherv([2 * 1024 * 1024 + 5], T=16)
 
 
-def oracle_allgatherv(port, xs, eb, L, T, segsize):
+def oracle_allgatherv(port, xs, eb, L, T, segsize, fixed=False):
+    comp = port.compress_fixed if fixed else port.compress
+    decomp = port.decompress_fixed if fixed else port.decompress
     frames = []
     for x in xs:
         cnts, offs = segments(x.size, segsize)
         fr = []
         for n, o in zip(cnts, offs):
-            s = port.compress(np.ascontiguousarray(x[o: o + n]), eb, L, T)
+            s = comp(np.ascontiguousarray(x[o: o + n]), eb, L, T)
             fr.append(len(s).to_bytes(8, "little") + s)
         frames.append(fr)
     recv = []
@@ -45,7 +47,7 @@ def oracle_allgatherv(port, xs, eb, L, T, segsize):
                 parts.append(x)
             else:
                 cnts, _ = segments(x.size, segsize)
-                parts += [port.decompress(f[8:], n, eb, L, T) for f, n in zip(frames[c], cnts)]
+                parts += [decomp(f[8:], n, eb, L, T) for f, n in zip(frames[c], cnts)]
         recv.append(np.concatenate(parts))
     return frames, recv
 
@@ -84,3 +86,22 @@ def test_segmented_allgatherv_matches_oracle(torch, port, counts, T, segsize):
         assert np.array_equal(y.cpu().numpy().view(np.uint32), recv[r].view(np.uint32)), r
     y0 = ag.run([torch.from_numpy(x).cuda() for x in xs], eb)  # rank 0 only
     assert np.array_equal(y0.cpu().numpy().view(np.uint32), recv[0].view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_segmented_allgatherv_fixed_rate_matches_oracle(torch, port):
+    """The appendix variant (ZCCL/src/ZCCL_appendix.c:756-941): the same
+    frames with the fixed-rate codec."""
+    from zccl_gb300.allgather import SegmentedAllgatherv
+    counts, T, L, segsize = [48000, 40000, 36000], 4, 32, 64 * 1024
+    rng = np.random.default_rng(5)
+    xs = [np.cumsum(rng.normal(0, 0.01, c)).astype(np.float32) for c in counts]
+    eb = float(np.float32(1e-4 * (max(x.max() for x in xs) - min(x.min() for x in xs))))
+    ag = SegmentedAllgatherv(counts, L, T, segsize=segsize, fixed=True)
+    ys = ag.run([torch.from_numpy(x).cuda() for x in xs], eb, per_rank_outputs=True)
+    frames, recv = oracle_allgatherv(port, xs, eb, L, T, segsize, fixed=True)
+    for c in range(len(xs)):
+        for f, g in zip(ag.sent[c], frames[c]):
+            assert frame_bytes(f) == g
+    for r, y in enumerate(ys):
+        assert np.array_equal(y.cpu().numpy().view(np.uint32), recv[r].view(np.uint32)), r

@@ -17,6 +17,8 @@ messages cut into segments:
 
 So chunk c's floats are the owner's originals on rank c and the same
 decompressed floats on every other rank; frames are never recompressed.
+MPIR_Allgatherv_intra_ring_RI2_mt_oa_record_seg_2 (ZCCL/src/ZCCL_appendix.c:756-941)
+is the same exchange with the fixed-rate appendix codec (`fixed=True`).
 The reference measures the element extent as sizeof(MPI_Datatype), which is
 4 bytes under MPICH (an int handle) and equals sizeof(float); 4 is used here.
 
@@ -53,10 +55,11 @@ class SegmentedAllgatherv:
     placed at `displs[r]` of every receive buffer (contiguous by default)."""
 
     def __init__(self, counts, L: int = 32, T: int = 1, segsize: int = SEGSIZE, displs=None,
-                 device: str = "cuda"):
+                 device: str = "cuda", fixed: bool = False):
         import torch
         self.counts = [int(c) for c in counts]
         self.P, self.L, self.T, self.segsize = len(self.counts), int(L), int(T), int(segsize)
+        self.fixed = bool(fixed)
         if segsize % EXTENT or segsize <= 0:
             raise ValueError("segsize must be a positive multiple of 4 bytes")
         if displs is None:
@@ -79,7 +82,7 @@ class SegmentedAllgatherv:
         key = (n, which)
         if key not in self._codecs:
             self._codecs[key] = Codec(n, self.L, self.T, device=str(self.device),
-                                      stream=self.sc if which == "c" else self.sd)
+                                      stream=self.sc if which == "c" else self.sd, fixed=self.fixed)
         return self._codecs[key]
 
     def frames(self, x, eb: float, events: bool = False):
