@@ -84,8 +84,15 @@ def test_segmented_allgatherv_matches_oracle(torch, port, counts, T, segsize):
             assert frame_bytes(f) == g
     for r, y in enumerate(ys):
         assert np.array_equal(y.cpu().numpy().view(np.uint32), recv[r].view(np.uint32)), r
-    y0 = ag.run([torch.from_numpy(x).cuda() for x in xs], eb)  # rank 0 only
+    xd = [torch.from_numpy(x).cuda() for x in xs]
+    y0 = ag.run(xd, eb)  # rank 0 only
     assert np.array_equal(y0.cpu().numpy().view(np.uint32), recv[0].view(np.uint32))
+    g, yg = ag.capture(xd, eb)  # the same exchange replayed from a CUDA graph
+    yg.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    ag.check()
+    assert np.array_equal(yg.cpu().numpy().view(np.uint32), recv[0].view(np.uint32))
 
 
 @pytest.mark.gpu

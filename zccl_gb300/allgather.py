@@ -97,7 +97,8 @@ class SegmentedAllgatherv:
             with torch.cuda.stream(self.sc):  # allocated (and its index zeroed) where it is written
                 frame = torch.empty(8 + c.max_stream_bytes, dtype=torch.uint8, device=self.device)
                 s = DeviceStream(c, data=frame[8:])
-            frame.record_stream(self.sd)  # read there by the receivers
+            if not torch.cuda.is_current_stream_capturing():
+                frame.record_stream(self.sd)  # read there by the receivers (a graph keeps its own pool)
             c.compress(x[o: o + n], eb, out=s)
             _check(lib().zccl_gpu_frame_size(ctypes.byref(s.desc), frame.data_ptr(),
                                              ctypes.c_void_p(self.sc.cuda_stream)), "zccl_gpu_frame_size")
@@ -116,7 +117,7 @@ class SegmentedAllgatherv:
             s = DeviceStream(c, data=frame[8:])  # a fresh index: the header walk rebuilds it
         c.decompress(s, eb, out=y)
 
-    def run(self, xs, eb: float, per_rank_outputs: bool = False):
+    def run(self, xs, eb: float, per_rank_outputs: bool = False, _check: bool = True):
         """Allgather the P tensors in xs.  Returns rank 0's receive buffer, or
         every rank's with per_rank_outputs, and keeps the frames in
         self.sent (chunk c's frames are rank c's)."""
@@ -146,6 +147,28 @@ class SegmentedAllgatherv:
         self.sent = [f for f, _ in sent]
         cur.wait_stream(self.sd)
         cur.wait_stream(self.sc)
+        if _check:
+            for cd in self._codecs.values():
+                cd.check()
+        return [recv[r] for r in ranks] if per_rank_outputs else recv[0]
+
+    def capture(self, xs, eb: float, per_rank_outputs: bool = False):
+        """Record the whole exchange (P compressions, every decompression on
+        the second stream, the events between them) into one CUDA graph
+        once; returns (graph, outputs).  graph.replay() repeats it on the
+        same input tensors (write new data into them) and outputs, without
+        host work per codec call.  check() reads the device status after
+        replays."""
+        import torch
+        self.run(xs, eb, per_rank_outputs)  # the codecs and their scratch exist before capture
+        side = torch.cuda.Stream(device=self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side, capture_error_mode="relaxed"):
+            outs = self.run(xs, eb, per_rank_outputs, _check=False)
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        return g, outs
+
+    def check(self) -> None:
         for cd in self._codecs.values():
             cd.check()
-        return [recv[r] for r in ranks] if per_rank_outputs else recv[0]

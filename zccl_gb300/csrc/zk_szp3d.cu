@@ -121,28 +121,54 @@ __device__ __forceinline__ void sz3_elem(const Sz3Block &k, uint32_t t, uint64_t
 
 __device__ __forceinline__ uint32_t mag(uint32_t v) { return (int32_t)v < 0 ? 0u - v : v; }
 
-/* ---- K1: rates and payload sizes (one CTA per block) -------------------- */
+/* Blocks go to groups of G threads: a warp per block (G = 32) up to
+ * 512 elements, the whole CTA (G = SZ_THREADS) above. */
+template <uint32_t G>
+__device__ __forceinline__ void group_sync()
+{
+    if (G == 32)
+        __syncwarp();
+    else
+        __syncthreads();
+}
+
+/* ---- K1: rates and payload sizes (a group per block) -------------------- */
+template <uint32_t G>
 __global__ void __launch_bounds__(SZ_THREADS) k_sz3_rates(const int32_t *q, Sz3Dims g, uint8_t *out, uint32_t *sizes)
 {
     __shared__ uint32_t wmax[SZ_THREADS / 32];
-    for (uint64_t b = blockIdx.x; b < g.nblocks; b += gridDim.x) {
-        const Sz3Block k = sz3_block(g, b);
+    const uint32_t per = SZ_THREADS / G, sub = threadIdx.x / G, gt = threadIdx.x % G;
+    for (uint64_t b0 = (uint64_t)blockIdx.x * per; b0 < g.nblocks; b0 += (uint64_t)gridDim.x * per) {
+        const uint64_t b = b0 + sub;
+        const bool live = b < g.nblocks; /* uniform over the group */
         uint32_t m = 0;
-        for (uint32_t t = threadIdx.x; t < k.n; t += blockDim.x) {
-            uint64_t i, j, z;
-            sz3_elem(k, t, i, j, z);
-            m = max(m, mag(sz3_diff(q, g, i, j, z)));
+        Sz3Block k = {};
+        if (live) {
+            k = sz3_block(g, b);
+            for (uint32_t t = gt; t < k.n; t += G) {
+                uint64_t i, j, z;
+                sz3_elem(k, t, i, j, z);
+                m = max(m, mag(sz3_diff(q, g, i, j, z)));
+            }
         }
         m = __reduce_max_sync(0xffffffffu, m);
-        if ((threadIdx.x & 31u) == 0) wmax[threadIdx.x >> 5] = m;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            for (uint32_t w = 1; w < blockDim.x / 32; w++) m = max(m, wmax[w]);
-            const uint32_t rate = 32u - __clz(max(m, wmax[0]));
-            out[b] = (uint8_t)rate;
-            sizes[b] = sz3_payload(rate, k.n);
+        if (G == 32) {
+            if (live && gt == 0) {
+                const uint32_t rate = 32u - __clz(m);
+                out[b] = (uint8_t)rate;
+                sizes[b] = sz3_payload(rate, k.n);
+            }
+        } else {
+            if ((threadIdx.x & 31u) == 0) wmax[threadIdx.x >> 5] = m;
+            __syncthreads();
+            if (threadIdx.x == 0 && live) {
+                for (uint32_t w = 0; w < blockDim.x / 32; w++) m = max(m, wmax[w]);
+                const uint32_t rate = 32u - __clz(m);
+                out[b] = (uint8_t)rate;
+                sizes[b] = sz3_payload(rate, k.n);
+            }
+            __syncthreads();
         }
-        __syncthreads();
     }
 }
 
@@ -252,78 +278,90 @@ __global__ void __launch_bounds__(1024) k_sz3_offsets(const uint32_t *sizes, uin
     }
 }
 
-/* ---- compress K3: pack every block at its offset ------------------------ */
+/* ---- compress K3: pack every block at its offset (a group per block) ---- */
+template <uint32_t G>
 __global__ void __launch_bounds__(SZ_THREADS) k_sz3_pack(const int32_t *q, Sz3Dims g, uint8_t *out, uint64_t cap,
                                                          const uint64_t *offs, uint32_t *err)
 {
-    extern __shared__ uint32_t e[]; /* bs^3 differences */
-    for (uint64_t b = blockIdx.x; b < g.nblocks; b += gridDim.x) {
-        const uint32_t rate = out[b];
-        if (!rate) continue; /* uniform over the CTA */
-        const Sz3Block k = sz3_block(g, b);
+    extern __shared__ uint32_t e_all[]; /* bs^3 differences per group */
+    const uint32_t per = SZ_THREADS / G, sub = threadIdx.x / G, gt = threadIdx.x % G;
+    uint32_t *e = e_all + sub * (g.bs * g.bs * g.bs);
+    for (uint64_t b0 = (uint64_t)blockIdx.x * per; b0 < g.nblocks; b0 += (uint64_t)gridDim.x * per) {
+        const uint64_t b = b0 + sub;
+        /* every exit below is uniform over the group; a CTA-wide group meets
+         * its barriers in every case */
+        uint32_t rate = b < g.nblocks ? out[b] : 0u;
+        const Sz3Block k = rate ? sz3_block(g, b) : Sz3Block{};
         const uint32_t n = k.n, B = rate >> 3, r = rate & 7u, ns = (n + 7) / 8;
-        const uint64_t base = g.nblocks + offs[b];
-        if (base + sz3_payload(rate, n) > cap) { /* uniform: the stream does not fit */
-            if (threadIdx.x == 0) atomicOr(err, ZERR_CAPACITY);
-            continue;
+        const uint64_t base = rate ? g.nblocks + offs[b] : 0;
+        if (rate && base + sz3_payload(rate, n) > cap) {
+            if (gt == 0) atomicOr(err, ZERR_CAPACITY);
+            rate = 0;
         }
-        for (uint32_t t = threadIdx.x; t < n; t += blockDim.x) {
-            uint64_t i, j, z;
-            sz3_elem(k, t, i, j, z);
-            e[t] = sz3_diff(q, g, i, j, z);
+        if (rate) {
+            for (uint32_t t = gt; t < n; t += G) {
+                uint64_t i, j, z;
+                sz3_elem(k, t, i, j, z);
+                e[t] = sz3_diff(q, g, i, j, z);
+            }
         }
-        __syncthreads();
-        uint8_t *o = out + base;
-        /* signs: bit 7 - t % 8 of byte t / 8 */
-        for (uint32_t c = threadIdx.x; c < ns; c += blockDim.x) {
-            uint32_t v = 0;
-            for (uint32_t u = 0; u < 8 && 8 * c + u < n; u++) v |= ((e[8 * c + u] >> 31) & 1u) << (7 - u);
-            o[c] = (uint8_t)v;
-        }
-        /* high bytes: element t's B bytes, little-endian */
-        uint8_t *h = o + ns;
-        for (uint32_t c = threadIdx.x; c < B * n; c += blockDim.x) {
-            const uint32_t t = c / B, byte = c % B;
-            h[c] = (uint8_t)((mag(e[t]) >> r) >> (8 * byte));
-        }
-        /* low bits: eight elements fill r bytes, MSB first */
-        if (r) {
-            uint8_t *l = h + B * n;
-            const uint32_t mask = (1u << r) - 1u, ng = (n + 7) / 8, tail = (r * n + 7) / 8;
-            for (uint32_t gi = threadIdx.x; gi < ng; gi += blockDim.x) {
-                uint64_t acc = 0;
-                for (uint32_t u = 0; u < 8; u++) {
-                    const uint32_t t = 8 * gi + u;
-                    acc = (acc << r) | (t < n ? (mag(e[t]) & mask) : 0u);
-                }
-                /* 8 r bits: byte gi * r + m is bits [8 m, 8 m + 8) from the top */
-                for (uint32_t m = 0; m < r; m++) {
-                    const uint32_t at = gi * r + m;
-                    if (at < tail) l[at] = (uint8_t)(acc >> (8 * (r - 1 - m)));
+        group_sync<G>();
+        if (rate) {
+            uint8_t *o = out + base;
+            /* signs: bit 7 - t % 8 of byte t / 8 */
+            for (uint32_t c = gt; c < ns; c += G) {
+                uint32_t v = 0;
+                for (uint32_t u = 0; u < 8 && 8 * c + u < n; u++) v |= ((e[8 * c + u] >> 31) & 1u) << (7 - u);
+                o[c] = (uint8_t)v;
+            }
+            /* high bytes: element t's B bytes, little-endian */
+            uint8_t *h = o + ns;
+            for (uint32_t c = gt; c < B * n; c += G) {
+                const uint32_t t = c / B, byte = c % B;
+                h[c] = (uint8_t)((mag(e[t]) >> r) >> (8 * byte));
+            }
+            /* low bits: eight elements fill r bytes, MSB first */
+            if (r) {
+                uint8_t *l = h + B * n;
+                const uint32_t mask = (1u << r) - 1u, ng = (n + 7) / 8, tail = (r * n + 7) / 8;
+                for (uint32_t gi = gt; gi < ng; gi += G) {
+                    uint64_t acc = 0;
+                    for (uint32_t u = 0; u < 8; u++) {
+                        const uint32_t t = 8 * gi + u;
+                        acc = (acc << r) | (t < n ? (mag(e[t]) & mask) : 0u);
+                    }
+                    for (uint32_t m = 0; m < r; m++) {
+                        const uint32_t at = gi * r + m;
+                        if (at < tail) l[at] = (uint8_t)(acc >> (8 * (r - 1 - m)));
+                    }
                 }
             }
         }
-        __syncthreads();
+        group_sync<G>();
     }
 }
 
-/* ---- decompress K3: every block's differences into the volume ---------- */
+/* ---- decompress K3: every block's differences into the volume (a group per block) */
+template <uint32_t G>
 __global__ void __launch_bounds__(SZ_THREADS) k_sz3_unpack(const uint8_t *in, uint64_t avail, Sz3Dims g,
                                                            const uint64_t *offs, uint32_t *vol, uint32_t *err)
 {
     const uint64_t s0 = g.d2 * g.d3, s1 = g.d3;
-    for (uint64_t b = blockIdx.x; b < g.nblocks; b += gridDim.x) {
+    const uint32_t per = SZ_THREADS / G, sub = threadIdx.x / G, gt = threadIdx.x % G;
+    for (uint64_t b0 = (uint64_t)blockIdx.x * per; b0 < g.nblocks; b0 += (uint64_t)gridDim.x * per) {
+        const uint64_t b = b0 + sub;
+        if (b >= g.nblocks) continue; /* no barrier below */
         const Sz3Block k = sz3_block(g, b);
         uint32_t rate = b < avail ? in[b] : 0u;
         const uint64_t base = g.nblocks + offs[b];
         const uint32_t n = k.n;
         if (rate > 32 || base + sz3_payload(rate, n) > avail) { /* uniform over the CTA */
-            if (threadIdx.x == 0) atomicOr(err, rate > 32 ? ZERR_CORRUPT : ZERR_BOUNDS);
+            if (gt == 0) atomicOr(err, rate > 32 ? ZERR_CORRUPT : ZERR_BOUNDS);
             rate = 0;
         }
         const uint32_t B = rate >> 3, r = rate & 7u, ns = (n + 7) / 8;
         const uint8_t *sg = in + base, *h = sg + ns, *l = h + B * n;
-        for (uint32_t t = threadIdx.x; t < n; t += blockDim.x) {
+        for (uint32_t t = gt; t < n; t += G) {
             uint32_t v = 0;
             if (rate) {
                 for (uint32_t byte = 0; byte < B; byte++) v |= (uint32_t)h[t * B + byte] << (8 * byte);
@@ -459,13 +497,23 @@ cudaError_t sz3_compress(uint8_t *out, uint64_t cap, const float *x, uint64_t d1
     k_sz3_quant<<<grid_for(n, 1024), 256, 0, st>>>(x, w.q, n, 0.5 / eb, w.err);
     /* the rate table is part of the stream: cap must hold it */
     if (cap < g.nblocks) return cudaErrorInvalidValue;
-    k_sz3_rates<<<grid_for(g.nblocks, 1), SZ_THREADS, 0, st>>>(w.q, g, out, w.sizes);
+    const bool wb = bs * bs * bs <= 512; /* a warp per block */
+    if (wb)
+        k_sz3_rates<32><<<grid_for(g.nblocks, SZ_THREADS / 32), SZ_THREADS, 0, st>>>(w.q, g, out, w.sizes);
+    else
+        k_sz3_rates<SZ_THREADS><<<grid_for(g.nblocks, 1), SZ_THREADS, 0, st>>>(w.q, g, out, w.sizes);
     if ((e = sz3_scan(g, w, st)) != cudaSuccess) return e;
-    const size_t smem = 4ull * bs * bs * bs;
-    if (smem > 48 * 1024 &&
-        (e = cudaFuncSetAttribute(k_sz3_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
-        return e;
-    k_sz3_pack<<<grid_for(g.nblocks, 1), SZ_THREADS, smem, st>>>(w.q, g, out, cap, w.offs, w.err);
+    if (wb) {
+        k_sz3_pack<32><<<grid_for(g.nblocks, SZ_THREADS / 32), SZ_THREADS, 4ull * bs * bs * bs * (SZ_THREADS / 32), st>>>(
+            w.q, g, out, cap, w.offs, w.err);
+    } else {
+        const size_t smem = 4ull * bs * bs * bs;
+        if (smem > 48 * 1024 && (e = cudaFuncSetAttribute(k_sz3_pack<SZ_THREADS>,
+                                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+                                    cudaSuccess)
+            return e;
+        k_sz3_pack<SZ_THREADS><<<grid_for(g.nblocks, 1), SZ_THREADS, smem, st>>>(w.q, g, out, cap, w.offs, w.err);
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     return d_size ? cudaMemcpyAsync(d_size, w.total, 8, cudaMemcpyDeviceToDevice, st) : cudaSuccess;
 }
@@ -480,7 +528,10 @@ cudaError_t sz3_decompress(float *y, const uint8_t *in, uint64_t avail, uint64_t
     k_sz3_sizes<<<grid_for(g.nblocks, 256), 256, 0, st>>>(in, avail, g, w.sizes, w.err);
     if ((e = sz3_scan(g, w, st)) != cudaSuccess) return e;
     uint32_t *vol = reinterpret_cast<uint32_t *>(y);
-    k_sz3_unpack<<<grid_for(g.nblocks, 1), SZ_THREADS, 0, st>>>(in, avail, g, w.offs, vol, w.err);
+    if (bs * bs * bs <= 512)
+        k_sz3_unpack<32><<<grid_for(g.nblocks, SZ_THREADS / 32), SZ_THREADS, 0, st>>>(in, avail, g, w.offs, vol, w.err);
+    else
+        k_sz3_unpack<SZ_THREADS><<<grid_for(g.nblocks, 1), SZ_THREADS, 0, st>>>(in, avail, g, w.offs, vol, w.err);
     const uint64_t rows = d1 * d2;
     k_sz3_scan_z<<<(unsigned)((rows * 32 + 255) / 256), 256, 0, st>>>(vol, rows, d3);
     k_sz3_scan_y<<<(unsigned)((d1 * d3 + 255) / 256), 256, 0, st>>>(vol, d1, d2, d3);

@@ -32,6 +32,7 @@
 namespace {
 
 constexpr uint32_t WARPS_W1 = 8;
+constexpr uint32_t WARPS_W3 = 16; /* warps per group in W3: two windows each */
 
 __device__ __forceinline__ uint64_t load_u64(const uint8_t *p)
 {
@@ -343,7 +344,7 @@ __global__ void k_walk_segments(const WalkArgs a)
 }
 
 /* ---- W3: the true walk of every window ------------------------------- */
-__global__ void __launch_bounds__(128) k_walk_final(const WalkArgs a)
+__global__ void __launch_bounds__(32 * WARPS_W3) k_walk_final(const WalkArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const ZGeom &g = a.g;
@@ -504,11 +505,11 @@ cudaError_t launch_walk(const WalkArgs &a0, cudaStream_t st)
     k_walk_segments<<<a.g.T, 256, smem2, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const uint32_t wstride = (uint32_t)walk_w1_warp_bytes(a.M);
-    const uint32_t smem3 = 12 * WALK_G + 4 * wstride;
+    const uint32_t smem3 = 12 * WALK_G + WARPS_W3 * wstride;
     if ((e = cudaFuncSetAttribute(k_walk_final, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   smem3)) != cudaSuccess)
         return e;
-    k_walk_final<<<a.max_groups, 128, smem3, st>>>(a);
+    k_walk_final<<<a.max_groups, 32 * WARPS_W3, smem3, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     k_walk_finish<<<1, 32, 0, st>>>(a);
     return cudaGetLastError();
