@@ -102,3 +102,31 @@ def test_dropin_host_and_device_pointers(torch):
         dy = torch.zeros(x.size, dtype=torch.float32, device="cuda")
         Z3.SZp_decompress3D(dy, dout, *dims, bs, eb)
         assert sha(dy.cpu().numpy()) == c["dec"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("eb", [1e-4 * 1.37, 2.0 ** -9, 3.3e-7])
+def test_gpu_rounding_near_ties(torch, port, eb):
+    """Inputs placed on and one to three ulps either side of the points where
+    x * (0.5 / eb) + 0.5 is an integer, with quantized values up to 2^27 (both
+    sides of 2^24 and 2^26), so that quantization and reconstruction meet the
+    cases their double rounding decides; stream and floats must equal the
+    oracle's bit for bit."""
+    from zccl_gb300.szp3d import Szp3D
+    dims, bs = (48, 40, 56), 4
+    n = dims[0] * dims[1] * dims[2]
+    rng = np.random.default_rng(7)
+    inv = 0.5 / eb
+    mag = np.where(rng.random(n) < 0.5, 2.0 ** 12, 2.0 ** rng.integers(20, 28, n))
+    j = np.floor(rng.uniform(-1, 1, n) * mag)
+    x = ((j - 0.5) / inv).astype(np.float32)
+    x = (x.view(np.int32) + rng.integers(-3, 4, n).astype(np.int32)).view(np.float32)
+    assert np.isfinite(x).all()
+    s = port.szp3d_compress(x, dims, bs, eb)
+    codec = Szp3D(dims, bs)
+    buf, size = codec.compress(torch.from_numpy(x).cuda(), eb)
+    m = codec.size(size)
+    assert buf[:m].cpu().numpy().tobytes() == s
+    y = codec.decompress(buf, eb, avail=m).cpu().numpy()
+    codec.check()
+    assert np.array_equal(y.view(np.uint32), port.szp3d_decompress(s, dims, bs, eb).view(np.uint32))

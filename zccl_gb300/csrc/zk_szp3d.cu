@@ -10,8 +10,9 @@
  * its inverse is the 3-D prefix sum.  So here every step is data parallel:
  *
  * compress   K0  q = (int)floor((double)x * (0.5 / eb) + 0.5) for every
- *                element (ZCCL_float.h:57-61), in FP64 so that the rounding
- *                is the reference's, into an int32 volume;
+ *                element (ZCCL_float.h:57-61) with the reference's double
+ *                rounding (float pairs where that is provably the same,
+ *                FP64 for the rest), into an int32 volume;
  *            K1  one CTA per block: the differences of its elements, their
  *                largest magnitude, the rate (its bit length) into the
  *                rate table at the stream's start, the payload size;
@@ -83,20 +84,86 @@ __host__ __device__ inline uint32_t sz3_payload(uint32_t b, uint32_t n)
     return (n + 7) / 8 + (b >> 3) * n + ((b & 7u) * n + 7) / 8;
 }
 
+/* A double as a pair of floats, hi = RN(d), lo = RN(d - hi), so that
+ * hi + lo is within 2^-48 of d; ok only where both are normal floats
+ * (2^-90 <= d <= 2^90), else the kernels take the double steps. */
+struct Sz3Split {
+    double d;
+    float hi, lo;
+    int ok;
+};
+
+Sz3Split sz3_split(double d)
+{
+    Sz3Split s;
+    s.d = d;
+    s.hi = (float)d;
+    s.lo = (float)(d - (double)s.hi);
+    s.ok = d >= 0x1p-90 && d <= 0x1p90;
+    return s;
+}
+
+/* (int)floor((double)x * inv + 0.5), each step rounded as double
+ * arithmetic rounds it (ZCCL_float.h:57-61).  FP64 is slow on this GPU, so
+ * the product is first formed as a float pair: hi = x*ih, its exact error
+ * by FMA, plus x*il, within 2^-19 of x*inv + 0.5 when |x*ih| < 2^26.  When
+ * the fractional part of that sum is more than 2^-12 from an integer, no
+ * rounding of the exact product (at most 2^-27 here) can move it across
+ * one, so its floor is the reference's; otherwise (about one element in
+ * two thousand, or out of range, or not finite) the double steps run as
+ * they are.  *bad is set where the reference is undefined. */
+__device__ __forceinline__ int32_t sz3_quantize(float x, const Sz3Split &inv, uint32_t &bad)
+{
+    const float th = __fmul_rn(x, inv.hi);
+    if (inv.ok && fabsf(th) < 67108864.0f) { /* 2^26; NaN takes the double path */
+        const float tl = __fmaf_rn(x, inv.lo, __fmaf_rn(x, inv.hi, -th));
+        const float s = __fadd_rn(th, 0.5f); /* th + 0.5 = s + e exactly (TwoSum) */
+        const float bb = __fsub_rn(s, th);
+        const float e = __fadd_rn(__fsub_rn(th, __fsub_rn(s, bb)), __fsub_rn(0.5f, bb));
+        const float n = floorf(s);
+        float fr = __fadd_rn(__fsub_rn(s, n), __fadd_rn(e, tl));
+        const float m = floorf(fr);
+        fr = __fsub_rn(fr, m);
+        if (fr > 2.44140625e-4f && fr < 0.999755859375f) return (int32_t)n + (int32_t)m;
+    }
+    const double v = floor(__dadd_rn(__dmul_rn((double)x, inv.d), 0.5));
+    if (!(v >= -2147483648.0 && v < 2147483648.0)) { /* not finite, or outside int: undefined in the reference */
+        bad = 1;
+        return 0;
+    }
+    return (int32_t)v;
+}
+
+/* (float)((double)q * twice) (ZCCLd_float.c:2857): with the product as a
+ * float pair (within 2^-22 of an ulp of the result for |q| < 2^24), its
+ * nearest float is the reference's unless the pair lies within 2^-18 of
+ * half an ulp from it (a midpoint the double rounding could decide) or the
+ * result is a power of two or tiny; those take the double steps. */
+__device__ __forceinline__ float sz3_value(int32_t q, const Sz3Split &tw)
+{
+    if (tw.ok && q == 0) return 0.0f;
+    if (tw.ok && q > -16777216 && q < 16777216) {
+        const float qf = (float)q;
+        const float hi = __fmul_rn(qf, tw.hi);
+        const float lo = __fmaf_rn(qf, tw.lo, __fmaf_rn(qf, tw.hi, -hi));
+        const float r = __fadd_rn(hi, lo);
+        const uint32_t rb = __float_as_uint(r) & 0x7FFFFFFFu, ex = rb >> 23;
+        if (ex > 24u && ex < 254u && (rb & 0x7FFFFFu) != 0u) {
+            const float half = __uint_as_float((ex - 24u) << 23); /* half an ulp of r */
+            const float d = __fadd_rn(__fsub_rn(hi, r), lo);      /* (hi + lo) - r */
+            if (fabsf(d) < __fmul_rn(half, 0.999996185302734375f)) return r; /* 1 - 2^-18 */
+        }
+    }
+    return (float)__dmul_rn((double)q, tw.d);
+}
+
 /* ---- K0: quantization -------------------------------------------------- */
-__global__ void k_sz3_quant(const float *__restrict__ x, int32_t *__restrict__ q, uint64_t n, double inv,
+__global__ void k_sz3_quant(const float *__restrict__ x, int32_t *__restrict__ q, uint64_t n, Sz3Split inv,
                             uint32_t *err)
 {
     uint32_t bad = 0;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const double v = floor(__dadd_rn(__dmul_rn((double)x[i], inv), 0.5));
-        if (!(v >= -2147483648.0 && v < 2147483648.0)) { /* not finite, or outside int: undefined in the reference */
-            bad = 1;
-            q[i] = 0;
-        } else {
-            q[i] = (int32_t)v;
-        }
-    }
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        q[i] = sz3_quantize(x[i], inv, bad);
     if (bad) atomicOr(err, ZERR_RANGE);
 }
 
@@ -414,7 +481,7 @@ __global__ void k_sz3_scan_y(uint32_t *vol, uint64_t d1, uint64_t d2, uint64_t d
 }
 
 /* x: a thread per (j, k), i sequential; writes the floats in place */
-__global__ void k_sz3_scan_x(uint32_t *vol, uint64_t d1, uint64_t plane, double twice)
+__global__ void k_sz3_scan_x(uint32_t *vol, uint64_t d1, uint64_t plane, Sz3Split twice)
 {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= plane) return;
@@ -422,7 +489,7 @@ __global__ void k_sz3_scan_x(uint32_t *vol, uint64_t d1, uint64_t plane, double 
 #pragma unroll 8
     for (uint64_t i = 0; i < d1; i++) {
         run += vol[i * plane + t];
-        reinterpret_cast<float *>(vol)[i * plane + t] = (float)__dmul_rn((double)(int32_t)run, twice);
+        reinterpret_cast<float *>(vol)[i * plane + t] = sz3_value((int32_t)run, twice);
     }
 }
 
@@ -494,7 +561,7 @@ cudaError_t sz3_compress(uint8_t *out, uint64_t cap, const float *x, uint64_t d1
     cudaError_t e = cudaMemsetAsync(w.err, 0, 16, st);
     if (e != cudaSuccess) return e;
     const uint64_t n = d1 * d2 * d3;
-    k_sz3_quant<<<grid_for(n, 1024), 256, 0, st>>>(x, w.q, n, 0.5 / eb, w.err);
+    k_sz3_quant<<<grid_for(n, 1024), 256, 0, st>>>(x, w.q, n, sz3_split(0.5 / eb), w.err);
     /* the rate table is part of the stream: cap must hold it */
     if (cap < g.nblocks) return cudaErrorInvalidValue;
     const bool wb = bs * bs * bs <= 512; /* a warp per block */
@@ -535,6 +602,6 @@ cudaError_t sz3_decompress(float *y, const uint8_t *in, uint64_t avail, uint64_t
     const uint64_t rows = d1 * d2;
     k_sz3_scan_z<<<(unsigned)((rows * 32 + 255) / 256), 256, 0, st>>>(vol, rows, d3);
     k_sz3_scan_y<<<(unsigned)((d1 * d3 + 255) / 256), 256, 0, st>>>(vol, d1, d2, d3);
-    k_sz3_scan_x<<<(unsigned)((d2 * d3 + 255) / 256), 256, 0, st>>>(vol, d1, d2 * d3, eb * 2);
+    k_sz3_scan_x<<<(unsigned)((d2 * d3 + 255) / 256), 256, 0, st>>>(vol, d1, d2 * d3, sz3_split(eb * 2));
     return cudaGetLastError();
 }
