@@ -36,6 +36,7 @@ namespace {
 
 constexpr uint32_t SZ_THREADS = 256;
 constexpr uint32_t SZ_CHUNK = 2048; /* sizes per CTA in the scan */
+constexpr uint32_t SZ_SCAN_BATCH = 8; /* rows loaded together in the y and x prefix sums */
 
 struct Sz3Dims {
     uint64_t d1, d2, d3;
@@ -345,6 +346,64 @@ __global__ void __launch_bounds__(1024) k_sz3_offsets(const uint32_t *sizes, uin
     }
 }
 
+/* One block's n differences e[] (element order) packed at o with rate
+ * `rate` > 0: sign bits (bit 7 - t % 8 of byte t / 8), B = rate/8 high
+ * bytes per element (little-endian), then the r = rate%8 low bits, eight
+ * elements to r bytes, MSB first; every byte by one of G threads (gt). */
+template <uint32_t G>
+__device__ __forceinline__ void sz3_pack_block(const uint32_t *e, uint32_t n, uint32_t rate, uint8_t *o, uint32_t gt)
+{
+    const uint32_t B = rate >> 3, r = rate & 7u, ns = (n + 7) / 8;
+    for (uint32_t c = gt; c < ns; c += G) {
+        uint32_t v = 0;
+        for (uint32_t u = 0; u < 8 && 8 * c + u < n; u++) v |= ((e[8 * c + u] >> 31) & 1u) << (7 - u);
+        o[c] = (uint8_t)v;
+    }
+    uint8_t *h = o + ns;
+    if (B == 1) {
+        for (uint32_t t = gt; t < n; t += G) h[t] = (uint8_t)(mag(e[t]) >> r);
+    } else {
+        for (uint32_t c = gt; c < B * n; c += G) {
+            const uint32_t t = c / B, byte = c % B;
+            h[c] = (uint8_t)((mag(e[t]) >> r) >> (8 * byte));
+        }
+    }
+    if (r) {
+        uint8_t *l = h + B * n;
+        const uint32_t mask = (1u << r) - 1u, ng = (n + 7) / 8, tail = (r * n + 7) / 8;
+        for (uint32_t gi = gt; gi < ng; gi += G) {
+            uint64_t acc = 0;
+            for (uint32_t u = 0; u < 8; u++) {
+                const uint32_t t = 8 * gi + u;
+                acc = (acc << r) | (t < n ? (mag(e[t]) & mask) : 0u);
+            }
+            for (uint32_t m = 0; m < r; m++) {
+                const uint32_t at = gi * r + m;
+                if (at < tail) l[at] = (uint8_t)(acc >> (8 * (r - 1 - m)));
+            }
+        }
+    }
+}
+
+/* Element t of a block packed at `sg` with rate <= 32 (0: all zero). */
+__device__ __forceinline__ uint32_t sz3_unpack_elem(const uint8_t *sg, uint32_t rate, uint32_t n, uint32_t t)
+{
+    if (!rate) return 0u;
+    const uint32_t B = rate >> 3, r = rate & 7u, ns = (n + 7) / 8;
+    const uint8_t *h = sg + ns, *l = h + B * n;
+    uint32_t v = 0;
+    for (uint32_t byte = 0; byte < B; byte++) v |= (uint32_t)h[t * B + byte] << (8 * byte);
+    v <<= r;
+    if (r) { /* bits [t r, t r + r) of the low section, MSB first */
+        const uint64_t bit = (uint64_t)t * r;
+        const uint64_t by = bit >> 3;
+        const uint32_t w = ((uint32_t)l[by] << 8) | (by + 1 < (r * (uint64_t)n + 7) / 8 ? l[by + 1] : 0u);
+        v |= (w >> (16 - (uint32_t)(bit & 7u) - r)) & ((1u << r) - 1u);
+    }
+    if ((sg[t >> 3] >> (7 - (t & 7u))) & 1u) v = 0u - v;
+    return v;
+}
+
 /* ---- compress K3: pack every block at its offset (a group per block) ---- */
 template <uint32_t G>
 __global__ void __launch_bounds__(SZ_THREADS) k_sz3_pack(const int32_t *q, Sz3Dims g, uint8_t *out, uint64_t cap,
@@ -359,7 +418,7 @@ __global__ void __launch_bounds__(SZ_THREADS) k_sz3_pack(const int32_t *q, Sz3Di
          * its barriers in every case */
         uint32_t rate = b < g.nblocks ? out[b] : 0u;
         const Sz3Block k = rate ? sz3_block(g, b) : Sz3Block{};
-        const uint32_t n = k.n, B = rate >> 3, r = rate & 7u, ns = (n + 7) / 8;
+        const uint32_t n = k.n;
         const uint64_t base = rate ? g.nblocks + offs[b] : 0;
         if (rate && base + sz3_payload(rate, n) > cap) {
             if (gt == 0) atomicOr(err, ZERR_CAPACITY);
@@ -373,37 +432,7 @@ __global__ void __launch_bounds__(SZ_THREADS) k_sz3_pack(const int32_t *q, Sz3Di
             }
         }
         group_sync<G>();
-        if (rate) {
-            uint8_t *o = out + base;
-            /* signs: bit 7 - t % 8 of byte t / 8 */
-            for (uint32_t c = gt; c < ns; c += G) {
-                uint32_t v = 0;
-                for (uint32_t u = 0; u < 8 && 8 * c + u < n; u++) v |= ((e[8 * c + u] >> 31) & 1u) << (7 - u);
-                o[c] = (uint8_t)v;
-            }
-            /* high bytes: element t's B bytes, little-endian */
-            uint8_t *h = o + ns;
-            for (uint32_t c = gt; c < B * n; c += G) {
-                const uint32_t t = c / B, byte = c % B;
-                h[c] = (uint8_t)((mag(e[t]) >> r) >> (8 * byte));
-            }
-            /* low bits: eight elements fill r bytes, MSB first */
-            if (r) {
-                uint8_t *l = h + B * n;
-                const uint32_t mask = (1u << r) - 1u, ng = (n + 7) / 8, tail = (r * n + 7) / 8;
-                for (uint32_t gi = gt; gi < ng; gi += G) {
-                    uint64_t acc = 0;
-                    for (uint32_t u = 0; u < 8; u++) {
-                        const uint32_t t = 8 * gi + u;
-                        acc = (acc << r) | (t < n ? (mag(e[t]) & mask) : 0u);
-                    }
-                    for (uint32_t m = 0; m < r; m++) {
-                        const uint32_t at = gi * r + m;
-                        if (at < tail) l[at] = (uint8_t)(acc >> (8 * (r - 1 - m)));
-                    }
-                }
-            }
-        }
+        if (rate) sz3_pack_block<G>(e, n, rate, out + base, gt);
         group_sync<G>();
     }
 }
@@ -426,26 +455,257 @@ __global__ void __launch_bounds__(SZ_THREADS) k_sz3_unpack(const uint8_t *in, ui
             if (gt == 0) atomicOr(err, rate > 32 ? ZERR_CORRUPT : ZERR_BOUNDS);
             rate = 0;
         }
-        const uint32_t B = rate >> 3, r = rate & 7u, ns = (n + 7) / 8;
-        const uint8_t *sg = in + base, *h = sg + ns, *l = h + B * n;
+        const uint8_t *sg = in + base;
         for (uint32_t t = gt; t < n; t += G) {
-            uint32_t v = 0;
-            if (rate) {
-                for (uint32_t byte = 0; byte < B; byte++) v |= (uint32_t)h[t * B + byte] << (8 * byte);
-                v <<= r;
-                if (r) { /* bits [t r, t r + r) of the low section, MSB first */
-                    const uint64_t bit = (uint64_t)t * r;
-                    const uint64_t by = bit >> 3;
-                    const uint32_t w = ((uint32_t)l[by] << 8) | (by + 1 < (r * (uint64_t)n + 7) / 8 ? l[by + 1] : 0u);
-                    v |= (w >> (16 - (uint32_t)(bit & 7u) - r)) & ((1u << r) - 1u);
-                }
-                if ((sg[t >> 3] >> (7 - (t & 7u))) & 1u) v = 0u - v;
-            }
+            const uint32_t v = sz3_unpack_elem(sg, rate, n, t);
             uint64_t i, j, z;
             sz3_elem(k, t, i, j, z);
             vol[i * s0 + j * s1 + z] = v;
         }
     }
+}
+
+/* ---- block sides 2, 4 and 8: row-mapped kernels -------------------------
+ * A warp takes a unit of U = 32 / BS consecutive blocks along z with the
+ * same block row and plane: lane l owns z = z0 + l, in block l / BS.  It
+ * walks the unit's rows plane by plane, row by row (the order of the
+ * elements in a block), loads each row of x once, coalesced, quantizes it
+ * and forms the mixed difference from neighbours it holds: the z neighbour
+ * by a shuffle (lane 0 loads its own), the previous row's z-difference and
+ * the previous plane's 2-D differences in registers.  The row and plane
+ * before the unit come in once more for that (zeros outside the volume).
+ * So compress reads x twice (rates, then packing) and keeps no quantized
+ * volume; decompress writes whole rows. */
+struct Sz3Unit {
+    uint64_t bi, bj, bk0, i0, j0, z0;
+    uint32_t sx, sy;
+};
+
+template <uint32_t BS>
+__host__ __device__ inline uint64_t sz3_units(const Sz3Dims &g)
+{
+    return g.nb1 * g.nb2 * ((g.nb3 + 32 / BS - 1) / (32 / BS));
+}
+
+template <uint32_t BS>
+__device__ __forceinline__ Sz3Unit sz3_unit(const Sz3Dims &g, uint64_t u)
+{
+    constexpr uint32_t U = 32 / BS;
+    const uint64_t nzc = (g.nb3 + U - 1) / U;
+    Sz3Unit k;
+    k.bj = (u / nzc) % g.nb2;
+    k.bi = u / (nzc * g.nb2);
+    k.bk0 = (u % nzc) * U;
+    k.i0 = k.bi * BS;
+    k.j0 = k.bj * BS;
+    k.z0 = k.bk0 * BS;
+    k.sx = (uint32_t)min((uint64_t)BS, g.d1 - k.i0);
+    k.sy = (uint32_t)min((uint64_t)BS, g.d2 - k.j0);
+    return k;
+}
+
+/* Extent along z of the unit's block c (0 past the volume). */
+template <uint32_t BS>
+__device__ __forceinline__ uint32_t sz3_unit_sz(const Sz3Dims &g, const Sz3Unit &k, uint32_t c)
+{
+    const uint64_t bk = k.bk0 + c;
+    return bk < g.nb3 ? (uint32_t)min((uint64_t)BS, g.d3 - bk * BS) : 0u;
+}
+
+/* row(di, dj, e): the difference at (i0 + di, j0 + dj, z0 + lane) for every
+ * lane (meaningless where z0 + lane >= d3); called by the whole warp. */
+template <uint32_t BS, class Row>
+__device__ __forceinline__ void sz3_walk(const float *__restrict__ x, const Sz3Dims &g, const Sz3Split &inv,
+                                         const Sz3Unit &k, uint32_t &bad, Row row)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t s0 = g.d2 * g.d3, s1 = g.d3, z = k.z0 + lane;
+    const bool zin = z < g.d3;
+    auto live = [&](uint32_t r) { return r == 0 ? k.j0 > 0 : r - 1 < k.sy; }; /* row j0 - 1 + r */
+    /* plane i's rows j0 - 1 .. j0 + BS - 1 (v), and in lane r the element
+     * before z0 of row r (l), which lane 0 needs; all loads issued before
+     * any is used; rows outside read as 0 */
+    auto load = [&](uint64_t i, float (&v)[BS + 1], float &l) {
+#pragma unroll
+        for (uint32_t r = 0; r <= BS; r++) {
+            const uint64_t o = i * s0 + (k.j0 + r - 1) * s1; /* wraps only where not live */
+            v[r] = live(r) && zin ? x[o + z] : 0.0f;
+        }
+        const uint64_t o = i * s0 + (k.j0 + lane - 1) * s1;
+        l = lane <= BS && live(lane) && k.z0 ? x[o + k.z0 - 1] : 0.0f;
+    };
+    uint32_t dp[BS]; /* the previous plane's 2-D differences, row by row */
+#pragma unroll
+    for (uint32_t dj = 0; dj < BS; dj++) dp[dj] = 0;
+    int di = k.i0 ? -1 : 0;
+    float cv[BS + 1], nv[BS + 1], cl, nl = 0.0f;
+    load((uint64_t)((int64_t)k.i0 + di), cv, cl);
+    for (; di < (int)k.sx; di++) {
+        if (di + 1 < (int)k.sx) load(k.i0 + (uint64_t)(di + 1), nv, nl); /* the next plane, in flight meanwhile */
+        const uint32_t qleft = (uint32_t)sz3_quantize(cl, inv, bad); /* 0 where cl is */
+        auto zdiff = [&](uint32_t r) -> uint32_t {                   /* q(z) - q(z - 1) of row r */
+            const uint32_t q = zin ? (uint32_t)sz3_quantize(cv[r], inv, bad) : 0u;
+            const uint32_t up = __shfl_up_sync(0xffffffffu, q, 1), l0 = __shfl_sync(0xffffffffu, qleft, r);
+            return q - (lane ? up : l0);
+        };
+        uint32_t rp = k.j0 ? zdiff(0) : 0u;
+#pragma unroll
+        for (uint32_t dj = 0; dj < BS; dj++) {
+            if (dj < k.sy) {
+                const uint32_t rc = zdiff(dj + 1);
+                const uint32_t d = rc - rp;
+                rp = rc;
+                if (di >= 0) row((uint32_t)di, dj, d - dp[dj]);
+                dp[dj] = d;
+            }
+        }
+#pragma unroll
+        for (uint32_t r = 0; r <= BS; r++) cv[r] = nv[r];
+        cl = nl;
+    }
+}
+
+/* compress K1 (quantization included): a warp per unit */
+template <uint32_t BS>
+__global__ void __launch_bounds__(SZ_THREADS) k_sz3_rates_rows(const float *__restrict__ x, Sz3Dims g, Sz3Split inv,
+                                                               uint8_t *out, uint32_t *sizes, uint32_t *err)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t units = sz3_units<BS>(g);
+    uint32_t bad = 0;
+    for (uint64_t u = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < units;
+         u += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+        const Sz3Unit k = sz3_unit<BS>(g, u);
+        uint32_t m = 0;
+        sz3_walk<BS>(x, g, inv, k, bad, [&](uint32_t, uint32_t, uint32_t e) { m = max(m, mag(e)); });
+        if (k.z0 + lane >= g.d3) m = 0;
+#pragma unroll
+        for (uint32_t o = 1; o < BS; o <<= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        const uint32_t sz = sz3_unit_sz<BS>(g, k, lane / BS);
+        if (lane % BS == 0 && sz) {
+            const uint64_t b = (k.bi * g.nb2 + k.bj) * g.nb3 + k.bk0 + lane / BS;
+            const uint32_t rate = 32u - __clz(m);
+            out[b] = (uint8_t)rate;
+            sizes[b] = sz3_payload(rate, k.sx * k.sy * sz);
+        }
+    }
+    if (bad) atomicOr(err, ZERR_RANGE);
+}
+
+/* compress K3 (quantization included): a warp per unit; the unit's
+ * differences go to shared memory in element order, then each block is
+ * packed by the whole warp */
+template <uint32_t BS>
+__global__ void __launch_bounds__(SZ_THREADS) k_sz3_pack_rows(const float *__restrict__ x, Sz3Dims g, Sz3Split inv,
+                                                              uint8_t *out, uint64_t cap, const uint64_t *offs,
+                                                              uint32_t *err)
+{
+    constexpr uint32_t U = 32 / BS, NB = BS * BS * BS;
+    extern __shared__ uint32_t e_all[]; /* U blocks per warp */
+    const uint32_t lane = threadIdx.x & 31u, dz = lane % BS;
+    uint32_t *e = e_all + (threadIdx.x >> 5) * (U * NB);
+    const uint64_t units = sz3_units<BS>(g);
+    uint32_t bad = 0, full = 0;
+    for (uint64_t u = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < units;
+         u += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+        const Sz3Unit k = sz3_unit<BS>(g, u);
+        const uint32_t sz = sz3_unit_sz<BS>(g, k, lane / BS);
+        const bool zin = k.z0 + lane < g.d3;
+        uint32_t *eb = e + (lane / BS) * NB;
+        __syncwarp(); /* the previous unit is packed */
+        sz3_walk<BS>(x, g, inv, k, bad, [&](uint32_t di, uint32_t dj, uint32_t v) {
+            if (zin) eb[(di * k.sy + dj) * sz + dz] = v;
+        });
+        uint32_t rate = 0;
+        uint64_t base = 0;
+        if (lane < U && k.bk0 + lane < g.nb3) { /* lane c: block c's rate and place */
+            const uint64_t b = (k.bi * g.nb2 + k.bj) * g.nb3 + k.bk0 + lane;
+            rate = out[b];
+            base = g.nblocks + offs[b];
+        }
+        __syncwarp();
+        for (uint32_t c = 0; c < U; c++) {
+            const uint32_t rc = __shfl_sync(0xffffffffu, rate, c);
+            const uint64_t bc = __shfl_sync(0xffffffffu, base, c);
+            const uint32_t n = k.sx * k.sy * sz3_unit_sz<BS>(g, k, c);
+            if (!rc || !n) continue; /* uniform */
+            if (bc + sz3_payload(rc, n) > cap) {
+                full = 1;
+                continue;
+            }
+            sz3_pack_block<32>(e + c * NB, n, rc, out + bc, lane);
+        }
+    }
+    if (bad) atomicOr(err, ZERR_RANGE);
+    if (full && lane == 0) atomicOr(err, ZERR_CAPACITY);
+}
+
+/* Bytes that hold a unit's blocks at most (every block at rate 32). */
+template <uint32_t BS>
+__host__ __device__ constexpr uint32_t sz3_unit_stage()
+{
+    return ((32 / BS) * ((BS * BS * BS + 7) / 8 + 4 * BS * BS * BS) + 15) & ~15u;
+}
+
+/* decompress K3: a warp per unit; the unit's blocks, consecutive in the
+ * stream, come into shared memory in one coalesced copy, then every lane
+ * decodes its own elements straight into whole rows of the output */
+template <uint32_t BS>
+__global__ void __launch_bounds__(SZ_THREADS) k_sz3_unpack_rows(const uint8_t *__restrict__ in, uint64_t avail,
+                                                                Sz3Dims g, const uint64_t *__restrict__ offs,
+                                                                uint32_t *__restrict__ vol, uint32_t *err)
+{
+    constexpr uint32_t U = 32 / BS, STAGE = sz3_unit_stage<BS>();
+    extern __shared__ __align__(16) uint8_t st_all[];
+    const uint32_t lane = threadIdx.x & 31u, dz = lane % BS, c = lane / BS;
+    uint8_t *stg = st_all + (threadIdx.x >> 5) * STAGE;
+    const uint64_t units = sz3_units<BS>(g), s0 = g.d2 * g.d3, s1 = g.d3;
+    uint32_t flag = 0;
+    for (uint64_t u = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < units;
+         u += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+        const Sz3Unit k = sz3_unit<BS>(g, u);
+        uint32_t rate = 0;
+        uint64_t base = 0, end = 0;
+        if (lane < U && k.bk0 + lane < g.nb3) { /* lane c: block c's rate and place */
+            const uint64_t b = (k.bi * g.nb2 + k.bj) * g.nb3 + k.bk0 + lane;
+            const uint32_t n = k.sx * k.sy * sz3_unit_sz<BS>(g, k, lane);
+            rate = b < avail ? in[b] : 0u;
+            base = g.nblocks + offs[b];
+            if (rate > 32 || base + sz3_payload(rate, n) > avail) {
+                flag |= rate > 32 ? ZERR_CORRUPT : ZERR_BOUNDS;
+                rate = 0;
+            }
+            end = rate ? base + sz3_payload(rate, n) : 0;
+        }
+        /* blocks follow one another in the stream: the unit's bytes are
+         * [block 0's place, the last end), at most STAGE of them (the places
+         * come from the same rates; checked all the same) */
+        const uint64_t first = __shfl_sync(0xffffffffu, base, 0);
+        if (rate && (base < first || end - first > STAGE)) {
+            flag |= ZERR_CORRUPT;
+            rate = 0;
+            end = 0;
+        }
+#pragma unroll
+        for (uint32_t o = 16; o; o >>= 1) end = max(end, __shfl_xor_sync(0xffffffffu, end, o));
+        const uint32_t nbytes = end > first ? (uint32_t)min(end - first, (uint64_t)STAGE) : 0u;
+        __syncwarp(); /* the previous unit is decoded */
+#pragma unroll 8
+        for (uint32_t t = lane; t < nbytes; t += 32) stg[t] = in[first + t];
+        __syncwarp();
+        const uint32_t rl = __shfl_sync(0xffffffffu, rate, c);
+        const uint64_t bl = __shfl_sync(0xffffffffu, base, c);
+        const uint32_t sz = sz3_unit_sz<BS>(g, k, c), n = k.sx * k.sy * sz;
+        if (k.z0 + lane < g.d3) {
+            const uint8_t *sg = stg + (rl ? bl - first : 0);
+            uint32_t *o = vol + k.i0 * s0 + k.j0 * s1 + k.z0 + lane;
+            for (uint32_t di = 0; di < k.sx; di++)
+#pragma unroll
+                for (uint32_t dj = 0; dj < BS; dj++)
+                    if (dj < k.sy) o[di * s0 + dj * s1] = sz3_unpack_elem(sg, rl, n, (di * k.sy + dj) * sz + dz);
+        }
+    }
+    if (flag) atomicOr(err, flag);
 }
 
 /* ---- decompress K4-K6: the 3-D prefix sum ------------------------------ */
@@ -473,10 +733,15 @@ __global__ void k_sz3_scan_y(uint32_t *vol, uint64_t d1, uint64_t d2, uint64_t d
     const uint64_t i = t / d3, k = t % d3;
     uint32_t *p = vol + i * d2 * d3 + k;
     uint32_t run = 0;
-#pragma unroll 8
-    for (uint64_t j = 0; j < d2; j++) {
-        run += p[j * d3];
-        p[j * d3] = run;
+    for (uint64_t j0 = 0; j0 < d2; j0 += SZ_SCAN_BATCH) { /* the loads of a batch ahead of its stores */
+        uint32_t v[SZ_SCAN_BATCH];
+#pragma unroll
+        for (uint32_t u = 0; u < SZ_SCAN_BATCH; u++) v[u] = j0 + u < d2 ? p[(j0 + u) * d3] : 0u;
+#pragma unroll
+        for (uint32_t u = 0; u < SZ_SCAN_BATCH; u++) {
+            run += v[u];
+            if (j0 + u < d2) p[(j0 + u) * d3] = run;
+        }
     }
 }
 
@@ -486,10 +751,15 @@ __global__ void k_sz3_scan_x(uint32_t *vol, uint64_t d1, uint64_t plane, Sz3Spli
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= plane) return;
     uint32_t run = 0;
-#pragma unroll 8
-    for (uint64_t i = 0; i < d1; i++) {
-        run += vol[i * plane + t];
-        reinterpret_cast<float *>(vol)[i * plane + t] = sz3_value((int32_t)run, twice);
+    for (uint64_t i0 = 0; i0 < d1; i0 += SZ_SCAN_BATCH) {
+        uint32_t v[SZ_SCAN_BATCH];
+#pragma unroll
+        for (uint32_t u = 0; u < SZ_SCAN_BATCH; u++) v[u] = i0 + u < d1 ? vol[(i0 + u) * plane + t] : 0u;
+#pragma unroll
+        for (uint32_t u = 0; u < SZ_SCAN_BATCH; u++) {
+            run += v[u];
+            if (i0 + u < d1) reinterpret_cast<float *>(vol)[(i0 + u) * plane + t] = sz3_value((int32_t)run, twice);
+        }
     }
 }
 
@@ -537,6 +807,42 @@ cudaError_t sz3_scan(const Sz3Dims &g, const Sz3Ws &w, cudaStream_t st)
     return cudaGetLastError();
 }
 
+/* Block sides with the row-mapped kernels. */
+bool sz3_rows(uint32_t bs) { return bs == 2 || bs == 4 || bs == 8; }
+
+template <uint32_t BS>
+cudaError_t sz3_compress_rows(uint8_t *out, uint64_t cap, const float *x, const Sz3Dims &g, const Sz3Ws &w,
+                              const Sz3Split &inv, cudaStream_t st)
+{
+    const uint64_t units = sz3_units<BS>(g);
+    const unsigned grid = grid_for(units, SZ_THREADS / 32);
+    k_sz3_rates_rows<BS><<<grid, SZ_THREADS, 0, st>>>(x, g, inv, out, w.sizes, w.err);
+    cudaError_t e = sz3_scan(g, w, st);
+    if (e != cudaSuccess) return e;
+    const size_t smem = 4ull * 32 * BS * BS * (SZ_THREADS / 32);
+    if (smem > 48 * 1024 &&
+        (e = cudaFuncSetAttribute(k_sz3_pack_rows<BS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+            cudaSuccess)
+        return e;
+    k_sz3_pack_rows<BS><<<grid, SZ_THREADS, smem, st>>>(x, g, inv, out, cap, w.offs, w.err);
+    return cudaGetLastError();
+}
+
+template <uint32_t BS>
+cudaError_t sz3_unpack_rows(const uint8_t *in, uint64_t avail, const Sz3Dims &g, const Sz3Ws &w, uint32_t *vol,
+                            cudaStream_t st)
+{
+    const size_t smem = (size_t)sz3_unit_stage<BS>() * (SZ_THREADS / 32);
+    cudaError_t e;
+    if (smem > 48 * 1024 &&
+        (e = cudaFuncSetAttribute(k_sz3_unpack_rows<BS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+            cudaSuccess)
+        return e;
+    k_sz3_unpack_rows<BS><<<grid_for(sz3_units<BS>(g), SZ_THREADS / 32), SZ_THREADS, smem, st>>>(in, avail, g, w.offs,
+                                                                                                 vol, w.err);
+    return cudaGetLastError();
+}
+
 } // namespace
 
 size_t sz3_workspace_bytes(uint64_t d1, uint64_t d2, uint64_t d3, uint32_t bs, bool compress)
@@ -544,7 +850,7 @@ size_t sz3_workspace_bytes(uint64_t d1, uint64_t d2, uint64_t d3, uint32_t bs, b
     const Sz3Dims g = sz3_dims(d1, d2, d3, bs);
     Sz3Ws w = sz3_bind(nullptr, g);
     const size_t head = (size_t)reinterpret_cast<uintptr_t>(w.q);
-    return head + (compress ? 4 * (size_t)(d1 * d2 * d3) : 0) + 256;
+    return head + (compress && !sz3_rows(bs) ? 4 * (size_t)(d1 * d2 * d3) : 0) + 256;
 }
 
 size_t sz3_max_stream_bytes(uint64_t d1, uint64_t d2, uint64_t d3, uint32_t bs)
@@ -560,10 +866,17 @@ cudaError_t sz3_compress(uint8_t *out, uint64_t cap, const float *x, uint64_t d1
     const Sz3Ws w = sz3_bind(ws, g);
     cudaError_t e = cudaMemsetAsync(w.err, 0, 16, st);
     if (e != cudaSuccess) return e;
-    const uint64_t n = d1 * d2 * d3;
-    k_sz3_quant<<<grid_for(n, 1024), 256, 0, st>>>(x, w.q, n, sz3_split(0.5 / eb), w.err);
     /* the rate table is part of the stream: cap must hold it */
     if (cap < g.nblocks) return cudaErrorInvalidValue;
+    const Sz3Split inv = sz3_split(0.5 / eb);
+    if (sz3_rows(bs)) {
+        e = bs == 2 ? sz3_compress_rows<2>(out, cap, x, g, w, inv, st)
+                    : bs == 4 ? sz3_compress_rows<4>(out, cap, x, g, w, inv, st) : sz3_compress_rows<8>(out, cap, x, g, w, inv, st);
+        if (e != cudaSuccess) return e;
+        return d_size ? cudaMemcpyAsync(d_size, w.total, 8, cudaMemcpyDeviceToDevice, st) : cudaSuccess;
+    }
+    const uint64_t n = d1 * d2 * d3;
+    k_sz3_quant<<<grid_for(n, 1024), 256, 0, st>>>(x, w.q, n, inv, w.err);
     const bool wb = bs * bs * bs <= 512; /* a warp per block */
     if (wb)
         k_sz3_rates<32><<<grid_for(g.nblocks, SZ_THREADS / 32), SZ_THREADS, 0, st>>>(w.q, g, out, w.sizes);
@@ -595,7 +908,11 @@ cudaError_t sz3_decompress(float *y, const uint8_t *in, uint64_t avail, uint64_t
     k_sz3_sizes<<<grid_for(g.nblocks, 256), 256, 0, st>>>(in, avail, g, w.sizes, w.err);
     if ((e = sz3_scan(g, w, st)) != cudaSuccess) return e;
     uint32_t *vol = reinterpret_cast<uint32_t *>(y);
-    if (bs * bs * bs <= 512)
+    if (sz3_rows(bs)) {
+        e = bs == 2 ? sz3_unpack_rows<2>(in, avail, g, w, vol, st)
+                    : bs == 4 ? sz3_unpack_rows<4>(in, avail, g, w, vol, st) : sz3_unpack_rows<8>(in, avail, g, w, vol, st);
+        if (e != cudaSuccess) return e;
+    } else if (bs * bs * bs <= 512)
         k_sz3_unpack<32><<<grid_for(g.nblocks, SZ_THREADS / 32), SZ_THREADS, 0, st>>>(in, avail, g, w.offs, vol, w.err);
     else
         k_sz3_unpack<SZ_THREADS><<<grid_for(g.nblocks, 1), SZ_THREADS, 0, st>>>(in, avail, g, w.offs, vol, w.err);
