@@ -9,25 +9,30 @@
  * volume (ZCCL_float.h:63-73), which every element can form on its own, and
  * its inverse is the 3-D prefix sum.  So here every step is data parallel:
  *
- * compress   K0  q = (int)floor((double)x * (0.5 / eb) + 0.5) for every
- *                element (ZCCL_float.h:57-61) with the reference's double
- *                rounding (float pairs where that is provably the same,
- *                FP64 for the rest), into an int32 volume;
- *            K1  one CTA per block: the differences of its elements, their
- *                largest magnitude, the rate (its bit length) into the
- *                rate table at the stream's start, the payload size;
+ * quantization  q = (int)floor((double)x * (0.5 / eb) + 0.5) (ZCCL_float.h:57-61)
+ *                with the reference's double rounding: float pairs where that
+ *                is provably the same, FP64 for the rest;
+ * compress   K1  the rate of every block (the bit length of its largest
+ *                difference magnitude) into the rate table at the stream's
+ *                start, and its payload size;
  *            K2  an exclusive scan of the payload sizes (three kernels);
- *            K3  one CTA per block: the differences again, packed at the
- *                block's offset: sign bits, then B = rate/8 high bytes per
- *                element, then the r = rate%8 low bits (the fastmode1
- *                packers' layout, ZCCL/src/ZCCL_TypeManager.c:12-91,824-848),
- *                every byte by one thread;
+ *            K3  every block packed at its offset: sign bits, then B =
+ *                rate/8 high bytes per element, then the r = rate%8 low bits
+ *                (the fastmode1 packers' layout,
+ *                ZCCL/src/ZCCL_TypeManager.c:12-91,824-848);
  * decompress K1  payload sizes from the rate table, K2 the same scan,
- *            K3  one CTA per block: its differences into the output
- *                buffer, viewed as int32;
+ *            K3  every block's differences into the output buffer, viewed
+ *                as int32;
  *            K4-K6 inclusive prefix sums along z (a warp per row), y and x
- *                (a thread per column), the last one writing
- *                (float)((double)q * (2 eb)) in place (ZCCLd_float.c:2855-2857).
+ *                (a thread per column, rows loaded in batches), the last one
+ *                writing (float)((double)q * (2 eb)) in place
+ *                (ZCCLd_float.c:2855-2857).
+ * Block sides 2, 4 and 8 (row-mapped kernels): a warp takes a run of 32 / bs
+ * blocks along z and walks their rows, coalesced, with the neighbours in
+ * registers; compress K1 and K3 quantize as they load (x is read twice, no
+ * quantized volume is kept), decompress K3 stages the run's bytes in shared
+ * memory and writes whole rows.  Other block sides: a quantized volume, then
+ * a warp (up to 512 elements) or a CTA per block.
  * Integer sums wrap modulo 2^32 like the reference's int.
  */
 #include "zkern.cuh"

@@ -138,31 +138,37 @@ __global__ void k_walk_setup(const WalkArgs a)
  *
  * A window of WW = 32 x 128 bytes sits in shared memory.  Lane j walks the
  * headers speculatively from byte 128 j until it leaves its sub-window and
- * records the positions it visited (a 128-bit map).  A walk from a true
- * block start is the true path, and two walks that meet at a position go
- * on together, so the true path from a known entry is stitched across the
- * sub-windows: where it enters sub-window j at a position lane j visited,
- * it is lane j's walk from there on; otherwise it is walked until it meets
- * lane j's walk or leaves the sub-window (a few blocks).  Bytes that cannot
- * be headers (above 32) count as 1-byte blocks, so walks stay bounded. */
+ * keeps the positions it visited (a 128-bit map) and where it left.  A walk
+ * from a true block start is the true path, and two walks that meet at a
+ * position go on together, so the true path is stitched across the
+ * sub-windows by the warp: lane j takes the true path from where it enters
+ * sub-window j -- lane j's walk from there if that position is on it, else
+ * walked until it meets lane j's walk or leaves the sub-window (a few
+ * blocks) -- and hands its exit to lane j + 1.  Every lane first assumes it
+ * is entered where lane j - 1's speculative walk left (where the walks have
+ * nearly always merged); rounds repeat until no entry changes, so the
+ * result is exact.  Bytes that cannot be headers (above 32) count as 1-byte
+ * blocks, so walks stay bounded. */
 constexpr uint32_t SUB = WALK_WW / 32; /* bytes per sub-window */
 static_assert(SUB == 128, "a sub-window map is four 32-bit words");
 
 struct WinPath {
-    uint32_t spec[32][4]; /* lane j's visited positions in sub-window j */
-    uint32_t sx[32];      /* where lane j's walk left its sub-window */
-    uint32_t tm[32][4];   /* the true path's positions, per sub-window */
-    uint32_t pref[33];    /* true-path positions before sub-window j; [32] = all */
-    uint32_t exit;        /* where the true path leaves the window */
+    uint32_t tm[32][4]; /* the true path's positions, per sub-window */
+    uint32_t pref[33];  /* true-path positions before sub-window j; [32] = all */
+    uint32_t exit;      /* where the true path leaves the window */
 };
 
-__device__ __forceinline__ bool map_bit(const uint32_t *m, uint32_t i)
+/* Bits i .. 127 of a 128-bit map. */
+__device__ __forceinline__ void map_from(const uint32_t (&m)[4], uint32_t i, uint32_t (&t)[4])
 {
-    return (m[i >> 5] >> (i & 31u)) & 1u;
+#pragma unroll
+    for (uint32_t w = 0; w < 4; w++)
+        t[w] |= w < (i >> 5) ? 0u : w > (i >> 5) ? m[w] : m[w] & ~((1u << (i & 31u)) - 1u);
 }
 
-/* All lanes: the speculative sub-window walks. */
-__device__ __forceinline__ void spec_walks(const uint8_t *bytes, uint32_t L, uint32_t fmt, WinPath *wp)
+/* All lanes: lane j's speculative walk of sub-window j (visited map sp, exit sx). */
+__device__ __forceinline__ void spec_walks(const uint8_t *bytes, uint32_t L, uint32_t fmt, uint32_t (&sp)[4],
+                                           uint32_t &sx)
 {
     const uint32_t lane = threadIdx.x & 31u, lo = lane * SUB;
     uint32_t m0 = 0, m1 = 0, m2 = 0, m3 = 0, pos = lo;
@@ -174,110 +180,151 @@ __device__ __forceinline__ void spec_walks(const uint8_t *bytes, uint32_t L, uin
         m3 |= w == 3 ? bit : 0u;
         pos += full_size(bytes[pos], L, fmt);
     }
-    wp->spec[lane][0] = m0;
-    wp->spec[lane][1] = m1;
-    wp->spec[lane][2] = m2;
-    wp->spec[lane][3] = m3;
-    wp->sx[lane] = pos;
+    sp[0] = m0;
+    sp[1] = m1;
+    sp[2] = m2;
+    sp[3] = m3;
+    sx = pos;
 }
 
-/* One lane: the true path from window position `entry`, per sub-window,
- * with the prefix counts; returns where it leaves the window. */
-__device__ __forceinline__ uint32_t stitch(const uint8_t *bytes, uint32_t L, uint32_t fmt, uint32_t entry, WinPath *wp)
+/* All lanes: the true path from window position `entry` into wp (maps,
+ * prefix counts, exit), from the speculative walks sp / sx. */
+__device__ __forceinline__ void stitch(const uint8_t *bytes, uint32_t L, uint32_t fmt, uint32_t entry,
+                                       const uint32_t (&sp)[4], uint32_t sx, WinPath *wp)
 {
-    uint32_t p = entry, cnt = 0;
-    for (uint32_t j = 0; j < 32; j++) {
-        const uint32_t lo = j * SUB, hi = lo + SUB;
-        uint32_t t[4] = {0, 0, 0, 0};
-        wp->pref[j] = cnt;
-        if (p < hi) {
-            uint32_t q = p;
-            for (;;) {
-                const uint32_t i = q - lo;
-                if (map_bit(wp->spec[j], i)) { /* joins lane j's walk: the rest of it */
-#pragma unroll
-                    for (uint32_t w = 0; w < 4; w++) {
-                        const uint32_t sw = wp->spec[j][w];
-                        t[w] |= w < (i >> 5) ? 0u : w > (i >> 5) ? sw : sw & ~((1u << (i & 31u)) - 1u);
-                    }
-                    q = wp->sx[j];
-                    break;
-                }
-#pragma unroll
-                for (uint32_t w = 0; w < 4; w++) t[w] |= w == (i >> 5) ? 1u << (i & 31u) : 0u;
-                q += full_size(bytes[q], L, fmt);
-                if (q >= hi) break;
+    const uint32_t lane = threadIdx.x & 31u, lo = lane * SUB, hi = lo + SUB;
+    uint32_t in = __shfl_up_sync(0xffffffffu, sx, 1);
+    if (lane == 0) in = entry;
+    uint32_t t[4], ex = in;
+    for (uint32_t round = 0; round <= 32; round++) { /* lane r is final after round r */
+        t[0] = t[1] = t[2] = t[3] = 0;
+        uint32_t q = in; /* >= lo: where sub-window j - 1 was left */
+        while (q < hi) {
+            const uint32_t i = q - lo;
+            const uint32_t wi = i >> 5, mw = wi == 0 ? sp[0] : wi == 1 ? sp[1] : wi == 2 ? sp[2] : sp[3];
+            if ((mw >> (i & 31u)) & 1u) { /* joins lane j's walk: the rest of it */
+                map_from(sp, i, t);
+                q = sx;
+                break;
             }
-            p = q;
-        }
 #pragma unroll
-        for (uint32_t w = 0; w < 4; w++) {
-            wp->tm[j][w] = t[w];
-            cnt += __popc(t[w]);
+            for (uint32_t w = 0; w < 4; w++) t[w] |= w == (i >> 5) ? 1u << (i & 31u) : 0u;
+            q += full_size(bytes[q], L, fmt);
         }
+        ex = q;
+        uint32_t nin = __shfl_up_sync(0xffffffffu, ex, 1);
+        if (lane == 0) nin = entry;
+        if (!__any_sync(0xffffffffu, nin != in)) break;
+        in = nin;
     }
-    wp->pref[32] = cnt;
-    wp->exit = p;
-    return p;
+    const uint32_t cnt = __popc(t[0]) + __popc(t[1]) + __popc(t[2]) + __popc(t[3]);
+    const uint32_t incl = warp_incl_scan(cnt);
+#pragma unroll
+    for (uint32_t w = 0; w < 4; w++) wp->tm[lane][w] = t[w];
+    wp->pref[lane] = incl - cnt;
+    if (lane == 31) {
+        wp->pref[32] = incl;
+        wp->exit = ex;
+    }
 }
 
-/* True-path positions before window position q (q < WW). */
-__device__ __forceinline__ uint32_t path_rank(const WinPath *wp, uint32_t q)
-{
-    const uint32_t j = q / SUB, i = q % SUB;
-    uint32_t r = wp->pref[j];
-#pragma unroll
-    for (uint32_t w = 0; w < 4; w++) {
-        const uint32_t m = wp->tm[j][w];
-        r += w < (i >> 5) ? __popc(m) : w == (i >> 5) ? __popc(m & ((1u << (i & 31u)) - 1u)) : 0u;
-    }
-    return r;
-}
+/* Bytes of a warp's window area: the window with its alignment slack,
+ * then the WinPath. */
+__host__ __device__ inline uint32_t win_area(uint32_t M) { return (WALK_WW + M + 32u + 15u) & ~15u; }
 
-__device__ __forceinline__ void load_window(const WalkArgs &a, uint64_t start, uint8_t *bytes)
+/* The window [start, start + WW + M) of the stream into the 16-byte-aligned
+ * area buf (bytes past avail read as 0), by aligned 16-byte loads that the
+ * warp issues together; returns where the window's first byte landed. */
+__device__ __forceinline__ const uint8_t *load_window(const WalkArgs &a, uint64_t start, uint8_t *buf)
 {
     const uint32_t lane = threadIdx.x & 31u;
-    for (uint32_t i = lane; i < WALK_WW + a.M; i += 32) {
-        const uint64_t p = start + i;
-        bytes[i] = p < a.avail ? a.in[p] : 0;
+    const uintptr_t base = reinterpret_cast<uintptr_t>(a.in), end = base + a.avail;
+    const uintptr_t lo = (base + start) & ~(uintptr_t)15;
+    const uint32_t ph = (uint32_t)(base + start - lo), nl = (ph + WALK_WW + a.M + 15u) / 16u;
+    uint4 *d = reinterpret_cast<uint4 *>(buf);
+#pragma unroll 8
+    for (uint32_t i = lane; i < nl; i += 32) {
+        const uintptr_t p = lo + 16u * i;
+        if (p >= base && p + 16u <= end) {
+            d[i] = *reinterpret_cast<const uint4 *>(p);
+        } else { /* a line across either end of the readable bytes */
+            uint32_t v[4] = {0, 0, 0, 0};
+            for (uint32_t k = 0; k < 16; k++) {
+                const uintptr_t q = p + k;
+                if (q >= base && q < end) v[k >> 2] |= (uint32_t)*reinterpret_cast<const uint8_t *>(q) << (8 * (k & 3));
+            }
+            d[i] = make_uint4(v[0], v[1], v[2], v[3]);
+        }
     }
+    return buf + ph;
 }
 
-/* ---- W1 -------------------------------------------------------------- */
+/* ---- W1 --------------------------------------------------------------
+ * Per window, lane j makes one backward pass over sub-window j: for every
+ * position p, where a walk from p leaves the sub-window and how many blocks
+ * it passes on the way, from the result at the position p steps to.  A walk
+ * from any entry then takes one hop per sub-window.  The bytes are copied
+ * into rows of SUB + 4 and the results kept at i * 33 + j (position i of
+ * sub-window j), so that lanes in step hit distinct shared-memory banks.
+ * A result is (exit - end of the sub-window) << 8 | blocks passed (<= SUB),
+ * 16 bits while blocks are shorter than 256 bytes (block sizes up to 48),
+ * else 32.  Per warp: the results (the plain window copy lands there
+ * first), then the skewed rows. */
+constexpr uint32_t W1_ROW = SUB + 4;  /* bytes per skewed row */
+constexpr uint32_t W1_RES = SUB * 33; /* results */
+
+__host__ __device__ inline uint32_t w1_warp_bytes(uint32_t M)
+{
+    const uint32_t res = W1_RES * (M < 256 ? 2u : 4u), win = win_area(M);
+    return (res > win ? res : win) + 32u * W1_ROW;
+}
+
+template <class R>
 __global__ void __launch_bounds__(32 * WARPS_W1) k_walk_tables(const WalkArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ uint32_t szt[33]; /* full_size of each header byte */
     const ZGeom &g = a.g;
     const WalkScratch &w = a.ws;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t M = a.M;
-    const uint32_t wg = blockIdx.x * WARPS_W1 + warp;
-    if (wg >= w.win_base[g.T]) return;
-    const uint32_t s = find_seg(w.win_base, g.T, wg);
-    const uint64_t start = w.seg_P[s] + (uint64_t)(wg - w.win_base[s]) * WALK_WW;
+    if (threadIdx.x < 33) szt[threadIdx.x] = full_size(threadIdx.x, g.L, g.fmt);
+    __syncthreads();
+    /* persistent: the warps stride over the windows the header gives */
+    for (uint32_t wg = blockIdx.x * WARPS_W1 + warp; wg < w.win_base[g.T]; wg += gridDim.x * WARPS_W1) {
+        const uint32_t s = find_seg(w.win_base, g.T, wg);
+        const uint64_t start = w.seg_P[s] + (uint64_t)(wg - w.win_base[s]) * WALK_WW;
 
-    /* per-warp shared area: bytes[WW + M + 16] | WinPath */
-    uint8_t *bytes = smem + warp * a.w1_warp_bytes;
-    WinPath *wp = reinterpret_cast<WinPath *>(bytes + ((WALK_WW + M + 16 + 15) & ~15u));
-    load_window(a, start, bytes);
-    __syncwarp();
-    spec_walks(bytes, g.L, g.fmt, wp);
-    __syncwarp();
-    if (lane == 0) stitch(bytes, g.L, g.fmt, 0, wp);
-    __syncwarp();
-    /* entry e: walk until the path from entry 0 is met (then its exit and
-     * the blocks left on it) or the window ends */
-    const uint32_t x0 = wp->exit - WALK_WW, c0 = wp->pref[32];
-    uint32_t *tab = a.ws.wtab + (uint64_t)wg * M;
-    for (uint32_t e = lane; e < M; e += 32) {
-        uint32_t q = e, k = 0;
-        while (q < WALK_WW && !map_bit(wp->tm[q / SUB], q % SUB)) {
-            q += full_size(bytes[q], g.L, g.fmt);
-            k++;
+        uint8_t *area = smem + warp * a.w1_warp_bytes;
+        R *res = reinterpret_cast<R *>(area);
+        uint8_t *rows = area + (a.w1_warp_bytes - 32u * W1_ROW);
+        const uint8_t *bytes = load_window(a, start, area);
+        __syncwarp();
+#pragma unroll 4
+        for (uint32_t k = 0; k < 32; k++) { /* row k: lane copies bytes 4 lane .. 4 lane + 3 */
+            const uint8_t *src = bytes + SUB * k + 4u * lane;
+            const uint32_t v = (uint32_t)src[0] | (uint32_t)src[1] << 8 | (uint32_t)src[2] << 16 | (uint32_t)src[3] << 24;
+            *reinterpret_cast<uint32_t *>(rows + W1_ROW * k + 4u * lane) = v;
         }
-        const uint32_t ex = q < WALK_WW ? x0 : q - WALK_WW;
-        const uint32_t cnt = q < WALK_WW ? k + c0 - path_rank(wp, q) : k;
-        tab[e] = (ex << 16) | cnt;
+        __syncwarp();
+        /* result = (exit - end of the sub-window) << 8 | blocks passed (<= SUB) */
+        const uint8_t *row = rows + W1_ROW * lane;
+        for (int i = (int)SUB - 1; i >= 0; i--) {
+            const uint32_t b = row[i], nxt = (uint32_t)i + (b <= 32 ? szt[b] : 1u);
+            res[i * 33 + lane] = (R)(nxt >= SUB ? (nxt - SUB) << 8 | 1u : (uint32_t)res[nxt * 33 + lane] + 1u);
+        }
+        __syncwarp();
+        uint32_t *tab = a.ws.wtab + (uint64_t)wg * M;
+        for (uint32_t e = lane; e < M; e += 32) {
+            uint32_t pos = e, cnt = 0;
+            while (pos < WALK_WW) {
+                const uint32_t j = pos / SUB, r = res[(pos % SUB) * 33 + j];
+                cnt += r & 0xFFu;
+                pos = (j + 1) * SUB + (r >> 8);
+            }
+            tab[e] = (pos - WALK_WW) << 16 | cnt;
+        }
+        __syncwarp(); /* the area is reused for the next window */
     }
 }
 
@@ -344,87 +391,100 @@ __global__ void k_walk_segments(const WalkArgs a)
 }
 
 /* ---- W3: the true walk of every window ------------------------------- */
+/* Shared bytes before W3's window areas: entries, block bases, tables;
+ * then per warp the window and its WinPath. */
+__host__ __device__ inline uint32_t w3_warp_bytes(uint32_t M) { return (win_area(M) + (uint32_t)sizeof(WinPath) + 15u) & ~15u; }
+__host__ __device__ inline uint32_t w3_head(uint32_t M) { return (12u * WALK_G + 4u * WALK_G * M + 15u) & ~15u; }
+
 __global__ void __launch_bounds__(32 * WARPS_W3) k_walk_final(const WalkArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const ZGeom &g = a.g;
     const WalkScratch &w = a.ws;
-    const uint32_t gg = blockIdx.x;
-    if (gg >= w.grp_base[g.T]) return;
-    const uint32_t s = find_seg(w.grp_base, g.T, gg);
-    if (!w.seg_ok[s]) return;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const uint32_t nwin = w.win_base[s + 1] - w.win_base[s];
-    const uint32_t w0 = (gg - w.grp_base[s]) * WALK_G;
-    const uint32_t w1 = min(w0 + WALK_G, nwin);
     uint32_t *entry = reinterpret_cast<uint32_t *>(smem);
     uint64_t *bbase = reinterpret_cast<uint64_t *>(smem + 4 * WALK_G);
-    uint8_t *wbuf = smem + 12 * WALK_G;
-    const uint32_t wstride = a.w1_warp_bytes;
+    uint32_t *tabs = reinterpret_cast<uint32_t *>(smem + 12 * WALK_G); /* the group's window tables */
+    uint8_t *wbuf = smem + w3_head(a.M);
+    const uint32_t wstride = w3_warp_bytes(a.M);
+    /* persistent: the CTAs stride over the groups the header gives */
+    for (uint32_t gg = blockIdx.x; gg < w.grp_base[g.T]; gg += gridDim.x) {
+        const uint32_t s = find_seg(w.grp_base, g.T, gg);
+        if (!w.seg_ok[s]) continue; /* uniform over the CTA */
+        const uint32_t nwin = w.win_base[s + 1] - w.win_base[s];
+        const uint32_t w0 = (gg - w.grp_base[s]) * WALK_G;
+        const uint32_t w1 = min(w0 + WALK_G, nwin);
 
-    const uint64_t nb = g.nb_reg;
-    const uint64_t nfull = (g.tbs - 1) / g.L;
-    const uint32_t ntail = (uint32_t)((g.tbs - 1) % g.L);
-    const uint64_t gblk0 = (uint64_t)s * g.nb_reg, tile0 = (uint64_t)s * g.nt_reg;
+        const uint64_t nb = g.nb_reg;
+        const uint64_t nfull = (g.tbs - 1) / g.L;
+        const uint32_t ntail = (uint32_t)((g.tbs - 1) % g.L);
+        const uint64_t gblk0 = (uint64_t)s * g.nb_reg, tile0 = (uint64_t)s * g.nt_reg;
 
-    if (threadIdx.x == 0) {
-        uint32_t x = w.gentry[gg];
-        uint64_t b = w.gbase[gg];
-        for (uint32_t k = w0; k < w1; k++) {
-            entry[k - w0] = x;
-            bbase[k - w0] = b;
-            if (b >= nb) continue;
-            uint32_t t = w.wtab[(uint64_t)(w.win_base[s] + k) * a.M + x];
-            b += t & 0xFFFFu;
-            x = t >> 16;
-        }
-    }
-    __syncthreads();
-    for (uint32_t k = w0 + warp; k < w1; k += nw) {
-        const uint64_t b0 = bbase[k - w0];
-        if (b0 >= nb) continue;
-        const uint64_t start = w.seg_P[s] + (uint64_t)k * WALK_WW;
-        uint8_t *buf = wbuf + warp * wstride;
-        WinPath *wp = reinterpret_cast<WinPath *>(buf + ((WALK_WW + a.M + 16 + 15) & ~15u));
-        load_window(a, start, buf);
-        __syncwarp();
-        spec_walks(buf, g.L, g.fmt, wp);
-        __syncwarp();
-        if (lane == 0) stitch(buf, g.L, g.fmt, entry[k - w0], wp);
-        __syncwarp();
-        /* lane j records the true-path blocks of its sub-window */
-        uint64_t blk = b0 + wp->pref[lane];
-#pragma unroll
-        for (uint32_t wd = 0; wd < 4; wd++) {
-            uint32_t m = wp->tm[lane][wd];
-            while (m && blk < nb) {
-                const uint32_t pos = lane * SUB + wd * 32 + (uint32_t)(__ffs(m) - 1);
-                m &= m - 1;
-                const uint64_t gpos = start + pos;
-                if (gpos >= a.avail) {
-                    atomicOr(a.err, ZERR_BOUNDS);
-                    m = 0;
-                    break;
-                }
-                const uint32_t b = buf[pos];
-                if (b > 32) {
-                    atomicOr(a.err, ZERR_CORRUPT);
-                    m = 0;
-                    break;
-                }
-                if (blk % g.TB == 0 && blk) a.idx.tile_off[tile0 + blk / g.TB] = gpos;
-                a.idx.widths[gblk0 + blk] = (uint8_t)b;
-                const uint32_t n = blk < nfull ? g.L : ntail;
-                blk++;
-                if (blk == nb) {
-                    const uint64_t end = gpos + zg_block_bytes_f(g.fmt, b, n);
-                    if (end > a.avail) atomicOr(a.err, ZERR_BOUNDS);
-                    w.seg_end[s] = end;
-                    if (s + 1 < g.T && end != w.seg_R[s]) atomicOr(a.err, ZERR_CORRUPT);
-                }
+        /* the chain through the group's windows runs on tables staged in shared
+         * memory by the whole CTA (one coalesced copy) */
+        const uint32_t *gt = w.wtab + (uint64_t)(w.win_base[s] + w0) * a.M;
+        for (uint32_t i = threadIdx.x; i < (w1 - w0) * a.M; i += blockDim.x) tabs[i] = gt[i];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t x = w.gentry[gg];
+            uint64_t b = w.gbase[gg];
+            for (uint32_t k = w0; k < w1; k++) {
+                entry[k - w0] = x;
+                bbase[k - w0] = b;
+                if (b >= nb) continue;
+                uint32_t t = tabs[(k - w0) * a.M + x];
+                b += t & 0xFFFFu;
+                x = t >> 16;
             }
         }
-        __syncwarp();
+        __syncthreads();
+        for (uint32_t k = w0 + warp; k < w1; k += nw) {
+            const uint64_t b0 = bbase[k - w0];
+            if (b0 >= nb) continue;
+            const uint64_t start = w.seg_P[s] + (uint64_t)k * WALK_WW;
+            uint8_t *area = wbuf + warp * wstride;
+            WinPath *wp = reinterpret_cast<WinPath *>(area + win_area(a.M));
+            const uint8_t *buf = load_window(a, start, area);
+            __syncwarp();
+            uint32_t sp[4], sx;
+            spec_walks(buf, g.L, g.fmt, sp, sx);
+            stitch(buf, g.L, g.fmt, entry[k - w0], sp, sx, wp);
+            __syncwarp();
+            /* lane j records the true-path blocks of its sub-window */
+            uint64_t blk = b0 + wp->pref[lane];
+#pragma unroll
+            for (uint32_t wd = 0; wd < 4; wd++) {
+                uint32_t m = wp->tm[lane][wd];
+                while (m && blk < nb) {
+                    const uint32_t pos = lane * SUB + wd * 32 + (uint32_t)(__ffs(m) - 1);
+                    m &= m - 1;
+                    const uint64_t gpos = start + pos;
+                    if (gpos >= a.avail) {
+                        atomicOr(a.err, ZERR_BOUNDS);
+                        m = 0;
+                        break;
+                    }
+                    const uint32_t b = buf[pos];
+                    if (b > 32) {
+                        atomicOr(a.err, ZERR_CORRUPT);
+                        m = 0;
+                        break;
+                    }
+                    if (blk % g.TB == 0 && blk) a.idx.tile_off[tile0 + blk / g.TB] = gpos;
+                    a.idx.widths[gblk0 + blk] = (uint8_t)b;
+                    const uint32_t n = blk < nfull ? g.L : ntail;
+                    blk++;
+                    if (blk == nb) {
+                        const uint64_t end = gpos + zg_block_bytes_f(g.fmt, b, n);
+                        if (end > a.avail) atomicOr(a.err, ZERR_BOUNDS);
+                        w.seg_end[s] = end;
+                        if (s + 1 < g.T && end != w.seg_R[s]) atomicOr(a.err, ZERR_CORRUPT);
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        __syncthreads(); /* the group's shared state is reused */
     }
 }
 
@@ -474,9 +534,18 @@ __global__ void k_walk_finish(const WalkArgs a)
 
 } // namespace
 
-size_t walk_w1_warp_bytes(uint32_t M)
+size_t walk_w1_warp_bytes(uint32_t M) { return w1_warp_bytes(M); }
+
+/* Persistent grid: the CTAs that fit at once, at most `most`. */
+static unsigned walk_grid(const void *fn, unsigned threads, size_t smem, unsigned most)
 {
-    return ((WALK_WW + M + 16 + 15) & ~15u) + sizeof(WinPath);
+    int dev = 0, nsm = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, (int)threads, smem) != cudaSuccess || per < 1)
+        per = 1;
+    const unsigned g = (unsigned)(nsm > 0 ? nsm : 1) * (unsigned)per;
+    return most < g ? (most ? most : 1) : g;
 }
 
 cudaError_t launch_walk(const WalkArgs &a0, cudaStream_t st)
@@ -488,10 +557,13 @@ cudaError_t launch_walk(const WalkArgs &a0, cudaStream_t st)
     k_walk_setup<<<1, 256, 0, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const uint32_t smem1 = WARPS_W1 * a.w1_warp_bytes;
-    if ((e = cudaFuncSetAttribute(k_walk_tables, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  smem1)) != cudaSuccess)
-        return e;
-    k_walk_tables<<<(a.max_windows + WARPS_W1 - 1) / WARPS_W1, 32 * WARPS_W1, smem1, st>>>(a);
+    const void *f1 = a.M < 256 ? (const void *)k_walk_tables<uint16_t> : (const void *)k_walk_tables<uint32_t>;
+    if ((e = cudaFuncSetAttribute(f1, cudaFuncAttributeMaxDynamicSharedMemorySize, smem1)) != cudaSuccess) return e;
+    const unsigned grid1 = walk_grid(f1, 32 * WARPS_W1, smem1, (a.max_windows + WARPS_W1 - 1) / WARPS_W1);
+    if (a.M < 256)
+        k_walk_tables<uint16_t><<<grid1, 32 * WARPS_W1, smem1, st>>>(a);
+    else
+        k_walk_tables<uint32_t><<<grid1, 32 * WARPS_W1, smem1, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     k_walk_groups<<<a.max_groups, 128, 0, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -504,12 +576,19 @@ cudaError_t launch_walk(const WalkArgs &a0, cudaStream_t st)
         return e;
     k_walk_segments<<<a.g.T, 256, smem2, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    const uint32_t wstride = (uint32_t)walk_w1_warp_bytes(a.M);
-    const uint32_t smem3 = 12 * WALK_G + WARPS_W3 * wstride;
+    const uint32_t wstride = w3_warp_bytes(a.M);
+    /* as many warps as fit beside the staged tables (fewer for the largest blocks) */
+    int dev = 0, smax = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess)
+        return e;
+    uint32_t warps3 = WARPS_W3;
+    while (warps3 > 1 && w3_head(a.M) + warps3 * wstride > (uint32_t)smax) warps3--;
+    const uint32_t smem3 = w3_head(a.M) + warps3 * wstride;
     if ((e = cudaFuncSetAttribute(k_walk_final, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   smem3)) != cudaSuccess)
         return e;
-    k_walk_final<<<a.max_groups, 32 * WARPS_W3, smem3, st>>>(a);
+    k_walk_final<<<walk_grid((const void *)k_walk_final, 32 * warps3, smem3, a.max_groups), 32 * warps3, smem3, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     k_walk_finish<<<1, 32, 0, st>>>(a);
     return cudaGetLastError();
