@@ -12,16 +12,17 @@
  *       and window count; heads' tile offsets.
  *   W1  for every window and every possible entry offset e in [0, M) (M = the
  *       largest block): the exit offset into the next window and the blocks
- *       passed.  The path from entry 0 is stitched from 32 speculative
- *       sub-window walks run in parallel (see below), and every other entry
- *       is walked only until it meets that path, so a window costs a few
- *       dozen dependent steps instead of a full walk.
+ *       passed.  Each lane makes one backward pass over its 128-byte
+ *       sub-window, giving for every position where a walk from it leaves the
+ *       sub-window and how many blocks it passes; a walk from any entry is
+ *       then one hop per sub-window.
  *   W2  compose the tables: per group of G windows (parallel), then per
  *       segment across groups, giving each group its true entry offset and
  *       first block number.
- *   W3  per window, the path from its true entry, stitched the same way,
- *       gives every block's width and every tile's offset, written by all
- *       lanes at once; each chunk must end where the next starts.
+ *   W3  per window, the path from its true entry, stitched across 32
+ *       speculative sub-window walks run in parallel (see below), gives
+ *       every block's width and every tile's offset, written by all lanes at
+ *       once; each chunk must end where the next starts.
  *   W4  the extra segment of the last chunk (N % T elements) and the total
  *       size.
  * Widths above 32, chunk ends that disagree with the header, and blocks past
@@ -134,7 +135,7 @@ __global__ void k_walk_setup(const WalkArgs a)
     }
 }
 
-/* ---- shared by W1 and W3: the path of the headers through one window ---
+/* ---- W3: the path of the headers through one window -------------------
  *
  * A window of WW = 32 x 128 bytes sits in shared memory.  Lane j walks the
  * headers speculatively from byte 128 j until it leaves its sub-window and
