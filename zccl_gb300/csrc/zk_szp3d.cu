@@ -29,9 +29,10 @@
  *                (ZCCLd_float.c:2855-2857).
  * Block sides 2, 4 and 8 (row-mapped kernels): a warp takes a run of 32 / bs
  * blocks along z and walks their rows, coalesced, with the neighbours in
- * registers; compress K1 and K3 quantize as they load (x is read twice, no
- * quantized volume is kept), decompress K3 stages the run's bytes in shared
- * memory and writes whole rows.  Other block sides: a quantized volume, then
+ * registers; compress is one pass (K1-K3 together, quantizing as it loads,
+ * the run's place in the stream by decoupled look-back; no quantized
+ * volume), decompress K3 stages the run's bytes in shared memory and writes
+ * whole rows.  Other block sides: a quantized volume, then
  * a warp (up to 512 elements) or a CTA per block.
  * Integer sums wrap modulo 2^32 like the reference's int.
  */
@@ -570,40 +571,17 @@ __device__ __forceinline__ void sz3_walk(const float *__restrict__ x, const Sz3D
     }
 }
 
-/* compress K1 (quantization included): a warp per unit */
+/* compress, one pass (quantization included): warps take units in ticket
+ * order; a unit's differences go to shared memory in element order while
+ * their largest magnitudes give the blocks' rates and payload sizes; the
+ * unit's place in the stream comes from a decoupled look-back over the
+ * units before it (the unit's bytes are its blocks', consecutive), then
+ * each block is packed by the whole warp.  The last unit records the
+ * stream's size. */
 template <uint32_t BS>
-__global__ void __launch_bounds__(SZ_THREADS) k_sz3_rates_rows(const float *__restrict__ x, Sz3Dims g, Sz3Split inv,
-                                                               uint8_t *out, uint32_t *sizes, uint32_t *err)
-{
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint64_t units = sz3_units<BS>(g);
-    uint32_t bad = 0;
-    for (uint64_t u = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < units;
-         u += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
-        const Sz3Unit k = sz3_unit<BS>(g, u);
-        uint32_t m = 0;
-        sz3_walk<BS>(x, g, inv, k, bad, [&](uint32_t, uint32_t, uint32_t e) { m = max(m, mag(e)); });
-        if (k.z0 + lane >= g.d3) m = 0;
-#pragma unroll
-        for (uint32_t o = 1; o < BS; o <<= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-        const uint32_t sz = sz3_unit_sz<BS>(g, k, lane / BS);
-        if (lane % BS == 0 && sz) {
-            const uint64_t b = (k.bi * g.nb2 + k.bj) * g.nb3 + k.bk0 + lane / BS;
-            const uint32_t rate = 32u - __clz(m);
-            out[b] = (uint8_t)rate;
-            sizes[b] = sz3_payload(rate, k.sx * k.sy * sz);
-        }
-    }
-    if (bad) atomicOr(err, ZERR_RANGE);
-}
-
-/* compress K3 (quantization included): a warp per unit; the unit's
- * differences go to shared memory in element order, then each block is
- * packed by the whole warp */
-template <uint32_t BS>
-__global__ void __launch_bounds__(SZ_THREADS) k_sz3_pack_rows(const float *__restrict__ x, Sz3Dims g, Sz3Split inv,
-                                                              uint8_t *out, uint64_t cap, const uint64_t *offs,
-                                                              uint32_t *err)
+__global__ void __launch_bounds__(SZ_THREADS) k_sz3_compress_rows(const float *__restrict__ x, Sz3Dims g, Sz3Split inv,
+                                                                  uint8_t *out, uint64_t cap, uint64_t *status,
+                                                                  uint32_t *ticket, uint64_t *total, uint32_t *err)
 {
     constexpr uint32_t U = 32 / BS, NB = BS * BS * BS;
     extern __shared__ uint32_t e_all[]; /* U blocks per warp */
@@ -611,23 +589,35 @@ __global__ void __launch_bounds__(SZ_THREADS) k_sz3_pack_rows(const float *__res
     uint32_t *e = e_all + (threadIdx.x >> 5) * (U * NB);
     const uint64_t units = sz3_units<BS>(g);
     uint32_t bad = 0, full = 0;
-    for (uint64_t u = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < units;
-         u += ((uint64_t)gridDim.x * blockDim.x) >> 5) {
+    for (;;) {
+        uint32_t u = 0;
+        if (lane == 0) u = atomicAdd(ticket, 1u);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if (u >= units) break; /* uniform */
         const Sz3Unit k = sz3_unit<BS>(g, u);
         const uint32_t sz = sz3_unit_sz<BS>(g, k, lane / BS);
         const bool zin = k.z0 + lane < g.d3;
         uint32_t *eb = e + (lane / BS) * NB;
+        uint32_t m = 0;
         __syncwarp(); /* the previous unit is packed */
         sz3_walk<BS>(x, g, inv, k, bad, [&](uint32_t di, uint32_t dj, uint32_t v) {
-            if (zin) eb[(di * k.sy + dj) * sz + dz] = v;
+            if (zin) {
+                eb[(di * k.sy + dj) * sz + dz] = v;
+                m = max(m, mag(v));
+            }
         });
-        uint32_t rate = 0;
-        uint64_t base = 0;
-        if (lane < U && k.bk0 + lane < g.nb3) { /* lane c: block c's rate and place */
-            const uint64_t b = (k.bi * g.nb2 + k.bj) * g.nb3 + k.bk0 + lane;
-            rate = out[b];
-            base = g.nblocks + offs[b];
-        }
+#pragma unroll
+        for (uint32_t o = 1; o < BS; o <<= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        /* lane c < U: block c's rate and size */
+        const uint32_t mc = __shfl_sync(0xffffffffu, m, (lane % U) * BS);
+        const uint32_t szc = lane < U ? sz3_unit_sz<BS>(g, k, lane) : 0u;
+        const uint32_t rate = szc ? 32u - __clz(mc) : 0u, size = szc ? sz3_payload(rate, k.sx * k.sy * szc) : 0u;
+        const uint32_t inc = warp_incl_scan(size), agg = __shfl_sync(0xffffffffu, inc, 31);
+        lb_publish(status, u, agg, u == 0, 0);
+        const uint64_t prefix = lb_resolve(status, u, agg, u == 0, 0, err);
+        const uint64_t base = g.nblocks + prefix + (inc - size);
+        if (szc) out[(k.bi * g.nb2 + k.bj) * g.nb3 + k.bk0 + lane] = (uint8_t)rate;
+        if (u == units - 1 && lane == 0) *total = g.nblocks + prefix + agg;
         __syncwarp();
         for (uint32_t c = 0; c < U; c++) {
             const uint32_t rc = __shfl_sync(0xffffffffu, rate, c);
@@ -815,21 +805,32 @@ cudaError_t sz3_scan(const Sz3Dims &g, const Sz3Ws &w, cudaStream_t st)
 /* Block sides with the row-mapped kernels. */
 bool sz3_rows(uint32_t bs) { return bs == 2 || bs == 4 || bs == 8; }
 
+/* One pass; the units' look-back flags use the offsets array (8 bytes a
+ * block, at least 8 a unit) and the ticket the third of the four scratch
+ * words before it (the first two are error words the status check reads),
+ * both zeroed first. */
 template <uint32_t BS>
 cudaError_t sz3_compress_rows(uint8_t *out, uint64_t cap, const float *x, const Sz3Dims &g, const Sz3Ws &w,
                               const Sz3Split &inv, cudaStream_t st)
 {
     const uint64_t units = sz3_units<BS>(g);
-    const unsigned grid = grid_for(units, SZ_THREADS / 32);
-    k_sz3_rates_rows<BS><<<grid, SZ_THREADS, 0, st>>>(x, g, inv, out, w.sizes, w.err);
-    cudaError_t e = sz3_scan(g, w, st);
+    if (units >> 32) return cudaErrorInvalidValue; /* tickets are 32-bit */
+    uint64_t *status = w.offs;
+    cudaError_t e = cudaMemsetAsync(status, 0, 8 * units, st);
     if (e != cudaSuccess) return e;
     const size_t smem = 4ull * 32 * BS * BS * (SZ_THREADS / 32);
-    if (smem > 48 * 1024 &&
-        (e = cudaFuncSetAttribute(k_sz3_pack_rows<BS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-            cudaSuccess)
+    const void *fn = (const void *)k_sz3_compress_rows<BS>;
+    if (smem > 48 * 1024 && (e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+                                cudaSuccess)
         return e;
-    k_sz3_pack_rows<BS><<<grid, SZ_THREADS, smem, st>>>(x, g, inv, out, cap, w.offs, w.err);
+    int dev = 0, nsm = 0, per = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+        (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, SZ_THREADS, smem)) != cudaSuccess)
+        return e;
+    const uint64_t want = (units + SZ_THREADS / 32 - 1) / (SZ_THREADS / 32), most = (uint64_t)nsm * (per > 0 ? per : 1);
+    const unsigned grid = (unsigned)(want < most ? want : most);
+    k_sz3_compress_rows<BS><<<grid, SZ_THREADS, smem, st>>>(x, g, inv, out, cap, status, w.err + 2, w.total, w.err);
     return cudaGetLastError();
 }
 
