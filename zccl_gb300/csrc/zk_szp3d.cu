@@ -31,8 +31,8 @@
  * blocks along z and walks their rows, coalesced, with the neighbours in
  * registers; compress is one pass (K1-K3 together, quantizing as it loads,
  * the run's place in the stream by decoupled look-back; no quantized
- * volume), decompress K3 stages the run's bytes in shared memory and writes
- * whole rows.  Other block sides: a quantized volume, then
+ * volume); decompress K3 stages each run's bytes in shared memory and
+ * writes whole rows.  Other block sides: a quantized volume, then
  * a warp (up to 512 elements) or a CTA per block.
  * Integer sums wrap modulo 2^32 like the reference's int.
  */
@@ -576,7 +576,8 @@ __device__ __forceinline__ void sz3_walk(const float *__restrict__ x, const Sz3D
  * their largest magnitudes give the blocks' rates and payload sizes; the
  * unit's place in the stream comes from a decoupled look-back over the
  * units before it (the unit's bytes are its blocks', consecutive), then
- * each block is packed by the whole warp.  The last unit records the
+ * its blocks are packed (all at once, BS lanes each, for BS up to 4; else
+ * one after another by the whole warp).  The last unit records the
  * stream's size. */
 template <uint32_t BS>
 __global__ void __launch_bounds__(SZ_THREADS) k_sz3_compress_rows(const float *__restrict__ x, Sz3Dims g, Sz3Split inv,
@@ -619,20 +620,33 @@ __global__ void __launch_bounds__(SZ_THREADS) k_sz3_compress_rows(const float *_
         if (szc) out[(k.bi * g.nb2 + k.bj) * g.nb3 + k.bk0 + lane] = (uint8_t)rate;
         if (u == units - 1 && lane == 0) *total = g.nblocks + prefix + agg;
         __syncwarp();
-        for (uint32_t c = 0; c < U; c++) {
+        if constexpr (BS <= 4) { /* all blocks of the unit at once, BS lanes each */
+            const uint32_t c = lane / BS;
             const uint32_t rc = __shfl_sync(0xffffffffu, rate, c);
             const uint64_t bc = __shfl_sync(0xffffffffu, base, c);
-            const uint32_t n = k.sx * k.sy * sz3_unit_sz<BS>(g, k, c);
-            if (!rc || !n) continue; /* uniform */
-            if (bc + sz3_payload(rc, n) > cap) {
-                full = 1;
-                continue;
+            const uint32_t n = k.sx * k.sy * sz;
+            if (rc && n) {
+                if (bc + sz3_payload(rc, n) > cap)
+                    full = 1;
+                else
+                    sz3_pack_block<BS>(e + c * NB, n, rc, out + bc, dz);
             }
-            sz3_pack_block<32>(e + c * NB, n, rc, out + bc, lane);
+        } else { /* blocks of 512 elements: one after another, the whole warp on each */
+            for (uint32_t c = 0; c < U; c++) {
+                const uint32_t rc = __shfl_sync(0xffffffffu, rate, c);
+                const uint64_t bc = __shfl_sync(0xffffffffu, base, c);
+                const uint32_t n = k.sx * k.sy * sz3_unit_sz<BS>(g, k, c);
+                if (!rc || !n) continue; /* uniform */
+                if (bc + sz3_payload(rc, n) > cap) {
+                    full = 1;
+                    continue;
+                }
+                sz3_pack_block<32>(e + c * NB, n, rc, out + bc, lane);
+            }
         }
     }
     if (bad) atomicOr(err, ZERR_RANGE);
-    if (full && lane == 0) atomicOr(err, ZERR_CAPACITY);
+    if (full) atomicOr(err, ZERR_CAPACITY);
 }
 
 /* Bytes that hold a unit's blocks at most (every block at rate 32). */
