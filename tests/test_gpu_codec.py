@@ -181,6 +181,28 @@ def test_generic_block_sizes_against_port(port, torch):
             codec.check()
 
 
+def test_walk_long_blocks_against_port(port, torch):
+    """Byte-only streams (the header walk rebuilds the index) with blocks of
+    up to 64, 128 and 256 elements: blocks of 256 bytes or more take the
+    walk's 32-bit window tables and, at 256 elements, its final pass with
+    fewer warps.  Noisy data with a wide range gives widths up to the top;
+    decompress and the add of two such streams must equal the oracle's."""
+    rng = np.random.default_rng(19)
+    for L in (48, 64, 128, 256):
+        for T in (1, 3):
+            n = 40 * L * 64 + 5 * L + 7
+            x = (np.cumsum(rng.normal(0, 1.0, n)) * rng.choice([1.0, 3e3], n)).astype(np.float32)
+            y = np.cumsum(rng.normal(0, 0.01, n)).astype(np.float32)
+            eb = float(np.float32(1e-4 * (x.max() - x.min())))
+            sa, sb = port.compress(x, eb, L, T), port.compress(y, eb, L, T)
+            codec = Z.Codec(n, L, T)
+            fa = Z.DeviceStream.from_bytes(codec, sa)
+            assert np.array_equal(codec.decompress(fa, eb).cpu().numpy(), port.decompress(sa, n, eb, L, T)), (L, T)
+            fa, fb = Z.DeviceStream.from_bytes(codec, sa), Z.DeviceStream.from_bytes(codec, sb)
+            assert codec.homadd([fa, fb]).tobytes() == port.homadd(sa, sb, n, eb, L, T), (L, T)
+            codec.check()
+
+
 def test_box_tiles_and_exact_quantization_against_port(port, torch):
     """Full tiles whose element before them starts a 32-float row of a
     16-byte-aligned buffer move as TMA boxes; the others (segments starting
