@@ -233,7 +233,7 @@ ZG_HD ZSmem zg_smem_base(uint32_t kind, uint32_t L, uint32_t TB)
     const uint32_t tile_in = zg_tile_worst(L, TB) + 48u;  /* bytes, superset + reader slack */
     const uint32_t tile_out = zg_ring_bytes(L, TB) + 48u; /* the ring; readers look 32 past */
     const int need_rows = kind != 2 || L > 32;
-    m.rows = 512u;
+    m.rows = 1024u;
     if (kind == 0) {
         if (L <= 32) {
             m.in0 = m.rows;

@@ -135,6 +135,7 @@ __global__ void __launch_bounds__(320, 2) k_homadd(const __grid_constant__ HomAd
     uint64_t *empty = reinterpret_cast<uint64_t *>(smem + 16);  /* [2] input buffer consumed */
     uint32_t *wsum0 = reinterpret_cast<uint32_t *>(smem + 48);  /* [33] scan scratch, even tiles */
     uint32_t *wsum1 = reinterpret_cast<uint32_t *>(smem + 184); /* [33] odd tiles */
+    static_assert(320 + sizeof(ZRing4) <= 1024, "the ring's control block fits below the rows");
     ZRing4 *ring = reinterpret_cast<ZRing4 *>(smem + 320);
     ZPlace *pj = reinterpret_cast<ZPlace *>(smem + a.sm.jobs);
     HStage *stage = reinterpret_cast<HStage *>(smem + a.sm.jobs + zg_a16(sizeof(ZPlace))); /* [2] */

@@ -263,7 +263,7 @@ __device__ __forceinline__ void ring_publish(ZRing *ring, uint32_t k, uint64_t t
 }
 
 /* ------------------------------------------------------------------
- * The same hand-off with early sizes and four slots.  A tile's identity and
+ * The same hand-off with early sizes and ZR_SLOTS slots.  A tile's identity and
  * size go to the placer (mbarrier `sized`, one arrival by thread 0) right
  * after the scan has found them, so the placer's look-back runs while the
  * tile is still being packed; `packed` (one arrival per packing warp) then
@@ -271,9 +271,13 @@ __device__ __forceinline__ void ring_publish(ZRing *ring, uint32_t k, uint64_t t
  * takes the next `need` bytes (skipping to the ring's start when it would
  * not fit before the end) and may be written once the placer's running
  * count of released bytes, `tail`, shows that the space is free.  Up to
- * four packed tiles wait at once.
+ * ZR_SLOTS tiles are between sizing and write-out at once (the ring's bytes
+ * hold one worst-case tile, far more typical ones), so the packing warps do
+ * not wait for a placer delayed by a slow look-back; 16 measured 3.7 %
+ * faster than 4 on the two-way add.  Its control block sits below the
+ * rows at offset 1024 of shared memory.
  * ------------------------------------------------------------------ */
-#define ZR_SLOTS 4u
+#define ZR_SLOTS 16u
 
 struct ZRing4 {
     uint32_t placed; /* tiles written out (placer lane 0, release) */
