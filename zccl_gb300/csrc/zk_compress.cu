@@ -20,8 +20,10 @@
  *      shared memory, then hand it to the placer.
  * The packed tiles wait in a shared-memory ring that holds two typical
  * tiles.  The placer finds each one's byte offset with the look-back, writes
- * its bytes with 16-byte vector stores realigned to that offset and records
- * the offset, all while the compute warps work on the next tiles, so the
+ * its bytes with 16-byte vector stores realigned to that offset, records
+ * the offset and zeroes the ring bytes it has written out (the ring starts
+ * zeroed, so packing needs no zeroing pass and the tile's scan one barrier),
+ * all while the compute warps work on the next tiles, so the
  * look-back's latency never stalls them (the reference's per-thread scan and
  * second memcpy pass, ZCCL_float.c:774-791, disappear).
  * Full 32-element blocks with exact fast quantization take straight-line
@@ -91,7 +93,8 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
 {
     extern __shared__ __align__(16) uint8_t smem[];
     uint64_t *bar_tma = reinterpret_cast<uint64_t *>(smem);      /* the tile's floats arrived */
-    uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 32);    /* [33] */
+    uint32_t *wsum0 = reinterpret_cast<uint32_t *>(smem + 32);   /* [33] scan scratch, even rounds */
+    uint32_t *wsum1 = reinterpret_cast<uint32_t *>(smem + 320);  /* [33] odd rounds */
     uint64_t *s_tile = reinterpret_cast<uint64_t *>(smem + 168); /* the claimed tile (within its job) */
     uint32_t *s_amax = reinterpret_cast<uint32_t *>(smem + 176);
     uint32_t *s_pos = reinterpret_cast<uint32_t *>(smem + 184);  /* ring position of this tile */
@@ -119,12 +122,15 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
         ring->packed = 0;
         ring->placed = 0;
     }
+    /* the ring starts zeroed, and the placer zeroes what it has written out */
+    for (uint32_t i = tid; i < (zg_ring_bytes(L, blockDim.x - 32) + 48u) / 16u; i += blockDim.x)
+        reinterpret_cast<uint4 *>(outb)[i] = make_uint4(0, 0, 0, 0);
     __syncthreads();
 
     if (tid >= NC) { /* the placer warp */
         const uint64_t max_tiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
         placer_loop(
-            ring, outb, pj, a.w.err, max_tiles, bad, false,
+            ring, outb, pj, a.w.err, max_tiles, bad, true,
             [&](uint64_t k) {
                 if (lane == 0) ring_wait(&ring->packed, (uint32_t)k + 1, a.w.err);
             },
@@ -330,7 +336,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
          *    place */
         const uint32_t headb = z.has_head ? 4u : 0u;
         uint32_t total;
-        const uint32_t off = grp_excl_scan(size, wsum, &total, NC, 1);
+        const uint32_t off = grp_excl_scan1(size, (it & 1u) ? wsum1 : wsum0, &total, NC, 1);
         total += headb;
         if (warp == 0) lb_publish(J.status, tile, total, tile == 0, 0);
         uint32_t ticket = 0; /* the next tile's, taken now and used after the ring reservation */
@@ -351,9 +357,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
         named_sync(1, NC);
         const uint32_t pos = *s_pos;
         uint8_t *pk = outb + pos;
-        const uint32_t pk_sa = smem_u32(pk);
-        smem_zero(pk, total + 8, tid, NC);
-        named_sync(1, NC);
+        const uint32_t pk_sa = smem_u32(pk); /* zeroed: at the start, then by the placer */
         if (z.has_head && tid == 0) *reinterpret_cast<int32_t *>(pk) = qprev0;
         const uint32_t o = headb + off;
         if (FAST) {
