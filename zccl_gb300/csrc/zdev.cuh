@@ -697,6 +697,27 @@ __device__ __forceinline__ void grp_excl_scan2(uint32_t v0, uint32_t v1, uint32_
     named_sync(id, n);
 }
 
+/* grp_excl_scan2 with one barrier: every warp reads all warp sums.  Callers
+ * alternate between two pairs of scratch arrays on consecutive calls, as
+ * for grp_excl_scan1. */
+__device__ __forceinline__ void grp_excl_scan2_1(uint32_t v0, uint32_t v1, uint32_t *ws0, uint32_t *ws1,
+                                                 uint32_t &r0, uint32_t &r1, uint32_t &t0, uint32_t &t1,
+                                                 uint32_t n, uint32_t id)
+{
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = n >> 5;
+    const uint32_t i0 = warp_incl_scan(v0), i1 = warp_incl_scan(v1);
+    if (lane == 31) {
+        ws0[warp] = i0;
+        ws1[warp] = i1;
+    }
+    named_sync(id, n);
+    const uint32_t a = lane < nw ? ws0[lane] : 0u, b = lane < nw ? ws1[lane] : 0u;
+    t0 = __reduce_add_sync(0xffffffffu, a);
+    t1 = __reduce_add_sync(0xffffffffu, b);
+    r0 = __reduce_add_sync(0xffffffffu, lane < warp ? a : 0u) + i0 - v0;
+    r1 = __reduce_add_sync(0xffffffffu, lane < warp ? b : 0u) + i1 - v1;
+}
+
 /* The same over the whole CTA. */
 __device__ __forceinline__ uint32_t cta_excl_scan(uint32_t v, uint32_t *wsum, uint32_t *total)
 {

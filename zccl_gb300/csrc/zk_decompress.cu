@@ -114,10 +114,11 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
     extern __shared__ __align__(16) uint8_t smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem); /* [2] */
     uint32_t *wsum = reinterpret_cast<uint32_t *>(smem + 16);
-    uint64_t *bc = reinterpret_cast<uint64_t *>(smem + 160);     /* [2] the tile's starting value */
     uint64_t *s_base = reinterpret_cast<uint64_t *>(smem + 192); /* [2] */
     uint32_t *s_q0 = reinterpret_cast<uint32_t *>(smem + 208);   /* [2] */
     uint32_t *ws1 = reinterpret_cast<uint32_t *>(smem + 320); /* [33] second scan scratch */
+    uint32_t *ws2 = reinterpret_cast<uint32_t *>(smem + 464); /* [33] the same pair, odd rounds */
+    uint32_t *ws3 = reinterpret_cast<uint32_t *>(smem + 608); /* [33] */
     float *rows = reinterpret_cast<float *>(smem + a.sm.rows);
 
     const ZGeom &g = a.g;
@@ -150,9 +151,13 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
     if (tile < g.ntiles) cur = stage_tile(a, tile, ix, smem + a.sm.in0, &bar[0], wsum, &s_base[0], &s_q0[0], bad);
     ix = load_idx(a, tnext);
 
+    /* Two barriers a tile: the scan's and the one before the rows leave.
+     * The input buffer the next copy overwrites was last read before this
+     * tile's scan; the tile's byte offset and starting value (thread 0, at
+     * the copy) are visible through the copy's mbarrier; the box is free
+     * again once thread 0 has seen the last store read it, before the scan. */
     for (uint32_t it = 0;; it++) {
         const uint32_t cb = it & 1u;
-        __syncthreads(); /* the previous tile's buffer, rows and slots are free */
         if (tile >= g.ntiles) break;
         ZTile z;
         zg_tile(&g, tile, &z);
@@ -205,7 +210,8 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
                 }
             }
             uint32_t totn;
-            grp_excl_scan2(bsum, sizen, wsum, ws1, pre, nxt.off, tsum, totn, blockDim.x, 0);
+            if (!SUMS && tid == 0) bulk_wait_read0(); /* the previous box has left the rows */
+            grp_excl_scan2_1(bsum, sizen, cb ? wsum : ws2, cb ? ws1 : ws3, pre, nxt.off, tsum, totn, blockDim.x, 0);
             if (tnext < g.ntiles && tid == 0)
                 issue_tile(a, ix, totn + (zn.has_head ? 4u : 0u), smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u],
                            &s_base[cb ^ 1u], &s_q0[cb ^ 1u], bad);
@@ -218,10 +224,7 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
             tnext += gridDim.x;
             continue;
         }
-        if (tid == 0) bc[2] = z.has_head ? (uint32_t)head : s_q0[cb];
-        if (tid == 0) bulk_wait_read0(); /* the previous box has left the rows */
-        __syncthreads();
-        const uint32_t q0 = (uint32_t)bc[2];
+        const uint32_t q0 = z.has_head ? (uint32_t)head : s_q0[cb];
         const bool box = rows_ok && z.nblk == 256 && z.e_end - z.e_first == 8192 && ((z.e_first - 1) & 31) == 0;
 
         /* 4. values into rows, then out */
