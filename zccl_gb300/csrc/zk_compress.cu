@@ -413,7 +413,7 @@ cudaError_t launch_compress(const CompressArgs &a, cudaStream_t st)
     CompressArgs b = a;
     alignas(64) CUtensorMap map;
     memset(&map, 0, sizeof map);
-    b.rows_map = fast && !a.batch.jobs && zk_rows_map(&map, a.job.x, a.job.g.n);
+    b.rows_map = fast && !a.batch.jobs && zk_rows_map(&map, a.job.x, a.job.g.n, 256);
     if (fast)
         k_compress<true><<<grid, threads, a.sm.total, st>>>(b, map);
     else

@@ -126,10 +126,11 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
     const uint32_t L = g.L, stride = zg_row_stride(L);
     uint32_t bad = 0;
     /* Full tiles of L = 32 whose first element minus one starts a 128-byte
-     * row of y leave by one TMA tensor store: 256 rows of 32 floats, the
-     * element before the tile first, in a 1024-byte-aligned box with the
-     * 128-byte swizzle (16-byte chunk k of row r at chunk k ^ (r & 7)), so
-     * that each thread's vector stores of its row meet no bank conflict. */
+     * row of y leave by TMA tensor stores, one per warp of 32 rows of 32
+     * floats (the element before the tile first), from a 1024-byte-aligned
+     * box with the 128-byte swizzle (16-byte chunk k of row r at chunk
+     * k ^ (r & 7)), so that each thread's vector stores of its row meet no
+     * bank conflict. */
     const uint32_t rows_sa = smem_u32(rows);
     const uint32_t box_sa = (rows_sa + 1023u) & ~1023u;
     const bool rows_ok = FAST && a.rows_map && L == 32 && g.TB == 256 && blockDim.x == 256 &&
@@ -151,11 +152,13 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
     if (tile < g.ntiles) cur = stage_tile(a, tile, ix, smem + a.sm.in0, &bar[0], wsum, &s_base[0], &s_q0[0], bad);
     ix = load_idx(a, tnext);
 
-    /* Two barriers a tile: the scan's and the one before the rows leave.
-     * The input buffer the next copy overwrites was last read before this
-     * tile's scan; the tile's byte offset and starting value (thread 0, at
-     * the copy) are visible through the copy's mbarrier; the box is free
-     * again once thread 0 has seen the last store read it, before the scan. */
+    /* One barrier a tile, the scan's (one more before the rows leave when a
+     * tile has short or long blocks).  The input buffer the next copy
+     * overwrites was last read before this tile's scan; the tile's byte
+     * offset and starting value (thread 0, at the copy) are visible through
+     * the copy's mbarrier; each warp writes and sends out only its own 32
+     * rows, and its box rows are free again once its lane 0 has seen its
+     * last store read them, before the scan. */
     for (uint32_t it = 0;; it++) {
         const uint32_t cb = it & 1u;
         if (tile >= g.ntiles) break;
@@ -210,7 +213,7 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
                 }
             }
             uint32_t totn;
-            if (!SUMS && tid == 0) bulk_wait_read0(); /* the previous box has left the rows */
+            if (!SUMS && lane == 0) bulk_wait_read0(); /* the warp's last box store has left the rows */
             grp_excl_scan2_1(bsum, sizen, cb ? wsum : ws2, cb ? ws1 : ws3, pre, nxt.off, tsum, totn, blockDim.x, 0);
             if (tnext < g.ntiles && tid == 0)
                 issue_tile(a, ix, totn + (zn.has_head ? 4u : 0u), smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u],
@@ -231,31 +234,26 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
         float *row = rows + tid * stride;
         if (box) { /* every block is full: element e_first + 32 tid + j is box float 1 + 32 tid + j */
             uint32_t q = q0 + pre;
+            /* the float before this block, the previous block's last (or the
+             * value before the tile: the head, or the previous tile's last
+             * element, stored there too with the same bits) */
+            const float prev = __fmul_rn(__int2float_rn((int32_t)q), a.eb);
             float v[32];
 #pragma unroll
             for (int j = 0; j < 32; j++) {
                 q += d[j];
                 v[j] = __fmul_rn(__int2float_rn((int32_t)q), a.eb);
             }
-            /* the float before this block: the previous thread's last, or for
-             * thread 0 the value before the tile (the head or the previous
-             * tile's last element, stored there too with the same bits) */
-            float prev = __shfl_up_sync(0xffffffffu, v[31], 1);
-            if (tid == 0) prev = __fmul_rn(__int2float_rn((int32_t)q0), a.eb);
             const uint32_t rb = box_sa + tid * 128u, x4 = (tid & 7u) << 4;
-            if (lane != 0 || tid == 0) {
-                st_shared_v4(rb | x4, prev, v[0], v[1], v[2]);
-            } else { /* chunk 0's first float is the previous warp's to write */
-                st_shared_f32((rb | x4) + 4u, v[0]);
-                st_shared_f32((rb | x4) + 8u, v[1]);
-                st_shared_f32((rb | x4) + 12u, v[2]);
-            }
+            st_shared_v4(rb | x4, prev, v[0], v[1], v[2]);
 #pragma unroll
             for (uint32_t k = 1; k < 8; k++)
                 st_shared_v4(rb | ((k << 4) ^ x4), v[4 * k - 1], v[4 * k], v[4 * k + 1], v[4 * k + 2]);
-            if (lane == 31 && tid != 255) st_shared_f32(rb + 128u, v[31]); /* row tid + 1, chunk 0 at 0 */
-            if (tid == 255) a.y[z.e_end - 1] = v[31];                      /* past the box */
+            if (tid == 255) a.y[z.e_end - 1] = v[31]; /* past the box; the others are the next rows' first */
             fence_proxy_async_smem();
+            __syncwarp();
+            /* the warp's 32 rows leave by one TMA store */
+            if (lane == 0) tma_store_2d(&ymap, box_sa + warp * 4096u, 0, (int32_t)((z.e_first - 1) >> 5) + 32 * (int32_t)warp);
         } else if (full) {
             uint32_t q = q0 + pre;
 #pragma unroll
@@ -274,20 +272,19 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
                 g.fmt);
         }
         if (z.has_head && tid == 0) a.y[z.seg_start] = __fmul_rn(__int2float_rn(head), a.eb);
-        __syncthreads();
-        if (box) {
-            if (tid == 0) tma_store_2d(&ymap, box_sa, 0, (int32_t)((z.e_first - 1) >> 5));
-        } else if (FAST && L == 32 && z.nblk == g.TB && z.e_end - z.e_first == 32ull * g.TB) {
-            /* a full tile: 32-float rows, unrolled so that many stores are
-             * in flight per warp */
+        if (box) { /* each warp has sent its rows out above */
+        } else if (FAST && L == 32 && z.nblk == g.TB && z.e_end - z.e_first == 32ull * g.TB && nw * 32u == g.TB) {
+            /* a full tile: each warp stores its own 32 rows (no barrier),
+             * unrolled so that many stores are in flight */
+            __syncwarp();
             float *dst = a.y + z.e_first + lane;
-            const uint32_t nrow = g.TB / nw; /* rows per warp */
 #pragma unroll 8
-            for (uint32_t r = 0; r < nrow; r++) {
-                const uint32_t k = warp + r * nw;
+            for (uint32_t r = 0; r < 32; r++) {
+                const uint32_t k = warp * 32u + r;
                 dst[k * 32u] = rows[k * stride + lane];
             }
         } else {
+            __syncthreads();
             for (uint32_t k = warp; k < z.nblk; k += nw) {
                 const uint32_t nk = zg_block_len(z.seg_len, L, z.blk0 + k);
                 float *dst = a.y + z.e_first + (uint64_t)k * L;
@@ -298,7 +295,7 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
         tile = tnext;
         tnext += gridDim.x;
     }
-    if (tid == 0) bulk_wait0();
+    if (lane == 0) bulk_wait0();
     if (bad) atomicOr(a.w.err, bad);
 }
 
@@ -352,7 +349,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_tiled()
 
 } // namespace
 
-bool zk_rows_map(CUtensorMap *map, const void *p, uint64_t n)
+bool zk_rows_map(CUtensorMap *map, const void *p, uint64_t n, uint32_t box_rows)
 {
     const uint64_t nrows = n / 32u;
     if (((uintptr_t)p & 15u) || nrows < 256u || nrows > 0x7fffffffull) return false;
@@ -360,7 +357,7 @@ bool zk_rows_map(CUtensorMap *map, const void *p, uint64_t n)
     if (!enc) return false;
     const cuuint64_t dim[2] = {32u, nrows};
     const cuuint64_t stride[1] = {128u};
-    const cuuint32_t box[2] = {32u, 256u};
+    const cuuint32_t box[2] = {32u, box_rows};
     const cuuint32_t estride[2] = {1u, 1u};
     return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(p), dim, stride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
                CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
@@ -395,7 +392,7 @@ cudaError_t launch_decompress(const DecompressArgs &a, cudaStream_t st)
     b.qprev_valid = 1;
     alignas(64) CUtensorMap map;
     memset(&map, 0, sizeof map);
-    b.rows_map = fast && zk_rows_map(&map, a.y, a.g.n);
+    b.rows_map = fast && zk_rows_map(&map, a.y, a.g.n, 32);
     void *args[] = {&b, &map};
     return cudaLaunchKernel(fn, dim3(grid), dim3(a.g.TB), args, a.sm.total, st);
 }

@@ -513,11 +513,12 @@ cudaError_t sz3_compress(uint8_t *out, uint64_t cap, const float *x, uint64_t d1
 cudaError_t sz3_decompress(float *y, const uint8_t *in, uint64_t avail, uint64_t d1, uint64_t d2, uint64_t d3,
                            uint32_t bs, double eb, void *ws, cudaStream_t st);
 
-/* Host: a 2-D TMA map of the floats p[0, n) as rows of 32, boxes of 256
- * rows, 128-byte swizzle (16-byte chunk k of row r lands at chunk k ^ (r & 7)
- * of a 1024-byte-aligned box).  False when p is not 16-byte aligned, holds
- * fewer than one box, or the driver's encoder is unavailable. */
-bool zk_rows_map(CUtensorMap *map, const void *p, uint64_t n);
+/* Host: a 2-D TMA map of the floats p[0, n) as rows of 32, boxes of
+ * box_rows rows (256: a whole tile; 32: one warp's rows), 128-byte swizzle
+ * (16-byte chunk k of row r lands at chunk k ^ (r & 7) of a 1024-byte-aligned
+ * box).  False when p is not 16-byte aligned, holds fewer than one tile's
+ * 256 rows, or the driver's encoder is unavailable. */
+bool zk_rows_map(CUtensorMap *map, const void *p, uint64_t n, uint32_t box_rows);
 cudaError_t launch_homadd(const HomAddArgs &a, cudaStream_t st);
 cudaError_t launch_walk(const WalkArgs &a, cudaStream_t st);
 
