@@ -692,6 +692,8 @@ struct DevBuf {
 struct DropCtx {
     std::mutex mu;
     cudaStream_t st = nullptr;
+    cudaStream_t st2 = nullptr; /* a second input's copy, beside the first one's walk */
+    cudaEvent_t ev = nullptr;
     DevBuf fin, fout, s[3], ix[3], ws;
 };
 
@@ -704,7 +706,9 @@ DropCtx *drop_ctx()
     std::lock_guard<std::mutex> lk(gmu);
     if (!ctxs[dev]) {
         DropCtx *c = new DropCtx();
-        if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) {
+        if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->ev, cudaEventDisableTiming) != cudaSuccess) {
             delete c;
             return nullptr;
         }
@@ -764,7 +768,7 @@ void report(const char *fn, int rc)
  * *capped reports whether a host copy stopped short of the largest size the
  * stream could have. */
 int stage_stream(DropCtx *c, int slot, const unsigned char *cmp, const ZGeom &g,
-                 zccl_gpu_stream *s, bool full, bool *capped)
+                 zccl_gpu_stream *s, bool full, bool *capped, cudaStream_t cst = nullptr)
 {
     *capped = false;
     size_t ixb = index_layout(g).total;
@@ -789,7 +793,7 @@ int stage_stream(DropCtx *c, int slot, const unsigned char *cmp, const ZGeom &g,
     size_t bytes = (full || want < room) ? want : room;
     *capped = bytes < want;
     if (int rc = c->s[slot].ensure(bytes)) return rc;
-    if (cudaMemcpyAsync(c->s[slot].p, cmp, bytes, cudaMemcpyHostToDevice, c->st) != cudaSuccess)
+    if (cudaMemcpyAsync(c->s[slot].p, cmp, bytes, cudaMemcpyHostToDevice, cst ? cst : c->st) != cudaSuccess)
         return ZCCL_GPU_ECUDA;
     s->bytes = (unsigned char *)c->s[slot].p;
     s->capacity = bytes;
@@ -895,10 +899,21 @@ int dropin_homadd(unsigned char *final_cmp, size_t *final_size, size_t n, float 
     out.index = c->ix[2].p;
     for (int pass = 0;; pass++) { /* second pass: see dropin_decompress */
         bool cap1, cap2;
+        /* the first input's index walk runs while the second input is
+         * copied on the other stream; then the second's walk, a check of
+         * both, and the add of the indexed inputs */
+        if (cudaMemsetAsync(c->ws.p, 0, ws_clear_bytes(g), c->st) != cudaSuccess) return ZCCL_GPU_ECUDA;
         if (int rc = stage_stream(c, 0, cmp1, g, &in[0], pass > 0, &cap1)) return rc;
-        if (int rc = stage_stream(c, 1, cmp2, g, &in[1], pass > 0, &cap2)) return rc;
-        if (int rc = zccl_gpu_homadd(&out, in, 2, n, L, T, c->ws.p, c->st)) return rc;
+        if (int rc = walk_stream(&in[0], g, c->ws.p, c->st)) return rc;
+        if (int rc = stage_stream(c, 1, cmp2, g, &in[1], pass > 0, &cap2, c->st2)) return rc;
+        if (cudaEventRecord(c->ev, c->st2) != cudaSuccess || cudaStreamWaitEvent(c->st, c->ev, 0) != cudaSuccess)
+            return ZCCL_GPU_ECUDA;
+        if (int rc = walk_stream(&in[1], g, c->ws.p, c->st)) return rc;
         int rc = finish(c, c->ws.p);
+        if (rc == ZCCL_GPU_OK) {
+            if ((rc = zccl_gpu_homadd(&out, in, 2, n, L, T, c->ws.p, c->st))) return rc;
+            rc = finish(c, c->ws.p);
+        }
         if (rc == ZCCL_GPU_EBOUNDS && (cap1 || cap2) && pass == 0) continue;
         if (rc) return rc;
         break;
