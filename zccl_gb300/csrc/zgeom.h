@@ -249,9 +249,15 @@ ZG_HD ZSmem zg_smem_base(uint32_t kind, uint32_t L, uint32_t TB)
         return m;
     }
     m.in0 = zg_a16(m.rows + (need_rows ? rows_bytes : 0u));
+    if (kind == 1) { /* one input buffer: three CTAs per SM instead of two buffers' two */
+        m.in1 = m.in0;
+        m.out = zg_a16(m.in0 + tile_in);
+        m.total = m.out;
+        return m;
+    }
     m.in1 = zg_a16(m.in0 + tile_in);
     m.out = zg_a16(m.in1 + tile_in);
-    m.total = zg_a16(m.out + (kind == 1 ? 0u : tile_out));
+    m.total = zg_a16(m.out + tile_out);
     return m;
 }
 

@@ -109,7 +109,7 @@ __device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, uint64_
  * the tile after next already loading.  SUMS: only each tile's wrapped sum of
  * deltas, into the index's tile_qprev (k_qprev_scan completes it). */
 template <bool FAST, bool SUMS>
-__global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, const __grid_constant__ CUtensorMap ymap)
+__global__ void __launch_bounds__(256, 3) k_decompress(const DecompressArgs a, const __grid_constant__ CUtensorMap ymap)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem); /* [2] */
@@ -166,6 +166,9 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
         zg_tile(&g, tile, &z);
 
         BlockSlot nxt = {0, 0, 0}; /* the next tile's block, found in step 3 */
+        uint32_t next_bytes = 0;  /* the next tile's bytes */
+        bool issue_now = true;    /* its copy starts right after the scan */
+        TileIdx ixn;              /* its index entries */
 
         /* 2. unpack this tile's deltas */
         mbar_wait(&bar[cb], (it >> 1) & 1u, a.w.err);
@@ -215,9 +218,15 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
             uint32_t totn;
             if (!SUMS && lane == 0) bulk_wait_read0(); /* the warp's last box store has left the rows */
             grp_excl_scan2_1(bsum, sizen, cb ? wsum : ws2, cb ? ws1 : ws3, pre, nxt.off, tsum, totn, blockDim.x, 0);
-            if (tnext < g.ntiles && tid == 0)
-                issue_tile(a, ix, totn + (zn.has_head ? 4u : 0u), smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u],
-                           &s_base[cb ^ 1u], &s_q0[cb ^ 1u], bad);
+            /* with one input buffer, a tile with short or long blocks reads
+             * it again for the values: its successor's copy waits for that */
+            next_bytes = totn + (tnext < g.ntiles && zn.has_head ? 4u : 0u);
+            issue_now = SUMS || a.sm.in0 != a.sm.in1 ||
+                        (FAST && L == 32 && z.nblk == g.TB && z.e_end - z.e_first == 32ull * g.TB);
+            if (tnext < g.ntiles && tid == 0 && issue_now)
+                issue_tile(a, ix, next_bytes, smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u], &s_base[cb ^ 1u],
+                           &s_q0[cb ^ 1u], bad);
+            ixn = ix;
             ix = load_idx(a, tnext + gridDim.x);
         }
         if (SUMS) { /* the tile's delta sum; the values wait for the scan */
@@ -285,6 +294,9 @@ __global__ void __launch_bounds__(256) k_decompress(const DecompressArgs a, cons
             }
         } else {
             __syncthreads();
+            if (!issue_now && tnext < g.ntiles && tid == 0) /* every read of the one input buffer is done */
+                issue_tile(a, ixn, next_bytes, smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u], &s_base[cb ^ 1u],
+                           &s_q0[cb ^ 1u], bad);
             for (uint32_t k = warp; k < z.nblk; k += nw) {
                 const uint32_t nk = zg_block_len(z.seg_len, L, z.blk0 + k);
                 float *dst = a.y + z.e_first + (uint64_t)k * L;
