@@ -57,7 +57,8 @@ __device__ __forceinline__ bool box_tile(const CompressArgs &a, const ZGeom &g, 
  * caller synchronises before reading them. */
 __device__ __forceinline__ void claim_tile(const CompressArgs &a, uint64_t t, uint8_t *in, uint64_t *bar,
                                            uint64_t *s_tile, uint32_t *s_job, uint32_t *s_amax,
-                                           CompressJob *slot, uint8_t *box, const CUtensorMap *xmap)
+                                           CompressJob *slot, uint32_t *slot_job, uint8_t *box,
+                                           const CUtensorMap *xmap)
 {
     if (threadIdx.x != 0) return;
     *s_amax = 0;
@@ -68,8 +69,11 @@ __device__ __forceinline__ void claim_tile(const CompressArgs &a, uint64_t t, ui
     }
     uint64_t local;
     const uint32_t j = batch_job(a.batch, t, &local);
-    copy16(slot, a.batch.jobs ? static_cast<const CompressJob *>(a.batch.jobs) + j : &a.job,
-           sizeof(CompressJob));
+    if (*slot_job != j) { /* the slot keeps its job from tile to tile */
+        copy16(slot, a.batch.jobs ? static_cast<const CompressJob *>(a.batch.jobs) + j : &a.job,
+               sizeof(CompressJob));
+        *slot_job = j;
+    }
     *s_tile = local;
     *s_job = j;
     ZTile zt;
@@ -99,6 +103,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
     uint32_t *s_amax = reinterpret_cast<uint32_t *>(smem + 176);
     uint32_t *s_pos = reinterpret_cast<uint32_t *>(smem + 184);  /* ring position of this tile */
     uint32_t *s_job = reinterpret_cast<uint32_t *>(smem + 188);  /* the claimed tile's job */
+    uint32_t *s_slot = reinterpret_cast<uint32_t *>(smem + 192); /* [2] the job each job slot holds */
     ZRing *ring = reinterpret_cast<ZRing *>(smem + 256);
     CompressJob *cj = reinterpret_cast<CompressJob *>(smem + a.sm.jobs); /* [2], by round */
     ZPlace *pj = reinterpret_cast<ZPlace *>(smem + a.sm.jobs + 2 * sizeof(CompressJob));
@@ -121,6 +126,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
         mbar_init(bar_tma, 1);
         ring->packed = 0;
         ring->placed = 0;
+        s_slot[0] = s_slot[1] = 0xFFFFFFFFu;
     }
     /* the ring starts zeroed, and the placer zeroes what it has written out */
     for (uint32_t i = tid; i < (zg_ring_bytes(L, blockDim.x - 32) + 48u) / 16u; i += blockDim.x)
@@ -157,7 +163,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
     /* the compute warps */
     const uint32_t R = zg_ring_bytes(L, NC);
     uint32_t pos_prev = 0, end_prev = 0; /* thread 0: the previous tile's place in the ring */
-    if (tid == 0) claim_tile(a, atomicAdd(a.w.ticket, 1u), in, bar_tma, s_tile, s_job, s_amax, &cj[0], box, &xmap);
+    if (tid == 0) claim_tile(a, atomicAdd(a.w.ticket, 1u), in, bar_tma, s_tile, s_job, s_amax, &cj[0], &s_slot[0], box, &xmap);
     named_sync(1, NC);
     uint64_t tile = *s_tile;
     uint32_t job = *s_job;
@@ -352,7 +358,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
          *    while holding a claimed tile whose size is not yet published. */
         if (tid == 0) {
             *s_pos = ring_reserve(ring, it, zg_ring_need(total), R, pos_prev, end_prev, a.w.err);
-            if (FAST) claim_tile(a, ticket, in, bar_tma, s_tile, s_job, s_amax, &cj[(it + 1) & 1u], box, &xmap);
+            if (FAST) claim_tile(a, ticket, in, bar_tma, s_tile, s_job, s_amax, &cj[(it + 1) & 1u], &s_slot[(it + 1) & 1u], box, &xmap);
         }
         named_sync(1, NC);
         const uint32_t pos = *s_pos;
@@ -388,7 +394,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
                     g.fmt);
             }
             named_sync(1, NC); /* the rows have been read for the last time */
-            if (tid == 0) claim_tile(a, ticket, in, bar_tma, s_tile, s_job, s_amax, &cj[(it + 1) & 1u], box, &xmap);
+            if (tid == 0) claim_tile(a, ticket, in, bar_tma, s_tile, s_job, s_amax, &cj[(it + 1) & 1u], &s_slot[(it + 1) & 1u], box, &xmap);
         }
         named_sync(1, NC); /* the packed tile is complete; the claimed index is visible */
         if (tid == 0) ring_publish(ring, it, tile, job, total, pos);
