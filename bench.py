@@ -187,19 +187,21 @@ def host_read_bytes(stream_bytes: bytes, n: int, L: int, T: int) -> int:
 
 def cpu_codec_rate(x, y, eb, L, T, reps=1):
     """GB/s of uncompressed input for compress + decompress + homomorphic add
-    with the oracle port on all host cores; returns (GB/s, seconds/pass)."""
+    with the oracle port on T host threads: the best of `reps` passes after
+    one warm-up pass; returns (GB/s, seconds/pass)."""
     from oracle import zoracle
     port = zoracle.port()
     n = x.size
     sb = port.compress(y, eb, L, T)
     best = None
-    for _ in range(reps + 1):
+    for k in range(reps + 1):
         t0 = time.perf_counter()
         sa = port.compress(x, eb, L, T)
         port.decompress(sa, n, eb, L, T)
         port.homadd(sa, sb, n, eb, L, T)
         dt = time.perf_counter() - t0
-        best = dt if best is None else min(best, dt)
+        if k:
+            best = dt if best is None else min(best, dt)
     return 3 * 4 * n / best / 1e9, best
 
 
@@ -742,10 +744,17 @@ def run_ours(args, rank, world, local_rank):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        rate, secs = cpu_codec_rate(xh, yh, eb, L, T)
+        rate, secs = cpu_codec_rate(xh, yh, eb, L, T, reps=5)
+        m = n // 16
+        Z.set_omp_threads(1)
+        rate1, secs1 = cpu_codec_rate(xh[:m], yh[:m], eb, L, 1, reps=1)
+        Z.set_omp_threads(T)
         cpu = {"value": round(rate, 3), "unit": "GB/s", "cores": T, "kind": "port",
-               "sample": f"whole field, one pass ({secs:.2f} s) of compress+decompress+homadd, "
-                         f"oracle C restatement, OpenMP {T} threads"}
+               "sample": f"whole field, best of 5 passes after one warm-up ({secs:.2f} s a pass) of "
+                         f"compress+decompress+homadd, oracle C restatement, OpenMP {T} threads",
+               "single_thread": {"value": round(rate1, 3), "unit": "GB/s", "cores": 1,
+                                 "sample": f"first {m} elements, T=1, best of 1 after one warm-up "
+                                           f"({secs1:.2f} s a pass)"}}
 
     extras = {}
     if rank == 0 and not args.no_extras:
