@@ -112,7 +112,8 @@ Sz3Split sz3_split(double d)
 
 /* (int)floor((double)x * inv + 0.5), each step rounded as double
  * arithmetic rounds it (ZCCL_float.h:57-61).  FP64 is slow on this GPU, so
- * the product is first formed as a float pair: hi = x*ih, its exact error
+ * small products take one FMA (below); larger ones are first formed as a
+ * float pair: hi = x*ih, its exact error
  * by FMA, plus x*il, within 2^-19 of x*inv + 0.5 when |x*ih| < 2^26.  When
  * the fractional part of that sum is more than 2^-12 from an integer, no
  * rounding of the exact product (at most 2^-27 here) can move it across
@@ -121,6 +122,14 @@ Sz3Split sz3_split(double d)
  * they are.  *bad is set where the reference is undefined. */
 __device__ __forceinline__ int32_t sz3_quantize(float x, const Sz3Split &inv, uint32_t &bad)
 {
+    /* Below 2^11 one FMA suffices: x * ih + 0.5 rounded once is within
+     * 2^-12.4 of x * inv + 0.5 (x * il and half an ulp), so a fraction more
+     * than 2^-12 from an integer floors like the exact value. */
+    const float t1 = __fmaf_rn(x, inv.hi, 0.5f);
+    if (inv.ok && fabsf(t1) < 2048.0f) { /* NaN fails */
+        const float n1 = floorf(t1), f1 = __fsub_rn(t1, n1);
+        if (f1 > 2.44140625e-4f && f1 < 0.999755859375f) return (int32_t)n1;
+    }
     const float th = __fmul_rn(x, inv.hi);
     if (inv.ok && fabsf(th) < 67108864.0f) { /* 2^26; NaN takes the double path */
         const float tl = __fmaf_rn(x, inv.lo, __fmaf_rn(x, inv.hi, -th));
@@ -580,7 +589,7 @@ __device__ __forceinline__ void sz3_walk(const float *__restrict__ x, const Sz3D
  * one after another by the whole warp).  The last unit records the
  * stream's size. */
 template <uint32_t BS>
-__global__ void __launch_bounds__(SZ_THREADS) k_sz3_compress_rows(const float *__restrict__ x, Sz3Dims g, Sz3Split inv,
+__global__ void __launch_bounds__(SZ_THREADS, BS <= 4 ? 4 : 3) k_sz3_compress_rows(const float *__restrict__ x, Sz3Dims g, Sz3Split inv,
                                                                   uint8_t *out, uint64_t cap, uint64_t *status,
                                                                   uint32_t *ticket, uint64_t *total, uint32_t *err)
 {
