@@ -7,6 +7,8 @@ from __future__ import annotations
 import hashlib
 import json
 import os
+import shutil
+import subprocess
 
 import numpy as np
 import pytest
@@ -23,6 +25,23 @@ def load_golden():
 
 def sha(a) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def test_float_rounding_tiers_match_double(tmp_path):
+    """The codec's float quantization and reconstruction tiers (one FMA,
+    float pairs, then the double steps near ties), restated in C with IEEE
+    float arithmetic, give the double steps' integers and floats on about
+    80 million seeded random, near-tie and wide-range inputs."""
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    exe = tmp_path / "sz3_rounding"
+    src = os.path.join(os.path.dirname(__file__), "native", "sz3_rounding.c")
+    subprocess.run([cc, "-O2", "-ffp-contract=off", "-o", str(exe), src, "-lm"], check=True)
+    out = subprocess.run([str(exe), "160000"], capture_output=True, text=True, timeout=120)
+    bad, checks = map(int, out.stdout.split())
+    assert checks > 50_000_000
+    assert bad == 0
 
 
 def test_port_matches_reference_golden(port):
