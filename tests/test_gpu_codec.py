@@ -181,6 +181,35 @@ def test_generic_block_sizes_against_port(port, torch):
             codec.check()
 
 
+def test_dropin_host_stream_with_a_long_last_chunk(port, torch):
+    """A host stream carries no length: its last chunk is first read at
+    twice the other chunks' average size, and read again in full when the
+    walk runs past that.  Here the last of four chunks is noise and the rest
+    nearly constant, so the first read falls short; decompress and the add
+    must still give the oracle's floats and bytes."""
+    T, L = 4, 32
+    Z.set_omp_threads(T)
+    rng = np.random.default_rng(23)
+    n = 4 * 50000 + 3
+    x = np.full(n, 1.0, np.float32)
+    x[3 * (n // 4):] = rng.normal(0, 1.0, n - 3 * (n // 4)).astype(np.float32)
+    y = (x + np.float32(0.5)).astype(np.float32)
+    eb = float(np.float32(1e-4 * (x.max() - x.min())))
+    sx, sy = port.compress(x, eb, L, T), port.compress(y, eb, L, T)
+    last = int.from_bytes(sx[8 * (T - 1): 8 * T], "little")
+    assert len(sx) - 8 * T - last > 2 * last // (T - 1) + 65536  # the first read is short
+    cap = 4 * n + 8 * T + 4096
+    s = np.zeros(cap, np.uint8)
+    s[: len(sx)] = np.frombuffer(sx, np.uint8)
+    t = np.zeros(cap, np.uint8)
+    t[: len(sy)] = np.frombuffer(sy, np.uint8)
+    out = np.zeros(n, np.float32)
+    Z.ZCCL_float_decompress_openmp_threadblock_arg(out, n, eb, L, s)
+    assert np.array_equal(out.view(np.uint32), port.decompress(sx, n, eb, L, T).view(np.uint32))
+    acc = Z.ZCCL_float_homomophic_add_openmp_threadblock(t, 0, n, eb, L, s, t)
+    assert t[:acc].tobytes() == port.homadd(sx, sy, n, eb, L, T)
+
+
 def test_walk_long_blocks_against_port(port, torch):
     """Byte-only streams (the header walk rebuilds the index) with blocks of
     up to 64, 128 and 256 elements: blocks of 256 bytes or more take the

@@ -782,8 +782,9 @@ int stage_stream(DropCtx *c, int slot, const unsigned char *cmp, const ZGeom &g,
         return s->capacity ? ZCCL_GPU_OK : ZCCL_GPU_EINVAL;
     }
     /* Host stream: the header gives the first T-1 chunk lengths; the last
-     * chunk is read up to its largest possible size, but not past the
-     * 4*nbEle bytes every reference caller allocates for a stream. */
+     * chunk is read up to its largest possible size (first at most twice the
+     * others' average), but not past the 4*nbEle bytes every reference
+     * caller allocates for a stream. */
     const size_t hdr = 8ull * g.T;
     uint64_t last;
     memcpy(&last, cmp + 8ull * (g.T - 1), 8);
@@ -791,6 +792,13 @@ int stage_stream(DropCtx *c, int slot, const unsigned char *cmp, const ZGeom &g,
     size_t want = known + (size_t)(zg_seg_worst(g.tbs, g.L) + zg_seg_worst(g.rem, g.L));
     size_t room = 4 * (size_t)g.n > known + 4 ? 4 * (size_t)g.n : known + 4;
     size_t bytes = (full || want < room) ? want : room;
+    /* a first read: the last chunk at twice the others' average length (a
+     * chunk at its worst size is six times a typical one); a walk that runs
+     * past it reports EBOUNDS and the caller reads again in full */
+    if (!full && g.T > 1) {
+        const size_t guess = known + 2 * ((size_t)last / (g.T - 1)) + 65536;
+        if (guess < bytes) bytes = guess;
+    }
     *capped = bytes < want;
     if (int rc = c->s[slot].ensure(bytes)) return rc;
     if (cudaMemcpyAsync(c->s[slot].p, cmp, bytes, cudaMemcpyHostToDevice, cst ? cst : c->st) != cudaSuccess)
