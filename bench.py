@@ -177,12 +177,18 @@ def seg_worst(length: int, L: int) -> int:
 
 def host_read_bytes(stream_bytes: bytes, n: int, L: int, T: int) -> int:
     """Bytes the drop-in copies to the device for a host stream: the chunk
-    offsets give all but the last chunk, which is read up to its largest
-    possible size but not past 4*n bytes (include/zccl_gpu.h)."""
+    offsets give all but the last chunk, which is read at twice the others'
+    average length (plus 64 KiB), and again up to its largest possible size
+    (not past 4*n bytes) only when its headers run past that."""
     last = int.from_bytes(stream_bytes[8 * (T - 1): 8 * T], "little")
     known = 8 * T + last
     want = known + seg_worst(n // T, L) + seg_worst(n % T, L)
-    return min(want, max(4 * n, known + 4))
+    first = min(want, max(4 * n, known + 4))
+    if T > 1:
+        first = min(first, known + 2 * (last // (T - 1)) + 65536)
+    if len(stream_bytes) > first:  # the walk runs past the first read: read again in full
+        first += want
+    return first
 
 
 def cpu_codec_rate(x, y, eb, L, T, reps=1):
