@@ -409,19 +409,6 @@ __device__ __forceinline__ void add_at(uint32_t (&v)[32], uint32_t j, uint32_t x
         if ((uint32_t)k == j) v[k] += x;
 }
 
-/* Zero shared bytes [0, nbytes) (rounded up to 16) of a 16-byte-aligned buffer. */
-__device__ __forceinline__ void smem_zero(uint8_t *s, uint32_t nbytes, uint32_t t, uint32_t nt)
-{
-    uint4 *s4 = reinterpret_cast<uint4 *>(s);
-    const uint4 z = make_uint4(0, 0, 0, 0);
-    for (uint32_t i = t; i < (nbytes + 15u) >> 4; i += nt) s4[i] = z;
-}
-
-__device__ __forceinline__ void smem_zero(uint8_t *s, uint32_t nbytes)
-{
-    smem_zero(s, nbytes, threadIdx.x, blockDim.x);
-}
-
 /* Barrier `id` (1..15) over the first n threads of the CTA (a multiple of
  * 32), for kernels whose warps split into groups; id 0 is __syncthreads. */
 __device__ __forceinline__ void named_sync(uint32_t id, uint32_t n)
@@ -664,42 +651,10 @@ __device__ __forceinline__ uint32_t grp_excl_scan1(uint32_t v, uint32_t *ws, uin
     return __reduce_add_sync(0xffffffffu, lane < warp ? t : 0u) + inc - v;
 }
 
-/* Two exclusive scans at once on the same barriers: v0 with scratch ws0,
- * v1 with ws1 (33 words each). */
-__device__ __forceinline__ void grp_excl_scan2(uint32_t v0, uint32_t v1, uint32_t *ws0, uint32_t *ws1,
-                                               uint32_t &r0, uint32_t &r1, uint32_t &t0, uint32_t &t1,
-                                               uint32_t n, uint32_t id)
-{
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = n >> 5;
-    const uint32_t i0 = warp_incl_scan(v0), i1 = warp_incl_scan(v1);
-    if (lane == 31) {
-        ws0[warp] = i0;
-        ws1[warp] = i1;
-    }
-    named_sync(id, n);
-    if (warp == 0) {
-        const uint32_t a = lane < nw ? ws0[lane] : 0u, b = lane < nw ? ws1[lane] : 0u;
-        const uint32_t ai = warp_incl_scan(a), bi = warp_incl_scan(b);
-        if (lane < nw) {
-            ws0[lane] = ai - a;
-            ws1[lane] = bi - b;
-        }
-        if (lane == 31) {
-            ws0[32] = ai;
-            ws1[32] = bi;
-        }
-    }
-    named_sync(id, n);
-    r0 = ws0[warp] + i0 - v0;
-    r1 = ws1[warp] + i1 - v1;
-    t0 = ws0[32];
-    t1 = ws1[32];
-    named_sync(id, n);
-}
-
-/* grp_excl_scan2 with one barrier: every warp reads all warp sums.  Callers
- * alternate between two pairs of scratch arrays on consecutive calls, as
- * for grp_excl_scan1. */
+/* Two exclusive scans at once (v0 with scratch ws0, v1 with ws1, 33 words
+ * each) over the first n threads, with one barrier: every warp reads all
+ * warp sums.  Callers alternate between two pairs of scratch arrays on
+ * consecutive calls, as for grp_excl_scan1. */
 __device__ __forceinline__ void grp_excl_scan2_1(uint32_t v0, uint32_t v1, uint32_t *ws0, uint32_t *ws1,
                                                  uint32_t &r0, uint32_t &r1, uint32_t &t0, uint32_t &t1,
                                                  uint32_t n, uint32_t id)
