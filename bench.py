@@ -18,6 +18,10 @@ roofline: algorithmic bytes of the dominant kernel per launch over its mean
          event-timed duration, against the measured HBM copy bandwidth.
 cpu_baseline: the oracle's C restatement of the reference codec with every
          host core, on the same field.
+parity: the GPU streams, homomorphic sums and decompressed floats of the
+         timed field (at eb = 1e-4 and 1e-3 of range) and of the P = 8 x 16M
+         reduction compared byte for byte with the oracle on the same
+         inputs; a mismatch fails the run after the line is printed.
 
 Launched as ``python bench.py --gpus N --steps K --warmup W``; for N > 1
 under torchrun every rank compresses its own field (weak scaling, no
@@ -53,6 +57,7 @@ def parse():
     p.add_argument("--T", type=int, default=0, help="writer thread count (default: host cores)")
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-parity", action="store_true", help="skip the byte-for-byte checks against the oracle")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the P-way reduction, batched and serving measurements")
     p.add_argument("--red-n", type=int, default=1 << 24, help="floats per rank chunk (reduction)")
@@ -86,58 +91,101 @@ def peaks():
 
 
 def make_field(side: int, seed: int, device):
-    """Log-normal Gaussian random field: white noise shaped to P(k) ~ k^-3 in
-    Fourier space, normalised to unit variance, then exp(1.5 g)."""
-    import torch
-    g = torch.Generator(device=device).manual_seed(seed)
-    kx = torch.fft.fftfreq(side, device=device)
-    kz = torch.fft.rfftfreq(side, device=device)
-    k2 = kx[:, None, None] ** 2 + kx[None, :, None] ** 2 + kz[None, None, :] ** 2
-    amp = torch.where(k2 > 0, k2.clamp_min(1e-12) ** (-0.75), torch.zeros_like(k2))  # |k|^-1.5
-    del k2
-    shape = (side, side, side // 2 + 1)
-    spec = torch.complex(torch.randn(shape, generator=g, device=device),
-                         torch.randn(shape, generator=g, device=device)) * amp
-    del amp
-    f = torch.fft.irfftn(spec, s=(side, side, side))
-    del spec
-    f = (f - f.mean()) / f.std()
-    return torch.exp(1.5 * f).reshape(-1).contiguous().float()
+    from zccl_gb300.workloads import grf_lognormal
+    return grf_lognormal(side, seed, device)
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle samples every 200 ms while running."""
+    """SM clock and throttle-reason samples while the timed region runs.
 
+    Reads NVML (libnvidia-ml, shipped with the driver) every 2 ms from a
+    background thread, so even a timed region of a few milliseconds gets
+    samples; where NVML cannot be loaded, nvidia-smi every 50 ms instead.
+    Only reads: no clock or other GPU setting is changed."""
+
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+    # nvmlClocksEventReason* bits
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40}
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_id: str):
         self.gpu_id = gpu_id
-        self.lines = []
+        self.samples = []  # (sm_mhz, max_mhz, set of reasons)
         self.proc = None
+        self.stop = threading.Event()
+        self.thread = None
+        self.source = None
+
+    def _nvml(self):
+        import ctypes
+        try:
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return None
+        if nv.nvmlInit_v2() != 0:
+            return None
+        h = ctypes.c_void_p()
+        gid = self.gpu_id.strip()
+        rc = (nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(int(gid)), ctypes.byref(h)) if gid.isdigit()
+              else nv.nvmlDeviceGetHandleByUUID(gid.encode(), ctypes.byref(h)))
+        if rc != 0:
+            return None
+        reasons_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        return nv, h, reasons_fn
+
+    def _poll_nvml(self, nv, h, reasons_fn):
+        import ctypes
+        mhz, mx, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop.is_set():
+            if (nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(mhz)) == 0 and
+                    nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0 and
+                    reasons_fn(h, ctypes.byref(rs)) == 0):
+                active = {k for k, b in self.BITS.items() if rs.value & b}
+                self.samples.append((float(mhz.value), float(mx.value), active))
+            time.sleep(0.002)
+
+    def _read_smi(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.strip().split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm, mx = float(parts[1]), float(parts[2])
+            except ValueError:
+                continue
+            active = {n for n, v in zip(self.NAMES, parts[5:9]) if v.lower().startswith("active")}
+            self.samples.append((sm, mx, active))
 
     def __enter__(self):
-        try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "50", "-i", self.gpu_id], stdout=subprocess.PIPE,
-                stderr=subprocess.DEVNULL, text=True)
-            threading.Thread(target=self._read, daemon=True).start()
-        except OSError:
-            self.proc = None
+        nvml = self._nvml()
+        if nvml:
+            self.source = "nvml, 2 ms"
+            self.thread = threading.Thread(target=self._poll_nvml, args=nvml, daemon=True)
+            self.thread.start()
+        else:
+            try:
+                self.proc = subprocess.Popen(
+                    ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                     "-lms", "50", "-i", self.gpu_id], stdout=subprocess.PIPE,
+                    stderr=subprocess.DEVNULL, text=True)
+                self.source = "nvidia-smi, 50 ms"
+                threading.Thread(target=self._read_smi, daemon=True).start()
+            except OSError:
+                self.proc = None
         # sampling is live before the timed region starts
         t0 = time.perf_counter()
-        while self.proc and not self.lines and time.perf_counter() - t0 < 3.0:
-            time.sleep(0.01)
-        self.lines = []  # keep only samples taken from here on
+        while (self.thread or self.proc) and not self.samples and time.perf_counter() - t0 < 3.0:
+            time.sleep(0.001)
+        self.samples = []  # keep only samples taken from here on
         return self
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
-
     def __exit__(self, *exc):
+        self.stop.set()
+        if self.thread:
+            self.thread.join(timeout=2)
         if self.proc:
             self.proc.terminate()
             try:
@@ -146,24 +194,14 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                sm.append(float(parts[1]))
-                mx.append(float(parts[2]))
-            except ValueError:
-                continue
-            for name, v in zip(names, parts[5:9]):
-                if v.lower().startswith("active"):
-                    reasons.add(name)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
-                "reasons": sorted(reasons), "samples": len(sm)}
+        samples = list(self.samples)
+        if not samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0, "source": self.source}
+        reasons = set()
+        for _, _, r in samples:
+            reasons |= r
+        return {"sm_mhz": statistics.median(s[0] for s in samples), "sm_max_mhz": max(s[1] for s in samples),
+                "reasons": sorted(reasons), "samples": len(samples), "source": self.source}
 
 
 def seg_worst(length: int, L: int) -> int:
@@ -194,7 +232,8 @@ def host_read_bytes(stream_bytes: bytes, n: int, L: int, T: int) -> int:
 def cpu_codec_rate(x, y, eb, L, T, reps=1):
     """GB/s of uncompressed input for compress + decompress + homomorphic add
     with the oracle port on T host threads: the best of `reps` passes after
-    one warm-up pass; returns (GB/s, seconds/pass)."""
+    one warm-up pass; returns (GB/s, seconds/pass, outputs of the last pass:
+    stream of x, its decompressed floats, stream of x + y)."""
     from oracle import zoracle
     port = zoracle.port()
     n = x.size
@@ -203,12 +242,29 @@ def cpu_codec_rate(x, y, eb, L, T, reps=1):
     for k in range(reps + 1):
         t0 = time.perf_counter()
         sa = port.compress(x, eb, L, T)
-        port.decompress(sa, n, eb, L, T)
-        port.homadd(sa, sb, n, eb, L, T)
+        ya = port.decompress(sa, n, eb, L, T)
+        ha = port.homadd(sa, sb, n, eb, L, T)
         dt = time.perf_counter() - t0
         if k:
             best = dt if best is None else min(best, dt)
-    return 3 * 4 * n / best / 1e9, best
+    return 3 * 4 * n / best / 1e9, best, {"stream": sa, "floats": ya, "sum": ha}
+
+
+def same_bits(a, b) -> bool:
+    """Two float32 arrays equal bit for bit (signed zeros and NaNs included)."""
+    import numpy as np
+    a, b = np.ascontiguousarray(a, np.float32), np.ascontiguousarray(b, np.float32)
+    return a.shape == b.shape and bool(np.array_equal(a.view(np.uint32), b.view(np.uint32)))
+
+
+def oracle_outputs(xh, yh, eb, L, T):
+    """The oracle's stream of x, decompressed floats and stream of x + y."""
+    from oracle import zoracle
+    port = zoracle.port()
+    n = xh.size
+    sa = port.compress(xh, eb, L, T)
+    return {"stream": sa, "floats": port.decompress(sa, n, eb, L, T),
+            "sum": port.homadd(sa, port.compress(yh, eb, L, T), n, eb, L, T)}
 
 
 def max_over_ranks(v: float, world: int, device) -> float:
@@ -262,23 +318,8 @@ def run_reference(args, rank, world):
 
 
 def make_rank_chunks(n: int, P: int, seed: int, device):
-    """P ranks' chunks: a shared smooth base (a sum of 8 random-phase
-    sinusoids) plus each rank's N(0, 0.05) perturbation from seed r."""
-    import math
-    import torch
-    g = torch.Generator(device=device).manual_seed(seed)
-    i = torch.arange(n, device=device, dtype=torch.float64)
-    period = 500.0 + 49500.0 * torch.rand(8, generator=g, device=device, dtype=torch.float64)
-    phase = 2 * math.pi * torch.rand(8, generator=g, device=device, dtype=torch.float64)
-    base = torch.zeros(n, device=device, dtype=torch.float64)
-    for k in range(8):
-        base += torch.sin(2 * math.pi * i / period[k] + phase[k])
-    del i
-    xs = []
-    for r in range(P):
-        gr = torch.Generator(device=device).manual_seed(r)
-        xs.append((base + 0.05 * torch.randn(n, generator=gr, device=device, dtype=torch.float64)).float())
-    return xs
+    from zccl_gb300.workloads import rank_chunks
+    return rank_chunks(n, P, seed, device)
 
 
 def timed(fn, reps, stream):
@@ -371,9 +412,39 @@ def reduction_bench(args, L, T, dev):
             "homomorphic": round(float((y_rho.double() - exact).abs().max()) / eb, 3),
             "doc": round(float((y_rdoc.double() - exact).abs().max()) / eb, 3)},
     }
+    if not args.no_parity:
+        res["parity"] = reduction_parity(codec, xs, streams, out, y_ho, ring, eb, L, T)
     del xs, exact
     torch.cuda.empty_cache()
     return res
+
+
+def reduction_parity(codec, xs, streams, out, y_ho, ring, eb, L, T):
+    """The P-way sum against the oracle's pairwise fold of the oracle's own
+    streams (the reference ring's acc = add(received, acc) order), every
+    rank's stream, the decompressed sum, and the emulated homomorphic ring's
+    reduced chunks against the same ring run by the oracle."""
+    from oracle import zoracle
+    port = zoracle.port()
+    n, P = codec.n, len(xs)
+    xh = [x.cpu().numpy() for x in xs]
+    sref = [port.compress(v, eb, L, T) for v in xh]
+    fold = port.homadd_fold(sref, n, eb, L, T)
+    chunks_ok = True
+    ring.homomorphic(xs, eb)
+    for c in range(P):
+        lo, m = ring.displs[c], ring.cnts[c]
+        S = [port.compress(xh[r][lo: lo + m], eb, L, T) for r in range(P)]
+        for i in range(P - 1):
+            for r in range(P):
+                src, cc = (r - 1) % P, (r - 2 - i) % P
+                if cc == c:
+                    S[r] = port.homadd(S[src], S[r], m, eb, L, T)
+        chunks_ok &= ring.reduced[c].tobytes() == S[c]
+    return {"rank_streams": all(s.tobytes() == r for s, r in zip(streams, sref)),
+            "pway_sum": out.tobytes() == fold,
+            "floats": same_bits(y_ho.cpu().numpy(), port.decompress(fold, n, eb, L, T)),
+            "ring_reduced_chunks": bool(chunks_ok)}
 
 
 def szp3d_bench(args, dev):
@@ -438,31 +509,13 @@ def batched_bench(args, L, dev):
     import numpy as np
     import torch
     import zccl_gb300 as Z
+    from zccl_gb300.workloads import gradient_buckets
     lib = Z.lib()
     npairs = args.batch_pairs
-    rng = np.random.default_rng(7)
-    sizes = np.exp(rng.uniform(np.log(1024), np.log(4 << 20), npairs)).astype(np.int64)
-    const = rng.random(npairs) < 0.05
-    eb_rel = rng.choice([1e-3, 1e-4, 1e-5], npairs)
     T = 1
-    total = int(2 * sizes.sum())
-    data = torch.empty(total, dtype=torch.float32, device=dev)
-    g = torch.Generator(device=dev).manual_seed(7)
-    u = (torch.rand(total, generator=g, device=dev, dtype=torch.float32) - 0.5).clamp_(-0.4999999, 0.4999999)
-    data.copy_(-1e-3 * torch.sign(u) * torch.log1p(-2 * u.abs()))  # Laplace(0, 1e-3)
-    del u
-    off, xs = 0, []
-    for k in range(npairs):
-        n = int(sizes[k])
-        pair = [data[off: off + n], data[off + n: off + 2 * n]]
-        off += 2 * n
-        if const[k]:
-            pair[0].fill_(0.5)
-            pair[1].fill_(0.25)
-        xs.append(pair)
-    lo = [min(float(p[0].min()), float(p[1].min())) for p in xs]
-    hi = [max(float(p[0].max()), float(p[1].max())) for p in xs]
-    ebs = [float(np.float32(eb_rel[k] * max(hi[k] - lo[k], 1e-3))) for k in range(npairs)]
+    bk = gradient_buckets(npairs, 7, dev)
+    sizes, xs, ebs, data = bk.sizes, bk.xs, bk.ebs, bk.data
+    total = data.numel()
     caps = [lib.zccl_gpu_max_stream_bytes(int(n), L, T) for n in sizes]
     idxb = [lib.zccl_gpu_index_bytes(int(n), L, T) for n in sizes]
     a16 = lambda v: (v + 255) // 256 * 256
@@ -496,6 +549,29 @@ def batched_bench(args, L, dev):
     batched()
     bc.check()
     bh.check()
+    # whole streams of 64 pairs spread over the size range, against the oracle
+    parity = None
+    step = max(1, npairs // 64)
+    sample = list(range(0, npairs, step))[:64]
+
+    def whole(k, r):
+        n = int(sizes[k])
+        sz = ctypes.c_size_t(0)
+        lib.zccl_gpu_stream_size(ctypes.byref(S[k][r].desc), n, L, T, ctypes.byref(sz), sp)
+        o = S[k][r].desc.bytes - sbytes.data_ptr()
+        return bytes(sbytes[o: o + sz.value].cpu().numpy())
+
+    if not args.no_parity:
+        from oracle import zoracle
+        port = zoracle.port()
+        ok_c = ok_h = True
+        for k in sample:
+            n = int(sizes[k])
+            a, b = xs[k][0].cpu().numpy(), xs[k][1].cpu().numpy()
+            ra, rb = port.compress(a, ebs[k], L, T), port.compress(b, ebs[k], L, T)
+            ok_c &= whole(k, 0) == ra and whole(k, 1) == rb
+            ok_h &= whole(k, 2) == port.homadd(ra, rb, n, ebs[k], L, T)
+        parity = {"pairs_checked": len(sample), "streams": bool(ok_c), "sums": bool(ok_h)}
     sum_b = [(S[k][2].desc.index, S[k][2].desc.bytes) for k in range(0, npairs, 97)]
     digest_b = [bytes(sbytes[d - sbytes.data_ptr(): d - sbytes.data_ptr() + 64].cpu().numpy())
                 for _, d in sum_b]
@@ -551,6 +627,8 @@ def batched_bench(args, L, dev):
         "autotuned_grid": {"compress": grid_c, "homadd": grid_h},
         "outputs_equal_sampled": same,
     }
+    if parity:
+        res["parity"] = parity
     del data, xs, sbytes, ibytes, ws, gp, gb
     torch.cuda.empty_cache()
     return res
@@ -748,12 +826,12 @@ def run_ours(args, rank, world, local_rank):
            "d2h_bytes_per_step": ca + 4 * n + cs,
            "api": "ZCCL_float_openmp_threadblock_arg / _decompress_ / _homomophic_add_ (host)"}
 
-    cpu = None
+    cpu, ref_out = None, None
     if rank == 0 and world == 1 and not args.no_cpu:
-        rate, secs = cpu_codec_rate(xh, yh, eb, L, T, reps=5)
+        rate, secs, ref_out = cpu_codec_rate(xh, yh, eb, L, T, reps=5)
         m = n // 16
         Z.set_omp_threads(1)
-        rate1, secs1 = cpu_codec_rate(xh[:m], yh[:m], eb, L, 1, reps=1)
+        rate1, secs1, _ = cpu_codec_rate(xh[:m], yh[:m], eb, L, 1, reps=1)
         Z.set_omp_threads(T)
         cpu = {"value": round(rate, 3), "unit": "GB/s", "cores": T, "kind": "port",
                "sample": f"whole field, best of 5 passes after one warm-up ({secs:.2f} s a pass) of "
@@ -761,6 +839,49 @@ def run_ours(args, rank, world, local_rank):
                "single_thread": {"value": round(rate1, 3), "unit": "GB/s", "cores": 1,
                                  "sample": f"first {m} elements, T=1, best of 1 after one warm-up "
                                            f"({secs1:.2f} s a pass)"}}
+
+    # byte-for-byte parity of the timed workload with the oracle: the device
+    # path's resident stream, sum and floats, and the host-buffer entry
+    # points' outputs
+    parity = {}
+    eb_sweep = {}
+    if rank == 0 and not args.no_parity:
+        if ref_out is None:
+            ref_out = oracle_outputs(xh, yh, eb, L, T)
+        parity[f"eb{args.eb_rel:g}"] = {
+            "stream": sa.tobytes() == ref_out["stream"],
+            "sum": ss.tobytes() == ref_out["sum"],
+            "floats": same_bits(xo.cpu().numpy(), ref_out["floats"]),
+            "e2e_stream": hs_a[:ca].tobytes() == ref_out["stream"],
+            "e2e_sum": hs_s[:cs].tobytes() == ref_out["sum"],
+            "e2e_floats": same_bits(hy, ref_out["floats"]),
+        }
+        del ref_out
+        # the same field at the other error bound of the sweep (1e-3 of range)
+        for rel in (1e-3, 1e-4):
+            if rel == args.eb_rel:
+                continue
+            eb2 = float(np.float32(rel * max(float(x.max() - x.min()), float(y.max() - y.min()))))
+            sa2, sb2, ss2 = codec.new_stream(), codec.new_stream(), codec.new_stream()
+            xo2 = torch.empty(n, dtype=torch.float32, device=dev)
+            codec.compress(y, eb2, out=sb2)
+            t_c = timed(lambda: codec.compress(x, eb2, out=sa2), 20, st)
+            t_d = timed(lambda: codec.decompress(sa2, eb2, out=xo2), 20, st)
+            t_h = timed(lambda: codec.homadd([sa2, sb2], out=ss2), 20, st)
+            codec.check()
+            c2a, c2b, c2s = sa2.size(), sb2.size(), ss2.size()
+            alg2 = {"compress": 4 * n + c2a, "decompress": c2a + 4 * n, "homadd": c2a + c2b + c2s}
+            ops = {}
+            for name, t_ms in zip(("compress", "decompress", "homadd"), (t_c, t_d, t_h)):
+                gbs = alg2[name] / (t_ms * 1e-3) / 1e9
+                ops[name] = {"ms": round(t_ms, 4), "uncompressed_GBps": round(4 * n / (t_ms * 1e-3) / 1e9, 1),
+                             "algorithmic_GBps": round(gbs, 1), "roofline_frac": round(gbs / peak, 4)}
+            r2 = oracle_outputs(xh, yh, eb2, L, T)
+            parity[f"eb{rel:g}"] = {"stream": sa2.tobytes() == r2["stream"], "sum": ss2.tobytes() == r2["sum"],
+                                    "floats": same_bits(xo2.cpu().numpy(), r2["floats"])}
+            eb_sweep[f"{rel:g}"] = {"eb": eb2, "per_op": ops,
+                                    "compression_ratio": {"A": round(4 * n / c2a, 3), "sum": round(4 * n / c2s, 3)}}
+            del sa2, sb2, ss2, xo2, r2
 
     extras = {}
     if rank == 0 and not args.no_extras:
@@ -783,8 +904,22 @@ def run_ours(args, rank, world, local_rank):
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * args.steps,
             "clocks": clk.summary(),
         }
+        if eb_sweep:
+            line["eb_sweep"] = eb_sweep
         line.update(extras)
+        red = extras.get("reduction", {}).get("parity")
+        if red:
+            parity["reduction_p8"] = red
+        bat = extras.get("batched", {}).get("parity")
+        if bat:
+            parity["batched"] = bat
+        if parity:
+            line["parity"] = parity
         print(json.dumps(line), flush=True)
+        bad = [f"{k}.{kk}" for k, v in parity.items() for kk, vv in v.items() if vv is False]
+        if bad:
+            sys.stderr.write(f"parity with the oracle FAILED: {', '.join(bad)}\n")
+            sys.exit(1)
 
 
 def main():

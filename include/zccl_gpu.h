@@ -108,7 +108,12 @@ typedef struct zccl_gpu_stream {
 size_t zccl_gpu_max_stream_bytes(size_t n, int L, int T);
 /* Bytes of the side index of one stream (about n/L + 12 per 8192 floats). */
 size_t zccl_gpu_index_bytes(size_t n, int L, int T);
-/* Bytes of device scratch one call needs (look-back state, error word). */
+/* Bytes of device scratch one call needs (look-back state, error word).
+ * Its first 8 bytes are two status words: zero them once when the
+ * workspace is allocated.  Every call leaves them alone (it zeroes only its
+ * own look-back state) and ORs the errors it detects into them, so the
+ * errors of every call on a workspace since the last zccl_gpu_check() are
+ * reported by that check, which then clears them. */
 size_t zccl_gpu_workspace_bytes(size_t n, int L, int T);
 
 /* Compress n device floats into out->bytes and fill out's index.
@@ -156,9 +161,11 @@ int zccl_gpu_homadd_cases(zccl_gpu_stream *out, zccl_gpu_stream *ins, int P, siz
  * calls on a device share the one array: two calls whose work overlaps in
  * time (different streams or host threads) race on it, so order them, for
  * example by issuing them on one stream.  The output, status and size are
- * those of zccl_gpu_compress.  When d_scratch is not NULL it receives the
- * array's address, which zccl_gpu_check() takes to read this call's device
- * status (before the next call on the device reuses the array). */
+ * those of zccl_gpu_compress.  When d_scratch is not NULL and the call
+ * returns ZCCL_GPU_OK it receives the array's address (else NULL), which
+ * zccl_gpu_check() takes to read the device status of the calls made since
+ * the last check.  The address is looked up once per device and kept, so
+ * the library does not support cudaDeviceReset() between calls. */
 int zccl_gpu_compress_noalloc(zccl_gpu_stream *out, const float *d_in, size_t n, float eb, int L,
                               int T, void *cuda_stream, void **d_scratch);
 
@@ -232,7 +239,9 @@ int zccl_gpu_szp3d_decompress(float *d_out, const unsigned char *d_in, size_t av
 int zccl_gpu_frame_size(const zccl_gpu_stream *s, void *d_frame, void *cuda_stream);
 
 /* Synchronize cuda_stream and turn the workspace's device error bits into a
- * status code (ZCCL_GPU_OK when none). */
+ * status code (ZCCL_GPU_OK when none), then clear them.  The bits are those
+ * of every call on the workspace since the previous check; a failed header
+ * walk also makes later calls on the workspace stop early until checked. */
 int zccl_gpu_check(void *d_ws, void *cuda_stream);
 
 /* -------------------------------------------------------------------
@@ -290,7 +299,8 @@ int zccl_gpu_batch_run(const zccl_gpu_batch *b, void *cuda_stream);
  * (running it several times) and keep the fastest in b->grid. */
 int zccl_gpu_batch_tune(zccl_gpu_batch *b, void *cuda_stream);
 
-/* Synchronize cuda_stream and return the batch's device status. */
+/* Synchronize cuda_stream and return the batch's device status (the errors
+ * of every run since the plan or the previous check), then clear it. */
 int zccl_gpu_batch_check(const zccl_gpu_batch *b, void *cuda_stream);
 
 /* Status of the last drop-in call made by this thread. */

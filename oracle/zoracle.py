@@ -31,9 +31,22 @@ _f32p = ctypes.POINTER(ctypes.c_float)
 _szp = ctypes.POINTER(ctypes.c_size_t)
 
 
+def reference_root() -> str | None:
+    """The reference checkout the oracle compiles from: $ZCCL_REFERENCE_ROOT,
+    else a checkout named ``reference`` beside this repository; None when
+    neither holds the codec sources."""
+    cands = [os.environ.get("ZCCL_REFERENCE_ROOT"),
+             os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")]
+    for c in cands:
+        if c and os.path.isfile(os.path.join(c, "ZCCL", "src", "ZCCL_float.c")):
+            return os.path.abspath(c)
+    return None
+
+
 def build(ref: bool = True) -> None:
     """Compile the port (and the reference library when its sources exist)."""
-    targets = ["port"] + (["ref"] if ref else [])
+    root = reference_root() if ref else None
+    targets = ["port"] + (["ref", f"REF_ROOT={root}"] if root else [])
     subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
 
 

@@ -343,3 +343,22 @@ def test_errors_are_reported_not_faulted(torch):
     with pytest.raises(Z.ZcclError) as e:
         codec.check()
     assert e.value.status == -8
+
+
+def test_errors_stay_until_checked(torch):
+    """The device status words keep every call's errors until a check reads
+    and clears them: an early failed call is still reported after later
+    calls on the same workspace succeeded, and the check after that is
+    clean again."""
+    n, L, T = 20000, 32, 2
+    codec = Z.Codec(n, L, T)
+    x = dev(torch, np.linspace(-1, 1, n).astype(np.float32))
+    codec.compress(x, 1e-3, out=codec.new_stream(capacity=64))  # ECAPACITY
+    good = codec.compress(x, 1e-3)
+    codec.decompress(good, 1e-3)
+    codec.homadd([good, good])
+    with pytest.raises(Z.ZcclError) as e:
+        codec.check()
+    assert e.value.status == -8
+    codec.compress(x, 1e-3)
+    codec.check()

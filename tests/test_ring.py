@@ -122,3 +122,28 @@ def test_one_shot_reductions_match_oracle(torch, port):
         total += port.decompress(h, n, eb, L, T)
     assert doc.tobytes() == port.compress(total, eb, L, T)
     codec.check()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant", ["homomorphic", "doc"])
+def test_ring_raises_on_an_early_failed_step(torch, variant):
+    """An error in the first step (a compressed chunk written into a stream
+    too small for it) must surface when the ring returns, although many
+    later calls run on the same codec before it checks."""
+    import zccl_gb300 as Z
+    from zccl_gb300.ring import RingAllreduce
+    count, P, T, L = 24000, 4, 1, 32
+    xs = rank_data(count, P, seed=4)
+    eb = float(np.float32(1e-4 * (max(x.max() for x in xs) - min(x.min() for x in xs))))
+    ring = RingAllreduce(count, P, L, T)
+    cd = ring.codec(0)
+    orig, calls = cd.new_stream, [0]
+
+    def first_too_small(capacity=None):
+        calls[0] += 1
+        return orig(64) if calls[0] == 1 else orig(capacity)
+
+    cd.new_stream = first_too_small
+    with pytest.raises(Z.ZcclError):
+        getattr(ring, variant)([torch.from_numpy(x).cuda() for x in xs], eb)
+    assert calls[0] > 1

@@ -107,6 +107,15 @@ struct WalkLayout {
 
 size_t ws_clear_bytes(const ZGeom &g) { return 16 + 8 * g.ntiles; }
 
+/* Zero what a call needs zeroed at launch: the tile ticket and the
+ * look-back words.  The two status words in front of them are left alone,
+ * so errors of earlier calls on the workspace stay visible until
+ * zccl_gpu_check() reads and clears them. */
+cudaError_t ws_clear(void *ws, const ZGeom &g, cudaStream_t st)
+{
+    return cudaMemsetAsync((uint8_t *)ws + 8, 0, ws_clear_bytes(g) - 8, st);
+}
+
 WalkLayout walk_layout(const ZGeom &g)
 {
     WalkLayout l;
@@ -256,7 +265,7 @@ static int compress_fmt(zccl_gpu_stream *out, const float *d_in, size_t n, float
     a.job.status = a.w.status;
     a.wt = width_table();
     a.sm = compress_smem(g);
-    if (cudaMemsetAsync(d_ws, 0, ws_clear_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    if (ws_clear(d_ws, g, st) != cudaSuccess) return ZCCL_GPU_ECUDA;
     int rc = cuda_status(launch_compress(a, st));
     if (rc == ZCCL_GPU_OK) {
         out->indexed = 1;
@@ -283,7 +292,7 @@ extern "C" int zccl_gpu_build_index(zccl_gpu_stream *s, size_t n, int L, int T, 
     ZGeom g;
     if (make_geom(n, L, T, &g) || !valid_stream(s) || !d_ws) return ZCCL_GPU_EINVAL;
     cudaStream_t st = (cudaStream_t)cuda_stream;
-    if (cudaMemsetAsync(d_ws, 0, ws_clear_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    if (ws_clear(d_ws, g, st) != cudaSuccess) return ZCCL_GPU_ECUDA;
     return walk_stream(s, g, d_ws, st);
 }
 
@@ -295,7 +304,7 @@ static int decompress_fmt(float *d_out, zccl_gpu_stream *in, size_t n, float eb,
     if (make_geom(n, L, T, &g) || !valid_stream(in) || !d_out || !d_ws) return ZCCL_GPU_EINVAL;
     g.fmt = fmt;
     cudaStream_t st = (cudaStream_t)cuda_stream;
-    if (cudaMemsetAsync(d_ws, 0, ws_clear_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    if (ws_clear(d_ws, g, st) != cudaSuccess) return ZCCL_GPU_ECUDA;
     ZWork w = bind_ws(d_ws);
     if (!in->indexed) {
         int rc = walk_stream(in, g, d_ws, st);
@@ -338,7 +347,7 @@ extern "C" int zccl_gpu_homadd_cases(zccl_gpu_stream *out, zccl_gpu_stream *ins,
     for (int p = 0; p < P; p++)
         if (!valid_stream(&ins[p]) || ins[p].bytes == out->bytes) return ZCCL_GPU_EINVAL;
     cudaStream_t st = (cudaStream_t)cuda_stream;
-    if (cudaMemsetAsync(d_ws, 0, ws_clear_bytes(g), st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    if (ws_clear(d_ws, g, st) != cudaSuccess) return ZCCL_GPU_ECUDA;
     ZWork w = bind_ws(d_ws);
     HomAddArgs a;
     memset(&a, 0, sizeof(a));
@@ -411,6 +420,8 @@ extern "C" int zccl_gpu_check(void *d_ws, void *cuda_stream)
     uint32_t bits[2] = {0, 0};
     if (cudaMemcpyAsync(bits, d_ws, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess)
         return ZCCL_GPU_ECUDA;
+    /* read once: the next call starts with clean status words */
+    if (cudaMemsetAsync(d_ws, 0, 8, st) != cudaSuccess) return ZCCL_GPU_ECUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return ZCCL_GPU_ECUDA;
     /* a failed walk leaves nothing for the codec kernels to report */
     return status_of_bits(bits[1] ? bits[1] : bits[0]);
@@ -545,7 +556,8 @@ extern "C" int zccl_gpu_batch_plan(zccl_gpu_batch *b, int kind, const zccl_gpu_b
     cudaStream_t st = (cudaStream_t)cuda_stream;
     const void *jsrc = kind == ZCCL_GPU_BATCH_COMPRESS ? (const void *)cj.data() : (const void *)hj.data();
     const size_t jbytes = njobs * (kind == ZCCL_GPU_BATCH_COMPRESS ? sizeof(CompressJob) : sizeof(HomAddJob));
-    if (cudaMemcpyAsync(base + lay.jobs, jsrc, jbytes, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+    if (cudaMemsetAsync(base, 0, 8, st) != cudaSuccess || /* clean status words */
+        cudaMemcpyAsync(base + lay.jobs, jsrc, jbytes, cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemcpyAsync(base + lay.map, map.data(), 2 * ntiles, cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemcpyAsync(base + lay.tile0, tile0.data(), 8 * njobs, cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
@@ -577,7 +589,8 @@ extern "C" int zccl_gpu_batch_run(const zccl_gpu_batch *b, void *cuda_stream)
     if (!b || !b->d_mem || !b->ntiles) return ZCCL_GPU_EINVAL;
     cudaStream_t st = (cudaStream_t)cuda_stream;
     uint8_t *base = static_cast<uint8_t *>(b->d_mem);
-    if (cudaMemsetAsync(base, 0, b->clear_bytes, st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    /* the status words stay until zccl_gpu_batch_check() reads them */
+    if (cudaMemsetAsync(base + 8, 0, b->clear_bytes - 8, st) != cudaSuccess) return ZCCL_GPU_ECUDA;
     ZBatch bt;
     bt.jobs = base + b->jobs_off;
     bt.tile_job = reinterpret_cast<const uint16_t *>(base + b->map_off);
@@ -682,6 +695,12 @@ struct DevBuf {
         if (cudaMalloc(&p, want) != cudaSuccess) {
             cudaGetLastError();
             return ZCCL_GPU_ENOMEM;
+        }
+        /* a workspace starts with clean status words */
+        if (cudaMemset(p, 0, 16) != cudaSuccess) {
+            cudaFree(p);
+            p = nullptr;
+            return ZCCL_GPU_ECUDA;
         }
         n = want;
         return ZCCL_GPU_OK;
@@ -910,7 +929,7 @@ int dropin_homadd(unsigned char *final_cmp, size_t *final_size, size_t n, float 
         /* the first input's index walk runs while the second input is
          * copied on the other stream; then the second's walk, a check of
          * both, and the add of the indexed inputs */
-        if (cudaMemsetAsync(c->ws.p, 0, ws_clear_bytes(g), c->st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+        if (ws_clear(c->ws.p, g, c->st) != cudaSuccess) return ZCCL_GPU_ECUDA;
         if (int rc = stage_stream(c, 0, cmp1, g, &in[0], pass > 0, &cap1)) return rc;
         if (int rc = walk_stream(&in[0], g, c->ws.p, c->st)) return rc;
         if (int rc = stage_stream(c, 1, cmp2, g, &in[1], pass > 0, &cap2, c->st2)) return rc;

@@ -8,10 +8,14 @@
  * Here they live in g_scratch, a file-scope __device__ array that exists
  * once per device from the moment the library's device code is loaded.
  * Its address is looked up with cudaGetSymbolAddress the first time a call
- * runs with that device current, kept per device, and then handed to the
- * ordinary compressor as its workspace, which clears the part that must
- * start at zero on the caller's stream and launches the same kernel.  No
- * call here allocates: no cudaMalloc, no cudaFree, no allocating library.
+ * runs with that device current, kept per device (so a cudaDeviceReset()
+ * between calls is not supported: the module, and the array with it, may
+ * move), and then handed to the ordinary compressor as its workspace, which
+ * clears the part that must start at zero on the caller's stream and
+ * launches the same kernel.  The array's two status words start at zero
+ * with the module and collect the errors of every call until
+ * zccl_gpu_check() reads and clears them.  No call here allocates: no
+ * cudaMalloc, no cudaFree, no allocating library.
  *
  * One array per device is shared by every call on that device, so two calls
  * whose work overlaps in time on that device (two streams, or two host
@@ -66,6 +70,7 @@ extern "C" int zccl_gpu_compress_noalloc(zccl_gpu_stream *out, const float *d_in
     if (16ull + 8ull * g.ntiles > (uint64_t)ZCCL_GPU_NOALLOC_SCRATCH_BYTES) return ZCCL_GPU_ESCRATCH;
     void *scratch = nullptr;
     if (int rc = scratch_address(&scratch)) return rc;
-    if (d_scratch) *d_scratch = scratch;
-    return zccl_gpu_compress(out, d_in, n, eb, L, T, scratch, cuda_stream);
+    const int rc = zccl_gpu_compress(out, d_in, n, eb, L, T, scratch, cuda_stream);
+    if (rc == ZCCL_GPU_OK && d_scratch) *d_scratch = scratch;
+    return rc;
 }

@@ -893,7 +893,7 @@ cudaError_t sz3_compress(uint8_t *out, uint64_t cap, const float *x, uint64_t d1
 {
     const Sz3Dims g = sz3_dims(d1, d2, d3, bs);
     const Sz3Ws w = sz3_bind(ws, g);
-    cudaError_t e = cudaMemsetAsync(w.err, 0, 16, st);
+    cudaError_t e = cudaMemsetAsync(w.err + 2, 0, 8, st); /* the ticket; status words stay until checked */
     if (e != cudaSuccess) return e;
     /* the rate table is part of the stream: cap must hold it */
     if (cap < g.nblocks) return cudaErrorInvalidValue;
@@ -932,7 +932,7 @@ cudaError_t sz3_decompress(float *y, const uint8_t *in, uint64_t avail, uint64_t
 {
     const Sz3Dims g = sz3_dims(d1, d2, d3, bs);
     const Sz3Ws w = sz3_bind(ws, g);
-    cudaError_t e = cudaMemsetAsync(w.err, 0, 16, st);
+    cudaError_t e = cudaMemsetAsync(w.err + 2, 0, 8, st); /* the ticket; status words stay until checked */
     if (e != cudaSuccess) return e;
     k_sz3_sizes<<<grid_for(g.nblocks, 256), 256, 0, st>>>(in, avail, g, w.sizes, w.err);
     if ((e = sz3_scan(g, w, st)) != cudaSuccess) return e;

@@ -70,6 +70,12 @@ class RingAllreduce:
     def _chunk(self, x, c):
         return x[self.displs[c]: self.displs[c] + self.cnts[c]]
 
+    def _check(self):
+        """Raise if any call on any chunk's codec failed since the last check
+        (the device status words keep every call's errors until read)."""
+        for cd in self._codecs.values():
+            cd.check()
+
     def _allgather_decompress(self, reduced, eb, per_rank_outputs):
         """Every rank decompresses all P reduced chunks into its result."""
         import torch
@@ -79,6 +85,7 @@ class RingAllreduce:
             for c in range(self.P):
                 self.codec(c).decompress(reduced[c], eb, out=self._chunk(y, c))
             outs.append(y)
+        self._check()
         return outs if per_rank_outputs else outs[0]
 
     def homomorphic(self, xs, eb: float, per_rank_outputs: bool = False):
@@ -95,8 +102,7 @@ class RingAllreduce:
                 src, c = (r - 1) % P, (r - 2 - i) % P
                 S[r][c] = self.codec(c).homadd([S[src][c], S[r][c]])
         self.reduced = [S[c][c] for c in range(P)]
-        for cd in self._codecs.values():
-            cd.check()
+        self._check()
         return self._allgather_decompress(self.reduced, eb, per_rank_outputs)
 
     def doc(self, xs, eb: float, per_rank_outputs: bool = False):
@@ -113,8 +119,7 @@ class RingAllreduce:
                 self._chunk(acc[r], c).add_(self.codec(c).decompress(msgs[src], eb))
         # the allgather compresses each rank's reduced chunk (ZCCL_ring.c:863-869)
         self.reduced = [self.codec(c).compress(self._chunk(acc[c], c), eb) for c in range(P)]
-        for cd in self._codecs.values():
-            cd.check()
+        self._check()
         return self._allgather_decompress(self.reduced, eb, per_rank_outputs)
 
 
