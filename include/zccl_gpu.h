@@ -80,6 +80,65 @@ void ZCCL_float_homomophic_add_single_thread(unsigned char *final_cmpBytes, size
                                              size_t nbEle, float absErrBound, int blockSize,
                                              unsigned char *cmpBytes, unsigned char *cmpBytes2);
 
+/* Replaces ZCCL_float_openmp_threadblock (ZCCL/include/ZCCL_float.h:27-29,
+ * ZCCL/src/ZCCL_float.c:192-499): compresses into a buffer it mallocs,
+ * which the caller frees with free(); ASSIGNS *outSize; NULL on failure.
+ * The stream is ZCCL_float_openmp_threadblock_arg's.  Where N % T != 0 the
+ * reference packs the remainder segment's tail block with the regular
+ * segments' tail count (ZCCL_float.c:452,456) -- a stream its decompressor
+ * cannot read back whenever the two counts differ; here that block has its
+ * own count, so both variants write the same bytes. */
+unsigned char *ZCCL_float_openmp_threadblock(float *oriData, size_t *outSize, float absErrBound, size_t nbEle,
+                                             int blockSize);
+
+/* Replaces ZCCL_float_decompress_openmp_threadblock
+ * (ZCCL/include/ZCCLd_float.h:19, ZCCL/src/ZCCLd_float.c:22-245):
+ * *newData = malloc(4 * nbEle) (the caller frees it, also after a failed
+ * call), then decompressed like the _arg variant. */
+void ZCCL_float_decompress_openmp_threadblock(float **newData, size_t nbEle, float absErrBound, int blockSize,
+                                              unsigned char *cmpBytes);
+
+/* Replaces ZCCL_float_single_thread_arg_record
+ * (ZCCL/include/ZCCL_float.h:36-37, ZCCL/src/ZCCL_float.c:990-1209): the
+ * T = 1 stream, and the value the reference returns -- its own count of the
+ * bytes its scalar code reads and writes while producing that stream (12
+ * per element, each block's bytes plus 8 per element of a non-zero-width
+ * block, the chunk copied out twice, 76 of bookkeeping).  The count is a
+ * function of the stream, computed from it here; it does not measure the
+ * GPU's memory traffic.  0 on failure. */
+size_t ZCCL_float_single_thread_arg_record(unsigned char *outputBytes, float *oriData, size_t *outSize,
+                                           float absErrBound, size_t nbEle, int blockSize);
+
+/* Replaces ZCCL_float_decompress_single_thread_arg_record
+ * (ZCCL/include/ZCCLd_float.h:25, ZCCL/src/ZCCLd_float.c:376-536): T = 1
+ * decompression, returning the reference's count for it (each block's
+ * bytes, 8 per element of a zero-width block, 20 per element of any other,
+ * 24 of bookkeeping), computed from the stream.  0 on failure. */
+size_t ZCCL_float_decompress_single_thread_arg_record(float *newData, size_t nbEle, float absErrBound,
+                                                      int blockSize, unsigned char *cmpBytes);
+
+/* Replaces ZCCL_float_single_thread_arg_split_record
+ * (ZCCL/include/ZCCL_float.h:45-52, ZCCL/src/ZCCL_float.c:1530-1705), which
+ * the split allreduce calls once per chunk (ZCCL/src/ZCCL_ring.c:1496,1510):
+ * the T = 1 stream into outputBytes, *outSize assigned, and the same size
+ * stored as the size_t at index chunk_iter of chunk_arr (host or device
+ * memory, any alignment). */
+void ZCCL_float_single_thread_arg_split_record(unsigned char *outputBytes, float *oriData, size_t *outSize,
+                                               float absErrBound, size_t nbEle, int blockSize,
+                                               unsigned char *chunk_arr, size_t chunk_iter);
+
+/* Replaces ZCCL_float_homomophic_add_openmp_threadblock_record
+ * (ZCCL/include/ZCCLd_float.h:31, ZCCL/src/ZCCLd_float.c:2067-2800): the
+ * homomorphic add, and the reference's four branch counters over every
+ * block pair ADDED to the ints: counter_1 both widths 0, counter_2 only the
+ * first 0, counter_3 only the second 0, counter_4 neither (the device
+ * counters of zccl_gpu_homadd_cases). */
+void ZCCL_float_homomophic_add_openmp_threadblock_record(unsigned char *final_cmpBytes, size_t *final_cmpSize,
+                                                         size_t nbEle, float absErrBound, int blockSize,
+                                                         unsigned char *cmpBytes, unsigned char *cmpBytes2,
+                                                         int *total_counter_1, int *total_counter_2,
+                                                         int *total_counter_3, int *total_counter_4);
+
 /* ===================================================================
  * 2. Device API
  * =================================================================== */

@@ -541,3 +541,84 @@ void port_szp3d_decompress(float *y, const unsigned char *cmp, size_t d1, size_t
     free(q);
 }
 #undef ZP3
+
+/* ======================================================================
+ * The counts the reference's _record variants return.
+ * ====================================================================== */
+
+/* Walks the blocks of a segment of len elements starting at p (after its
+ * raw head): adds the bytes of the blocks to *bytes and the elements of the
+ * blocks of non-zero width to *nz; returns the byte after the segment. */
+static const unsigned char *walk_segment(const unsigned char *p, size_t len, size_t L, size_t *bytes, size_t *nz)
+{
+    if (len == 0) return p;
+    p += 4;
+    for (size_t left = len - 1; left > 0;) {
+        const size_t m = left < L ? left : L;
+        const int b = p[0];
+        const size_t s = block_bytes(b, m);
+        *bytes += s;
+        if (b) *nz += m;
+        p += s;
+        left -= m;
+    }
+    return p;
+}
+
+void port_record_counts(const unsigned char *cmp, size_t n, int L, size_t *compress_count,
+                        size_t *decompress_count)
+{
+    size_t bytes = 0, nz = 0;
+    walk_segment(cmp + 8, n, (size_t)L, &bytes, &nz);
+    const size_t C = 8 + 4 + bytes;
+    /* ZCCL_float_single_thread_arg_record (ZCCL/src/ZCCL_float.c:990-1209):
+     * 20 bytes around the head; 12 per element of every block (the float
+     * read and two 4-byte stores whatever the delta's sign); per block its
+     * bytes, plus 8 per element (the sign and magnitude arrays read by the
+     * packers) when its width is not 0; 56 for the offset table and the
+     * copies' bookkeeping; the chunk copied out, read and written. */
+    *compress_count = 20 + 12 * (n - 1) + bytes + 8 * nz + 56 + 2 * (C - 8);
+    /* ZCCL_float_decompress_single_thread_arg_record
+     * (ZCCL/src/ZCCLd_float.c:376-536): 24 bytes around the head; per block
+     * its bytes, plus 8 per element for a constant block (a float read and
+     * written) or 20 per element otherwise (the unpacked sign and magnitude
+     * arrays, the delta read, the float written and read). */
+    *decompress_count = 24 + bytes + 8 * (n - 1) + 12 * nz;
+}
+
+/* Classifies the block pairs of one segment of two streams. */
+static void cases_segment(const unsigned char **pa, const unsigned char **pb, size_t len, size_t L,
+                          unsigned long long c[4])
+{
+    if (len == 0) return;
+    const unsigned char *a = *pa + 4, *b = *pb + 4;
+    for (size_t left = len - 1; left > 0;) {
+        const size_t m = left < L ? left : L;
+        const int wa = a[0], wb = b[0];
+        c[!wa && !wb ? 0 : !wa ? 1 : !wb ? 2 : 3]++;
+        a += block_bytes(wa, m);
+        b += block_bytes(wb, m);
+        left -= m;
+    }
+    *pa = a;
+    *pb = b;
+}
+
+void port_homadd_cases(const unsigned char *cmp1, const unsigned char *cmp2, size_t nbEle, int blockSize, int T,
+                       unsigned long long counts[4])
+{
+    /* ZCCL_float_homomophic_add_openmp_threadblock_record
+     * (ZCCL/src/ZCCLd_float.c:2067-2800): counter_1 both widths 0,
+     * counter_2 only the first 0, counter_3 only the second 0, counter_4
+     * neither, over every block pair of every segment. */
+    const size_t L = (size_t)blockSize, tbs = nbEle / (size_t)T, rem = nbEle % (size_t)T;
+    counts[0] = counts[1] = counts[2] = counts[3] = 0;
+    for (int t = 0; t < T; t++) {
+        uint64_t o1, o2;
+        memcpy(&o1, cmp1 + 8 * (size_t)t, 8);
+        memcpy(&o2, cmp2 + 8 * (size_t)t, 8);
+        const unsigned char *a = cmp1 + 8 * (size_t)T + o1, *b = cmp2 + 8 * (size_t)T + o2;
+        cases_segment(&a, &b, tbs, L, counts);
+        if (t == T - 1 && rem) cases_segment(&a, &b, rem, L, counts);
+    }
+}

@@ -58,6 +58,22 @@ void port_szp3d_compress(const float *x, unsigned char *out, size_t d1, size_t d
 void port_szp3d_decompress(float *y, const unsigned char *cmp, size_t d1, size_t d2, size_t d3, int bs,
                            double eb);
 
+/* The counts of the reference's _record variants, from a stream.  For a
+ * T = 1 stream of nbEle floats: the memory-access counts returned by
+ * ZCCL_float_single_thread_arg_record (ZCCL/src/ZCCL_float.c:990-1209)
+ * when it wrote the stream, and by
+ * ZCCL_float_decompress_single_thread_arg_record
+ * (ZCCL/src/ZCCLd_float.c:376-536) when it reads it. */
+void port_record_counts(const unsigned char *cmp, size_t nbEle, int blockSize, size_t *compress_count,
+                        size_t *decompress_count);
+
+/* The four branch counters that
+ * ZCCL_float_homomophic_add_openmp_threadblock_record
+ * (ZCCL/src/ZCCLd_float.c:2067-2800) adds up for two streams written with T
+ * threads: both widths 0, first 0, second 0, neither. */
+void port_homadd_cases(const unsigned char *cmp1, const unsigned char *cmp2, size_t nbEle, int blockSize, int T,
+                       unsigned long long counts[4]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -200,6 +200,66 @@ class _Codec:
                  ctypes.c_double(eb))
         return y
 
+    # ---- the _record variants' counts ------------------------------------
+    def record_counts(self, stream: bytes, n: int, L: int):
+        """(compress count, decompress count) the reference's T = 1 _record
+        variants return for this stream (port only)."""
+        c, d = ctypes.c_size_t(0), ctypes.c_size_t(0)
+        f = self.lib.port_record_counts
+        f.argtypes = [_u8p, ctypes.c_size_t, ctypes.c_int, _szp, _szp]
+        f.restype = None
+        buf = np.frombuffer(stream, np.uint8).copy()
+        f(_ptr(buf, _u8p), n, L, ctypes.byref(c), ctypes.byref(d))
+        return c.value, d.value
+
+    def homadd_cases(self, s1: bytes, s2: bytes, n: int, L: int, T: int):
+        """The four branch counters of the two-input add (port only)."""
+        out = (ctypes.c_ulonglong * 4)()
+        f = self.lib.port_homadd_cases
+        f.argtypes = [_u8p, _u8p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong * 4]
+        f.restype = None
+        a, b = np.frombuffer(s1, np.uint8).copy(), np.frombuffer(s2, np.uint8).copy()
+        f(_ptr(a, _u8p), _ptr(b, _u8p), n, L, T, out)
+        return list(out)
+
+    def ref_record(self, x: np.ndarray, eb: float, L: int):
+        """The reference library's ZCCL_float_single_thread_arg_record and
+        ZCCL_float_decompress_single_thread_arg_record on x: (stream,
+        compress count, decompressed floats, decompress count)."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        n = x.size
+        out = np.zeros(worst_stream_bytes(n, L, 1), dtype=np.uint8)
+        size = ctypes.c_size_t(0)
+        fc = self.lib.ZCCL_float_single_thread_arg_record
+        fc.argtypes = [_u8p, _f32p, _szp, ctypes.c_float, ctypes.c_size_t, ctypes.c_int]
+        fc.restype = ctypes.c_size_t
+        cc = fc(_ptr(out, _u8p), _ptr(x, _f32p), ctypes.byref(size), ctypes.c_float(eb), n, L)
+        stream = out[: size.value].tobytes()
+        buf = np.concatenate([out[: size.value], np.zeros(16, np.uint8)])
+        y = np.zeros(n, np.float32)
+        fd = self.lib.ZCCL_float_decompress_single_thread_arg_record
+        fd.argtypes = [_f32p, ctypes.c_size_t, ctypes.c_float, ctypes.c_int, _u8p]
+        fd.restype = ctypes.c_size_t
+        dc = fd(_ptr(y, _f32p), n, ctypes.c_float(eb), L, _ptr(buf, _u8p))
+        return stream, cc, y, dc
+
+    def ref_homadd_record(self, s1: bytes, s2: bytes, n: int, eb: float, L: int, T: int):
+        """The reference's ZCCL_float_homomophic_add_openmp_threadblock_record
+        with T threads: (sum stream, [counter_1 .. counter_4])."""
+        a = np.concatenate([np.frombuffer(s1, np.uint8), np.zeros(16, np.uint8)])
+        b = np.concatenate([np.frombuffer(s2, np.uint8), np.zeros(16, np.uint8)])
+        out = np.zeros(worst_stream_bytes(n, L, T), dtype=np.uint8)
+        size = ctypes.c_size_t(0)
+        cnt = [ctypes.c_int(0) for _ in range(4)]
+        f = self.lib.ZCCL_float_homomophic_add_openmp_threadblock_record
+        f.argtypes = [_u8p, _szp, ctypes.c_size_t, ctypes.c_float, ctypes.c_int, _u8p, _u8p] + \
+            [ctypes.POINTER(ctypes.c_int)] * 4
+        f.restype = None
+        self._set_threads(T)
+        f(_ptr(out, _u8p), ctypes.byref(size), n, ctypes.c_float(eb), L, _ptr(a, _u8p), _ptr(b, _u8p),
+          *[ctypes.byref(c) for c in cnt])
+        return out[: size.value].tobytes(), [c.value for c in cnt]
+
     def homadd_fold(self, streams, n: int, eb: float, L: int, T: int) -> bytes:
         """P-way sum folded pairwise the way the ring's reduce-scatter does it
         (acc = add(received, acc), ZCCL/src/ZCCL_ring_ho.c:281-287)."""

@@ -362,3 +362,35 @@ def test_errors_stay_until_checked(torch):
     assert e.value.status == -8
     codec.compress(x, 1e-3)
     codec.check()
+
+
+def test_record_and_split_variants_with_device_pointers(port, torch):
+    """The T = 1 _record variants and the split variant on device memory:
+    the oracle's stream and floats, the reference's counts (restated by the
+    oracle), and the size slot written into a device frame table."""
+    rng = np.random.default_rng(31)
+    n, L = 200003, 32
+    x = np.cumsum(rng.normal(0, 0.02, n)).astype(np.float32)
+    x[5000:60000] = np.float32(1.5)
+    eb = float(np.float32(1e-4 * float(x.max() - x.min())))
+    s1 = port.compress(x, eb, L, 1)
+    cc, dc = port.record_counts(s1, n, L)
+    xd = dev(torch, x)
+    out = torch.zeros(len(s1) + 4096, dtype=torch.uint8, device="cuda")
+    size, count = Z.ZCCL_float_single_thread_arg_record(out, xd, eb, n, L)
+    assert out[:size].cpu().numpy().tobytes() == s1 and count == cc
+    y = torch.zeros(n, dtype=torch.float32, device="cuda")
+    assert Z.ZCCL_float_decompress_single_thread_arg_record(y, n, eb, L, out) == dc
+    assert np.array_equal(y.cpu().numpy(), port.decompress(s1, n, eb, L, 1))
+    frame = torch.zeros(len(s1) + 4096, dtype=torch.uint8, device="cuda")
+    size = Z.ZCCL_float_single_thread_arg_split_record(frame[24:], xd, eb, n, L, frame, 2)
+    assert size == len(s1)
+    assert frame[24: 24 + size].cpu().numpy().tobytes() == s1
+    assert int(np.frombuffer(frame[16:24].cpu().numpy().tobytes(), "<u8")[0]) == len(s1)
+    Z.set_omp_threads(3)
+    assert Z.ZCCL_float_openmp_threadblock(x, eb, n, L) == port.compress(x, eb, L, 3)
+    sx = port.compress(x, eb, L, 3)
+    host = np.zeros(4 * n + 4096, np.uint8)  # the 4*nbEle bytes a reference caller gives a stream
+    host[: len(sx)] = np.frombuffer(sx, np.uint8)
+    assert np.array_equal(Z.ZCCL_float_decompress_openmp_threadblock(n, eb, L, host),
+                          port.decompress(sx, n, eb, L, 3))

@@ -34,6 +34,9 @@ EXPORTS = [
     "ZCCL_float_openmp_threadblock_arg", "ZCCL_float_single_thread_arg",
     "ZCCL_float_decompress_openmp_threadblock_arg", "ZCCL_float_decompress_single_thread_arg",
     "ZCCL_float_homomophic_add_openmp_threadblock", "ZCCL_float_homomophic_add_single_thread",
+    "ZCCL_float_openmp_threadblock", "ZCCL_float_decompress_openmp_threadblock",
+    "ZCCL_float_single_thread_arg_record", "ZCCL_float_decompress_single_thread_arg_record",
+    "ZCCL_float_single_thread_arg_split_record", "ZCCL_float_homomophic_add_openmp_threadblock_record",
     "zccl_gpu_max_stream_bytes", "zccl_gpu_index_bytes", "zccl_gpu_workspace_bytes",
     "zccl_gpu_compress", "zccl_gpu_decompress", "zccl_gpu_homadd", "zccl_gpu_homadd_cases",
     "zccl_gpu_build_index", "zccl_gpu_stream_size", "zccl_gpu_frame_size", "zccl_gpu_check", "zccl_gpu_last_status",
@@ -97,6 +100,12 @@ def lib() -> ctypes.CDLL:
         "ZCCL_float_decompress_single_thread_arg": (None, [vp, sz, f, i, vp]),
         "ZCCL_float_homomophic_add_openmp_threadblock": (None, [vp, vp, sz, f, i, vp, vp]),
         "ZCCL_float_homomophic_add_single_thread": (None, [vp, vp, sz, f, i, vp, vp]),
+        "ZCCL_float_openmp_threadblock": (vp, [vp, vp, f, sz, i]),
+        "ZCCL_float_decompress_openmp_threadblock": (None, [vp, sz, f, i, vp]),
+        "ZCCL_float_single_thread_arg_record": (sz, [vp, vp, vp, f, sz, i]),
+        "ZCCL_float_decompress_single_thread_arg_record": (sz, [vp, sz, f, i, vp]),
+        "ZCCL_float_single_thread_arg_split_record": (None, [vp, vp, vp, f, sz, i, vp, sz]),
+        "ZCCL_float_homomophic_add_openmp_threadblock_record": (None, [vp, vp, sz, f, i, vp, vp, vp, vp, vp, vp]),
         "zccl_gpu_max_stream_bytes": (sz, [sz, i, i]),
         "zccl_gpu_index_bytes": (sz, [sz, i, i]),
         "zccl_gpu_workspace_bytes": (sz, [sz, i, i]),
@@ -241,6 +250,76 @@ def ZCCL_float_homomophic_add_single_thread(final_cmpBytes, final_cmpSize, nbEle
                                                   _ptr(cmpBytes2))
     _check(lib().zccl_gpu_last_status(), "ZCCL_float_homomophic_add_single_thread")
     return s.value
+
+
+def _libc():
+    return ctypes.CDLL(None)
+
+
+def ZCCL_float_openmp_threadblock(oriData, absErrBound, nbEle, blockSize) -> bytes:
+    """ZCCL/src/ZCCL_float.c:192: compresses into a buffer the library
+    mallocs; returns the stream's bytes (the buffer is freed here)."""
+    s = ctypes.c_size_t(0)
+    p = lib().ZCCL_float_openmp_threadblock(_ptr(oriData), ctypes.byref(s), absErrBound, nbEle, blockSize)
+    _check(lib().zccl_gpu_last_status(), "ZCCL_float_openmp_threadblock")
+    try:
+        return ctypes.string_at(p, s.value)
+    finally:
+        _libc().free(ctypes.c_void_p(p))
+
+
+def ZCCL_float_decompress_openmp_threadblock(nbEle, absErrBound, blockSize, cmpBytes) -> np.ndarray:
+    """ZCCL/src/ZCCLd_float.c:22: decompresses into a buffer the library
+    mallocs; returns a copy of the floats (the buffer is freed here)."""
+    out = ctypes.c_void_p(0)
+    lib().ZCCL_float_decompress_openmp_threadblock(ctypes.byref(out), nbEle, absErrBound, blockSize,
+                                                   _ptr(cmpBytes))
+    try:
+        _check(lib().zccl_gpu_last_status(), "ZCCL_float_decompress_openmp_threadblock")
+        return np.ctypeslib.as_array(ctypes.cast(out, ctypes.POINTER(ctypes.c_float)), (nbEle,)).copy()
+    finally:
+        _libc().free(out)
+
+
+def ZCCL_float_single_thread_arg_record(outputBytes, oriData, absErrBound, nbEle, blockSize):
+    """ZCCL/src/ZCCL_float.c:990; returns (size, the reference's memory-access count)."""
+    s = ctypes.c_size_t(0)
+    cnt = lib().ZCCL_float_single_thread_arg_record(_ptr(outputBytes), _ptr(oriData), ctypes.byref(s),
+                                                    absErrBound, nbEle, blockSize)
+    _check(lib().zccl_gpu_last_status(), "ZCCL_float_single_thread_arg_record")
+    return s.value, cnt
+
+
+def ZCCL_float_decompress_single_thread_arg_record(newData, nbEle, absErrBound, blockSize, cmpBytes) -> int:
+    """ZCCL/src/ZCCLd_float.c:376; returns the reference's memory-access count."""
+    cnt = lib().ZCCL_float_decompress_single_thread_arg_record(_ptr(newData), nbEle, absErrBound, blockSize,
+                                                               _ptr(cmpBytes))
+    _check(lib().zccl_gpu_last_status(), "ZCCL_float_decompress_single_thread_arg_record")
+    return cnt
+
+
+def ZCCL_float_single_thread_arg_split_record(outputBytes, oriData, absErrBound, nbEle, blockSize, chunk_arr,
+                                              chunk_iter):
+    """ZCCL/src/ZCCL_float.c:1530; returns the assigned size (also stored
+    as size_t number chunk_iter of chunk_arr)."""
+    s = ctypes.c_size_t(0)
+    lib().ZCCL_float_single_thread_arg_split_record(_ptr(outputBytes), _ptr(oriData), ctypes.byref(s),
+                                                    absErrBound, nbEle, blockSize, _ptr(chunk_arr), chunk_iter)
+    _check(lib().zccl_gpu_last_status(), "ZCCL_float_single_thread_arg_split_record")
+    return s.value
+
+
+def ZCCL_float_homomophic_add_openmp_threadblock_record(final_cmpBytes, final_cmpSize, nbEle, absErrBound,
+                                                        blockSize, cmpBytes, cmpBytes2, counters=None):
+    """ZCCL/src/ZCCLd_float.c:2067; returns (accumulated size, the four
+    counters after the call's increments, starting from `counters`)."""
+    s = _size_slot(final_cmpSize)
+    c = [ctypes.c_int(v) for v in (counters or [0, 0, 0, 0])]
+    lib().ZCCL_float_homomophic_add_openmp_threadblock_record(
+        _ptr(final_cmpBytes), ctypes.byref(s), nbEle, absErrBound, blockSize, _ptr(cmpBytes), _ptr(cmpBytes2),
+        *[ctypes.byref(v) for v in c])
+    _check(lib().zccl_gpu_last_status(), "ZCCL_float_homomophic_add_openmp_threadblock_record")
+    return s.value, [v.value for v in c]
 
 
 # ---------------------------------------------------------------------------

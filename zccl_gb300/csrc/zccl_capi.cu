@@ -11,6 +11,7 @@
 #include <math.h>
 #include <omp.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -682,6 +683,23 @@ namespace {
 
 thread_local int t_last_status = ZCCL_GPU_OK;
 
+/* Elements in the blocks of non-zero width of a stream, from its width
+ * index: the one quantity besides n and the stream size that the
+ * reference's memory-access counts depend on. */
+__global__ void k_nonzero_elements(const uint8_t *widths, ZGeom g, unsigned long long *out)
+{
+    unsigned long long acc = 0;
+    const uint64_t reg = (uint64_t)g.T * g.nb_reg;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < g.nblocks;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        if (!widths[i]) continue;
+        acc += i < reg ? zg_block_len(g.tbs, g.L, i % g.nb_reg) : zg_block_len(g.rem, g.L, i - reg);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31u) == 0 && acc) atomicAdd(out, acc);
+}
+
 struct DevBuf {
     void *p = nullptr;
     size_t n = 0;
@@ -714,6 +732,7 @@ struct DropCtx {
     cudaStream_t st2 = nullptr; /* a second input's copy, beside the first one's walk */
     cudaEvent_t ev = nullptr;
     DevBuf fin, fout, s[3], ix[3], ws;
+    DevBuf aux; /* counters read back by the _record entry points */
 };
 
 DropCtx *drop_ctx()
@@ -777,6 +796,24 @@ int finish(DropCtx *c, void *ws)
     return rc;
 }
 
+/* Elements in the non-zero-width blocks of the indexed stream whose index
+ * is at `index` (synchronous). */
+int nonzero_elements(DropCtx *c, void *index, const ZGeom &g, uint64_t *nz)
+{
+    if (int rc = c->aux.ensure(64)) return rc;
+    unsigned long long *d = static_cast<unsigned long long *>(c->aux.p);
+    if (cudaMemsetAsync(d, 0, 8, c->st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    const uint64_t want = (g.nblocks + 255) / 256;
+    const unsigned grid = (unsigned)std::min<uint64_t>(want ? want : 1, 4096);
+    k_nonzero_elements<<<grid, 256, 0, c->st>>>(bind_index(index, g).widths, g, d);
+    unsigned long long v = 0;
+    if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(&v, d, 8, cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
+        cudaStreamSynchronize(c->st) != cudaSuccess)
+        return ZCCL_GPU_ECUDA;
+    *nz = v;
+    return ZCCL_GPU_OK;
+}
+
 void report(const char *fn, int rc)
 {
     t_last_status = rc;
@@ -828,7 +865,7 @@ int stage_stream(DropCtx *c, int slot, const unsigned char *cmp, const ZGeom &g,
 }
 
 int dropin_compress(unsigned char *outputBytes, const float *oriData, size_t *outSize, float eb,
-                    size_t n, int L, int T, uint32_t fmt = ZG_FASTMODE1)
+                    size_t n, int L, int T, uint32_t fmt = ZG_FASTMODE1, uint64_t *nz_out = nullptr)
 {
     ZGeom g;
     if (!outputBytes || !oriData || !outSize || make_geom(n, L, T, &g)) return ZCCL_GPU_EINVAL;
@@ -861,6 +898,8 @@ int dropin_compress(unsigned char *outputBytes, const float *oriData, size_t *ou
     if (int rc = finish(c, c->ws.p)) return rc;
     size_t size = 0;
     if (int rc = zccl_gpu_stream_size(&s, n, L, T, &size, c->st)) return rc;
+    if (nz_out)
+        if (int rc = nonzero_elements(c, s.index, g, nz_out)) return rc;
     if (s.bytes != outputBytes) {
         if (dout && size > room) return ZCCL_GPU_ECAPACITY;
         cudaMemcpyKind k = dout ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
@@ -872,7 +911,7 @@ int dropin_compress(unsigned char *outputBytes, const float *oriData, size_t *ou
 }
 
 int dropin_decompress(float *newData, size_t n, float eb, int L, const unsigned char *cmp, int T,
-                      uint32_t fmt = ZG_FASTMODE1)
+                      uint32_t fmt = ZG_FASTMODE1, uint64_t *nz_out = nullptr, uint64_t *size_out = nullptr)
 {
     ZGeom g;
     if (!newData || !cmp || make_geom(n, L, T, &g)) return ZCCL_GPU_EINVAL;
@@ -897,6 +936,10 @@ int dropin_decompress(float *newData, size_t n, float eb, int L, const unsigned 
         int rc = finish(c, c->ws.p);
         if (rc == ZCCL_GPU_EBOUNDS && capped && pass == 0) continue;
         if (rc) return rc;
+        if (nz_out)
+            if ((rc = nonzero_elements(c, s.index, g, nz_out))) return rc;
+        if (size_out)
+            if ((rc = zccl_gpu_stream_size(&s, n, L, T, (size_t *)size_out, c->st))) return rc;
         break;
     }
     if (!dout) {
@@ -908,7 +951,8 @@ int dropin_decompress(float *newData, size_t n, float eb, int L, const unsigned 
 }
 
 int dropin_homadd(unsigned char *final_cmp, size_t *final_size, size_t n, float eb, int L,
-                  const unsigned char *cmp1, const unsigned char *cmp2, int T)
+                  const unsigned char *cmp1, const unsigned char *cmp2, int T,
+                  unsigned long long *cases_out = nullptr)
 {
     (void)eb;
     ZGeom g;
@@ -937,10 +981,20 @@ int dropin_homadd(unsigned char *final_cmp, size_t *final_size, size_t n, float 
             return ZCCL_GPU_ECUDA;
         if (int rc = walk_stream(&in[1], g, c->ws.p, c->st)) return rc;
         int rc = finish(c, c->ws.p);
+        unsigned long long *d_cases = nullptr;
+        if (rc == ZCCL_GPU_OK && cases_out) {
+            if ((rc = c->aux.ensure(64))) return rc;
+            d_cases = static_cast<unsigned long long *>(c->aux.p) + 1;
+            if (cudaMemsetAsync(d_cases, 0, 32, c->st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+        }
         if (rc == ZCCL_GPU_OK) {
-            if ((rc = zccl_gpu_homadd(&out, in, 2, n, L, T, c->ws.p, c->st))) return rc;
+            if ((rc = zccl_gpu_homadd_cases(&out, in, 2, n, L, T, c->ws.p, d_cases, c->st))) return rc;
             rc = finish(c, c->ws.p);
         }
+        if (rc == ZCCL_GPU_OK && d_cases &&
+            (cudaMemcpyAsync(cases_out, d_cases, 32, cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
+             cudaStreamSynchronize(c->st) != cudaSuccess))
+            return ZCCL_GPU_ECUDA;
         if (rc == ZCCL_GPU_EBOUNDS && (cap1 || cap2) && pass == 0) continue;
         if (rc) return rc;
         break;
@@ -1108,6 +1162,119 @@ extern "C" void ZCCL_float_homomophic_add_single_thread(unsigned char *final_cmp
 {
     report(__func__, dropin_homadd(final_cmpBytes, final_cmpSize, nbEle, absErrBound, blockSize,
                                    cmpBytes, cmpBytes2, 1));
+}
+
+/* ---- the allocating and the _record variants ----------------------------- */
+
+extern "C" unsigned char *ZCCL_float_openmp_threadblock(float *oriData, size_t *outSize, float absErrBound,
+                                                        size_t nbEle, int blockSize)
+{
+    /* The reference mallocs 4*nbEle bytes (ZCCL_float.c:204); the buffer
+     * here holds the largest stream the geometry allows, which is never
+     * less.  The caller frees it with free(). */
+    const int T = omp_threads();
+    ZGeom g;
+    unsigned char *out = nullptr;
+    int rc = ZCCL_GPU_EINVAL;
+    if (outSize && make_geom(nbEle, blockSize, T, &g) == ZCCL_GPU_OK) {
+        out = static_cast<unsigned char *>(malloc(std::max<size_t>(4 * nbEle, (size_t)zg_stream_worst(&g))));
+        rc = out ? dropin_compress(out, oriData, outSize, absErrBound, nbEle, blockSize, T) : ZCCL_GPU_ENOMEM;
+        if (rc != ZCCL_GPU_OK) {
+            free(out);
+            out = nullptr;
+        }
+    }
+    report(__func__, rc);
+    return out;
+}
+
+extern "C" void ZCCL_float_decompress_openmp_threadblock(float **newData, size_t nbEle, float absErrBound,
+                                                        int blockSize, unsigned char *cmpBytes)
+{
+    /* *newData = malloc(4*nbEle) as in the reference (ZCCLd_float.c:29),
+     * kept for the caller to free even when the call fails */
+    if (!newData) {
+        report(__func__, ZCCL_GPU_EINVAL);
+        return;
+    }
+    *newData = static_cast<float *>(malloc(sizeof(float) * (nbEle ? nbEle : 1)));
+    if (!*newData) {
+        report(__func__, ZCCL_GPU_ENOMEM);
+        return;
+    }
+    report(__func__, dropin_decompress(*newData, nbEle, absErrBound, blockSize, cmpBytes, omp_threads()));
+}
+
+extern "C" size_t ZCCL_float_single_thread_arg_record(unsigned char *outputBytes, float *oriData, size_t *outSize,
+                                                      float absErrBound, size_t nbEle, int blockSize)
+{
+    uint64_t nz = 0;
+    const int rc = dropin_compress(outputBytes, oriData, outSize, absErrBound, nbEle, blockSize, 1, ZG_FASTMODE1,
+                                   &nz);
+    report(__func__, rc);
+    if (rc != ZCCL_GPU_OK) return 0;
+    /* The reference's own count of the bytes its scalar code touches
+     * (ZCCL_float.c:997-1208): 20 around the head, 12 per element of every
+     * block, each block's bytes plus 8 per element of a non-zero-width one,
+     * 56 for the offset table, and the chunk copied out (read and written).
+     * It depends on the stream only, so it is computed from it. */
+    const size_t C = *outSize, blocks = C - 12;
+    return 20 + 12 * (nbEle - 1) + blocks + 8 * (size_t)nz + 56 + 2 * (C - 8);
+}
+
+extern "C" size_t ZCCL_float_decompress_single_thread_arg_record(float *newData, size_t nbEle, float absErrBound,
+                                                                 int blockSize, unsigned char *cmpBytes)
+{
+    uint64_t nz = 0, C = 0;
+    const int rc = dropin_decompress(newData, nbEle, absErrBound, blockSize, cmpBytes, 1, ZG_FASTMODE1, &nz, &C);
+    report(__func__, rc);
+    if (rc != ZCCL_GPU_OK) return 0;
+    /* The reference's count (ZCCLd_float.c:383-533): 24 around the head,
+     * each block's bytes, 8 per element of a zero-width block and 20 per
+     * element of any other. */
+    return 24 + (size_t)(C - 12) + 8 * (nbEle - 1) + 12 * (size_t)nz;
+}
+
+extern "C" void ZCCL_float_single_thread_arg_split_record(unsigned char *outputBytes, float *oriData, size_t *outSize,
+                                                          float absErrBound, size_t nbEle, int blockSize,
+                                                          unsigned char *chunk_arr, size_t chunk_iter)
+{
+    /* The T = 1 stream, and its size also stored as size_t number
+     * chunk_iter of chunk_arr (ZCCL_float.c:1691-1692), the frame table of
+     * the split allreduce (ZCCL_ring.c:1496-1518).  chunk_arr may be host or
+     * device memory. */
+    int rc = dropin_compress(outputBytes, oriData, outSize, absErrBound, nbEle, blockSize, 1);
+    if (rc == ZCCL_GPU_OK && chunk_arr) {
+        const size_t v = *outSize;
+        unsigned char *dst = chunk_arr + chunk_iter * sizeof(size_t);
+        if (is_device_ptr(chunk_arr))
+            rc = cudaMemcpy(dst, &v, sizeof v, cudaMemcpyHostToDevice) == cudaSuccess ? ZCCL_GPU_OK : ZCCL_GPU_ECUDA;
+        else
+            memcpy(dst, &v, sizeof v);
+    }
+    report(__func__, rc);
+}
+
+extern "C" void ZCCL_float_homomophic_add_openmp_threadblock_record(unsigned char *final_cmpBytes,
+                                                                    size_t *final_cmpSize, size_t nbEle,
+                                                                    float absErrBound, int blockSize,
+                                                                    unsigned char *cmpBytes, unsigned char *cmpBytes2,
+                                                                    int *total_counter_1, int *total_counter_2,
+                                                                    int *total_counter_3, int *total_counter_4)
+{
+    /* The add, and the reference's four branch counters over every block
+     * pair (ZCCLd_float.c:2184-2246 and the tail and remainder copies):
+     * both widths 0, first 0, second 0, neither; ADDED to the four ints
+     * (ZCCLd_float.c:2759-2765), from device counters of the same add. */
+    unsigned long long cases[4] = {0, 0, 0, 0};
+    const int rc = dropin_homadd(final_cmpBytes, final_cmpSize, nbEle, absErrBound, blockSize, cmpBytes, cmpBytes2,
+                                 omp_threads(), cases);
+    if (rc == ZCCL_GPU_OK) {
+        int *const dst[4] = {total_counter_1, total_counter_2, total_counter_3, total_counter_4};
+        for (int k = 0; k < 4; k++)
+            if (dst[k]) *dst[k] += (int)cases[k];
+    }
+    report(__func__, rc);
 }
 
 /* ---- SZp 3-D codec ---------------------------------------------------- */
