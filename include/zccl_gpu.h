@@ -228,6 +228,16 @@ int zccl_gpu_homadd_cases(zccl_gpu_stream *out, zccl_gpu_stream *ins, int P, siz
 int zccl_gpu_compress_noalloc(zccl_gpu_stream *out, const float *d_in, size_t n, float eb, int L,
                               int T, void *cuda_stream, void **d_scratch);
 
+/* Decompress and add: d_acc[i] = d_acc[i] + x'[i] for the n floats x' of
+ * the stream, each sum rounded once -- the float sum MPI_Reduce_local forms
+ * in the decompress-add-recompress allreduce's reduce step
+ * (ZCCL/src/ZCCL_ring.c:1074-1076), in one pass without a buffer of
+ * decompressed floats.  The stream must be indexed with its tile starting
+ * values (in->indexed and in->qprev_valid, as compression and sums leave
+ * it); no counterpart function in the reference. */
+int zccl_gpu_decompress_accumulate(float *d_acc, const zccl_gpu_stream *in, size_t n, float eb, int L, int T,
+                                   void *d_ws, void *cuda_stream);
+
 /* Build the side index of a stream that arrived as bytes only. */
 int zccl_gpu_build_index(zccl_gpu_stream *s, size_t n, int L, int T, void *d_ws, void *cuda_stream);
 
@@ -276,6 +286,33 @@ void SZp_decompress3D(float *decData, unsigned char *cmpData, size_t dim1, size_
 void SZp_decompress3D_fast(float *decData, unsigned char *cmpData, size_t dim1, size_t dim2, size_t dim3,
                            int blockSideLength, double errorBound);
 
+/* ---- SZp 3-D codec, OpenMP stream form --------------------------------
+ * Drop-ins for SZp_compress3D_fast_openmp (ZCCL/include/ZCCL_float.h:98-101,
+ * ZCCL/src/ZCCL_float.c:1862) and SZp_decompress3D_fast_openmp
+ * (ZCCL/include/ZCCLd_float.h:45-48, ZCCL/src/ZCCLd_float.c:2873), which the
+ * 3-D allgatherv calls (ZCCL/src/ZCCL_ring.c:2084,2174).  With T =
+ * omp_get_max_threads() the volume is split into a grid of T sub-volumes
+ * (My_Dims_create's factorisation of T, ZCCL/src/ZCCL_multidim.c:100-140);
+ * the stream is T size_t offsets followed by each sub-volume's serial-form
+ * stream.  Every axis must have at least as many planes as it has parts
+ * (the reference needs the same), else ZCCL_GPU_EINVAL. */
+void SZp_compress3D_fast_openmp(const float *oriData, unsigned char *cmpData, size_t dim1, size_t dim2, size_t dim3,
+                                int blockSideLength, double errorBound, size_t *cmpSize);
+void SZp_decompress3D_fast_openmp(float *decData, unsigned char *cmpData, size_t dim1, size_t dim2, size_t dim3,
+                                  int blockSideLength, double errorBound);
+
+/* Device API of the OpenMP form with T explicit: largest stream, scratch
+ * (its first 16 bytes are the status words zccl_gpu_check() reads), and the
+ * two passes on cuda_stream.  compress writes the stream size to the device
+ * size_t at d_size when it is not null; decompress reads the T offsets
+ * (one synchronization) and needs `avail` readable bytes at d_in. */
+size_t zccl_gpu_szp3d_split_max_bytes(size_t d1, size_t d2, size_t d3, int bs, int T);
+size_t zccl_gpu_szp3d_split_workspace_bytes(size_t d1, size_t d2, size_t d3, int bs, int T);
+int zccl_gpu_szp3d_compress_split(unsigned char *d_out, size_t capacity, const float *d_in, size_t d1, size_t d2,
+                                  size_t d3, int bs, double eb, int T, void *d_ws, size_t *d_size, void *cuda_stream);
+int zccl_gpu_szp3d_decompress_split(float *d_out, const unsigned char *d_in, size_t avail, size_t d1, size_t d2,
+                                    size_t d3, int bs, double eb, int T, void *d_ws, void *cuda_stream);
+
 /* Device API of the same codec: the largest stream, device scratch (the
  * first 16 bytes hold the status words zccl_gpu_check() reads), and the two
  * passes enqueued on cuda_stream.  compress writes the stream size to the
@@ -318,19 +355,23 @@ int zccl_gpu_check(void *d_ws, void *cuda_stream);
  * ------------------------------------------------------------------- */
 #define ZCCL_GPU_BATCH_COMPRESS 0
 #define ZCCL_GPU_BATCH_HOMADD 1
+#define ZCCL_GPU_BATCH_DECOMPRESS 2
 
 typedef struct zccl_gpu_batch_job {
     const float *d_in;    /* compression: n device floats */
-    zccl_gpu_stream *ins; /* sum: P indexed input streams */
+    zccl_gpu_stream *ins; /* sum: P indexed input streams; decompression: the stream (P = 1),
+                             indexed with its tile starting values (qprev_valid) */
     int P;                /* sum: number of inputs (1..32) */
     size_t n;             /* floats of the buffer */
-    float eb;             /* compression: absolute error bound */
+    float eb;             /* compression, decompression: absolute error bound */
     int T;                /* writer thread count of the stream layout */
-    zccl_gpu_stream *out; /* output stream (capacity >= zccl_gpu_max_stream_bytes) */
+    zccl_gpu_stream *out; /* compression, sum: output stream (capacity >= zccl_gpu_max_stream_bytes) */
+    float *d_out;         /* decompression: n device floats */
+    int accumulate;       /* decompression: add the floats to d_out[] instead of storing them */
 } zccl_gpu_batch_job;
 
 typedef struct zccl_gpu_batch {
-    int kind;         /* ZCCL_GPU_BATCH_COMPRESS or ZCCL_GPU_BATCH_HOMADD */
+    int kind;         /* ZCCL_GPU_BATCH_COMPRESS, _HOMADD or _DECOMPRESS */
     int L;            /* block size of every job */
     unsigned grid;    /* CTAs per launch, 0 = as many as fit; set by zccl_gpu_batch_tune() */
     size_t njobs;     /* jobs in the batch */

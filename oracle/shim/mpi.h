@@ -19,4 +19,9 @@ typedef struct { int MPI_SOURCE, MPI_TAG, MPI_ERROR; } MPI_Status;
 #define MPI_SUCCESS 0
 #define MPI_INT 1
 #define MPI_BYTE 2
+/* and those the 3-D decomposition file (ZCCL/src/ZCCL_multidim.c) names in
+ * its scatter helpers; the oracle only calls its My_Dims_create */
+#define MPI_FLOAT 3
+#define MPI_ORDER_C 0
+#define MPI_STATUS_IGNORE ((MPI_Status *)0)
 #endif

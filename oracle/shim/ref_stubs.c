@@ -1,15 +1,10 @@
-/* Link-time stubs for the symbols the reference codec files reference from
- * the MPI side: My_Dims_create (ZCCL/src/ZCCL_multidim.c:100), called only by
- * the OpenMP 3-D SZp codec, and the MPI calls of the appendix file's
- * allgather variants (ZCCL/src/ZCCL_appendix.c:591-941).  The oracle never
- * calls any of them; the MPI stubs abort if it ever did. */
+/* Link-time stubs for the MPI calls that the reference codec files make
+ * outside the codec: the allgather variants of the appendix file
+ * (ZCCL/src/ZCCL_appendix.c:591-941) and the scatter helpers of the 3-D
+ * decomposition file (ZCCL/src/ZCCL_multidim.c:13-95), whose My_Dims_create
+ * the OpenMP SZp 3-D codec calls.  The oracle never calls any of them; they
+ * abort if it ever did. */
 #include <stdlib.h>
-void My_Dims_create(int nnodes, int ndims, int dims[])
-{
-    int i;
-    for (i = 0; i < ndims; i++) dims[i] = 1;
-    if (ndims > 0) dims[0] = nnodes;
-}
 
 #define ORACLE_NO_MPI(name) \
     int name() { abort(); }
@@ -24,3 +19,7 @@ ORACLE_NO_MPI(MPI_Sendrecv)
 ORACLE_NO_MPI(MPI_Test)
 ORACLE_NO_MPI(MPI_Wait)
 ORACLE_NO_MPI(MPI_Waitall)
+ORACLE_NO_MPI(MPI_Cart_coords)
+ORACLE_NO_MPI(MPI_Type_create_subarray)
+ORACLE_NO_MPI(MPI_Type_commit)
+ORACLE_NO_MPI(MPI_Type_free)

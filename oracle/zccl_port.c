@@ -622,3 +622,98 @@ void port_homadd_cases(const unsigned char *cmp1, const unsigned char *cmp2, siz
         if (t == T - 1 && rem) cases_segment(&a, &b, rem, L, counts);
     }
 }
+
+/* ======================================================================
+ * SZp 3-D codec, OpenMP form (SZp_compress3D_fast_openmp,
+ * ZCCL/src/ZCCL_float.c:1862-2048; SZp_decompress3D_fast_openmp,
+ * ZCCL/src/ZCCLd_float.c:2873-3034): the volume is split among T threads
+ * by a 3-D grid of tdims[0] x tdims[1] x tdims[2] sub-volumes; the stream
+ * is T little-endian size_t offsets (relative to the end of the offsets)
+ * followed by every sub-volume's serial-form stream in thread order.
+ * ====================================================================== */
+
+static int cmp_int_desc(const void *a, const void *b)
+{
+    const int x = *(const int *)a, y = *(const int *)b;
+    return (x < y) - (x > y);
+}
+
+/* My_Dims_create(n, 3, {0, 0, 0}) (ZCCL/src/ZCCL_multidim.c:100-140): the
+ * prime factors of n, largest first, each multiplied into the currently
+ * smallest dimension (the first of equals), the result sorted descending. */
+void port_dims3(int n, int d[3])
+{
+    int f[64], nf = 0;
+    d[0] = d[1] = d[2] = 1;
+    for (int i = 2, rem = n; i <= rem; i++)
+        while (rem % i == 0) {
+            f[nf++] = i;
+            rem /= i;
+        }
+    qsort(f, (size_t)nf, sizeof(int), cmp_int_desc);
+    for (int i = 0; i < nf; i++) {
+        int m = 0;
+        for (int j = 1; j < 3; j++)
+            if (d[j] < d[m]) m = j;
+        d[m] *= f[i];
+    }
+    qsort(d, 3, sizeof(int), cmp_int_desc);
+}
+
+/* Sub-volume of thread r: origin o[3] and extent s[3] (ZCCL_float.c:1904-1933:
+ * extents base + 1 for the first `rem` parts of each axis, thread order
+ * x-major). */
+static void split_meta(size_t d1, size_t d2, size_t d3, const int td[3], int r, size_t o[3], size_t s[3])
+{
+    const size_t dim[3] = {d1, d2, d3};
+    int c[3];
+    c[0] = r / (td[1] * td[2]);
+    c[1] = (r / td[2]) % td[1];
+    c[2] = r % td[2];
+    for (int a = 0; a < 3; a++) {
+        const size_t base = dim[a] / (size_t)td[a], rem = dim[a] % (size_t)td[a];
+        o[a] = (size_t)c[a] * base + ((size_t)c[a] < rem ? (size_t)c[a] : rem);
+        s[a] = base + ((size_t)c[a] < rem ? 1u : 0u);
+    }
+}
+
+void port_szp3d_compress_split(const float *x, unsigned char *out, size_t d1, size_t d2, size_t d3, int bs,
+                               double eb, int T, size_t *cmpSize)
+{
+    int td[3];
+    port_dims3(T, td);
+    size_t off = 0;
+    for (int r = 0; r < T; r++) {
+        size_t o[3], s[3];
+        split_meta(d1, d2, d3, td, r, o, s);
+        float *sub = (float *)malloc((s[0] * s[1] * s[2] + 1) * sizeof(float));
+        for (size_t i = 0; i < s[0]; i++)
+            for (size_t j = 0; j < s[1]; j++)
+                memcpy(sub + (i * s[1] + j) * s[2], x + ((o[0] + i) * d2 + o[1] + j) * d3 + o[2], s[2] * sizeof(float));
+        size_t sz = 0;
+        memcpy(out + 8 * (size_t)r, &off, 8);
+        port_szp3d_compress(sub, out + 8 * (size_t)T + off, s[0], s[1], s[2], bs, eb, &sz);
+        off += sz;
+        free(sub);
+    }
+    *cmpSize = 8 * (size_t)T + off;
+}
+
+void port_szp3d_decompress_split(float *y, const unsigned char *cmp, size_t d1, size_t d2, size_t d3, int bs,
+                                 double eb, int T)
+{
+    int td[3];
+    port_dims3(T, td);
+    for (int r = 0; r < T; r++) {
+        size_t o[3], s[3];
+        split_meta(d1, d2, d3, td, r, o, s);
+        uint64_t off;
+        memcpy(&off, cmp + 8 * (size_t)r, 8);
+        float *sub = (float *)malloc((s[0] * s[1] * s[2] + 1) * sizeof(float));
+        port_szp3d_decompress(sub, cmp + 8 * (size_t)T + off, s[0], s[1], s[2], bs, eb);
+        for (size_t i = 0; i < s[0]; i++)
+            for (size_t j = 0; j < s[1]; j++)
+                memcpy(y + ((o[0] + i) * d2 + o[1] + j) * d3 + o[2], sub + (i * s[1] + j) * s[2], s[2] * sizeof(float));
+        free(sub);
+    }
+}

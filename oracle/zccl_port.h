@@ -58,6 +58,17 @@ void port_szp3d_compress(const float *x, unsigned char *out, size_t d1, size_t d
 void port_szp3d_decompress(float *y, const unsigned char *cmp, size_t d1, size_t d2, size_t d3, int bs,
                            double eb);
 
+/* The same codec in its OpenMP form (SZp_compress3D_fast_openmp,
+ * ZCCL/src/ZCCL_float.c:1862-2048, and SZp_decompress3D_fast_openmp,
+ * ZCCL/src/ZCCLd_float.c:2873-3034) for T threads: T size_t offsets, then
+ * the serial-form stream of each thread's sub-volume; port_dims3 is the
+ * thread grid, My_Dims_create(T, 3, {0,0,0}) (ZCCL/src/ZCCL_multidim.c:100). */
+void port_dims3(int n, int d[3]);
+void port_szp3d_compress_split(const float *x, unsigned char *out, size_t d1, size_t d2, size_t d3, int bs,
+                               double eb, int T, size_t *cmpSize);
+void port_szp3d_decompress_split(float *y, const unsigned char *cmp, size_t d1, size_t d2, size_t d3, int bs,
+                                 double eb, int T);
+
 /* The counts of the reference's _record variants, from a stream.  For a
  * T = 1 stream of nbEle floats: the memory-access counts returned by
  * ZCCL_float_single_thread_arg_record (ZCCL/src/ZCCL_float.c:990-1209)

@@ -260,6 +260,62 @@ class _Codec:
           *[ctypes.byref(c) for c in cnt])
         return out[: size.value].tobytes(), [c.value for c in cnt]
 
+    # ---- the OpenMP form of the SZp 3-D codec -------------------------------
+    def szp3d_compress_split(self, x: np.ndarray, dims, bs: int, eb: float, T: int) -> bytes:
+        """SZp_compress3D_fast_openmp with T threads (the reference through
+        omp_set_num_threads; the port with T explicit)."""
+        x = np.ascontiguousarray(x, dtype=np.float32).ravel()
+        nb = 1
+        for d in dims:
+            nb *= (d - 1) // bs + 1
+        out = np.zeros(8 * T + T * 64 + nb + nb * (bs ** 3) * 5 + 64, dtype=np.uint8)
+        size = ctypes.c_size_t(0)
+        args = [_ptr(x, _f32p), _ptr(out, _u8p), *[ctypes.c_size_t(d) for d in dims], ctypes.c_int(bs),
+                ctypes.c_double(eb)]
+        if self.kind == "port":
+            f = self.lib.port_szp3d_compress_split
+            f.argtypes = [_f32p, _u8p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int,
+                          ctypes.c_double, ctypes.c_int, _szp]
+            f.restype = None
+            f(*args, ctypes.c_int(T), ctypes.byref(size))
+        else:
+            f = self.lib.SZp_compress3D_fast_openmp
+            f.argtypes = [_f32p, _u8p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int,
+                          ctypes.c_double, _szp]
+            f.restype = None
+            self._set_threads(T)
+            f(*args, ctypes.byref(size))
+        return out[: size.value].tobytes()
+
+    def szp3d_decompress_split(self, stream: bytes, dims, bs: int, eb: float, T: int) -> np.ndarray:
+        buf = np.concatenate([np.frombuffer(stream, dtype=np.uint8), np.zeros(64, np.uint8)])
+        y = np.zeros(int(np.prod(dims)), dtype=np.float32)
+        args = [_ptr(y, _f32p), _ptr(buf, _u8p), *[ctypes.c_size_t(d) for d in dims], ctypes.c_int(bs),
+                ctypes.c_double(eb)]
+        if self.kind == "port":
+            f = self.lib.port_szp3d_decompress_split
+            f.argtypes = [_f32p, _u8p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int,
+                          ctypes.c_double, ctypes.c_int]
+            f.restype = None
+            f(*args, ctypes.c_int(T))
+        else:
+            f = self.lib.SZp_decompress3D_fast_openmp
+            f.argtypes = [_f32p, _u8p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int,
+                          ctypes.c_double]
+            f.restype = None
+            self._set_threads(T)
+            f(*args)
+        return y
+
+    def dims3(self, n: int):
+        """My_Dims_create(n, 3, {0, 0, 0}): the reference's own, or the port's."""
+        d = (ctypes.c_int * 3)(0, 0, 0)
+        if self.kind == "port":
+            self.lib.port_dims3(ctypes.c_int(n), d)
+        else:
+            self.lib.My_Dims_create(ctypes.c_int(n), ctypes.c_int(3), d)
+        return list(d)
+
     def homadd_fold(self, streams, n: int, eb: float, L: int, T: int) -> bytes:
         """P-way sum folded pairwise the way the ring's reduce-scatter does it
         (acc = add(received, acc), ZCCL/src/ZCCL_ring_ho.c:281-287)."""

@@ -68,13 +68,13 @@ def torch():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("count,P,T", [(80011, 8, 3), (24000, 4, 1)])
-def test_homomorphic_ring_matches_oracle(torch, port, count, P, T):
+@pytest.mark.parametrize("count,P,T,batched", [(80011, 8, 3, True), (24000, 4, 1, True), (80011, 8, 3, False)])
+def test_homomorphic_ring_matches_oracle(torch, port, count, P, T, batched):
     from zccl_gb300.ring import RingAllreduce
     L = 32
     xs = rank_data(count, P)
     eb = float(np.float32(1e-4 * (max(x.max() for x in xs) - min(x.min() for x in xs))))
-    ring = RingAllreduce(count, P, L, T)
+    ring = RingAllreduce(count, P, L, T, batched=batched)
     ys = ring.homomorphic([torch.from_numpy(x).cuda() for x in xs], eb, per_rank_outputs=True)
     reduced, y_ref = oracle_ring_ho(port, xs, eb, L, T, P)
     for c in range(P):
@@ -87,18 +87,73 @@ def test_homomorphic_ring_matches_oracle(torch, port, count, P, T):
 
 
 @pytest.mark.gpu
-def test_doc_ring_matches_oracle(torch, port):
+@pytest.mark.parametrize("batched", [True, False])
+def test_doc_ring_matches_oracle(torch, port, batched):
     from zccl_gb300.ring import RingAllreduce
     count, P, T, L = 80011, 8, 3, 32
     xs = rank_data(count, P, seed=1)
     eb = float(np.float32(1e-4 * (max(x.max() for x in xs) - min(x.min() for x in xs))))
-    ring = RingAllreduce(count, P, L, T)
+    ring = RingAllreduce(count, P, L, T, batched=batched)
     ys = ring.doc([torch.from_numpy(x).cuda() for x in xs], eb, per_rank_outputs=True)
     reduced, y_ref = oracle_ring_doc(port, xs, eb, L, T, P)
     for c in range(P):
         assert ring.reduced[c].tobytes() == reduced[c], c
     for y in ys:
         assert np.array_equal(y.cpu().numpy().view(np.uint32), y_ref.view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_batched_ring_repeats_and_keeps_variants_apart(torch, port):
+    """Repeated calls replay the cached batches and give the same floats;
+    the two variants' results live in different buffers."""
+    from zccl_gb300.ring import RingAllreduce
+    count, P, T, L = 50021, 4, 2, 32
+    xs = rank_data(count, P, seed=6)
+    eb = float(np.float32(1e-4 * (max(x.max() for x in xs) - min(x.min() for x in xs))))
+    ring = RingAllreduce(count, P, L, T)
+    xd = [torch.from_numpy(x).cuda() for x in xs]
+    _, y_ho = oracle_ring_ho(port, xs, eb, L, T, P)
+    _, y_doc = oracle_ring_doc(port, xs, eb, L, T, P)
+    for _ in range(2):
+        a = ring.homomorphic(xd, eb)
+        b = ring.doc(xd, eb)
+        assert np.array_equal(a.cpu().numpy().view(np.uint32), y_ho.view(np.uint32))
+        assert np.array_equal(b.cpu().numpy().view(np.uint32), y_doc.view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_decompress_accumulate_and_decompress_batch(torch, port):
+    """acc += decompress(stream) in one pass equals the float sum of the
+    oracle's floats; a decompression batch of uneven streams (one of them
+    accumulating) equals the oracle's floats."""
+    import zccl_gb300 as Z
+    rng = np.random.default_rng(14)
+    L = 32
+    sizes = [(5, 1), (33, 1), (8193, 2), (100003, 4), (300001, 3)]
+    streams, refs, ys, jobs = [], [], [], []
+    for k, (n, T) in enumerate(sizes):
+        x = np.cumsum(rng.normal(0, 0.05, n)).astype(np.float32)
+        eb = float(np.float32(1e-4 * (float(x.max() - x.min()) + 1e-3)))
+        codec = Z.Codec(n, L, T)
+        s = codec.compress(torch.from_numpy(x).cuda(), eb)
+        sx = port.compress(x, eb, L, T)
+        assert s.tobytes() == sx
+        ref = port.decompress(sx, n, eb, L, T)
+        base = rng.normal(0, 1.0, n).astype(np.float32)
+        acc = torch.from_numpy(base.copy()).cuda()
+        codec.decompress_accumulate(s, eb, acc)
+        codec.check()
+        assert np.array_equal(acc.cpu().numpy().view(np.uint32), (base + ref).view(np.uint32)), n
+        accumulate = k == 3
+        y = torch.from_numpy(base.copy()).cuda() if accumulate else torch.full((n,), np.nan, device="cuda")
+        jobs.append((s, eb, T, y, accumulate))
+        refs.append(base + ref if accumulate else ref)
+        ys.append(y)
+    b = Z.Batch(Z.BATCH_DECOMPRESS, jobs, L)
+    b.run()
+    b.check()
+    for y, ref in zip(ys, refs):
+        assert np.array_equal(y.cpu().numpy().view(np.uint32), ref.view(np.uint32))
 
 
 @pytest.mark.gpu

@@ -149,3 +149,97 @@ def test_gpu_rounding_near_ties(torch, port, eb):
     y = codec.decompress(buf, eb, avail=m).cpu().numpy()
     codec.check()
     assert np.array_equal(y.view(np.uint32), port.szp3d_decompress(s, dims, bs, eb).view(np.uint32))
+
+
+# ---- the OpenMP stream form (T sub-volumes) -------------------------------
+
+def load_split_golden():
+    with open(os.path.join(GOLD, "szp3d_split.json")) as f:
+        meta = json.load(f)
+    return meta["cases"], np.load(os.path.join(GOLD, "szp3d_split.npz"))
+
+
+def test_split_port_matches_reference_golden(port):
+    cases, arr = load_split_golden()
+    assert len(cases) == 40
+    for c in cases:
+        x, s = arr[f"x{c['i']}"], arr[f"s{c['i']}"].tobytes()
+        dims, bs, eb, T = tuple(c["dims"]), c["bs"], c["eb"], c["T"]
+        assert port.dims3(T) == c["tdims"]
+        assert port.szp3d_compress_split(x, dims, bs, eb, T) == s, c
+        assert sha(port.szp3d_decompress_split(s, dims, bs, eb, T)) == c["dec"], c
+
+
+def test_split_port_matches_reference_library(port):
+    from oracle import zoracle
+    if not zoracle.ref_available():
+        pytest.skip("reference library not built")
+    ref = zoracle.ref()
+    for n in list(range(1, 70)) + [72, 96, 144, 1024]:
+        assert port.dims3(n) == ref.dims3(n), n
+    rng = np.random.default_rng(4)
+    for dims in [(17, 19, 23), (40, 9, 12), (6, 6, 50)]:
+        x = np.cumsum(rng.normal(0, 0.1, int(np.prod(dims)))).astype(np.float32)
+        for bs, T in [(4, 5), (8, 6), (2, 4), (3, 16)]:
+            eb = 1e-3 * float(x.max() - x.min())
+            s = ref.szp3d_compress_split(x, dims, bs, eb, T)
+            assert port.szp3d_compress_split(x, dims, bs, eb, T) == s, (dims, bs, T)
+            assert np.array_equal(port.szp3d_decompress_split(s, dims, bs, eb, T).view(np.uint32),
+                                  ref.szp3d_decompress_split(s, dims, bs, eb, T).view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_split_gpu_matches_reference_golden(torch):
+    import zccl_gb300 as Z
+    from zccl_gb300 import szp3d as S
+    cases, arr = load_split_golden()
+    for c in cases:
+        x, s = arr[f"x{c['i']}"], arr[f"s{c['i']}"].tobytes()
+        dims, bs, eb, T = tuple(c["dims"]), c["bs"], c["eb"], c["T"]
+        codec = S.Szp3D(dims, bs, T=T)
+        buf, size = codec.compress(torch.from_numpy(x).cuda(), eb)
+        n = codec.size(size)
+        assert buf[:n].cpu().numpy().tobytes() == s, c
+        y = codec.decompress(buf, eb, avail=n)
+        codec.check()
+        assert sha(y.cpu().numpy()) == c["dec"], c
+        # the drop-ins, host pointers, T from the OpenMP thread count
+        Z.set_omp_threads(T)
+        out = np.zeros(codec.max_bytes + 64, np.uint8)
+        m = S.SZp_compress3D_fast_openmp(x, out, *dims, bs, eb)
+        assert out[:m].tobytes() == s, c
+        yh = np.zeros(x.size, np.float32)
+        S.SZp_decompress3D_fast_openmp(yh, np.frombuffer(s, np.uint8).copy(), *dims, bs, eb)
+        assert sha(yh) == c["dec"], c
+
+
+@pytest.mark.gpu
+def test_split_gpu_on_a_field_against_port(torch, port):
+    """A 96 x 80 x 100 log-normal field at T = 16 (a 4 x 2 x 2 grid), block
+    side 4, device pointers through the drop-ins."""
+    import zccl_gb300 as Z
+    from zccl_gb300 import szp3d as S
+    from zccl_gb300.workloads import grf_lognormal
+    f = grf_lognormal(100, 9, "cuda")[: 96 * 80 * 100].contiguous()
+    dims, bs, T = (96, 80, 100), 4, 16
+    eb = float(1e-4 * float(f.max() - f.min()))
+    ref = port.szp3d_compress_split(f.cpu().numpy(), dims, bs, eb, T)
+    Z.set_omp_threads(T)
+    out = torch.zeros(len(ref) + 4096, dtype=torch.uint8, device="cuda")
+    m = S.SZp_compress3D_fast_openmp(f, out, *dims, bs, eb)
+    assert out[:m].cpu().numpy().tobytes() == ref
+    y = torch.zeros_like(f)
+    S.SZp_decompress3D_fast_openmp(y, out, *dims, bs, eb)
+    assert np.array_equal(y.cpu().numpy().view(np.uint32),
+                          port.szp3d_decompress_split(ref, dims, bs, eb, T).view(np.uint32))
+
+
+def test_split_rejects_more_parts_than_planes():
+    import zccl_gb300 as Z
+    lib = Z.lib()
+    # T = 8 is a 2 x 2 x 2 grid: every axis needs two planes
+    assert lib.zccl_gpu_szp3d_split_max_bytes(2, 64, 64, 4, 8) > 0
+    assert lib.zccl_gpu_szp3d_split_max_bytes(1, 64, 64, 4, 8) == 0
+    assert lib.zccl_gpu_szp3d_split_max_bytes(64, 64, 1, 4, 8) == 0
+    assert lib.zccl_gpu_szp3d_split_workspace_bytes(64, 64, 1, 4, 8) == 0
+    assert lib.zccl_gpu_szp3d_split_max_bytes(64, 64, 64, 4, 0) == 0

@@ -39,6 +39,7 @@ EXPORTS = [
     "ZCCL_float_single_thread_arg_split_record", "ZCCL_float_homomophic_add_openmp_threadblock_record",
     "zccl_gpu_max_stream_bytes", "zccl_gpu_index_bytes", "zccl_gpu_workspace_bytes",
     "zccl_gpu_compress", "zccl_gpu_decompress", "zccl_gpu_homadd", "zccl_gpu_homadd_cases",
+    "zccl_gpu_decompress_accumulate",
     "zccl_gpu_build_index", "zccl_gpu_stream_size", "zccl_gpu_frame_size", "zccl_gpu_check", "zccl_gpu_last_status",
     "zccl_gpu_strerror", "zccl_gpu_width_table", "zccl_gpu_compress_noalloc",
     "zccl_gpu_batch_bytes", "zccl_gpu_batch_plan", "zccl_gpu_batch_run", "zccl_gpu_batch_tune",
@@ -48,6 +49,8 @@ EXPORTS = [
     "zccl_gpu_compress_fixed", "zccl_gpu_decompress_fixed",
     "zccl_gpu_szp3d_max_bytes", "zccl_gpu_szp3d_workspace_bytes", "zccl_gpu_szp3d_compress",
     "zccl_gpu_szp3d_decompress",
+    "SZp_compress3D_fast_openmp", "SZp_decompress3D_fast_openmp", "zccl_gpu_szp3d_split_max_bytes",
+    "zccl_gpu_szp3d_split_workspace_bytes", "zccl_gpu_szp3d_compress_split", "zccl_gpu_szp3d_decompress_split",
 ]
 
 
@@ -68,7 +71,7 @@ class BatchJobDesc(ctypes.Structure):
     """``zccl_gpu_batch_job`` of include/zccl_gpu.h."""
     _fields_ = [("d_in", ctypes.c_void_p), ("ins", ctypes.POINTER(StreamDesc)), ("P", ctypes.c_int),
                 ("n", ctypes.c_size_t), ("eb", ctypes.c_float), ("T", ctypes.c_int),
-                ("out", ctypes.POINTER(StreamDesc))]
+                ("out", ctypes.POINTER(StreamDesc)), ("d_out", ctypes.c_void_p), ("accumulate", ctypes.c_int)]
 
 
 class BatchDesc(ctypes.Structure):
@@ -116,6 +119,7 @@ def lib() -> ctypes.CDLL:
         "ZCCL_float_openmp_threadblock_arg_2": (None, [vp, vp, vp, f, sz, i]),
         "ZCCL_float_decompress_openmp_threadblock_arg_2": (None, [vp, sz, f, i, vp]),
         "zccl_gpu_homadd": (i, [sp, sp, i, sz, i, i, vp, vp]),
+        "zccl_gpu_decompress_accumulate": (i, [vp, sp, sz, f, i, i, vp, vp]),
         "zccl_gpu_homadd_cases": (i, [sp, sp, i, sz, i, i, vp, vp, vp]),
         "zccl_gpu_build_index": (i, [sp, sz, i, i, vp, vp]),
         "zccl_gpu_stream_size": (i, [sp, sz, i, i, ctypes.POINTER(sz), vp]),
@@ -128,6 +132,12 @@ def lib() -> ctypes.CDLL:
         "zccl_gpu_szp3d_workspace_bytes": (sz, [sz, sz, sz, i]),
         "zccl_gpu_szp3d_compress": (i, [vp, sz, vp, sz, sz, sz, i, ctypes.c_double, vp, vp, vp]),
         "zccl_gpu_szp3d_decompress": (i, [vp, vp, sz, sz, sz, sz, i, ctypes.c_double, vp, vp]),
+        "SZp_compress3D_fast_openmp": (None, [vp, vp, sz, sz, sz, i, ctypes.c_double, ctypes.POINTER(sz)]),
+        "SZp_decompress3D_fast_openmp": (None, [vp, vp, sz, sz, sz, i, ctypes.c_double]),
+        "zccl_gpu_szp3d_split_max_bytes": (sz, [sz, sz, sz, i, i]),
+        "zccl_gpu_szp3d_split_workspace_bytes": (sz, [sz, sz, sz, i, i]),
+        "zccl_gpu_szp3d_compress_split": (i, [vp, sz, vp, sz, sz, sz, i, ctypes.c_double, i, vp, vp, vp]),
+        "zccl_gpu_szp3d_decompress_split": (i, [vp, vp, sz, sz, sz, sz, i, ctypes.c_double, i, vp, vp]),
         "zccl_gpu_check": (i, [vp, vp]),
         "zccl_gpu_last_status": (i, []),
         "zccl_gpu_strerror": (ctypes.c_char_p, [i]),
@@ -400,6 +410,15 @@ class Codec:
                   self.stream_ptr), "zccl_gpu_decompress")
         return out
 
+    def decompress_accumulate(self, s: DeviceStream, eb: float, acc):
+        """acc += the stream's floats (one rounding per sum), in one pass; the
+        stream must carry its tile starting values (compressed or summed on
+        the device)."""
+        _check(lib().zccl_gpu_decompress_accumulate(acc.data_ptr(), ctypes.byref(s.desc), self.n, eb, self.L,
+                                                    self.T, self.ws.data_ptr(), self.stream_ptr),
+               "zccl_gpu_decompress_accumulate")
+        return acc
+
     def homadd(self, ins, out: DeviceStream | None = None, cases=None) -> DeviceStream:
         if self.fixed:
             raise ZcclError(-1, "the fixed-rate layout has no homomorphic add")
@@ -422,8 +441,31 @@ class Codec:
     def check(self) -> None:
         _check(lib().zccl_gpu_check(self.ws.data_ptr(), self.stream_ptr), "device status")
 
+    def _status_words(self):
+        return self.ws[:8]
 
-BATCH_COMPRESS, BATCH_HOMADD = 0, 1
+
+def check_all(objs) -> None:
+    """Check many Codecs and Batches with one device-to-host read: their
+    status words (the first 8 bytes of each workspace or batch memory) are
+    gathered into one tensor and read once; only when one is non-zero is
+    that object checked the usual way (which decodes, clears and raises)
+    and the others cleared.  Every object's work must be on the current
+    stream or ordered before it."""
+    import torch
+    objs = list(objs)
+    if not objs:
+        return
+    words = torch.stack([o._status_words() for o in objs]).cpu()
+    bad = [o for o, w in zip(objs, words) if bool(w.any())]
+    if bad:
+        for o in objs:
+            if o is not bad[0]:
+                o._status_words().zero_()
+        bad[0].check()
+
+
+BATCH_COMPRESS, BATCH_HOMADD, BATCH_DECOMPRESS = 0, 1, 2
 
 
 class Batch:
@@ -431,7 +473,10 @@ class Batch:
 
     kind BATCH_COMPRESS: jobs are (x, eb, T, out) with x a CUDA float
     tensor and out a DeviceStream; kind BATCH_HOMADD: jobs are (ins, T, out)
-    with ins a list of indexed DeviceStreams of one geometry.  Planned once;
+    with ins a list of indexed DeviceStreams of one geometry; kind
+    BATCH_DECOMPRESS: jobs are (s, eb, T, y, accumulate) with s an indexed
+    DeviceStream (with its tile starting values) and y a CUDA float tensor
+    that receives (or, with accumulate, is added) the floats.  Planned once;
     run() is one memset and one launch on `stream` (a torch stream, default
     the current one), which can be recorded into a CUDA graph."""
 
@@ -448,6 +493,13 @@ class Batch:
             if kind == BATCH_COMPRESS:
                 x, eb, T, out = job
                 d.d_in, d.n, d.eb, d.T = x.data_ptr(), x.numel(), float(eb), int(T)
+            elif kind == BATCH_DECOMPRESS:
+                s, eb, T, y, accumulate = job
+                d.ins = ctypes.pointer(s.desc)
+                d.P, d.n, d.eb, d.T = 1, y.numel(), float(eb), int(T)
+                d.d_out, d.accumulate = y.data_ptr(), int(bool(accumulate))
+                self._keep.append((s, y))
+                continue
             else:
                 ins, T, out = job
                 ia = (StreamDesc * len(ins))(*[s.desc for s in ins])
@@ -479,3 +531,6 @@ class Batch:
 
     def check(self, stream=None) -> None:
         _check(lib().zccl_gpu_batch_check(ctypes.byref(self.desc), self._st(stream)), "batch status")
+
+    def _status_words(self):
+        return self.mem[:8]

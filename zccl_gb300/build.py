@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libzccl_gpu.so")
 SOURCES = ["zk_compress.cu", "zk_decompress.cu", "zk_homadd.cu", "zk_walk.cu", "zccl_capi.cu",
-           "zccl_noalloc.cu", "zk_szp3d.cu"]
+           "zccl_noalloc.cu", "zk_szp3d.cu", "zk_decompress_jobs.cu", "zk_szp3d_split.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [

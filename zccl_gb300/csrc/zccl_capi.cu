@@ -212,6 +212,10 @@ ZSmem homadd_smem(const ZGeom &g)
     return zg_smem(2, g.L, g.TB, homadd_job_bytes(g.TB));
 }
 
+/* The decompressor's layout (padded rows, one input buffer) with room for
+ * the copy of the job in progress. */
+ZSmem decompress_jobs_smem(const ZGeom &g) { return zg_smem(1, g.L, g.TB, (uint32_t)sizeof(DecompressJob)); }
+
 } // namespace
 
 /* ==================================================================== */
@@ -338,6 +342,29 @@ extern "C" int zccl_gpu_decompress_fixed(float *d_out, zccl_gpu_stream *in, size
     return decompress_fmt(d_out, in, n, eb, L, T, d_ws, cuda_stream, ZG_FIXED_BYTES);
 }
 
+extern "C" int zccl_gpu_decompress_accumulate(float *d_acc, const zccl_gpu_stream *in, size_t n, float eb, int L,
+                                              int T, void *d_ws, void *cuda_stream)
+{
+    ZGeom g;
+    if (make_geom(n, L, T, &g) || !valid_stream(in) || !in->indexed || !in->qprev_valid || !d_acc || !d_ws ||
+        !(eb > 0.0f) || !isfinite(eb))
+        return ZCCL_GPU_EINVAL;
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    if (ws_clear(d_ws, g, st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    DecompressJobsArgs a;
+    memset(&a, 0, sizeof(a));
+    a.job.g = g;
+    a.job.in = in->bytes;
+    a.job.avail = in->capacity;
+    a.job.y = d_acc;
+    a.job.idx = bind_index(in->index, g);
+    a.job.eb = eb;
+    a.job.accumulate = 1;
+    a.w = bind_ws(d_ws);
+    a.sm = decompress_jobs_smem(g);
+    return cuda_status(launch_decompress_jobs(a, st));
+}
+
 extern "C" int zccl_gpu_homadd_cases(zccl_gpu_stream *out, zccl_gpu_stream *ins, int P, size_t n,
                                      int L, int T, void *d_ws, unsigned long long *d_cases,
                                      void *cuda_stream)
@@ -451,6 +478,14 @@ extern "C" const char *zccl_gpu_strerror(int status)
 
 namespace {
 
+size_t batch_job_size(int kind)
+{
+    return kind == ZCCL_GPU_BATCH_COMPRESS ? sizeof(CompressJob)
+           : kind == ZCCL_GPU_BATCH_HOMADD ? sizeof(HomAddJob)
+                                           : sizeof(DecompressJob);
+}
+
+
 /* d_mem: err | walk_err | ticket | pad | status[ntiles] | jobs | tile_job[ntiles] | job_tile0[njobs] */
 struct BatchLayout {
     size_t clear, jobs, map, tile0, total;
@@ -461,7 +496,7 @@ BatchLayout batch_layout(int kind, size_t njobs, size_t ntiles)
     BatchLayout l;
     l.clear = 16 + 8 * ntiles;
     l.jobs = align16(l.clear);
-    l.map = align16(l.jobs + njobs * (kind == ZCCL_GPU_BATCH_COMPRESS ? sizeof(CompressJob) : sizeof(HomAddJob)));
+    l.map = align16(l.jobs + njobs * batch_job_size(kind));
     l.tile0 = align16(l.map + 2 * ntiles);
     l.total = l.tile0 + 8 * njobs;
     return l;
@@ -470,14 +505,23 @@ BatchLayout batch_layout(int kind, size_t njobs, size_t ntiles)
 /* Geometry of every job, checked; returns the total tile count or 0. */
 size_t batch_geoms(int kind, const zccl_gpu_batch_job *jobs, size_t njobs, int L, std::vector<ZGeom> &gs)
 {
-    if ((kind != ZCCL_GPU_BATCH_COMPRESS && kind != ZCCL_GPU_BATCH_HOMADD) || !jobs || njobs < 1 ||
-        njobs > 65535)
+    if ((kind != ZCCL_GPU_BATCH_COMPRESS && kind != ZCCL_GPU_BATCH_HOMADD && kind != ZCCL_GPU_BATCH_DECOMPRESS) ||
+        !jobs || njobs < 1 || njobs > 65535)
         return 0;
     gs.resize(njobs);
     size_t ntiles = 0;
     for (size_t j = 0; j < njobs; j++) {
         const zccl_gpu_batch_job &J = jobs[j];
-        if (make_geom(J.n, L, J.T, &gs[j]) || !valid_stream(J.out)) return 0;
+        if (make_geom(J.n, L, J.T, &gs[j])) return 0;
+        if (kind == ZCCL_GPU_BATCH_DECOMPRESS) {
+            /* one input stream, indexed with its starting values */
+            if (!J.ins || J.P != 1 || !valid_stream(J.ins) || !J.ins->indexed || !J.ins->qprev_valid ||
+                !J.d_out || !(J.eb > 0.0f) || !isfinite(J.eb))
+                return 0;
+            ntiles += gs[j].ntiles;
+            continue;
+        }
+        if (!valid_stream(J.out)) return 0;
         if (kind == ZCCL_GPU_BATCH_COMPRESS) {
             if (!J.d_in || !(J.eb > 0.0f) || !isfinite(J.eb)) return 0;
         } else {
@@ -513,6 +557,7 @@ extern "C" int zccl_gpu_batch_plan(zccl_gpu_batch *b, int kind, const zccl_gpu_b
     std::vector<uint64_t> tile0(njobs);
     std::vector<CompressJob> cj(kind == ZCCL_GPU_BATCH_COMPRESS ? njobs : 0);
     std::vector<HomAddJob> hj(kind == ZCCL_GPU_BATCH_HOMADD ? njobs : 0);
+    std::vector<DecompressJob> dj(kind == ZCCL_GPU_BATCH_DECOMPRESS ? njobs : 0);
     int qv = 1;
     size_t t0 = 0;
     for (size_t j = 0; j < njobs; j++) {
@@ -530,6 +575,16 @@ extern "C" int zccl_gpu_batch_plan(zccl_gpu_batch *b, int kind, const zccl_gpu_b
             c.idx = bind_index(J.out->index, g);
             c.status = status + t0;
             c.inv = 1.0f / J.eb; /* float division, as ZCCL/src/ZCCL_float.c:540 */
+        } else if (kind == ZCCL_GPU_BATCH_DECOMPRESS) {
+            DecompressJob &d = dj[j];
+            memset(&d, 0, sizeof(d));
+            d.g = g;
+            d.in = J.ins->bytes;
+            d.avail = J.ins->capacity;
+            d.y = J.d_out;
+            d.idx = bind_index(J.ins->index, g);
+            d.eb = J.eb;
+            d.accumulate = J.accumulate ? 1 : 0;
         } else {
             HomAddJob &h = hj[j];
             memset(&h, 0, sizeof(h));
@@ -555,8 +610,10 @@ extern "C" int zccl_gpu_batch_plan(zccl_gpu_batch *b, int kind, const zccl_gpu_b
         t0 += g.ntiles;
     }
     cudaStream_t st = (cudaStream_t)cuda_stream;
-    const void *jsrc = kind == ZCCL_GPU_BATCH_COMPRESS ? (const void *)cj.data() : (const void *)hj.data();
-    const size_t jbytes = njobs * (kind == ZCCL_GPU_BATCH_COMPRESS ? sizeof(CompressJob) : sizeof(HomAddJob));
+    const void *jsrc = kind == ZCCL_GPU_BATCH_COMPRESS ? (const void *)cj.data()
+                       : kind == ZCCL_GPU_BATCH_HOMADD ? (const void *)hj.data()
+                                                       : (const void *)dj.data();
+    const size_t jbytes = njobs * batch_job_size(kind);
     if (cudaMemsetAsync(base, 0, 8, st) != cudaSuccess || /* clean status words */
         cudaMemcpyAsync(base + lay.jobs, jsrc, jbytes, cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemcpyAsync(base + lay.map, map.data(), 2 * ntiles, cudaMemcpyHostToDevice, st) != cudaSuccess ||
@@ -574,14 +631,17 @@ extern "C" int zccl_gpu_batch_plan(zccl_gpu_batch *b, int kind, const zccl_gpu_b
     b->map_off = lay.map;
     b->tile0_off = lay.tile0;
     b->tb = gs[0].TB;
-    const ZSmem sm = kind == ZCCL_GPU_BATCH_COMPRESS ? compress_smem(gs[0]) : homadd_smem(gs[0]);
+    const ZSmem sm = kind == ZCCL_GPU_BATCH_COMPRESS ? compress_smem(gs[0])
+                     : kind == ZCCL_GPU_BATCH_HOMADD ? homadd_smem(gs[0])
+                                                     : decompress_jobs_smem(gs[0]);
     static_assert(sizeof(sm) == sizeof(b->smem), "layout fields");
     memcpy(b->smem, &sm, sizeof(sm));
-    b->qprev_valid = kind == ZCCL_GPU_BATCH_COMPRESS ? 1 : qv;
-    for (size_t j = 0; j < njobs; j++) {
-        jobs[j].out->indexed = 1;
-        jobs[j].out->qprev_valid = b->qprev_valid;
-    }
+    b->qprev_valid = kind == ZCCL_GPU_BATCH_HOMADD ? qv : 1;
+    if (kind != ZCCL_GPU_BATCH_DECOMPRESS)
+        for (size_t j = 0; j < njobs; j++) {
+            jobs[j].out->indexed = 1;
+            jobs[j].out->qprev_valid = b->qprev_valid;
+        }
     return ZCCL_GPU_OK;
 }
 
@@ -611,6 +671,17 @@ extern "C" int zccl_gpu_batch_run(const zccl_gpu_batch *b, void *cuda_stream)
         a.sm = sm;
         a.grid = b->grid;
         return cuda_status(launch_compress(a, st));
+    }
+    if (b->kind == ZCCL_GPU_BATCH_DECOMPRESS) {
+        DecompressJobsArgs a;
+        memset(&a, 0, sizeof(a));
+        a.job.g.L = (uint32_t)b->L;
+        a.job.g.TB = b->tb;
+        a.batch = bt;
+        a.w = bind_ws(base);
+        a.sm = sm;
+        a.grid = b->grid;
+        return cuda_status(launch_decompress_jobs(a, st));
     }
     HomAddArgs a;
     memset(&a, 0, sizeof(a));
@@ -1110,6 +1181,89 @@ int dropin_szp3d_decompress(float *y, const unsigned char *cmp, size_t d1, size_
     return ZCCL_GPU_OK;
 }
 
+/* The OpenMP form: T = omp_get_max_threads() sub-volumes. */
+int dropin_szp3d_compress_split(const float *x, unsigned char *cmp, size_t d1, size_t d2, size_t d3, int bs, double eb,
+                                size_t *cmpSize, int T)
+{
+    Sz3Split3 sp;
+    if (!x || !cmp || !cmpSize || !sz3_args_ok(d1, d2, d3, bs, eb) || !sz3_split_plan(d1, d2, d3, (uint32_t)T, &sp))
+        return ZCCL_GPU_EINVAL;
+    DropCtx *c = drop_ctx();
+    if (!c) return ZCCL_GPU_ECUDA;
+    std::lock_guard<std::mutex> lk(c->mu);
+    const size_t n = d1 * d2 * d3, cap = sz3_split_max_stream_bytes(sp, (uint32_t)bs);
+    const size_t wsb = sz3_split_workspace_bytes(sp, (uint32_t)bs, true);
+    if (int rc = c->ws.ensure(wsb + 16)) return rc;
+    const bool din = is_device_ptr(x), dout = is_device_ptr(cmp);
+    const float *d_x = x;
+    if (!din) {
+        if (int rc = c->fin.ensure(4 * n)) return rc;
+        if (cudaMemcpyAsync(c->fin.p, x, 4 * n, cudaMemcpyHostToDevice, c->st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+        d_x = (const float *)c->fin.p;
+    }
+    unsigned char *d_out = cmp;
+    const size_t room = dout ? device_room(cmp) : cap;
+    if (!dout) {
+        if (int rc = c->s[0].ensure(cap)) return rc;
+        d_out = (unsigned char *)c->s[0].p;
+    }
+    uint64_t *d_size = (uint64_t *)((uint8_t *)c->ws.p + wsb);
+    if (cudaError_t e = sz3_split_compress(d_out, room, d_x, sp, (uint32_t)bs, eb, c->ws.p, d_size, c->st))
+        return e == cudaErrorInvalidValue ? ZCCL_GPU_ECAPACITY : ZCCL_GPU_ECUDA;
+    uint64_t size = 0;
+    if (cudaMemcpyAsync(&size, d_size, 8, cudaMemcpyDeviceToHost, c->st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    if (int rc = finish(c, c->ws.p)) return rc;
+    if (!dout && (cudaMemcpyAsync(cmp, d_out, size, cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
+                  cudaStreamSynchronize(c->st) != cudaSuccess))
+        return ZCCL_GPU_ECUDA;
+    *cmpSize = (size_t)size;
+    return ZCCL_GPU_OK;
+}
+
+int dropin_szp3d_decompress_split(float *y, const unsigned char *cmp, size_t d1, size_t d2, size_t d3, int bs,
+                                  double eb, int T)
+{
+    Sz3Split3 sp;
+    if (!y || !cmp || !sz3_args_ok(d1, d2, d3, bs, eb) || !sz3_split_plan(d1, d2, d3, (uint32_t)T, &sp))
+        return ZCCL_GPU_EINVAL;
+    DropCtx *c = drop_ctx();
+    if (!c) return ZCCL_GPU_ECUDA;
+    std::lock_guard<std::mutex> lk(c->mu);
+    const size_t n = d1 * d2 * d3, hdr = 8ull * (size_t)T;
+    if (int rc = c->ws.ensure(sz3_split_workspace_bytes(sp, (uint32_t)bs, false))) return rc;
+    const bool din = is_device_ptr(cmp), dout = is_device_ptr(y);
+    std::vector<uint64_t> offs(T);
+    const unsigned char *d_in = cmp;
+    size_t avail;
+    if (din) {
+        avail = device_room(cmp);
+        if (avail < hdr || cudaMemcpy(offs.data(), cmp, hdr, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return ZCCL_GPU_EINVAL;
+    } else {
+        /* the stream's length: the last sub-stream's offset and its size
+         * from its rate table */
+        memcpy(offs.data(), cmp, hdr);
+        uint64_t s[3];
+        sz3_split_extent(sp, (uint32_t)T - 1, s);
+        avail = hdr + (size_t)offs[T - 1] + sz3_host_stream_bytes(cmp + hdr + offs[T - 1], s[0], s[1], s[2], bs);
+        if (int rc = c->s[0].ensure(avail)) return rc;
+        if (cudaMemcpyAsync(c->s[0].p, cmp, avail, cudaMemcpyHostToDevice, c->st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+        d_in = (const unsigned char *)c->s[0].p;
+    }
+    float *d_y = y;
+    if (!dout) {
+        if (int rc = c->fout.ensure(4 * n)) return rc;
+        d_y = (float *)c->fout.p;
+    }
+    if (cudaError_t e = sz3_split_decompress(d_y, d_in, avail, offs.data(), sp, (uint32_t)bs, eb, c->ws.p, c->st))
+        return e == cudaErrorInvalidValue ? ZCCL_GPU_EBOUNDS : ZCCL_GPU_ECUDA;
+    if (int rc = finish(c, c->ws.p)) return rc;
+    if (!dout && (cudaMemcpyAsync(y, d_y, 4 * n, cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
+                  cudaStreamSynchronize(c->st) != cudaSuccess))
+        return ZCCL_GPU_ECUDA;
+    return ZCCL_GPU_OK;
+}
+
 } // namespace
 
 extern "C" int zccl_gpu_last_status(void) { return t_last_status; }
@@ -1331,6 +1485,64 @@ extern "C" void SZp_decompress3D_fast(float *decData, unsigned char *cmpData, si
                                       size_t dim3, int blockSideLength, double errorBound)
 {
     report(__func__, dropin_szp3d_decompress(decData, cmpData, dim1, dim2, dim3, blockSideLength, errorBound));
+}
+
+extern "C" void SZp_compress3D_fast_openmp(const float *oriData, unsigned char *cmpData, size_t dim1, size_t dim2,
+                                           size_t dim3, int blockSideLength, double errorBound, size_t *cmpSize)
+{
+    report(__func__, dropin_szp3d_compress_split(oriData, cmpData, dim1, dim2, dim3, blockSideLength, errorBound,
+                                                 cmpSize, omp_threads()));
+}
+
+extern "C" void SZp_decompress3D_fast_openmp(float *decData, unsigned char *cmpData, size_t dim1, size_t dim2,
+                                             size_t dim3, int blockSideLength, double errorBound)
+{
+    report(__func__, dropin_szp3d_decompress_split(decData, cmpData, dim1, dim2, dim3, blockSideLength, errorBound,
+                                                   omp_threads()));
+}
+
+extern "C" size_t zccl_gpu_szp3d_split_max_bytes(size_t d1, size_t d2, size_t d3, int bs, int T)
+{
+    Sz3Split3 sp;
+    if (!sz3_args_ok(d1, d2, d3, bs, 1.0) || T < 1 || !sz3_split_plan(d1, d2, d3, (uint32_t)T, &sp)) return 0;
+    return sz3_split_max_stream_bytes(sp, (uint32_t)bs);
+}
+
+extern "C" size_t zccl_gpu_szp3d_split_workspace_bytes(size_t d1, size_t d2, size_t d3, int bs, int T)
+{
+    Sz3Split3 sp;
+    if (!sz3_args_ok(d1, d2, d3, bs, 1.0) || T < 1 || !sz3_split_plan(d1, d2, d3, (uint32_t)T, &sp)) return 0;
+    return std::max(sz3_split_workspace_bytes(sp, (uint32_t)bs, true), sz3_split_workspace_bytes(sp, (uint32_t)bs, false));
+}
+
+extern "C" int zccl_gpu_szp3d_compress_split(unsigned char *d_out, size_t capacity, const float *d_in, size_t d1,
+                                             size_t d2, size_t d3, int bs, double eb, int T, void *d_ws, size_t *d_size,
+                                             void *cuda_stream)
+{
+    Sz3Split3 sp;
+    if (!d_out || !d_in || !d_ws || !sz3_args_ok(d1, d2, d3, bs, eb) || T < 1 ||
+        !sz3_split_plan(d1, d2, d3, (uint32_t)T, &sp))
+        return ZCCL_GPU_EINVAL;
+    const cudaError_t e = sz3_split_compress(d_out, capacity, d_in, sp, (uint32_t)bs, eb, d_ws,
+                                             reinterpret_cast<uint64_t *>(d_size), (cudaStream_t)cuda_stream);
+    return e == cudaSuccess ? ZCCL_GPU_OK : e == cudaErrorInvalidValue ? ZCCL_GPU_ECAPACITY : ZCCL_GPU_ECUDA;
+}
+
+extern "C" int zccl_gpu_szp3d_decompress_split(float *d_out, const unsigned char *d_in, size_t avail, size_t d1,
+                                               size_t d2, size_t d3, int bs, double eb, int T, void *d_ws,
+                                               void *cuda_stream)
+{
+    Sz3Split3 sp;
+    if (!d_out || !d_in || !d_ws || !sz3_args_ok(d1, d2, d3, bs, eb) || T < 1 ||
+        !sz3_split_plan(d1, d2, d3, (uint32_t)T, &sp) || avail < 8ull * (size_t)T)
+        return ZCCL_GPU_EINVAL;
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    std::vector<uint64_t> offs((size_t)T);
+    if (cudaMemcpyAsync(offs.data(), d_in, 8ull * (size_t)T, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return ZCCL_GPU_ECUDA;
+    const cudaError_t e = sz3_split_decompress(d_out, d_in, avail, offs.data(), sp, (uint32_t)bs, eb, d_ws, st);
+    return e == cudaSuccess ? ZCCL_GPU_OK : e == cudaErrorInvalidValue ? ZCCL_GPU_EBOUNDS : ZCCL_GPU_ECUDA;
 }
 
 /* ---- the fixed-rate appendix codec ------------------------------------ */

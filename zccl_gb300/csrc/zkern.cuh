@@ -98,6 +98,26 @@ struct alignas(16) HomAddJob {
     uint64_t *status; /* look-back words of the output, one per tile */
 };
 
+/* One indexed stream to decompress (with its tiles' starting values): the
+ * floats go to y, or are added to y with accumulate. */
+struct alignas(16) DecompressJob {
+    ZGeom g;
+    const uint8_t *in;
+    uint64_t avail; /* readable bytes at `in` */
+    float *y;
+    ZIndex idx;
+    float eb;
+    int accumulate;
+};
+
+struct DecompressJobsArgs {
+    DecompressJob job; /* the single job (batch.jobs == null) */
+    ZBatch batch;
+    ZWork w; /* err, walk_err */
+    ZSmem sm;
+    uint32_t grid; /* CTAs to launch, 0 = as many as fit */
+};
+
 /* One staged input tile of the homomorphic add: which tile and input it
  * is, and where its bytes start within the buffer (the TMA copy keeps the
  * source's 16-byte phase). */
@@ -513,6 +533,26 @@ cudaError_t sz3_compress(uint8_t *out, uint64_t cap, const float *x, uint64_t d1
 cudaError_t sz3_decompress(float *y, const uint8_t *in, uint64_t avail, uint64_t d1, uint64_t d2, uint64_t d3,
                            uint32_t bs, double eb, void *ws, cudaStream_t st);
 
+/* The OpenMP form of the SZp 3-D codec (zk_szp3d_split.cu): the thread
+ * grid of T threads over a d1 x d2 x d3 volume, its sizes, and the two
+ * passes (sub-volume after sub-volume through the serial-form kernels).
+ * sz3_split_plan fails when T is out of range or an axis has fewer planes
+ * than parts.  Decompression takes the T header offsets on the host. */
+struct Sz3Split3 {
+    uint32_t T;
+    uint32_t parts[3]; /* thread grid, parts[0] >= parts[1] >= parts[2] */
+    uint64_t dim[3];
+};
+bool sz3_split_plan(uint64_t d1, uint64_t d2, uint64_t d3, uint32_t T, Sz3Split3 *sp);
+void sz3_split_origin(const Sz3Split3 &sp, uint32_t r, uint64_t o[3], uint64_t s[3]);
+void sz3_split_extent(const Sz3Split3 &sp, uint32_t r, uint64_t s[3]);
+size_t sz3_split_max_stream_bytes(const Sz3Split3 &sp, uint32_t bs);
+size_t sz3_split_workspace_bytes(const Sz3Split3 &sp, uint32_t bs, bool compress);
+cudaError_t sz3_split_compress(uint8_t *out, uint64_t cap, const float *x, const Sz3Split3 &sp, uint32_t bs, double eb,
+                               void *ws, uint64_t *d_size, cudaStream_t st);
+cudaError_t sz3_split_decompress(float *y, const uint8_t *in, uint64_t avail, const uint64_t *offs, const Sz3Split3 &sp,
+                                 uint32_t bs, double eb, void *ws, cudaStream_t st);
+
 /* Host: a 2-D TMA map of the floats p[0, n) as rows of 32, boxes of
  * box_rows rows (256: a whole tile; 32: one warp's rows), 128-byte swizzle
  * (16-byte chunk k of row r lands at chunk k ^ (r & 7) of a 1024-byte-aligned
@@ -520,6 +560,7 @@ cudaError_t sz3_decompress(float *y, const uint8_t *in, uint64_t avail, uint64_t
  * 256 rows, or the driver's encoder is unavailable. */
 bool zk_rows_map(CUtensorMap *map, const void *p, uint64_t n, uint32_t box_rows);
 cudaError_t launch_homadd(const HomAddArgs &a, cudaStream_t st);
+cudaError_t launch_decompress_jobs(const DecompressJobsArgs &a, cudaStream_t st);
 cudaError_t launch_walk(const WalkArgs &a, cudaStream_t st);
 
 #endif

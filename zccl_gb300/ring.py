@@ -30,7 +30,7 @@ benchmark measures.
 """
 from __future__ import annotations
 
-from . import Codec, DeviceStream
+from . import BATCH_COMPRESS, BATCH_DECOMPRESS, BATCH_HOMADD, Batch, Codec, DeviceStream, check_all
 
 
 def ring_counts(count: int, P: int) -> tuple[list[int], list[int]]:
@@ -51,15 +51,30 @@ def ring_counts(count: int, P: int) -> tuple[list[int], list[int]]:
 
 
 class RingAllreduce:
-    """Both ring allreduces for P ranks of `count` floats on one device."""
+    """Both ring allreduces for P ranks of `count` floats on one device.
 
-    def __init__(self, count: int, P: int, L: int = 32, T: int = 1, device: str = "cuda"):
+    batched (default): every step's P codec calls of the same kind run as
+    one batch launch (zccl_gpu_batch_*): the homomorphic ring is one
+    compression batch of the P x P chunks, P - 1 sum batches and one
+    decompression batch; the DOC ring, per step, a compression batch and a
+    decompress-and-accumulate batch, then the allgather's compression and
+    decompression batches.  The streams and float buffers the steps pass
+    around belong to the ring object and the batches are planned once per
+    input and error bound, so repeated calls replay the same launches; the
+    returned floats live in a buffer the next call reuses.
+    batched=False: one C-ABI call per chunk and step, the reference's call
+    sequence (the results are the same bytes)."""
+
+    def __init__(self, count: int, P: int, L: int = 32, T: int = 1, device: str = "cuda", batched: bool = True):
         self.count, self.P, self.L, self.T = int(count), int(P), int(L), int(T)
         self.cnts, self.displs = ring_counts(self.count, self.P)
         if min(self.cnts) < self.T:
             raise ValueError(f"every ring chunk needs at least T={T} floats: {self.cnts}")
         self.device = device
+        self.batched = bool(batched)
         self._codecs: dict[int, Codec] = {}
+        self._plans: dict = {}
+        self._bufs = None
 
     def codec(self, c: int) -> Codec:
         n = self.cnts[c]
@@ -70,12 +85,13 @@ class RingAllreduce:
     def _chunk(self, x, c):
         return x[self.displs[c]: self.displs[c] + self.cnts[c]]
 
-    def _check(self):
-        """Raise if any call on any chunk's codec failed since the last check
-        (the device status words keep every call's errors until read)."""
-        for cd in self._codecs.values():
-            cd.check()
+    def _check(self, extra=()):
+        """Raise if any call on any chunk's codec, or any batch, failed since
+        the last check (the device status words keep every call's errors
+        until read); one device-to-host read for all of them."""
+        check_all(list(self._codecs.values()) + list(self._plans.values()) + list(extra))
 
+    # ---- one call per chunk and step -------------------------------------
     def _allgather_decompress(self, reduced, eb, per_rank_outputs):
         """Every rank decompresses all P reduced chunks into its result."""
         import torch
@@ -92,6 +108,8 @@ class RingAllreduce:
         """MPI_Allreduce_ZCCL_RI2_mt_oa_ho_record for the P tensors in xs.
         Returns the allreduced floats (or every rank's copy) and leaves the
         reduced compressed chunks in self.reduced (chunk c is rank c's)."""
+        if self.batched:
+            return self._homomorphic_batched(xs, eb, per_rank_outputs)
         P = self.P
         # every rank compresses its P chunks (ZCCL_ring_ho.c:250-258)
         S = [[self.codec(c).compress(self._chunk(xs[r], c), eb) for c in range(P)] for r in range(P)]
@@ -107,6 +125,8 @@ class RingAllreduce:
 
     def doc(self, xs, eb: float, per_rank_outputs: bool = False):
         """MPI_Allreduce_ZCCL_RI2_mt_oa_record for the P tensors in xs."""
+        if self.batched:
+            return self._doc_batched(xs, eb, per_rank_outputs)
         P = self.P
         acc = [x.clone() for x in xs]
         for i in range(P - 1):
@@ -116,11 +136,100 @@ class RingAllreduce:
             # ... and adds the decompressed chunk it receives (ZCCL_ring.c:1074-1077)
             for r in range(P):
                 src, c = (r - 1) % P, (r - 2 - i) % P
-                self._chunk(acc[r], c).add_(self.codec(c).decompress(msgs[src], eb))
+                self.codec(c).decompress_accumulate(msgs[src], eb, self._chunk(acc[r], c))
         # the allgather compresses each rank's reduced chunk (ZCCL_ring.c:863-869)
         self.reduced = [self.codec(c).compress(self._chunk(acc[c], c), eb) for c in range(P)]
         self._check()
         return self._allgather_decompress(self.reduced, eb, per_rank_outputs)
+
+    # ---- one batch per step ----------------------------------------------
+    def _buffers(self):
+        """The ring's own streams and floats, made once: the P x P chunk
+        streams and a spare stream per rank (homomorphic), P float
+        accumulators, P message streams and P reduced streams (DOC), and the
+        result."""
+        import torch
+        if self._bufs is None:
+            P = self.P
+            self._bufs = {
+                "S": [[self.codec(c).new_stream() for c in range(P)] for _ in range(P)],
+                "spare": [self.codec(c).new_stream() for c in range(P)],
+                "acc": [torch.empty(self.count, dtype=torch.float32, device=self.device) for _ in range(P)],
+                "msg": [self.codec(c).new_stream() for c in range(P)],
+                "red": [self.codec(c).new_stream() for c in range(P)],
+                "y_ho": torch.empty(self.count, dtype=torch.float32, device=self.device),
+                "y_doc": torch.empty(self.count, dtype=torch.float32, device=self.device),
+            }
+        return self._bufs
+
+    def _plan(self, key, kind, jobs):
+        b = self._plans.get(key)
+        if b is None:
+            b = Batch(kind, jobs, self.L, device=self.device)
+            self._plans[key] = b
+        return b
+
+    def _gather_batched(self, reduced, eb, per_rank_outputs, tag):
+        import torch
+        P = self.P
+        if per_rank_outputs:  # every rank's copy, one batch of P x P decompressions
+            ys = [torch.empty(self.count, dtype=torch.float32, device=self.device) for _ in range(P)]
+            jobs = [(reduced[c], eb, self.T, self._chunk(y, c), False) for y in ys for c in range(P)]
+            b = Batch(BATCH_DECOMPRESS, jobs, self.L, device=self.device)
+            b.run()
+            self._check([b])
+            return ys
+        y = self._buffers()["y_" + tag]
+        self._plan((tag, "gather", eb), BATCH_DECOMPRESS,
+                   [(reduced[c], eb, self.T, self._chunk(y, c), False) for c in range(P)]).run()
+        self._check()
+        return y
+
+    def _homomorphic_batched(self, xs, eb, per_rank_outputs):
+        P = self.P
+        B = self._buffers()
+        S = [row[:] for row in B["S"]]
+        spare = B["spare"][:]
+        key = ("ho", "compress", eb, tuple(x.data_ptr() for x in xs))
+        if key not in self._plans:  # a new input: forget the previous one's plan
+            for k in [k for k in self._plans if k[:2] == ("ho", "compress")]:
+                del self._plans[k]
+        self._plan(key, BATCH_COMPRESS,
+                   [(self._chunk(xs[r], c), eb, self.T, S[r][c]) for r in range(P) for c in range(P)]).run()
+        for i in range(P - 1):
+            jobs = []
+            for r in range(P):
+                src, c = (r - 1) % P, (r - 2 - i) % P
+                jobs.append(([S[src][c], S[r][c]], self.T, spare[c]))
+            self._plan(("ho", "step", i), BATCH_HOMADD, jobs).run()
+            for r in range(P):  # the sums become the ranks' chunks; the old chunks the spares
+                c = (r - 2 - i) % P
+                S[r][c], spare[c] = spare[c], S[r][c]
+        self.reduced = [S[c][c] for c in range(P)]
+        return self._gather_batched(self.reduced, eb, per_rank_outputs, "ho")
+
+    def _doc_batched(self, xs, eb, per_rank_outputs):
+        P = self.P
+        B = self._buffers()
+        acc, msg, red = B["acc"], B["msg"], B["red"]
+        for a, x in zip(acc, xs):
+            a.copy_(x)
+        for i in range(P - 1):
+            # every rank compresses the chunk it sends (a message per chunk:
+            # the P ranks send P different chunks in a step) ...
+            self._plan(("doc", "send", i, eb), BATCH_COMPRESS,
+                       [(self._chunk(acc[r], (r - 1 - i) % P), eb, self.T, msg[(r - 1 - i) % P])
+                        for r in range(P)]).run()
+            # ... and adds the one it receives, decompressed, into its own
+            jobs = []
+            for r in range(P):
+                c = (r - 2 - i) % P
+                jobs.append((msg[c], eb, self.T, self._chunk(acc[r], c), True))
+            self._plan(("doc", "add", i, eb), BATCH_DECOMPRESS, jobs).run()
+        self._plan(("doc", "reduced", eb), BATCH_COMPRESS,
+                   [(self._chunk(acc[c], c), eb, self.T, red[c]) for c in range(P)]).run()
+        self.reduced = red[:]
+        return self._gather_batched(self.reduced, eb, per_rank_outputs, "doc")
 
 
 def reduce_homomorphic(codec: Codec, streams: list[DeviceStream], out: DeviceStream | None = None):
