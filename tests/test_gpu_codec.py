@@ -394,3 +394,28 @@ def test_record_and_split_variants_with_device_pointers(port, torch):
     host[: len(sx)] = np.frombuffer(sx, np.uint8)
     assert np.array_equal(Z.ZCCL_float_decompress_openmp_threadblock(n, eb, L, host),
                           port.decompress(sx, n, eb, L, 3))
+
+
+def test_lookback_wait_gives_up_and_reports_timeout(torch, monkeypatch):
+    """A bounded device wait that runs out: with the library's test hook the
+    compressor hands out tiles from 1 on, so tile 0 never publishes its size
+    and tile 1's look-back gives up after 4096 polls.  The call returns at
+    once, the check reports ZCCL_GPU_ETIMEOUT (no fault, no hang), and the
+    next call on the same workspace is clean and exact again."""
+    import time
+    n, L, T = 1 << 20, 32, 1
+    codec = Z.Codec(n, L, T)
+    x = dev(torch, np.sin(np.arange(n, dtype=np.float64) * 1e-3).astype(np.float32))
+    ref = codec.compress(x, 1e-4)
+    codec.check()
+    monkeypatch.setenv("ZCCL_GPU_TEST_STALL_TILE0", "1")
+    t0 = time.perf_counter()
+    codec.compress(x, 1e-4)
+    with pytest.raises(Z.ZcclError) as e:
+        codec.check()
+    assert time.perf_counter() - t0 < 10.0
+    assert e.value.status == -6
+    monkeypatch.delenv("ZCCL_GPU_TEST_STALL_TILE0")
+    again = codec.compress(x, 1e-4)
+    codec.check()
+    assert again.tobytes() == ref.tobytes()

@@ -148,7 +148,19 @@ ZWork bind_ws(void *ws)
     w.walk_err = (uint32_t *)(p + 4);
     w.ticket = (uint32_t *)(p + 8);
     w.status = (uint64_t *)(p + 16);
+    w.lb_spin = LB_SPIN_LIMIT;
     return w;
+}
+
+/* Test hook: with ZCCL_GPU_TEST_STALL_TILE0=1 in the environment a
+ * compression hands out tiles from 1 on, so tile 0 never publishes its size
+ * and its successor's look-back must give up, after 4096 polls instead of
+ * the usual limit.  The call then reports ZCCL_GPU_ETIMEOUT; nothing waits
+ * without bound on the way. */
+bool test_stall_tile0()
+{
+    const char *v = getenv("ZCCL_GPU_TEST_STALL_TILE0");
+    return v && v[0] == '1' && v[1] == 0;
 }
 
 int status_of_bits(uint32_t bits)
@@ -271,6 +283,13 @@ static int compress_fmt(zccl_gpu_stream *out, const float *d_in, size_t n, float
     a.wt = width_table();
     a.sm = compress_smem(g);
     if (ws_clear(d_ws, g, st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    if (test_stall_tile0()) {
+        static const uint32_t one = 1;
+        if (cudaMemcpyAsync(a.w.ticket, &one, 4, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            return ZCCL_GPU_ECUDA;
+        a.w.lb_spin = 4096;
+    }
     int rc = cuda_status(launch_compress(a, st));
     if (rc == ZCCL_GPU_OK) {
         out->indexed = 1;

@@ -4,13 +4,13 @@
  *   quantize*()          bit-exact stand-ins for (int)((double)x * (double)inv)
  *   width_of()           bit-exact stand-in for (int)log2f((float)m) + 1
  *   encode_full/decode_full   one 32-element block, registers <-> packed bytes
+ *   encode_small/decode_small/decode_add_full   the same for widths below 16
  *   encode_any/decode_any     any block, one element at a time
  *   Packer / Reader      MSB-first bit streams in shared memory
  *   tma_load_superset()  TMA bulk copy global -> shared
  *   store_realign()      shared -> global at any byte alignment
  *   cta_excl_scan()      block-wide exclusive scan
  *   lb_publish/resolve   single-pass decoupled look-back across tiles
- *   lb_resolve_cta       the same look-back with every warp of the CTA
  */
 #ifndef ZCCL_GB300_ZDEV_CUH
 #define ZCCL_GB300_ZDEV_CUH
@@ -226,6 +226,52 @@ __device__ __forceinline__ void encode_full(uint32_t sbase, uint32_t o, uint32_t
     pk.finish();
 }
 
+/* encode_full for a width of 1..15 bits (B = b/8 <= 1 whole byte per
+ * magnitude), the common case at the error bounds the collectives use, with
+ * whole words instead of the bit packer where the layout allows: the header
+ * and the four sign bytes as one 40-bit little-endian value placed at byte o
+ * (two word ORs), and for B = 1 the 32 high bytes as eight little-endian
+ * words realigned to their byte offset by funnel shifts (nine word ORs); the
+ * low bits go through the packer as in encode_full.  Same bytes as
+ * encode_full in the fastmode1 layout. */
+__device__ __forceinline__ void encode_small(uint32_t sbase, uint32_t o, uint32_t b, uint32_t smask,
+                                             const uint32_t (&m)[32])
+{
+    const uint32_t B = b >> 3, r = b & 7u;
+    {
+        const uint32_t q = o >> 2, s8 = (o & 3u) * 8u;
+        const uint64_t v = ((uint64_t)bswap32(smask) << 8 | b) << s8; /* at most 40 + 24 bits */
+        sh_or(sbase + 4u * q, (uint32_t)v);
+        sh_or(sbase + 4u * q + 4u, (uint32_t)(v >> 32));
+    }
+    const uint32_t hb = o + 5u;
+    if (B) {
+        const uint32_t q = hb >> 2, sh = (hb & 3u) * 8u;
+        uint32_t prev = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t lo2 = __byte_perm(m[4 * k] >> r, m[4 * k + 1] >> r, 0x0040u);
+            const uint32_t hi2 = __byte_perm(m[4 * k + 2] >> r, m[4 * k + 3] >> r, 0x0040u);
+            const uint32_t W = __byte_perm(lo2, hi2, 0x5410u); /* bytes of elements 4k .. 4k + 3 */
+            sh_or(sbase + 4u * (q + (uint32_t)k), __funnelshift_l(prev, W, sh));
+            prev = W;
+        }
+        if (sh) sh_or(sbase + 4u * (q + 8u), prev >> (32u - sh));
+    }
+    if (r) {
+        const uint32_t p = 1u << r, mask = p - 1u;
+        Packer pk;
+        pk.init(sbase, hb + 32u * B);
+#pragma unroll
+        for (int j = 0; j < 32; j += 4) {
+            const uint32_t v0 = m[j] & mask, v1 = m[j + 1] & mask, v2 = m[j + 2] & mask, v3 = m[j + 3] & mask;
+            pk.put(((v0 * p + v1) * p + v2) * p + v3, 4u * r);
+            pk.flush();
+        }
+        pk.finish();
+    }
+}
+
 /* Bytes a .. a + 7 of the shared words w as a 64-bit big-endian value
  * (hi: bytes a .. a + 3).  Reads the three words that hold them. */
 __device__ __forceinline__ void be64_at(const uint32_t *w, uint32_t a, uint32_t &hi, uint32_t &lo)
@@ -324,6 +370,114 @@ __device__ __forceinline__ uint32_t decode_full(const uint32_t *w, uint32_t o, u
         }
     }
     return sum;
+}
+
+/* decode_full for a fastmode1 block of width 0..15 (B <= 1), the same
+ * instructions for every such width so that a warp whose blocks mix one- and
+ * zero-byte magnitudes does not split: the high byte of element 8g + k is
+ * byte k of the realigned words of group g, replaced by zero when B = 0; its
+ * r low bits are field k of the group's r-byte window; the sign mask comes as
+ * in decode_full.  Returns the wrapped sum of the deltas. */
+__device__ __forceinline__ uint32_t decode_small(const uint32_t *w, uint32_t o, uint32_t b, uint32_t (&d)[32])
+{
+    if (b == 0) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) d[j] = 0;
+        return 0;
+    }
+    const uint32_t B = b >> 3, r = b & 7u;
+    uint32_t sg, unused;
+    be64_at(w, o + 1, sg, unused);
+    const uint32_t hb = o + 5, lb = hb + 32u * B;
+    const uint32_t k0 = hb >> 2, sh = (hb & 3u) * 8u;
+    const uint32_t zsel = B ? 0u : 4u; /* selector nibble 4..7: a byte of the zero operand */
+    uint32_t tk[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) tk[k] = sg << k; /* element 8g + k's sign: top bit of byte 3 - g */
+    const uint32_t r1 = r, r2 = 2u * r, r3 = 3u * r;
+    uint32_t prev = w[k0], sum = 0;
+#pragma unroll
+    for (int g = 0; g < 4; g++) {
+        const uint32_t n1 = w[k0 + 2 * g + 1], n2 = w[k0 + 2 * g + 2];
+        const uint32_t A0 = __funnelshift_r(prev, n1, sh), A1 = __funnelshift_r(n1, n2, sh);
+        prev = n2;
+        uint32_t hi, lo;
+        be64_at(w, lb + (uint32_t)g * r, hi, lo);
+        const uint32_t h2 = __funnelshift_l(lo, hi, 4u * r); /* fields 4 .. 7 on top */
+        const uint32_t sel = 0x1111u * (8u | (3u - (uint32_t)g));
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t A = k < 4 ? A0 : A1;
+            const uint32_t H = __byte_perm(A, 0, 0x4440u | (uint32_t)(k & 3) | zsel);
+            const uint32_t src = k < 4 ? hi : h2;
+            const uint32_t s1 = (k & 3) == 0 ? 0u : (k & 3) == 1 ? r1 : (k & 3) == 2 ? r2 : r3;
+            const uint32_t m = __funnelshift_l(src << s1, H, r);
+            const uint32_t s = prmt_sign(tk[k], sel); /* all ones when negative */
+            d[8 * g + k] = (m ^ s) - s;
+            sum += d[8 * g + k];
+        }
+    }
+    return sum;
+}
+
+/* The deltas of a fastmode1 block of width b at byte o added into acc
+ * (acc[j] += delta j), for the homomorphic add.  Widths 1..15 take the
+ * width-uniform path of decode_small; 16..32 read two to four whole bytes per
+ * magnitude group by group, so that no second array of 32 values is live. */
+__device__ __forceinline__ void decode_add_full(const uint32_t *w, uint32_t o, uint32_t b, uint32_t (&acc)[32])
+{
+    if (b == 0) return;
+    const uint32_t B = b >> 3, r = b & 7u;
+    uint32_t sg, unused;
+    be64_at(w, o + 1, sg, unused);
+    if (b >= 16) {
+        const uint32_t hb = o + 5, lb = hb + 32u * B;
+        const uint32_t bmask = B >= 4 ? 0xFFFFFFFFu : (1u << (8u * B)) - 1u;
+#pragma unroll
+        for (int g = 0; g < 4; g++) {
+            uint32_t hi = 0, lo = 0;
+            be64_at(w, lb + (uint32_t)g * r, hi, lo);
+            const uint32_t h2 = __funnelshift_l(lo, hi, 4u * r);
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const uint32_t a = hb + (uint32_t)(8 * g + k) * B; /* element 8g + k's little-endian bytes */
+                const uint32_t H = __funnelshift_r(w[a >> 2], w[(a >> 2) + 1], (a & 3u) * 8u) & bmask;
+                const uint32_t src = k < 4 ? hi : h2;
+                const uint32_t m = __funnelshift_l(src << ((uint32_t)(k & 3) * r), H, r);
+                const uint32_t s = (uint32_t)((int32_t)(sg << (8 * g + k)) >> 31); /* all ones when negative */
+                acc[8 * g + k] += (m ^ s) - s;
+            }
+        }
+        return;
+    }
+    const uint32_t hb = o + 5, lb = hb + 32u * B;
+    const uint32_t k0 = hb >> 2, sh = (hb & 3u) * 8u;
+    const uint32_t zsel = B ? 0u : 4u;
+    uint32_t tk[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) tk[k] = sg << k;
+    const uint32_t r1 = r, r2 = 2u * r, r3 = 3u * r;
+    uint32_t prev = w[k0];
+#pragma unroll
+    for (int g = 0; g < 4; g++) {
+        const uint32_t n1 = w[k0 + 2 * g + 1], n2 = w[k0 + 2 * g + 2];
+        const uint32_t A0 = __funnelshift_r(prev, n1, sh), A1 = __funnelshift_r(n1, n2, sh);
+        prev = n2;
+        uint32_t hi, lo;
+        be64_at(w, lb + (uint32_t)g * r, hi, lo);
+        const uint32_t h2 = __funnelshift_l(lo, hi, 4u * r);
+        const uint32_t sel = 0x1111u * (8u | (3u - (uint32_t)g));
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t A = k < 4 ? A0 : A1;
+            const uint32_t H = __byte_perm(A, 0, 0x4440u | (uint32_t)(k & 3) | zsel);
+            const uint32_t src = k < 4 ? hi : h2;
+            const uint32_t s1 = (k & 3) == 0 ? 0u : (k & 3) == 1 ? r1 : (k & 3) == 2 ? r2 : r3;
+            const uint32_t m = __funnelshift_l(src << s1, H, r);
+            const uint32_t s = prmt_sign(tk[k], sel);
+            acc[8 * g + k] += (m ^ s) - s;
+        }
+    }
 }
 
 /* Any block (n elements, any width), one element at a time: separate
@@ -686,6 +840,9 @@ __device__ __forceinline__ uint32_t cta_excl_scan(uint32_t v, uint32_t *wsum, ui
  * so every tile a CTA waits on belongs to a CTA that is already running and
  * never waits on a later tile.
  * ------------------------------------------------------------------- */
+/* Polls of a predecessor's word before the look-back gives up (about a
+ * second at the 32 ns back-off; callers may pass a smaller limit). */
+#define LB_SPIN_LIMIT (1u << 22)
 #define LB_FLAG_A (1ull << 62)
 #define LB_FLAG_P (2ull << 62)
 #define LB_VAL (LB_FLAG_A - 1ull)
@@ -736,7 +893,8 @@ __device__ __forceinline__ void lb_publish(uint64_t *status, uint64_t tile, uint
  * number of polls: ZERR_TIMEOUT is set, the missing value counts as 0 and
  * the inclusive value is still published, so successors never hang. */
 static __device__ __noinline__ uint64_t lb_resolve(uint64_t *status, uint64_t tile, uint64_t agg,
-                                                   bool first, uint64_t start, uint32_t *err)
+                                                   bool first, uint64_t start, uint32_t *err,
+                                                   uint32_t spin_limit = LB_SPIN_LIMIT)
 {
     const uint32_t lane = threadIdx.x & 31u;
     if (first) return start;
@@ -768,7 +926,7 @@ static __device__ __noinline__ uint64_t lb_resolve(uint64_t *status, uint64_t ti
             }
         }
         if (pending) {
-            if (++spins < (1u << 22)) {
+            if (++spins < spin_limit) {
                 __nanosleep(32);
                 continue;
             }
@@ -788,86 +946,6 @@ static __device__ __noinline__ uint64_t lb_resolve(uint64_t *status, uint64_t ti
         spins = 0;
     }
     if (lane == 0) st_flag(status + tile, LB_FLAG_P | ((prefix + agg) & LB_VAL));
-    return prefix & LB_VAL;
-}
-
-/* lb_resolve for all threads of the CTA at once: warp w inspects the 256
- * predecessors from distance 256w + 1 on, so one round covers 256 per warp
- * (1024 with four warps), and the warps' findings are combined nearest
- * first through rec (two words per warp of shared scratch).  Every thread
- * returns the same prefix; thread 0 publishes the inclusive value.  The
- * same bounded wait as lb_resolve. */
-static __device__ __forceinline__ uint64_t lb_resolve_cta(uint64_t *status, uint64_t tile, uint64_t agg,
-                                                       bool first, uint64_t start, uint32_t *err,
-                                                       uint64_t *rec)
-{
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (first) return start;
-    uint64_t prefix = 0;
-    int64_t pos = (int64_t)tile - 1 - 256 * (int64_t)warp;
-    uint32_t spins = 0;
-    for (;;) {
-        uint64_t v[8];
-#pragma unroll
-        for (int k = 0; k < 8; k++) {
-            int64_t idx = pos - (int64_t)(lane + 32u * k);
-            v[k] = idx >= 0 ? ld_flag(status + idx) : LB_FLAG_P; /* before tile 0: value 0 */
-        }
-        uint32_t kp = 8, fp = 31, pending = 0;
-#pragma unroll
-        for (int k = 0; k < 8; k++) {
-            const uint32_t flag = (uint32_t)(v[k] >> 62);
-            const uint32_t pm = __ballot_sync(0xffffffffu, flag == 2u);
-            const uint32_t xm = __ballot_sync(0xffffffffu, flag == 0u);
-            if (kp == 8) {
-                if (pm) {
-                    kp = k;
-                    fp = (uint32_t)(__ffs(pm) - 1);
-                    pending |= xm & ((1u << fp) - 1u);
-                } else {
-                    pending |= xm;
-                }
-            }
-        }
-        uint64_t c = 0;
-#pragma unroll
-        for (int k = 0; k < 8; k++) {
-            const bool ready = (v[k] >> 62) != 0;
-            if ((uint32_t)k < kp || ((uint32_t)k == kp && lane <= fp))
-                c += ready ? (v[k] & LB_VAL) : 0ull;
-        }
-        c = warp_sum_u64(c);
-        if (lane == 0) {
-            rec[2 * warp] = c;
-            rec[2 * warp + 1] = (kp < 8 ? 1u : 0u) | (pending ? 2u : 0u);
-        }
-        __syncthreads();
-        uint64_t sum = 0;
-        bool found = false, pend = false;
-        for (uint32_t w = 0; w < nw; w++) {
-            const uint64_t st = rec[2 * w + 1];
-            sum += rec[2 * w];
-            pend |= (st & 2u) != 0;
-            if (st & 1u) {
-                found = true;
-                break;
-            }
-        }
-        __syncthreads(); /* rec is rewritten by the next round */
-        if (pend) {
-            if (++spins < (1u << 22)) {
-                __nanosleep(32);
-                continue;
-            }
-            /* give up: missing values count as 0 */
-            if (threadIdx.x == 0) atomicOr(err, ZERR_TIMEOUT);
-        }
-        prefix += sum;
-        if (found) break;
-        pos -= 256 * (int64_t)nw;
-        spins = 0;
-    }
-    if (threadIdx.x == 0) st_flag(status + tile, LB_FLAG_P | ((prefix + agg) & LB_VAL));
     return prefix & LB_VAL;
 }
 

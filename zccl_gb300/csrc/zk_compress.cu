@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
     if (tid >= NC) { /* the placer warp */
         const uint64_t max_tiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
         placer_loop(
-            ring, outb, pj, a.w.err, max_tiles, bad, true,
+            ring, outb, pj, a.w.err, max_tiles, bad, true, a.w.lb_spin,
             [&](uint64_t k) {
                 if (lane == 0) ring_wait(&ring->packed, (uint32_t)k + 1, a.w.err);
             },
@@ -368,7 +368,10 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
         const uint32_t o = headb + off;
         if (FAST) {
             if (n == 32) {
-                encode_full(pk_sa, o, b, smask, m, g.fmt);
+                if (b && b < 16 && g.fmt == ZG_FASTMODE1)
+                    encode_small(pk_sa, o, b, smask, m);
+                else
+                    encode_full(pk_sa, o, b, smask, m, g.fmt);
             } else if (own) {
                 encode_any(
                     pk_sa, o, b, n,

@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(256, 3) k_decompress_jobs(const __grid_constan
     float *rows = reinterpret_cast<float *>(smem + a.sm.rows);
     uint8_t *buf = smem + a.sm.in0;
 
-    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, nw = blockDim.x >> 5;
+    const uint32_t tid = threadIdx.x;
     const uint32_t L = a.job.g.L, stride = zg_row_stride(L); /* one L for the whole batch */
     uint32_t bad = 0;
     if (*(volatile const uint32_t *)a.w.walk_err) return;
@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(256, 3) k_decompress_jobs(const __grid_constan
         uint32_t bsum = 0;
         if (own && buf[o] != b) bad |= ZERR_CORRUPT;
         if (full) {
-            bsum = decode_full(sw, o, b, d, g.fmt);
+            bsum = g.fmt == ZG_FASTMODE1 && b < 16 ? decode_small(sw, o, b, d) : decode_full(sw, o, b, d, g.fmt);
         } else if (own) {
             decode_any(sw, o, b, n, [&](uint32_t, uint32_t v) { bsum += v; }, g.fmt);
         }
@@ -143,14 +143,32 @@ __global__ void __launch_bounds__(256, 3) k_decompress_jobs(const __grid_constan
             const float h = __fmul_rn(__int2float_rn(head), eb);
             J.y[z.seg_start] = acc ? __fadd_rn(J.y[z.seg_start], h) : h;
         }
-        for (uint32_t k = warp; k < z.nblk; k += nw) {
-            const uint32_t nk = zg_block_len(z.seg_len, L, z.blk0 + k);
-            float *dst = J.y + z.e_first + (uint64_t)k * L;
-            if (acc) {
-                for (uint32_t j = lane; j < nk; j += 32) dst[j] = __fadd_rn(dst[j], rows[k * stride + j]);
-            } else {
-                for (uint32_t j = lane; j < nk; j += 32) dst[j] = rows[k * stride + j];
+        /* the tile's floats are contiguous after the head: element i is row
+         * i / L, column i % L, and a warp's 32 consecutive i share one row
+         * when L = 32 */
+        const uint32_t cnt = (uint32_t)(z.e_end - z.e_first);
+        float *dst = J.y + z.e_first;
+        const uint32_t nt = blockDim.x;
+        if (acc) {
+            /* the destination's floats are read 16 per thread ahead of the
+             * adds, so that the loads overlap instead of each waiting for
+             * the one before */
+            constexpr uint32_t U = 16;
+            for (uint32_t i0 = 0; i0 < cnt; i0 += U * nt) {
+                float v[U];
+#pragma unroll
+                for (uint32_t u = 0; u < U; u++) {
+                    const uint32_t i = i0 + u * nt + tid;
+                    v[u] = i < cnt ? dst[i] : 0.f;
+                }
+#pragma unroll
+                for (uint32_t u = 0; u < U; u++) {
+                    const uint32_t i = i0 + u * nt + tid;
+                    if (i < cnt) dst[i] = __fadd_rn(v[u], rows[(i / L) * stride + i % L]);
+                }
             }
+        } else {
+            for (uint32_t i = tid; i < cnt; i += nt) dst[i] = rows[(i / L) * stride + i % L];
         }
     }
     if (bad) atomicOr(a.w.err, bad);

@@ -43,13 +43,13 @@ __device__ __forceinline__ const HomAddJob &job_of(const HomAddArgs &a, uint32_t
  * look-back always progresses. */
 template <bool FAST>
 __device__ __forceinline__ void loader_loop(const HomAddArgs &a, uint8_t *buf0, uint8_t *buf1, HStage *stage,
-                                            uint32_t *btab0, uint32_t *btab1, uint64_t *full, uint64_t *empty,
-                                            uint32_t &bad)
+                                            HTile *td, uint32_t *btab0, uint32_t *btab1, uint64_t *full,
+                                            uint64_t *empty, uint32_t &bad)
 {
     const uint32_t lane = threadIdx.x & 31u;
     const uint64_t ntiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
     uint32_t seq = 0; /* copies handed over so far */
-    for (;;) {
+    for (uint32_t ti = 0;; ti++) {
         uint64_t t = 0, tk = 0;
         uint32_t j = 0;
         if (lane == 0) {
@@ -97,6 +97,21 @@ __device__ __forceinline__ void loader_loop(const HomAddArgs &a, uint8_t *buf0, 
             const uint32_t total = __shfl_sync(0xffffffffu, incl, 31) + (z.has_head ? 4u : 0u);
             const uint32_t s = seq & 1u;
             if (seq >= 2) mbar_wait(&empty[s], ((seq >> 1) + 1u) & 1u, a.w.err); /* copy seq - 2 consumed */
+            if (p == 0 && lane == 0) { /* the tile's record, before its first copy is handed over */
+                HTile &d = td[ti % ZH_TILE_RECS];
+                uint32_t qsum = 0;
+                if (J.qprev_valid)
+                    for (uint32_t q = 0; q < P; q++) qsum += (uint32_t)J.in[q].tile_qprev[t];
+                d.gblk0 = z.gblk0;
+                d.widths = J.idx.widths;
+                d.tile_qprev = J.qprev_valid ? J.idx.tile_qprev : nullptr;
+                d.status = J.status;
+                d.P = P;
+                d.nblk = z.nblk;
+                d.nlast = z.nblk ? zg_block_len(z.seg_len, J.g.L, z.blk0 + z.nblk - 1) : 0u;
+                d.has_head = z.has_head;
+                d.qsum = qsum;
+            }
 #pragma unroll
             for (int k = 0; k < 8; k++) {
                 const uint32_t i = 8u * lane + (uint32_t)k;
@@ -139,7 +154,8 @@ __global__ void __launch_bounds__(320, 2) k_homadd(const __grid_constant__ HomAd
     ZRing4 *ring = reinterpret_cast<ZRing4 *>(smem + 320);
     ZPlace *pj = reinterpret_cast<ZPlace *>(smem + a.sm.jobs);
     HStage *stage = reinterpret_cast<HStage *>(smem + a.sm.jobs + zg_a16(sizeof(ZPlace))); /* [2] */
-    uint32_t *const btab0 = reinterpret_cast<uint32_t *>(stage + 2), *const btab1 = btab0 + a.job.g.TB;
+    HTile *td = reinterpret_cast<HTile *>(stage + 2); /* [ZH_TILE_RECS] */
+    uint32_t *const btab0 = reinterpret_cast<uint32_t *>(td + ZH_TILE_RECS), *const btab1 = btab0 + a.job.g.TB;
     uint32_t *acc_rows = reinterpret_cast<uint32_t *>(smem + a.sm.rows);
     uint8_t *outs = smem + a.sm.out; /* the ring of packed sums */
     uint8_t *const buf0 = smem + a.sm.in0, *const buf1 = smem + a.sm.in1;
@@ -164,7 +180,7 @@ __global__ void __launch_bounds__(320, 2) k_homadd(const __grid_constant__ HomAd
 
     if (warp == nwc) { /* the placer warp */
         const uint64_t max_tiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;
-        placer_loop4(ring, outs, pj, a.w.err, max_tiles, bad, [&](uint32_t j, ZPlace *p) {
+        placer_loop4(ring, outs, pj, a.w.err, max_tiles, bad, a.w.lb_spin, [&](uint32_t j, ZPlace *p) {
                 const HomAddJob &J = job_of(a, j);
                 p->g = J.g;
                 p->out = J.out;
@@ -176,7 +192,7 @@ __global__ void __launch_bounds__(320, 2) k_homadd(const __grid_constant__ HomAd
         return;
     }
     if (warp == nwc + 1) { /* the loader warp */
-        loader_loop<FAST>(a, buf0, buf1, stage, btab0, btab1, full, empty, bad);
+        loader_loop<FAST>(a, buf0, buf1, stage, td, btab0, btab1, full, empty, bad);
         if (bad) atomicOr(a.w.err, bad);
         return;
     }
@@ -195,13 +211,11 @@ __global__ void __launch_bounds__(320, 2) k_homadd(const __grid_constant__ HomAd
             break;
         }
         const uint32_t job = stage[s].job;
-        const HomAddJob &J = job_of(a, job);
-        const ZGeom &g = J.g;
-        const uint32_t P = J.P;
-        ZTile z;
-        zg_tile(&g, tile, &z);
-        const bool own = tid < z.nblk;
-        const uint32_t n = own ? zg_block_len(z.seg_len, L, z.blk0 + tid) : 0u;
+        const HTile &D = td[it % ZH_TILE_RECS];
+        const uint32_t P = D.P, nblk = D.nblk;
+        const bool has_head = D.has_head != 0;
+        const bool own = tid < nblk;
+        const uint32_t n = !own ? 0u : tid + 1u < nblk ? L : D.nlast;
         const bool full32 = FAST && own && n == 32;
         if (FAST) {
 #pragma unroll
@@ -209,17 +223,16 @@ __global__ void __launch_bounds__(320, 2) k_homadd(const __grid_constant__ HomAd
         } else if (own) {
             for (uint32_t j = 0; j < n; j++) acc_rows[tid * stride + j] = 0;
         }
-        uint32_t hsum = 0, qsum = 0, nzmask = 0;
-        const uint32_t headb = z.has_head ? 4u : 0u;
+        uint32_t hsum = 0, nzmask = 0;
+        const uint32_t headb = has_head ? 4u : 0u;
 
         for (uint32_t p = 0; p < P; p++, seq++) {
             s = seq & 1u;
             if (p) mbar_wait(&full[s], (seq >> 1) & 1u, a.w.err);
-            if (J.qprev_valid && tid == 0) qsum += (uint32_t)J.in[p].tile_qprev[tile];
             const uint8_t *buf = s ? buf1 : buf0;
             const uint32_t *sw = reinterpret_cast<const uint32_t *>(buf);
             const uint32_t ph = stage[s].ph;
-            if (z.has_head && tid == 0) {
+            if (has_head && tid == 0) {
                 uint32_t h = 0;
 #pragma unroll
                 for (int k = 0; k < 4; k++) h |= (uint32_t)buf[ph + k] << (8 * k);
@@ -231,10 +244,7 @@ __global__ void __launch_bounds__(320, 2) k_homadd(const __grid_constant__ HomAd
                 if (b) {
                     nzmask |= 1u << (p & 31);
                     if (full32) {
-                        uint32_t v[32];
-                        decode_full(sw, o, b, v);
-#pragma unroll
-                        for (int j = 0; j < 32; j++) acc[j] += v[j];
+                        decode_add_full(sw, o, b, acc);
                     } else if (FAST) {
                         decode_any(sw, o, b, n, [&](uint32_t j, uint32_t v) { add_at(acc, j, v); });
                     } else {
@@ -266,7 +276,7 @@ __global__ void __launch_bounds__(320, 2) k_homadd(const __grid_constant__ HomAd
             uint32_t mx = 0;
 #pragma unroll
             for (int j = 0; j < 32; j++) {
-                smask = (smask << 1) | (acc[j] >> 31);
+                smask = __funnelshift_l(acc[j], smask, 1); /* (smask << 1) | sign of element j */
                 acc[j] = (uint32_t)abs((int32_t)acc[j]);
                 mx = max(mx, acc[j]);
             }
@@ -284,10 +294,10 @@ __global__ void __launch_bounds__(320, 2) k_homadd(const __grid_constant__ HomAd
         uint32_t total;
         const uint32_t off = grp_excl_scan1(size, (it & 1u) ? wsum1 : wsum0, &total, NC, 1);
         total += headb;
-        if (warp == 0) lb_publish(J.status, tile, total, tile == 0, 0);
+        if (warp == 0) lb_publish(D.status, tile, total, tile == 0, 0);
         if (tid == 0) ring4_sized(ring, it, tile, job, total, a.w.err); /* the placer's look-back starts */
-        if (own) J.idx.widths[z.gblk0 + tid] = (uint8_t)b;
-        if (tid == 0 && J.qprev_valid) J.idx.tile_qprev[tile] = (int32_t)qsum;
+        if (own) D.widths[D.gblk0 + tid] = (uint8_t)b;
+        if (tid == 0 && D.tile_qprev) D.tile_qprev[tile] = (int32_t)D.qsum;
 
         /* room for the packed sum in the ring: every thread finds the same
          * place and waits, if need be, for the placer to have written out
@@ -296,10 +306,13 @@ __global__ void __launch_bounds__(320, 2) k_homadd(const __grid_constant__ HomAd
         const uint32_t pos = ring4_space(ring, zg_ring_need(total), R, H, hp, mend, a.w.err);
         uint8_t *pk = outs + pos;
         const uint32_t pk_sa = smem_u32(pk);
-        if (z.has_head && tid == 0) *reinterpret_cast<uint32_t *>(pk) = hsum;
+        if (has_head && tid == 0) *reinterpret_cast<uint32_t *>(pk) = hsum;
         const uint32_t o = headb + off;
         if (full32) {
-            encode_full(pk_sa, o, b, smask, acc);
+            if (b && b < 16)
+                encode_small(pk_sa, o, b, smask, acc);
+            else
+                encode_full(pk_sa, o, b, smask, acc);
         } else if (own) {
             encode_any(pk_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
                 const uint32_t v = FAST ? pick(acc, j) : acc_rows[tid * stride + j];

@@ -21,6 +21,7 @@ struct ZWork {
     uint32_t *walk_err; /* ZERR_* bits of the index walk that ran before, if any */
     uint32_t *ticket;   /* next tile to hand out */
     uint64_t *status;   /* decoupled look-back state, one word per tile */
+    uint32_t lb_spin;   /* polls before a look-back wait gives up */
 };
 
 /* Side index of a resident stream: enough to find every block without
@@ -129,6 +130,24 @@ struct HStage {
     uint32_t pad[3];
 };
 
+/* What the adding warps need of a claimed tile, written by the loader with
+ * the tile's first input so that the adders read shared memory instead of
+ * the job in device or parameter memory.  ZH_TILE_RECS records, by tile
+ * count: the loader runs at most two input copies ahead of the adders, so a
+ * record is reused only after its tile is packed. */
+struct HTile {
+    uint64_t gblk0;      /* first block of the tile in its stream */
+    uint8_t *widths;     /* the sum's width index */
+    int32_t *tile_qprev; /* the sum's tile starting values, or null */
+    uint64_t *status;    /* the sum's look-back words */
+    uint32_t P, nblk;
+    uint32_t nlast;      /* elements of the tile's last block */
+    uint32_t has_head;   /* tile 0 of its segment */
+    uint32_t qsum;       /* the inputs' starting values of the tile, summed */
+    uint32_t pad[3];
+};
+#define ZH_TILE_RECS 4u
+
 struct HomAddArgs {
     HomAddJob job; /* the single job (batch.jobs == null) */
     ZBatch batch;
@@ -175,43 +194,7 @@ size_t walk_w1_warp_bytes(uint32_t M);
 
 /* Grid of a persistent kernel: every CTA that fits on the device at once,
  * but no more CTAs than tiles. */
-/* A packed tile in shared memory waiting for its place in the stream. */
-struct ZPending {
-    uint64_t tile;  /* ZP_NONE when there is none (uniform over the CTA) */
-    uint32_t total; /* its bytes */
-    uint32_t b;     /* this thread's block width */
-    uint32_t q;     /* thread 0: quantized value before the tile, for the index */
-};
-#define ZP_NONE (~0ull)
-
-/* All threads of the CTA: find the pending tile's byte offset with the
- * CTA-wide look-back, write its side-index entries (and its segment's chunk
- * offset when it opens a segment), and store its bytes from s_out.  The
- * caller synchronises before s_out is reused. */
-__device__ __forceinline__ void place_tile(const ZGeom &g, const ZPending &pd, const uint8_t *s_out,
-                                           uint8_t *out, uint64_t cap, const ZIndex &idx, bool write_q,
-                                           uint64_t *status, uint32_t *err, uint64_t *rec,
-                                           uint32_t &bad)
-{
-    const uint64_t prefix = lb_resolve_cta(status, pd.tile, pd.total, pd.tile == 0, 0, err, rec);
-    const uint64_t base = 8ull * g.T + prefix;
-    const bool fits = base + pd.total <= cap; /* uniform over the CTA */
-    if (!fits) bad |= ZERR_CAPACITY;
-    ZTile z;
-    zg_tile(&g, pd.tile, &z);
-    if (threadIdx.x < z.nblk) idx.widths[z.gblk0 + threadIdx.x] = (uint8_t)pd.b;
-    if (threadIdx.x == 0) {
-        idx.tile_off[pd.tile] = base;
-        if (write_q) idx.tile_qprev[pd.tile] = (int32_t)pd.q;
-        if (fits && z.has_head && z.seg < g.T) {
-            const uint64_t h = base - 8ull * g.T;
-#pragma unroll
-            for (int k = 0; k < 8; k++) out[8ull * z.seg + k] = (uint8_t)(h >> (8 * k));
-        }
-        if (pd.tile == g.ntiles - 1) *idx.size = base + pd.total;
-    }
-    if (fits) store_realign(out + base, s_out, pd.total);
-}
+#define ZP_NONE (~0ull) /* no more tiles */
 
 /* ------------------------------------------------------------------
  * Hand-off of packed tiles from the compute warps to the placer warp.
@@ -375,10 +358,12 @@ struct ZPlace {
 };
 
 /* Shared bytes of the homomorphic add's job region: the placer's job, two
- * stage records and two block tables (offset << 8 | width per block). */
+ * stage records, the tile records and two block tables (offset << 8 |
+ * width per block). */
 static inline uint32_t homadd_job_bytes(uint32_t TB)
 {
-    return zg_a16((uint32_t)sizeof(ZPlace)) + 2u * (uint32_t)sizeof(HStage) + 2u * TB * 4u;
+    return zg_a16((uint32_t)sizeof(ZPlace)) + 2u * (uint32_t)sizeof(HStage) + ZH_TILE_RECS * (uint32_t)sizeof(HTile) +
+           2u * TB * 4u;
 }
 
 
@@ -392,8 +377,8 @@ static inline uint32_t homadd_job_bytes(uint32_t TB)
  * back to zero once written out, so the packers find zeroed space. */
 template <class Wait, class Fetch>
 __device__ __forceinline__ void placer_loop(ZRing *ring, uint8_t *ringb, ZPlace *pj, uint32_t *err,
-                                            uint64_t max_tiles, uint32_t &bad, bool zero, Wait wait_packed,
-                                            Fetch fetch)
+                                            uint64_t max_tiles, uint32_t &bad, bool zero, uint32_t spin,
+                                            Wait wait_packed, Fetch fetch)
 {
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t cur_job = 0xFFFFFFFFu;
@@ -411,7 +396,7 @@ __device__ __forceinline__ void placer_loop(ZRing *ring, uint8_t *ringb, ZPlace 
             cur_job = job;
         }
         const ZGeom &g = pj->g;
-        const uint64_t base = 8ull * g.T + lb_resolve(pj->status, t, total, t == 0, 0, err);
+        const uint64_t base = 8ull * g.T + lb_resolve(pj->status, t, total, t == 0, 0, err, spin);
         const bool fits = base + total <= pj->cap;
         if (!fits) bad |= ZERR_CAPACITY;
         if (lane == 0) {
@@ -441,7 +426,7 @@ __device__ __forceinline__ void placer_loop(ZRing *ring, uint8_t *ringb, ZPlace 
  * packed its bytes go out and its ring bytes are zeroed and released. */
 template <class Fetch>
 __device__ __forceinline__ void placer_loop4(ZRing4 *r, uint8_t *ringb, ZPlace *pj, uint32_t *err,
-                                             uint64_t max_tiles, uint32_t &bad, Fetch fetch)
+                                             uint64_t max_tiles, uint32_t &bad, uint32_t spin, Fetch fetch)
 {
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t cur_job = 0xFFFFFFFFu;
@@ -457,7 +442,7 @@ __device__ __forceinline__ void placer_loop4(ZRing4 *r, uint8_t *ringb, ZPlace *
             cur_job = job;
         }
         const ZGeom &g = pj->g;
-        const uint64_t base = 8ull * g.T + lb_resolve(pj->status, t, total, t == 0, 0, err);
+        const uint64_t base = 8ull * g.T + lb_resolve(pj->status, t, total, t == 0, 0, err, spin);
         const bool fits = base + total <= pj->cap;
         if (!fits) bad |= ZERR_CAPACITY;
         if (lane == 0) {
