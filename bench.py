@@ -13,7 +13,8 @@ value  = uncompressed bytes handled per second, 3 * 4N per step (GB/s), the
          reference's own convention (one input's bytes per operation),
          device-resident inputs, CUDA events on the launching stream.
 e2e    = the same step through the reference-facing C-ABI entry points with
-         host buffers (host->device and device->host copies inside).
+         host buffers in pinned memory (host->device and device->host copies
+         inside); e2e.pageable_value the same with ordinary pageable arrays.
 roofline: algorithmic bytes of the dominant kernel per launch over its mean
          event-timed duration, against the measured HBM copy bandwidth.
 cpu_baseline: the oracle's C restatement of the reference codec with every
@@ -67,7 +68,8 @@ def parse():
     p.add_argument("--batch-pairs", type=int, default=2048, help="buffer pairs (batched)")
     p.add_argument("--serve-side", type=int, default=400, help="side of the serving field")
     p.add_argument("--serve-slots", type=int, default=4)
-    p.add_argument("--serve-secs", type=float, default=0.4, help="arrival window per load point")
+    p.add_argument("--serve-secs", type=float, default=2.0, help="arrival window per load point")
+    p.add_argument("--serve-max", type=int, default=60000, help="most requests per load point")
     return p.parse_args()
 
 
@@ -359,9 +361,11 @@ def reduction_bench(args, L, T, dev):
     out = codec.new_stream()
     ms_compress = timed(lambda: [codec.compress(x, eb, out=s) for x, s in zip(xs, streams)], 3, st)
     ms_pway = timed(lambda: reduce_homomorphic(codec, streams, out=out), 5, st)
-    ms_pair = timed(lambda: reduce_pairwise(codec, streams), 3, st)
+    pair_outs = [codec.new_stream(), codec.new_stream()]
+    ms_pair = timed(lambda: reduce_pairwise(codec, streams, pair_outs), 5, st)
     docs = codec.new_stream()
-    ms_doc = timed(lambda: reduce_doc(codec, streams, eb, out=docs), 3, st)
+    doc_total = torch.empty(n, dtype=torch.float32, device=dev)
+    ms_doc = timed(lambda: reduce_doc(codec, streams, eb, out=docs, total=doc_total), 5, st)
     codec.check()
     same = reduce_homomorphic(codec, streams, out=out).tobytes() == reduce_pairwise(codec, streams).tobytes()
     exact = torch.zeros(n, dtype=torch.float64, device=dev)
@@ -647,12 +651,17 @@ def serving_bench(args, L, dev):
     """Poisson arrivals: 50 % compress, 30 % decompress, 20 % homomorphic
     add of 2-8 resident streams; sizes log-uniform 64 KB - 256 MB of float32
     cut from a log-normal GRF (as the 512^3 field, at 400^3); eb = 1e-4 *
-    range; 120 GB admission budget.  The peak is the throughput of a closed
-    burst; offered load sweeps 10 % - 120 % of it, reporting achieved
-    throughput and p50 / p99 latency per point."""
+    range; 120 GB admission budget (inputs, outputs and scratch counted).
+    The peak is the saturated open-loop throughput: arrivals offered far
+    faster than the device serves them for serve_secs.  The sweep then
+    offers 10 % - 200 % of the peak, serve_secs of arrivals per point (at
+    most serve_max requests), and reports achieved throughput, p50 / p99
+    latency, the device overlap of units and the host's enqueue time per
+    point; max_sustained is the highest load served at >= 95 % of the
+    offered rate."""
     import numpy as np
     import torch
-    from zccl_gb300.serve import COMPRESS, DECOMPRESS, HOMADD, Request, Server, percentile
+    from zccl_gb300.serve import COMPRESS, DECOMPRESS, HOMADD, Request, Server, device_overlap, percentile
     field = make_field(args.serve_side, 5, dev)
     nf = field.numel()
     eb = float(np.float32(1e-4 * float(field.max() - field.min())))
@@ -685,7 +694,7 @@ def serving_bench(args, L, dev):
         return Request(t, rid[0], HOMADD, ins=[keys[int(k)] for k in rng.choice(8, P, replace=False)]), 4 * n * P
 
     def serve(reqs):
-        srv.log = []
+        srv.log, srv.units, srv.max_inflight, srv.host_launch_s = [], [], 0, 0.0
         base = srv.now()
         for q, _ in reqs:
             q.arrival += base
@@ -694,28 +703,50 @@ def serving_bench(args, L, dev):
         nbytes = sum(b for _, b in reqs)
         span = max(q.done for q in log) - min(q.arrival for q in log)
         lat = [1e3 * (q.done - q.arrival) for q in log]
-        return nbytes / span / 1e9, percentile(lat, 50), percentile(lat, 99), len(log)
+        ov = device_overlap(srv.units)
+        return {"GBps": nbytes / span / 1e9, "p50": percentile(lat, 50), "p99": percentile(lat, 99),
+                "count": len(log), "span_s": span, "overlap": ov, "max_inflight": srv.max_inflight,
+                "host_launch_frac": srv.host_launch_s / span}
 
-    serve([make(0.0) for _ in range(60)])  # warm-up: allocator, first launches
-    peak, b50, b99, _ = serve([make(0.0) for _ in range(400)])
-    mean_b = float(np.mean([make(0.0)[1] for _ in range(4000)]))
-    points = []
-    for load in (0.1, 0.25, 0.5, 0.75, 0.9, 1.0, 1.2):
-        lam = load * peak * 1e9 / mean_b  # requests per second
+    def arrivals(rate_gbs, secs, cap):
+        lam = rate_gbs * 1e9 / mean_b  # requests per second
         t, reqs = 0.0, []
-        while t < args.serve_secs and len(reqs) < 600:
+        while t < secs and len(reqs) < cap:
             t += float(rng.exponential(1.0 / lam))
             reqs.append(make(t))
-        thr, p50, p99, cnt = serve(reqs)
-        points.append({"offered_frac": load, "offered_GBps": round(load * peak, 1), "achieved_GBps": round(thr, 1),
-                       "p50_ms": round(p50, 3), "p99_ms": round(p99, 3), "requests": cnt})
-    sustained = [p for p in points if p["achieved_GBps"] >= 0.9 * p["offered_GBps"]]
+        return reqs
+
+    serve([make(0.0) for _ in range(60)])  # warm-up: allocator, first launches
+    burst = serve([make(0.0) for _ in range(400)])
+    mean_b = float(np.mean([make(0.0)[1] for _ in range(4000)]))
+    # saturation: offered at four times the closed burst's rate
+    sat = serve(arrivals(4.0 * burst["GBps"], args.serve_secs, args.serve_max))
+    peak = sat["GBps"]
+    points = []
+    for load in (0.1, 0.25, 0.5, 0.75, 0.9, 1.0, 1.2, 1.5, 2.0):
+        reqs = arrivals(load * peak, args.serve_secs, args.serve_max)
+        r = serve(reqs)
+        points.append({"offered_frac": load, "offered_GBps": round(load * peak, 1), "achieved_GBps": round(r["GBps"], 1),
+                       "p50_ms": round(r["p50"], 3), "p99_ms": round(r["p99"], 3), "requests": r["count"],
+                       "arrival_s": round(reqs[-1][0].arrival - reqs[0][0].arrival if len(reqs) > 1 else 0.0, 3),
+                       "device_busy_frac": round(r["overlap"]["busy_ms"] / (1e3 * r["span_s"]), 3),
+                       "device_overlap_ms": round(r["overlap"]["overlap_ms"], 2),
+                       "max_units_in_flight": r["max_inflight"],
+                       "host_launch_frac": round(r["host_launch_frac"], 3)})
+        if load >= 1.0 and r["GBps"] < 0.95 * load * peak:
+            break
+    sustained = [p for p in points if p["achieved_GBps"] >= 0.95 * p["offered_GBps"]]
     res = {
         "workload": "Poisson arrivals, 50% compress / 30% decompress / 20% homomorphic add of 2-8 resident "
                     f"streams, log-uniform 64 KB-256 MB float32 from a {args.serve_side}^3 log-normal GRF, "
                     f"eb=1e-4*range, 120 GB budget, {args.serve_slots} slots, continuous batching",
-        "peak_GBps_closed_burst": round(peak, 1),
-        "burst_p50_ms": round(b50, 3), "burst_p99_ms": round(b99, 3),
+        "peak_GBps_saturated": round(peak, 1),
+        "saturated": {"offered_GBps": round(4.0 * burst["GBps"], 1), "requests": sat["count"],
+                      "p50_ms": round(sat["p50"], 3), "p99_ms": round(sat["p99"], 3),
+                      "max_units_in_flight": sat["max_inflight"],
+                      "device_busy_frac": round(sat["overlap"]["busy_ms"] / (1e3 * sat["span_s"]), 3),
+                      "host_launch_frac": round(sat["host_launch_frac"], 3)},
+        "closed_burst_GBps": round(burst["GBps"], 1),
         "sweep": points,
         "max_sustained": sustained[-1] if sustained else None,
         "bytes_counted": "uncompressed input floats: 4n (compress, decompress), 4n*P (add)",
@@ -806,33 +837,44 @@ def run_ours(args, rank, world, local_rank):
                 "unit": "GB/s", "frac": per_op[dom]["roofline_frac"], "traffic": traffic,
                 "kernel": dom, "peak_source": f"{peak_kind} hbm_gbs"}
 
-    # e2e through the reference-facing entry points with host buffers
-    xh, yh = x.cpu().numpy(), y.cpu().numpy()
+    # e2e through the reference-facing entry points with host buffers: the
+    # fields, streams and floats in pinned host memory (a caller's MPI
+    # buffers), then the same step once more on ordinary pageable arrays
     Z.set_omp_threads(T)
     cap = max(4 * n, codec.max_stream_bytes)
-    hs_a = np.zeros(cap, np.uint8)
-    hs_b = np.zeros(cap, np.uint8)
-    hs_s = np.zeros(cap, np.uint8)
-    hy = np.zeros(n, np.float32)
-    Z.ZCCL_float_openmp_threadblock_arg(hs_b, yh, 0, eb, n, L)
 
-    def e2e_step():
-        size = Z.ZCCL_float_openmp_threadblock_arg(hs_a, xh, 0, eb, n, L)
-        Z.ZCCL_float_decompress_openmp_threadblock_arg(hy, n, eb, L, hs_a)
-        Z.ZCCL_float_homomophic_add_openmp_threadblock(hs_s, 0, n, eb, L, hs_a, hs_b)
-        return size
+    def host_array(count, dtype, pinned):
+        if pinned:
+            return torch.zeros(count, dtype=dtype, pin_memory=True).numpy()
+        return np.zeros(count, {torch.float32: np.float32, torch.uint8: np.uint8}[dtype])
 
-    e2e_step()
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
+    def e2e_run(pinned):
+        xh, yh = host_array(n, torch.float32, pinned), host_array(n, torch.float32, pinned)
+        xh[:], yh[:] = x.cpu().numpy(), y.cpu().numpy()
+        bufs = [host_array(cap, torch.uint8, pinned) for _ in range(3)] + [host_array(n, torch.float32, pinned)]
+        hs_a, hs_b, hs_s, hy = bufs
+        Z.ZCCL_float_openmp_threadblock_arg(hs_b, yh, 0, eb, n, L)
+
+        def e2e_step():
+            Z.ZCCL_float_openmp_threadblock_arg(hs_a, xh, 0, eb, n, L)
+            Z.ZCCL_float_decompress_openmp_threadblock_arg(hy, n, eb, L, hs_a)
+            Z.ZCCL_float_homomophic_add_openmp_threadblock(hs_s, 0, n, eb, L, hs_a, hs_b)
+
         e2e_step()
-    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-    sa_host = hs_a[:ca].tobytes()
-    rd_a = host_read_bytes(sa_host, n, L, T)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        return (time.perf_counter() - t0) / args.e2e_steps, xh, yh, bufs
+
+    e2e_s, xh, yh, (hs_a, hs_b, hs_s, hy) = e2e_run(True)
+    e2e_pageable_s = e2e_run(False)[0]
+    rd_a = host_read_bytes(hs_a[:ca].tobytes(), n, L, T)
     rd_b = host_read_bytes(hs_b[:cb].tobytes(), n, L, T)
     e2e = {"value": round(world * 3 * 4 * n / e2e_s / 1e9, 3), "unit": "GB/s",
            "h2d_bytes_per_step": 4 * n + 2 * rd_a + rd_b,
            "d2h_bytes_per_step": ca + 4 * n + cs,
+           "host_memory": "pinned",
+           "pageable_value": round(world * 3 * 4 * n / e2e_pageable_s / 1e9, 3),
            "api": "ZCCL_float_openmp_threadblock_arg / _decompress_ / _homomophic_add_ (host)"}
 
     cpu, ref_out = None, None

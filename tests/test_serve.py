@@ -123,3 +123,50 @@ def test_budget_holds_requests_back(torch):
     assert len(log) == len(reqs) and srv.in_use == 0
     for q in reqs:
         assert served(q) == alone(torch, srv, q), (q.kind, q.rid)
+
+
+@pytest.mark.gpu
+def test_units_overlap_on_the_device(torch):
+    """Units on different slots run at the same time on the device: three
+    8-way sums of 32M-element streams arriving together, one per slot, are
+    all incomplete on the device at some enqueue, and their device intervals
+    (start and end events) overlap.  The budget counts each unit's output and
+    scratch, and every byte is returned."""
+    from zccl_gb300.serve import HOMADD, Request, Server, device_overlap
+    n = 1 << 25
+    t = torch.arange(n, dtype=torch.float32, device="cuda")
+    base = torch.sin(t * 1e-4) + 0.01 * torch.sin(t * 0.37)
+    eb = float(np.float32(1e-4 * 2.0))
+    srv = Server(8 << 30, slots=3, batching=False)
+    keys = []
+    for r in range(8):
+        srv.put(r, torch.roll(base, 1000 * r), eb, 1)
+        keys.append(r)
+    del t
+    for warm in range(2):  # the first pass grows the slots' scratch
+        srv.units, srv.max_inflight, srv.log = [], 0, []
+        for i in range(3):
+            srv.submit(Request(0.0, 10 * warm + i, HOMADD, ins=keys))
+        log = srv.run()
+    assert len(log) == 3 and srv.in_use == 0
+    ov = device_overlap(srv.units)
+    assert srv.max_inflight >= 2, srv.max_inflight
+    assert ov["max_concurrent"] >= 2 and ov["overlap_ms"] > 0, ov
+
+
+def test_device_overlap_arithmetic():
+    """Busy time, time with two units running and the peak concurrency, from
+    start and end marks (event stand-ins)."""
+    from zccl_gb300.serve import device_overlap
+
+    class Mark:
+        def __init__(self, t):
+            self.t = t
+
+        def elapsed_time(self, other):
+            return other.t - self.t
+
+    units = [(Mark(0.0), Mark(10.0), None), (Mark(5.0), Mark(12.0), None), (Mark(20.0), Mark(21.0), None)]
+    ov = device_overlap(units)
+    assert ov == {"span_ms": 21.0, "busy_ms": 13.0, "overlap_ms": 5.0, "max_concurrent": 2}
+    assert device_overlap([])["max_concurrent"] == 0

@@ -143,24 +143,27 @@ class RingAllreduce:
         return self._allgather_decompress(self.reduced, eb, per_rank_outputs)
 
     # ---- one batch per step ----------------------------------------------
-    def _buffers(self):
-        """The ring's own streams and floats, made once: the P x P chunk
-        streams and a spare stream per rank (homomorphic), P float
-        accumulators, P message streams and P reduced streams (DOC), and the
-        result."""
+    def _buffers(self, variant: str):
+        """The ring's own streams and floats for one variant, made on its
+        first run: the P x P chunk streams and a spare stream per rank
+        ("ho"), or P float accumulators, P message streams and P reduced
+        streams ("doc"); and the variant's result."""
         import torch
         if self._bufs is None:
+            self._bufs = {}
+        b = self._bufs.get(variant)
+        if b is None:
             P = self.P
-            self._bufs = {
-                "S": [[self.codec(c).new_stream() for c in range(P)] for _ in range(P)],
-                "spare": [self.codec(c).new_stream() for c in range(P)],
-                "acc": [torch.empty(self.count, dtype=torch.float32, device=self.device) for _ in range(P)],
-                "msg": [self.codec(c).new_stream() for c in range(P)],
-                "red": [self.codec(c).new_stream() for c in range(P)],
-                "y_ho": torch.empty(self.count, dtype=torch.float32, device=self.device),
-                "y_doc": torch.empty(self.count, dtype=torch.float32, device=self.device),
-            }
-        return self._bufs
+            if variant == "ho":
+                b = {"S": [[self.codec(c).new_stream() for c in range(P)] for _ in range(P)],
+                     "spare": [self.codec(c).new_stream() for c in range(P)]}
+            else:
+                b = {"acc": [torch.empty(self.count, dtype=torch.float32, device=self.device) for _ in range(P)],
+                     "msg": [self.codec(c).new_stream() for c in range(P)],
+                     "red": [self.codec(c).new_stream() for c in range(P)]}
+            b["y"] = torch.empty(self.count, dtype=torch.float32, device=self.device)
+            self._bufs[variant] = b
+        return b
 
     def _plan(self, key, kind, jobs):
         b = self._plans.get(key)
@@ -179,7 +182,7 @@ class RingAllreduce:
             b.run()
             self._check([b])
             return ys
-        y = self._buffers()["y_" + tag]
+        y = self._buffers(tag)["y"]
         self._plan((tag, "gather", eb), BATCH_DECOMPRESS,
                    [(reduced[c], eb, self.T, self._chunk(y, c), False) for c in range(P)]).run()
         self._check()
@@ -187,7 +190,7 @@ class RingAllreduce:
 
     def _homomorphic_batched(self, xs, eb, per_rank_outputs):
         P = self.P
-        B = self._buffers()
+        B = self._buffers("ho")
         S = [row[:] for row in B["S"]]
         spare = B["spare"][:]
         key = ("ho", "compress", eb, tuple(x.data_ptr() for x in xs))
@@ -210,7 +213,7 @@ class RingAllreduce:
 
     def _doc_batched(self, xs, eb, per_rank_outputs):
         P = self.P
-        B = self._buffers()
+        B = self._buffers("doc")
         acc, msg, red = B["acc"], B["msg"], B["red"]
         for a, x in zip(acc, xs):
             a.copy_(x)
@@ -237,19 +240,26 @@ def reduce_homomorphic(codec: Codec, streams: list[DeviceStream], out: DeviceStr
     return codec.homadd(streams, out=out)
 
 
-def reduce_pairwise(codec: Codec, streams: list[DeviceStream]):
+def reduce_pairwise(codec: Codec, streams: list[DeviceStream], outs: list[DeviceStream] | None = None):
     """The same sum folded pairwise, as the ring's P - 1 steps do
-    (acc = received + acc, ZCCL/src/ZCCL_ring_ho.c:281-287)."""
+    (acc = received + acc, ZCCL/src/ZCCL_ring_ho.c:281-287).  With outs (two
+    streams) the partial sums alternate between them instead of new ones."""
     acc = streams[0]
-    for s in streams[1:]:
-        acc = codec.homadd([s, acc])
+    for i, s in enumerate(streams[1:]):
+        acc = codec.homadd([s, acc], out=outs[i & 1] if outs else None)
     return acc
 
 
-def reduce_doc(codec: Codec, streams: list[DeviceStream], eb: float, out: DeviceStream | None = None):
-    """Decompress every chunk, add the floats in rank order, recompress."""
+def reduce_doc(codec: Codec, streams: list[DeviceStream], eb: float, out: DeviceStream | None = None,
+               total=None):
+    """Decompress every chunk, add the floats in rank order, recompress: the
+    first chunk decompressed, each later one decompressed and added in one
+    pass (the float sum of MPI_Reduce_local, ZCCL/src/ZCCL_ring.c:1074-1076).
+    total, if given, is the float buffer to use."""
     import torch
-    total = torch.zeros(codec.n, dtype=torch.float32, device=codec.device)
-    for s in streams:
-        total.add_(codec.decompress(s, eb))
+    if total is None:
+        total = torch.empty(codec.n, dtype=torch.float32, device=codec.device)
+    codec.decompress(streams[0], eb, out=total)
+    for s in streams[1:]:
+        codec.decompress_accumulate(s, eb, total)
     return codec.compress(total, eb, out=out), total

@@ -12,6 +12,14 @@ slots overlaps on the device; a request's latency runs from its arrival to
 the completion event of the launch that carried it, and its bytes and slot
 are released then.
 
+The admission budget counts everything a request holds on the device while
+it is in flight: its input floats (compress), its outputs (stream and side
+index, or floats) and the scratch of its geometry.  Geometry sizes are
+cached per shape, and released output buffers go back to a per-shape pool,
+so admission makes no library size queries or allocator calls for shapes it
+has seen.  Every unit of work is bracketed by device events, so the device
+time of each unit and the overlap between units can be read back.
+
 Results do not depend on the mix: every stream is the reference's byte
 layout for its own input, and batching or concurrency changes only which
 launch carries the work.
@@ -61,7 +69,7 @@ class Server:
     device memory stays within the budget over a long run."""
 
     def __init__(self, budget_bytes: int, slots: int = 4, L: int = 32, device: str = "cuda",
-                 batching: bool = True, keep_results: bool = False):
+                 batching: bool = True, keep_results: bool = False, pool_bytes: int = 1 << 30):
         import torch
         self.torch = torch
         self.L, self.device, self.batching, self.keep = int(L), device, batching, keep_results
@@ -74,20 +82,59 @@ class Server:
         self.inflight: list = []  # (event, slot, [requests], keep-alive objects)
         self.t0 = time.perf_counter()
         self.log: list = []
+        self._sizes: dict = {}    # (n, T) -> (stream capacity, index bytes, workspace bytes)
+        self._pool: dict = {}     # (n, T) -> released (buf, idx) pairs, oldest shape first
+        self._pool_bytes, self._pool_cap = 0, int(pool_bytes)
+        self.units: list = []     # (start event, end event, requests) of every unit launched
+        self.max_inflight = 0     # most units incomplete on the device at one enqueue
+        self.host_launch_s = 0.0  # host time spent enqueueing units
 
     # ---- resident buffers -------------------------------------------------
+    def _size(self, n: int, T: int):
+        """(stream capacity, index bytes, workspace bytes) of a geometry, cached."""
+        key = (n, T)
+        v = self._sizes.get(key)
+        if v is None:
+            v = (lib().zccl_gpu_max_stream_bytes(n, self.L, T), lib().zccl_gpu_index_bytes(n, self.L, T),
+                 lib().zccl_gpu_workspace_bytes(n, self.L, T))
+            if not v[0] or not v[1]:
+                raise ZcclError(-1, f"geometry n={n} T={T}")
+            self._sizes[key] = v
+        return v
+
     def _stream_for(self, n: int, T: int):
         torch = self.torch
-        cap = lib().zccl_gpu_max_stream_bytes(n, self.L, T)
-        ib = lib().zccl_gpu_index_bytes(n, self.L, T)
-        if not cap or not ib:
-            raise ZcclError(-1, f"geometry n={n} T={T}")
-        buf = torch.empty(cap, dtype=torch.uint8, device=self.device)
-        idx = torch.zeros(ib, dtype=torch.uint8, device=self.device)
+        cap, ib, _ = self._size(n, T)
+        pool = self._pool.get((n, T))
+        if pool:
+            buf, idx = pool.pop()
+            self._pool_bytes -= cap + ib
+        else:
+            buf = torch.empty(cap, dtype=torch.uint8, device=self.device)
+            idx = torch.zeros(ib, dtype=torch.uint8, device=self.device)
         return buf, idx, StreamDesc(buf.data_ptr(), cap, idx.data_ptr(), 0, 0)
 
+    def _release(self, res) -> None:
+        """Give a handed-back result's stream buffers to the pool, which
+        keeps at most pool_bytes (the oldest shapes leave first)."""
+        if not isinstance(res, Resident):
+            return
+        cap, ib, _ = self._size(res.n, res.T)
+        if cap + ib > self._pool_cap:
+            return
+        while self._pool_bytes + cap + ib > self._pool_cap:
+            key = next(iter(self._pool))
+            lst = self._pool[key]
+            c, i, _ = self._size(*key)
+            lst.pop()
+            self._pool_bytes -= c + i
+            if not lst:
+                del self._pool[key]
+        self._pool.setdefault((res.n, res.T), []).append((res.buf, res.index))
+        self._pool_bytes += cap + ib
+
     def _workspace(self, slot: int, n: int, T: int):
-        need = lib().zccl_gpu_workspace_bytes(n, self.L, T)
+        need = self._size(n, T)[2]
         ws = self.ws[slot]
         if ws is None or ws.numel() < need:
             ws = self.torch.zeros(need, dtype=self.torch.uint8, device=self.device)
@@ -112,28 +159,36 @@ class Server:
 
     def submit(self, req: Request) -> None:
         """Queue a request; one that could never fit the budget is refused."""
-        if self._out_bytes(req) > self.budget:
+        if self._bytes(req) > self.budget:
             raise ValueError(f"request {req.rid} needs more than the {self.budget}-byte budget")
         heapq.heappush(self.queue, (req.arrival, req.rid, req))
 
-    def _out_bytes(self, req: Request) -> int:
+    def _bytes(self, req: Request) -> int:
+        """Device bytes the request holds while in flight: its input floats
+        (compress), its outputs and the scratch of its geometry."""
         if req.kind == COMPRESS:
             n, T = req.x.numel(), req.T
-        else:
-            r = self.store[req.ins[0]]
-            n, T = r.n, r.T
-            if req.kind == DECOMPRESS:
-                return 4 * n
-        return lib().zccl_gpu_max_stream_bytes(n, self.L, T) + lib().zccl_gpu_index_bytes(n, self.L, T)
+            cap, ib, ws = self._size(n, T)
+            return 4 * n + cap + ib + ws
+        r = self.store[req.ins[0]]
+        cap, ib, ws = self._size(r.n, r.T)
+        if req.kind == DECOMPRESS:
+            return 4 * r.n + ws
+        return cap + ib + ws
 
     def _launch(self, slot: int, reqs: list) -> None:
         """Enqueue one unit of work (a batch or a lone request) on a slot."""
+        h0 = time.perf_counter()
         torch = self.torch
         st = self.streams[slot]
         sp = ctypes.c_void_p(st.cuda_stream)
         keep = []
         kind = reqs[0].kind
+        busy = sum(1 for u in self.inflight if not u[0].query())
+        self.max_inflight = max(self.max_inflight, busy + 1)
         with torch.cuda.stream(st):
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev0.record(st)
             if kind == DECOMPRESS or len(reqs) == 1:
                 for q in reqs:
                     if q.kind == COMPRESS:
@@ -179,9 +234,11 @@ class Server:
                 b = Batch(BATCH_HOMADD, jobs, self.L, stream=st)
                 b.run(st)
                 keep.append(b)
-            ev = torch.cuda.Event()
+            ev = torch.cuda.Event(enable_timing=True)
             ev.record(st)
         self.inflight.append((ev, slot, reqs, keep))
+        self.units.append((ev0, ev, reqs))
+        self.host_launch_s += time.perf_counter() - h0
 
     def _retire(self) -> None:
         still = []
@@ -198,6 +255,7 @@ class Server:
                     q.done = t
                     self.in_use -= q.nbytes
                     if not self.keep:  # the result has been handed back: its memory is free
+                        self._release(q.result)
                         q.result, q.x = None, None
                     self.log.append(q)
                 self.free_slots.append(slot)
@@ -213,7 +271,7 @@ class Server:
             # the head and, with batching, every other arrived request of its kind that fits
             while self.queue and self.queue[0][0] <= now:
                 _, _, q = heapq.heappop(self.queue)
-                need = self._out_bytes(q)
+                need = self._bytes(q)
                 if q.kind == kind and self.in_use + need <= self.budget and \
                         (not group or (self.batching and kind != DECOMPRESS)):
                     q.nbytes = need
@@ -239,6 +297,34 @@ class Server:
         self.torch.cuda.synchronize()
         self._retire()
         return self.log
+
+
+def device_overlap(units) -> dict:
+    """Device timeline of completed units (start and end events, as
+    Server.units holds them): the span from the first start to the last end,
+    the busy time (at least one unit running), the time with two or more
+    running, and the most running at once."""
+    if not units:
+        return {"span_ms": 0.0, "busy_ms": 0.0, "overlap_ms": 0.0, "max_concurrent": 0}
+    ref = units[0][0]
+    marks = []
+    for e0, e1, _ in units:
+        a, b = ref.elapsed_time(e0), ref.elapsed_time(e1)
+        marks.append((a, 1))
+        marks.append((b, -1))
+    marks.sort(key=lambda m: (m[0], m[1]))
+    busy = over = 0.0
+    cur = top = 0
+    prev = marks[0][0]
+    for t, d in marks:
+        if cur >= 1:
+            busy += t - prev
+        if cur >= 2:
+            over += t - prev
+        cur += d
+        top = max(top, cur)
+        prev = t
+    return {"span_ms": marks[-1][0] - marks[0][0], "busy_ms": busy, "overlap_ms": over, "max_concurrent": top}
 
 
 def percentile(vals, p):
