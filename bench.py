@@ -622,6 +622,8 @@ def batched_bench(args, L, dev):
         bc.run(side)
         bh.run(side)
     ms_batch = timed(gb.replay, 5, st)
+    ms_bc = timed(lambda: bc.run(st), 5, st)
+    ms_bh = timed(lambda: bh.run(st), 5, st)
     bc.check()
     bh.check()
     unc = 4 * total
@@ -636,6 +638,8 @@ def batched_bench(args, L, dev):
         "speedup_vs_per_buffer_eager": round(ms_eager / ms_batch, 2),
         "speedup_vs_per_buffer_graph": round(ms_graph_per / ms_batch, 2),
         "batched_GBps_uncompressed": round(unc / (ms_batch * 1e-3) / 1e9, 1),
+        "compress_batch_ms": round(ms_bc, 3),
+        "homadd_batch_ms": round(ms_bh, 3),
         "launches": {"batched": 2, "per_buffer": 3 * npairs},
         "autotuned_grid": {"compress": grid_c, "homadd": grid_h},
         "outputs_equal_sampled": same,

@@ -419,3 +419,43 @@ def test_lookback_wait_gives_up_and_reports_timeout(torch, monkeypatch):
     again = codec.compress(x, 1e-4)
     codec.check()
     assert again.tobytes() == ref.tobytes()
+
+
+@pytest.mark.parametrize("T,extra", [(16, 0), (16, 9), (7, 3), (3, 0)])
+def test_host_dropins_pipelined_by_chunk_groups(port, torch, T, extra):
+    """Host buffers of 2^22 floats and more go through the pipelined drop-ins
+    (groups of chunks copied in, coded and copied out on three streams).
+    Their streams, floats and sums are the oracle's: remainder segments that
+    force the last group to hold several chunks, pageable and pinned
+    buffers, and the sum written over its second input as the ring does."""
+    n = (1 << 22) + extra
+    L = 32
+    rng = np.random.default_rng(T + extra)
+    t = np.arange(n, dtype=np.float64)
+    x = (np.sin(t * 1e-3) + rng.normal(0, 0.01, n)).astype(np.float32)
+    y = (np.cos(t * 7e-4) + rng.normal(0, 0.01, n)).astype(np.float32)
+    eb = float(np.float32(2e-4))
+    sx, sy = port.compress(x, eb, L, T), port.compress(y, eb, L, T)
+    dx = port.decompress(sx, n, eb, L, T)
+    sxy = port.homadd(sx, sy, n, eb, L, T)
+    Z.set_omp_threads(T)
+    cap = 4 * n + 8 * T + 4096
+
+    def host(count, dtype, pinned):
+        if pinned:
+            return torch.zeros(count, dtype=dtype, pin_memory=True).numpy()
+        return np.zeros(count, {torch.float32: np.float32, torch.uint8: np.uint8}[dtype])
+
+    for pinned in (False, True):
+        xh = host(n, torch.float32, pinned)
+        xh[:] = x
+        hs = host(cap, torch.uint8, pinned)
+        size = Z.ZCCL_float_openmp_threadblock_arg(hs, xh, 0, eb, n, L)
+        assert hs[:size].tobytes() == sx, (T, extra, pinned)
+        out = host(n, torch.float32, pinned)
+        Z.ZCCL_float_decompress_openmp_threadblock_arg(out, n, eb, L, hs)
+        assert np.array_equal(out.view(np.uint32), dx.view(np.uint32)), (T, extra, pinned)
+        acc = host(cap, torch.uint8, pinned)
+        acc[: len(sy)] = np.frombuffer(sy, np.uint8)
+        total = Z.ZCCL_float_homomophic_add_openmp_threadblock(acc, 0, n, eb, L, hs, acc)
+        assert total == len(sxy) and acc[:total].tobytes() == sxy, (T, extra, pinned)

@@ -170,3 +170,20 @@ def test_device_overlap_arithmetic():
     ov = device_overlap(units)
     assert ov == {"span_ms": 21.0, "busy_ms": 13.0, "overlap_ms": 5.0, "max_concurrent": 2}
     assert device_overlap([])["max_concurrent"] == 0
+
+
+def test_buffer_pool_stays_bounded():
+    """Released output buffers go to a per-shape pool that keeps at most
+    pool_bytes, dropping the oldest shapes first; a pooled buffer is reused
+    for its shape.  Host-side logic, on stand-in buffers."""
+    from zccl_gb300.serve import Resident, Server
+    srv = Server.__new__(Server)
+    srv._sizes, srv._pool, srv._pool_bytes, srv._pool_cap = {}, {}, 0, 1000
+    srv._size = lambda n, T: (n, 10, 0)  # capacity n, index 10 bytes
+    for n in (100, 200, 300, 100, 400):
+        srv._release(Resident(n, 1.0, 1, object(), object(), None))
+        assert srv._pool_bytes <= 1000
+        assert srv._pool_bytes == sum(srv._size(*k)[0] + 10 for k, v in srv._pool.items() for _ in v)
+    assert (400, 1) in srv._pool and all(v for v in srv._pool.values())
+    srv._release(Resident(2000, 1.0, 1, object(), object(), None))  # larger than the pool: not kept
+    assert (2000, 1) not in srv._pool

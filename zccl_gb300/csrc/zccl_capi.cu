@@ -815,14 +815,40 @@ struct DevBuf {
     }
 };
 
+/* Pinned host memory for small device-to-host reads that must be
+ * asynchronous (sizes and stream headers of the pipelined drop-ins). */
+struct PinBuf {
+    void *p = nullptr;
+    size_t n = 0;
+    int ensure(size_t bytes)
+    {
+        if (bytes <= n) return ZCCL_GPU_OK;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            return ZCCL_GPU_ENOMEM;
+        }
+        n = bytes;
+        return ZCCL_GPU_OK;
+    }
+};
+
+/* Most chunk groups a pipelined drop-in splits a stream into. */
+constexpr uint32_t kMaxGroups = 8;
+
 /* Cached device buffers of the drop-in layer, one set per device. */
 struct DropCtx {
     std::mutex mu;
     cudaStream_t st = nullptr;
     cudaStream_t st2 = nullptr; /* a second input's copy, beside the first one's walk */
+    cudaStream_t st_in = nullptr, st_out = nullptr; /* the pipelined drop-ins' copies */
     cudaEvent_t ev = nullptr;
+    cudaEvent_t ev_in[kMaxGroups] = {}, ev_k[kMaxGroups] = {};
     DevBuf fin, fout, s[3], ix[3], ws;
     DevBuf aux; /* counters read back by the _record entry points */
+    PinBuf pin;
 };
 
 DropCtx *drop_ctx()
@@ -834,9 +860,16 @@ DropCtx *drop_ctx()
     std::lock_guard<std::mutex> lk(gmu);
     if (!ctxs[dev]) {
         DropCtx *c = new DropCtx();
-        if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&c->ev, cudaEventDisableTiming) != cudaSuccess) {
+        bool ok = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaStreamCreateWithFlags(&c->st_in, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaStreamCreateWithFlags(&c->st_out, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaEventCreateWithFlags(&c->ev, cudaEventDisableTiming) == cudaSuccess;
+        for (uint32_t i = 0; ok && i < kMaxGroups; i++)
+            ok = cudaEventCreateWithFlags(&c->ev_in[i], cudaEventDisableTiming) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&c->ev_k[i], cudaEventDisableTiming) == cudaSuccess;
+        if (!ok) {
+            cudaGetLastError();
             delete c;
             return nullptr;
         }
@@ -954,6 +987,368 @@ int stage_stream(DropCtx *c, int slot, const unsigned char *cmp, const ZGeom &g,
     return ZCCL_GPU_OK;
 }
 
+/* ---- pipelined host-buffer drop-ins --------------------------------
+ * A stream's T chunks are independent (chunk t holds segment t, the last
+ * also the remainder segment), and chunks s0 .. s1 - 1 with their offsets
+ * rebased are themselves a valid stream of (s1 - s0) tbs (+ rem) elements
+ * written by s1 - s0 threads: the same segments, the same bytes.  For host
+ * buffers the drop-ins cut a call into such groups of chunks and run, group
+ * by group, the host-to-device copy on one stream, the kernels on a second
+ * and the device-to-host copy on a third, so that the two directions of the
+ * CPU-GPU link and the kernels of neighbouring groups overlap instead of
+ * following one another.  The output bytes are those of the whole-stream
+ * path. */
+
+struct Group {
+    uint32_t s0, s1; /* chunks */
+    uint64_t n, e0;  /* elements, first element */
+    ZGeom g;         /* geometry of the group's stream */
+};
+
+size_t a256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+/* Whether host ranges [a, a + na) and [b, b + nb) share a byte. */
+bool overlaps(const void *a, size_t na, const void *b, size_t nb)
+{
+    const uintptr_t x = (uintptr_t)a, y = (uintptr_t)b;
+    return x < y + nb && y < x + na;
+}
+
+/* The chunk groups of a call on geometry g, or none when the call is not
+ * worth cutting (one chunk, or fewer than 2^22 elements).  The last group
+ * holds more chunks than the remainder segment has elements, so its stream
+ * splits exactly like the whole one's tail. */
+std::vector<Group> chunk_groups(const ZGeom &g)
+{
+    std::vector<Group> out;
+    const uint32_t T = g.T;
+    if (T < 2 || g.n < (1ull << 22)) return out;
+    const uint32_t G = std::min<uint32_t>(T, kMaxGroups);
+    std::vector<uint32_t> cut;
+    for (uint32_t k = 0; k <= G; k++) cut.push_back((uint32_t)((uint64_t)T * k / G));
+    while (cut.size() > 2 && T - cut[cut.size() - 2] <= g.rem) cut.erase(cut.end() - 2);
+    if (cut.size() < 3) return out;
+    for (size_t k = 0; k + 1 < cut.size(); k++) {
+        Group q;
+        q.s0 = cut[k];
+        q.s1 = cut[k + 1];
+        const bool last = q.s1 == T;
+        q.n = (uint64_t)(q.s1 - q.s0) * g.tbs + (last ? g.rem : 0u);
+        q.e0 = (uint64_t)q.s0 * g.tbs;
+        if (make_geom((size_t)q.n, (int)g.L, (int)(q.s1 - q.s0), &q.g) || q.g.tbs != g.tbs ||
+            q.g.rem != (last ? g.rem : 0u)) {
+            out.clear();
+            return out;
+        }
+        q.g.fmt = g.fmt;
+        out.push_back(q);
+    }
+    return out;
+}
+
+size_t max_ws_bytes(const std::vector<Group> &gr)
+{
+    size_t m = 0;
+    for (const Group &q : gr) m = std::max(m, ws_bytes(q.g));
+    return m;
+}
+
+size_t max_index_bytes(const std::vector<Group> &gr)
+{
+    size_t m = 0;
+    for (const Group &q : gr) m = std::max(m, index_layout(q.g).total);
+    return m;
+}
+
+/* Waits for every copy and kernel of a pipelined call, then reads (and
+ * clears) the workspace's status words. */
+int pipe_finish(DropCtx *c, int rc)
+{
+    const bool sync_ok = cudaStreamSynchronize(c->st_in) == cudaSuccess &&
+                         cudaStreamSynchronize(c->st_out) == cudaSuccess;
+    const int rc2 = finish(c, c->ws.p);
+    if (!sync_ok) return ZCCL_GPU_ECUDA;
+    return rc ? rc : rc2;
+}
+
+/* The caller's output stream from the groups' device streams: per group (in
+ * order, as each one's size and header arrive in pinned memory) its chunk
+ * offsets rebased into the caller's header and its chunk bytes copied out.
+ * dev[k] is group k's device stream, cap[k] its capacity, pin + poff[k] its
+ * size and header.  Returns the chunk bytes placed. */
+int pipe_place(DropCtx *c, const std::vector<Group> &gr, uint8_t *const *dev, const size_t *cap,
+               const size_t *poff, unsigned char *out, uint32_t T, uint64_t *placed)
+{
+    const uint8_t *pin = (const uint8_t *)c->pin.p;
+    uint64_t run = 0;
+    for (size_t k = 0; k < gr.size(); k++) {
+        const Group &q = gr[k];
+        if (cudaEventSynchronize(c->ev_k[k]) != cudaSuccess) return ZCCL_GPU_ECUDA;
+        uint64_t size;
+        memcpy(&size, pin + poff[k], 8);
+        const uint64_t hdr = 8ull * (q.s1 - q.s0);
+        if (size < hdr || size > cap[k]) return ZCCL_GPU_ECORRUPT; /* the status words tell why */
+        for (uint32_t i = 0; i < q.s1 - q.s0; i++) {
+            uint64_t e;
+            memcpy(&e, pin + poff[k] + 8 + 8ull * i, 8);
+            e += run;
+            memcpy(out + 8ull * (q.s0 + i), &e, 8);
+        }
+        if (cudaStreamWaitEvent(c->st_out, c->ev_k[k], 0) != cudaSuccess ||
+            cudaMemcpyAsync(out + 8ull * T + run, dev[k] + hdr, size - hdr, cudaMemcpyDeviceToHost, c->st_out) !=
+                cudaSuccess)
+            return ZCCL_GPU_ECUDA;
+        run += size - hdr;
+    }
+    *placed = run;
+    return ZCCL_GPU_OK;
+}
+
+/* Compression of host floats into a host stream, group by group. */
+int pipe_compress(DropCtx *c, unsigned char *out, const float *x, size_t *outSize, float eb, const ZGeom &g,
+                  const std::vector<Group> &gr)
+{
+    const size_t G = gr.size();
+    size_t soff[kMaxGroups + 1] = {0}, poff[kMaxGroups + 1] = {0}, cap[kMaxGroups];
+    for (size_t k = 0; k < G; k++) {
+        cap[k] = (size_t)zg_stream_worst(&gr[k].g);
+        soff[k + 1] = soff[k] + a256(cap[k]);
+        poff[k + 1] = poff[k] + 8 + 8ull * (gr[k].s1 - gr[k].s0);
+    }
+    if (int rc = c->fin.ensure(4 * g.n)) return rc;
+    if (int rc = c->s[0].ensure(soff[G])) return rc;
+    if (int rc = c->ix[0].ensure(max_index_bytes(gr))) return rc;
+    if (int rc = c->ws.ensure(max_ws_bytes(gr))) return rc;
+    if (int rc = c->pin.ensure(poff[G])) return rc;
+    float *fin = (float *)c->fin.p;
+    uint8_t *dev[kMaxGroups];
+    int rc = ZCCL_GPU_OK;
+    for (size_t k = 0; k < G && !rc; k++) {
+        const Group &q = gr[k];
+        dev[k] = (uint8_t *)c->s[0].p + soff[k];
+        if (cudaMemcpyAsync(fin + q.e0, x + q.e0, 4 * q.n, cudaMemcpyHostToDevice, c->st_in) != cudaSuccess ||
+            cudaEventRecord(c->ev_in[k], c->st_in) != cudaSuccess ||
+            cudaStreamWaitEvent(c->st, c->ev_in[k], 0) != cudaSuccess) {
+            rc = ZCCL_GPU_ECUDA;
+            break;
+        }
+        zccl_gpu_stream sub;
+        sub.bytes = dev[k];
+        sub.capacity = cap[k];
+        sub.index = c->ix[0].p;
+        sub.indexed = 0;
+        sub.qprev_valid = 0;
+        if ((rc = compress_fmt(&sub, fin + q.e0, (size_t)q.n, eb, (int)g.L, (int)(q.s1 - q.s0), c->ws.p, c->st,
+                               g.fmt)))
+            break;
+        uint8_t *pin = (uint8_t *)c->pin.p + poff[k];
+        if (cudaMemcpyAsync(pin, c->ix[0].p, 8, cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
+            cudaMemcpyAsync(pin + 8, dev[k], 8ull * (q.s1 - q.s0), cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
+            cudaEventRecord(c->ev_k[k], c->st) != cudaSuccess)
+            rc = ZCCL_GPU_ECUDA;
+    }
+    uint64_t placed = 0;
+    if (!rc) rc = pipe_place(c, gr, dev, cap, poff, out, g.T, &placed);
+    rc = pipe_finish(c, rc);
+    if (rc) return rc;
+    *outSize = (size_t)(8ull * g.T + placed);
+    return ZCCL_GPU_OK;
+}
+
+/* Chunk offsets of a host stream's header (T entries). */
+std::vector<uint64_t> host_header(const unsigned char *cmp, uint32_t T)
+{
+    std::vector<uint64_t> e(T);
+    memcpy(e.data(), cmp, 8ull * T);
+    return e;
+}
+
+/* Bytes of host stream cmp that group q's chunks take: exact for all but
+ * the group holding the last chunk, whose end is not in the header; that
+ * one is read as the whole-stream path reads it (twice the others' average
+ * chunk first, or up to the largest possible size when `full`). */
+bool group_bytes(const ZGeom &g, const std::vector<uint64_t> &e, const Group &q, bool full, uint64_t *len,
+                 bool *capped)
+{
+    *capped = false;
+    const uint32_t T = g.T;
+    if (q.s1 < T) {
+        if (e[q.s1] < e[q.s0]) return false;
+        *len = e[q.s1] - e[q.s0];
+        return true;
+    }
+    const uint64_t last = e[T - 1];
+    if (last < e[q.s0]) return false;
+    const uint64_t known = last - e[q.s0]; /* bytes of the group's chunks before the last */
+    const uint64_t worst = zg_seg_worst(g.tbs, g.L) + zg_seg_worst(g.rem, g.L);
+    uint64_t want = known + worst;
+    if (!full) {
+        const uint64_t guess = known + 2 * (last / (T - 1)) + 65536;
+        if (guess < want) {
+            want = guess;
+            *capped = true;
+        }
+    }
+    *len = want;
+    return true;
+}
+
+/* Decompression of a host stream into host floats, group by group.  *capped
+ * reports whether the last group was read short (an EBOUNDS then calls for
+ * the full read). */
+int pipe_decompress(DropCtx *c, float *y, const unsigned char *cmp, float eb, const ZGeom &g,
+                    const std::vector<Group> &gr, bool full, bool *capped)
+{
+    const size_t G = gr.size();
+    const std::vector<uint64_t> e = host_header(cmp, g.T);
+    uint64_t len[kMaxGroups];
+    size_t soff[kMaxGroups + 1] = {0}, poff[kMaxGroups + 1] = {0};
+    *capped = false;
+    for (size_t k = 0; k < G; k++) {
+        bool cp = false;
+        if (!group_bytes(g, e, gr[k], full, &len[k], &cp)) return ZCCL_GPU_ECORRUPT;
+        *capped |= cp;
+        soff[k + 1] = soff[k] + a256(8ull * (gr[k].s1 - gr[k].s0) + len[k] + 64);
+        poff[k + 1] = poff[k] + 8ull * (gr[k].s1 - gr[k].s0);
+    }
+    if (int rc = c->fout.ensure(4 * g.n)) return rc;
+    if (int rc = c->s[0].ensure(soff[G])) return rc;
+    if (int rc = c->ix[0].ensure(max_index_bytes(gr))) return rc;
+    if (int rc = c->ws.ensure(max_ws_bytes(gr))) return rc;
+    if (int rc = c->pin.ensure(poff[G])) return rc;
+    float *fout = (float *)c->fout.p;
+    uint8_t *pin = (uint8_t *)c->pin.p;
+    const unsigned char *body = cmp + 8ull * g.T;
+    int rc = ZCCL_GPU_OK;
+    for (size_t k = 0; k < G && !rc; k++) {
+        const Group &q = gr[k];
+        const uint32_t Ts = q.s1 - q.s0;
+        uint8_t *dev = (uint8_t *)c->s[0].p + soff[k];
+        for (uint32_t i = 0; i < Ts; i++) { /* the group's own header, its offsets rebased */
+            const uint64_t v = e[q.s0 + i] - e[q.s0];
+            memcpy(pin + poff[k] + 8ull * i, &v, 8);
+        }
+        if (cudaMemcpyAsync(dev, pin + poff[k], 8ull * Ts, cudaMemcpyHostToDevice, c->st_in) != cudaSuccess ||
+            cudaMemcpyAsync(dev + 8ull * Ts, body + e[q.s0], len[k], cudaMemcpyHostToDevice, c->st_in) !=
+                cudaSuccess ||
+            cudaEventRecord(c->ev_in[k], c->st_in) != cudaSuccess ||
+            cudaStreamWaitEvent(c->st, c->ev_in[k], 0) != cudaSuccess) {
+            rc = ZCCL_GPU_ECUDA;
+            break;
+        }
+        zccl_gpu_stream sub;
+        sub.bytes = dev;
+        sub.capacity = 8ull * Ts + len[k];
+        sub.index = c->ix[0].p;
+        sub.indexed = 0;
+        sub.qprev_valid = 0;
+        if ((rc = decompress_fmt(fout + q.e0, &sub, (size_t)q.n, eb, (int)g.L, (int)Ts, c->ws.p, c->st, g.fmt)))
+            break;
+        if (cudaEventRecord(c->ev_k[k], c->st) != cudaSuccess ||
+            cudaStreamWaitEvent(c->st_out, c->ev_k[k], 0) != cudaSuccess ||
+            cudaMemcpyAsync(y + q.e0, fout + q.e0, 4 * q.n, cudaMemcpyDeviceToHost, c->st_out) != cudaSuccess)
+            rc = ZCCL_GPU_ECUDA;
+    }
+    return pipe_finish(c, rc);
+}
+
+/* Two-way homomorphic add of host streams into a host stream, group by
+ * group: both inputs' chunks copied in, walked and added, the sum's chunks
+ * copied out as each group's size arrives. */
+int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned char *cmp1,
+                const unsigned char *cmp2, const ZGeom &g, const std::vector<Group> &gr, bool full, bool *capped)
+{
+    const size_t G = gr.size();
+    const unsigned char *cmp[2] = {cmp1, cmp2};
+    const std::vector<uint64_t> e[2] = {host_header(cmp1, g.T), host_header(cmp2, g.T)};
+    uint64_t len[2][kMaxGroups];
+    size_t ioff[kMaxGroups + 1] = {0}, soff[kMaxGroups + 1] = {0}, poff[kMaxGroups + 1] = {0}, cap[kMaxGroups];
+    *capped = false;
+    for (size_t k = 0; k < G; k++) {
+        const uint64_t Ts = gr[k].s1 - gr[k].s0;
+        for (int i = 0; i < 2; i++) {
+            bool cp = false;
+            if (!group_bytes(g, e[i], gr[k], full, &len[i][k], &cp)) return ZCCL_GPU_ECORRUPT;
+            *capped |= cp;
+        }
+        ioff[k + 1] = ioff[k] + a256(8 * Ts + len[0][k] + 64) + a256(8 * Ts + len[1][k] + 64);
+        cap[k] = (size_t)zg_stream_worst(&gr[k].g);
+        soff[k + 1] = soff[k] + a256(cap[k]);
+        /* pinned: the sum's size and header, then both inputs' rebased headers */
+        poff[k + 1] = poff[k] + 8 + 8 * Ts + 2 * 8 * Ts;
+    }
+    if (int rc = c->s[1].ensure(ioff[G])) return rc;
+    if (int rc = c->s[2].ensure(soff[G])) return rc;
+    const size_t ixb = max_index_bytes(gr);
+    for (int i = 0; i < 3; i++)
+        if (int rc = c->ix[i].ensure(ixb)) return rc;
+    if (int rc = c->ws.ensure(max_ws_bytes(gr))) return rc;
+    if (int rc = c->pin.ensure(poff[G])) return rc;
+    uint8_t *pin = (uint8_t *)c->pin.p;
+    uint8_t *dev[kMaxGroups];
+    int rc = ZCCL_GPU_OK;
+    for (size_t k = 0; k < G && !rc; k++) {
+        const Group &q = gr[k];
+        const uint32_t Ts = q.s1 - q.s0;
+        zccl_gpu_stream in[2], sum;
+        uint8_t *ib = (uint8_t *)c->s[1].p + ioff[k];
+        for (int i = 0; i < 2 && !rc; i++) {
+            uint8_t *h = pin + poff[k] + 8 + 8ull * Ts + 8ull * Ts * i;
+            for (uint32_t j = 0; j < Ts; j++) {
+                const uint64_t v = e[i][q.s0 + j] - e[i][q.s0];
+                memcpy(h + 8ull * j, &v, 8);
+            }
+            if (cudaMemcpyAsync(ib, h, 8ull * Ts, cudaMemcpyHostToDevice, c->st_in) != cudaSuccess ||
+                cudaMemcpyAsync(ib + 8ull * Ts, cmp[i] + 8ull * g.T + e[i][q.s0], len[i][k], cudaMemcpyHostToDevice,
+                                c->st_in) != cudaSuccess)
+                rc = ZCCL_GPU_ECUDA;
+            in[i].bytes = ib;
+            in[i].capacity = 8ull * Ts + len[i][k];
+            in[i].index = c->ix[i].p;
+            in[i].indexed = 0;
+            in[i].qprev_valid = 0;
+            ib += a256(8ull * Ts + len[i][k] + 64);
+        }
+        if (rc || cudaEventRecord(c->ev_in[k], c->st_in) != cudaSuccess ||
+            cudaStreamWaitEvent(c->st, c->ev_in[k], 0) != cudaSuccess) {
+            rc = rc ? rc : ZCCL_GPU_ECUDA;
+            break;
+        }
+        dev[k] = (uint8_t *)c->s[2].p + soff[k];
+        sum.bytes = dev[k];
+        sum.capacity = cap[k];
+        sum.index = c->ix[2].p;
+        sum.indexed = 0;
+        sum.qprev_valid = 0;
+        if (ws_clear(c->ws.p, q.g, c->st) != cudaSuccess) {
+            rc = ZCCL_GPU_ECUDA;
+            break;
+        }
+        if ((rc = walk_stream(&in[0], q.g, c->ws.p, c->st)) || (rc = walk_stream(&in[1], q.g, c->ws.p, c->st)) ||
+            (rc = zccl_gpu_homadd_cases(&sum, in, 2, (size_t)q.n, (int)g.L, (int)Ts, c->ws.p, nullptr, c->st)))
+            break;
+        uint8_t *pk = pin + poff[k];
+        if (cudaMemcpyAsync(pk, c->ix[2].p, 8, cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
+            cudaMemcpyAsync(pk + 8, dev[k], 8ull * Ts, cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
+            cudaEventRecord(c->ev_k[k], c->st) != cudaSuccess)
+            rc = ZCCL_GPU_ECUDA;
+    }
+    /* the sum written over an input (the ring adds into its receive
+     * buffer): no byte goes out before every input byte is in */
+    const size_t out_span = (size_t)zg_stream_worst(&g);
+    const size_t in_span0 = 8ull * g.T + (size_t)(e[0][gr[G - 1].s0] + len[0][G - 1]);
+    const size_t in_span1 = 8ull * g.T + (size_t)(e[1][gr[G - 1].s0] + len[1][G - 1]);
+    if (!rc && (overlaps(out, out_span, cmp1, in_span0) || overlaps(out, out_span, cmp2, in_span1)) &&
+        (cudaEventRecord(c->ev, c->st_in) != cudaSuccess || cudaStreamWaitEvent(c->st_out, c->ev, 0) != cudaSuccess))
+        rc = ZCCL_GPU_ECUDA;
+    uint64_t placed = 0;
+    if (!rc) rc = pipe_place(c, gr, dev, cap, poff, out, g.T, &placed);
+    rc = pipe_finish(c, rc);
+    if (rc) return rc;
+    *out_size += (size_t)(8ull * g.T + placed);
+    return ZCCL_GPU_OK;
+}
+
 int dropin_compress(unsigned char *outputBytes, const float *oriData, size_t *outSize, float eb,
                     size_t n, int L, int T, uint32_t fmt = ZG_FASTMODE1, uint64_t *nz_out = nullptr)
 {
@@ -963,6 +1358,12 @@ int dropin_compress(unsigned char *outputBytes, const float *oriData, size_t *ou
     if (!c) return ZCCL_GPU_ECUDA;
     std::lock_guard<std::mutex> lk(c->mu);
     const float *d_in = oriData;
+    if (!nz_out && !is_device_ptr(oriData) && !is_device_ptr(outputBytes) &&
+        !overlaps(outputBytes, (size_t)zg_stream_worst(&g), oriData, 4 * n)) {
+        g.fmt = fmt;
+        const std::vector<Group> gr = chunk_groups(g);
+        if (!gr.empty()) return pipe_compress(c, outputBytes, oriData, outSize, eb, g, gr);
+    }
     if (!is_device_ptr(oriData)) {
         if (int rc = c->fin.ensure(4 * n)) return rc;
         if (cudaMemcpyAsync(c->fin.p, oriData, 4 * n, cudaMemcpyHostToDevice, c->st) != cudaSuccess)
@@ -1008,8 +1409,19 @@ int dropin_decompress(float *newData, size_t n, float eb, int L, const unsigned 
     DropCtx *c = drop_ctx();
     if (!c) return ZCCL_GPU_ECUDA;
     std::lock_guard<std::mutex> lk(c->mu);
-    if (int rc = c->ws.ensure(ws_bytes(g))) return rc;
     const bool dout = is_device_ptr(newData);
+    if (!dout && !nz_out && !size_out && !is_device_ptr(cmp) &&
+        !overlaps(newData, 4 * n, cmp, (size_t)zg_stream_worst(&g))) {
+        g.fmt = fmt;
+        const std::vector<Group> gr = chunk_groups(g);
+        if (!gr.empty()) {
+            bool capped = false;
+            int rc = pipe_decompress(c, newData, cmp, eb, g, gr, false, &capped);
+            if (rc == ZCCL_GPU_EBOUNDS && capped) rc = pipe_decompress(c, newData, cmp, eb, g, gr, true, &capped);
+            return rc;
+        }
+    }
+    if (int rc = c->ws.ensure(ws_bytes(g))) return rc;
     float *d_out = newData;
     if (!dout) {
         if (int rc = c->fout.ensure(4 * n)) return rc;
@@ -1050,6 +1462,15 @@ int dropin_homadd(unsigned char *final_cmp, size_t *final_size, size_t n, float 
     DropCtx *c = drop_ctx();
     if (!c) return ZCCL_GPU_ECUDA;
     std::lock_guard<std::mutex> lk(c->mu);
+    if (!cases_out && !is_device_ptr(final_cmp) && !is_device_ptr(cmp1) && !is_device_ptr(cmp2)) {
+        const std::vector<Group> gr = chunk_groups(g);
+        if (!gr.empty()) {
+            bool capped = false;
+            int rc = pipe_homadd(c, final_cmp, final_size, cmp1, cmp2, g, gr, false, &capped);
+            if (rc == ZCCL_GPU_EBOUNDS && capped) rc = pipe_homadd(c, final_cmp, final_size, cmp1, cmp2, g, gr, true, &capped);
+            return rc;
+        }
+    }
     if (int rc = c->ws.ensure(ws_bytes(g))) return rc;
     zccl_gpu_stream in[2], out;
     const size_t worst = (size_t)zg_stream_worst(&g);

@@ -109,6 +109,8 @@ class Server:
         if pool:
             buf, idx = pool.pop()
             self._pool_bytes -= cap + ib
+            if not pool:
+                del self._pool[(n, T)]
         else:
             buf = torch.empty(cap, dtype=torch.uint8, device=self.device)
             idx = torch.zeros(ib, dtype=torch.uint8, device=self.device)
@@ -122,12 +124,13 @@ class Server:
         cap, ib, _ = self._size(res.n, res.T)
         if cap + ib > self._pool_cap:
             return
-        while self._pool_bytes + cap + ib > self._pool_cap:
+        while self._pool and self._pool_bytes + cap + ib > self._pool_cap:
             key = next(iter(self._pool))
             lst = self._pool[key]
             c, i, _ = self._size(*key)
-            lst.pop()
-            self._pool_bytes -= c + i
+            if lst:
+                lst.pop()
+                self._pool_bytes -= c + i
             if not lst:
                 del self._pool[key]
         self._pool.setdefault((res.n, res.T), []).append((res.buf, res.index))
