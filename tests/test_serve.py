@@ -187,3 +187,32 @@ def test_buffer_pool_stays_bounded():
     assert (400, 1) in srv._pool and all(v for v in srv._pool.values())
     srv._release(Resident(2000, 1.0, 1, object(), object(), None))  # larger than the pool: not kept
     assert (2000, 1) not in srv._pool
+
+
+def test_admission_takes_the_oldest_kind_in_fifo_order():
+    """Admission moves arrived requests to per-kind queues and forms each
+    unit from the oldest arrived request and the next ones of its kind (up
+    to max_batch, while they fit the budget); decompressions go alone.
+    Host-side logic with a stand-in launch."""
+    from collections import deque
+    from zccl_gb300.serve import COMPRESS, DECOMPRESS, HOMADD, Request, Server
+    srv = Server.__new__(Server)
+    srv.queue, srv.inflight, srv.log = [], [], []
+    srv.ready = {COMPRESS: deque(), DECOMPRESS: deque(), HOMADD: deque()}
+    srv.free_slots, srv.batching, srv.max_batch = [0, 1, 2], True, 3
+    srv.budget, srv.in_use = 100, 0
+    srv.now = lambda: 10.0
+    srv._bytes = lambda q: q.eb  # the request's size stands in the eb field
+    units = []
+    srv._launch = lambda slot, group: units.append([q.rid for q in group])
+    import heapq
+    kinds = [HOMADD, COMPRESS, COMPRESS, DECOMPRESS, COMPRESS, COMPRESS, COMPRESS, HOMADD]
+    for i, k in enumerate(kinds):
+        heapq.heappush(srv.queue, (float(i), i, Request(float(i), i, k, eb=10.0)))
+    heapq.heappush(srv.queue, (99.0, 99, Request(99.0, 99, COMPRESS, eb=10.0)))  # not arrived yet
+    srv._admit()
+    assert units == [[0, 7], [1, 2, 4], [3]]  # oldest first; batches of up to 3; decompress alone
+    assert srv.in_use == 60 and [q.rid for q in srv.ready[COMPRESS]] == [5, 6] and len(srv.queue) == 1
+    srv.free_slots, srv.in_use = [0], 95  # the oldest does not fit: nothing is launched
+    srv._admit()
+    assert len(units) == 3 and [q.rid for q in srv.ready[COMPRESS]] == [5, 6]

@@ -219,9 +219,30 @@ ZSmem compress_smem(const ZGeom &g)
     return zg_smem(0, g.L, g.TB, (uint32_t)(2 * sizeof(CompressJob) + sizeof(ZPlace)));
 }
 
+/* The add's layout.  Two CTAs share an SM (registers allow no more), so
+ * the shared memory they leave unused goes to the ring of packed sums: the
+ * longer the ring, the longer a tile may wait there for its look-back before
+ * the adding warps run out of room. */
 ZSmem homadd_smem(const ZGeom &g)
 {
-    return zg_smem(2, g.L, g.TB, homadd_job_bytes(g.TB));
+    ZSmem m = zg_smem(2, g.L, g.TB, homadd_job_bytes(g.TB));
+    static int per_cta = -1;
+    if (per_cta < 0) {
+        int dev = 0, sm = 0, rsv = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&rsv, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess) {
+            cudaGetLastError();
+            sm = 0;
+        }
+        per_cta = sm > 0 ? sm / 2 - rsv - 1024 : 0; /* a kilobyte of margin */
+    }
+    if (per_cta > (int)m.total) {
+        const uint32_t extra = ((uint32_t)per_cta - m.total) & ~15u;
+        m.jobs += extra;
+        m.total += extra;
+    }
+    return m;
 }
 
 /* The decompressor's layout (padded rows, one input buffer) with room for
@@ -835,8 +856,15 @@ struct PinBuf {
     }
 };
 
-/* Most chunk groups a pipelined drop-in splits a stream into. */
+/* Most chunk groups a pipelined drop-in splits a stream into, and the
+ * compute streams ("lanes") their kernels are spread over: a group's index
+ * walk launches few CTAs, so neighbouring groups' kernels run side by side. */
 constexpr uint32_t kMaxGroups = 8;
+constexpr uint32_t kLanes = 4;
+/* groups per call: compression has no walk, so finer groups overlap more;
+ * decompression and the add walk each group's headers, whose kernels carry
+ * a fixed cost per launch */
+constexpr uint32_t kGroupsCompress = 8, kGroupsDecompress = 8, kGroupsHomadd = 8;
 
 /* Cached device buffers of the drop-in layer, one set per device. */
 struct DropCtx {
@@ -846,6 +874,8 @@ struct DropCtx {
     cudaStream_t st_in = nullptr, st_out = nullptr; /* the pipelined drop-ins' copies */
     cudaEvent_t ev = nullptr;
     cudaEvent_t ev_in[kMaxGroups] = {}, ev_k[kMaxGroups] = {};
+    cudaStream_t lane[kLanes] = {};
+    DevBuf lws[kLanes], lix[kLanes][3]; /* per lane: workspace, indexes */
     DevBuf fin, fout, s[3], ix[3], ws;
     DevBuf aux; /* counters read back by the _record entry points */
     PinBuf pin;
@@ -868,6 +898,8 @@ DropCtx *drop_ctx()
         for (uint32_t i = 0; ok && i < kMaxGroups; i++)
             ok = cudaEventCreateWithFlags(&c->ev_in[i], cudaEventDisableTiming) == cudaSuccess &&
                  cudaEventCreateWithFlags(&c->ev_k[i], cudaEventDisableTiming) == cudaSuccess;
+        for (uint32_t i = 0; ok && i < kLanes; i++)
+            ok = cudaStreamCreateWithFlags(&c->lane[i], cudaStreamNonBlocking) == cudaSuccess;
         if (!ok) {
             cudaGetLastError();
             delete c;
@@ -1018,12 +1050,12 @@ bool overlaps(const void *a, size_t na, const void *b, size_t nb)
  * worth cutting (one chunk, or fewer than 2^22 elements).  The last group
  * holds more chunks than the remainder segment has elements, so its stream
  * splits exactly like the whole one's tail. */
-std::vector<Group> chunk_groups(const ZGeom &g)
+std::vector<Group> chunk_groups(const ZGeom &g, uint32_t most)
 {
     std::vector<Group> out;
     const uint32_t T = g.T;
     if (T < 2 || g.n < (1ull << 22)) return out;
-    const uint32_t G = std::min<uint32_t>(T, kMaxGroups);
+    const uint32_t G = std::min<uint32_t>(T, std::min<uint32_t>(most, kMaxGroups));
     std::vector<uint32_t> cut;
     for (uint32_t k = 0; k <= G; k++) cut.push_back((uint32_t)((uint64_t)T * k / G));
     while (cut.size() > 2 && T - cut[cut.size() - 2] <= g.rem) cut.erase(cut.end() - 2);
@@ -1062,14 +1094,20 @@ size_t max_index_bytes(const std::vector<Group> &gr)
 
 /* Waits for every copy and kernel of a pipelined call, then reads (and
  * clears) the workspace's status words. */
-int pipe_finish(DropCtx *c, int rc)
+int pipe_finish(DropCtx *c, int rc, uint32_t lanes)
 {
-    const bool sync_ok = cudaStreamSynchronize(c->st_in) == cudaSuccess &&
-                         cudaStreamSynchronize(c->st_out) == cudaSuccess;
-    const int rc2 = finish(c, c->ws.p);
+    bool sync_ok = cudaStreamSynchronize(c->st_in) == cudaSuccess &&
+                   cudaStreamSynchronize(c->st_out) == cudaSuccess;
+    int rc2 = ZCCL_GPU_OK;
+    for (uint32_t l = 0; l < lanes; l++) {
+        const int r = c->lws[l].p ? zccl_gpu_check(c->lws[l].p, c->lane[l]) : ZCCL_GPU_OK;
+        if (!rc2) rc2 = r;
+    }
     if (!sync_ok) return ZCCL_GPU_ECUDA;
     return rc ? rc : rc2;
 }
+
+uint32_t lanes_for(size_t groups) { return (uint32_t)std::min<size_t>(groups, kLanes); }
 
 /* The caller's output stream from the groups' device streams: per group (in
  * order, as each one's size and header arrive in pinned memory) its chunk
@@ -1115,41 +1153,46 @@ int pipe_compress(DropCtx *c, unsigned char *out, const float *x, size_t *outSiz
         soff[k + 1] = soff[k] + a256(cap[k]);
         poff[k + 1] = poff[k] + 8 + 8ull * (gr[k].s1 - gr[k].s0);
     }
+    const uint32_t NL = lanes_for(G);
     if (int rc = c->fin.ensure(4 * g.n)) return rc;
     if (int rc = c->s[0].ensure(soff[G])) return rc;
-    if (int rc = c->ix[0].ensure(max_index_bytes(gr))) return rc;
-    if (int rc = c->ws.ensure(max_ws_bytes(gr))) return rc;
+    for (uint32_t l = 0; l < NL; l++) {
+        if (int rc = c->lix[l][0].ensure(max_index_bytes(gr))) return rc;
+        if (int rc = c->lws[l].ensure(max_ws_bytes(gr))) return rc;
+    }
     if (int rc = c->pin.ensure(poff[G])) return rc;
     float *fin = (float *)c->fin.p;
     uint8_t *dev[kMaxGroups];
     int rc = ZCCL_GPU_OK;
     for (size_t k = 0; k < G && !rc; k++) {
         const Group &q = gr[k];
+        const uint32_t l = (uint32_t)(k % NL);
+        cudaStream_t st = c->lane[l];
         dev[k] = (uint8_t *)c->s[0].p + soff[k];
         if (cudaMemcpyAsync(fin + q.e0, x + q.e0, 4 * q.n, cudaMemcpyHostToDevice, c->st_in) != cudaSuccess ||
             cudaEventRecord(c->ev_in[k], c->st_in) != cudaSuccess ||
-            cudaStreamWaitEvent(c->st, c->ev_in[k], 0) != cudaSuccess) {
+            cudaStreamWaitEvent(st, c->ev_in[k], 0) != cudaSuccess) {
             rc = ZCCL_GPU_ECUDA;
             break;
         }
         zccl_gpu_stream sub;
         sub.bytes = dev[k];
         sub.capacity = cap[k];
-        sub.index = c->ix[0].p;
+        sub.index = c->lix[l][0].p;
         sub.indexed = 0;
         sub.qprev_valid = 0;
-        if ((rc = compress_fmt(&sub, fin + q.e0, (size_t)q.n, eb, (int)g.L, (int)(q.s1 - q.s0), c->ws.p, c->st,
+        if ((rc = compress_fmt(&sub, fin + q.e0, (size_t)q.n, eb, (int)g.L, (int)(q.s1 - q.s0), c->lws[l].p, st,
                                g.fmt)))
             break;
         uint8_t *pin = (uint8_t *)c->pin.p + poff[k];
-        if (cudaMemcpyAsync(pin, c->ix[0].p, 8, cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
-            cudaMemcpyAsync(pin + 8, dev[k], 8ull * (q.s1 - q.s0), cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
-            cudaEventRecord(c->ev_k[k], c->st) != cudaSuccess)
+        if (cudaMemcpyAsync(pin, sub.index, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(pin + 8, dev[k], 8ull * (q.s1 - q.s0), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaEventRecord(c->ev_k[k], st) != cudaSuccess)
             rc = ZCCL_GPU_ECUDA;
     }
     uint64_t placed = 0;
     if (!rc) rc = pipe_place(c, gr, dev, cap, poff, out, g.T, &placed);
-    rc = pipe_finish(c, rc);
+    rc = pipe_finish(c, rc, NL);
     if (rc) return rc;
     *outSize = (size_t)(8ull * g.T + placed);
     return ZCCL_GPU_OK;
@@ -1211,10 +1254,13 @@ int pipe_decompress(DropCtx *c, float *y, const unsigned char *cmp, float eb, co
         soff[k + 1] = soff[k] + a256(8ull * (gr[k].s1 - gr[k].s0) + len[k] + 64);
         poff[k + 1] = poff[k] + 8ull * (gr[k].s1 - gr[k].s0);
     }
+    const uint32_t NL = lanes_for(G);
     if (int rc = c->fout.ensure(4 * g.n)) return rc;
     if (int rc = c->s[0].ensure(soff[G])) return rc;
-    if (int rc = c->ix[0].ensure(max_index_bytes(gr))) return rc;
-    if (int rc = c->ws.ensure(max_ws_bytes(gr))) return rc;
+    for (uint32_t l = 0; l < NL; l++) {
+        if (int rc = c->lix[l][0].ensure(max_index_bytes(gr))) return rc;
+        if (int rc = c->lws[l].ensure(max_ws_bytes(gr))) return rc;
+    }
     if (int rc = c->pin.ensure(poff[G])) return rc;
     float *fout = (float *)c->fout.p;
     uint8_t *pin = (uint8_t *)c->pin.p;
@@ -1223,6 +1269,8 @@ int pipe_decompress(DropCtx *c, float *y, const unsigned char *cmp, float eb, co
     for (size_t k = 0; k < G && !rc; k++) {
         const Group &q = gr[k];
         const uint32_t Ts = q.s1 - q.s0;
+        const uint32_t l = (uint32_t)(k % NL);
+        cudaStream_t st = c->lane[l];
         uint8_t *dev = (uint8_t *)c->s[0].p + soff[k];
         for (uint32_t i = 0; i < Ts; i++) { /* the group's own header, its offsets rebased */
             const uint64_t v = e[q.s0 + i] - e[q.s0];
@@ -1232,24 +1280,24 @@ int pipe_decompress(DropCtx *c, float *y, const unsigned char *cmp, float eb, co
             cudaMemcpyAsync(dev + 8ull * Ts, body + e[q.s0], len[k], cudaMemcpyHostToDevice, c->st_in) !=
                 cudaSuccess ||
             cudaEventRecord(c->ev_in[k], c->st_in) != cudaSuccess ||
-            cudaStreamWaitEvent(c->st, c->ev_in[k], 0) != cudaSuccess) {
+            cudaStreamWaitEvent(st, c->ev_in[k], 0) != cudaSuccess) {
             rc = ZCCL_GPU_ECUDA;
             break;
         }
         zccl_gpu_stream sub;
         sub.bytes = dev;
         sub.capacity = 8ull * Ts + len[k];
-        sub.index = c->ix[0].p;
+        sub.index = c->lix[l][0].p;
         sub.indexed = 0;
         sub.qprev_valid = 0;
-        if ((rc = decompress_fmt(fout + q.e0, &sub, (size_t)q.n, eb, (int)g.L, (int)Ts, c->ws.p, c->st, g.fmt)))
+        if ((rc = decompress_fmt(fout + q.e0, &sub, (size_t)q.n, eb, (int)g.L, (int)Ts, c->lws[l].p, st, g.fmt)))
             break;
-        if (cudaEventRecord(c->ev_k[k], c->st) != cudaSuccess ||
+        if (cudaEventRecord(c->ev_k[k], st) != cudaSuccess ||
             cudaStreamWaitEvent(c->st_out, c->ev_k[k], 0) != cudaSuccess ||
             cudaMemcpyAsync(y + q.e0, fout + q.e0, 4 * q.n, cudaMemcpyDeviceToHost, c->st_out) != cudaSuccess)
             rc = ZCCL_GPU_ECUDA;
     }
-    return pipe_finish(c, rc);
+    return pipe_finish(c, rc, NL);
 }
 
 /* Two-way homomorphic add of host streams into a host stream, group by
@@ -1277,12 +1325,15 @@ int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned
         /* pinned: the sum's size and header, then both inputs' rebased headers */
         poff[k + 1] = poff[k] + 8 + 8 * Ts + 2 * 8 * Ts;
     }
+    const uint32_t NL = lanes_for(G);
     if (int rc = c->s[1].ensure(ioff[G])) return rc;
     if (int rc = c->s[2].ensure(soff[G])) return rc;
     const size_t ixb = max_index_bytes(gr);
-    for (int i = 0; i < 3; i++)
-        if (int rc = c->ix[i].ensure(ixb)) return rc;
-    if (int rc = c->ws.ensure(max_ws_bytes(gr))) return rc;
+    for (uint32_t l = 0; l < NL; l++) {
+        for (int i = 0; i < 3; i++)
+            if (int rc = c->lix[l][i].ensure(ixb)) return rc;
+        if (int rc = c->lws[l].ensure(max_ws_bytes(gr))) return rc;
+    }
     if (int rc = c->pin.ensure(poff[G])) return rc;
     uint8_t *pin = (uint8_t *)c->pin.p;
     uint8_t *dev[kMaxGroups];
@@ -1290,6 +1341,9 @@ int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned
     for (size_t k = 0; k < G && !rc; k++) {
         const Group &q = gr[k];
         const uint32_t Ts = q.s1 - q.s0;
+        const uint32_t l = (uint32_t)(k % NL);
+        cudaStream_t st = c->lane[l];
+        void *ws = c->lws[l].p;
         zccl_gpu_stream in[2], sum;
         uint8_t *ib = (uint8_t *)c->s[1].p + ioff[k];
         for (int i = 0; i < 2 && !rc; i++) {
@@ -1304,33 +1358,33 @@ int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned
                 rc = ZCCL_GPU_ECUDA;
             in[i].bytes = ib;
             in[i].capacity = 8ull * Ts + len[i][k];
-            in[i].index = c->ix[i].p;
+            in[i].index = c->lix[l][i].p;
             in[i].indexed = 0;
             in[i].qprev_valid = 0;
             ib += a256(8ull * Ts + len[i][k] + 64);
         }
         if (rc || cudaEventRecord(c->ev_in[k], c->st_in) != cudaSuccess ||
-            cudaStreamWaitEvent(c->st, c->ev_in[k], 0) != cudaSuccess) {
+            cudaStreamWaitEvent(st, c->ev_in[k], 0) != cudaSuccess) {
             rc = rc ? rc : ZCCL_GPU_ECUDA;
             break;
         }
         dev[k] = (uint8_t *)c->s[2].p + soff[k];
         sum.bytes = dev[k];
         sum.capacity = cap[k];
-        sum.index = c->ix[2].p;
+        sum.index = c->lix[l][2].p;
         sum.indexed = 0;
         sum.qprev_valid = 0;
-        if (ws_clear(c->ws.p, q.g, c->st) != cudaSuccess) {
+        if (ws_clear(ws, q.g, st) != cudaSuccess) {
             rc = ZCCL_GPU_ECUDA;
             break;
         }
-        if ((rc = walk_stream(&in[0], q.g, c->ws.p, c->st)) || (rc = walk_stream(&in[1], q.g, c->ws.p, c->st)) ||
-            (rc = zccl_gpu_homadd_cases(&sum, in, 2, (size_t)q.n, (int)g.L, (int)Ts, c->ws.p, nullptr, c->st)))
+        if ((rc = walk_stream(&in[0], q.g, ws, st)) || (rc = walk_stream(&in[1], q.g, ws, st)) ||
+            (rc = zccl_gpu_homadd_cases(&sum, in, 2, (size_t)q.n, (int)g.L, (int)Ts, ws, nullptr, st)))
             break;
         uint8_t *pk = pin + poff[k];
-        if (cudaMemcpyAsync(pk, c->ix[2].p, 8, cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
-            cudaMemcpyAsync(pk + 8, dev[k], 8ull * Ts, cudaMemcpyDeviceToHost, c->st) != cudaSuccess ||
-            cudaEventRecord(c->ev_k[k], c->st) != cudaSuccess)
+        if (cudaMemcpyAsync(pk, sum.index, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(pk + 8, dev[k], 8ull * Ts, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaEventRecord(c->ev_k[k], st) != cudaSuccess)
             rc = ZCCL_GPU_ECUDA;
     }
     /* the sum written over an input (the ring adds into its receive
@@ -1343,7 +1397,7 @@ int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned
         rc = ZCCL_GPU_ECUDA;
     uint64_t placed = 0;
     if (!rc) rc = pipe_place(c, gr, dev, cap, poff, out, g.T, &placed);
-    rc = pipe_finish(c, rc);
+    rc = pipe_finish(c, rc, NL);
     if (rc) return rc;
     *out_size += (size_t)(8ull * g.T + placed);
     return ZCCL_GPU_OK;
@@ -1361,7 +1415,7 @@ int dropin_compress(unsigned char *outputBytes, const float *oriData, size_t *ou
     if (!nz_out && !is_device_ptr(oriData) && !is_device_ptr(outputBytes) &&
         !overlaps(outputBytes, (size_t)zg_stream_worst(&g), oriData, 4 * n)) {
         g.fmt = fmt;
-        const std::vector<Group> gr = chunk_groups(g);
+        const std::vector<Group> gr = chunk_groups(g, kGroupsCompress);
         if (!gr.empty()) return pipe_compress(c, outputBytes, oriData, outSize, eb, g, gr);
     }
     if (!is_device_ptr(oriData)) {
@@ -1413,7 +1467,7 @@ int dropin_decompress(float *newData, size_t n, float eb, int L, const unsigned 
     if (!dout && !nz_out && !size_out && !is_device_ptr(cmp) &&
         !overlaps(newData, 4 * n, cmp, (size_t)zg_stream_worst(&g))) {
         g.fmt = fmt;
-        const std::vector<Group> gr = chunk_groups(g);
+        const std::vector<Group> gr = chunk_groups(g, kGroupsDecompress);
         if (!gr.empty()) {
             bool capped = false;
             int rc = pipe_decompress(c, newData, cmp, eb, g, gr, false, &capped);
@@ -1463,7 +1517,7 @@ int dropin_homadd(unsigned char *final_cmp, size_t *final_size, size_t n, float 
     if (!c) return ZCCL_GPU_ECUDA;
     std::lock_guard<std::mutex> lk(c->mu);
     if (!cases_out && !is_device_ptr(final_cmp) && !is_device_ptr(cmp1) && !is_device_ptr(cmp2)) {
-        const std::vector<Group> gr = chunk_groups(g);
+        const std::vector<Group> gr = chunk_groups(g, kGroupsHomadd);
         if (!gr.empty()) {
             bool capped = false;
             int rc = pipe_homadd(c, final_cmp, final_size, cmp1, cmp2, g, gr, false, &capped);

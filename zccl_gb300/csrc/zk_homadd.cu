@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(320, 2) k_homadd(const __grid_constant__ HomAd
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t NC = blockDim.x - 64, nwc = NC >> 5; /* adding threads (TB), adding warps */
     const uint32_t L = a.job.g.L, stride = zg_row_stride(L); /* one L for the whole batch */
-    const uint32_t R = zg_ring_bytes(L, NC);
+    const uint32_t R = a.sm.jobs - a.sm.out - 48u; /* the ring: every byte up to the job region, less the slack */
     uint32_t bad = 0;
     /* see k_decompress: a failed index walk stops every CTA alike */
     if (*(volatile const uint32_t *)a.w.walk_err) return;

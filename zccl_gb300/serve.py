@@ -30,6 +30,7 @@ import ctypes
 import heapq
 import time
 import types
+from collections import deque
 from dataclasses import dataclass, field
 
 from . import BATCH_COMPRESS, BATCH_HOMADD, Batch, StreamDesc, ZcclError, _check, lib
@@ -69,7 +70,8 @@ class Server:
     device memory stays within the budget over a long run."""
 
     def __init__(self, budget_bytes: int, slots: int = 4, L: int = 32, device: str = "cuda",
-                 batching: bool = True, keep_results: bool = False, pool_bytes: int = 1 << 30):
+                 batching: bool = True, keep_results: bool = False, pool_bytes: int = 1 << 30,
+                 max_batch: int = 256):
         import torch
         self.torch = torch
         self.L, self.device, self.batching, self.keep = int(L), device, batching, keep_results
@@ -78,7 +80,9 @@ class Server:
         self.free_slots = list(range(slots))
         self.ws = [None] * slots  # per-slot scratch, grown on demand
         self.store: dict = {}     # key -> Resident
-        self.queue: list = []     # (arrival, rid, Request) not yet admitted
+        self.queue: list = []     # (arrival, rid, Request) not yet arrived
+        self.ready = {COMPRESS: deque(), DECOMPRESS: deque(), HOMADD: deque()}  # arrived, per kind
+        self.max_batch = int(max_batch)
         self.inflight: list = []  # (event, slot, [requests], keep-alive objects)
         self.t0 = time.perf_counter()
         self.log: list = []
@@ -267,30 +271,42 @@ class Server:
         self.inflight = still
 
     def _admit(self) -> None:
+        """Move arrived requests to their kind's FIFO, then fill free slots:
+        the oldest arrived request and, with batching, the next ones of its
+        kind (up to max_batch, while they fit the budget) form one unit.
+        Costs O(arrived) per call, however long the backlog."""
         now = self.now()
-        while self.free_slots and self.queue and self.queue[0][0] <= now:
-            kind = self.queue[0][2].kind
-            group, tmp = [], []
-            # the head and, with batching, every other arrived request of its kind that fits
-            while self.queue and self.queue[0][0] <= now:
-                _, _, q = heapq.heappop(self.queue)
+        while self.queue and self.queue[0][0] <= now:
+            _, _, q = heapq.heappop(self.queue)
+            self.ready[q.kind].append(q)
+        while self.free_slots:
+            heads = [d[0] for d in self.ready.values() if d]
+            if not heads:
+                return
+            head = min(heads, key=lambda q: (q.arrival, q.rid))
+            dq = self.ready[head.kind]
+            group = []
+            while dq and len(group) < self.max_batch:
+                q = dq[0]
                 need = self._bytes(q)
-                if q.kind == kind and self.in_use + need <= self.budget and \
-                        (not group or (self.batching and kind != DECOMPRESS)):
-                    q.nbytes = need
-                    self.in_use += need
-                    group.append(q)
-                else:
-                    tmp.append(q)
-            for q in tmp:
-                heapq.heappush(self.queue, (q.arrival, q.rid, q))
+                if self.in_use + need > self.budget:
+                    break
+                dq.popleft()
+                q.nbytes = need
+                self.in_use += need
+                group.append(q)
+                if not self.batching or q.kind == DECOMPRESS:
+                    break
             if not group:
-                return  # the head does not fit the budget yet
+                return  # the oldest does not fit the budget yet
             self._launch(self.free_slots.pop(0), group)
+
+    def _pending(self) -> bool:
+        return bool(self.queue or self.inflight or any(self.ready.values()))
 
     def run(self, deadline: float | None = None) -> list:
         """Serve until every submitted request is done (or the deadline)."""
-        while self.queue or self.inflight:
+        while self._pending():
             self._retire()
             self._admit()
             if deadline is not None and self.now() > deadline:
