@@ -413,7 +413,7 @@ cudaError_t launch_compress(const CompressArgs &a, cudaStream_t st)
 {
     const bool fast = a.job.g.L <= 32;
     const void *fn = fast ? (const void *)k_compress<true> : (const void *)k_compress<false>;
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
+    cudaError_t e = set_max_smem(fn, a.sm.total);
     if (e != cudaSuccess) return e;
     const unsigned threads = a.job.g.TB + 32; /* compute warps and the placer warp */
     const uint64_t tiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;

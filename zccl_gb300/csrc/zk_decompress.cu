@@ -382,7 +382,7 @@ cudaError_t launch_decompress(const DecompressArgs &a, cudaStream_t st)
     /* a stream without starting values: tile sums, then the scan per segment */
     if (!a.qprev_valid) {
         const void *fs = fast ? (const void *)k_decompress<true, true> : (const void *)k_decompress<false, true>;
-        cudaError_t e = cudaFuncSetAttribute(fs, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
+        cudaError_t e = set_max_smem(fs, a.sm.total);
         if (e != cudaSuccess) return e;
         alignas(64) CUtensorMap none;
         memset(&none, 0, sizeof none);
@@ -397,7 +397,7 @@ cudaError_t launch_decompress(const DecompressArgs &a, cudaStream_t st)
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     const void *fn = fast ? (const void *)k_decompress<true, false> : (const void *)k_decompress<false, false>;
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
+    cudaError_t e = set_max_smem(fn, a.sm.total);
     if (e != cudaSuccess) return e;
     unsigned grid = persistent_grid(fn, a.g.TB, a.sm.total, a.g.ntiles);
     DecompressArgs b = a;

@@ -180,7 +180,7 @@ cudaError_t launch_decompress_jobs(const DecompressJobsArgs &a, cudaStream_t st)
 {
     const bool fast = a.job.g.L <= 32;
     const void *fn = fast ? (const void *)k_decompress_jobs<true> : (const void *)k_decompress_jobs<false>;
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
+    cudaError_t e = set_max_smem(fn, a.sm.total);
     if (e != cudaSuccess) return e;
     const uint32_t TB = a.job.g.TB;
     const uint64_t tiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;

@@ -484,7 +484,7 @@ cudaError_t launch_homadd(const HomAddArgs &a, cudaStream_t st)
 {
     const bool fast = a.job.g.L <= 32;
     const void *fn = fast ? (const void *)k_homadd<true> : (const void *)k_homadd<false>;
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.sm.total);
+    cudaError_t e = set_max_smem(fn, a.sm.total);
     if (e != cudaSuccess) return e;
     const unsigned threads = a.job.g.TB + 64; /* adding warps, the placer warp, the loader warp */
     const uint64_t tiles = a.batch.jobs ? a.batch.ntiles : a.job.g.ntiles;

@@ -451,8 +451,15 @@ __global__ void __launch_bounds__(32 * WARPS_W3) k_walk_final(const WalkArgs a)
             spec_walks(buf, g.L, g.fmt, sp, sx);
             stitch(buf, g.L, g.fmt, entry[k - w0], sp, sx, wp);
             __syncwarp();
-            /* lane j records the true-path blocks of its sub-window */
+            /* lane j records the true-path blocks of its sub-window; the
+             * next tile boundary at or after its first block is found once */
             uint64_t blk = b0 + wp->pref[lane];
+            const uint64_t tq = blk / g.TB;
+            uint64_t tnext = tq * g.TB, tidx = tq;
+            if (tnext < blk) {
+                tnext += g.TB;
+                tidx++;
+            }
 #pragma unroll
             for (uint32_t wd = 0; wd < 4; wd++) {
                 uint32_t m = wp->tm[lane][wd];
@@ -471,7 +478,11 @@ __global__ void __launch_bounds__(32 * WARPS_W3) k_walk_final(const WalkArgs a)
                         m = 0;
                         break;
                     }
-                    if (blk % g.TB == 0 && blk) a.idx.tile_off[tile0 + blk / g.TB] = gpos;
+                    if (blk == tnext) {
+                        if (blk) a.idx.tile_off[tile0 + tidx] = gpos;
+                        tnext += g.TB;
+                        tidx++;
+                    }
                     a.idx.widths[gblk0 + blk] = (uint8_t)b;
                     const uint32_t n = blk < nfull ? g.L : ntail;
                     blk++;
@@ -540,12 +551,7 @@ size_t walk_w1_warp_bytes(uint32_t M) { return w1_warp_bytes(M); }
 /* Persistent grid: the CTAs that fit at once, at most `most`. */
 static unsigned walk_grid(const void *fn, unsigned threads, size_t smem, unsigned most)
 {
-    int dev = 0, nsm = 0, per = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, (int)threads, smem) != cudaSuccess || per < 1)
-        per = 1;
-    const unsigned g = (unsigned)(nsm > 0 ? nsm : 1) * (unsigned)per;
+    const unsigned g = (unsigned)sm_count() * (unsigned)blocks_per_sm(fn, (int)threads, smem);
     return most < g ? (most ? most : 1) : g;
 }
 
@@ -559,7 +565,7 @@ cudaError_t launch_walk(const WalkArgs &a0, cudaStream_t st)
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const uint32_t smem1 = WARPS_W1 * a.w1_warp_bytes;
     const void *f1 = a.M < 256 ? (const void *)k_walk_tables<uint16_t> : (const void *)k_walk_tables<uint32_t>;
-    if ((e = cudaFuncSetAttribute(f1, cudaFuncAttributeMaxDynamicSharedMemorySize, smem1)) != cudaSuccess) return e;
+    if ((e = set_max_smem(f1, smem1)) != cudaSuccess) return e;
     const unsigned grid1 = walk_grid(f1, 32 * WARPS_W1, smem1, (a.max_windows + WARPS_W1 - 1) / WARPS_W1);
     if (a.M < 256)
         k_walk_tables<uint16_t><<<grid1, 32 * WARPS_W1, smem1, st>>>(a);
@@ -572,8 +578,7 @@ cudaError_t launch_walk(const WalkArgs &a0, cudaStream_t st)
     if (a.seg_batch > WALK_G) a.seg_batch = WALK_G;
     if (a.seg_batch < 1) a.seg_batch = 1;
     const uint32_t smem2 = a.seg_batch * a.M * 8u;
-    if ((e = cudaFuncSetAttribute(k_walk_segments, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  smem2)) != cudaSuccess)
+    if ((e = set_max_smem((const void *)k_walk_segments, smem2)) != cudaSuccess)
         return e;
     k_walk_segments<<<a.g.T, 256, smem2, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -586,8 +591,7 @@ cudaError_t launch_walk(const WalkArgs &a0, cudaStream_t st)
     uint32_t warps3 = WARPS_W3;
     while (warps3 > 1 && w3_head(a.M) + warps3 * wstride > (uint32_t)smax) warps3--;
     const uint32_t smem3 = w3_head(a.M) + warps3 * wstride;
-    if ((e = cudaFuncSetAttribute(k_walk_final, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  smem3)) != cudaSuccess)
+    if ((e = set_max_smem((const void *)k_walk_final, smem3)) != cudaSuccess)
         return e;
     k_walk_final<<<walk_grid((const void *)k_walk_final, 32 * warps3, smem3, a.max_groups), 32 * warps3, smem3, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;

@@ -9,6 +9,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "zdev.cuh"
 #include "zgeom.h"
 
@@ -492,15 +494,99 @@ __device__ __forceinline__ uint32_t batch_job(const ZBatch &b, uint64_t t, uint6
     return j;
 }
 
+/* Launch-shape queries, remembered per device and kernel: the occupancy
+ * calculator and the shared-memory attribute cost host time on every
+ * launch, and a pipelined host-buffer call launches a hundred kernels. */
+struct LaunchCache {
+    struct Occ {
+        const void *fn;
+        int dev, threads, per;
+        size_t smem;
+    };
+    struct Attr {
+        const void *fn;
+        int dev;
+        size_t smem;
+    };
+    std::mutex mu;
+    Occ occ[96];
+    Attr attr[64];
+    int nocc = 0, nattr = 0;
+    int nsm[64] = {0};
+};
+
+static inline LaunchCache &launch_cache()
+{
+    static LaunchCache c;
+    return c;
+}
+
+/* Blocks of fn per SM at this block size and shared memory (at least 1). */
+static inline int blocks_per_sm(const void *fn, int threads, size_t smem)
+{
+    LaunchCache &c = launch_cache();
+    int dev = 0;
+    cudaGetDevice(&dev);
+    {
+        std::lock_guard<std::mutex> lk(c.mu);
+        for (int i = 0; i < c.nocc; i++)
+            if (c.occ[i].fn == fn && c.occ[i].dev == dev && c.occ[i].threads == threads && c.occ[i].smem == smem)
+                return c.occ[i].per;
+    }
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, threads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        per = 0;
+    }
+    if (per < 1) per = 1;
+    std::lock_guard<std::mutex> lk(c.mu);
+    if (c.nocc < 96) c.occ[c.nocc++] = {fn, dev, threads, per, smem};
+    return per;
+}
+
+/* SMs of the current device. */
+static inline int sm_count()
+{
+    LaunchCache &c = launch_cache();
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && c.nsm[dev] > 0) return c.nsm[dev];
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        return 1;
+    }
+    if (dev >= 0 && dev < 64) c.nsm[dev] = n;
+    return n;
+}
+
+/* cudaFuncSetAttribute(fn, MaxDynamicSharedMemorySize, smem), skipped when
+ * an equal or larger value is already set for fn on this device. */
+static inline cudaError_t set_max_smem(const void *fn, size_t smem)
+{
+    LaunchCache &c = launch_cache();
+    int dev = 0;
+    cudaGetDevice(&dev);
+    {
+        std::lock_guard<std::mutex> lk(c.mu);
+        for (int i = 0; i < c.nattr; i++)
+            if (c.attr[i].fn == fn && c.attr[i].dev == dev && c.attr[i].smem >= smem) return cudaSuccess;
+    }
+    const cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(c.mu);
+    for (int i = 0; i < c.nattr; i++)
+        if (c.attr[i].fn == fn && c.attr[i].dev == dev) {
+            c.attr[i].smem = smem;
+            return cudaSuccess;
+        }
+    if (c.nattr < 64) c.attr[c.nattr++] = {fn, dev, smem};
+    return cudaSuccess;
+}
+
 static inline unsigned persistent_grid(const void *fn, int threads, size_t smem, uint64_t ntiles)
 {
-    int dev = 0, nsm = 0, occ = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, smem);
-    if (nsm < 1) nsm = 1;
-    if (occ < 1) occ = 1;
-    uint64_t g = (uint64_t)nsm * (uint64_t)occ;
+    const uint64_t g = (uint64_t)sm_count() * (uint64_t)blocks_per_sm(fn, threads, smem);
     return (unsigned)(g < ntiles ? g : ntiles);
 }
 
