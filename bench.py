@@ -366,6 +366,28 @@ def reduction_bench(args, L, T, dev):
     docs = codec.new_stream()
     doc_total = torch.empty(n, dtype=torch.float32, device=dev)
     ms_doc = timed(lambda: reduce_doc(codec, streams, eb, out=docs, total=doc_total), 5, st)
+    # the same three reductions replayed from CUDA graphs: device time alone,
+    # without the host's per-call enqueue between the fold's and DOC's calls
+    graph = {}
+    gst = torch.cuda.Stream(dev)
+    gcodec = Z.Codec(n, L, T, device=str(dev), stream=gst)
+    keep = []
+    for name, fn in (("pway_homadd_ms", lambda: reduce_homomorphic(gcodec, streams, out=out)),
+                     ("pairwise_fold_ms", lambda: reduce_pairwise(gcodec, streams, pair_outs)),
+                     ("doc_ms", lambda: reduce_doc(gcodec, streams, eb, out=docs, total=doc_total))):
+        try:
+            with torch.cuda.stream(gst):
+                fn()
+                gst.synchronize()
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g, stream=gst, capture_error_mode="relaxed"):
+                    fn()
+                graph[name] = round(timed(g.replay, 10, gst), 4)
+            keep.append(g)
+        except Exception as e:  # a call that cannot be captured: report it, keep going
+            graph[name] = f"not captured: {type(e).__name__}"
+    gcodec.check()
+    del keep
     codec.check()
     same = reduce_homomorphic(codec, streams, out=out).tobytes() == reduce_pairwise(codec, streams).tobytes()
     exact = torch.zeros(n, dtype=torch.float64, device=dev)
@@ -406,6 +428,7 @@ def reduction_bench(args, L, T, dev):
         "pway_homadd_GBps_uncompressed": round(4 * n * P / (ms_pway * 1e-3) / 1e9, 1),
         "pairwise_fold_ms": round(ms_pair, 4),
         "doc_ms": round(ms_doc, 4),
+        "graph_replay_ms": graph,
         "compress_all_ms": round(ms_compress, 4),
         "pway_equals_pairwise_bytes": same,
         "max_err_over_eb": {"homomorphic": round(err_ho, 3), "doc": round(err_doc, 3), "bound": P},

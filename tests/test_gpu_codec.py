@@ -459,3 +459,44 @@ def test_host_dropins_pipelined_by_chunk_groups(port, torch, T, extra):
         acc[: len(sy)] = np.frombuffer(sy, np.uint8)
         total = Z.ZCCL_float_homomophic_add_openmp_threadblock(acc, 0, n, eb, L, hs, acc)
         assert total == len(sxy) and acc[:total].tobytes() == sxy, (T, extra, pinned)
+
+
+def test_host_dropins_pipelined_report_bad_streams(port, torch):
+    """Damaged host streams on the pipelined path end in a status code, not a
+    fault or a hang: header bytes above 32 inside a middle chunk group, a
+    chunk offset that runs past the stream, and the add of a damaged input.
+    A good call right after each is exact again."""
+    n, L, T = 1 << 22, 32, 16
+    x = np.sin(np.arange(n, dtype=np.float64) * 1e-3).astype(np.float32)
+    eb = float(np.float32(2e-4))
+    good = port.compress(x, eb, L, T)
+    Z.set_omp_threads(T)
+    cap = 4 * n + 8 * T + 4096
+    hdr = np.frombuffer(good[: 8 * T], "<u8")
+    out = np.zeros(n, np.float32)
+    ref = port.decompress(good, n, eb, L, T)
+
+    def host(b):
+        h = np.zeros(cap, np.uint8)
+        h[: len(b)] = np.frombuffer(b, np.uint8)
+        return h
+
+    bad = host(good)
+    mid = 8 * T + int(hdr[6]) + 64  # inside chunk 6, in the fourth of eight groups
+    bad[mid: mid + 32] = 0xEE       # not a width byte
+    with pytest.raises(Z.ZcclError):
+        Z.ZCCL_float_decompress_openmp_threadblock_arg(out, n, eb, L, bad)
+    Z.ZCCL_float_decompress_openmp_threadblock_arg(out, n, eb, L, host(good))
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+
+    far = host(good)
+    far[8 * 5: 8 * 6] = np.frombuffer(np.uint64(3 * cap).tobytes(), np.uint8)  # chunk 5 starts past the end
+    with pytest.raises(Z.ZcclError):
+        Z.ZCCL_float_decompress_openmp_threadblock_arg(out, n, eb, L, far)
+
+    acc = host(good)
+    with pytest.raises(Z.ZcclError):
+        Z.ZCCL_float_homomophic_add_openmp_threadblock(acc, 0, n, eb, L, bad, acc)
+    acc = host(good)
+    total = Z.ZCCL_float_homomophic_add_openmp_threadblock(acc, 0, n, eb, L, host(good), acc)
+    assert acc[:total].tobytes() == port.homadd(good, good, n, eb, L, T)
