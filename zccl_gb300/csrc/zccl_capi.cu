@@ -861,6 +861,7 @@ struct PinBuf {
  * walk launches few CTAs, so neighbouring groups' kernels run side by side. */
 constexpr uint32_t kMaxGroups = 8;
 constexpr uint32_t kLanes = 4;
+constexpr uint32_t kWalkLanes = 2 * kLanes; /* the add walks its second input on lane l + kLanes */
 /* groups per call: compression has no walk, so finer groups overlap more;
  * decompression and the add walk each group's headers, whose kernels carry
  * a fixed cost per launch */
@@ -873,9 +874,9 @@ struct DropCtx {
     cudaStream_t st2 = nullptr; /* a second input's copy, beside the first one's walk */
     cudaStream_t st_in = nullptr, st_out = nullptr; /* the pipelined drop-ins' copies */
     cudaEvent_t ev = nullptr;
-    cudaEvent_t ev_in[kMaxGroups] = {}, ev_k[kMaxGroups] = {};
-    cudaStream_t lane[kLanes] = {};
-    DevBuf lws[kLanes], lix[kLanes][3]; /* per lane: workspace, indexes */
+    cudaEvent_t ev_in[kMaxGroups] = {}, ev_k[kMaxGroups] = {}, ev_w[kMaxGroups] = {};
+    cudaStream_t lane[kWalkLanes] = {};
+    DevBuf lws[kWalkLanes], lix[kLanes][3]; /* per lane: workspace; per compute lane: indexes */
     DevBuf fin, fout, s[3], ix[3], ws;
     DevBuf aux; /* counters read back by the _record entry points */
     PinBuf pin;
@@ -898,7 +899,9 @@ DropCtx *drop_ctx()
         for (uint32_t i = 0; ok && i < kMaxGroups; i++)
             ok = cudaEventCreateWithFlags(&c->ev_in[i], cudaEventDisableTiming) == cudaSuccess &&
                  cudaEventCreateWithFlags(&c->ev_k[i], cudaEventDisableTiming) == cudaSuccess;
-        for (uint32_t i = 0; ok && i < kLanes; i++)
+        for (uint32_t i = 0; ok && i < kMaxGroups; i++)
+            ok = cudaEventCreateWithFlags(&c->ev_w[i], cudaEventDisableTiming) == cudaSuccess;
+        for (uint32_t i = 0; ok && i < kWalkLanes; i++)
             ok = cudaStreamCreateWithFlags(&c->lane[i], cudaStreamNonBlocking) == cudaSuccess;
         if (!ok) {
             cudaGetLastError();
@@ -1094,15 +1097,17 @@ size_t max_index_bytes(const std::vector<Group> &gr)
 
 /* Waits for every copy and kernel of a pipelined call, then reads (and
  * clears) the workspace's status words. */
-int pipe_finish(DropCtx *c, int rc, uint32_t lanes)
+int pipe_finish(DropCtx *c, int rc, uint32_t lanes, bool walk_lanes = false)
 {
     bool sync_ok = cudaStreamSynchronize(c->st_in) == cudaSuccess &&
                    cudaStreamSynchronize(c->st_out) == cudaSuccess;
     int rc2 = ZCCL_GPU_OK;
-    for (uint32_t l = 0; l < lanes; l++) {
-        const int r = c->lws[l].p ? zccl_gpu_check(c->lws[l].p, c->lane[l]) : ZCCL_GPU_OK;
-        if (!rc2) rc2 = r;
-    }
+    for (uint32_t l = 0; l < lanes; l++)
+        for (uint32_t h = 0; h < (walk_lanes ? 2u : 1u); h++) {
+            const uint32_t i = l + h * kLanes;
+            const int r = c->lws[i].p ? zccl_gpu_check(c->lws[i].p, c->lane[i]) : ZCCL_GPU_OK;
+            if (!rc2) rc2 = r;
+        }
     if (!sync_ok) return ZCCL_GPU_ECUDA;
     return rc ? rc : rc2;
 }
@@ -1333,6 +1338,7 @@ int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned
         for (int i = 0; i < 3; i++)
             if (int rc = c->lix[l][i].ensure(ixb)) return rc;
         if (int rc = c->lws[l].ensure(max_ws_bytes(gr))) return rc;
+        if (int rc = c->lws[kLanes + l].ensure(max_ws_bytes(gr))) return rc;
     }
     if (int rc = c->pin.ensure(poff[G])) return rc;
     uint8_t *pin = (uint8_t *)c->pin.p;
@@ -1342,8 +1348,8 @@ int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned
         const Group &q = gr[k];
         const uint32_t Ts = q.s1 - q.s0;
         const uint32_t l = (uint32_t)(k % NL);
-        cudaStream_t st = c->lane[l];
-        void *ws = c->lws[l].p;
+        cudaStream_t st = c->lane[l], st2 = c->lane[kLanes + l]; /* the second input is walked beside the first */
+        void *ws = c->lws[l].p, *ws2 = c->lws[kLanes + l].p;
         zccl_gpu_stream in[2], sum;
         uint8_t *ib = (uint8_t *)c->s[1].p + ioff[k];
         for (int i = 0; i < 2 && !rc; i++) {
@@ -1363,8 +1369,12 @@ int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned
             in[i].qprev_valid = 0;
             ib += a256(8ull * Ts + len[i][k] + 64);
         }
+        /* the second input's index is the lane pair's: its walk for this
+         * group waits until the add of the pair's previous group is done */
         if (rc || cudaEventRecord(c->ev_in[k], c->st_in) != cudaSuccess ||
-            cudaStreamWaitEvent(st, c->ev_in[k], 0) != cudaSuccess) {
+            cudaStreamWaitEvent(st, c->ev_in[k], 0) != cudaSuccess ||
+            cudaStreamWaitEvent(st2, c->ev_in[k], 0) != cudaSuccess ||
+            (k >= NL && cudaStreamWaitEvent(st2, c->ev_k[k - NL], 0) != cudaSuccess)) {
             rc = rc ? rc : ZCCL_GPU_ECUDA;
             break;
         }
@@ -1374,12 +1384,19 @@ int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned
         sum.index = c->lix[l][2].p;
         sum.indexed = 0;
         sum.qprev_valid = 0;
-        if (ws_clear(ws, q.g, st) != cudaSuccess) {
+        if (ws_clear(ws, q.g, st) != cudaSuccess || ws_clear(ws2, q.g, st2) != cudaSuccess) {
             rc = ZCCL_GPU_ECUDA;
             break;
         }
-        if ((rc = walk_stream(&in[0], q.g, ws, st)) || (rc = walk_stream(&in[1], q.g, ws, st)) ||
-            (rc = zccl_gpu_homadd_cases(&sum, in, 2, (size_t)q.n, (int)g.L, (int)Ts, ws, nullptr, st)))
+        /* a failed walk of the second input is reported by its lane's
+         * status words; the add never trusts an index for its bounds */
+        if ((rc = walk_stream(&in[0], q.g, ws, st)) || (rc = walk_stream(&in[1], q.g, ws2, st2)))
+            break;
+        if (cudaEventRecord(c->ev_w[k], st2) != cudaSuccess || cudaStreamWaitEvent(st, c->ev_w[k], 0) != cudaSuccess) {
+            rc = ZCCL_GPU_ECUDA;
+            break;
+        }
+        if ((rc = zccl_gpu_homadd_cases(&sum, in, 2, (size_t)q.n, (int)g.L, (int)Ts, ws, nullptr, st)))
             break;
         uint8_t *pk = pin + poff[k];
         if (cudaMemcpyAsync(pk, sum.index, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
@@ -1397,7 +1414,7 @@ int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned
         rc = ZCCL_GPU_ECUDA;
     uint64_t placed = 0;
     if (!rc) rc = pipe_place(c, gr, dev, cap, poff, out, g.T, &placed);
-    rc = pipe_finish(c, rc, NL);
+    rc = pipe_finish(c, rc, NL, true);
     if (rc) return rc;
     *out_size += (size_t)(8ull * g.T + placed);
     return ZCCL_GPU_OK;
