@@ -405,34 +405,16 @@ extern "C" int zccl_gpu_decompress_accumulate(float *d_acc, const zccl_gpu_strea
     return cuda_status(launch_decompress_jobs(a, st));
 }
 
-extern "C" int zccl_gpu_homadd_cases(zccl_gpu_stream *out, zccl_gpu_stream *ins, int P, size_t n,
-                                     int L, int T, void *d_ws, unsigned long long *d_cases,
-                                     void *cuda_stream)
+/* The add of P inputs given by their bytes and index arrays (which need
+ * not sit in one stream's index layout), on a cleared workspace. */
+static int homadd_inputs(zccl_gpu_stream *out, const HomInput *in, int P, int qv, const ZGeom &g, void *d_ws,
+                         unsigned long long *d_cases, cudaStream_t st)
 {
-    ZGeom g;
-    if (make_geom(n, L, T, &g) || !valid_stream(out) || !ins || P < 1 || P > ZH_MAXP || !d_ws)
-        return ZCCL_GPU_EINVAL;
-    for (int p = 0; p < P; p++)
-        if (!valid_stream(&ins[p]) || ins[p].bytes == out->bytes) return ZCCL_GPU_EINVAL;
-    cudaStream_t st = (cudaStream_t)cuda_stream;
     if (ws_clear(d_ws, g, st) != cudaSuccess) return ZCCL_GPU_ECUDA;
     ZWork w = bind_ws(d_ws);
     HomAddArgs a;
     memset(&a, 0, sizeof(a));
-    int qv = 1;
-    for (int p = 0; p < P; p++) {
-        if (!ins[p].indexed) {
-            int rc = walk_stream(&ins[p], g, d_ws, st);
-            if (rc) return rc;
-        }
-        ZIndex ix = bind_index(ins[p].index, g);
-        a.job.in[p].bytes = ins[p].bytes;
-        a.job.in[p].avail = ins[p].capacity;
-        a.job.in[p].widths = ix.widths;
-        a.job.in[p].tile_off = ix.tile_off;
-        a.job.in[p].tile_qprev = ix.tile_qprev;
-        qv &= ins[p].qprev_valid ? 1 : 0;
-    }
+    for (int p = 0; p < P; p++) a.job.in[p] = in[p];
     a.job.P = (uint32_t)P;
     a.job.qprev_valid = qv;
     a.job.out = out->bytes;
@@ -450,6 +432,35 @@ extern "C" int zccl_gpu_homadd_cases(zccl_gpu_stream *out, zccl_gpu_stream *ins,
         out->qprev_valid = qv;
     }
     return rc;
+}
+
+extern "C" int zccl_gpu_homadd_cases(zccl_gpu_stream *out, zccl_gpu_stream *ins, int P, size_t n,
+                                     int L, int T, void *d_ws, unsigned long long *d_cases,
+                                     void *cuda_stream)
+{
+    ZGeom g;
+    if (make_geom(n, L, T, &g) || !valid_stream(out) || !ins || P < 1 || P > ZH_MAXP || !d_ws)
+        return ZCCL_GPU_EINVAL;
+    for (int p = 0; p < P; p++)
+        if (!valid_stream(&ins[p]) || ins[p].bytes == out->bytes) return ZCCL_GPU_EINVAL;
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    if (ws_clear(d_ws, g, st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    HomInput in[ZH_MAXP];
+    int qv = 1;
+    for (int p = 0; p < P; p++) {
+        if (!ins[p].indexed) {
+            int rc = walk_stream(&ins[p], g, d_ws, st);
+            if (rc) return rc;
+        }
+        ZIndex ix = bind_index(ins[p].index, g);
+        in[p].bytes = ins[p].bytes;
+        in[p].avail = ins[p].capacity;
+        in[p].widths = ix.widths;
+        in[p].tile_off = ix.tile_off;
+        in[p].tile_qprev = ix.tile_qprev;
+        qv &= ins[p].qprev_valid ? 1 : 0;
+    }
+    return homadd_inputs(out, in, P, qv, g, d_ws, d_cases, st);
 }
 
 extern "C" int zccl_gpu_homadd(zccl_gpu_stream *out, zccl_gpu_stream *ins, int P, size_t n, int L,
@@ -1331,14 +1342,30 @@ int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned
         poff[k + 1] = poff[k] + 8 + 8 * Ts + 2 * 8 * Ts;
     }
     const uint32_t NL = lanes_for(G);
+    /* every group but the last (whose final chunk has no known end) walks
+     * both inputs as one stream of 2 Ts chunks, the first input's chunks and
+     * then the second's: one walk instead of two, each input's index a half
+     * of the pair's */
+    ZGeom gc[kMaxGroups];
+    bool comb[kMaxGroups];
+    size_t ixb = max_index_bytes(gr), wsb = max_ws_bytes(gr);
+    for (size_t k = 0; k < G; k++) {
+        const uint32_t Ts = gr[k].s1 - gr[k].s0;
+        comb[k] = gr[k].s1 < g.T && !make_geom((size_t)(2 * gr[k].n), (int)g.L, (int)(2 * Ts), &gc[k]) &&
+                  gc[k].tbs == g.tbs && gc[k].rem == 0;
+        if (comb[k]) {
+            gc[k].fmt = g.fmt;
+            ixb = std::max(ixb, index_layout(gc[k]).total);
+            wsb = std::max(wsb, ws_bytes(gc[k]));
+        }
+    }
     if (int rc = c->s[1].ensure(ioff[G])) return rc;
     if (int rc = c->s[2].ensure(soff[G])) return rc;
-    const size_t ixb = max_index_bytes(gr);
     for (uint32_t l = 0; l < NL; l++) {
         for (int i = 0; i < 3; i++)
             if (int rc = c->lix[l][i].ensure(ixb)) return rc;
-        if (int rc = c->lws[l].ensure(max_ws_bytes(gr))) return rc;
-        if (int rc = c->lws[kLanes + l].ensure(max_ws_bytes(gr))) return rc;
+        if (int rc = c->lws[l].ensure(wsb)) return rc;
+        if (int rc = c->lws[kLanes + l].ensure(wsb)) return rc;
     }
     if (int rc = c->pin.ensure(poff[G])) return rc;
     uint8_t *pin = (uint8_t *)c->pin.p;
@@ -1352,6 +1379,58 @@ int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned
         void *ws = c->lws[l].p, *ws2 = c->lws[kLanes + l].p;
         zccl_gpu_stream in[2], sum;
         uint8_t *ib = (uint8_t *)c->s[1].p + ioff[k];
+        if (comb[k]) {
+            uint8_t *h = pin + poff[k] + 8 + 8ull * Ts; /* the 2 Ts combined chunk offsets */
+            for (uint32_t j = 0; j < 2 * Ts; j++) {
+                const int i = j < Ts ? 0 : 1;
+                const uint64_t v = (i ? len[0][k] : 0) + e[i][q.s0 + j - i * Ts] - e[i][q.s0];
+                memcpy(h + 8ull * j, &v, 8);
+            }
+            const size_t hb = 16ull * Ts;
+            if (cudaMemcpyAsync(ib, h, hb, cudaMemcpyHostToDevice, c->st_in) != cudaSuccess ||
+                cudaMemcpyAsync(ib + hb, cmp[0] + 8ull * g.T + e[0][q.s0], len[0][k], cudaMemcpyHostToDevice,
+                                c->st_in) != cudaSuccess ||
+                cudaMemcpyAsync(ib + hb + len[0][k], cmp[1] + 8ull * g.T + e[1][q.s0], len[1][k],
+                                cudaMemcpyHostToDevice, c->st_in) != cudaSuccess ||
+                cudaEventRecord(c->ev_in[k], c->st_in) != cudaSuccess ||
+                cudaStreamWaitEvent(st, c->ev_in[k], 0) != cudaSuccess) {
+                rc = ZCCL_GPU_ECUDA;
+                break;
+            }
+            zccl_gpu_stream both;
+            both.bytes = ib;
+            both.capacity = hb + len[0][k] + len[1][k];
+            both.index = c->lix[l][0].p;
+            both.indexed = 0;
+            both.qprev_valid = 0;
+            dev[k] = (uint8_t *)c->s[2].p + soff[k];
+            sum.bytes = dev[k];
+            sum.capacity = cap[k];
+            sum.index = c->lix[l][2].p;
+            sum.indexed = 0;
+            sum.qprev_valid = 0;
+            if (ws_clear(ws, gc[k], st) != cudaSuccess) {
+                rc = ZCCL_GPU_ECUDA;
+                break;
+            }
+            if ((rc = walk_stream(&both, gc[k], ws, st))) break;
+            const ZIndex ix = bind_index(both.index, gc[k]);
+            HomInput hi[2];
+            for (int i = 0; i < 2; i++) {
+                hi[i].bytes = ib;
+                hi[i].avail = both.capacity;
+                hi[i].widths = ix.widths + (size_t)i * q.g.nblocks;
+                hi[i].tile_off = ix.tile_off + (size_t)i * q.g.ntiles;
+                hi[i].tile_qprev = ix.tile_qprev + (size_t)i * q.g.ntiles;
+            }
+            if ((rc = homadd_inputs(&sum, hi, 2, 0, q.g, ws, nullptr, st))) break;
+            uint8_t *pk = pin + poff[k];
+            if (cudaMemcpyAsync(pk, sum.index, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaMemcpyAsync(pk + 8, dev[k], 8ull * Ts, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaEventRecord(c->ev_k[k], st) != cudaSuccess)
+                rc = ZCCL_GPU_ECUDA;
+            continue;
+        }
         for (int i = 0; i < 2 && !rc; i++) {
             uint8_t *h = pin + poff[k] + 8 + 8ull * Ts + 8ull * Ts * i;
             for (uint32_t j = 0; j < Ts; j++) {
