@@ -349,7 +349,7 @@ def reduction_bench(args, L, T, dev):
     import numpy as np
     import torch
     import zccl_gb300 as Z
-    from zccl_gb300.ring import RingAllreduce, reduce_doc, reduce_homomorphic, reduce_pairwise
+    from zccl_gb300.ring import PairwiseTree, RingAllreduce, reduce_doc, reduce_homomorphic, reduce_pairwise
     n, P = args.red_n, args.red_p
     xs = make_rank_chunks(n, P, 3, dev)
     lo = min(float(x.min()) for x in xs)
@@ -363,6 +363,8 @@ def reduction_bench(args, L, T, dev):
     ms_pway = timed(lambda: reduce_homomorphic(codec, streams, out=out), 5, st)
     pair_outs = [codec.new_stream(), codec.new_stream()]
     ms_pair = timed(lambda: reduce_pairwise(codec, streams, pair_outs), 5, st)
+    tree = PairwiseTree(codec, streams, stream=st)
+    ms_tree = timed(tree.run, 5, st)
     docs = codec.new_stream()
     doc_total = torch.empty(n, dtype=torch.float32, device=dev)
     ms_doc = timed(lambda: reduce_doc(codec, streams, eb, out=docs, total=doc_total), 5, st)
@@ -371,9 +373,11 @@ def reduction_bench(args, L, T, dev):
     graph = {}
     gst = torch.cuda.Stream(dev)
     gcodec = Z.Codec(n, L, T, device=str(dev), stream=gst)
+    gtree = PairwiseTree(gcodec, streams, stream=gst)
     keep = []
     for name, fn in (("pway_homadd_ms", lambda: reduce_homomorphic(gcodec, streams, out=out)),
                      ("pairwise_fold_ms", lambda: reduce_pairwise(gcodec, streams, pair_outs)),
+                     ("pairwise_tree_ms", gtree.run),
                      ("doc_ms", lambda: reduce_doc(gcodec, streams, eb, out=docs, total=doc_total))):
         try:
             with torch.cuda.stream(gst):
@@ -387,9 +391,13 @@ def reduction_bench(args, L, T, dev):
         except Exception as e:  # a call that cannot be captured: report it, keep going
             graph[name] = f"not captured: {type(e).__name__}"
     gcodec.check()
-    del keep
+    gtree.check()
+    del keep, gtree
     codec.check()
     same = reduce_homomorphic(codec, streams, out=out).tobytes() == reduce_pairwise(codec, streams).tobytes()
+    same_tree = tree.run().tobytes() == out.tobytes()
+    tree.check()
+    del tree
     exact = torch.zeros(n, dtype=torch.float64, device=dev)
     for x in xs:
         exact += x.double()
@@ -427,10 +435,12 @@ def reduction_bench(args, L, T, dev):
         "pway_homadd_GBps_alg": round((cin + cout) / (ms_pway * 1e-3) / 1e9, 1),
         "pway_homadd_GBps_uncompressed": round(4 * n * P / (ms_pway * 1e-3) / 1e9, 1),
         "pairwise_fold_ms": round(ms_pair, 4),
+        "pairwise_tree_ms": round(ms_tree, 4),
         "doc_ms": round(ms_doc, 4),
         "graph_replay_ms": graph,
         "compress_all_ms": round(ms_compress, 4),
         "pway_equals_pairwise_bytes": same,
+        "pway_equals_pairwise_tree_bytes": same_tree,
         "max_err_over_eb": {"homomorphic": round(err_ho, 3), "doc": round(err_doc, 3), "bound": P},
         "ring_allreduce_emulated_ms": {"homomorphic": round(ms_ring_ho, 3), "doc": round(ms_ring_doc, 3),
                                        "note": f"all {P} ranks' codec work on one GPU, each step's {P} codec "

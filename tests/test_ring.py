@@ -159,7 +159,7 @@ def test_decompress_accumulate_and_decompress_batch(torch, port):
 @pytest.mark.gpu
 def test_one_shot_reductions_match_oracle(torch, port):
     import zccl_gb300 as Z
-    from zccl_gb300.ring import reduce_doc, reduce_homomorphic, reduce_pairwise
+    from zccl_gb300.ring import PairwiseTree, reduce_doc, reduce_homomorphic, reduce_pairwise
     n, P, T, L = 100003, 8, 4, 32
     xs = rank_data(n, P, seed=2)
     eb = float(np.float32(1e-4 * (max(x.max() for x in xs) - min(x.min() for x in xs))))
@@ -171,6 +171,16 @@ def test_one_shot_reductions_match_oracle(torch, port):
     fold = port.homadd_fold(host, n, eb, L, T)
     assert reduce_homomorphic(codec, streams).tobytes() == fold
     assert reduce_pairwise(codec, streams).tobytes() == fold
+    tree = PairwiseTree(codec, streams)
+    assert len(tree.plans) == 3
+    assert tree.run().tobytes() == fold
+    assert tree.run().tobytes() == fold  # replayed
+    tree.check()
+    # an odd count: the odd one out goes up a level unchanged
+    tree5 = PairwiseTree(codec, streams[:5])
+    assert len(tree5.plans) == 3 and len(tree5.sums) == 4
+    assert tree5.run().tobytes() == port.homadd_fold(host[:5], n, eb, L, T)
+    tree5.check()
     doc, _ = reduce_doc(codec, streams, eb)
     total = np.zeros(n, np.float32)
     for h in host:

@@ -5,6 +5,8 @@
  *   width_of()           bit-exact stand-in for (int)log2f((float)m) + 1
  *   encode_full/decode_full   one 32-element block, registers <-> packed bytes
  *   encode_small/decode_small/decode_add_full   the same for widths below 16
+ *   encode_mid/decode_mid     the same for widths 16..23 (two high bytes)
+ *   encode_block32/decode_block32   the fastest of these for a block's width
  *   encode_any/decode_any     any block, one element at a time
  *   Packer / Reader      MSB-first bit streams in shared memory
  *   tma_load_superset()  TMA bulk copy global -> shared
@@ -226,24 +228,45 @@ __device__ __forceinline__ void encode_full(uint32_t sbase, uint32_t o, uint32_t
     pk.finish();
 }
 
+/* The width byte and the four sign bytes of a 32-element fastmode1 block as
+ * one 40-bit little-endian value placed at byte o of the zeroed packing
+ * buffer (two word ORs). */
+__device__ __forceinline__ void put_head(uint32_t sbase, uint32_t o, uint32_t b, uint32_t smask)
+{
+    const uint32_t q = o >> 2, s8 = (o & 3u) * 8u;
+    const uint64_t v = ((uint64_t)bswap32(smask) << 8 | b) << s8; /* at most 40 + 24 bits */
+    sh_or(sbase + 4u * q, (uint32_t)v);
+    sh_or(sbase + 4u * q + 4u, (uint32_t)(v >> 32));
+}
+
+/* The r low bits of the 32 magnitudes m, MSB-first from byte lb (four r-bit
+ * fields merged per put). */
+__device__ __forceinline__ void put_low_bits(uint32_t sbase, uint32_t lb, uint32_t r, const uint32_t (&m)[32])
+{
+    const uint32_t p = 1u << r, mask = p - 1u;
+    Packer pk;
+    pk.init(sbase, lb);
+#pragma unroll
+    for (int j = 0; j < 32; j += 4) {
+        const uint32_t v0 = m[j] & mask, v1 = m[j + 1] & mask, v2 = m[j + 2] & mask, v3 = m[j + 3] & mask;
+        pk.put(((v0 * p + v1) * p + v2) * p + v3, 4u * r);
+        pk.flush();
+    }
+    pk.finish();
+}
+
 /* encode_full for a width of 1..15 bits (B = b/8 <= 1 whole byte per
  * magnitude), the common case at the error bounds the collectives use, with
  * whole words instead of the bit packer where the layout allows: the header
- * and the four sign bytes as one 40-bit little-endian value placed at byte o
- * (two word ORs), and for B = 1 the 32 high bytes as eight little-endian
- * words realigned to their byte offset by funnel shifts (nine word ORs); the
- * low bits go through the packer as in encode_full.  Same bytes as
- * encode_full in the fastmode1 layout. */
+ * and the four sign bytes by put_head, and for B = 1 the 32 high bytes as
+ * eight little-endian words realigned to their byte offset by funnel shifts
+ * (nine word ORs); the low bits go through the packer as in encode_full.
+ * Same bytes as encode_full in the fastmode1 layout. */
 __device__ __forceinline__ void encode_small(uint32_t sbase, uint32_t o, uint32_t b, uint32_t smask,
                                              const uint32_t (&m)[32])
 {
     const uint32_t B = b >> 3, r = b & 7u;
-    {
-        const uint32_t q = o >> 2, s8 = (o & 3u) * 8u;
-        const uint64_t v = ((uint64_t)bswap32(smask) << 8 | b) << s8; /* at most 40 + 24 bits */
-        sh_or(sbase + 4u * q, (uint32_t)v);
-        sh_or(sbase + 4u * q + 4u, (uint32_t)(v >> 32));
-    }
+    put_head(sbase, o, b, smask);
     const uint32_t hb = o + 5u;
     if (B) {
         const uint32_t q = hb >> 2, sh = (hb & 3u) * 8u;
@@ -258,18 +281,42 @@ __device__ __forceinline__ void encode_small(uint32_t sbase, uint32_t o, uint32_
         }
         if (sh) sh_or(sbase + 4u * (q + 8u), prev >> (32u - sh));
     }
-    if (r) {
-        const uint32_t p = 1u << r, mask = p - 1u;
-        Packer pk;
-        pk.init(sbase, hb + 32u * B);
+    if (r) put_low_bits(sbase, hb + 32u * B, r, m);
+}
+
+/* encode_full for a width of 16..23 bits (B = 2 whole bytes per magnitude):
+ * the header by put_head, the 32 two-byte high parts (little-endian per
+ * element) as sixteen words of two elements each, realigned to their byte
+ * offset by funnel shifts (seventeen word ORs), the low bits through the
+ * packer.  Same bytes as encode_full in the fastmode1 layout. */
+__device__ __forceinline__ void encode_mid(uint32_t sbase, uint32_t o, uint32_t b, uint32_t smask,
+                                           const uint32_t (&m)[32])
+{
+    const uint32_t r = b & 7u;
+    put_head(sbase, o, b, smask);
+    const uint32_t hb = o + 5u, q = hb >> 2, sh = (hb & 3u) * 8u;
+    uint32_t prev = 0;
 #pragma unroll
-        for (int j = 0; j < 32; j += 4) {
-            const uint32_t v0 = m[j] & mask, v1 = m[j + 1] & mask, v2 = m[j + 2] & mask, v3 = m[j + 3] & mask;
-            pk.put(((v0 * p + v1) * p + v2) * p + v3, 4u * r);
-            pk.flush();
-        }
-        pk.finish();
+    for (int k = 0; k < 16; k++) {
+        const uint32_t W = __byte_perm(m[2 * k] >> r, m[2 * k + 1] >> r, 0x5410u); /* elements 2k, 2k + 1 */
+        sh_or(sbase + 4u * (q + (uint32_t)k), __funnelshift_l(prev, W, sh));
+        prev = W;
     }
+    if (sh) sh_or(sbase + 4u * (q + 16u), prev >> (32u - sh));
+    if (r) put_low_bits(sbase, hb + 64u, r, m);
+}
+
+/* The fastmode1 encoder for a full 32-element block of width b: the word
+ * forms for widths 1..23, encode_full otherwise. */
+__device__ __forceinline__ void encode_block32(uint32_t sbase, uint32_t o, uint32_t b, uint32_t smask,
+                                               const uint32_t (&m)[32])
+{
+    if (b && b < 16)
+        encode_small(sbase, o, b, smask, m);
+    else if (b >= 16 && b < 24)
+        encode_mid(sbase, o, b, smask, m);
+    else
+        encode_full(sbase, o, b, smask, m);
 }
 
 /* Bytes a .. a + 7 of the shared words w as a 64-bit big-endian value
@@ -420,13 +467,78 @@ __device__ __forceinline__ uint32_t decode_small(const uint32_t *w, uint32_t o, 
     return sum;
 }
 
+/* decode_full for a fastmode1 block of width 16..23 (B = 2), the form of
+ * decode_small with two bytes per magnitude: group g's sixteen high bytes are
+ * four realigned words, two elements each (little-endian halves); the low
+ * bits and signs come as in decode_small.  ADD: d[j] += delta j (the
+ * homomorphic add's accumulation, returns 0); otherwise d[j] = delta j and
+ * the wrapped sum of the deltas is returned. */
+template <bool ADD>
+__device__ __forceinline__ uint32_t decode_mid(const uint32_t *w, uint32_t o, uint32_t b, uint32_t (&d)[32])
+{
+    const uint32_t r = b & 7u;
+    uint32_t sg, unused;
+    be64_at(w, o + 1, sg, unused);
+    const uint32_t hb = o + 5, lb = hb + 64u;
+    const uint32_t k0 = hb >> 2, sh = (hb & 3u) * 8u;
+    uint32_t tk[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) tk[k] = sg << k; /* element 8g + k's sign: top bit of byte 3 - g */
+    const uint32_t r1 = r, r2 = 2u * r, r3 = 3u * r;
+    uint32_t prev = w[k0], sum = 0;
+#pragma unroll
+    for (int g = 0; g < 4; g++) {
+        uint32_t A[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint32_t nx = w[k0 + 4 * g + i + 1];
+            A[i] = __funnelshift_r(prev, nx, sh); /* bytes hb + 16g + 4i .. + 3: elements 8g + 2i, 8g + 2i + 1 */
+            prev = nx;
+        }
+        uint32_t hi, lo;
+        be64_at(w, lb + (uint32_t)g * r, hi, lo);
+        const uint32_t h2 = __funnelshift_l(lo, hi, 4u * r); /* fields 4 .. 7 on top */
+        const uint32_t sel = 0x1111u * (8u | (3u - (uint32_t)g));
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t H = __byte_perm(A[k >> 1], 0, (k & 1) ? 0x4432u : 0x4410u);
+            const uint32_t src = k < 4 ? hi : h2;
+            const uint32_t s1 = (k & 3) == 0 ? 0u : (k & 3) == 1 ? r1 : (k & 3) == 2 ? r2 : r3;
+            const uint32_t m = __funnelshift_l(src << s1, H, r);
+            const uint32_t s = prmt_sign(tk[k], sel); /* all ones when negative */
+            const uint32_t v = (m ^ s) - s;
+            if (ADD) {
+                d[8 * g + k] += v;
+            } else {
+                d[8 * g + k] = v;
+                sum += v;
+            }
+        }
+    }
+    return sum;
+}
+
+/* The fastmode1 decoder for a full 32-element block of width b: the word
+ * forms for widths 0..23, decode_full otherwise.  Returns the wrapped sum. */
+__device__ __forceinline__ uint32_t decode_block32(const uint32_t *w, uint32_t o, uint32_t b, uint32_t (&d)[32])
+{
+    if (b < 16) return decode_small(w, o, b, d);
+    if (b < 24) return decode_mid<false>(w, o, b, d);
+    return decode_full(w, o, b, d);
+}
+
 /* The deltas of a fastmode1 block of width b at byte o added into acc
  * (acc[j] += delta j), for the homomorphic add.  Widths 1..15 take the
- * width-uniform path of decode_small; 16..32 read two to four whole bytes per
- * magnitude group by group, so that no second array of 32 values is live. */
+ * width-uniform path of decode_small, 16..23 decode_mid; 24..32 read three
+ * or four whole bytes per magnitude group by group, so that no second array
+ * of 32 values is live. */
 __device__ __forceinline__ void decode_add_full(const uint32_t *w, uint32_t o, uint32_t b, uint32_t (&acc)[32])
 {
     if (b == 0) return;
+    if (b >= 16 && b < 24) {
+        decode_mid<true>(w, o, b, acc);
+        return;
+    }
     const uint32_t B = b >> 3, r = b & 7u;
     uint32_t sg, unused;
     be64_at(w, o + 1, sg, unused);

@@ -368,8 +368,8 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
         const uint32_t o = headb + off;
         if (FAST) {
             if (n == 32) {
-                if (b && b < 16 && g.fmt == ZG_FASTMODE1)
-                    encode_small(pk_sa, o, b, smask, m);
+                if (g.fmt == ZG_FASTMODE1)
+                    encode_block32(pk_sa, o, b, smask, m);
                 else
                     encode_full(pk_sa, o, b, smask, m, g.fmt);
             } else if (own) {

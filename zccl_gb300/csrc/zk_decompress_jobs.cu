@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(256, 3) k_decompress_jobs(const __grid_constan
         uint32_t bsum = 0;
         if (own && buf[o] != b) bad |= ZERR_CORRUPT;
         if (full) {
-            bsum = g.fmt == ZG_FASTMODE1 && b < 16 ? decode_small(sw, o, b, d) : decode_full(sw, o, b, d, g.fmt);
+            bsum = g.fmt == ZG_FASTMODE1 ? decode_block32(sw, o, b, d) : decode_full(sw, o, b, d, g.fmt);
         } else if (own) {
             decode_any(sw, o, b, n, [&](uint32_t, uint32_t v) { bsum += v; }, g.fmt);
         }

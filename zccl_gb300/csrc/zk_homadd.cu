@@ -460,10 +460,7 @@ __global__ void __launch_bounds__(320, 2) k_homadd(const __grid_constant__ HomAd
         if (has_head && tid == 0) *reinterpret_cast<uint32_t *>(pk) = hsum;
         const uint32_t o = headb + off;
         if (full32) {
-            if (b && b < 16)
-                encode_small(pk_sa, o, b, smask, acc);
-            else
-                encode_full(pk_sa, o, b, smask, acc);
+            encode_block32(pk_sa, o, b, smask, acc);
         } else if (own) {
             encode_any(pk_sa, o, b, n, [&](uint32_t j, uint32_t &neg, uint32_t &mg) {
                 const uint32_t v = FAST ? pick(acc, j) : acc_rows[tid * stride + j];

@@ -25,8 +25,8 @@ stream of one GPU.  All ranks end with the same floats, so one copy of the
 result is returned; `per_rank_outputs=True` keeps every rank's copy.
 
 Also here: the one-shot reduction of P ranks' chunks (the P-way
-homomorphic add against decompress-add-recompress) that the P = 8 x 16M
-benchmark measures.
+homomorphic add, the pairwise fold, the pairwise tree, against
+decompress-add-recompress) that the P = 8 x 16M benchmark measures.
 """
 from __future__ import annotations
 
@@ -248,6 +248,47 @@ def reduce_pairwise(codec: Codec, streams: list[DeviceStream], outs: list[Device
     for i, s in enumerate(streams[1:]):
         acc = codec.homadd([s, acc], out=outs[i & 1] if outs else None)
     return acc
+
+
+class PairwiseTree:
+    """The same sum by two-way adds arranged as a binary tree: level k adds
+    pairs of level k - 1's sums (an odd one out goes up unchanged), every
+    pair of a level in one batch launch, so ceil(log2 P) launches instead of
+    the fold's P - 1 calls.  Addition modulo 2^32 is associative and a
+    sum's encoding depends on its values alone, so the result is the fold's
+    bytes.  Planned once for the given streams, whose buffers the plans
+    bind; each sum gets a stream of its own (P - 1 in all), so no add
+    writes over a stream another add of its level reads.  run() replays the
+    levels on `stream` (a torch stream, default the current one) and returns
+    the sum."""
+
+    def __init__(self, codec: Codec, streams: list[DeviceStream], stream=None):
+        if len(streams) < 2:
+            raise ValueError("a pairwise tree needs at least two streams")
+        self.stream = stream
+        self.plans: list[Batch] = []
+        self.sums: list[DeviceStream] = []
+        cur = list(streams)
+        while len(cur) > 1:
+            nxt, jobs = [], []
+            for i in range(0, len(cur) - 1, 2):
+                o = codec.new_stream()
+                self.sums.append(o)
+                jobs.append(([cur[i], cur[i + 1]], codec.T, o))
+                nxt.append(o)
+            if len(cur) & 1:
+                nxt.append(cur[-1])
+            self.plans.append(Batch(BATCH_HOMADD, jobs, codec.L, device=codec.device, stream=stream))
+            cur = nxt
+        self.result = cur[0]
+
+    def run(self) -> DeviceStream:
+        for b in self.plans:
+            b.run(self.stream)
+        return self.result
+
+    def check(self):
+        check_all(self.plans)
 
 
 def reduce_doc(codec: Codec, streams: list[DeviceStream], eb: float, out: DeviceStream | None = None,
