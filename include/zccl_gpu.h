@@ -167,7 +167,9 @@ typedef struct zccl_gpu_stream {
 size_t zccl_gpu_max_stream_bytes(size_t n, int L, int T);
 /* Bytes of the side index of one stream (about n/L + 12 per 8192 floats). */
 size_t zccl_gpu_index_bytes(size_t n, int L, int T);
-/* Bytes of device scratch one call needs (look-back state, error word).
+/* Bytes of device scratch one call needs (look-back state, error word, and
+ * for streams that arrive without an index the header walk's tables, about
+ * one byte per byte of the largest stream of this geometry).
  * Its first 8 bytes are two status words: zero them once when the
  * workspace is allocated.  Every call leaves them alone (it zeroes only its
  * own look-back state) and ORs the errors it detects into them, so the

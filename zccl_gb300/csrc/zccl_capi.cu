@@ -103,7 +103,7 @@ ZIndex bind_index(void *mem, const ZGeom &g)
  * header-walk scratch.  Only the first part is cleared per call. */
 struct WalkLayout {
     uint32_t M, max_windows, max_groups;
-    size_t seg_P, seg_R, seg_end, seg_ok, win_base, grp_base, wtab, gtab, gentry, gbase, total;
+    size_t seg_P, seg_R, seg_end, seg_ok, win_base, grp_base, wtab, gtab, gentry, gbase, wexit, total;
 };
 
 size_t ws_clear_bytes(const ZGeom &g) { return 16 + 8 * g.ntiles; }
@@ -134,6 +134,7 @@ WalkLayout walk_layout(const ZGeom &g)
     l.gtab = o; o = align16(o + 8ull * l.max_groups * l.M);
     l.gentry = o; o = align16(o + 4ull * l.max_groups);
     l.gbase = o; o = align16(o + 8ull * l.max_groups);
+    l.wexit = o; o = align16(o + (size_t)WALK_WW * l.max_windows * (l.M < 256 ? 1u : 2u));
     l.total = o + 16;
     return l;
 }
@@ -199,6 +200,7 @@ int walk_stream(zccl_gpu_stream *s, const ZGeom &g, void *ws, cudaStream_t st)
     a.ws.gtab = (uint64_t *)(p + l.gtab);
     a.ws.gentry = (uint32_t *)(p + l.gentry);
     a.ws.gbase = (uint64_t *)(p + l.gbase);
+    a.ws.wexit = p + l.wexit;
     a.max_windows = l.max_windows;
     a.max_groups = l.max_groups;
     int rc = cuda_status(launch_walk(a, st));
@@ -872,7 +874,7 @@ struct PinBuf {
  * walk launches few CTAs, so neighbouring groups' kernels run side by side. */
 constexpr uint32_t kMaxGroups = 8;
 constexpr uint32_t kLanes = 4;
-constexpr uint32_t kWalkLanes = 2 * kLanes; /* the add walks its second input on lane l + kLanes */
+constexpr uint32_t kWalkLanes = 2 * kLanes; /* workspaces: the add's second walk of lane l uses l + kLanes */
 /* groups per call: compression has no walk, so finer groups overlap more;
  * decompression and the add walk each group's headers, whose kernels carry
  * a fixed cost per launch */
@@ -886,8 +888,8 @@ struct DropCtx {
     cudaStream_t st_in = nullptr, st_out = nullptr; /* the pipelined drop-ins' copies */
     cudaEvent_t ev = nullptr;
     cudaEvent_t ev_in[kMaxGroups] = {}, ev_k[kMaxGroups] = {}, ev_w[kMaxGroups] = {};
-    cudaStream_t lane[kWalkLanes] = {};
-    DevBuf lws[kWalkLanes], lix[kLanes][3]; /* per lane: workspace; per compute lane: indexes */
+    cudaStream_t lane[kLanes] = {};
+    DevBuf lws[kWalkLanes], lix[kLanes][3]; /* per lane: two workspaces and three indexes */
     DevBuf fin, fout, s[3], ix[3], ws;
     DevBuf aux; /* counters read back by the _record entry points */
     PinBuf pin;
@@ -902,18 +904,24 @@ DropCtx *drop_ctx()
     std::lock_guard<std::mutex> lk(gmu);
     if (!ctxs[dev]) {
         DropCtx *c = new DropCtx();
-        bool ok = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) == cudaSuccess &&
-                  cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking) == cudaSuccess &&
-                  cudaStreamCreateWithFlags(&c->st_in, cudaStreamNonBlocking) == cudaSuccess &&
-                  cudaStreamCreateWithFlags(&c->st_out, cudaStreamNonBlocking) == cudaSuccess &&
-                  cudaEventCreateWithFlags(&c->ev, cudaEventDisableTiming) == cudaSuccess;
+        /* The device feeds streams through a fixed number of hardware queues
+         * (eight unless CUDA_DEVICE_MAX_CONNECTIONS says otherwise), and two
+         * streams that share one run one after the other.  The pipelined
+         * drop-ins therefore send their outputs out on the lanes that made
+         * them (a separate copy stream was seen to wait behind another
+         * lane's kernels) and keep to st_in and four lanes. */
+        bool ok = cudaStreamCreateWithFlags(&c->st_in, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaStreamCreateWithFlags(&c->st_out, cudaStreamNonBlocking) == cudaSuccess;
+        for (uint32_t i = 0; ok && i < kLanes; i++)
+            ok = cudaStreamCreateWithFlags(&c->lane[i], cudaStreamNonBlocking) == cudaSuccess;
+        ok = ok && cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) == cudaSuccess &&
+             cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking) == cudaSuccess &&
+             cudaEventCreateWithFlags(&c->ev, cudaEventDisableTiming) == cudaSuccess;
         for (uint32_t i = 0; ok && i < kMaxGroups; i++)
             ok = cudaEventCreateWithFlags(&c->ev_in[i], cudaEventDisableTiming) == cudaSuccess &&
                  cudaEventCreateWithFlags(&c->ev_k[i], cudaEventDisableTiming) == cudaSuccess;
         for (uint32_t i = 0; ok && i < kMaxGroups; i++)
             ok = cudaEventCreateWithFlags(&c->ev_w[i], cudaEventDisableTiming) == cudaSuccess;
-        for (uint32_t i = 0; ok && i < kWalkLanes; i++)
-            ok = cudaStreamCreateWithFlags(&c->lane[i], cudaStreamNonBlocking) == cudaSuccess;
         if (!ok) {
             cudaGetLastError();
             delete c;
@@ -922,6 +930,18 @@ DropCtx *drop_ctx()
         ctxs[dev] = c;
     }
     return ctxs[dev];
+}
+
+/* Page-locked host memory (cudaHostAlloc, cudaHostRegister): copies from it
+ * are asynchronous; from pageable memory the host waits for each one. */
+bool is_pinned_ptr(const void *p)
+{
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
 }
 
 bool is_device_ptr(const void *p)
@@ -1112,11 +1132,13 @@ int pipe_finish(DropCtx *c, int rc, uint32_t lanes, bool walk_lanes = false)
 {
     bool sync_ok = cudaStreamSynchronize(c->st_in) == cudaSuccess &&
                    cudaStreamSynchronize(c->st_out) == cudaSuccess;
+    for (uint32_t l = 0; l < lanes; l++) /* after an early stop, work may remain on any lane */
+        sync_ok = cudaStreamSynchronize(c->lane[l]) == cudaSuccess && sync_ok;
     int rc2 = ZCCL_GPU_OK;
     for (uint32_t l = 0; l < lanes; l++)
         for (uint32_t h = 0; h < (walk_lanes ? 2u : 1u); h++) {
             const uint32_t i = l + h * kLanes;
-            const int r = c->lws[i].p ? zccl_gpu_check(c->lws[i].p, c->lane[i]) : ZCCL_GPU_OK;
+            const int r = c->lws[i].p ? zccl_gpu_check(c->lws[i].p, c->lane[l]) : ZCCL_GPU_OK;
             if (!rc2) rc2 = r;
         }
     if (!sync_ok) return ZCCL_GPU_ECUDA;
@@ -1125,18 +1147,31 @@ int pipe_finish(DropCtx *c, int rc, uint32_t lanes, bool walk_lanes = false)
 
 uint32_t lanes_for(size_t groups) { return (uint32_t)std::min<size_t>(groups, kLanes); }
 
-/* The caller's output stream from the groups' device streams: per group (in
- * order, as each one's size and header arrive in pinned memory) its chunk
- * offsets rebased into the caller's header and its chunk bytes copied out.
+/* The caller's output stream from the groups' device streams, group by
+ * group in order: group k's size and header (in pinned memory once its
+ * event has fired) give its chunk offsets, rebased into the caller's header,
+ * and its chunk bytes are copied out on the stream given: the group's own
+ * lane, before anything else is queued there.  (A separate copy stream can
+ * share a hardware queue with a busy lane and wait behind its kernels.)
  * dev[k] is group k's device stream, cap[k] its capacity, pin + poff[k] its
- * size and header.  Returns the chunk bytes placed. */
-int pipe_place(DropCtx *c, const std::vector<Group> &gr, uint8_t *const *dev, const size_t *cap,
-               const size_t *poff, unsigned char *out, uint32_t T, uint64_t *placed)
-{
-    const uint8_t *pin = (const uint8_t *)c->pin.p;
-    uint64_t run = 0;
-    for (size_t k = 0; k < gr.size(); k++) {
+ * size and header; with after_inputs every copy waits for c->ev (recorded
+ * once every input copy is issued), for an output written over an input. */
+struct Placer {
+    DropCtx *c;
+    const std::vector<Group> &gr;
+    uint8_t *const *dev;
+    const size_t *cap, *poff;
+    unsigned char *out;
+    uint32_t T;
+    bool after_inputs;
+    uint64_t run = 0; /* chunk bytes placed */
+    size_t next = 0;  /* the next group to place */
+
+    int place(cudaStream_t st)
+    {
+        const size_t k = next++;
         const Group &q = gr[k];
+        const uint8_t *pin = (const uint8_t *)c->pin.p;
         if (cudaEventSynchronize(c->ev_k[k]) != cudaSuccess) return ZCCL_GPU_ECUDA;
         uint64_t size;
         memcpy(&size, pin + poff[k], 8);
@@ -1148,15 +1183,14 @@ int pipe_place(DropCtx *c, const std::vector<Group> &gr, uint8_t *const *dev, co
             e += run;
             memcpy(out + 8ull * (q.s0 + i), &e, 8);
         }
-        if (cudaStreamWaitEvent(c->st_out, c->ev_k[k], 0) != cudaSuccess ||
-            cudaMemcpyAsync(out + 8ull * T + run, dev[k] + hdr, size - hdr, cudaMemcpyDeviceToHost, c->st_out) !=
+        if ((after_inputs && cudaStreamWaitEvent(st, c->ev, 0) != cudaSuccess) ||
+            cudaMemcpyAsync(out + 8ull * T + run, dev[k] + hdr, size - hdr, cudaMemcpyDeviceToHost, st) !=
                 cudaSuccess)
             return ZCCL_GPU_ECUDA;
         run += size - hdr;
+        return ZCCL_GPU_OK;
     }
-    *placed = run;
-    return ZCCL_GPU_OK;
-}
+};
 
 /* Compression of host floats into a host stream, group by group. */
 int pipe_compress(DropCtx *c, unsigned char *out, const float *x, size_t *outSize, float eb, const ZGeom &g,
@@ -1180,14 +1214,28 @@ int pipe_compress(DropCtx *c, unsigned char *out, const float *x, size_t *outSiz
     float *fin = (float *)c->fin.p;
     uint8_t *dev[kMaxGroups];
     int rc = ZCCL_GPU_OK;
+    /* from pinned memory every group's floats are queued for the link first,
+     * so that the host waiting to place an earlier group never leaves the
+     * link idle; from pageable memory (each copy holds the host) group by
+     * group, each just before its kernels */
+    auto copy_in = [&](size_t k) {
+        return cudaMemcpyAsync(fin + gr[k].e0, x + gr[k].e0, 4 * gr[k].n, cudaMemcpyHostToDevice, c->st_in) ==
+                       cudaSuccess &&
+                       cudaEventRecord(c->ev_in[k], c->st_in) == cudaSuccess
+                   ? ZCCL_GPU_OK
+                   : ZCCL_GPU_ECUDA;
+    };
+    const bool upfront = is_pinned_ptr(x);
+    for (size_t k = 0; upfront && k < G && !rc; k++) rc = copy_in(k);
+    for (size_t k = 0; k < G; k++) dev[k] = (uint8_t *)c->s[0].p + soff[k];
+    Placer pl{c, gr, dev, cap, poff, out, g.T, false};
     for (size_t k = 0; k < G && !rc; k++) {
         const Group &q = gr[k];
         const uint32_t l = (uint32_t)(k % NL);
         cudaStream_t st = c->lane[l];
-        dev[k] = (uint8_t *)c->s[0].p + soff[k];
-        if (cudaMemcpyAsync(fin + q.e0, x + q.e0, 4 * q.n, cudaMemcpyHostToDevice, c->st_in) != cudaSuccess ||
-            cudaEventRecord(c->ev_in[k], c->st_in) != cudaSuccess ||
-            cudaStreamWaitEvent(st, c->ev_in[k], 0) != cudaSuccess) {
+        if (!upfront && (rc = copy_in(k))) break;
+        if (k >= NL && (rc = pl.place(st))) break; /* group k - NL, which ran on this lane */
+        if (cudaStreamWaitEvent(st, c->ev_in[k], 0) != cudaSuccess) {
             rc = ZCCL_GPU_ECUDA;
             break;
         }
@@ -1206,11 +1254,10 @@ int pipe_compress(DropCtx *c, unsigned char *out, const float *x, size_t *outSiz
             cudaEventRecord(c->ev_k[k], st) != cudaSuccess)
             rc = ZCCL_GPU_ECUDA;
     }
-    uint64_t placed = 0;
-    if (!rc) rc = pipe_place(c, gr, dev, cap, poff, out, g.T, &placed);
+    while (!rc && pl.next < G) rc = pl.place(c->lane[pl.next % NL]);
     rc = pipe_finish(c, rc, NL);
     if (rc) return rc;
-    *outSize = (size_t)(8ull * g.T + placed);
+    *outSize = (size_t)(8ull * g.T + pl.run);
     return ZCCL_GPU_OK;
 }
 
@@ -1308,9 +1355,9 @@ int pipe_decompress(DropCtx *c, float *y, const unsigned char *cmp, float eb, co
         sub.qprev_valid = 0;
         if ((rc = decompress_fmt(fout + q.e0, &sub, (size_t)q.n, eb, (int)g.L, (int)Ts, c->lws[l].p, st, g.fmt)))
             break;
-        if (cudaEventRecord(c->ev_k[k], st) != cudaSuccess ||
-            cudaStreamWaitEvent(c->st_out, c->ev_k[k], 0) != cudaSuccess ||
-            cudaMemcpyAsync(y + q.e0, fout + q.e0, 4 * q.n, cudaMemcpyDeviceToHost, c->st_out) != cudaSuccess)
+        /* the floats leave on the group's lane: a separate copy stream may
+         * share a hardware queue with a busy lane (see drop_ctx) */
+        if (cudaMemcpyAsync(y + q.e0, fout + q.e0, 4 * q.n, cudaMemcpyDeviceToHost, st) != cudaSuccess)
             rc = ZCCL_GPU_ECUDA;
     }
     return pipe_finish(c, rc, NL);
@@ -1371,13 +1418,14 @@ int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned
     uint8_t *pin = (uint8_t *)c->pin.p;
     uint8_t *dev[kMaxGroups];
     int rc = ZCCL_GPU_OK;
-    for (size_t k = 0; k < G && !rc; k++) {
+    /* from pinned memory every group's input bytes are queued for the link
+     * first, so that the host waiting to place an earlier group never leaves
+     * the link idle; from pageable memory (each copy holds the host) group
+     * by group, each just before its kernels */
+    auto copy_in = [&](size_t k) -> int {
+        int rc = ZCCL_GPU_OK;
         const Group &q = gr[k];
         const uint32_t Ts = q.s1 - q.s0;
-        const uint32_t l = (uint32_t)(k % NL);
-        cudaStream_t st = c->lane[l], st2 = c->lane[kLanes + l]; /* the second input is walked beside the first */
-        void *ws = c->lws[l].p, *ws2 = c->lws[kLanes + l].p;
-        zccl_gpu_stream in[2], sum;
         uint8_t *ib = (uint8_t *)c->s[1].p + ioff[k];
         if (comb[k]) {
             uint8_t *h = pin + poff[k] + 8 + 8ull * Ts; /* the 2 Ts combined chunk offsets */
@@ -1391,25 +1439,63 @@ int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned
                 cudaMemcpyAsync(ib + hb, cmp[0] + 8ull * g.T + e[0][q.s0], len[0][k], cudaMemcpyHostToDevice,
                                 c->st_in) != cudaSuccess ||
                 cudaMemcpyAsync(ib + hb + len[0][k], cmp[1] + 8ull * g.T + e[1][q.s0], len[1][k],
-                                cudaMemcpyHostToDevice, c->st_in) != cudaSuccess ||
-                cudaEventRecord(c->ev_in[k], c->st_in) != cudaSuccess ||
-                cudaStreamWaitEvent(st, c->ev_in[k], 0) != cudaSuccess) {
+                                cudaMemcpyHostToDevice, c->st_in) != cudaSuccess)
                 rc = ZCCL_GPU_ECUDA;
-                break;
+        } else {
+            for (int i = 0; i < 2 && !rc; i++) {
+                uint8_t *h = pin + poff[k] + 8 + 8ull * Ts + 8ull * Ts * i;
+                for (uint32_t j = 0; j < Ts; j++) {
+                    const uint64_t v = e[i][q.s0 + j] - e[i][q.s0];
+                    memcpy(h + 8ull * j, &v, 8);
+                }
+                if (cudaMemcpyAsync(ib, h, 8ull * Ts, cudaMemcpyHostToDevice, c->st_in) != cudaSuccess ||
+                    cudaMemcpyAsync(ib + 8ull * Ts, cmp[i] + 8ull * g.T + e[i][q.s0], len[i][k],
+                                    cudaMemcpyHostToDevice, c->st_in) != cudaSuccess)
+                    rc = ZCCL_GPU_ECUDA;
+                ib += a256(8ull * Ts + len[i][k] + 64);
             }
+        }
+        if (!rc && cudaEventRecord(c->ev_in[k], c->st_in) != cudaSuccess) rc = ZCCL_GPU_ECUDA;
+        return rc;
+    };
+    const bool upfront = is_pinned_ptr(cmp1) && is_pinned_ptr(cmp2);
+    for (size_t k = 0; upfront && k < G && !rc; k++) rc = copy_in(k);
+    /* the sum written over an input (the ring adds into its receive
+     * buffer): no byte goes out before every input byte is in */
+    const size_t out_span = (size_t)zg_stream_worst(&g);
+    const size_t in_span0 = 8ull * g.T + (size_t)(e[0][gr[G - 1].s0] + len[0][G - 1]);
+    const size_t in_span1 = 8ull * g.T + (size_t)(e[1][gr[G - 1].s0] + len[1][G - 1]);
+    const bool after_inputs = overlaps(out, out_span, cmp1, in_span0) || overlaps(out, out_span, cmp2, in_span1);
+    if (!upfront && after_inputs) /* an output over pageable inputs: every input in first */
+        for (size_t k = 0; k < G && !rc; k++) rc = copy_in(k);
+    if (!rc && after_inputs && cudaEventRecord(c->ev, c->st_in) != cudaSuccess) rc = ZCCL_GPU_ECUDA;
+    const bool per_group = !upfront && !after_inputs;
+    for (size_t k = 0; k < G; k++) dev[k] = (uint8_t *)c->s[2].p + soff[k];
+    Placer pl{c, gr, dev, cap, poff, out, g.T, after_inputs};
+    for (size_t k = 0; k < G && !rc; k++) {
+        const Group &q = gr[k];
+        const uint32_t Ts = q.s1 - q.s0;
+        const uint32_t l = (uint32_t)(k % NL);
+        /* a second input's walk runs on the next lane, beside the first's */
+        cudaStream_t st = c->lane[l], st2 = c->lane[(l + 1) % NL];
+        void *ws = c->lws[l].p, *ws2 = c->lws[kLanes + l].p;
+        if (per_group && (rc = copy_in(k))) break;
+        if (k >= NL && (rc = pl.place(st))) break; /* group k - NL, which ran on this lane */
+        zccl_gpu_stream in[2], sum;
+        uint8_t *ib = (uint8_t *)c->s[1].p + ioff[k];
+        sum.bytes = dev[k];
+        sum.capacity = cap[k];
+        sum.index = c->lix[l][2].p;
+        sum.indexed = 0;
+        sum.qprev_valid = 0;
+        if (comb[k]) {
             zccl_gpu_stream both;
             both.bytes = ib;
-            both.capacity = hb + len[0][k] + len[1][k];
+            both.capacity = 16ull * Ts + len[0][k] + len[1][k];
             both.index = c->lix[l][0].p;
             both.indexed = 0;
             both.qprev_valid = 0;
-            dev[k] = (uint8_t *)c->s[2].p + soff[k];
-            sum.bytes = dev[k];
-            sum.capacity = cap[k];
-            sum.index = c->lix[l][2].p;
-            sum.indexed = 0;
-            sum.qprev_valid = 0;
-            if (ws_clear(ws, gc[k], st) != cudaSuccess) {
+            if (cudaStreamWaitEvent(st, c->ev_in[k], 0) != cudaSuccess || ws_clear(ws, gc[k], st) != cudaSuccess) {
                 rc = ZCCL_GPU_ECUDA;
                 break;
             }
@@ -1424,75 +1510,44 @@ int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned
                 hi[i].tile_qprev = ix.tile_qprev + (size_t)i * q.g.ntiles;
             }
             if ((rc = homadd_inputs(&sum, hi, 2, 0, q.g, ws, nullptr, st))) break;
-            uint8_t *pk = pin + poff[k];
-            if (cudaMemcpyAsync(pk, sum.index, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-                cudaMemcpyAsync(pk + 8, dev[k], 8ull * Ts, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-                cudaEventRecord(c->ev_k[k], st) != cudaSuccess)
-                rc = ZCCL_GPU_ECUDA;
-            continue;
-        }
-        for (int i = 0; i < 2 && !rc; i++) {
-            uint8_t *h = pin + poff[k] + 8 + 8ull * Ts + 8ull * Ts * i;
-            for (uint32_t j = 0; j < Ts; j++) {
-                const uint64_t v = e[i][q.s0 + j] - e[i][q.s0];
-                memcpy(h + 8ull * j, &v, 8);
+        } else {
+            for (int i = 0; i < 2; i++) {
+                in[i].bytes = ib;
+                in[i].capacity = 8ull * Ts + len[i][k];
+                in[i].index = c->lix[l][i].p;
+                in[i].indexed = 0;
+                in[i].qprev_valid = 0;
+                ib += a256(8ull * Ts + len[i][k] + 64);
             }
-            if (cudaMemcpyAsync(ib, h, 8ull * Ts, cudaMemcpyHostToDevice, c->st_in) != cudaSuccess ||
-                cudaMemcpyAsync(ib + 8ull * Ts, cmp[i] + 8ull * g.T + e[i][q.s0], len[i][k], cudaMemcpyHostToDevice,
-                                c->st_in) != cudaSuccess)
+            /* the next lane's last group leaves before the second walk is
+             * queued there; that walk's index is this lane's, free once the
+             * add of this lane's previous group is done */
+            if (st2 != st && pl.next + NL == k + 1 && (rc = pl.place(st2))) break;
+            if (cudaStreamWaitEvent(st, c->ev_in[k], 0) != cudaSuccess ||
+                cudaStreamWaitEvent(st2, c->ev_in[k], 0) != cudaSuccess ||
+                (k >= NL && cudaStreamWaitEvent(st2, c->ev_k[k - NL], 0) != cudaSuccess) ||
+                ws_clear(ws, q.g, st) != cudaSuccess || ws_clear(ws2, q.g, st2) != cudaSuccess) {
                 rc = ZCCL_GPU_ECUDA;
-            in[i].bytes = ib;
-            in[i].capacity = 8ull * Ts + len[i][k];
-            in[i].index = c->lix[l][i].p;
-            in[i].indexed = 0;
-            in[i].qprev_valid = 0;
-            ib += a256(8ull * Ts + len[i][k] + 64);
+                break;
+            }
+            /* a failed walk of the second input is reported by its lane's
+             * status words; the add never trusts an index for its bounds */
+            if ((rc = walk_stream(&in[0], q.g, ws, st)) || (rc = walk_stream(&in[1], q.g, ws2, st2))) break;
+            if (cudaEventRecord(c->ev_w[k], st2) != cudaSuccess ||
+                cudaStreamWaitEvent(st, c->ev_w[k], 0) != cudaSuccess) {
+                rc = ZCCL_GPU_ECUDA;
+                break;
+            }
+            if ((rc = zccl_gpu_homadd_cases(&sum, in, 2, (size_t)q.n, (int)g.L, (int)Ts, ws, nullptr, st))) break;
         }
-        /* the second input's index is the lane pair's: its walk for this
-         * group waits until the add of the pair's previous group is done */
-        if (rc || cudaEventRecord(c->ev_in[k], c->st_in) != cudaSuccess ||
-            cudaStreamWaitEvent(st, c->ev_in[k], 0) != cudaSuccess ||
-            cudaStreamWaitEvent(st2, c->ev_in[k], 0) != cudaSuccess ||
-            (k >= NL && cudaStreamWaitEvent(st2, c->ev_k[k - NL], 0) != cudaSuccess)) {
-            rc = rc ? rc : ZCCL_GPU_ECUDA;
-            break;
-        }
-        dev[k] = (uint8_t *)c->s[2].p + soff[k];
-        sum.bytes = dev[k];
-        sum.capacity = cap[k];
-        sum.index = c->lix[l][2].p;
-        sum.indexed = 0;
-        sum.qprev_valid = 0;
-        if (ws_clear(ws, q.g, st) != cudaSuccess || ws_clear(ws2, q.g, st2) != cudaSuccess) {
-            rc = ZCCL_GPU_ECUDA;
-            break;
-        }
-        /* a failed walk of the second input is reported by its lane's
-         * status words; the add never trusts an index for its bounds */
-        if ((rc = walk_stream(&in[0], q.g, ws, st)) || (rc = walk_stream(&in[1], q.g, ws2, st2)))
-            break;
-        if (cudaEventRecord(c->ev_w[k], st2) != cudaSuccess || cudaStreamWaitEvent(st, c->ev_w[k], 0) != cudaSuccess) {
-            rc = ZCCL_GPU_ECUDA;
-            break;
-        }
-        if ((rc = zccl_gpu_homadd_cases(&sum, in, 2, (size_t)q.n, (int)g.L, (int)Ts, ws, nullptr, st)))
-            break;
         uint8_t *pk = pin + poff[k];
         if (cudaMemcpyAsync(pk, sum.index, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
             cudaMemcpyAsync(pk + 8, dev[k], 8ull * Ts, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
             cudaEventRecord(c->ev_k[k], st) != cudaSuccess)
             rc = ZCCL_GPU_ECUDA;
     }
-    /* the sum written over an input (the ring adds into its receive
-     * buffer): no byte goes out before every input byte is in */
-    const size_t out_span = (size_t)zg_stream_worst(&g);
-    const size_t in_span0 = 8ull * g.T + (size_t)(e[0][gr[G - 1].s0] + len[0][G - 1]);
-    const size_t in_span1 = 8ull * g.T + (size_t)(e[1][gr[G - 1].s0] + len[1][G - 1]);
-    if (!rc && (overlaps(out, out_span, cmp1, in_span0) || overlaps(out, out_span, cmp2, in_span1)) &&
-        (cudaEventRecord(c->ev, c->st_in) != cudaSuccess || cudaStreamWaitEvent(c->st_out, c->ev, 0) != cudaSuccess))
-        rc = ZCCL_GPU_ECUDA;
-    uint64_t placed = 0;
-    if (!rc) rc = pipe_place(c, gr, dev, cap, poff, out, g.T, &placed);
+    while (!rc && pl.next < G) rc = pl.place(c->lane[pl.next % NL]);
+    const uint64_t placed = pl.run;
     rc = pipe_finish(c, rc, NL, true);
     if (rc) return rc;
     *out_size += (size_t)(8ull * g.T + placed);

@@ -19,10 +19,10 @@
  *   W2  compose the tables: per group of G windows (parallel), then per
  *       segment across groups, giving each group its true entry offset and
  *       first block number.
- *   W3  per window, the path from its true entry, stitched across 32
- *       speculative sub-window walks run in parallel (see below), gives
- *       every block's width and every tile's offset, written by all lanes at
- *       once; each chunk must end where the next starts.
+ *   W3  per window, the path from its true entry, followed by one lane
+ *       along 32 speculative sub-window walks run in parallel (see below),
+ *       gives every block's width and every tile's offset, written by all
+ *       lanes at once; each chunk must end where the next starts.
  *   W4  the extra segment of the last chunk (N % T elements) and the total
  *       size.
  * Widths above 32, chunk ends that disagree with the header, and blocks past
@@ -33,7 +33,7 @@
 namespace {
 
 constexpr uint32_t WARPS_W1 = 8;
-constexpr uint32_t WARPS_W3 = 16; /* warps per group in W3: two windows each */
+constexpr uint32_t WARPS_W3 = 8; /* warps per group in W3: four windows each */
 
 __device__ __forceinline__ uint64_t load_u64(const uint8_t *p)
 {
@@ -49,6 +49,20 @@ __device__ __forceinline__ uint32_t full_size(uint32_t b, uint32_t L, uint32_t f
 {
     return b <= 32 ? zg_block_bytes_f(fmt, b, L) : 1u;
 }
+
+/* full_size on a walk's critical path: for 32-element fastmode1 blocks
+ * (header, four sign bytes, 4 b bytes of magnitudes; a zero-width block is
+ * its header alone) two operations instead of the general formula. */
+struct Sizer {
+    uint32_t L, fmt, fast;
+    __device__ __forceinline__ Sizer(uint32_t L_, uint32_t fmt_)
+        : L(L_), fmt(fmt_), fast(L_ == 32u && fmt_ == ZG_FASTMODE1) {}
+    __device__ __forceinline__ uint32_t operator()(uint32_t b) const
+    {
+        if (fast) return b - 1u < 32u ? 4u * b + 5u : 1u;
+        return full_size(b, L, fmt);
+    }
+};
 
 /* Segment of a window / group index: last s with base[s] <= i. */
 __device__ __forceinline__ uint32_t find_seg(const uint32_t *base, uint32_t T, uint32_t i)
@@ -135,97 +149,42 @@ __global__ void k_walk_setup(const WalkArgs a)
     }
 }
 
-/* ---- W3: the path of the headers through one window -------------------
+/* ---- the exits of every position of a sub-window ----------------------
  *
- * A window of WW = 32 x 128 bytes sits in shared memory.  Lane j walks the
- * headers speculatively from byte 128 j until it leaves its sub-window and
- * keeps the positions it visited (a 128-bit map) and where it left.  A walk
- * from a true block start is the true path, and two walks that meet at a
- * position go on together, so the true path is stitched across the
- * sub-windows by the warp: lane j takes the true path from where it enters
- * sub-window j -- lane j's walk from there if that position is on it, else
- * walked until it meets lane j's walk or leaves the sub-window (a few
- * blocks) -- and hands its exit to lane j + 1.  Every lane first assumes it
- * is entered where lane j - 1's speculative walk left (where the walks have
- * nearly always merged); rounds repeat until no entry changes, so the
- * result is exact.  Bytes that cannot be headers (above 32) count as 1-byte
- * blocks, so walks stay bounded. */
+ * A window of WW = 32 x 128 bytes sits in shared memory, copied into rows of
+ * SUB + 4 bytes so that lane j reads sub-window j with no bank conflict.
+ * Lane j makes one backward pass over its sub-window: for every position i,
+ * where a walk of the headers from i leaves the sub-window (and, for W1, how
+ * many blocks it passes), from the result at the position i steps to.  The
+ * results are kept at i * 33 + j, again free of bank conflicts.  A walk from
+ * any entry then takes one hop per sub-window.  Bytes that cannot be headers
+ * (above 32) count as 1-byte blocks, so walks stay bounded. */
 constexpr uint32_t SUB = WALK_WW / 32; /* bytes per sub-window */
 static_assert(SUB == 128, "a sub-window map is four 32-bit words");
+constexpr uint32_t W1_ROW = SUB + 4;  /* bytes per skewed row */
+constexpr uint32_t W1_RES = SUB * 33; /* results */
 
-struct WinPath {
-    uint32_t tm[32][4]; /* the true path's positions, per sub-window */
-    uint32_t pref[33];  /* true-path positions before sub-window j; [32] = all */
-    uint32_t exit;      /* where the true path leaves the window */
-};
-
-/* Bits i .. 127 of a 128-bit map. */
-__device__ __forceinline__ void map_from(const uint32_t (&m)[4], uint32_t i, uint32_t (&t)[4])
+/* All lanes: the window's bytes into the skewed rows (row k: sub-window k). */
+__device__ __forceinline__ void copy_rows(const uint8_t *bytes, uint8_t *rows)
 {
-#pragma unroll
-    for (uint32_t w = 0; w < 4; w++)
-        t[w] |= w < (i >> 5) ? 0u : w > (i >> 5) ? m[w] : m[w] & ~((1u << (i & 31u)) - 1u);
+    const uint32_t lane = threadIdx.x & 31u;
+#pragma unroll 4
+    for (uint32_t k = 0; k < 32; k++) { /* row k: lane copies bytes 4 lane .. 4 lane + 3 */
+        const uint8_t *src = bytes + SUB * k + 4u * lane;
+        const uint32_t v = (uint32_t)src[0] | (uint32_t)src[1] << 8 | (uint32_t)src[2] << 16 | (uint32_t)src[3] << 24;
+        *reinterpret_cast<uint32_t *>(rows + W1_ROW * k + 4u * lane) = v;
+    }
 }
 
-/* All lanes: lane j's speculative walk of sub-window j (visited map sp, exit sx). */
-__device__ __forceinline__ void spec_walks(const uint8_t *bytes, uint32_t L, uint32_t fmt, uint32_t (&sp)[4],
-                                           uint32_t &sx)
+/* Lane j's backward pass over its row: res[i * 33 + j] = (exit - SUB) << 8 |
+ * blocks passed. */
+template <class R>
+__device__ __forceinline__ void backward_pass(const uint8_t *row, R *res, const Sizer &size)
 {
-    const uint32_t lane = threadIdx.x & 31u, lo = lane * SUB;
-    uint32_t m0 = 0, m1 = 0, m2 = 0, m3 = 0, pos = lo;
-    while (pos < lo + SUB) {
-        const uint32_t i = pos - lo, bit = 1u << (i & 31u), w = i >> 5;
-        m0 |= w == 0 ? bit : 0u;
-        m1 |= w == 1 ? bit : 0u;
-        m2 |= w == 2 ? bit : 0u;
-        m3 |= w == 3 ? bit : 0u;
-        pos += full_size(bytes[pos], L, fmt);
-    }
-    sp[0] = m0;
-    sp[1] = m1;
-    sp[2] = m2;
-    sp[3] = m3;
-    sx = pos;
-}
-
-/* All lanes: the true path from window position `entry` into wp (maps,
- * prefix counts, exit), from the speculative walks sp / sx. */
-__device__ __forceinline__ void stitch(const uint8_t *bytes, uint32_t L, uint32_t fmt, uint32_t entry,
-                                       const uint32_t (&sp)[4], uint32_t sx, WinPath *wp)
-{
-    const uint32_t lane = threadIdx.x & 31u, lo = lane * SUB, hi = lo + SUB;
-    uint32_t in = __shfl_up_sync(0xffffffffu, sx, 1);
-    if (lane == 0) in = entry;
-    uint32_t t[4], ex = in;
-    for (uint32_t round = 0; round <= 32; round++) { /* lane r is final after round r */
-        t[0] = t[1] = t[2] = t[3] = 0;
-        uint32_t q = in; /* >= lo: where sub-window j - 1 was left */
-        while (q < hi) {
-            const uint32_t i = q - lo;
-            const uint32_t wi = i >> 5, mw = wi == 0 ? sp[0] : wi == 1 ? sp[1] : wi == 2 ? sp[2] : sp[3];
-            if ((mw >> (i & 31u)) & 1u) { /* joins lane j's walk: the rest of it */
-                map_from(sp, i, t);
-                q = sx;
-                break;
-            }
-#pragma unroll
-            for (uint32_t w = 0; w < 4; w++) t[w] |= w == (i >> 5) ? 1u << (i & 31u) : 0u;
-            q += full_size(bytes[q], L, fmt);
-        }
-        ex = q;
-        uint32_t nin = __shfl_up_sync(0xffffffffu, ex, 1);
-        if (lane == 0) nin = entry;
-        if (!__any_sync(0xffffffffu, nin != in)) break;
-        in = nin;
-    }
-    const uint32_t cnt = __popc(t[0]) + __popc(t[1]) + __popc(t[2]) + __popc(t[3]);
-    const uint32_t incl = warp_incl_scan(cnt);
-#pragma unroll
-    for (uint32_t w = 0; w < 4; w++) wp->tm[lane][w] = t[w];
-    wp->pref[lane] = incl - cnt;
-    if (lane == 31) {
-        wp->pref[32] = incl;
-        wp->exit = ex;
+    const uint32_t lane = threadIdx.x & 31u;
+    for (int i = (int)SUB - 1; i >= 0; i--) {
+        const uint32_t nxt = (uint32_t)i + size(row[i]);
+        res[i * 33 + lane] = (R)(nxt >= SUB ? (nxt - SUB) << 8 | 1u : (uint32_t)res[nxt * 33 + lane] + 1u);
     }
 }
 
@@ -261,18 +220,14 @@ __device__ __forceinline__ const uint8_t *load_window(const WalkArgs &a, uint64_
 }
 
 /* ---- W1 --------------------------------------------------------------
- * Per window, lane j makes one backward pass over sub-window j: for every
- * position p, where a walk from p leaves the sub-window and how many blocks
- * it passes on the way, from the result at the position p steps to.  A walk
- * from any entry then takes one hop per sub-window.  The bytes are copied
- * into rows of SUB + 4 and the results kept at i * 33 + j (position i of
- * sub-window j), so that lanes in step hit distinct shared-memory banks.
- * A result is (exit - end of the sub-window) << 8 | blocks passed (<= SUB),
- * 16 bits while blocks are shorter than 256 bytes (block sizes up to 48),
- * else 32.  Per warp: the results (the plain window copy lands there
- * first), then the skewed rows. */
-constexpr uint32_t W1_ROW = SUB + 4;  /* bytes per skewed row */
-constexpr uint32_t W1_RES = SUB * 33; /* results */
+ * Per window, the backward passes give every position's exit from its
+ * sub-window and the blocks passed.  The exits go out to the workspace
+ * (one byte per position, for W3), and the window's table is made: for
+ * every entry offset e < M, the exit offset into the next window and the
+ * blocks passed, a walk of one hop per sub-window.  A result is (exit - end
+ * of the sub-window) << 8 | blocks passed (<= SUB), 16 bits while blocks are
+ * shorter than 256 bytes (block sizes up to 48), else 32.  Per warp: the
+ * results (the plain window copy lands there first), then the skewed rows. */
 
 __host__ __device__ inline uint32_t w1_warp_bytes(uint32_t M)
 {
@@ -284,13 +239,11 @@ template <class R>
 __global__ void __launch_bounds__(32 * WARPS_W1) k_walk_tables(const WalkArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
-    __shared__ uint32_t szt[33]; /* full_size of each header byte */
     const ZGeom &g = a.g;
     const WalkScratch &w = a.ws;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t M = a.M;
-    if (threadIdx.x < 33) szt[threadIdx.x] = full_size(threadIdx.x, g.L, g.fmt);
-    __syncthreads();
+    const Sizer size(g.L, g.fmt);
     /* persistent: the warps stride over the windows the header gives */
     for (uint32_t wg = blockIdx.x * WARPS_W1 + warp; wg < w.win_base[g.T]; wg += gridDim.x * WARPS_W1) {
         const uint32_t s = find_seg(w.win_base, g.T, wg);
@@ -301,20 +254,23 @@ __global__ void __launch_bounds__(32 * WARPS_W1) k_walk_tables(const WalkArgs a)
         uint8_t *rows = area + (a.w1_warp_bytes - 32u * W1_ROW);
         const uint8_t *bytes = load_window(a, start, area);
         __syncwarp();
+        copy_rows(bytes, rows);
+        __syncwarp();
+        backward_pass(rows + W1_ROW * lane, res, size);
+        __syncwarp();
+        /* the exits, element p = 128 j + i of the window's row of WW (bytes
+         * while blocks are shorter than 256 bytes, else 16 bits), as whole
+         * words: lane l writes words l, l + 32, ... */
+        constexpr uint32_t EB = sizeof(R) / 2; /* bytes per exit */
+        uint32_t *ex = reinterpret_cast<uint32_t *>(a.ws.wexit + (uint64_t)wg * WALK_WW * EB);
 #pragma unroll 4
-        for (uint32_t k = 0; k < 32; k++) { /* row k: lane copies bytes 4 lane .. 4 lane + 3 */
-            const uint8_t *src = bytes + SUB * k + 4u * lane;
-            const uint32_t v = (uint32_t)src[0] | (uint32_t)src[1] << 8 | (uint32_t)src[2] << 16 | (uint32_t)src[3] << 24;
-            *reinterpret_cast<uint32_t *>(rows + W1_ROW * k + 4u * lane) = v;
+        for (uint32_t q = lane; q < WALK_WW * EB / 4u; q += 32) {
+            const uint32_t p0 = q * (4u / EB), j = p0 / SUB, i = p0 % SUB;
+            uint32_t v = 0;
+#pragma unroll
+            for (uint32_t t = 0; t < 4u / EB; t++) v |= ((uint32_t)res[(i + t) * 33 + j] >> 8) << (8 * EB * t);
+            ex[q] = v;
         }
-        __syncwarp();
-        /* result = (exit - end of the sub-window) << 8 | blocks passed (<= SUB) */
-        const uint8_t *row = rows + W1_ROW * lane;
-        for (int i = (int)SUB - 1; i >= 0; i--) {
-            const uint32_t b = row[i], nxt = (uint32_t)i + (b <= 32 ? szt[b] : 1u);
-            res[i * 33 + lane] = (R)(nxt >= SUB ? (nxt - SUB) << 8 | 1u : (uint32_t)res[nxt * 33 + lane] + 1u);
-        }
-        __syncwarp();
         uint32_t *tab = a.ws.wtab + (uint64_t)wg * M;
         for (uint32_t e = lane; e < M; e += 32) {
             uint32_t pos = e, cnt = 0;
@@ -391,12 +347,71 @@ __global__ void k_walk_segments(const WalkArgs a)
     }
 }
 
-/* ---- W3: the true walk of every window ------------------------------- */
-/* Shared bytes before W3's window areas: entries, block bases, tables;
- * then per warp the window and its WinPath. */
-__host__ __device__ inline uint32_t w3_warp_bytes(uint32_t M) { return (win_area(M) + (uint32_t)sizeof(WinPath) + 15u) & ~15u; }
+/* ---- W3: the true walk of every window -------------------------------
+ * Per window, from its true entry (chained through the group's window
+ * tables): lane 0 hops once per sub-window from the entry, on the exits W1
+ * left for every position, and notes where the true path enters each one;
+ * then every lane walks its sub-window from there, and all lanes write the
+ * widths and tile offsets of their blocks at once.  Shared bytes before the
+ * warps' areas: entries, block bases, the group's tables; per warp: the
+ * window, its exits, the path. */
+constexpr uint32_t NOT_ENTERED = 0xFFFFFFFFu;
+
+struct WinPath {
+    uint32_t tm[32][4]; /* the true path's positions, per sub-window */
+    uint32_t ent[32];   /* where the true path enters sub-window j, or NOT_ENTERED */
+    uint32_t pref[33];  /* true-path positions before sub-window j; [32] = all */
+};
+
+__host__ __device__ inline uint32_t w3_exit_bytes(uint32_t M) { return WALK_WW * (M < 256 ? 1u : 2u); }
+__host__ __device__ inline uint32_t w3_warp_bytes(uint32_t M)
+{
+    return (win_area(M) + w3_exit_bytes(M) + (uint32_t)sizeof(WinPath) + 15u) & ~15u;
+}
 __host__ __device__ inline uint32_t w3_head(uint32_t M) { return (12u * WALK_G + 4u * WALK_G * M + 15u) & ~15u; }
 
+/* All lanes: the window's exits (W1's row of WW elements) into ex, by
+ * aligned 16-byte loads. */
+__device__ __forceinline__ void load_exits(const uint8_t *src, uint8_t *ex, uint32_t bytes)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+#pragma unroll 4
+    for (uint32_t i = lane; i < bytes / 16u; i += 32)
+        reinterpret_cast<uint4 *>(ex)[i] = reinterpret_cast<const uint4 *>(src)[i];
+}
+
+/* All lanes: the true path of the window from `entry` into wp (maps, prefix
+ * counts), from the window's bytes and exits. */
+template <class E>
+__device__ __forceinline__ void true_path(const uint8_t *bytes, const E *ex, uint32_t entry, const Sizer &size,
+                                          WinPath *wp)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    wp->ent[lane] = NOT_ENTERED;
+    __syncwarp();
+    if (lane == 0) { /* one hop per sub-window (a long block may step over one) */
+        uint32_t pos = entry;
+        while (pos < WALK_WW) {
+            const uint32_t j = pos / SUB;
+            wp->ent[j] = pos % SUB;
+            pos = (j + 1) * SUB + (uint32_t)ex[pos];
+        }
+    }
+    __syncwarp();
+    uint32_t t[4] = {0, 0, 0, 0};
+    const uint8_t *sub = bytes + lane * SUB;
+    for (uint32_t q = wp->ent[lane]; q < SUB; q += size(sub[q])) /* NOT_ENTERED: no step */
+#pragma unroll
+        for (uint32_t w = 0; w < 4; w++) t[w] |= w == (q >> 5) ? 1u << (q & 31u) : 0u;
+#pragma unroll
+    for (uint32_t w = 0; w < 4; w++) wp->tm[lane][w] = t[w];
+    const uint32_t cnt = __popc(t[0]) + __popc(t[1]) + __popc(t[2]) + __popc(t[3]);
+    const uint32_t incl = warp_incl_scan(cnt);
+    wp->pref[lane] = incl - cnt;
+    if (lane == 31) wp->pref[32] = incl;
+}
+
+template <class E>
 __global__ void __launch_bounds__(32 * WARPS_W3) k_walk_final(const WalkArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
@@ -407,7 +422,8 @@ __global__ void __launch_bounds__(32 * WARPS_W3) k_walk_final(const WalkArgs a)
     uint64_t *bbase = reinterpret_cast<uint64_t *>(smem + 4 * WALK_G);
     uint32_t *tabs = reinterpret_cast<uint32_t *>(smem + 12 * WALK_G); /* the group's window tables */
     uint8_t *wbuf = smem + w3_head(a.M);
-    const uint32_t wstride = w3_warp_bytes(a.M);
+    const uint32_t wstride = w3_warp_bytes(a.M), xb = w3_exit_bytes(a.M);
+    const Sizer size(g.L, g.fmt);
     /* persistent: the CTAs stride over the groups the header gives */
     for (uint32_t gg = blockIdx.x; gg < w.grp_base[g.T]; gg += gridDim.x) {
         const uint32_t s = find_seg(w.grp_base, g.T, gg);
@@ -444,12 +460,12 @@ __global__ void __launch_bounds__(32 * WARPS_W3) k_walk_final(const WalkArgs a)
             if (b0 >= nb) continue;
             const uint64_t start = w.seg_P[s] + (uint64_t)k * WALK_WW;
             uint8_t *area = wbuf + warp * wstride;
-            WinPath *wp = reinterpret_cast<WinPath *>(area + win_area(a.M));
-            const uint8_t *buf = load_window(a, start, area);
+            E *ex = reinterpret_cast<E *>(area + win_area(a.M));
+            WinPath *wp = reinterpret_cast<WinPath *>(area + win_area(a.M) + xb);
+            load_exits(w.wexit + (uint64_t)(w.win_base[s] + k) * xb, reinterpret_cast<uint8_t *>(ex), xb);
+            const uint8_t *bytes = load_window(a, start, area);
             __syncwarp();
-            uint32_t sp[4], sx;
-            spec_walks(buf, g.L, g.fmt, sp, sx);
-            stitch(buf, g.L, g.fmt, entry[k - w0], sp, sx, wp);
+            true_path(bytes, ex, entry[k - w0], size, wp);
             __syncwarp();
             /* lane j records the true-path blocks of its sub-window; the
              * next tile boundary at or after its first block is found once */
@@ -472,7 +488,7 @@ __global__ void __launch_bounds__(32 * WARPS_W3) k_walk_final(const WalkArgs a)
                         m = 0;
                         break;
                     }
-                    const uint32_t b = buf[pos];
+                    const uint32_t b = bytes[pos];
                     if (b > 32) {
                         atomicOr(a.err, ZERR_CORRUPT);
                         m = 0;
@@ -591,9 +607,13 @@ cudaError_t launch_walk(const WalkArgs &a0, cudaStream_t st)
     uint32_t warps3 = WARPS_W3;
     while (warps3 > 1 && w3_head(a.M) + warps3 * wstride > (uint32_t)smax) warps3--;
     const uint32_t smem3 = w3_head(a.M) + warps3 * wstride;
-    if ((e = set_max_smem((const void *)k_walk_final, smem3)) != cudaSuccess)
-        return e;
-    k_walk_final<<<walk_grid((const void *)k_walk_final, 32 * warps3, smem3, a.max_groups), 32 * warps3, smem3, st>>>(a);
+    const void *f3 = a.M < 256 ? (const void *)k_walk_final<uint8_t> : (const void *)k_walk_final<uint16_t>;
+    if ((e = set_max_smem(f3, smem3)) != cudaSuccess) return e;
+    const unsigned grid3 = walk_grid(f3, 32 * warps3, smem3, a.max_groups);
+    if (a.M < 256)
+        k_walk_final<uint8_t><<<grid3, 32 * warps3, smem3, st>>>(a);
+    else
+        k_walk_final<uint16_t><<<grid3, 32 * warps3, smem3, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     k_walk_finish<<<1, 32, 0, st>>>(a);
     return cudaGetLastError();

@@ -175,6 +175,7 @@ struct WalkScratch {
     uint64_t *gtab;     /* [max_groups * M]  blocks << 32 | exit offset, per group */
     uint32_t *gentry;   /* [max_groups] true entry offset of each group */
     uint64_t *gbase;    /* [max_groups] first block (in its segment) of each group */
+    uint8_t *wexit;     /* [max_windows * WW] per position: exit - end of its sub-window */
 };
 
 struct WalkArgs {
