@@ -45,12 +45,10 @@ struct TileIdx {
     uint32_t q0;
 };
 
-__device__ __forceinline__ TileIdx load_idx(const DecompressArgs &a, uint64_t t)
+__device__ __forceinline__ TileIdx load_idx(const DecompressArgs &a, uint64_t t, const ZTile &z)
 {
     TileIdx r = {0, 0, 0};
     if (t >= a.g.ntiles) return r;
-    ZTile z;
-    zg_tile(&a.g, t, &z);
     if (threadIdx.x < z.nblk) r.b = a.idx.widths[z.gblk0 + threadIdx.x];
     if (threadIdx.x == 0) {
         r.base = a.idx.tile_off[t];
@@ -78,17 +76,15 @@ __device__ __forceinline__ void issue_tile(const DecompressArgs &a, const TileId
     tma_load_superset(buf, a.in + base, nload, bar);
 }
 
-/* All threads: sizes of tile t's blocks, their offsets, and (thread 0) the
- * TMA copy of the tile's bytes into buf.  Returns the slot of this thread's
- * block; the tile's byte offset lands in *s_base, its starting value in
- * *s_q0. */
-__device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, uint64_t t, const TileIdx &ix,
+/* All threads: sizes of tile t's blocks (geometry z), their offsets, and
+ * (thread 0) the TMA copy of the tile's bytes into buf.  Returns the slot of
+ * this thread's block; the tile's byte offset lands in *s_base, its starting
+ * value in *s_q0. */
+__device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, const ZTile &z, const TileIdx &ix,
                                                 uint8_t *buf, uint64_t *bar, uint32_t *wsum,
                                                 uint64_t *s_base, uint32_t *s_q0, uint32_t &bad)
 {
     BlockSlot sl = {0, 0, 0};
-    ZTile z;
-    zg_tile(&a.g, t, &z);
     uint32_t size = 0;
     if (threadIdx.x < z.nblk) {
         sl.n = zg_block_len(z.seg_len, a.g.L, z.blk0 + threadIdx.x);
@@ -119,6 +115,12 @@ __global__ void __launch_bounds__(256, 3) k_decompress(const DecompressArgs a, c
     uint32_t *ws1 = reinterpret_cast<uint32_t *>(smem + 320); /* [33] second scan scratch */
     uint32_t *ws2 = reinterpret_cast<uint32_t *>(smem + 464); /* [33] the same pair, odd rounds */
     uint32_t *ws3 = reinterpret_cast<uint32_t *>(smem + 608); /* [33] */
+    /* [4] geometry of the tiles in flight, each found once by thread 0 before
+     * a scan's barrier: the tile's (it % 4), the next one's, the one after
+     * (for its index entries); a slot is rewritten two rounds after its
+     * tile's, when every thread is past that tile */
+    ZTile *zs = reinterpret_cast<ZTile *>(smem + 752);
+    static_assert(752 + 4 * sizeof(ZTile) <= 1024, "the tile records fit below the rows");
     float *rows = reinterpret_cast<float *>(smem + a.sm.rows);
 
     const ZGeom &g = a.g;
@@ -140,17 +142,19 @@ __global__ void __launch_bounds__(256, 3) k_decompress(const DecompressArgs a, c
      * CTA waits on another. */
     if (*(volatile const uint32_t *)a.w.walk_err) return;
 
+    uint64_t tile = blockIdx.x;
+    uint64_t tnext = tile + gridDim.x; /* the static order's next tile */
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
+        if (tile < g.ntiles) zg_tile(&g, tile, &zs[0]);
+        if (tnext < g.ntiles) zg_tile(&g, tnext, &zs[1]);
     }
     __syncthreads();
-    uint64_t tile = blockIdx.x;
-    uint64_t tnext = tile + gridDim.x; /* the static order's next tile */
-    TileIdx ix = load_idx(a, tile);
+    TileIdx ix = load_idx(a, tile, zs[0]);
     BlockSlot cur = {0, 0, 0};
-    if (tile < g.ntiles) cur = stage_tile(a, tile, ix, smem + a.sm.in0, &bar[0], wsum, &s_base[0], &s_q0[0], bad);
-    ix = load_idx(a, tnext);
+    if (tile < g.ntiles) cur = stage_tile(a, zs[0], ix, smem + a.sm.in0, &bar[0], wsum, &s_base[0], &s_q0[0], bad);
+    ix = load_idx(a, tnext, zs[1]);
 
     /* One barrier a tile, the scan's (one more before the rows leave when a
      * tile has short or long blocks).  The input buffer the next copy
@@ -162,8 +166,7 @@ __global__ void __launch_bounds__(256, 3) k_decompress(const DecompressArgs a, c
     for (uint32_t it = 0;; it++) {
         const uint32_t cb = it & 1u;
         if (tile >= g.ntiles) break;
-        ZTile z;
-        zg_tile(&g, tile, &z);
+        const ZTile &z = zs[it & 3u];
 
         BlockSlot nxt = {0, 0, 0}; /* the next tile's block, found in step 3 */
         uint32_t next_bytes = 0;  /* the next tile's bytes */
@@ -201,10 +204,10 @@ __global__ void __launch_bounds__(256, 3) k_decompress(const DecompressArgs a, c
          *    ago), and its copy starts right after, into the other buffer. */
         uint32_t tsum, pre;
         {
-            ZTile zn;
+            const ZTile &zn = zs[(it + 1u) & 3u];
             uint32_t sizen = 0;
+            if (tid == 0 && tnext + gridDim.x < g.ntiles) zg_tile(&g, tnext + gridDim.x, &zs[(it + 2u) & 3u]);
             if (tnext < g.ntiles) {
-                zg_tile(&g, tnext, &zn);
                 if (tid < zn.nblk) {
                     nxt.n = zg_block_len(zn.seg_len, L, zn.blk0 + tid);
                     nxt.b = ix.b;
@@ -227,7 +230,7 @@ __global__ void __launch_bounds__(256, 3) k_decompress(const DecompressArgs a, c
                 issue_tile(a, ix, next_bytes, smem + (cb ? a.sm.in0 : a.sm.in1), &bar[cb ^ 1u], &s_base[cb ^ 1u],
                            &s_q0[cb ^ 1u], bad);
             ixn = ix;
-            ix = load_idx(a, tnext + gridDim.x);
+            ix = load_idx(a, tnext + gridDim.x, zs[(it + 2u) & 3u]);
         }
         if (SUMS) { /* the tile's delta sum; the values wait for the scan */
             if (tid == 0) a.idx.tile_qprev[tile] = (int32_t)tsum;
