@@ -311,7 +311,7 @@ __device__ __forceinline__ void encode_mid(uint32_t sbase, uint32_t o, uint32_t 
 __device__ __forceinline__ void encode_block32(uint32_t sbase, uint32_t o, uint32_t b, uint32_t smask,
                                                const uint32_t (&m)[32])
 {
-    if (b && b < 16)
+    if (__builtin_expect(b - 1u < 15u, 1))
         encode_small(sbase, o, b, smask, m);
     else if (b >= 16 && b < 24)
         encode_mid(sbase, o, b, smask, m);
@@ -535,14 +535,14 @@ __device__ __forceinline__ uint32_t decode_block32(const uint32_t *w, uint32_t o
 __device__ __forceinline__ void decode_add_full(const uint32_t *w, uint32_t o, uint32_t b, uint32_t (&acc)[32])
 {
     if (b == 0) return;
-    if (b >= 16 && b < 24) {
-        decode_mid<true>(w, o, b, acc);
-        return;
-    }
     const uint32_t B = b >> 3, r = b & 7u;
     uint32_t sg, unused;
-    be64_at(w, o + 1, sg, unused);
-    if (b >= 16) {
+    if (__builtin_expect(b >= 16, 0)) { /* rare at the bounds the collectives use: out of the hot path */
+        if (b < 24) {
+            decode_mid<true>(w, o, b, acc);
+            return;
+        }
+        be64_at(w, o + 1, sg, unused);
         const uint32_t hb = o + 5, lb = hb + 32u * B;
         const uint32_t bmask = B >= 4 ? 0xFFFFFFFFu : (1u << (8u * B)) - 1u;
 #pragma unroll
@@ -562,6 +562,7 @@ __device__ __forceinline__ void decode_add_full(const uint32_t *w, uint32_t o, u
         }
         return;
     }
+    be64_at(w, o + 1, sg, unused);
     const uint32_t hb = o + 5, lb = hb + 32u * B;
     const uint32_t k0 = hb >> 2, sh = (hb & 3u) * 8u;
     const uint32_t zsel = B ? 0u : 4u;
