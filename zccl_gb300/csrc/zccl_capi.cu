@@ -103,7 +103,7 @@ ZIndex bind_index(void *mem, const ZGeom &g)
  * header-walk scratch.  Only the first part is cleared per call. */
 struct WalkLayout {
     uint32_t M, max_windows, max_groups;
-    size_t seg_P, seg_R, seg_end, seg_ok, win_base, grp_base, wtab, gtab, gentry, gbase, wexit, total;
+    size_t seg_P, seg_R, seg_end, seg_ok, win_base, grp_base, wtab, gtab, gentry, gbase, wexit, gwin, total;
 };
 
 size_t ws_clear_bytes(const ZGeom &g) { return 16 + 8 * g.ntiles; }
@@ -135,6 +135,7 @@ WalkLayout walk_layout(const ZGeom &g)
     l.gentry = o; o = align16(o + 4ull * l.max_groups);
     l.gbase = o; o = align16(o + 8ull * l.max_groups);
     l.wexit = o; o = align16(o + (size_t)WALK_WW * l.max_windows * (l.M < 256 ? 1u : 2u));
+    l.gwin = o; o = align16(o + 4ull * l.max_groups * l.M * WALK_G);
     l.total = o + 16;
     return l;
 }
@@ -201,6 +202,7 @@ int walk_stream(zccl_gpu_stream *s, const ZGeom &g, void *ws, cudaStream_t st)
     a.ws.gentry = (uint32_t *)(p + l.gentry);
     a.ws.gbase = (uint64_t *)(p + l.gbase);
     a.ws.wexit = p + l.wexit;
+    a.ws.gwin = (uint32_t *)(p + l.gwin);
     a.max_windows = l.max_windows;
     a.max_groups = l.max_groups;
     int rc = cuda_status(launch_walk(a, st));
@@ -893,6 +895,7 @@ struct DropCtx {
     DevBuf fin, fout, s[3], ix[3], ws;
     DevBuf aux; /* counters read back by the _record entry points */
     PinBuf pin;
+    PinBuf stat; /* the lanes' workspace status words, read back together */
 };
 
 DropCtx *drop_ctx()
@@ -1127,21 +1130,38 @@ size_t max_index_bytes(const std::vector<Group> &gr)
 }
 
 /* Waits for every copy and kernel of a pipelined call, then reads (and
- * clears) the workspace's status words. */
+ * clears) the lanes' workspace status words, as zccl_gpu_check() does, with
+ * one wait for all of them. */
 int pipe_finish(DropCtx *c, int rc, uint32_t lanes, bool walk_lanes = false)
 {
     bool sync_ok = cudaStreamSynchronize(c->st_in) == cudaSuccess &&
                    cudaStreamSynchronize(c->st_out) == cudaSuccess;
     for (uint32_t l = 0; l < lanes; l++) /* after an early stop, work may remain on any lane */
         sync_ok = cudaStreamSynchronize(c->lane[l]) == cudaSuccess && sync_ok;
-    int rc2 = ZCCL_GPU_OK;
+    if (!sync_ok) return ZCCL_GPU_ECUDA;
+    if (int e = c->stat.ensure(8 * kWalkLanes)) return rc ? rc : e;
+    uint32_t *bits = (uint32_t *)c->stat.p;
+    uint32_t idx[kWalkLanes], n = 0;
+    cudaStream_t st = c->lane[0];
     for (uint32_t l = 0; l < lanes; l++)
         for (uint32_t h = 0; h < (walk_lanes ? 2u : 1u); h++) {
             const uint32_t i = l + h * kLanes;
-            const int r = c->lws[i].p ? zccl_gpu_check(c->lws[i].p, c->lane[l]) : ZCCL_GPU_OK;
-            if (!rc2) rc2 = r;
+            if (!c->lws[i].p) continue;
+            if (cudaMemcpyAsync(bits + 2 * n, c->lws[i].p, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+                return ZCCL_GPU_ECUDA;
+            idx[n++] = i;
         }
-    if (!sync_ok) return ZCCL_GPU_ECUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+    int rc2 = ZCCL_GPU_OK;
+    bool cleared = false;
+    for (uint32_t j = 0; j < n; j++) {
+        if (!(bits[2 * j] | bits[2 * j + 1])) continue;
+        /* a failed walk leaves nothing for the codec kernels to report */
+        if (!rc2) rc2 = status_of_bits(bits[2 * j + 1] ? bits[2 * j + 1] : bits[2 * j]);
+        if (cudaMemsetAsync(c->lws[idx[j]].p, 0, 8, st) != cudaSuccess) return ZCCL_GPU_ECUDA;
+        cleared = true;
+    }
+    if (cleared && cudaStreamSynchronize(st) != cudaSuccess) return ZCCL_GPU_ECUDA;
     return rc ? rc : rc2;
 }
 

@@ -33,7 +33,7 @@
 namespace {
 
 constexpr uint32_t WARPS_W1 = 8;
-constexpr uint32_t WARPS_W3 = 8; /* warps per group in W3: four windows each */
+constexpr uint32_t WARPS_W3 = 8; /* warps per CTA in W3, a window each at a time */
 
 __device__ __forceinline__ uint64_t load_u64(const uint8_t *p)
 {
@@ -285,7 +285,11 @@ __global__ void __launch_bounds__(32 * WARPS_W1) k_walk_tables(const WalkArgs a)
     }
 }
 
-/* ---- W2a: compose the window tables of each group ---------------------- */
+/* ---- W2a: compose the window tables of each group ----------------------
+ * For every entry offset into the group, the walk through its windows'
+ * tables; each step's entry offset and the blocks passed before it are kept
+ * (gwin), so that once the group's true entry is known every window's is a
+ * single load. */
 __global__ void k_walk_groups(const WalkArgs a)
 {
     const ZGeom &g = a.g;
@@ -299,7 +303,9 @@ __global__ void k_walk_groups(const WalkArgs a)
     for (uint32_t e = threadIdx.x; e < a.M; e += blockDim.x) {
         uint32_t x = e;
         uint64_t c = 0;
+        uint32_t *gw = w.gwin + ((uint64_t)gg * a.M + e) * WALK_G;
         for (uint32_t k = w0; k < w1; k++) {
+            gw[k - w0] = (uint32_t)c << 12 | x; /* c < 32 windows x 4096 blocks; x < M < 4096 */
             uint32_t t = __ldg(w.wtab + (uint64_t)(w.win_base[s] + k) * a.M + x);
             c += t & 0xFFFFu;
             x = t >> 16;
@@ -348,13 +354,12 @@ __global__ void k_walk_segments(const WalkArgs a)
 }
 
 /* ---- W3: the true walk of every window -------------------------------
- * Per window, from its true entry (chained through the group's window
- * tables): lane 0 hops once per sub-window from the entry, on the exits W1
- * left for every position, and notes where the true path enters each one;
- * then every lane walks its sub-window from there, and all lanes write the
- * widths and tile offsets of their blocks at once.  Shared bytes before the
- * warps' areas: entries, block bases, the group's tables; per warp: the
- * window, its exits, the path. */
+ * One warp per window: its true entry and first block are one load (gwin at
+ * its group's true entry); lane 0 hops once per sub-window from the entry,
+ * on the exits W1 left for every position, and notes where the true path
+ * enters each one; then every lane walks its sub-window from there, and all
+ * lanes write the widths and tile offsets of their blocks at once.  Shared
+ * bytes per warp: the window, its exits, the path. */
 constexpr uint32_t NOT_ENTERED = 0xFFFFFFFFu;
 
 struct WinPath {
@@ -368,7 +373,6 @@ __host__ __device__ inline uint32_t w3_warp_bytes(uint32_t M)
 {
     return (win_area(M) + w3_exit_bytes(M) + (uint32_t)sizeof(WinPath) + 15u) & ~15u;
 }
-__host__ __device__ inline uint32_t w3_head(uint32_t M) { return (12u * WALK_G + 4u * WALK_G * M + 15u) & ~15u; }
 
 /* All lanes: the window's exits (W1's row of WW elements) into ex, by
  * aligned 16-byte loads. */
@@ -412,107 +416,80 @@ __device__ __forceinline__ void true_path(const uint8_t *bytes, const E *ex, uin
 }
 
 template <class E>
-__global__ void __launch_bounds__(32 * WARPS_W3) k_walk_final(const WalkArgs a)
+__global__ void __launch_bounds__(32 * WARPS_W3, 3) k_walk_final(const WalkArgs a)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     const ZGeom &g = a.g;
     const WalkScratch &w = a.ws;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    uint32_t *entry = reinterpret_cast<uint32_t *>(smem);
-    uint64_t *bbase = reinterpret_cast<uint64_t *>(smem + 4 * WALK_G);
-    uint32_t *tabs = reinterpret_cast<uint32_t *>(smem + 12 * WALK_G); /* the group's window tables */
-    uint8_t *wbuf = smem + w3_head(a.M);
-    const uint32_t wstride = w3_warp_bytes(a.M), xb = w3_exit_bytes(a.M);
+    const uint32_t xb = w3_exit_bytes(a.M);
     const Sizer size(g.L, g.fmt);
-    /* persistent: the CTAs stride over the groups the header gives */
-    for (uint32_t gg = blockIdx.x; gg < w.grp_base[g.T]; gg += gridDim.x) {
-        const uint32_t s = find_seg(w.grp_base, g.T, gg);
-        if (!w.seg_ok[s]) continue; /* uniform over the CTA */
-        const uint32_t nwin = w.win_base[s + 1] - w.win_base[s];
-        const uint32_t w0 = (gg - w.grp_base[s]) * WALK_G;
-        const uint32_t w1 = min(w0 + WALK_G, nwin);
-
-        const uint64_t nb = g.nb_reg;
-        const uint64_t nfull = (g.tbs - 1) / g.L;
-        const uint32_t ntail = (uint32_t)((g.tbs - 1) % g.L);
+    const uint64_t nb = g.nb_reg;
+    const uint64_t nfull = (g.tbs - 1) / g.L;
+    const uint32_t ntail = (uint32_t)((g.tbs - 1) % g.L);
+    uint8_t *area = smem + warp * w3_warp_bytes(a.M);
+    E *ex = reinterpret_cast<E *>(area + win_area(a.M));
+    WinPath *wp = reinterpret_cast<WinPath *>(area + win_area(a.M) + xb);
+    /* persistent: the warps stride over the windows the header gives */
+    for (uint32_t wi = blockIdx.x * nw + warp; wi < w.win_base[g.T]; wi += gridDim.x * nw) {
+        const uint32_t s = find_seg(w.win_base, g.T, wi);
+        if (!w.seg_ok[s]) continue; /* uniform over the warp */
+        const uint32_t k = wi - w.win_base[s]; /* the window within its segment */
+        const uint32_t gg = w.grp_base[s] + k / WALK_G;
+        const uint32_t v = w.gwin[((uint64_t)gg * a.M + w.gentry[gg]) * WALK_G + k % WALK_G];
+        const uint64_t b0 = w.gbase[gg] + (v >> 12);
+        if (b0 >= nb) continue;
         const uint64_t gblk0 = (uint64_t)s * g.nb_reg, tile0 = (uint64_t)s * g.nt_reg;
-
-        /* the chain through the group's windows runs on tables staged in shared
-         * memory by the whole CTA (one coalesced copy) */
-        const uint32_t *gt = w.wtab + (uint64_t)(w.win_base[s] + w0) * a.M;
-        for (uint32_t i = threadIdx.x; i < (w1 - w0) * a.M; i += blockDim.x) tabs[i] = gt[i];
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t x = w.gentry[gg];
-            uint64_t b = w.gbase[gg];
-            for (uint32_t k = w0; k < w1; k++) {
-                entry[k - w0] = x;
-                bbase[k - w0] = b;
-                if (b >= nb) continue;
-                uint32_t t = tabs[(k - w0) * a.M + x];
-                b += t & 0xFFFFu;
-                x = t >> 16;
-            }
+        const uint64_t start = w.seg_P[s] + (uint64_t)k * WALK_WW;
+        load_exits(w.wexit + (uint64_t)wi * xb, reinterpret_cast<uint8_t *>(ex), xb);
+        const uint8_t *bytes = load_window(a, start, area);
+        __syncwarp();
+        true_path(bytes, ex, v & 0xFFFu, size, wp);
+        __syncwarp();
+        /* lane j records the true-path blocks of its sub-window; the
+         * next tile boundary at or after its first block is found once */
+        uint64_t blk = b0 + wp->pref[lane];
+        const uint64_t tq = blk / g.TB;
+        uint64_t tnext = tq * g.TB, tidx = tq;
+        if (tnext < blk) {
+            tnext += g.TB;
+            tidx++;
         }
-        __syncthreads();
-        for (uint32_t k = w0 + warp; k < w1; k += nw) {
-            const uint64_t b0 = bbase[k - w0];
-            if (b0 >= nb) continue;
-            const uint64_t start = w.seg_P[s] + (uint64_t)k * WALK_WW;
-            uint8_t *area = wbuf + warp * wstride;
-            E *ex = reinterpret_cast<E *>(area + win_area(a.M));
-            WinPath *wp = reinterpret_cast<WinPath *>(area + win_area(a.M) + xb);
-            load_exits(w.wexit + (uint64_t)(w.win_base[s] + k) * xb, reinterpret_cast<uint8_t *>(ex), xb);
-            const uint8_t *bytes = load_window(a, start, area);
-            __syncwarp();
-            true_path(bytes, ex, entry[k - w0], size, wp);
-            __syncwarp();
-            /* lane j records the true-path blocks of its sub-window; the
-             * next tile boundary at or after its first block is found once */
-            uint64_t blk = b0 + wp->pref[lane];
-            const uint64_t tq = blk / g.TB;
-            uint64_t tnext = tq * g.TB, tidx = tq;
-            if (tnext < blk) {
-                tnext += g.TB;
-                tidx++;
-            }
 #pragma unroll
-            for (uint32_t wd = 0; wd < 4; wd++) {
-                uint32_t m = wp->tm[lane][wd];
-                while (m && blk < nb) {
-                    const uint32_t pos = lane * SUB + wd * 32 + (uint32_t)(__ffs(m) - 1);
-                    m &= m - 1;
-                    const uint64_t gpos = start + pos;
-                    if (gpos >= a.avail) {
-                        atomicOr(a.err, ZERR_BOUNDS);
-                        m = 0;
-                        break;
-                    }
-                    const uint32_t b = bytes[pos];
-                    if (b > 32) {
-                        atomicOr(a.err, ZERR_CORRUPT);
-                        m = 0;
-                        break;
-                    }
-                    if (blk == tnext) {
-                        if (blk) a.idx.tile_off[tile0 + tidx] = gpos;
-                        tnext += g.TB;
-                        tidx++;
-                    }
-                    a.idx.widths[gblk0 + blk] = (uint8_t)b;
-                    const uint32_t n = blk < nfull ? g.L : ntail;
-                    blk++;
-                    if (blk == nb) {
-                        const uint64_t end = gpos + zg_block_bytes_f(g.fmt, b, n);
-                        if (end > a.avail) atomicOr(a.err, ZERR_BOUNDS);
-                        w.seg_end[s] = end;
-                        if (s + 1 < g.T && end != w.seg_R[s]) atomicOr(a.err, ZERR_CORRUPT);
-                    }
+        for (uint32_t wd = 0; wd < 4; wd++) {
+            uint32_t m = wp->tm[lane][wd];
+            while (m && blk < nb) {
+                const uint32_t pos = lane * SUB + wd * 32 + (uint32_t)(__ffs(m) - 1);
+                m &= m - 1;
+                const uint64_t gpos = start + pos;
+                if (gpos >= a.avail) {
+                    atomicOr(a.err, ZERR_BOUNDS);
+                    m = 0;
+                    break;
+                }
+                const uint32_t b = bytes[pos];
+                if (b > 32) {
+                    atomicOr(a.err, ZERR_CORRUPT);
+                    m = 0;
+                    break;
+                }
+                if (blk == tnext) {
+                    if (blk) a.idx.tile_off[tile0 + tidx] = gpos;
+                    tnext += g.TB;
+                    tidx++;
+                }
+                a.idx.widths[gblk0 + blk] = (uint8_t)b;
+                const uint32_t n = blk < nfull ? g.L : ntail;
+                blk++;
+                if (blk == nb) {
+                    const uint64_t end = gpos + zg_block_bytes_f(g.fmt, b, n);
+                    if (end > a.avail) atomicOr(a.err, ZERR_BOUNDS);
+                    w.seg_end[s] = end;
+                    if (s + 1 < g.T && end != w.seg_R[s]) atomicOr(a.err, ZERR_CORRUPT);
                 }
             }
-            __syncwarp();
         }
-        __syncthreads(); /* the group's shared state is reused */
+        __syncwarp();
     }
 }
 
@@ -588,7 +565,8 @@ cudaError_t launch_walk(const WalkArgs &a0, cudaStream_t st)
     else
         k_walk_tables<uint32_t><<<grid1, 32 * WARPS_W1, smem1, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    k_walk_groups<<<a.max_groups, 128, 0, st>>>(a);
+    const unsigned threads2 = std::min(1024u, (a.M + 31u) / 32u * 32u); /* one thread per entry offset */
+    k_walk_groups<<<a.max_groups, threads2, 0, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     a.seg_batch = (160u * 1024u) / (8u * a.M);
     if (a.seg_batch > WALK_G) a.seg_batch = WALK_G;
@@ -599,17 +577,17 @@ cudaError_t launch_walk(const WalkArgs &a0, cudaStream_t st)
     k_walk_segments<<<a.g.T, 256, smem2, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const uint32_t wstride = w3_warp_bytes(a.M);
-    /* as many warps as fit beside the staged tables (fewer for the largest blocks) */
+    /* as many warps as fit (fewer for the largest blocks) */
     int dev = 0, smax = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
         (e = cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess)
         return e;
     uint32_t warps3 = WARPS_W3;
-    while (warps3 > 1 && w3_head(a.M) + warps3 * wstride > (uint32_t)smax) warps3--;
-    const uint32_t smem3 = w3_head(a.M) + warps3 * wstride;
+    while (warps3 > 1 && warps3 * wstride > (uint32_t)smax) warps3--;
+    const uint32_t smem3 = warps3 * wstride;
     const void *f3 = a.M < 256 ? (const void *)k_walk_final<uint8_t> : (const void *)k_walk_final<uint16_t>;
     if ((e = set_max_smem(f3, smem3)) != cudaSuccess) return e;
-    const unsigned grid3 = walk_grid(f3, 32 * warps3, smem3, a.max_groups);
+    const unsigned grid3 = walk_grid(f3, 32 * warps3, smem3, (a.max_windows + warps3 - 1) / warps3);
     if (a.M < 256)
         k_walk_final<uint8_t><<<grid3, 32 * warps3, smem3, st>>>(a);
     else

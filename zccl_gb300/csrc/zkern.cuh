@@ -176,6 +176,8 @@ struct WalkScratch {
     uint32_t *gentry;   /* [max_groups] true entry offset of each group */
     uint64_t *gbase;    /* [max_groups] first block (in its segment) of each group */
     uint8_t *wexit;     /* [max_windows * WW] per position: exit - end of its sub-window */
+    uint32_t *gwin;     /* [max_groups * M * WALK_G] per group, entry offset and window k of it:
+                           blocks before k << 12 | entry offset of k */
 };
 
 struct WalkArgs {
