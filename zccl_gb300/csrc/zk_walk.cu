@@ -292,6 +292,7 @@ __global__ void __launch_bounds__(32 * WARPS_W1) k_walk_tables(const WalkArgs a)
  * single load. */
 __global__ void k_walk_groups(const WalkArgs a)
 {
+    extern __shared__ __align__(16) uint32_t tabs[]; /* the group's window tables */
     const ZGeom &g = a.g;
     const WalkScratch &w = a.ws;
     const uint32_t gg = blockIdx.x;
@@ -300,13 +301,17 @@ __global__ void k_walk_groups(const WalkArgs a)
     const uint32_t nwin = w.win_base[s + 1] - w.win_base[s];
     const uint32_t w0 = (gg - w.grp_base[s]) * WALK_G;
     const uint32_t w1 = min(w0 + WALK_G, nwin);
+    /* one coalesced copy, so that the walks' dependent steps read shared memory */
+    const uint32_t *gt = w.wtab + (uint64_t)(w.win_base[s] + w0) * a.M;
+    for (uint32_t i = threadIdx.x; i < (w1 - w0) * a.M; i += blockDim.x) tabs[i] = __ldg(gt + i);
+    __syncthreads();
     for (uint32_t e = threadIdx.x; e < a.M; e += blockDim.x) {
         uint32_t x = e;
         uint64_t c = 0;
         uint32_t *gw = w.gwin + ((uint64_t)gg * a.M + e) * WALK_G;
-        for (uint32_t k = w0; k < w1; k++) {
-            gw[k - w0] = (uint32_t)c << 12 | x; /* c < 32 windows x 4096 blocks; x < M < 4096 */
-            uint32_t t = __ldg(w.wtab + (uint64_t)(w.win_base[s] + k) * a.M + x);
+        for (uint32_t k = 0; k < w1 - w0; k++) {
+            gw[k] = (uint32_t)c << 12 | x; /* c < 32 windows x 4096 blocks; x < M < 4096 */
+            const uint32_t t = tabs[k * a.M + x];
             c += t & 0xFFFFu;
             x = t >> 16;
         }
@@ -566,7 +571,9 @@ cudaError_t launch_walk(const WalkArgs &a0, cudaStream_t st)
         k_walk_tables<uint32_t><<<grid1, 32 * WARPS_W1, smem1, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const unsigned threads2 = std::min(1024u, (a.M + 31u) / 32u * 32u); /* one thread per entry offset */
-    k_walk_groups<<<a.max_groups, threads2, 0, st>>>(a);
+    const uint32_t smem2a = 4u * WALK_G * a.M;
+    if ((e = set_max_smem((const void *)k_walk_groups, smem2a)) != cudaSuccess) return e;
+    k_walk_groups<<<a.max_groups, threads2, smem2a, st>>>(a);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     a.seg_batch = (160u * 1024u) / (8u * a.M);
     if (a.seg_batch > WALK_G) a.seg_batch = WALK_G;
