@@ -1432,7 +1432,7 @@ int pipe_homadd(DropCtx *c, unsigned char *out, size_t *out_size, const unsigned
         for (int i = 0; i < 3; i++)
             if (int rc = c->lix[l][i].ensure(ixb)) return rc;
         if (int rc = c->lws[l].ensure(wsb)) return rc;
-        if (int rc = c->lws[kLanes + l].ensure(wsb)) return rc;
+        if (int rc = c->lws[kLanes + l].ensure(max_ws_bytes(gr))) return rc; /* second walks: one input's group */
     }
     if (int rc = c->pin.ensure(poff[G])) return rc;
     uint8_t *pin = (uint8_t *)c->pin.p;
