@@ -272,14 +272,51 @@ __global__ void __launch_bounds__(32 * WARPS_W1) k_walk_tables(const WalkArgs a)
             ex[q] = v;
         }
         uint32_t *tab = a.ws.wtab + (uint64_t)wg * M;
-        for (uint32_t e = lane; e < M; e += 32) {
-            uint32_t pos = e, cnt = 0;
+        /* the table: the walks from the M entries leave sub-window 0 at
+         * few distinct places (walks that meet go on together), so only
+         * the walks from those places are followed to the window's end,
+         * one lane each, and every entry adds its first hop; the rows'
+         * space (free after the backward passes) holds the places' flags
+         * and results */
+        auto walk = [&](uint32_t pos, uint32_t cnt) -> uint32_t {
             while (pos < WALK_WW) {
                 const uint32_t j = pos / SUB, r = res[(pos % SUB) * 33 + j];
                 cnt += r & 0xFFu;
                 pos = (j + 1) * SUB + (r >> 8);
             }
-            tab[e] = (pos - WALK_WW) << 16 | cnt;
+            return (pos - WALK_WW) << 16 | cnt;
+        };
+        /* where the walk from entry e leaves sub-window 0 (SUB + offset)
+         * and the blocks it passed there */
+        auto first = [&](uint32_t e, uint32_t &c0) -> uint32_t {
+            if (e >= SUB) {
+                c0 = 0;
+                return e;
+            }
+            const uint32_t r = res[e * 33];
+            c0 = r & 0xFFu;
+            return SUB + (r >> 8);
+        };
+        if (5u * M <= 32u * W1_ROW) {
+            uint8_t *need = rows;                                        /* [M] */
+            uint32_t *fin = reinterpret_cast<uint32_t *>(rows + ((M + 15u) & ~15u)); /* [M] */
+            for (uint32_t x = lane; x < M; x += 32) need[x] = 0;
+            __syncwarp();
+            for (uint32_t e = lane; e < M; e += 32) {
+                uint32_t c0;
+                need[first(e, c0) - SUB] = 1;
+            }
+            __syncwarp();
+            for (uint32_t x = lane; x < M; x += 32)
+                if (need[x]) fin[x] = walk(SUB + x, 0);
+            __syncwarp();
+            for (uint32_t e = lane; e < M; e += 32) {
+                uint32_t c0;
+                const uint32_t f = fin[first(e, c0) - SUB];
+                tab[e] = f + c0; /* the count in the low 16 bits stays below 2^16 */
+            }
+        } else {
+            for (uint32_t e = lane; e < M; e += 32) tab[e] = walk(e, 0);
         }
         __syncwarp(); /* the area is reused for the next window */
     }
