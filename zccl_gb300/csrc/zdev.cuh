@@ -35,6 +35,11 @@ struct ZWidthTable {
     uint32_t thr[33];
 };
 
+/* zg_block_bytes for a full 32-element fastmode1 block of width b <= 32: the
+ * header, four sign bytes and 4 b bytes of magnitudes; a zero-width block is
+ * its header alone. */
+__device__ __forceinline__ uint32_t block32_bytes(uint32_t b) { return b ? 4u * b + 5u : 1u; }
+
 /* (int)log2f((float)m) + 1 for m > 0 and 0 for m == 0, as the reference
  * computes it with the host libm (ZCCL/src/ZCCL_float.c:606). */
 __device__ __forceinline__ uint32_t width_of(uint32_t m, const ZWidthTable &wt)

@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
             }
             if (ok) {
                 b = width_of(mx, a.wt);
-                size = zg_block_bytes_f(g.fmt, b, 32);
+                size = g.fmt == ZG_FASTMODE1 ? block32_bytes(b) : zg_block_bytes_f(g.fmt, b, 32);
                 done = true;
             }
         }

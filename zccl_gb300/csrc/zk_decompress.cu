@@ -93,7 +93,7 @@ __device__ __forceinline__ BlockSlot stage_tile(const DecompressArgs &a, const Z
             bad |= ZERR_CORRUPT;
             sl.b = 0;
         }
-        size = zg_block_bytes_f(a.g.fmt, sl.b, sl.n);
+        size = a.g.fmt == ZG_FASTMODE1 && sl.n == 32 ? block32_bytes(sl.b) : zg_block_bytes_f(a.g.fmt, sl.b, sl.n);
     }
     uint32_t total;
     sl.off = cta_excl_scan(size, wsum, &total);
@@ -215,7 +215,8 @@ __global__ void __launch_bounds__(256, 3) k_decompress(const DecompressArgs a, c
                         bad |= ZERR_CORRUPT;
                         nxt.b = 0;
                     }
-                    sizen = zg_block_bytes_f(g.fmt, nxt.b, nxt.n);
+                    sizen = g.fmt == ZG_FASTMODE1 && nxt.n == 32 ? block32_bytes(nxt.b)
+                                                                  : zg_block_bytes_f(g.fmt, nxt.b, nxt.n);
                 }
             }
             uint32_t totn;

@@ -432,7 +432,7 @@ __global__ void __launch_bounds__(320, 2) k_homadd(const __grid_constant__ HomAd
                 mx = max(mx, acc[j]);
             }
             b = width_of(mx, a.wt);
-            size = zg_block_bytes(b, 32);
+            size = block32_bytes(b);
         } else if (own) {
             uint32_t mx = 0;
             for (uint32_t j = 0; j < n; j++) {
