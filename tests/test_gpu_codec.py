@@ -427,7 +427,8 @@ def test_host_dropins_pipelined_by_chunk_groups(port, torch, T, extra):
     (groups of chunks copied in, coded and copied out on three streams).
     Their streams, floats and sums are the oracle's: remainder segments that
     force the last group to hold several chunks, pageable and pinned
-    buffers, and the sum written over its second input as the ring does."""
+    buffers, and the sum written over its second input as the ring does and
+    into a buffer of its own."""
     n = (1 << 22) + extra
     L = 32
     rng = np.random.default_rng(T + extra)
@@ -457,8 +458,14 @@ def test_host_dropins_pipelined_by_chunk_groups(port, torch, T, extra):
         assert np.array_equal(out.view(np.uint32), dx.view(np.uint32)), (T, extra, pinned)
         acc = host(cap, torch.uint8, pinned)
         acc[: len(sy)] = np.frombuffer(sy, np.uint8)
+        ys = acc.copy() if not pinned else host(cap, torch.uint8, True)
+        ys[: len(sy)] = np.frombuffer(sy, np.uint8)
         total = Z.ZCCL_float_homomophic_add_openmp_threadblock(acc, 0, n, eb, L, hs, acc)
         assert total == len(sxy) and acc[:total].tobytes() == sxy, (T, extra, pinned)
+        # into a separate buffer: the outputs leave group by group while inputs arrive
+        sep = host(cap, torch.uint8, pinned)
+        total = Z.ZCCL_float_homomophic_add_openmp_threadblock(sep, 0, n, eb, L, hs, ys)
+        assert total == len(sxy) and sep[:total].tobytes() == sxy, (T, extra, pinned)
 
 
 def test_host_dropins_pipelined_report_bad_streams(port, torch):
