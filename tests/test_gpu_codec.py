@@ -424,7 +424,8 @@ def test_lookback_wait_gives_up_and_reports_timeout(torch, monkeypatch):
 @pytest.mark.parametrize("T,extra", [(16, 0), (16, 9), (7, 3), (3, 0)])
 def test_host_dropins_pipelined_by_chunk_groups(port, torch, T, extra):
     """Host buffers of 2^22 floats and more go through the pipelined drop-ins
-    (groups of chunks copied in, coded and copied out on three streams).
+    (groups of chunks copied in on one stream, coded and copied out on four
+    more).
     Their streams, floats and sums are the oracle's: remainder segments that
     force the last group to hold several chunks, pageable and pinned
     buffers, and the sum written over its second input as the ring does and
