@@ -887,7 +887,7 @@ struct DropCtx {
     std::mutex mu;
     cudaStream_t st = nullptr;
     cudaStream_t st2 = nullptr; /* a second input's copy, beside the first one's walk */
-    cudaStream_t st_in = nullptr, st_out = nullptr; /* the pipelined drop-ins' copies */
+    cudaStream_t st_in = nullptr; /* the pipelined drop-ins' input copies */
     cudaEvent_t ev = nullptr;
     cudaEvent_t ev_in[kMaxGroups] = {}, ev_k[kMaxGroups] = {}, ev_w[kMaxGroups] = {};
     cudaStream_t lane[kLanes] = {};
@@ -913,8 +913,7 @@ DropCtx *drop_ctx()
          * drop-ins therefore send their outputs out on the lanes that made
          * them (a separate copy stream was seen to wait behind another
          * lane's kernels) and keep to st_in and four lanes. */
-        bool ok = cudaStreamCreateWithFlags(&c->st_in, cudaStreamNonBlocking) == cudaSuccess &&
-                  cudaStreamCreateWithFlags(&c->st_out, cudaStreamNonBlocking) == cudaSuccess;
+        bool ok = cudaStreamCreateWithFlags(&c->st_in, cudaStreamNonBlocking) == cudaSuccess;
         for (uint32_t i = 0; ok && i < kLanes; i++)
             ok = cudaStreamCreateWithFlags(&c->lane[i], cudaStreamNonBlocking) == cudaSuccess;
         ok = ok && cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) == cudaSuccess &&
@@ -1134,8 +1133,7 @@ size_t max_index_bytes(const std::vector<Group> &gr)
  * one wait for all of them. */
 int pipe_finish(DropCtx *c, int rc, uint32_t lanes, bool walk_lanes = false)
 {
-    bool sync_ok = cudaStreamSynchronize(c->st_in) == cudaSuccess &&
-                   cudaStreamSynchronize(c->st_out) == cudaSuccess;
+    bool sync_ok = cudaStreamSynchronize(c->st_in) == cudaSuccess;
     for (uint32_t l = 0; l < lanes; l++) /* after an early stop, work may remain on any lane */
         sync_ok = cudaStreamSynchronize(c->lane[l]) == cudaSuccess && sync_ok;
     if (!sync_ok) return ZCCL_GPU_ECUDA;
