@@ -384,6 +384,7 @@ typedef struct zccl_gpu_batch {
     unsigned tb;      /* blocks per tile */
     unsigned smem[6]; /* shared-memory layout of the launch */
     int qprev_valid;  /* sums: every input carries its tile starting values */
+    size_t rows_off;  /* compress: the jobs' tensor maps inside d_mem, 0 = none */
 } zccl_gpu_batch;
 
 /* Device bytes a batch of these jobs needs (0 if a job is invalid). */

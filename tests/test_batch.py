@@ -33,19 +33,27 @@ def torch():
 
 def buckets(torch, seed=0):
     """Pairs of equal-size buffers of uneven sizes (a few floats to a few
-    hundred thousand), Laplace values, some constant, per-pair eb and T."""
+    hundred thousand), Laplace values, some constant, per-pair eb and T.
+    The last two pairs have T = 1 and several full tiles: one in aligned
+    buffers (its full tiles arrive as TMA boxes through the job's own tensor
+    map), one in buffers that start 4 bytes past an aligned address (no
+    tensor map, every tile copied into padded rows)."""
     rng = np.random.default_rng(seed)
     sizes = [5, 17, 31, 32, 33, 64, 1000, 4097, 8193, 65537] + [int(v) for v in np.exp(rng.uniform(np.log(40), np.log(400000), 20))]
+    sizes += [3 * 8192 + 7, 3 * 8192 + 7]
     pairs = []
     for k, n in enumerate(sizes):
         T = int(rng.choice([1, 1, 3, 4])) if n >= 4 else 1
+        shift = 1 if k == len(sizes) - 1 else 0
+        if k >= len(sizes) - 2:
+            T = 1
         xs = []
         for r in range(2):
-            if k % 9 == 4:
+            if k % 9 == 4 and k < len(sizes) - 2:
                 x = np.full(n, 0.25 * (r + 1), np.float32)
             else:
                 x = rng.laplace(0, 1e-3, n).astype(np.float32)
-            xs.append(torch.from_numpy(x).cuda())
+            xs.append(torch.from_numpy(np.concatenate([np.zeros(shift, np.float32), x])).cuda()[shift:])
         rng_ = max(float(max(x.max() for x in xs) - min(x.min() for x in xs)), 1e-3)
         eb = float(np.float32(float(rng.choice([1e-3, 1e-4, 1e-5])) * rng_))
         pairs.append((n, T, eb, xs))
@@ -69,6 +77,7 @@ def test_batch_matches_single_calls_and_graph_replay(torch):
         outs.append((bo, so))
     bc = Z.Batch(Z.BATCH_COMPRESS, comp_jobs)
     bh = Z.Batch(Z.BATCH_HOMADD, sum_jobs)
+    assert bc.desc.rows_off != 0  # some jobs have tensor maps
 
     def check_all():
         for (a, s), (bo, so) in zip(singles, outs):

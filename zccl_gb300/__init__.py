@@ -80,7 +80,7 @@ class BatchDesc(ctypes.Structure):
                 ("njobs", ctypes.c_size_t), ("ntiles", ctypes.c_size_t), ("d_mem", ctypes.c_void_p),
                 ("clear_bytes", ctypes.c_size_t), ("jobs_off", ctypes.c_size_t),
                 ("map_off", ctypes.c_size_t), ("tile0_off", ctypes.c_size_t), ("tb", ctypes.c_uint),
-                ("smem", ctypes.c_uint * 6), ("qprev_valid", ctypes.c_int)]
+                ("smem", ctypes.c_uint * 6), ("qprev_valid", ctypes.c_int), ("rows_off", ctypes.c_size_t)]
 
 
 _lib = None

@@ -541,9 +541,12 @@ size_t batch_job_size(int kind)
 }
 
 
-/* d_mem: err | walk_err | ticket | pad | status[ntiles] | jobs | tile_job[ntiles] | job_tile0[njobs] */
+/* d_mem: err | walk_err | ticket | pad | status[ntiles] | jobs | tile_job[ntiles] | job_tile0[njobs]
+ * and, for compress batches, room for a 64-byte-aligned CUtensorMap per job
+ * (rows: where that room starts; the maps start at its first 64-byte
+ * boundary in memory). */
 struct BatchLayout {
-    size_t clear, jobs, map, tile0, total;
+    size_t clear, jobs, map, tile0, rows, total;
 };
 
 BatchLayout batch_layout(int kind, size_t njobs, size_t ntiles)
@@ -553,7 +556,8 @@ BatchLayout batch_layout(int kind, size_t njobs, size_t ntiles)
     l.jobs = align16(l.clear);
     l.map = align16(l.jobs + njobs * batch_job_size(kind));
     l.tile0 = align16(l.map + 2 * ntiles);
-    l.total = l.tile0 + 8 * njobs;
+    l.rows = l.tile0 + 8 * njobs;
+    l.total = kind == ZCCL_GPU_BATCH_COMPRESS ? l.rows + 64 + sizeof(CUtensorMap) * njobs : l.rows;
     return l;
 }
 
@@ -611,6 +615,14 @@ extern "C" int zccl_gpu_batch_plan(zccl_gpu_batch *b, int kind, const zccl_gpu_b
     std::vector<uint16_t> map(ntiles);
     std::vector<uint64_t> tile0(njobs);
     std::vector<CompressJob> cj(kind == ZCCL_GPU_BATCH_COMPRESS ? njobs : 0);
+    /* compress: a rows-of-32-floats tensor map per job whose full tiles can
+     * arrive as TMA boxes (L = 32, 256-block tiles, 16-byte-aligned input) */
+    struct alignas(64) RowsMap { CUtensorMap m; };
+    std::vector<RowsMap> rmaps(kind == ZCCL_GPU_BATCH_COMPRESS ? njobs : 0);
+    const size_t rows_off = kind == ZCCL_GPU_BATCH_COMPRESS
+                                ? (size_t)(((uintptr_t)(base + lay.rows) + 63u) & ~(uintptr_t)63u) - (uintptr_t)base
+                                : 0;
+    bool any_boxed = false;
     std::vector<HomAddJob> hj(kind == ZCCL_GPU_BATCH_HOMADD ? njobs : 0);
     std::vector<DecompressJob> dj(kind == ZCCL_GPU_BATCH_DECOMPRESS ? njobs : 0);
     int qv = 1;
@@ -630,6 +642,9 @@ extern "C" int zccl_gpu_batch_plan(zccl_gpu_batch *b, int kind, const zccl_gpu_b
             c.idx = bind_index(J.out->index, g);
             c.status = status + t0;
             c.inv = 1.0f / J.eb; /* float division, as ZCCL/src/ZCCL_float.c:540 */
+            memset(&rmaps[j], 0, sizeof(RowsMap));
+            c.boxed = L == 32 && g.TB == 256 && zk_rows_map(&rmaps[j].m, J.d_in, g.n, 256) ? 1u : 0u;
+            any_boxed |= c.boxed != 0;
         } else if (kind == ZCCL_GPU_BATCH_DECOMPRESS) {
             DecompressJob &d = dj[j];
             memset(&d, 0, sizeof(d));
@@ -673,6 +688,8 @@ extern "C" int zccl_gpu_batch_plan(zccl_gpu_batch *b, int kind, const zccl_gpu_b
         cudaMemcpyAsync(base + lay.jobs, jsrc, jbytes, cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemcpyAsync(base + lay.map, map.data(), 2 * ntiles, cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaMemcpyAsync(base + lay.tile0, tile0.data(), 8 * njobs, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        (any_boxed &&
+         cudaMemcpyAsync(base + rows_off, rmaps.data(), sizeof(RowsMap) * njobs, cudaMemcpyHostToDevice, st) != cudaSuccess) ||
         cudaStreamSynchronize(st) != cudaSuccess)
         return ZCCL_GPU_ECUDA;
     memset(b, 0, sizeof(*b));
@@ -685,6 +702,7 @@ extern "C" int zccl_gpu_batch_plan(zccl_gpu_batch *b, int kind, const zccl_gpu_b
     b->jobs_off = lay.jobs;
     b->map_off = lay.map;
     b->tile0_off = lay.tile0;
+    b->rows_off = any_boxed ? rows_off : 0;
     b->tb = gs[0].TB;
     const ZSmem sm = kind == ZCCL_GPU_BATCH_COMPRESS ? compress_smem(gs[0])
                      : kind == ZCCL_GPU_BATCH_HOMADD ? homadd_smem(gs[0])
@@ -713,6 +731,7 @@ extern "C" int zccl_gpu_batch_run(const zccl_gpu_batch *b, void *cuda_stream)
     bt.job_tile0 = reinterpret_cast<const uint64_t *>(base + b->tile0_off);
     bt.njobs = (uint32_t)b->njobs;
     bt.ntiles = b->ntiles;
+    bt.maps = b->kind == ZCCL_GPU_BATCH_COMPRESS && b->rows_off ? base + b->rows_off : nullptr;
     ZSmem sm;
     memcpy(&sm, b->smem, sizeof(sm));
     if (b->kind == ZCCL_GPU_BATCH_COMPRESS) {

@@ -38,14 +38,16 @@
 namespace {
 
 /* A full tile of L = 32 whose element before it starts a 128-byte row of
- * the single job's input arrives by one TMA tensor load of 256 rows of 32
+ * its job's input (the single job's, or a batch job with a tensor map of
+ * its own) arrives by one TMA tensor load of 256 rows of 32
  * floats (the element before the tile first, 128-byte swizzle: 16-byte
  * chunk k of row r at chunk k ^ (r & 7)) and a 16-byte copy that starts at
  * its last element; every thread then reads its block straight from its
  * row with vector loads that meet no bank conflict. */
-__device__ __forceinline__ bool box_tile(const CompressArgs &a, const ZGeom &g, const ZTile &z)
+__device__ __forceinline__ bool box_tile(const CompressArgs &a, const CompressJob &J, const ZTile &z)
 {
-    return a.rows_map && !a.batch.jobs && g.L == 32 && g.TB == 256 && z.nblk == 256 &&
+    const ZGeom &g = J.g;
+    return a.rows_map && (!a.batch.jobs || J.boxed) && g.L == 32 && g.TB == 256 && z.nblk == 256 &&
            z.e_end - z.e_first == 8192 && ((z.e_first - 1) & 31) == 0;
 }
 
@@ -78,10 +80,11 @@ __device__ __forceinline__ void claim_tile(const CompressArgs &a, uint64_t t, ui
     *s_job = j;
     ZTile zt;
     zg_tile(&slot->g, local, &zt);
-    if (box && box_tile(a, slot->g, zt)) {
+    if (box && box_tile(a, *slot, zt)) {
         fence_proxy_async_smem(); /* earlier generic accesses of the box before the async writes */
         mbar_expect_tx(bar, 32768u + 16u);
-        tma_load_2d(smem_u32(box), xmap, 0, (int32_t)((zt.e_first - 1) >> 5), bar);
+        const CUtensorMap *m = a.batch.jobs ? static_cast<const CUtensorMap *>(a.batch.maps) + j : xmap;
+        tma_load_2d(smem_u32(box), m, 0, (int32_t)((zt.e_first - 1) >> 5), bar);
         bulk_g2s(box + 32768, slot->x + (zt.e_end - 1), 16u, bar); /* 16-byte aligned, like the row */
         return;
     }
@@ -188,7 +191,7 @@ __global__ void __launch_bounds__(288, 3) k_compress(const __grid_constant__ Com
          *    tile's largest magnitude, which decides whether the
          *    one-multiply quantization is exact for the whole tile. */
         mbar_wait(bar_tma, it & 1u, a.w.err);
-        const bool bx = FAST && box && box_tile(a, g, z);
+        const bool bx = FAST && box && box_tile(a, J, z);
         const float *xin =
             reinterpret_cast<const float *>(in + ((uintptr_t)(J.x + (z.e_first - 1)) & 15u));
         /* the head, or the last element of the previous tile */
@@ -422,7 +425,7 @@ cudaError_t launch_compress(const CompressArgs &a, cudaStream_t st)
     CompressArgs b = a;
     alignas(64) CUtensorMap map;
     memset(&map, 0, sizeof map);
-    b.rows_map = fast && !a.batch.jobs && zk_rows_map(&map, a.job.x, a.job.g.n, 256);
+    b.rows_map = fast && (a.batch.jobs ? a.batch.maps != nullptr : zk_rows_map(&map, a.job.x, a.job.g.n, 256));
     if (fast)
         k_compress<true><<<grid, threads, a.sm.total, st>>>(b, map);
     else

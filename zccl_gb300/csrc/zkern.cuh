@@ -48,6 +48,7 @@ struct alignas(16) CompressJob {
     ZIndex idx;
     uint64_t *status; /* this buffer's look-back words, one per tile */
     float inv;        /* 1.0f / eb, computed on the host in float */
+    uint32_t boxed;   /* batch job: batch.maps[job] views x as rows of 32 floats */
 };
 
 struct ZBatch {
@@ -55,7 +56,8 @@ struct ZBatch {
     const uint16_t *tile_job;  /* [ntiles] */
     const uint64_t *job_tile0; /* [njobs] */
     uint32_t njobs;
-    uint64_t ntiles; /* tiles of all jobs */
+    uint64_t ntiles;  /* tiles of all jobs */
+    const void *maps; /* compress: CUtensorMap[njobs] in device memory (used where a job is boxed), or null */
 };
 
 struct CompressArgs {
