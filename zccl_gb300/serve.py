@@ -311,6 +311,8 @@ class Server:
             self._admit()
             if deadline is not None and self.now() > deadline:
                 break
+            if not self.free_slots:
+                continue  # every slot busy: poll the units, so that a freed slot is refilled at once
             if self.inflight or (self.queue and self.queue[0][0] > self.now()):
                 time.sleep(0.00005)
         self.torch.cuda.synchronize()
