@@ -216,3 +216,24 @@ def test_admission_takes_the_oldest_kind_in_fifo_order():
     srv.free_slots, srv.in_use = [0], 95  # the oldest does not fit: nothing is launched
     srv._admit()
     assert len(units) == 3 and [q.rid for q in srv.ready[COMPRESS]] == [5, 6]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("batching", [True, False])
+def test_device_status_of_a_unit_is_raised(torch, batching):
+    """A compression whose input holds a NaN reports ERANGE on the device
+    (no fault); the loop reads the unit's status words when the unit ends
+    and raises, whether the request went out in a compression batch or as
+    a lone call."""
+    import zccl_gb300 as Z
+    from zccl_gb300.serve import COMPRESS, Request, Server
+    n = 20000
+    good = torch.linspace(-1, 1, n, device="cuda")
+    bad = good.clone()
+    bad[1234] = float("nan")
+    srv = Server(1 << 30, slots=2, batching=batching)
+    srv.submit(Request(0.0, 1, COMPRESS, x=good, eb=1e-3, T=1))
+    srv.submit(Request(0.0, 2, COMPRESS, x=bad, eb=1e-3, T=1))
+    with pytest.raises(Z.ZcclError) as e:
+        srv.run()
+    assert e.value.status == -3
